@@ -1,0 +1,323 @@
+"""Benchmark: bootstrap particle filter at scale on one GB300.
+
+Workload: d = 10 linear-Gaussian SSM (F = seeded QR x diag U(0.5, 0.95),
+Q = 0.1 I, H = I, R = 0.5 I), N = 2^20 particles, T = 1000 steps, float32
+states, ESS-triggered systematic resampling at 0.5 N, observations simulated
+from seed 0.  One bench step = one whole filter run (N T particle-steps).
+
+Metric: particle-steps/s (higher is better).
+  value     -- device-resident run replayed from a CUDA graph (inputs already in
+               HBM), timed with CUDA events; L2 flushed (256 MB write) between runs.
+  e2e       -- the public call run_particle_filter_for_marginals with host
+               observations / key, host read-back of log Z, ESS and error word.
+  roofline  -- the dominant kernel (fused propagate + weight, k_lg_step) timed
+               alone with CUDA events over rotating buffers larger than L2;
+               algorithmic bytes per particle = 8 d + 8 (state read + write,
+               ancestor or previous log-weight read, log-weight write).
+  cpu_baseline -- the oracle's C/OpenMP restatement of the same filter on the
+               host cores, on a bounded sample (N = 2^20, a few steps).
+
+--impl reference: times that CPU restatement alone (the reference itself is
+JAX and is not installable here) on the same workload, all host threads.
+Multi-GPU (torchrun): independent replicas, one filter per rank, no
+collective on the data path; value = all ranks' particle-steps / max time.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+D, N_DEFAULT, T_DEFAULT = 10, 1 << 20, 1000
+WORKLOAD = ("bootstrap particle filter, d=10 linear-Gaussian SSM (F seeded QR x diag U(0.5,0.95), Q=0.1I, H=I, "
+            "R=0.5I), N=2^20 particles, T=1000 steps, float32 states, ESS-triggered systematic resampling at 0.5N")
+METRIC = "particle-steps/s"
+
+
+def model_arrays(d=D, seed=0):
+    rng = np.random.default_rng(seed)
+    q, _ = np.linalg.qr(rng.standard_normal((d, d)))
+    F = q @ np.diag(rng.uniform(0.5, 0.95, d))
+    return dict(initial_mean=np.zeros(d), initial_covariance=np.eye(d), transition_matrix=F,
+                transition_covariance=0.1 * np.eye(d), likelihood_matrix=np.eye(d),
+                likelihood_covariance=0.5 * np.eye(d))
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(n, steps, threads=None):
+    """The oracle's C/OpenMP filter on a bounded sample; returns particle-steps/s and thread count."""
+    import oracle
+    from oracle import models
+    oracle.build()
+    if threads:
+        oracle.set_num_threads(threads)
+    a = model_arrays()
+    p = models.lg_params(**a)
+    rng = np.random.default_rng(1)
+    y = rng.standard_normal((steps, D)).astype(np.float32)
+    oracle.lg_run(p, 4096, oracle.PRNGKey(0), y[:2])  # warm the thread pool
+    t0 = time.perf_counter()
+    oracle.lg_run(p, n, oracle.PRNGKey(0), y, ess_threshold=0.5, scheme="systematic")
+    dt = time.perf_counter() - t0
+    return n * steps / dt, oracle.num_threads(), dt
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    steps_per_sample = args.ref_steps
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, cores, dt = cpu_baseline(args.n, steps_per_sample)
+        if i >= args.warmup:
+            vals.append(v)
+    v = statistics.median(vals)
+    line = {"metric": METRIC, "value": v, "unit": "particle-steps/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": args.n * steps_per_sample / v * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "sample": f"N=2^20, {steps_per_sample} filter steps per bench step"},
+            "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+                             "sample": f"N={args.n}, {steps_per_sample} steps of the same filter (oracle C/OpenMP "
+                                       "restatement; the reference is JAX, not installable here)"},
+            "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--T", type=int, default=T_DEFAULT)
+    ap.add_argument("--ref-steps", type=int, default=20)
+    ap.add_argument("--cpu-steps", type=int, default=10)
+    ap.add_argument("--kernel-iters", type=int, default=50)
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+
+    import torch
+    import torch.distributed as dist
+    import mocat_gb300 as mg
+    from mocat_gb300 import _dev, _lib
+    from mocat_gb300.ssm import _step
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dev = torch.device("cuda", local)
+    n, T = args.n, args.T
+    ssm = mg.ssm.TimeHomogenousLinearGaussian(**model_arrays())
+    sim = ssm.simulate(np.arange(T), mg.random.PRNGKey(0))
+    y_dev = sim.y.contiguous()
+    y_host = y_dev.cpu().pin_memory()
+    _, s = ssm.derived()
+    sc = 0
+    ws = _dev.workspace(_lib.lib().mgb_pf_lg_workspace(n, T, D, sc), dev)
+    key = mg.random.PRNGKey(1 + rank)
+    logz = torch.empty(1, dtype=torch.float64, device=dev)
+    ess = torch.empty(T, dtype=torch.float32, device=dev)
+    res = torch.empty(T, dtype=torch.int32, device=dev)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    xf = torch.empty((D, n), dtype=torch.float32, device=dev)
+    lf = torch.empty(n, dtype=torch.float32, device=dev)
+    out = _lib.PFOutputs(logz.data_ptr(), ess.data_ptr(), res.data_ptr(), None, None, xf.data_ptr(), lf.data_ptr(),
+                         err.data_ptr())
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def enqueue():
+        _lib.call("mgb_pf_lg_run", ctypes.byref(s), n, T, _dev.ptr(key), _dev.ptr(y_dev), 0.5, sc, _dev.ptr(ws),
+                  ws.numel(), ctypes.byref(out), _dev.stream_ptr())
+
+    # ---- device-resident: CUDA graph of one whole run
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        enqueue()
+    torch.cuda.current_stream().wait_stream(side)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        enqueue()
+    for _ in range(args.warmup):
+        flush.zero_()
+        g.replay()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    times = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            g.replay()
+            e1.record()
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+    if int(err.item()) != 0:
+        raise RuntimeError(f"device error word {int(err.item())}")
+    t_dev = sum(times)
+    tmax = torch.tensor([t_dev], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+    value = world * n * T * args.steps / float(tmax)
+    ms_per_step = float(tmax) / args.steps * 1e3
+    log_z = float(logz.item())
+
+    # ---- end to end through the public API (host observations and key, host read-back)
+    key_host = np.array([0, 1 + rank], dtype=np.uint32)
+    for _ in range(1):
+        o = mg.ssm.run_particle_filter_for_marginals(ssm, mg.ssm.BootstrapFilter(), y_host, np.arange(T), key_host,
+                                                     n=n, history=False)
+        float(o.log_z)
+    torch.cuda.synchronize()
+    e2e_t = []
+    for _ in range(max(2, args.steps // 2)):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        o = mg.ssm.run_particle_filter_for_marginals(ssm, mg.ssm.BootstrapFilter(), y_host, np.arange(T), key_host,
+                                                     n=n, history=False)
+        lz_h = float(o.log_z)
+        ess_h = o.ess.cpu()
+        e1.record()
+        torch.cuda.synchronize()
+        e2e_t.append(e0.elapsed_time(e1) / 1e3)
+    _ = (lz_h, ess_h)
+    e2e_val = world * n * T / statistics.median(e2e_t)
+    h2d = T * D * 4 + 8
+    d2h = 8 + T * 4 + 4
+
+    # ---- dominant kernel alone: fused propagate + weight with a resampled (gathering) step
+    nbuf = 4
+    xs = [torch.randn((D, n), device=dev) for _ in range(nbuf)]
+    xo = [torch.empty((D, n), device=dev) for _ in range(nbuf)]
+    lo = [torch.empty(n, device=dev) for _ in range(nbuf)]
+    lws = torch.randn(n, device=dev)
+    anc = mg.resample(lws, mg.random.PRNGKey(7), "systematic")
+    kt = mg.random.split(mg.random.PRNGKey(9), 1)[0].contiguous()
+    y0 = y_dev[1].contiguous()
+    for i in range(3):
+        _step(s, n, kt, y0, xs[i % nbuf], anc, None)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for i in range(args.kernel_iters):
+        _lib.call("mgb_pf_lg_propagate", ctypes.byref(s), n, _dev.ptr(kt), _dev.ptr(y0), _dev.ptr(xs[i % nbuf]),
+                  _dev.ptr(anc), None, _dev.ptr(xo[i % nbuf]), _dev.ptr(lo[i % nbuf]), _dev.stream_ptr())
+    e1.record()
+    torch.cuda.synchronize()
+    k_t = e0.elapsed_time(e1) / 1e3 / args.kernel_iters
+    alg_bytes = n * (8 * D + 8)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = alg_bytes / k_t / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "k_lg_step_d10_n1M.txt")
+    if os.path.exists(prof):
+        for ln in open(prof):
+            if ln.startswith("dram_bytes_per_launch:"):
+                traffic = float(ln.split(":")[1])
+
+    line = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (observations simulated on the GPU from seed 0)",
+            "config": {"workload": WORKLOAD, "n_particles": n, "T": T, "d": D, "resampling": "systematic, ESS<0.5N",
+                       "parallelism": f"replicas x{world}", "l2": "flushed between runs (256 MB write)",
+                       "log_z": log_z},
+            "e2e": {"value": e2e_val, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "roofline": {"bound": "hbm", "kernel": "k_lg_step<10,10> (fused propagate+weight+gather)",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": traffic, "alg_bytes_per_launch": alg_bytes, "launch_us": k_t * 1e6,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback"},
+            "gpu_launches": args.steps * (3 + 3 * (T - 1)),
+            "clocks": clk.summary()}
+    if rank == 0:
+        v_cpu, cores, dt = cpu_baseline(n, args.cpu_steps)
+        line["cpu_baseline"] = {"value": v_cpu, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+                                "sample": f"N={n}, {args.cpu_steps} filter steps ({dt:.1f} s), oracle C/OpenMP"}
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

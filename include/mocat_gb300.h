@@ -1,0 +1,154 @@
+/*
+ * mocat_gb300 C ABI (libmocatgb.so) -- the drop-in boundary of the
+ * particle-system step of mocat (propagate -> weight -> logsumexp/ESS ->
+ * resample -> gather) on GB300 (sm_103a).
+ *
+ * Conventions
+ *   - Every entry point returns an int status (MGB_OK = 0); nothing throws.
+ *   - Pointers suffixed _dev are caller-owned device memory; _host are host
+ *     memory read during the call only.  No entry point allocates: the
+ *     caller queries *_workspace() and passes a device workspace of at least
+ *     that many bytes (256-byte aligned).
+ *   - `stream` is a cudaStream_t (NULL = legacy default stream); all work is
+ *     enqueued on it and the call returns without synchronising.
+ *   - Keys are jax.random PRNG keys: two uint32 words (PRNGKey(seed) =
+ *     {0, seed}).  Draws reproduce jax.random's threefry2x32 counter layout.
+ *   - Particle states are float32, dimension-major ("SoA"): x[j * n + i] is
+ *     component j of particle i.  The reference's arrays are particle-major
+ *     (n, d); the Python layer transposes once at entry and exit.
+ *   - Device-side failures that cannot be returned synchronously (a spin
+ *     wait that ran out, degenerate weights) are OR-ed into an int32 error
+ *     word the caller passes (err_dev, may be NULL): bit 1 = a bounded wait
+ *     ran out, bit 2 = every weight was zero / non-finite.
+ * Thread-safety: calls on different streams with different workspaces are
+ * independent; the library has no global mutable state.
+ */
+#ifndef MOCAT_GB300_H
+#define MOCAT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  MGB_OK = 0,
+  MGB_ERR_BAD_ARG = 1,
+  MGB_ERR_UNSUPPORTED = 2,
+  MGB_ERR_LAUNCH = 3,
+  MGB_ERR_WORKSPACE = 4,
+  MGB_ERR_DEVICE_TIMEOUT = 5,
+  MGB_ERR_NONFINITE_WEIGHTS = 6,
+  MGB_ERR_CUDA = 7
+};
+
+/* resampling schemes */
+enum {
+  MGB_RESAMPLE_SYSTEMATIC = 0,  /* new: u = uniform(key), thresholds (k + u)/n      */
+  MGB_RESAMPLE_MULTINOMIAL = 1, /* new: inverse CDF at sorted uniforms from n+1 exponentials(key) */
+  MGB_RESAMPLE_CATEGORICAL = 2  /* mocat's random.categorical(key, lw, (n,)) Gumbel-max, O(n^2) */
+};
+
+const char *mgb_status_string(int status);
+int mgb_version(void);
+
+/* ------------------------------------------------------------ jax.random
+ * Replace the jax.random calls of the reference's hot path:
+ *   random.split          mocat/src/ssm/filtering.py:181, 267, 278, 294; mocat/src/transport/smc.py:82
+ *   random bits/uniform   (categorical's Gumbel draw) mocat/src/ssm/filtering.py:199
+ *   random.normal         mocat/src/ssm/linear_gaussian/linear_gaussian.py:51, 94
+ */
+int mgb_random_bits(const uint32_t *key_dev, int64_t n, uint32_t *out_dev, void *stream);
+int mgb_split(const uint32_t *key_dev, int64_t num, uint32_t *out_dev /* (num, 2) */, void *stream);
+int mgb_uniform(const uint32_t *key_dev, int64_t n, float *out_dev, void *stream);
+int mgb_normal(const uint32_t *key_dev, int64_t n, float *out_dev, void *stream);
+int mgb_exponential(const uint32_t *key_dev, int64_t n, float *out_dev, void *stream);
+int mgb_gumbel(const uint32_t *key_dev, int64_t n, float *out_dev, void *stream);
+/* vmap(lambda k: random.normal(k, (d,)))(keys): out (nkeys, d) particle-major */
+int mgb_normal_keys(const uint32_t *keys_dev, int64_t nkeys, int64_t d, float *out_dev, void *stream);
+/* the library's own float maths on device (op 0 = log, 1 = exp, 2 = erfinv) */
+int mgb_math_eval(int op, const float *x_dev, int64_t n, float *out_dev, void *stream);
+
+/* --------------------------------------------------- logsumexp and ESS
+ * Replaces log_ess_log_weight / ess_log_weight (mocat/src/metrics.py:69-78) and
+ * jax.scipy.special.logsumexp as used at mocat/src/transport/smc.py:160, 214-215.
+ * out4_dev = {max, logsumexp(lw), logsumexp(2 lw), ess} in float64.
+ */
+size_t mgb_lse_ess_workspace(int64_t n);
+int mgb_lse_ess(const float *lw_dev, int64_t n, double *out4_dev, void *ws_dev, size_t ws_bytes, void *stream);
+
+/* --------------------------------------------------------- resampling
+ * Replaces _resample / resample_particles (mocat/src/ssm/filtering.py:196-217)
+ * and SMCSampler.resample's index draw (mocat/src/transport/smc.py:61-67).
+ * Ancestors are int32 in [0, n).  Weights are quantised to 62-bit fixed
+ * point, so systematic / multinomial ancestors are independent of summation
+ * order.  key_dev is the step key (mocat's int_rand_key).
+ */
+size_t mgb_resample_workspace(int64_t n, int scheme);
+int mgb_resample(const float *lw_dev, int64_t n, int scheme, const uint32_t *key_dev, int32_t *ancestors_dev,
+                 void *ws_dev, size_t ws_bytes, int32_t *err_dev, void *stream);
+/* systematic with the uniform fed in as its 23-bit mantissa: u = m23 * 2^-23 */
+int mgb_resample_systematic_u(const float *lw_dev, int64_t n, uint32_t m23, int32_t *ancestors_dev, void *ws_dev,
+                              size_t ws_bytes, int32_t *err_dev, void *stream);
+
+/* ---------------------------------------------------------------- gather
+ * Replaces the fancy-index gathers x[..., idx, :] (mocat/src/ssm/filtering.py:199)
+ * and cdict.__getitem__ (mocat/src/core.py:46-56): out[k, :] = x[anc[k], :]
+ * for a particle-major (n_in, width) float32 array (any width; vectorised
+ * when rows are 16-byte aligned).
+ */
+int mgb_gather_rows(const float *x_dev, int64_t width, const int32_t *ancestors_dev, int64_t n_out, float *out_dev,
+                    void *stream);
+
+/* --------------------------------------- particle filter, linear Gaussian
+ * TimeHomogenousLinearGaussian (mocat/src/ssm/linear_gaussian/linear_gaussian.py:142-261)
+ * with BootstrapFilter (mocat/src/ssm/filtering.py:142-170):
+ *   x_t = F x_{t-1} + Lq eps,  eps = normal(split(k_t, n)[i], (d,))
+ *   potential(x, y) = 0.5 |(y - H x) @ P|^2 + c
+ * Model matrices are host pointers, row-major float32:
+ *   F, Lq, C0: d x d (transition_matrix, transition_covariance_sqrt,
+ *   initial_covariance_sqrt); H: dy x d (likelihood_matrix); P: dy x dy
+ *   (likelihood_precision_sqrt); m0: d; c = (dy log 2 pi - log det_prec) / 2.
+ * Supported (d, dy): d in {1,2,3,4,5,6,8,10,12,16}, dy in {1, d}.
+ */
+typedef struct {
+  int32_t d, dy;
+  const float *F, *Lq, *H, *P, *C0, *m0;
+  float c;
+} mgb_lg_model;
+
+/* initiate_particles (mocat/src/ssm/filtering.py:173-193): x (d, n), lw (n) */
+int mgb_pf_lg_init(const mgb_lg_model *model_host, int64_t n, const uint32_t *key_dev, const float *y0_dev,
+                   float *x_dev, float *lw_dev, void *stream);
+/* one propagate_and_intermediate_weight step (mocat/src/ssm/filtering.py:294-303):
+ * x_new[:, i] = F x_prev[:, anc[i]] + Lq eps_i, lw_new = lw_prev - potential.
+ * ancestors_dev == NULL means no resampling (identity); lw_prev_dev == NULL means 0. */
+int mgb_pf_lg_propagate(const mgb_lg_model *model_host, int64_t n, const uint32_t *key_t_dev, const float *y_t_dev,
+                        const float *x_prev_dev, const int32_t *ancestors_dev, const float *lw_prev_dev,
+                        float *x_new_dev, float *lw_new_dev, void *stream);
+
+/* outputs of a whole-filter run (device pointers, each may be NULL) */
+typedef struct {
+  double *log_z;      /* scalar: log-marginal-likelihood estimate from the log-weights */
+  float *ess;         /* (T,) ESS after each step (filtering.py:310) */
+  int32_t *resampled; /* (T,) 1 if step t began with a resample */
+  float *x_hist;      /* (T, d, n) particle history, dimension-major per step */
+  float *lw_hist;     /* (T, n) log-weight history */
+  float *x_final;     /* (d, n) final particles */
+  float *lw_final;    /* (n,) final log-weights */
+  int32_t *err;       /* device error word */
+} mgb_pf_outputs;
+
+/* run_particle_filter_for_marginals (mocat/src/ssm/filtering.py:255-324) with
+ * ESS-triggered resampling (resample at t when ess_{t-1} < ess_threshold * n). */
+size_t mgb_pf_lg_workspace(int64_t n, int64_t T, int32_t d, int scheme);
+int mgb_pf_lg_run(const mgb_lg_model *model_host, int64_t n, int64_t T, const uint32_t *key_dev, const float *y_dev,
+                  float ess_threshold, int scheme, void *ws_dev, size_t ws_bytes, const mgb_pf_outputs *out,
+                  void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

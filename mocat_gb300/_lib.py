@@ -1,0 +1,98 @@
+"""ctypes binding of the C ABI declared in include/mocat_gb300.h.
+
+The library is loaded from the package's own build folder; there is no CPU
+fallback: if it is missing, every entry point raises.
+"""
+import ctypes
+import os
+import re
+
+from .build import LIB
+
+_lib = None
+
+
+class MGBError(RuntimeError):
+    def __init__(self, status, where=""):
+        self.status = status
+        super().__init__(f"mocat_gb300: {where} failed with status {status} ({status_string(status)})")
+
+
+class LGModel(ctypes.Structure):
+    _fields_ = [("d", ctypes.c_int32), ("dy", ctypes.c_int32),
+                ("F", ctypes.c_void_p), ("Lq", ctypes.c_void_p), ("H", ctypes.c_void_p), ("P", ctypes.c_void_p),
+                ("C0", ctypes.c_void_p), ("m0", ctypes.c_void_p), ("c", ctypes.c_float)]
+
+
+class PFOutputs(ctypes.Structure):
+    _fields_ = [("log_z", ctypes.c_void_p), ("ess", ctypes.c_void_p), ("resampled", ctypes.c_void_p),
+                ("x_hist", ctypes.c_void_p), ("lw_hist", ctypes.c_void_p), ("x_final", ctypes.c_void_p),
+                ("lw_final", ctypes.c_void_p), ("err", ctypes.c_void_p)]
+
+
+_P = ctypes.c_void_p
+_I64 = ctypes.c_int64
+_I32 = ctypes.c_int
+_F = ctypes.c_float
+_SZ = ctypes.c_size_t
+
+_SIGNATURES = {
+    "mgb_status_string": ([_I32], ctypes.c_char_p),
+    "mgb_version": ([], _I32),
+    "mgb_random_bits": ([_P, _I64, _P, _P], _I32),
+    "mgb_split": ([_P, _I64, _P, _P], _I32),
+    "mgb_uniform": ([_P, _I64, _P, _P], _I32),
+    "mgb_normal": ([_P, _I64, _P, _P], _I32),
+    "mgb_exponential": ([_P, _I64, _P, _P], _I32),
+    "mgb_gumbel": ([_P, _I64, _P, _P], _I32),
+    "mgb_normal_keys": ([_P, _I64, _I64, _P, _P], _I32),
+    "mgb_math_eval": ([_I32, _P, _I64, _P, _P], _I32),
+    "mgb_lse_ess_workspace": ([_I64], _SZ),
+    "mgb_lse_ess": ([_P, _I64, _P, _P, _SZ, _P], _I32),
+    "mgb_resample_workspace": ([_I64, _I32], _SZ),
+    "mgb_resample": ([_P, _I64, _I32, _P, _P, _P, _SZ, _P, _P], _I32),
+    "mgb_resample_systematic_u": ([_P, _I64, ctypes.c_uint32, _P, _P, _SZ, _P, _P], _I32),
+    "mgb_gather_rows": ([_P, _I64, _P, _I64, _P, _P], _I32),
+    "mgb_pf_lg_init": ([ctypes.POINTER(LGModel), _I64, _P, _P, _P, _P, _P], _I32),
+    "mgb_pf_lg_propagate": ([ctypes.POINTER(LGModel), _I64, _P, _P, _P, _P, _P, _P, _P, _P], _I32),
+    "mgb_pf_lg_workspace": ([_I64, _I64, ctypes.c_int32, _I32], _SZ),
+    "mgb_pf_lg_run": ([ctypes.POINTER(LGModel), _I64, _I64, _P, _P, _F, _I32, _P, _SZ, ctypes.POINTER(PFOutputs), _P],
+                      _I32),
+}
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            raise MGBError(-1, f"loading {LIB} (not built; run __graft_entry__.build())")
+        L = ctypes.CDLL(LIB)
+        for name, (args, res) in _SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = L
+    return _lib
+
+
+def status_string(status):
+    try:
+        return lib().mgb_status_string(int(status)).decode()
+    except MGBError:
+        return "library not loaded"
+
+
+def call(name, *args):
+    st = getattr(lib(), name)(*args)
+    if st != 0:
+        raise MGBError(st, name)
+    return st
+
+
+def header_symbols(header=None):
+    """Names of the functions declared in include/mocat_gb300.h."""
+    header = header or os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
+                                    "mocat_gb300.h")
+    text = open(header).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(mgb_[a-z0-9_]+)\s*\(", text)))

@@ -1,0 +1,252 @@
+// Device building blocks shared by every kernel of libmocatgb:
+//   * jax.random restatement on the GPU: threefry2x32-20 (Random123, Salmon et
+//     al. SC'11) with jax's non-partitionable counter layout for split /
+//     random_bits / uniform / normal / exponential / gumbel
+//     (call sites in the reference: mocat/src/ssm/filtering.py:181,199,294;
+//     mocat/src/ssm/linear_gaussian/linear_gaussian.py:51,94;
+//     mocat/src/transport/smc.py:65,82);
+//   * float maths written from textbook methods with explicit IEEE-rounded
+//     intrinsics, so every value is reproducible on any IEEE host:
+//       logf   -- reduction to [sqrt(1/2), sqrt(2)) + 2 atanh(s) series;
+//       expf   -- Cody-Waite reduction by ln 2 + degree-7 Taylor polynomial;
+//       erfinv -- M. Giles, "Approximating the erfinv function" (2011),
+//                 single-precision branch;
+//   * block reductions and status codes.
+// Functions marked __host__ __device__ also run in the host-side driver.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#define MGB_HD __host__ __device__ __forceinline__
+
+namespace mgb {
+
+// ------------------------------------------------------------------ status
+enum Status : int {
+  OK = 0,
+  ERR_BAD_ARG = 1,
+  ERR_UNSUPPORTED = 2,
+  ERR_LAUNCH = 3,
+  ERR_WORKSPACE = 4,
+  ERR_DEVICE_TIMEOUT = 5,
+  ERR_NONFINITE_WEIGHTS = 6,
+  ERR_CUDA = 7,
+};
+// bits of the device-side error word
+enum ErrBits : int { EB_TIMEOUT = 1, EB_DEGENERATE = 2 };
+
+// ------------------------------------------------------------ threefry2x32
+MGB_HD uint32_t rotl32(uint32_t v, int r) { return (v << r) | (v >> (32 - r)); }
+
+MGB_HD void threefry2x32(uint32_t k0, uint32_t k1, uint32_t c0, uint32_t c1, uint32_t &r0, uint32_t &r1) {
+  const uint32_t k2 = k0 ^ k1 ^ 0x1BD11BDAu;
+  uint32_t x0 = c0 + k0, x1 = c1 + k1;
+#define MGB_TF_ROUND(R) { x0 += x1; x1 = rotl32(x1, R); x1 ^= x0; }
+#define MGB_TF_G0 MGB_TF_ROUND(13) MGB_TF_ROUND(15) MGB_TF_ROUND(26) MGB_TF_ROUND(6)
+#define MGB_TF_G1 MGB_TF_ROUND(17) MGB_TF_ROUND(29) MGB_TF_ROUND(16) MGB_TF_ROUND(24)
+  MGB_TF_G0 x0 += k1; x1 += k2 + 1u;
+  MGB_TF_G1 x0 += k2; x1 += k0 + 2u;
+  MGB_TF_G0 x0 += k0; x1 += k1 + 3u;
+  MGB_TF_G1 x0 += k1; x1 += k2 + 4u;
+  MGB_TF_G0 x0 += k2; x1 += k0 + 5u;
+#undef MGB_TF_G1
+#undef MGB_TF_G0
+#undef MGB_TF_ROUND
+  r0 = x0;
+  r1 = x1;
+}
+
+// element p of threefry_2x32(key, iota(n)) (count padded to even length with a
+// zero; outputs concatenated [first halves, second halves] and trimmed)
+MGB_HD uint32_t bits_at(uint32_t k0, uint32_t k1, uint64_t n, uint64_t p) {
+  const uint64_t h = (n + 1) >> 1;
+  uint32_t r0, r1;
+  if (p < h) {
+    const uint64_t c1 = p + h;
+    threefry2x32(k0, k1, (uint32_t)p, c1 < n ? (uint32_t)c1 : 0u, r0, r1);
+    return r0;
+  }
+  threefry2x32(k0, k1, (uint32_t)(p - h), (uint32_t)p, r0, r1);
+  return r1;
+}
+
+// split(key, num)[i]
+MGB_HD void split_at(uint32_t k0, uint32_t k1, uint64_t num, uint64_t i, uint32_t &o0, uint32_t &o1) {
+  o0 = bits_at(k0, k1, 2 * num, 2 * i);
+  o1 = bits_at(k0, k1, 2 * num, 2 * i + 1);
+}
+
+// random_bits(key, (D,)) for a compile-time D: ceil(D/2) cipher calls
+template <int D>
+__device__ __forceinline__ void bits_vec(uint32_t k0, uint32_t k1, uint32_t (&b)[D]) {
+  constexpr int H = (D + 1) / 2;
+#pragma unroll
+  for (int j = 0; j < H; ++j) {
+    uint32_t r0, r1;
+    threefry2x32(k0, k1, (uint32_t)j, (j + H < D) ? (uint32_t)(j + H) : 0u, r0, r1);
+    b[j] = r0;
+    if (j + H < D) b[j + H] = r1;
+  }
+}
+
+// ------------------------------------------------------------- float maths
+__device__ __forceinline__ float asf(uint32_t u) { return __uint_as_float(u); }
+__device__ __forceinline__ uint32_t asu(float f) { return __float_as_uint(f); }
+
+// natural log of a positive normal float
+__device__ __forceinline__ float logf_(float x) {
+  uint32_t ix = asu(x);
+  int e = (int)((ix >> 23) & 0xffu) - 127;
+  uint32_t mb = (ix & 0x007fffffu) | 0x3f800000u;
+  if (mb > 0x3fb504f3u) { mb -= 0x00800000u; e += 1; }
+  const float m = asf(mb);
+  const float s = __fdiv_rn(__fsub_rn(m, 1.0f), __fadd_rn(m, 1.0f));
+  const float z = __fmul_rn(s, s);
+  float p = __fmaf_rn(z, 0x1.745d18p-3f, 0x1.c71c72p-3f);
+  p = __fmaf_rn(z, p, 0x1.24924ap-2f);
+  p = __fmaf_rn(z, p, 0x1.99999ap-2f);
+  p = __fmaf_rn(z, p, 0x1.555556p-1f);
+  p = __fmaf_rn(z, p, 2.0f);
+  const float lm = __fmul_rn(s, p);
+  const float ef = (float)e;
+  return __fmaf_rn(ef, 0x1.63p-1f, __fmaf_rn(ef, -0x1.bd0106p-13f, lm));
+}
+
+// exp: 0 below -104, +inf above 88.5, NaN passes through
+__device__ __forceinline__ float expf_(float x) {
+  if (x != x) return x;
+  if (x < -104.0f) return 0.0f;
+  if (x > 88.5f) return __int_as_float(0x7f800000);
+  const float kf = rintf(__fmul_rn(x, 0x1.715476p+0f));
+  float r = __fmaf_rn(-kf, 0x1.63p-1f, x);
+  r = __fmaf_rn(-kf, -0x1.bd0106p-13f, r);
+  float p = __fmaf_rn(r, 0x1.a01a02p-13f, 0x1.6c16c2p-10f);
+  p = __fmaf_rn(r, p, 0x1.111112p-7f);
+  p = __fmaf_rn(r, p, 0x1.555556p-5f);
+  p = __fmaf_rn(r, p, 0x1.555556p-3f);
+  p = __fmaf_rn(r, p, 0.5f);
+  p = __fmaf_rn(r, p, 1.0f);
+  p = __fmaf_rn(r, p, 1.0f);
+  const int k = (int)kf;
+  if (k < -126) return __fmul_rn(__fmul_rn(p, asf((uint32_t)(k + 64 + 127) << 23)), 0x1p-64f);
+  if (k > 127) return __fmul_rn(__fmul_rn(p, 2.0f), asf((uint32_t)(k - 1 + 127) << 23));
+  return __fmul_rn(p, asf((uint32_t)(k + 127) << 23));
+}
+
+// Giles (2011) erfinv, single precision
+__device__ __forceinline__ float erfinv_(float x) {
+  float w = -logf_(__fmaf_rn(-x, x, 1.0f));
+  float p;
+  if (w < 5.0f) {
+    w = __fsub_rn(w, 2.5f);
+    p = 2.81022636e-08f;
+    p = __fmaf_rn(p, w, 3.43273939e-07f);
+    p = __fmaf_rn(p, w, -3.5233877e-06f);
+    p = __fmaf_rn(p, w, -4.39150654e-06f);
+    p = __fmaf_rn(p, w, 0.00021858087f);
+    p = __fmaf_rn(p, w, -0.00125372503f);
+    p = __fmaf_rn(p, w, -0.00417768164f);
+    p = __fmaf_rn(p, w, 0.246640727f);
+    p = __fmaf_rn(p, w, 1.50140941f);
+  } else {
+    w = __fsub_rn(__fsqrt_rn(w), 3.0f);
+    p = -0.000200214257f;
+    p = __fmaf_rn(p, w, 0.000100950558f);
+    p = __fmaf_rn(p, w, 0.00134934322f);
+    p = __fmaf_rn(p, w, -0.00367342844f);
+    p = __fmaf_rn(p, w, 0.00573950773f);
+    p = __fmaf_rn(p, w, -0.0076224613f);
+    p = __fmaf_rn(p, w, 0.00943887047f);
+    p = __fmaf_rn(p, w, 1.00167406f);
+    p = __fmaf_rn(p, w, 2.83297682f);
+  }
+  return __fmul_rn(p, x);
+}
+
+__device__ __forceinline__ float bits_to_unit(uint32_t b) { return __fsub_rn(asf((b >> 9) | 0x3f800000u), 1.0f); }
+
+// jax.random.normal from raw bits: u = max(lo, 2 f + lo), sqrt(2) erfinv(u)
+__device__ __forceinline__ float bits_to_normal(uint32_t b) {
+  const float lo = -0x1.fffffep-1f;
+  const float u = fmaxf(__fadd_rn(__fmul_rn(bits_to_unit(b), 2.0f), lo), lo);
+  return __fmul_rn(0x1.6a09e6p+0f, erfinv_(u));
+}
+
+// jax.random.exponential: -log1p(-u) = -log(1 - u), 1 - u exact
+__device__ __forceinline__ float bits_to_exponential(uint32_t b) { return -logf_(__fsub_rn(1.0f, bits_to_unit(b))); }
+
+// jax.random.gumbel with minval = tiny
+__device__ __forceinline__ float bits_to_gumbel(uint32_t b) {
+  const float tiny = 0x1p-126f;
+  const float u = fmaxf(__fadd_rn(bits_to_unit(b), tiny), tiny);
+  return -logf_(-logf_(u));
+}
+
+// ---------------------------------------------------------- fixed point
+MGB_HD int ceil_log2_u64(uint64_t n) {
+  int b = 0;
+  while (b < 63 && ((uint64_t)1 << b) < n) ++b;
+  return b;
+}
+// weights exp(lw - max) in [0, 1] are quantised with 2^weight_shift(n): total < 2^62
+MGB_HD int weight_shift(int64_t n) { return 61 - ceil_log2_u64((uint64_t)n); }
+// exponential spacings (< 16) quantised with 2^exp_shift(n) over n + 1 draws: total < 2^60
+MGB_HD int exp_shift(int64_t n) { return 56 - ceil_log2_u64((uint64_t)n + 1); }
+
+__device__ __forceinline__ uint64_t quantise_weight(float lw, float M, float scale) {
+  return __float2ull_rz(__fmul_rn(expf_(__fsub_rn(lw, M)), scale));
+}
+
+// 128-bit product comparison a*b <= c*d (all < 2^64)
+__device__ __forceinline__ bool mul_le(uint64_t a, uint64_t b, uint64_t c, uint64_t d) {
+  const uint64_t h1 = __umul64hi(a, b), l1 = a * b;
+  const uint64_t h2 = __umul64hi(c, d), l2 = c * d;
+  return h1 < h2 || (h1 == h2 && l1 <= l2);
+}
+
+// ---------------------------------------------------------- reductions
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+template <class T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ int warp_or(int v) { return __any_sync(0xffffffffu, v); }
+
+// block-wide max of one value per thread (all threads get the result)
+template <int TPB>
+__device__ __forceinline__ float block_max(float v, float *sm /* >= TPB/32 */) {
+  v = warp_max(v);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) sm[w] = v;
+  __syncthreads();
+  float r = sm[0];
+#pragma unroll
+  for (int i = 1; i < TPB / 32; ++i) r = fmaxf(r, sm[i]);
+  __syncthreads();
+  return r;
+}
+template <int TPB, class T>
+__device__ __forceinline__ T block_sum(T v, T *sm /* >= TPB/32 */) {
+  v = warp_sum(v);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) sm[w] = v;
+  __syncthreads();
+  T r = sm[0];
+#pragma unroll
+  for (int i = 1; i < TPB / 32; ++i) r += sm[i];
+  __syncthreads();
+  return r;
+}
+
+// record an error bit in a device-side error word (never traps)
+__device__ __forceinline__ void raise_err(int *err, int bit) {
+  if (err) atomicOr(err, bit);
+}
+
+}  // namespace mgb

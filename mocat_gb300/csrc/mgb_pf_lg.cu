@@ -1,0 +1,423 @@
+// Bootstrap particle filter for the time-homogeneous linear-Gaussian SSM:
+// fused propagate + weight (+ ancestor gather + online logsumexp / ESS)
+// kernels and the whole-filter driver.
+//
+// Reference path: run_particle_filter_for_marginals
+// (mocat/src/ssm/filtering.py:255-324) with BootstrapFilter (:142-170) on
+// TimeHomogenousLinearGaussian (mocat/src/ssm/linear_gaussian/linear_gaussian.py:
+// initial_sample :46-51, transition_sample :86-94, likelihood_potential :118-128).
+//
+// Data layout in HBM: particles dimension-major x[j * n + i] (each component
+// row is contiguous, so a warp's loads and stores are 128-byte coalesced and
+// the sorted ancestors of systematic / multinomial resampling keep the gather
+// coalesced); log-weights (n) float32; ancestors (n) int32.
+//
+// One thread per particle.  Per step and particle the kernel
+//   * derives key_i = split(k_t, n)[i] and draws eps = normal(key_i, (d,))
+//     (2 + ceil(d/2) threefry2x32 evaluations),
+//   * gathers x_prev[:, a_i] (a_i = i when the step did not resample),
+//   * x_new = F x + Lq eps, lw_new = lw_res - 0.5 |(y - H x_new) P|^2 - c,
+//   * reduces (max, sum e, sum e^2) over the block into a partial; the last
+//     block combines all partials (float64) into logsumexp / ESS, accumulates
+//     log Z, decides whether the next step resamples (ESS < threshold n) and
+//     clears the resampling scratch for it.
+// The resampling kernels of the next step read that decision from device
+// memory, so a whole run is enqueued without host round trips (and can be
+// captured in a CUDA graph).
+#include "mgb_internal.cuh"
+#include "mgb_resample.cuh"
+#include "mgb_kernels.cuh"
+
+namespace mgb {
+
+template <int D, int DY>
+struct LGP {
+  float F[D * D], Lq[D * D], H[DY * D], P[DY * DY], C0[D * D], m0[D];
+  float c;
+};
+
+struct PFState {
+  double logz;
+  double lse_prev;
+  float M;
+  int pad;
+};
+
+// per-run control block passed by value to the fused kernels
+struct PFCtl {
+  LsePartial *parts;
+  unsigned int *counter;
+  PFState *st;
+  float *ess_hist;     // (T,)
+  int32_t *res_hist;   // (T+1,): entry t = 1 if step t resamples
+  ResampleCtl *rctl;   // cleared by the finalising block for the next step
+  uint64_t *rstatus, *rstatus2;
+  int ntiles;
+  float thr_n;         // ess_threshold * n (float32, as the reference compares)
+  double logn;
+  double *logz_out;
+};
+
+constexpr int PF_TPB = 256;
+
+// last block: combine partials, update the running state, clear scratch
+template <int TPB>
+__device__ __forceinline__ void pf_finalize(const PFCtl &ctl, int64_t t, float *smf, double *smd) {
+  const LseOut o = combine_lse<TPB>(ctl.parts, gridDim.x, smf, smd);
+  if (threadIdx.x == 0) {
+    PFState *st = ctl.st;
+    const int res_t = t == 0 ? 0 : ctl.res_hist[t];
+    const double logz = t == 0 ? o.lse - ctl.logn : st->logz + o.lse - (res_t ? ctl.logn : st->lse_prev);
+    st->logz = logz;
+    st->lse_prev = o.lse;
+    st->M = o.M;
+    ctl.ess_hist[t] = (float)o.ess;
+    ctl.res_hist[t + 1] = ((float)o.ess < ctl.thr_n) ? 1 : 0;
+    if (ctl.logz_out) *ctl.logz_out = logz;
+    *ctl.counter = 0u;
+    ctl.rctl->tile_counter = 0u;
+    ctl.rctl->tile_counter2 = 0u;
+    ctl.rctl->degenerate = 0;
+    ctl.rctl->total = 0ull;
+  }
+  for (int j = threadIdx.x; j < ctl.ntiles; j += TPB) {
+    ctl.rstatus[j] = 0ull;
+    ctl.rstatus2[j] = 0ull;
+  }
+}
+
+template <int D, int DY>
+__device__ __forceinline__ float lg_potential(const LGP<D, DY> &p, const float (&x)[D], const float (&y)[DY]) {
+  float diff[DY];
+#pragma unroll
+  for (int j = 0; j < DY; ++j) {
+    float hx = __fmul_rn(p.H[j * D], x[0]);
+#pragma unroll
+    for (int k = 1; k < D; ++k) hx = __fmaf_rn(p.H[j * D + k], x[k], hx);
+    diff[j] = __fsub_rn(y[j], hx);
+  }
+  float quad = 0.0f;
+#pragma unroll
+  for (int k = 0; k < DY; ++k) {
+    float v = __fmul_rn(diff[0], p.P[k]);
+#pragma unroll
+    for (int j = 1; j < DY; ++j) v = __fmaf_rn(diff[j], p.P[j * DY + k], v);
+    quad = k == 0 ? __fmul_rn(v, v) : __fmaf_rn(v, v, quad);
+  }
+  return __fadd_rn(__fmul_rn(0.5f, quad), p.c);
+}
+
+template <int D>
+__device__ __forceinline__ void particle_normals(uint32_t k0, uint32_t k1, int64_t n, int64_t i, float (&e)[D]) {
+  uint32_t a0, a1;
+  split_at(k0, k1, (uint64_t)n, (uint64_t)i, a0, a1);
+  uint32_t b[D];
+  bits_vec<D>(a0, a1, b);
+#pragma unroll
+  for (int j = 0; j < D; ++j) e[j] = bits_to_normal(b[j]);
+}
+
+// block partial + (optionally) last-block finalize
+template <int TPB>
+__device__ __forceinline__ void pf_reduce(float lw, bool active, const PFCtl &ctl, int64_t t) {
+  __shared__ float smf[TPB / 32];
+  __shared__ double smd[TPB / 32];
+  __shared__ bool last;
+  const bool nan = active && lw != lw;
+  const LsePartial part = block_lse_partial<TPB>(active && !nan ? lw : -INFINITY, nan, smf, smd);
+  if (threadIdx.x == 0) {
+    ctl.parts[blockIdx.x] = part;
+    __threadfence();
+    last = atomicAdd(ctl.counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  pf_finalize<TPB>(ctl, t, smf, smd);
+}
+
+// initiate_particles: x_0 = C0 eps + m0, lw_0 = -potential(x_0, y_0)
+template <int D, int DY, bool FUSED>
+__global__ void __launch_bounds__(PF_TPB) k_lg_init(const __grid_constant__ LGP<D, DY> p, int64_t n,
+                                                     const uint32_t *key, const float *y0, float *__restrict__ x,
+                                                     float *__restrict__ lw, PFCtl ctl) {
+  const int64_t i = blockIdx.x * (int64_t)PF_TPB + threadIdx.x;
+  const uint32_t k0 = key[0], k1 = key[1];
+  float y[DY];
+#pragma unroll
+  for (int j = 0; j < DY; ++j) y[j] = y0 ? y0[j] : 0.0f;
+  float l = -INFINITY;
+  const bool active = i < n;
+  if (active) {
+    float e[D], xv[D];
+    particle_normals<D>(k0, k1, n, i, e);
+#pragma unroll
+    for (int r = 0; r < D; ++r) {
+      float v = __fmul_rn(p.C0[r * D], e[0]);
+#pragma unroll
+      for (int k = 1; k < D; ++k) v = __fmaf_rn(p.C0[r * D + k], e[k], v);
+      xv[r] = __fadd_rn(v, p.m0[r]);
+      x[r * n + i] = xv[r];
+    }
+    l = y0 ? -lg_potential<D, DY>(p, xv, y) : 0.0f;
+    lw[i] = l;
+  }
+  if (FUSED) pf_reduce<PF_TPB>(l, active, ctl, 0);
+}
+
+// one bootstrap step; res_flag (nullable) decides resampled vs identity at run time
+template <int D, int DY, bool FUSED>
+__global__ void __launch_bounds__(PF_TPB) k_lg_step(const __grid_constant__ LGP<D, DY> p, int64_t n,
+                                                     const uint32_t *key, const float *y_t,
+                                                     const float *__restrict__ x_prev, const int32_t *anc,
+                                                     const float *lw_prev, const int32_t *res_flag,
+                                                     float *__restrict__ x_new, float *__restrict__ lw_new,
+                                                     PFCtl ctl, int64_t t) {
+  const int64_t i = blockIdx.x * (int64_t)PF_TPB + threadIdx.x;
+  const bool res = res_flag ? (*res_flag != 0) : (anc != nullptr);
+  const uint32_t k0 = key[0], k1 = key[1];
+  float y[DY];
+#pragma unroll
+  for (int j = 0; j < DY; ++j) y[j] = y_t[j];
+  float l = -INFINITY;
+  const bool active = i < n;
+  if (active) {
+    float e[D], xs[D], xn[D];
+    particle_normals<D>(k0, k1, n, i, e);
+    const int64_t src = res ? (int64_t)anc[i] : i;
+#pragma unroll
+    for (int j = 0; j < D; ++j) xs[j] = __ldg(&x_prev[j * n + src]);
+#pragma unroll
+    for (int r = 0; r < D; ++r) {
+      float fx = __fmul_rn(p.F[r * D], xs[0]);
+#pragma unroll
+      for (int k = 1; k < D; ++k) fx = __fmaf_rn(p.F[r * D + k], xs[k], fx);
+      float le = __fmul_rn(p.Lq[r * D], e[0]);
+#pragma unroll
+      for (int k = 1; k < D; ++k) le = __fmaf_rn(p.Lq[r * D + k], e[k], le);
+      xn[r] = __fadd_rn(fx, le);
+      x_new[r * n + i] = xn[r];
+    }
+    // run mode (res_flag set): lw_res = 0 after a resample (filtering.py:292);
+    // standalone mode: lw_prev as given (NULL = 0)
+    const float *lws = res_flag ? (res ? nullptr : lw_prev) : lw_prev;
+    const float lres = lws ? lws[i] : 0.0f;
+    l = __fsub_rn(lres, lg_potential<D, DY>(p, xn, y));
+    lw_new[i] = l;
+  }
+  if (FUSED) pf_reduce<PF_TPB>(l, active, ctl, t);
+}
+
+// key schedule of run_particle_filter_for_marginals: (random_key, sub_key) =
+// split(key); step keys = split(random_key, T - 1).  out[0..1] = sub_key,
+// out[2t..2t+1] = key of step t (t >= 1).
+__global__ void k_setup_keys(const uint32_t *key, int64_t T, uint32_t *out) {
+  uint32_t r0, r1, s0, s1;
+  split_at(key[0], key[1], 2, 0, r0, r1);
+  split_at(key[0], key[1], 2, 1, s0, s1);
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < T; t += (int64_t)gridDim.x * blockDim.x) {
+    if (t == 0) {
+      out[0] = s0;
+      out[1] = s1;
+    } else {
+      uint32_t a, b;
+      split_at(r0, r1, (uint64_t)(T - 1), (uint64_t)(t - 1), a, b);
+      out[2 * t] = a;
+      out[2 * t + 1] = b;
+    }
+  }
+}
+
+__global__ void k_finish(const PFState *st, const int32_t *res_hist, int64_t T, double *logz, int32_t *resampled) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < T; t += (int64_t)gridDim.x * blockDim.x) {
+    if (resampled) resampled[t] = t == 0 ? 0 : res_hist[t];
+    if (t == 0 && logz) *logz = st->logz;
+  }
+}
+
+// ------------------------------------------------------------- host side
+template <int D, int DY>
+static LGP<D, DY> pack_lg(const mgb_lg_model *m) {
+  LGP<D, DY> p;
+  for (int i = 0; i < D * D; ++i) {
+    p.F[i] = m->F[i];
+    p.Lq[i] = m->Lq[i];
+    p.C0[i] = m->C0[i];
+  }
+  for (int i = 0; i < DY * D; ++i) p.H[i] = m->H[i];
+  for (int i = 0; i < DY * DY; ++i) p.P[i] = m->P[i];
+  for (int i = 0; i < D; ++i) p.m0[i] = m->m0[i];
+  p.c = m->c;
+  return p;
+}
+
+struct RunWs {
+  uint32_t *keys;
+  PFState *st;
+  LsePartial *parts;
+  unsigned int *counter;
+  int32_t *res_hist;
+  float *ess_hist;
+  float *xa, *xb, *la, *lb;
+  int32_t *anc;
+  ResampleWs rws;
+};
+
+static RunWs carve_run(Carver &c, int64_t n, int64_t T, int d, int scheme, bool need_x, bool need_lw, bool need_ess) {
+  RunWs w;
+  w.keys = c.take<uint32_t>(2 * (size_t)T);
+  w.st = c.take<PFState>(1);
+  w.parts = c.take<LsePartial>((size_t)((n + PF_TPB - 1) / PF_TPB));
+  w.counter = c.take<unsigned int>(1);
+  w.res_hist = c.take<int32_t>((size_t)T + 1);
+  w.ess_hist = need_ess ? c.take<float>((size_t)T) : nullptr;
+  w.xa = need_x ? c.take<float>((size_t)d * n) : nullptr;
+  w.xb = need_x ? c.take<float>((size_t)d * n) : nullptr;
+  w.la = need_lw ? c.take<float>((size_t)n) : nullptr;
+  w.lb = need_lw ? c.take<float>((size_t)n) : nullptr;
+  w.anc = c.take<int32_t>((size_t)n);
+  w.rws = carve_resample(c, n, scheme);
+  return w;
+}
+
+template <int D, int DY>
+static int run_lg(const mgb_lg_model *m, int64_t n, int64_t T, const uint32_t *key, const float *y, float thr,
+                  int scheme, void *ws, size_t ws_bytes, const mgb_pf_outputs *out, cudaStream_t s) {
+  const LGP<D, DY> p = pack_lg<D, DY>(m);
+  const bool hx = out && out->x_hist, hl = out && out->lw_hist;
+  Carver c(ws);
+  RunWs w = carve_run(c, n, T, D, scheme, !hx, !hl, !(out && out->ess));
+  if (c.bytes() > ws_bytes) return ERR_WORKSPACE;
+  float *ess = (out && out->ess) ? out->ess : w.ess_hist;
+  int *err = out ? out->err : nullptr;
+  if (cudaMemsetAsync(w.st, 0, sizeof(PFState), s) != cudaSuccess) return ERR_CUDA;
+  if (cudaMemsetAsync(w.counter, 0, sizeof(unsigned int), s) != cudaSuccess) return ERR_CUDA;
+  if (cudaMemsetAsync(w.res_hist, 0, sizeof(int32_t) * (T + 1), s) != cudaSuccess) return ERR_CUDA;
+  int st = reset_resample(w.rws, s);
+  if (st) return st;
+  k_setup_keys<<<grid_for(T, 256), 256, 0, s>>>(key, T, w.keys);
+
+  PFCtl ctl;
+  ctl.parts = w.parts;
+  ctl.counter = w.counter;
+  ctl.st = w.st;
+  ctl.ess_hist = ess;
+  ctl.res_hist = w.res_hist;
+  ctl.rctl = w.rws.ctl;
+  ctl.rstatus = w.rws.status;
+  ctl.rstatus2 = w.rws.status2;
+  ctl.ntiles = (int)w.rws.ntiles;
+  ctl.thr_n = thr * (float)n;
+  ctl.logn = log((double)n);
+  ctl.logz_out = nullptr;
+
+  const unsigned grid = (unsigned)((n + PF_TPB - 1) / PF_TPB);
+  auto xbuf = [&](int64_t t) -> float * { return hx ? out->x_hist + (size_t)t * D * n : (t & 1 ? w.xb : w.xa); };
+  auto lbuf = [&](int64_t t) -> float * { return hl ? out->lw_hist + (size_t)t * n : (t & 1 ? w.lb : w.la); };
+  k_lg_init<D, DY, true><<<grid, PF_TPB, 0, s>>>(p, n, w.keys, y, xbuf(0), lbuf(0), ctl);
+  if ((st = launch_status())) return st;
+  for (int64_t t = 1; t < T; ++t) {
+    st = launch_resample(lbuf(t - 1), n, scheme, &w.st->M, w.keys + 2 * t, 0, 0u, w.res_hist + t, w.rws, w.anc,
+                         err, s);
+    if (st) return st;
+    k_lg_step<D, DY, true><<<grid, PF_TPB, 0, s>>>(p, n, w.keys + 2 * t, y + (size_t)t * DY, xbuf(t - 1), w.anc,
+                                                    lbuf(t - 1), w.res_hist + t, xbuf(t), lbuf(t), ctl, t);
+    if ((st = launch_status())) return st;
+  }
+  k_finish<<<grid_for(T, 256), 256, 0, s>>>(w.st, w.res_hist, T, out ? out->log_z : nullptr,
+                                            out ? out->resampled : nullptr);
+  if (out && out->x_final && cudaMemcpyAsync(out->x_final, xbuf(T - 1), sizeof(float) * D * n,
+                                             cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+    return ERR_CUDA;
+  if (out && out->lw_final && cudaMemcpyAsync(out->lw_final, lbuf(T - 1), sizeof(float) * n,
+                                              cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+    return ERR_CUDA;
+  return launch_status();
+}
+
+template <int D, int DY>
+static int init_lg(const mgb_lg_model *m, int64_t n, const uint32_t *key, const float *y0, float *x, float *lw,
+                   cudaStream_t s) {
+  const LGP<D, DY> p = pack_lg<D, DY>(m);
+  PFCtl ctl{};
+  k_lg_init<D, DY, false><<<(unsigned)((n + PF_TPB - 1) / PF_TPB), PF_TPB, 0, s>>>(p, n, key, y0, x, lw, ctl);
+  return launch_status();
+}
+
+template <int D, int DY>
+static int step_lg(const mgb_lg_model *m, int64_t n, const uint32_t *key, const float *y, const float *xp,
+                   const int32_t *anc, const float *lwp, float *xn, float *lwn, cudaStream_t s) {
+  const LGP<D, DY> p = pack_lg<D, DY>(m);
+  PFCtl ctl{};
+  k_lg_step<D, DY, false><<<(unsigned)((n + PF_TPB - 1) / PF_TPB), PF_TPB, 0, s>>>(p, n, key, y, xp, anc, lwp,
+                                                                                    nullptr, xn, lwn, ctl, 0);
+  return launch_status();
+}
+
+// (d, dy) dispatch over the compiled instantiations
+#define MGB_LG_DISPATCH(FN, ...)                                   \
+  do {                                                             \
+    const int d_ = m->d, dy_ = m->dy;                              \
+    if (dy_ == 1) {                                                \
+      switch (d_) {                                                \
+        case 1: return FN<1, 1>(__VA_ARGS__);                      \
+        case 2: return FN<2, 1>(__VA_ARGS__);                      \
+        case 3: return FN<3, 1>(__VA_ARGS__);                      \
+        case 4: return FN<4, 1>(__VA_ARGS__);                      \
+        case 5: return FN<5, 1>(__VA_ARGS__);                      \
+        case 8: return FN<8, 1>(__VA_ARGS__);                      \
+        case 10: return FN<10, 1>(__VA_ARGS__);                    \
+        default: return ERR_UNSUPPORTED;                           \
+      }                                                            \
+    } else if (dy_ == d_) {                                        \
+      switch (d_) {                                                \
+        case 2: return FN<2, 2>(__VA_ARGS__);                      \
+        case 3: return FN<3, 3>(__VA_ARGS__);                      \
+        case 4: return FN<4, 4>(__VA_ARGS__);                      \
+        case 5: return FN<5, 5>(__VA_ARGS__);                      \
+        case 8: return FN<8, 8>(__VA_ARGS__);                      \
+        case 10: return FN<10, 10>(__VA_ARGS__);                   \
+        default: return ERR_UNSUPPORTED;                           \
+      }                                                            \
+    }                                                              \
+    return ERR_UNSUPPORTED;                                        \
+  } while (0)
+
+static bool lg_model_ok(const mgb_lg_model *m) {
+  return m && m->d >= 1 && m->dy >= 1 && m->F && m->Lq && m->H && m->P && m->C0 && m->m0;
+}
+
+}  // namespace mgb
+
+using namespace mgb;
+
+extern "C" {
+
+size_t mgb_pf_lg_workspace(int64_t n, int64_t T, int32_t d, int scheme) {
+  Carver c(nullptr);
+  carve_run(c, n, T < 1 ? 1 : T, d, scheme, true, true, true);
+  return c.bytes();
+}
+
+int mgb_pf_lg_init(const mgb_lg_model *m, int64_t n, const uint32_t *key, const float *y0, float *x, float *lw,
+                   void *stream) {
+  if (!lg_model_ok(m) || n < 1 || n > 0x7FFFFFFFll || !key || !x || !lw) return ERR_BAD_ARG;
+  MGB_LG_DISPATCH(init_lg, m, n, key, y0, x, lw, (cudaStream_t)stream);
+}
+
+int mgb_pf_lg_propagate(const mgb_lg_model *m, int64_t n, const uint32_t *key, const float *y, const float *xp,
+                        const int32_t *anc, const float *lwp, float *xn, float *lwn, void *stream) {
+  if (!lg_model_ok(m) || n < 1 || n > 0x7FFFFFFFll || !key || !y || !xp || !xn || !lwn) return ERR_BAD_ARG;
+  MGB_LG_DISPATCH(step_lg, m, n, key, y, xp, anc, lwp, xn, lwn, (cudaStream_t)stream);
+}
+
+int mgb_pf_lg_run(const mgb_lg_model *m, int64_t n, int64_t T, const uint32_t *key, const float *y, float thr,
+                  int scheme, void *ws, size_t ws_bytes, const mgb_pf_outputs *out, void *stream) {
+  if (!lg_model_ok(m) || n < 1 || n > 0x7FFFFFFFll || T < 1 || !key || !y || !ws) return ERR_BAD_ARG;
+  if (scheme < 0 || scheme > 2) return ERR_BAD_ARG;
+  if (scheme == MGB_RESAMPLE_CATEGORICAL && n > 46340) return ERR_UNSUPPORTED;
+  if (ws_bytes < mgb_pf_lg_workspace(n, T, m->d, scheme)) return ERR_WORKSPACE;
+  MGB_LG_DISPATCH(run_lg, m, n, T, key, y, thr, scheme, ws, ws_bytes, out, (cudaStream_t)stream);
+}
+
+}  // extern "C"

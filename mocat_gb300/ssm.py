@@ -1,0 +1,319 @@
+"""State-space models and particle filters with mocat's call signatures
+(mocat/src/ssm/ssm.py, linear_gaussian/linear_gaussian.py,
+scenarios/stochastic_volatility.py, filtering.py), running on the GPU.
+
+Differences from the reference, by design:
+  * ``resampling=`` selects the scheme; the default ``"systematic"`` is O(n).
+    ``"categorical"`` reproduces the reference's ``random.categorical``
+    (Gumbel-max, O(n^2)), ``"multinomial"`` is an O(n) inverse-CDF draw.
+  * The filter output cdict additionally carries ``log_z`` (log-marginal
+    likelihood from the log-weights) and ``resampled`` (per-step flags).
+  * ``history=False`` keeps only the final particles (the (T, n, d) history
+    of a 2^20-particle, 1000-step filter would be 42 GB).
+"""
+import ctypes
+import math
+
+import numpy as np
+import torch
+
+from . import _dev, _lib
+from . import random as mrandom
+from ._lib import call
+from .core import cdict
+from .metrics import ess_log_weight
+from .resampling import SCHEMES, resample
+
+LOG2PI = math.log(2.0 * math.pi)
+LG_SUPPORTED = {(1, 1), (2, 1), (3, 1), (4, 1), (5, 1), (8, 1), (10, 1),
+                (2, 2), (3, 3), (4, 4), (5, 5), (8, 8), (10, 10)}
+
+
+def _np(a):
+    if isinstance(a, torch.Tensor):
+        a = a.detach().cpu().numpy()
+    return np.asarray(a, dtype=np.float64)
+
+
+def _as_matrix(a, d):
+    a = _np(a)
+    if a.ndim == 0:
+        return np.eye(d) * float(a)
+    if a.ndim == 1:
+        return np.diag(a)
+    return a
+
+
+def _f32(a):
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float32))
+
+
+class StateSpaceModel:
+    """Plugin interface of mocat/src/ssm/ssm.py:18-81."""
+    name = None
+    dim = None
+    dim_obs = None
+
+    def __init__(self, name=None, **kwargs):
+        if name is not None:
+            self.name = name
+        for k, v in kwargs.items():
+            setattr(self, k, v)
+
+    def __repr__(self):
+        return f"mocat_gb300.StateSpaceModel.{self.__class__.__name__}"
+
+
+class TimeHomogenousLinearGaussian(StateSpaceModel):
+    """x_t ~ N(F x_{t-1}, Q), y_t ~ N(H x_t, R) (linear_gaussian.py:142-261).
+
+    Cached derived quantities follow reset_covariance (mocat/src/utils.py:247-262):
+    covariance square roots are Cholesky factors, precision square roots their
+    inverses, precision determinants 1 / det(covariance).
+    """
+    name = "Time-homogenous Linear Gaussian"
+    _PARAMS = ("initial_mean", "initial_covariance", "transition_matrix", "transition_covariance",
+               "likelihood_matrix", "likelihood_covariance")
+
+    def __init__(self, initial_mean=None, initial_covariance=None, transition_matrix=None,
+                 transition_covariance=None, likelihood_matrix=None, likelihood_covariance=None, name=None, **kwargs):
+        super().__init__(name=name, **kwargs)
+        if "dim" not in kwargs:
+            for a in (initial_mean, initial_covariance, transition_covariance, likelihood_matrix,
+                      likelihood_covariance):
+                if a is not None and np.ndim(_np(a)) > 0:
+                    self.dim = _np(a).shape[-1]
+                    break
+        if self.dim is None:
+            raise AttributeError(f"Could not find dimension for {self.__class__.__name__}")
+        d = self.dim
+        self.initial_mean = np.zeros(d) if initial_mean is None else _np(initial_mean).reshape(d)
+        self.initial_covariance = np.eye(d) if initial_covariance is None else _as_matrix(initial_covariance, d)
+        self.transition_matrix = np.eye(d) if transition_matrix is None else _as_matrix(transition_matrix, d)
+        self.transition_covariance = (np.eye(d) if transition_covariance is None
+                                      else _as_matrix(transition_covariance, d))
+        self.likelihood_matrix = np.eye(d) if likelihood_matrix is None else _as_matrix(likelihood_matrix, d)
+        self.dim_obs = self.likelihood_matrix.shape[0]
+        self.likelihood_covariance = (np.eye(self.dim_obs) if likelihood_covariance is None
+                                      else _as_matrix(likelihood_covariance, self.dim_obs))
+
+    def __setattr__(self, key, value):
+        self.__dict__[key] = value
+        if key in self._PARAMS:
+            self.__dict__.pop("_derived", None)
+
+    # derived float32 parameters and the C-ABI model struct
+    def derived(self):
+        if "_derived" not in self.__dict__:
+            R = self.likelihood_covariance
+            LR = np.linalg.cholesky(R)
+            det_prec = 1.0 / np.linalg.det(R)
+            p = dict(d=self.dim, dy=self.dim_obs, F=_f32(self.transition_matrix),
+                     Lq=_f32(np.linalg.cholesky(self.transition_covariance)), H=_f32(self.likelihood_matrix),
+                     P=_f32(np.linalg.inv(LR)), c=np.float32((self.dim_obs * LOG2PI - np.log(det_prec)) / 2.0),
+                     C0=_f32(np.linalg.cholesky(self.initial_covariance)), m0=_f32(self.initial_mean), LR=_f32(LR))
+            s = _lib.LGModel(p["d"], p["dy"], p["F"].ctypes.data, p["Lq"].ctypes.data, p["H"].ctypes.data,
+                             p["P"].ctypes.data, p["C0"].ctypes.data, p["m0"].ctypes.data, float(p["c"]))
+            self.__dict__["_derived"] = (p, s)
+        return self.__dict__["_derived"]
+
+    def gpu_supported(self):
+        return (self.dim, self.dim_obs) in LG_SUPPORTED
+
+    def simulate(self, t_all, random_key):
+        """StateSpaceModel.simulate (ssm.py:138-163): split(key, 2T), first T keys drive
+        the latent chain, the last T the observations.  Draws on the GPU."""
+        p, _ = self.derived()
+        T = len(t_all)
+        keys = mrandom.split(random_key, 2 * T)
+        d, dy = p["d"], p["dy"]
+        ex = _normal_keys(keys[:T], d).cpu().numpy()
+        ey = _normal_keys(keys[T:], dy).cpu().numpy()
+        x = np.empty((T, d), np.float32)
+        y = np.empty((T, dy), np.float32)
+        x[0] = (p["C0"] @ ex[0]).astype(np.float32) + p["m0"]
+        for t in range(1, T):
+            x[t] = (p["F"] @ x[t - 1]).astype(np.float32) + (p["Lq"] @ ex[t]).astype(np.float32)
+        for t in range(T):
+            y[t] = (p["H"] @ x[t]).astype(np.float32) + (p["LR"] @ ey[t]).astype(np.float32)
+        dev = _dev.device()
+        return cdict(x=torch.from_numpy(x).to(dev), y=torch.from_numpy(y).to(dev),
+                     t=torch.as_tensor(np.asarray(t_all), device=dev), name=f"{self.name} simulation")
+
+
+def _normal_keys(keys, d):
+    keys = _dev.as_key(keys)
+    out = torch.empty((keys.shape[0], d), dtype=torch.float32, device=keys.device)
+    call("mgb_normal_keys", _dev.ptr(keys), keys.shape[0], d, _dev.ptr(out), _dev.stream_ptr())
+    return out
+
+
+class ParticleFilter:
+    name = "Particle Filter"
+
+    def __init__(self, name=None):
+        if name is not None:
+            self.name = name
+
+    def __repr__(self):
+        return f"mocat_gb300.ParticleFilter.{self.__class__.__name__}"
+
+    def startup(self, ssm_scenario):
+        pass
+
+
+class BootstrapFilter(ParticleFilter):
+    """Propose from the transition, weight by the likelihood (filtering.py:142-170)."""
+    name = "Bootstrap Filter"
+
+
+def _check_lg(ssm_scenario, particle_filter):
+    if not isinstance(ssm_scenario, TimeHomogenousLinearGaussian):
+        raise NotImplementedError(f"{ssm_scenario.__class__.__name__}: no fused GPU kernel for this model")
+    if not isinstance(particle_filter, BootstrapFilter):
+        raise NotImplementedError(f"{particle_filter.__class__.__name__}: no fused GPU kernel for this filter")
+    if not ssm_scenario.gpu_supported():
+        raise NotImplementedError(f"(d, dy) = ({ssm_scenario.dim}, {ssm_scenario.dim_obs}) not compiled")
+
+
+def _y2(y, dy):
+    y = _dev.as_f32(y)
+    return y.reshape(-1, dy).contiguous()
+
+
+def initiate_particles(ssm_scenario, particle_filter, n, random_key, y=None, t=None):
+    """filtering.py:173-193: particles (1, n, d), log-weights (1, n), ess (1,)."""
+    _check_lg(ssm_scenario, particle_filter)
+    particle_filter.startup(ssm_scenario)
+    _, s = ssm_scenario.derived()
+    d = ssm_scenario.dim
+    dev = _dev.device()
+    key = _dev.as_key(random_key)
+    x = torch.empty((d, n), dtype=torch.float32, device=dev)
+    lw = torch.empty(n, dtype=torch.float32, device=dev)
+    yd = None if y is None else _y2(y, ssm_scenario.dim_obs).reshape(-1)
+    call("mgb_pf_lg_init", ctypes.byref(s), n, _dev.ptr(key), _dev.ptr(yd), _dev.ptr(x), _dev.ptr(lw),
+         _dev.stream_ptr())
+    return cdict(value=x.t().contiguous()[None], log_weight=lw[None],
+                 t=torch.atleast_1d(torch.as_tensor(0.0 if t is None else t, device=dev)),
+                 y=None if y is None else yd[None], ess=ess_log_weight(lw).reshape(1).float())
+
+
+def resample_particles(particles, random_key, resample_full=True, resampling="systematic"):
+    """filtering.py:202-217 (gather of the value history by the latest weights)."""
+    out = particles.copy()
+    lw = particles.log_weight if particles.log_weight.dim() == 1 else particles.log_weight[-1]
+    n = lw.numel()
+    anc = resample(lw, random_key, resampling).long()
+    if particles.log_weight.dim() == 1:
+        out.value = particles.value[anc]
+        out.log_weight = torch.zeros(n, device=lw.device)
+    elif resample_full:
+        out.value = particles.value[:, anc]
+        out.log_weight = particles.log_weight.clone()
+        out.log_weight[-1] = 0.0
+    else:
+        out.value = particles.value.clone()
+        out.value[-1] = particles.value[-1][anc]
+        out.log_weight = particles.log_weight.clone()
+        out.log_weight[-1] = 0.0
+    return out
+
+
+def _step(s, n, key, y_t, x_prev_soa, anc, lw_prev):
+    d = x_prev_soa.shape[0]
+    x_new = torch.empty_like(x_prev_soa)
+    lw_new = torch.empty(n, dtype=torch.float32, device=x_prev_soa.device)
+    call("mgb_pf_lg_propagate", ctypes.byref(s), n, _dev.ptr(key), _dev.ptr(y_t), _dev.ptr(x_prev_soa),
+         _dev.ptr(anc), _dev.ptr(lw_prev), _dev.ptr(x_new), _dev.ptr(lw_new), _dev.stream_ptr())
+    return x_new, lw_new
+
+
+def propagate_particle_filter(ssm_scenario, particle_filter, particles, y_new, t_new, random_key,
+                              ess_threshold=0.5, resample_full=True, resampling="systematic"):
+    """filtering.py:220-252: resample if ess < threshold n, then propagate and append."""
+    _check_lg(ssm_scenario, particle_filter)
+    _, s = ssm_scenario.derived()
+    n = particles.value.shape[1]
+    key = _dev.as_key(random_key)
+    if float(particles.ess[-1]) < ess_threshold * n:
+        particles = resample_particles(particles, key, resample_full, resampling)
+    x_prev = particles.value[-1].t().contiguous()
+    lw_prev = particles.log_weight[-1].contiguous()
+    y_t = _y2(y_new, ssm_scenario.dim_obs).reshape(-1)
+    x_new, lw_new = _step(s, n, key, y_t, x_prev, None, lw_prev)
+    out = particles.copy()
+    out.value = torch.cat([particles.value, x_new.t()[None]], 0)
+    out.log_weight = torch.cat([particles.log_weight, lw_new[None]], 0)
+    out.y = torch.cat([particles.y, y_t[None]], 0) if particles.y is not None else y_t[None]
+    out.t = torch.cat([particles.t, torch.atleast_1d(torch.as_tensor(t_new, device=out.t.device)).to(out.t.dtype)])
+    out.ess = torch.cat([particles.ess, ess_log_weight(lw_new).reshape(1).float()])
+    return out
+
+
+def run_particle_filter_for_marginals(ssm_scenario, particle_filter, y, t, random_key, n=None, initial_sample=None,
+                                      ess_threshold=0.5, resampling="systematic", history=True):
+    """filtering.py:255-324 on the GPU.
+
+    Returns cdict(value (T, n, d), log_weight (T, n), ess (T,), t, y, log_z, resampled)
+    (value/log_weight only the final step, shape (1, n, d) / (1, n), when history=False).
+    """
+    _check_lg(ssm_scenario, particle_filter)
+    particle_filter.startup(ssm_scenario)
+    _, s = ssm_scenario.derived()
+    d, dy = ssm_scenario.dim, ssm_scenario.dim_obs
+    dev = _dev.device()
+    y2 = _y2(y, dy)
+    key = _dev.as_key(random_key)
+    sc = SCHEMES[resampling]
+    if initial_sample is not None:
+        return _run_from(ssm_scenario, s, initial_sample, y2, t, key, ess_threshold, resampling)
+    T = y2.shape[0]
+    ws = _dev.workspace(_lib.lib().mgb_pf_lg_workspace(n, T, d, sc), dev)
+    logz = torch.empty(1, dtype=torch.float64, device=dev)
+    ess = torch.empty(T, dtype=torch.float32, device=dev)
+    res = torch.empty(T, dtype=torch.int32, device=dev)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    xh = torch.empty((T, d, n) if history else (1, d, n), dtype=torch.float32, device=dev)
+    lh = torch.empty((T, n) if history else (1, n), dtype=torch.float32, device=dev)
+    out = _lib.PFOutputs(logz.data_ptr(), ess.data_ptr(), res.data_ptr(), xh.data_ptr() if history else None,
+                         lh.data_ptr() if history else None, None if history else xh.data_ptr(),
+                         None if history else lh.data_ptr(), err.data_ptr())
+    call("mgb_pf_lg_run", ctypes.byref(s), n, T, _dev.ptr(key), _dev.ptr(y2), float(ess_threshold), sc,
+         _dev.ptr(ws), ws.numel(), ctypes.byref(out), _dev.stream_ptr())
+    e = int(err.item())
+    if e & 1:
+        raise _lib.MGBError(5, "run_particle_filter_for_marginals")
+    tt = torch.as_tensor(np.asarray(t if not isinstance(t, torch.Tensor) else t.cpu()), device=dev)
+    return cdict(value=xh.permute(0, 2, 1), log_weight=lh, ess=ess, t=tt, y=y2, log_z=logz[0],
+                 resampled=res.bool(), degenerate=bool(e & 2))
+
+
+def _run_from(ssm_scenario, s, initial_sample, y2, t, key, ess_threshold, resampling):
+    """Resume from given particles (filtering.py:266-275 with initial_sample set)."""
+    x = initial_sample.value[-1].t().contiguous()
+    lw = initial_sample.log_weight[-1].contiguous()
+    n = lw.numel()
+    ess = float(initial_sample.ess[-1])
+    T = y2.shape[0]
+    keys = mrandom.split(key, T)
+    vals, lws, esss, resd = [], [], [], []
+    logz = 0.0
+    lse_prev = float(torch.logsumexp(lw.double(), 0))
+    for i in range(T):
+        res = ess < ess_threshold * n
+        anc = resample(lw, keys[i], resampling) if res else None
+        x, lw = _step(s, n, keys[i], y2[i], x, anc, None if res else lw)
+        lse = float(torch.logsumexp(lw.double(), 0))
+        logz += lse - (math.log(n) if res else lse_prev)
+        lse_prev = lse
+        ess = float(ess_log_weight(lw))
+        vals.append(x.t())
+        lws.append(lw)
+        esss.append(ess)
+        resd.append(res)
+    dev = lw.device
+    return cdict(value=torch.stack(vals), log_weight=torch.stack(lws), ess=torch.tensor(esss, device=dev),
+                 t=torch.as_tensor(np.asarray(t if not isinstance(t, torch.Tensor) else t.cpu()), device=dev),
+                 y=y2, log_z=torch.tensor(logz, dtype=torch.float64, device=dev),
+                 resampled=torch.tensor(resd, device=dev))

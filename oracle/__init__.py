@@ -1,0 +1,343 @@
+"""ORACLE -- test infrastructure only.
+
+CPU restatement of mocat's particle-system step.  Only ``tests/``,
+``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg may import
+this package, and only as the checker (or the timed CPU baseline).  The
+product package ``mocat_gb300`` never imports it.
+
+Layers:
+  * ``oracle.c`` / ``oracle_rng.h`` (compiled by ``oracle/Makefile`` into
+    ``oracle/_build/liboracle.so``): jax.random restatement, particle-filter
+    step and run, resampling, LSE/ESS -- see the C headers for the
+    reference file:line each function follows.
+  * ``models.py``: parameter derivation of the reference's scenario classes
+    (``reset_covariance``, the optimal-proposal ``startup``), float64 -> float32.
+  * ``kalman.py``: float64 Kalman log-likelihood and its exact gradient.
+  * ``potentials.py``: numpy ``gaussian_potential``.
+  * ``smc.py``: numpy tempered SMC sampler.
+
+Parity status: the threefry2x32 core is pinned by the Random123 known-answer
+vectors and jax's documented ``split(PRNGKey(0))`` output; everything else is
+pinned by the reference's own tests (gaussian_potential vs scipy, bisect,
+leapfrog golden values, SMC log-normalising-constant closed form) and by the
+float64 Kalman oracle.  Bit parity of normals against XLA's erf_inv/log is
+unpinned (no JAX in this environment).
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+_lib = None
+
+u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
+f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+i64p = np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")
+vp = ctypes.c_void_p
+i64 = ctypes.c_int64
+
+
+def build():
+    """Compile the C restatement (idempotent)."""
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+
+
+class _LGModel(ctypes.Structure):
+    _fields_ = [("d", ctypes.c_int), ("dy", ctypes.c_int), ("F", vp), ("Lq", vp), ("H", vp), ("P", vp),
+                ("c", ctypes.c_float), ("C0", vp), ("m0", vp)]
+
+
+class _OptModel(ctypes.Structure):
+    _fields_ = [("d", ctypes.c_int), ("dy", ctypes.c_int), ("F", vp), ("H", vp), ("K", vp), ("S", vp), ("W", vp),
+                ("cw", ctypes.c_float), ("K0", vp), ("C0c", vp), ("m0", vp)]
+
+
+class _SVModel(ctypes.Structure):
+    _fields_ = [("phi", ctypes.c_float), ("bsig", ctypes.c_float), ("r2", ctypes.c_float),
+                ("cB", ctypes.c_float), ("c0", ctypes.c_float), ("m0", ctypes.c_float)]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            build()
+        L = ctypes.CDLL(_LIB_PATH)
+        L.o_threefry_block.argtypes = [ctypes.c_uint32, ctypes.c_uint32, u32p, u32p, i64, u32p, u32p]
+        for nm in ("o_random_bits", "o_split"):
+            getattr(L, nm).argtypes = [u32p, i64, u32p]
+        for nm in ("o_uniform", "o_normal", "o_exponential", "o_gumbel"):
+            getattr(L, nm).argtypes = [u32p, i64, f32p]
+        for nm in ("o_math_logf", "o_math_expf", "o_math_erfinvf"):
+            getattr(L, nm).argtypes = [f32p, i64, f32p]
+        L.o_lse_ess.argtypes = [f32p, i64, f64p]
+        L.o_weight_shift.argtypes = [i64]
+        L.o_weight_shift.restype = ctypes.c_int
+        L.o_exp_shift.argtypes = [i64]
+        L.o_exp_shift.restype = ctypes.c_int
+        L.o_quantise.argtypes = [f32p, i64, np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")]
+        L.o_quantise.restype = ctypes.c_int
+        L.o_resample_systematic.argtypes = [f32p, i64, ctypes.c_uint32, i32p]
+        L.o_resample_systematic.restype = ctypes.c_int
+        L.o_resample_multinomial.argtypes = [f32p, i64, u32p, i32p]
+        L.o_resample_multinomial.restype = ctypes.c_int
+        L.o_resample_gumbel.argtypes = [f32p, i64, i64, u32p, i32p]
+        L.o_lg_init.argtypes = [ctypes.POINTER(_LGModel), i64, u32p, vp, f32p, f32p]
+        L.o_lg_propagate.argtypes = [ctypes.POINTER(_LGModel), i64, u32p, f32p, f32p, vp, vp, f32p, f32p]
+        L.o_lg_run.argtypes = [ctypes.POINTER(_LGModel), i64, i64, u32p, f32p, ctypes.c_float, ctypes.c_int,
+                               f32p, i32p, vp, vp]
+        L.o_lg_run.restype = ctypes.c_double
+        L.o_opt_init.argtypes = [ctypes.POINTER(_OptModel), i64, u32p, f32p, f32p, f32p]
+        L.o_opt_propagate.argtypes = [ctypes.POINTER(_OptModel), i64, u32p, f32p, f32p, vp, vp, f32p, f32p]
+        L.o_opt_run.argtypes = [ctypes.POINTER(_OptModel), i64, i64, u32p, f32p, ctypes.c_float, ctypes.c_int,
+                                f32p, i32p, vp, vp]
+        L.o_opt_run.restype = ctypes.c_double
+        L.o_sv_run.argtypes = [ctypes.POINTER(_SVModel), i64, i64, u32p, f32p, ctypes.c_float, ctypes.c_int,
+                               vp, vp]
+        L.o_sv_run.restype = ctypes.c_double
+        L.o_sv_batch.argtypes = [ctypes.POINTER(_SVModel), i64, i64p, i64p, i64p, f32p, u32p, ctypes.c_float,
+                                 ctypes.c_int, f64p]
+        L.o_num_threads.restype = ctypes.c_int
+        L.o_set_num_threads.argtypes = [ctypes.c_int]
+        _lib = L
+    return _lib
+
+
+def _u32(a):
+    return np.ascontiguousarray(np.asarray(a, dtype=np.uint32))
+
+
+def _f32(a):
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float32))
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+# ----------------------------------------------------------------- RNG layer
+
+def threefry2x32(key, c0, c1):
+    c0, c1 = _u32(np.atleast_1d(c0)), _u32(np.atleast_1d(c1))
+    r0, r1 = np.empty_like(c0), np.empty_like(c1)
+    key = _u32(key)
+    lib().o_threefry_block(int(key[0]), int(key[1]), c0, c1, c0.size, r0, r1)
+    return r0, r1
+
+
+def PRNGKey(seed):
+    """jax.random.PRNGKey for a 32-bit seed: [seed >> 32 (= 0), seed & 0xffffffff]."""
+    s = int(seed)
+    return np.array([(s >> 32) & 0xFFFFFFFF if s >= 0 else 0, s & 0xFFFFFFFF], dtype=np.uint32)
+
+
+def random_bits(key, n):
+    out = np.empty(int(n), np.uint32)
+    lib().o_random_bits(_u32(key), out.size, out)
+    return out
+
+
+def split(key, num=2):
+    out = np.empty((int(num), 2), np.uint32)
+    lib().o_split(_u32(key), int(num), out.reshape(-1))
+    return out
+
+
+def _draw(fn, key, shape):
+    shape = tuple(np.atleast_1d(shape)) if shape != () else ()
+    n = int(np.prod(shape)) if shape else 1
+    out = np.empty(n, np.float32)
+    getattr(lib(), fn)(_u32(key), n, out)
+    return out.reshape(shape)
+
+
+def uniform(key, shape=()):
+    return _draw("o_uniform", key, shape)
+
+
+def normal(key, shape=()):
+    return _draw("o_normal", key, shape)
+
+
+def exponential(key, shape=()):
+    return _draw("o_exponential", key, shape)
+
+
+def gumbel(key, shape=()):
+    return _draw("o_gumbel", key, shape)
+
+
+def logf(x):
+    x = _f32(x)
+    out = np.empty_like(x)
+    lib().o_math_logf(x.reshape(-1), x.size, out.reshape(-1))
+    return out
+
+
+def expf(x):
+    x = _f32(x)
+    out = np.empty_like(x)
+    lib().o_math_expf(x.reshape(-1), x.size, out.reshape(-1))
+    return out
+
+
+def erfinvf(x):
+    x = _f32(x)
+    out = np.empty_like(x)
+    lib().o_math_erfinvf(x.reshape(-1), x.size, out.reshape(-1))
+    return out
+
+
+# ------------------------------------------------------ weights / resampling
+
+def lse_ess(lw):
+    """(max, logsumexp(lw), logsumexp(2 lw), ess) in float64 (metrics.py:69-78)."""
+    out = np.empty(4, np.float64)
+    lw = _f32(lw)
+    lib().o_lse_ess(lw, lw.size, out)
+    return out
+
+
+def quantise(lw):
+    lw = _f32(lw)
+    q = np.empty(lw.size, np.uint64)
+    ok = lib().o_quantise(lw, lw.size, q)
+    return q, bool(ok)
+
+
+def weight_shift(n):
+    return lib().o_weight_shift(int(n))
+
+
+def systematic_u_bits(key):
+    """23-bit mantissa m of u = uniform(key) = m 2^-23 (one draw, shape ())."""
+    return int(random_bits(key, 1)[0]) >> 9
+
+
+def resample_systematic(lw, m23):
+    lw = _f32(lw)
+    anc = np.empty(lw.size, np.int32)
+    ok = lib().o_resample_systematic(lw, lw.size, int(m23), anc)
+    return anc, bool(ok)
+
+
+def resample_multinomial(lw, key):
+    lw = _f32(lw)
+    anc = np.empty(lw.size, np.int32)
+    ok = lib().o_resample_multinomial(lw, lw.size, _u32(key), anc)
+    return anc, bool(ok)
+
+
+def resample_gumbel(lw, key, nout=None):
+    """random.categorical(key, lw, shape=(nout,)) -- mocat's _resample (filtering.py:196-199)."""
+    lw = _f32(lw)
+    nout = lw.size if nout is None else int(nout)
+    anc = np.empty(nout, np.int32)
+    lib().o_resample_gumbel(lw, lw.size, nout, _u32(key), anc)
+    return anc
+
+
+SCHEMES = {"systematic": 0, "multinomial": 1, "categorical": 2}
+
+
+# ----------------------------------------------------------- particle filters
+
+def _lg_struct(p):
+    keep = {k: _f32(v) for k, v in p.items() if isinstance(v, np.ndarray)}
+    s = _LGModel(int(p["d"]), int(p["dy"]), _ptr(keep["F"]), _ptr(keep["Lq"]), _ptr(keep["H"]), _ptr(keep["P"]),
+                 float(p["c"]), _ptr(keep["C0"]), _ptr(keep["m0"]))
+    return s, keep
+
+
+def lg_init(params, n, key, y0):
+    s, keep = _lg_struct(params)
+    x = np.empty((n, params["d"]), np.float32)
+    lw = np.empty(n, np.float32)
+    y0 = None if y0 is None else _f32(y0)
+    lib().o_lg_init(ctypes.byref(s), n, _u32(key), _ptr(y0), x.reshape(-1), lw)
+    return x, lw
+
+
+def lg_propagate(params, key_t, y, x_prev, anc=None, lw_prev=None):
+    s, keep = _lg_struct(params)
+    x_prev = _f32(x_prev)
+    n = x_prev.shape[0]
+    x_new = np.empty_like(x_prev)
+    lw_new = np.empty(n, np.float32)
+    anc = None if anc is None else np.ascontiguousarray(anc, dtype=np.int32)
+    lw_prev = None if lw_prev is None else _f32(lw_prev)
+    lib().o_lg_propagate(ctypes.byref(s), n, _u32(key_t), _f32(y), x_prev.reshape(-1), _ptr(anc), _ptr(lw_prev),
+                         x_new.reshape(-1), lw_new)
+    return x_new, lw_new
+
+
+def lg_run(params, n, key, y, ess_threshold=0.5, scheme="systematic", history=False):
+    s, keep = _lg_struct(params)
+    y = _f32(y).reshape(len(y), -1)
+    T = y.shape[0]
+    ess = np.empty(T, np.float32)
+    res = np.empty(T, np.int32)
+    xh = np.empty((T, n, params["d"]), np.float32) if history else None
+    lh = np.empty((T, n), np.float32) if history else None
+    logZ = lib().o_lg_run(ctypes.byref(s), n, T, _u32(key), y.reshape(-1), float(ess_threshold), SCHEMES[scheme],
+                          ess, res, _ptr(xh), _ptr(lh))
+    return dict(log_z=logZ, ess=ess, resampled=res.astype(bool), value=xh, log_weight=lh)
+
+
+def _opt_struct(p):
+    keep = {k: _f32(v) for k, v in p.items() if isinstance(v, np.ndarray)}
+    s = _OptModel(int(p["d"]), int(p["dy"]), _ptr(keep["F"]), _ptr(keep["H"]), _ptr(keep["K"]), _ptr(keep["S"]),
+                  _ptr(keep["W"]), float(p["cw"]), _ptr(keep["K0"]), _ptr(keep["C0c"]), _ptr(keep["m0"]))
+    return s, keep
+
+
+def opt_run(params, n, key, y, ess_threshold=0.5, scheme="systematic", history=False):
+    s, keep = _opt_struct(params)
+    y = _f32(y).reshape(len(y), -1)
+    T = y.shape[0]
+    ess = np.empty(T, np.float32)
+    res = np.empty(T, np.int32)
+    xh = np.empty((T, n, params["d"]), np.float32) if history else None
+    lh = np.empty((T, n), np.float32) if history else None
+    logZ = lib().o_opt_run(ctypes.byref(s), n, T, _u32(key), y.reshape(-1), float(ess_threshold), SCHEMES[scheme],
+                           ess, res, _ptr(xh), _ptr(lh))
+    return dict(log_z=logZ, ess=ess, resampled=res.astype(bool), value=xh, log_weight=lh)
+
+
+def _sv_struct(p):
+    return _SVModel(*(float(p[k]) for k in ("phi", "bsig", "r2", "cB", "c0", "m0")))
+
+
+def sv_run(params, n, key, y, ess_threshold=0.5, scheme="multinomial"):
+    s = _sv_struct(params)
+    y = _f32(y).reshape(-1)
+    T = y.size
+    ess = np.empty(T, np.float32)
+    res = np.empty(T, np.int32)
+    logZ = lib().o_sv_run(ctypes.byref(s), n, T, _u32(key), y, float(ess_threshold), SCHEMES[scheme],
+                          ess.ctypes.data, res.ctypes.data)
+    return dict(log_z=logZ, ess=ess, resampled=res.astype(bool))
+
+
+def sv_batch(params, n, T, y_off, y, keys, ess_threshold=0.5, scheme="multinomial"):
+    s = _sv_struct(params)
+    n = np.ascontiguousarray(n, np.int64)
+    T = np.ascontiguousarray(T, np.int64)
+    y_off = np.ascontiguousarray(y_off, np.int64)
+    out = np.empty(n.size, np.float64)
+    lib().o_sv_batch(ctypes.byref(s), n.size, n, T, y_off, _f32(y), _u32(keys).reshape(-1), float(ess_threshold),
+                     SCHEMES[scheme], out)
+    return out
+
+
+def num_threads():
+    return lib().o_num_threads()
+
+
+def set_num_threads(k):
+    lib().o_set_num_threads(int(k))

@@ -1,0 +1,629 @@
+/*
+ * ORACLE -- test infrastructure only (see oracle_rng.h).  CPU restatement of
+ * mocat's particle-system step, used by tests/ as the checker and by bench.py
+ * as the timed CPU baseline.  Never linked into the product library.
+ *
+ * What it restates (reference paths are relative to the mocat project):
+ *   - run_particle_filter_for_marginals / initiate_particles:
+ *       mocat/src/ssm/filtering.py:173-193, 255-324 (ESS trigger :286-292,
+ *       key reuse of int_rand_key for resampling and split :291/:294,
+ *       lw reset :292);
+ *   - BootstrapFilter weights: filtering.py:142-170;
+ *   - TimeHomogenousLinearGaussian sampling/potentials:
+ *       mocat/src/ssm/linear_gaussian/linear_gaussian.py:46-51, 86-94, 118-128;
+ *       gaussian_potential mocat/src/utils.py:49-105 (vectorised branch :90-104);
+ *   - StochasticVolatility: mocat/src/ssm/scenarios/stochastic_volatility.py:71-102;
+ *   - OptimalNonLinearGaussianParticleFilter fused step:
+ *       mocat/src/ssm/nonlinear_gaussian.py:198-209, 264-281;
+ *   - ESS / logsumexp: mocat/src/metrics.py:69-78 (max-shifted logsumexp of
+ *       jax.scipy.special.logsumexp, shift 0 when the max is not finite);
+ *   - _resample via random.categorical (Gumbel-max): filtering.py:196-199.
+ * New capabilities restated here with the same arithmetic as the device code:
+ *   systematic and sorted-uniform multinomial resampling on 62-bit fixed-point
+ *   weights (exact integer prefix sums, so ancestors do not depend on the
+ *   summation order), and the log-marginal-likelihood accumulated from the
+ *   filter's own log-weights.
+ *
+ * Build: oracle/Makefile (gcc -O2 -ffp-contract=off -fopenmp).
+ */
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#include <math.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+#include "oracle_rng.h"
+
+typedef unsigned __int128 u128;
+
+/* ------------------------------------------------------------------ RNG arrays */
+
+void o_threefry_block(uint32_t k0, uint32_t k1, const uint32_t *c0, const uint32_t *c1,
+                      int64_t n, uint32_t *r0, uint32_t *r1)
+{
+    for (int64_t i = 0; i < n; ++i) o_threefry2x32(k0, k1, c0[i], c1[i], &r0[i], &r1[i]);
+}
+
+void o_random_bits(const uint32_t *key, int64_t n, uint32_t *out)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t p = 0; p < n; ++p) out[p] = o_bits_at(key[0], key[1], (uint64_t)n, (uint64_t)p);
+}
+
+void o_split(const uint32_t *key, int64_t num, uint32_t *out)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < num; ++i)
+        o_split_at(key[0], key[1], (uint64_t)num, (uint64_t)i, &out[2 * i], &out[2 * i + 1]);
+}
+
+void o_uniform(const uint32_t *key, int64_t n, float *out)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t p = 0; p < n; ++p) out[p] = o_bits_to_unit(o_bits_at(key[0], key[1], (uint64_t)n, (uint64_t)p));
+}
+
+void o_normal(const uint32_t *key, int64_t n, float *out)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t p = 0; p < n; ++p) out[p] = o_bits_to_normal(o_bits_at(key[0], key[1], (uint64_t)n, (uint64_t)p));
+}
+
+void o_exponential(const uint32_t *key, int64_t n, float *out)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t p = 0; p < n; ++p)
+        out[p] = o_bits_to_exponential(o_bits_at(key[0], key[1], (uint64_t)n, (uint64_t)p));
+}
+
+void o_gumbel(const uint32_t *key, int64_t n, float *out)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t p = 0; p < n; ++p) out[p] = o_bits_to_gumbel(o_bits_at(key[0], key[1], (uint64_t)n, (uint64_t)p));
+}
+
+void o_math_logf(const float *x, int64_t n, float *out) { for (int64_t i = 0; i < n; ++i) out[i] = o_logf(x[i]); }
+void o_math_expf(const float *x, int64_t n, float *out) { for (int64_t i = 0; i < n; ++i) out[i] = o_expf(x[i]); }
+void o_math_erfinvf(const float *x, int64_t n, float *out) { for (int64_t i = 0; i < n; ++i) out[i] = o_erfinvf(x[i]); }
+
+/* ------------------------------------------------------------- LSE and ESS */
+
+/* out = {max, lse(lw), lse(2 lw), ess}; metrics.py:69-78 in float64. */
+void o_lse_ess(const float *lw, int64_t n, double *out)
+{
+    double m = -INFINITY;
+    int nan = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        if (lw[i] != lw[i]) nan = 1;
+        else if ((double)lw[i] > m) m = lw[i];
+    }
+    if (nan) { out[0] = out[1] = out[2] = out[3] = NAN; return; }
+    double sh = isfinite(m) ? m : 0.0;
+    double s1 = 0.0, s2 = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : s1, s2)
+    for (int64_t i = 0; i < n; ++i) {
+        double e = exp((double)lw[i] - sh);
+        s1 += e;
+        s2 += e * e;
+    }
+    double lse = log(s1) + sh, lse2 = log(s2) + 2.0 * sh;
+    out[0] = m;
+    out[1] = lse;
+    out[2] = lse2;
+    out[3] = exp(2.0 * lse - lse2);
+}
+
+/* ------------------------------------------------------ fixed-point weights */
+
+int o_ceil_log2(uint64_t n)
+{
+    int b = 0;
+    while (b < 63 && ((uint64_t)1 << b) < n) ++b;
+    return b;
+}
+
+/* Shift used to quantise normalised weights exp(lw - max) in (0, 1] so that
+ * the total of n of them stays below 2^62. */
+int o_weight_shift(int64_t n) { return 61 - o_ceil_log2((uint64_t)n); }
+
+/* q_i = trunc(expf(lw_i - max) * 2^S); returns 0 when the weights are
+ * degenerate (a NaN or +inf log-weight, or every weight zero). */
+int o_quantise(const float *lw, int64_t n, uint64_t *q)
+{
+    float m = -INFINITY;
+    for (int64_t i = 0; i < n; ++i) {
+        if (lw[i] != lw[i] || lw[i] == INFINITY) return 0;
+        if (lw[i] > m) m = lw[i];
+    }
+    if (m == -INFINITY) return 0;
+    float scale = ldexpf(1.0f, o_weight_shift(n));
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        float e = o_expf(lw[i] - m);
+        q[i] = (uint64_t)(e * scale);
+    }
+    uint64_t tot = 0;
+    for (int64_t i = 0; i < n; ++i) tot += q[i];
+    return tot > 0;
+}
+
+/* a_k = #{ i : C_i * den <= num_k * Q }, C inclusive prefix of q, num_k
+ * non-decreasing.  Two-pointer merge. */
+static void o_merge_search(const uint64_t *C, int64_t n, uint64_t Q, const uint64_t *num, uint64_t den,
+                           int64_t nout, int32_t *anc)
+{
+    int64_t i = 0;
+    for (int64_t k = 0; k < nout; ++k) {
+        u128 rhs = (u128)num[k] * Q;
+        while (i < n && (u128)C[i] * den <= rhs) ++i;
+        anc[k] = (int32_t)(i < n ? i : n - 1);
+    }
+}
+
+/* Systematic resampling: u = m 2^-23 (m = bits >> 9 of the step key);
+ * threshold numerators k 2^23 + m over denominator n 2^23. */
+int o_resample_systematic(const float *lw, int64_t n, uint32_t m23, int32_t *anc)
+{
+    uint64_t *q = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)n);
+    uint64_t *num = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)n);
+    int ok = o_quantise(lw, n, q);
+    if (ok) {
+        for (int64_t i = 1; i < n; ++i) q[i] += q[i - 1];
+        for (int64_t k = 0; k < n; ++k) num[k] = ((uint64_t)k << 23) + m23;
+        o_merge_search(q, n, q[n - 1], num, (uint64_t)n << 23, n, anc);
+    } else {
+        for (int64_t k = 0; k < n; ++k) anc[k] = 0;
+    }
+    free(q);
+    free(num);
+    return ok;
+}
+
+/* Multinomial resampling by inverse CDF at sorted uniforms built from n+1
+ * exponential spacings E = exponential(key, (n+1,)), quantised by 2^SE. */
+int o_exp_shift(int64_t n) { return 56 - o_ceil_log2((uint64_t)n + 1); }
+
+int o_resample_multinomial(const float *lw, int64_t n, const uint32_t *key, int32_t *anc)
+{
+    uint64_t *q = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)n);
+    uint64_t *S = (uint64_t *)calloc((size_t)(n + 1), sizeof(uint64_t));
+    int ok = o_quantise(lw, n, q);
+    if (ok) {
+        float sc = ldexpf(1.0f, o_exp_shift(n));
+        uint64_t acc = 0;
+        for (int64_t j = 0; j <= n; ++j) {
+            float E = o_bits_to_exponential(o_bits_at(key[0], key[1], (uint64_t)n + 1, (uint64_t)j));
+            acc += (uint64_t)(E * sc);
+            S[j] = acc;
+        }
+        for (int64_t i = 1; i < n; ++i) q[i] += q[i - 1];
+        if (S[n] == 0) ok = 0;
+        else o_merge_search(q, n, q[n - 1], S, S[n], n, anc);
+    }
+    if (!ok) for (int64_t k = 0; k < n; ++k) anc[k] = 0;
+    free(q);
+    free(S);
+    return ok;
+}
+
+/* random.categorical(key, lw, shape=(nout,)) = argmax_i(gumbel[k, i] + lw_i),
+ * gumbel drawn with shape (nout, n) (first maximum wins, as jnp.argmax;
+ * NaN entries are skipped and an all-NaN row gives index 0). */
+void o_resample_gumbel(const float *lw, int64_t n, int64_t nout, const uint32_t *key, int32_t *anc)
+{
+    uint64_t tot = (uint64_t)n * (uint64_t)nout;
+#pragma omp parallel for schedule(static)
+    for (int64_t k = 0; k < nout; ++k) {
+        float best = -INFINITY;
+        int32_t bi = 0;
+        int have = 0;
+        for (int64_t i = 0; i < n; ++i) {
+            float g = o_bits_to_gumbel(o_bits_at(key[0], key[1], tot, (uint64_t)k * (uint64_t)n + (uint64_t)i));
+            float v = g + lw[i];
+            if (v == v && (!have || v > best)) { best = v; bi = (int32_t)i; have = 1; }
+        }
+        anc[k] = bi;
+    }
+}
+
+/* --------------------------------------------------- linear-Gaussian model */
+
+typedef struct {
+    int d, dy;
+    const float *F;   /* d x d transition_matrix */
+    const float *Lq;  /* d x d transition_covariance_sqrt */
+    const float *H;   /* dy x d likelihood_matrix */
+    const float *P;   /* dy x dy likelihood_precision_sqrt */
+    float c;          /* (dy log 2pi - log likelihood_precision_det) / 2 */
+    const float *C0;  /* d x d initial_covariance_sqrt */
+    const float *m0;  /* d initial_mean */
+} o_lg_model;
+
+/* likelihood_potential(x, y) = 0.5 |(y - H x) @ P|^2 + c  (linear_gaussian.py:118-128) */
+static inline float o_lg_potential(const o_lg_model *md, const float *x, const float *y)
+{
+    float diff[64];
+    for (int j = 0; j < md->dy; ++j) {
+        const float *h = md->H + j * md->d;
+        float hx = h[0] * x[0];
+        for (int k = 1; k < md->d; ++k) hx = fmaf(h[k], x[k], hx);
+        diff[j] = y[j] - hx;
+    }
+    float quad = 0.0f;
+    for (int k = 0; k < md->dy; ++k) {
+        float v = diff[0] * md->P[k];
+        for (int j = 1; j < md->dy; ++j) v = fmaf(diff[j], md->P[j * md->dy + k], v);
+        quad = k == 0 ? v * v : fmaf(v, v, quad);
+    }
+    return 0.5f * quad + md->c;
+}
+
+/* normal(key, (d,)) into e */
+static inline void o_normal_vec(uint32_t k0, uint32_t k1, int d, float *e)
+{
+    for (int j = 0; j < d; ++j) e[j] = o_bits_to_normal(o_bits_at(k0, k1, (uint64_t)d, (uint64_t)j));
+}
+
+/* initiate_particles with TimeHomogenousLinearGaussian.initial_sample:
+ * x_i = C0 @ normal(split(key, n)[i], (d,)) + m0; lw_i = -potential(x_i, y0).
+ * x is particle-major (n, d). */
+void o_lg_init(const o_lg_model *md, int64_t n, const uint32_t *key, const float *y0, float *x, float *lw)
+{
+    const int d = md->d;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        uint32_t a0, a1;
+        float e[64];
+        o_split_at(key[0], key[1], (uint64_t)n, (uint64_t)i, &a0, &a1);
+        o_normal_vec(a0, a1, d, e);
+        float *xi = x + i * d;
+        for (int r = 0; r < d; ++r) {
+            const float *c = md->C0 + r * d;
+            float v = c[0] * e[0];
+            for (int k = 1; k < d; ++k) v = fmaf(c[k], e[k], v);
+            xi[r] = v + md->m0[r];
+        }
+        lw[i] = y0 ? -o_lg_potential(md, xi, y0) : 0.0f;
+    }
+}
+
+/* Bootstrap propagate + weight for one step (filtering.py:294-303):
+ * key_i = split(k_t, n)[i]; x_new = F x_src + Lq normal(key_i, (d,));
+ * lw_new = lw_res - potential(x_new, y_t).  anc may be NULL (no resampling),
+ * lw_prev NULL means lw_res = 0. */
+void o_lg_propagate(const o_lg_model *md, int64_t n, const uint32_t *kt, const float *y, const float *x_prev,
+                    const int32_t *anc, const float *lw_prev, float *x_new, float *lw_new)
+{
+    const int d = md->d;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        uint32_t a0, a1;
+        float e[64];
+        o_split_at(kt[0], kt[1], (uint64_t)n, (uint64_t)i, &a0, &a1);
+        o_normal_vec(a0, a1, d, e);
+        const float *xs = x_prev + (int64_t)(anc ? anc[i] : i) * d;
+        float *xn = x_new + i * d;
+        for (int r = 0; r < d; ++r) {
+            const float *f = md->F + r * d;
+            const float *l = md->Lq + r * d;
+            float fx = f[0] * xs[0];
+            for (int k = 1; k < d; ++k) fx = fmaf(f[k], xs[k], fx);
+            float le = l[0] * e[0];
+            for (int k = 1; k < d; ++k) le = fmaf(l[k], e[k], le);
+            xn[r] = fx + le;
+        }
+        float lres = lw_prev ? lw_prev[i] : 0.0f;
+        lw_new[i] = lres - o_lg_potential(md, xn, y);
+    }
+}
+
+/* Whole filter (filtering.py:255-324) with resampling scheme
+ * 0 = systematic, 1 = multinomial (sorted uniforms), 2 = categorical (Gumbel-max).
+ * Outputs: logZ (log-marginal-likelihood built from the log-weights),
+ * ess[T], resampled[T] (resampled[t] = 1 when step t started with a resample),
+ * optional histories x_hist (T, n, d) and lw_hist (T, n) (NULL to skip). */
+double o_lg_run(const o_lg_model *md, int64_t n, int64_t T, const uint32_t *key, const float *y,
+                float ess_threshold, int scheme, float *ess_out, int32_t *resampled_out,
+                float *x_hist, float *lw_hist)
+{
+    const int d = md->d, dy = md->dy;
+    float *xa = (float *)malloc(sizeof(float) * (size_t)(n * d));
+    float *xb = (float *)malloc(sizeof(float) * (size_t)(n * d));
+    float *la = (float *)malloc(sizeof(float) * (size_t)n);
+    float *lb = (float *)malloc(sizeof(float) * (size_t)n);
+    int32_t *anc = (int32_t *)malloc(sizeof(int32_t) * (size_t)n);
+    uint32_t keys2[4], rk[2], sk[2];
+    o_split(key, 2, keys2);
+    rk[0] = keys2[0]; rk[1] = keys2[1];
+    sk[0] = keys2[2]; sk[1] = keys2[3];
+
+    o_lg_init(md, n, sk, y, xa, la);
+    double st[4];
+    o_lse_ess(la, n, st);
+    double logn = log((double)n);
+    double logZ = st[1] - logn;
+    double lse_prev = st[1];
+    float ess_prev = (float)st[3];
+    ess_out[0] = ess_prev;
+    resampled_out[0] = 0;
+    if (x_hist) memcpy(x_hist, xa, sizeof(float) * (size_t)(n * d));
+    if (lw_hist) memcpy(lw_hist, la, sizeof(float) * (size_t)n);
+
+    uint32_t *tkeys = (uint32_t *)malloc(sizeof(uint32_t) * 2 * (size_t)(T > 1 ? T - 1 : 1));
+    if (T > 1) o_split(rk, T - 1, tkeys);
+    for (int64_t t = 1; t < T; ++t) {
+        const uint32_t *kt = tkeys + 2 * (t - 1);
+        int res = ess_prev < ess_threshold * (float)n;
+        if (res) {
+            if (scheme == 0) {
+                uint32_t b = o_bits_at(kt[0], kt[1], 1, 0);
+                o_resample_systematic(la, n, b >> 9, anc);
+            } else if (scheme == 1) {
+                o_resample_multinomial(la, n, kt, anc);
+            } else {
+                o_resample_gumbel(la, n, n, kt, anc);
+            }
+        }
+        o_lg_propagate(md, n, kt, y + t * dy, xa, res ? anc : NULL, res ? NULL : la, xb, lb);
+        o_lse_ess(lb, n, st);
+        logZ += st[1] - (res ? logn : lse_prev);
+        lse_prev = st[1];
+        ess_prev = (float)st[3];
+        ess_out[t] = ess_prev;
+        resampled_out[t] = res;
+        if (x_hist) memcpy(x_hist + t * n * d, xb, sizeof(float) * (size_t)(n * d));
+        if (lw_hist) memcpy(lw_hist + t * n, lb, sizeof(float) * (size_t)n);
+        float *tp = xa; xa = xb; xb = tp;
+        tp = la; la = lb; lb = tp;
+    }
+    free(tkeys);
+    free(xa); free(xb); free(la); free(lb); free(anc);
+    return logZ;
+}
+
+/* ------------------------------------------ optimal proposal (A6, linear f) */
+
+typedef struct {
+    int d, dy;
+    const float *F;    /* transition_function x -> F x */
+    const float *H;    /* dy x d */
+    const float *K;    /* d x dy proposal_kalman_gain */
+    const float *S;    /* d x d proposal_covariance_sqrt */
+    const float *W;    /* dy x dy weight_precision_sqrt */
+    float cw;          /* (dy log 2pi - log weight_precision_det) / 2 */
+    const float *K0;   /* d x dy initial_kalman_gain */
+    const float *C0c;  /* d x d initial_conditioned_covariance_sqrt */
+    const float *m0;   /* d */
+} o_opt_model;
+
+/* initial_sample (nonlinear_gaussian.py:198-209): mean + normal(keys[0], (n, d)) @ C0c
+ * with keys = split(key, n); initial weights are zero. */
+void o_opt_init(const o_opt_model *md, int64_t n, const uint32_t *key, const float *y0, float *x, float *lw)
+{
+    const int d = md->d, dy = md->dy;
+    uint32_t k0, k1;
+    o_split_at(key[0], key[1], (uint64_t)n, 0, &k0, &k1);
+    float mean[64], innov[64];
+    for (int j = 0; j < dy; ++j) {
+        float hm = md->H[j * d] * md->m0[0];
+        for (int k = 1; k < d; ++k) hm = fmaf(md->H[j * d + k], md->m0[k], hm);
+        innov[j] = y0[j] - hm;
+    }
+    for (int r = 0; r < d; ++r) {
+        float g = md->K0[r * dy] * innov[0];
+        for (int j = 1; j < dy; ++j) g = fmaf(md->K0[r * dy + j], innov[j], g);
+        mean[r] = md->m0[r] + g;
+    }
+    uint64_t tot = (uint64_t)n * (uint64_t)d;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        float e[64];
+        for (int j = 0; j < d; ++j) e[j] = o_bits_to_normal(o_bits_at(k0, k1, tot, (uint64_t)i * d + j));
+        for (int r = 0; r < d; ++r) {
+            float v = e[0] * md->C0c[r];
+            for (int k = 1; k < d; ++k) v = fmaf(e[k], md->C0c[k * d + r], v);
+            x[i * d + r] = mean[r] + v;
+        }
+        lw[i] = 0.0f;
+    }
+}
+
+/* fused vectorised step (nonlinear_gaussian.py:264-281): noise from keys[0] of
+ * split(k_t, n) with shape (n, d). */
+void o_opt_propagate(const o_opt_model *md, int64_t n, const uint32_t *kt, const float *y, const float *x_prev,
+                     const int32_t *anc, const float *lw_prev, float *x_new, float *lw_new)
+{
+    const int d = md->d, dy = md->dy;
+    uint32_t k0, k1;
+    o_split_at(kt[0], kt[1], (uint64_t)n, 0, &k0, &k1);
+    uint64_t tot = (uint64_t)n * (uint64_t)d;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        float mx[64], innov[64], e[64];
+        const float *xs = x_prev + (int64_t)(anc ? anc[i] : i) * d;
+        for (int r = 0; r < d; ++r) {
+            float v = md->F[r * d] * xs[0];
+            for (int k = 1; k < d; ++k) v = fmaf(md->F[r * d + k], xs[k], v);
+            mx[r] = v;
+        }
+        for (int j = 0; j < dy; ++j) {
+            float hm = mx[0] * md->H[j * d];
+            for (int k = 1; k < d; ++k) hm = fmaf(mx[k], md->H[j * d + k], hm);
+            innov[j] = y[j] - hm;
+        }
+        for (int j = 0; j < d; ++j) e[j] = o_bits_to_normal(o_bits_at(k0, k1, tot, (uint64_t)i * d + j));
+        for (int r = 0; r < d; ++r) {
+            float g = innov[0] * md->K[r * dy];
+            for (int j = 1; j < dy; ++j) g = fmaf(innov[j], md->K[r * dy + j], g);
+            float s = e[0] * md->S[r * d];
+            for (int k = 1; k < d; ++k) s = fmaf(e[k], md->S[r * d + k], s);
+            x_new[i * d + r] = (mx[r] + g) + s;
+        }
+        float quad = 0.0f;
+        for (int k = 0; k < dy; ++k) {
+            float v = innov[0] * md->W[k];
+            for (int j = 1; j < dy; ++j) v = fmaf(innov[j], md->W[j * dy + k], v);
+            quad = k == 0 ? v * v : fmaf(v, v, quad);
+        }
+        float lres = lw_prev ? lw_prev[i] : 0.0f;
+        lw_new[i] = lres - (0.5f * quad + md->cw);
+    }
+}
+
+double o_opt_run(const o_opt_model *md, int64_t n, int64_t T, const uint32_t *key, const float *y,
+                 float ess_threshold, int scheme, float *ess_out, int32_t *resampled_out,
+                 float *x_hist, float *lw_hist)
+{
+    const int d = md->d, dy = md->dy;
+    float *xa = (float *)malloc(sizeof(float) * (size_t)(n * d));
+    float *xb = (float *)malloc(sizeof(float) * (size_t)(n * d));
+    float *la = (float *)malloc(sizeof(float) * (size_t)n);
+    float *lb = (float *)malloc(sizeof(float) * (size_t)n);
+    int32_t *anc = (int32_t *)malloc(sizeof(int32_t) * (size_t)n);
+    uint32_t keys2[4], rk[2], sk[2];
+    o_split(key, 2, keys2);
+    rk[0] = keys2[0]; rk[1] = keys2[1];
+    sk[0] = keys2[2]; sk[1] = keys2[3];
+    o_opt_init(md, n, sk, y, xa, la);
+    double st[4];
+    o_lse_ess(la, n, st);
+    double logn = log((double)n);
+    double logZ = st[1] - logn, lse_prev = st[1];
+    float ess_prev = (float)st[3];
+    ess_out[0] = ess_prev;
+    resampled_out[0] = 0;
+    if (x_hist) memcpy(x_hist, xa, sizeof(float) * (size_t)(n * d));
+    if (lw_hist) memcpy(lw_hist, la, sizeof(float) * (size_t)n);
+    uint32_t *tkeys = (uint32_t *)malloc(sizeof(uint32_t) * 2 * (size_t)(T > 1 ? T - 1 : 1));
+    if (T > 1) o_split(rk, T - 1, tkeys);
+    for (int64_t t = 1; t < T; ++t) {
+        const uint32_t *kt = tkeys + 2 * (t - 1);
+        int res = ess_prev < ess_threshold * (float)n;
+        if (res) {
+            if (scheme == 0) o_resample_systematic(la, n, o_bits_at(kt[0], kt[1], 1, 0) >> 9, anc);
+            else if (scheme == 1) o_resample_multinomial(la, n, kt, anc);
+            else o_resample_gumbel(la, n, n, kt, anc);
+        }
+        o_opt_propagate(md, n, kt, y + t * dy, xa, res ? anc : NULL, res ? NULL : la, xb, lb);
+        o_lse_ess(lb, n, st);
+        logZ += st[1] - (res ? logn : lse_prev);
+        lse_prev = st[1];
+        ess_prev = (float)st[3];
+        ess_out[t] = ess_prev;
+        resampled_out[t] = res;
+        if (x_hist) memcpy(x_hist + t * n * d, xb, sizeof(float) * (size_t)(n * d));
+        if (lw_hist) memcpy(lw_hist + t * n, lb, sizeof(float) * (size_t)n);
+        float *tp = xa; xa = xb; xb = tp;
+        tp = la; la = lb; lb = tp;
+    }
+    free(tkeys);
+    free(xa); free(xb); free(la); free(lb); free(anc);
+    return logZ;
+}
+
+/* ---------------------------------------------- stochastic volatility, d = 1 */
+
+typedef struct {
+    float phi;    /* transition_matrix */
+    float bsig;   /* transition_covariance_sqrt * sqrt(t_new - t_prev) */
+    float r2;     /* likelihood_precision_diag_sqrt^2 = 1 / R */
+    float cB;     /* (log 2pi - log r2) / 2 */
+    float c0;     /* initial_covariance_sqrt */
+    float m0;     /* initial_mean */
+} o_sv_model;
+
+/* likelihood_potential (stochastic_volatility.py:96-102) with
+ * s = r / exp(x/2):  0.5 y^2 s^2 + 0.5 (log 2pi - log s^2)
+ *                 =  (0.5 y^2 r^2) exp(-x) + (0.5 x + cB). */
+static inline float o_sv_potential(const o_sv_model *md, float x, float y)
+{
+    float a = (0.5f * (y * y)) * md->r2;
+    return fmaf(a, o_expf(-x), fmaf(0.5f, x, md->cB));
+}
+
+/* One stochastic-volatility filter; scheme as in o_lg_run.  Returns logZ. */
+double o_sv_run(const o_sv_model *md, int64_t n, int64_t T, const uint32_t *key, const float *y,
+                float ess_threshold, int scheme, float *ess_out, int32_t *resampled_out)
+{
+    float *xa = (float *)malloc(sizeof(float) * (size_t)n), *xb = (float *)malloc(sizeof(float) * (size_t)n);
+    float *la = (float *)malloc(sizeof(float) * (size_t)n), *lb = (float *)malloc(sizeof(float) * (size_t)n);
+    int32_t *anc = (int32_t *)malloc(sizeof(int32_t) * (size_t)n);
+    uint32_t keys2[4], rk[2], sk[2];
+    o_split(key, 2, keys2);
+    rk[0] = keys2[0]; rk[1] = keys2[1];
+    sk[0] = keys2[2]; sk[1] = keys2[3];
+    for (int64_t i = 0; i < n; ++i) {
+        uint32_t a0, a1;
+        o_split_at(sk[0], sk[1], (uint64_t)n, (uint64_t)i, &a0, &a1);
+        float e = o_bits_to_normal(o_bits_at(a0, a1, 1, 0));
+        xa[i] = e * md->c0 + md->m0;
+        la[i] = -o_sv_potential(md, xa[i], y[0]);
+    }
+    double st[4];
+    o_lse_ess(la, n, st);
+    double logn = log((double)n);
+    double logZ = st[1] - logn, lse_prev = st[1];
+    float ess_prev = (float)st[3];
+    if (ess_out) ess_out[0] = ess_prev;
+    if (resampled_out) resampled_out[0] = 0;
+    uint32_t *tkeys = (uint32_t *)malloc(sizeof(uint32_t) * 2 * (size_t)(T > 1 ? T - 1 : 1));
+    if (T > 1) o_split(rk, T - 1, tkeys);
+    for (int64_t t = 1; t < T; ++t) {
+        const uint32_t *kt = tkeys + 2 * (t - 1);
+        int res = ess_prev < ess_threshold * (float)n;
+        if (res) {
+            if (scheme == 0) o_resample_systematic(la, n, o_bits_at(kt[0], kt[1], 1, 0) >> 9, anc);
+            else if (scheme == 1) o_resample_multinomial(la, n, kt, anc);
+            else o_resample_gumbel(la, n, n, kt, anc);
+        }
+        for (int64_t i = 0; i < n; ++i) {
+            uint32_t a0, a1;
+            o_split_at(kt[0], kt[1], (uint64_t)n, (uint64_t)i, &a0, &a1);
+            float e = o_bits_to_normal(o_bits_at(a0, a1, 1, 0));
+            float xs = xa[res ? anc[i] : i];
+            float xn = fmaf(xs, md->phi, e * md->bsig);
+            xb[i] = xn;
+            lb[i] = (res ? 0.0f : la[i]) - o_sv_potential(md, xn, y[t]);
+        }
+        o_lse_ess(lb, n, st);
+        logZ += st[1] - (res ? logn : lse_prev);
+        lse_prev = st[1];
+        ess_prev = (float)st[3];
+        if (ess_out) ess_out[t] = ess_prev;
+        if (resampled_out) resampled_out[t] = res;
+        float *tp = xa; xa = xb; xb = tp;
+        tp = la; la = lb; lb = tp;
+    }
+    free(tkeys);
+    free(xa); free(xb); free(la); free(lb); free(anc);
+    return logZ;
+}
+
+/* Many independent SV filters (the batched workload), each with its own
+ * (n_b, T_b, y_b, key_b); filters run in parallel across host threads. */
+void o_sv_batch(const o_sv_model *md, int64_t B, const int64_t *n, const int64_t *T, const int64_t *y_off,
+                const float *y, const uint32_t *keys, float ess_threshold, int scheme, double *logZ)
+{
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t b = 0; b < B; ++b)
+        logZ[b] = o_sv_run(md, n[b], T[b], keys + 2 * b, y + y_off[b], ess_threshold, scheme, NULL, NULL);
+}
+
+int o_num_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+void o_set_num_threads(int k)
+{
+#ifdef _OPENMP
+    omp_set_num_threads(k);
+#else
+    (void)k;
+#endif
+}

@@ -1,0 +1,124 @@
+"""GPU bootstrap particle filter (linear-Gaussian) vs the oracle and the Kalman filter.
+
+Bit-exact: particles, log-weights and ancestors (same float32 op sequence,
+integer resampling).  Float tolerance: log Z relative 1e-5 (float64
+reductions in different order), ESS relative 1e-5.
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle as O
+from oracle import kalman, models
+
+pytestmark = pytest.mark.gpu
+
+
+def _models(d, dy=None, seed=0, diag_r=True):
+    dy = dy or d
+    rng = np.random.default_rng(seed)
+    F = models.random_stable_matrix(d, seed)
+    Q = 0.1 * np.eye(d) + (0.02 * np.ones((d, d)) if d > 1 else 0)
+    H = np.eye(d) if dy == d else rng.standard_normal((dy, d)) / np.sqrt(d)
+    R = 0.5 * np.eye(dy) if diag_r else 0.5 * np.eye(dy) + 0.1 * np.ones((dy, dy))
+    S0 = np.eye(d)
+    p = models.lg_params(np.zeros(d), S0, F, Q, H, R)
+    import mocat_gb300 as mg
+    ssm = mg.ssm.TimeHomogenousLinearGaussian(np.zeros(d), S0, F, Q, H, R)
+    return p, ssm
+
+
+@pytest.mark.parametrize("d,dy", [(1, 1), (2, 1), (3, 3), (10, 10), (10, 1), (5, 5), (8, 8)])
+def test_init_and_step_bit_exact(cuda, d, dy):
+    import mocat_gb300 as mg
+    from mocat_gb300.ssm import _step
+    p, ssm = _models(d, dy, seed=d)
+    n = 3001
+    _, y = models.simulate_lg(p, 3, O.PRNGKey(0))
+    key = O.PRNGKey(1)
+    x0, lw0 = O.lg_init(p, n, key, y[0])
+    ip = mg.ssm.initiate_particles(ssm, mg.ssm.BootstrapFilter(), n, key, y[0])
+    assert np.array_equal(ip.value[0].cpu().numpy(), x0)
+    assert np.array_equal(ip.log_weight[0].cpu().numpy(), lw0)
+    _, s = ssm.derived()
+    kt = O.split(O.PRNGKey(2), 1)[0]
+    anc = np.sort(np.random.default_rng(0).integers(0, n, n)).astype(np.int32)
+    for a, lwp in ((None, lw0), (anc, None)):
+        xr, lr = O.lg_propagate(p, kt, y[1], x0, a, lwp)
+        xs = torch.from_numpy(np.ascontiguousarray(x0.T)).cuda()
+        xn, ln = _step(s, n, torch.from_numpy(kt.view(np.int32)).cuda().view(torch.uint32), torch.from_numpy(y[1]).cuda(),
+                       xs, None if a is None else torch.from_numpy(a).cuda(),
+                       None if lwp is None else torch.from_numpy(lwp).cuda())
+        assert np.array_equal(xn.t().cpu().numpy(), xr)
+        assert np.array_equal(ln.cpu().numpy(), lr)
+
+
+@pytest.mark.parametrize("scheme", ["systematic", "multinomial", "categorical"])
+@pytest.mark.parametrize("d", [1, 3, 10])
+def test_run_matches_oracle(cuda, scheme, d):
+    import mocat_gb300 as mg
+    p, ssm = _models(d, seed=10 + d)
+    T, n = 25, 1000 if scheme == "categorical" else 5003
+    _, y = models.simulate_lg(p, T, O.PRNGKey(0))
+    ref = O.lg_run(p, n, O.PRNGKey(3), y, ess_threshold=0.5, scheme=scheme, history=True)
+    out = mg.ssm.run_particle_filter_for_marginals(ssm, mg.ssm.BootstrapFilter(), y, np.arange(T), O.PRNGKey(3),
+                                                   n=n, ess_threshold=0.5, resampling=scheme)
+    assert np.array_equal(out.resampled.cpu().numpy(), ref["resampled"])
+    assert ref["resampled"].sum() >= 2
+    assert np.array_equal(out.value.cpu().numpy(), ref["value"])
+    assert np.array_equal(out.log_weight.cpu().numpy(), ref["log_weight"])
+    assert np.allclose(out.ess.cpu().numpy(), ref["ess"], rtol=1e-5)
+    assert abs(float(out.log_z) - ref["log_z"]) <= 1e-5 * abs(ref["log_z"])
+
+
+def test_config1_every_step_vs_kalman(cuda):
+    """1-D LG, F=0.9, Q=1, H=1, R=0.25, T=100, n=1000, systematic every step."""
+    import mocat_gb300 as mg
+    p = models.lg_params(np.zeros(1), np.eye(1), [[0.9]], np.eye(1), np.eye(1), [[0.25]])
+    ssm = mg.ssm.TimeHomogenousLinearGaussian(np.zeros(1), np.eye(1), [[0.9]], np.eye(1), np.eye(1), [[0.25]])
+    _, y = models.simulate_lg(p, 100, O.PRNGKey(0))
+    kl = kalman.loglik(p["F64"], p["Q"], p["H64"], p["R"], p["m064"], p["S0"], y)
+    ref = O.lg_run(p, 1000, O.PRNGKey(1), y, ess_threshold=2.0, scheme="systematic", history=True)
+    out = mg.ssm.run_particle_filter_for_marginals(ssm, mg.ssm.BootstrapFilter(), y, np.arange(100.0),
+                                                   mg.random.PRNGKey(1), n=1000, ess_threshold=2.0)
+    assert out.resampled.cpu().numpy()[1:].all()
+    assert np.array_equal(out.value.cpu().numpy(), ref["value"])
+    assert abs(float(out.log_z) - ref["log_z"]) <= 1e-5 * abs(ref["log_z"])
+    assert abs(float(out.log_z) - kl) < 1.5, (float(out.log_z), kl)
+
+
+def test_config2_full_size_vs_kalman(cuda):
+    """d=10, n=2^20, T=200 (of 1000), ESS-triggered systematic at 0.5 n: log Z vs Kalman,
+    a size-independent property (the estimator's error at this n is far below 1)."""
+    import mocat_gb300 as mg
+    d, T, n = 10, 200, 1 << 20
+    F = models.random_stable_matrix(d, 0)
+    p = models.lg_params(np.zeros(d), np.eye(d), F, 0.1 * np.eye(d), np.eye(d), 0.5 * np.eye(d))
+    ssm = mg.ssm.TimeHomogenousLinearGaussian(np.zeros(d), np.eye(d), F, 0.1 * np.eye(d), np.eye(d), 0.5 * np.eye(d))
+    _, y = models.simulate_lg(p, T, O.PRNGKey(0))
+    kl = kalman.loglik(p["F64"], p["Q"], p["H64"], p["R"], p["m064"], p["S0"], y)
+    out = mg.ssm.run_particle_filter_for_marginals(ssm, mg.ssm.BootstrapFilter(), y, np.arange(T),
+                                                   mg.random.PRNGKey(1), n=n, history=False)
+    lz = float(out.log_z)
+    assert abs(lz - kl) < 0.5, (lz, kl)
+    ess = out.ess.cpu().numpy()
+    assert (ess > 0).all() and (ess <= n * (1 + 1e-5)).all()
+    assert 0 < out.resampled.cpu().numpy().sum() < T
+
+
+def test_online_propagate_matches_run(cuda):
+    """propagate_particle_filter step by step reproduces run_particle_filter_for_marginals."""
+    import mocat_gb300 as mg
+    p, ssm = _models(2, 1, seed=4)
+    T, n = 8, 777
+    _, y = models.simulate_lg(p, T, O.PRNGKey(0))
+    full = mg.ssm.run_particle_filter_for_marginals(ssm, mg.ssm.BootstrapFilter(), y, np.arange(T),
+                                                    O.PRNGKey(5), n=n, ess_threshold=0.9)
+    keys = O.split(O.PRNGKey(5))
+    parts = mg.ssm.initiate_particles(ssm, mg.ssm.BootstrapFilter(), n, keys[1], y[0], 0.0)
+    step_keys = O.split(keys[0], T - 1)
+    for t in range(1, T):
+        parts = mg.ssm.propagate_particle_filter(ssm, mg.ssm.BootstrapFilter(), parts, y[t], float(t),
+                                                 step_keys[t - 1], ess_threshold=0.9)
+    assert np.array_equal(parts.value.cpu().numpy(), full.value.cpu().numpy())
+    assert np.allclose(parts.ess.cpu().numpy(), full.ess.cpu().numpy(), rtol=1e-5)
