@@ -107,7 +107,8 @@ def test_config2_full_size_vs_kalman(cuda):
 
 
 def test_online_propagate_matches_run(cuda):
-    """propagate_particle_filter step by step reproduces run_particle_filter_for_marginals."""
+    """propagate_particle_filter step by step reproduces run_particle_filter_for_marginals at the
+    latest step (resample_full=True also resamples the stored path history, filtering.py:210-212)."""
     import mocat_gb300 as mg
     p, ssm = _models(2, 1, seed=4)
     T, n = 8, 777
@@ -120,5 +121,6 @@ def test_online_propagate_matches_run(cuda):
     for t in range(1, T):
         parts = mg.ssm.propagate_particle_filter(ssm, mg.ssm.BootstrapFilter(), parts, y[t], float(t),
                                                  step_keys[t - 1], ess_threshold=0.9)
-    assert np.array_equal(parts.value.cpu().numpy(), full.value.cpu().numpy())
+    assert np.array_equal(parts.value[-1].cpu().numpy(), full.value[-1].cpu().numpy())
+    assert np.array_equal(parts.log_weight[-1].cpu().numpy(), full.log_weight[-1].cpu().numpy())
     assert np.allclose(parts.ess.cpu().numpy(), full.ess.cpu().numpy(), rtol=1e-5)
