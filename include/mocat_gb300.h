@@ -21,7 +21,8 @@
  *     word the caller passes (err_dev, may be NULL): bit 1 = a bounded wait
  *     ran out, bit 2 = every weight was zero / non-finite.
  * Thread-safety: calls on different streams with different workspaces are
- * independent; the library has no global mutable state.
+ * independent; the only global mutable state is the fixed scratch array of
+ * mgb_resample_systematic_u_noalloc.
  */
 #ifndef MOCAT_GB300_H
 #define MOCAT_GB300_H
@@ -92,6 +93,20 @@ int mgb_resample(const float *lw_dev, int64_t n, int scheme, const uint32_t *key
 /* systematic with the uniform fed in as its 23-bit mantissa: u = m23 * 2^-23 */
 int mgb_resample_systematic_u(const float *lw_dev, int64_t n, uint32_t m23, int32_t *ancestors_dev, void *ws_dev,
                               size_t ws_bytes, int32_t *err_dev, void *stream);
+
+/* Systematic resampling that allocates nothing.  No counterpart in the
+ * reference: it is for callers that cannot allocate device memory (an XLA
+ * custom call or framework-built CUDA-graph node handed only its buffers, a
+ * plugin inside a process whose allocator owns the device heap).  Same result
+ * as mgb_resample_systematic_u; the scratch lives in a fixed device array
+ * inside the library (256 KiB, resident on each device that loads it until
+ * exit), so n must not exceed MGB_NOALLOC_MAX_N (else MGB_ERR_UNSUPPORTED).
+ * The first call on a device looks up that array's address: make it before
+ * any stream capture.  Calls share the array; calls that overlap on the GPU
+ * race on it. */
+#define MGB_NOALLOC_MAX_N (1 << 24)
+int mgb_resample_systematic_u_noalloc(const float *lw_dev, int64_t n, uint32_t m23, int32_t *ancestors_dev,
+                                      int32_t *err_dev, void *stream);
 
 /* ---------------------------------------------------------------- gather
  * Replaces the fancy-index gathers x[..., idx, :] (mocat/src/ssm/filtering.py:199)

@@ -52,6 +52,7 @@ _SIGNATURES = {
     "mgb_resample_workspace": ([_I64, _I32], _SZ),
     "mgb_resample": ([_P, _I64, _I32, _P, _P, _P, _SZ, _P, _P], _I32),
     "mgb_resample_systematic_u": ([_P, _I64, ctypes.c_uint32, _P, _P, _SZ, _P, _P], _I32),
+    "mgb_resample_systematic_u_noalloc": ([_P, _I64, ctypes.c_uint32, _P, _P, _P], _I32),
     "mgb_gather_rows": ([_P, _I64, _P, _I64, _P, _P], _I32),
     "mgb_pf_lg_init": ([ctypes.POINTER(LGModel), _I64, _P, _P, _P, _P, _P], _I32),
     "mgb_pf_lg_propagate": ([ctypes.POINTER(LGModel), _I64, _P, _P, _P, _P, _P, _P, _P, _P], _I32),
