@@ -192,7 +192,7 @@ def main():
     xf = torch.empty((D, n), dtype=torch.float32, device=dev)
     lf = torch.empty(n, dtype=torch.float32, device=dev)
     out = _lib.PFOutputs(logz.data_ptr(), ess.data_ptr(), res.data_ptr(), None, None, xf.data_ptr(), lf.data_ptr(),
-                         err.data_ptr())
+                         err.data_ptr(), None)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
 
     def enqueue():

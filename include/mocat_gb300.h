@@ -154,10 +154,19 @@ typedef struct {
   float *x_final;     /* (d, n) final particles */
   float *lw_final;    /* (n,) final log-weights */
   int32_t *err;       /* device error word */
+  uint64_t *trace;    /* (T * 10 + 2048) diagnostics of the persistent kernel (NULL = off):
+                         [t * 10 + k] device-clock ns at the phase boundaries of step t seen by
+                         block 0 (start, propagate done, barrier, combine done, tile sums done,
+                         barrier, fill set-up done, fill done, barrier); [T * 10 + b] ns block b
+                         spent propagating step 1 */
 } mgb_pf_outputs;
 
 /* run_particle_filter_for_marginals (mocat/src/ssm/filtering.py:255-324) with
- * ESS-triggered resampling (resample at t when ess_{t-1} < ess_threshold * n). */
+ * ESS-triggered resampling (resample at t when ess_{t-1} < ess_threshold * n).
+ * Systematic resampling with even n <= 2^21 runs as one persistent cooperative
+ * kernel for all T steps; OR-ing MGB_RUN_LAUNCH_PER_STEP into `scheme` forces
+ * the launch-per-step path (same results). */
+#define MGB_RUN_LAUNCH_PER_STEP 0x100
 size_t mgb_pf_lg_workspace(int64_t n, int64_t T, int32_t d, int scheme);
 int mgb_pf_lg_run(const mgb_lg_model *model_host, int64_t n, int64_t T, const uint32_t *key_dev, const float *y_dev,
                   float ess_threshold, int scheme, void *ws_dev, size_t ws_bytes, const mgb_pf_outputs *out,

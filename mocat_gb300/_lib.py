@@ -27,7 +27,7 @@ class LGModel(ctypes.Structure):
 class PFOutputs(ctypes.Structure):
     _fields_ = [("log_z", ctypes.c_void_p), ("ess", ctypes.c_void_p), ("resampled", ctypes.c_void_p),
                 ("x_hist", ctypes.c_void_p), ("lw_hist", ctypes.c_void_p), ("x_final", ctypes.c_void_p),
-                ("lw_final", ctypes.c_void_p), ("err", ctypes.c_void_p)]
+                ("lw_final", ctypes.c_void_p), ("err", ctypes.c_void_p), ("trace", ctypes.c_void_p)]
 
 
 _P = ctypes.c_void_p

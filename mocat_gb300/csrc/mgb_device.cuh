@@ -36,7 +36,13 @@ enum Status : int {
 enum ErrBits : int { EB_TIMEOUT = 1, EB_DEGENERATE = 2 };
 
 // ------------------------------------------------------------ threefry2x32
-MGB_HD uint32_t rotl32(uint32_t v, int r) { return (v << r) | (v >> (32 - r)); }
+MGB_HD uint32_t rotl32(uint32_t v, int r) {
+#ifdef __CUDA_ARCH__
+  return __funnelshift_l(v, v, r);
+#else
+  return (v << r) | (v >> (32 - r));
+#endif
+}
 
 MGB_HD void threefry2x32(uint32_t k0, uint32_t k1, uint32_t c0, uint32_t c1, uint32_t &r0, uint32_t &r1) {
   const uint32_t k2 = k0 ^ k1 ^ 0x1BD11BDAu;
@@ -52,6 +58,34 @@ MGB_HD void threefry2x32(uint32_t k0, uint32_t k1, uint32_t c0, uint32_t c1, uin
 #undef MGB_TF_G1
 #undef MGB_TF_G0
 #undef MGB_TF_ROUND
+  r0 = x0;
+  r1 = x1;
+}
+
+// Device variant with the 32-bit additions issued as multiply-adds by a
+// runtime `one` (== 1, read from kernel parameters so it cannot be folded):
+// integer add / xor / funnel-shift all compete for the integer ALU pipe, while
+// IMAD issues to the FMA pipe.  Same values as threefry2x32.
+__device__ __forceinline__ uint32_t madd(uint32_t a, uint32_t one, uint32_t b) {
+  uint32_t r;
+  asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(one), "r"(b));
+  return r;
+}
+__device__ __forceinline__ void threefry2x32_m(uint32_t k0, uint32_t k1, uint32_t c0, uint32_t c1, uint32_t one,
+                                               uint32_t &r0, uint32_t &r1) {
+  const uint32_t k2 = k0 ^ k1 ^ 0x1BD11BDAu;
+  uint32_t x0 = madd(c0, one, k0), x1 = madd(c1, one, k1);
+#define MGB_TFM_ROUND(R) { x0 = madd(x1, one, x0); x1 = rotl32(x1, R); x1 ^= x0; }
+#define MGB_TFM_G0 MGB_TFM_ROUND(13) MGB_TFM_ROUND(15) MGB_TFM_ROUND(26) MGB_TFM_ROUND(6)
+#define MGB_TFM_G1 MGB_TFM_ROUND(17) MGB_TFM_ROUND(29) MGB_TFM_ROUND(16) MGB_TFM_ROUND(24)
+  MGB_TFM_G0 x0 = madd(k1, one, x0); x1 = madd(k2 + 1u, one, x1);
+  MGB_TFM_G1 x0 = madd(k2, one, x0); x1 = madd(k0 + 2u, one, x1);
+  MGB_TFM_G0 x0 = madd(k0, one, x0); x1 = madd(k1 + 3u, one, x1);
+  MGB_TFM_G1 x0 = madd(k1, one, x0); x1 = madd(k2 + 4u, one, x1);
+  MGB_TFM_G0 x0 = madd(k2, one, x0); x1 = madd(k0 + 5u, one, x1);
+#undef MGB_TFM_G1
+#undef MGB_TFM_G0
+#undef MGB_TFM_ROUND
   r0 = x0;
   r1 = x1;
 }
@@ -78,12 +112,12 @@ MGB_HD void split_at(uint32_t k0, uint32_t k1, uint64_t num, uint64_t i, uint32_
 
 // random_bits(key, (D,)) for a compile-time D: ceil(D/2) cipher calls
 template <int D>
-__device__ __forceinline__ void bits_vec(uint32_t k0, uint32_t k1, uint32_t (&b)[D]) {
+__device__ __forceinline__ void bits_vec(uint32_t k0, uint32_t k1, uint32_t (&b)[D], uint32_t one = 1u) {
   constexpr int H = (D + 1) / 2;
 #pragma unroll
   for (int j = 0; j < H; ++j) {
     uint32_t r0, r1;
-    threefry2x32(k0, k1, (uint32_t)j, (j + H < D) ? (uint32_t)(j + H) : 0u, r0, r1);
+    threefry2x32_m(k0, k1, (uint32_t)j, (j + H < D) ? (uint32_t)(j + H) : 0u, one, r0, r1);
     b[j] = r0;
     if (j + H < D) b[j + H] = r1;
   }
@@ -165,10 +199,12 @@ __device__ __forceinline__ float erfinv_(float x) {
 
 __device__ __forceinline__ float bits_to_unit(uint32_t b) { return __fsub_rn(asf((b >> 9) | 0x3f800000u), 1.0f); }
 
-// jax.random.normal from raw bits: u = max(lo, 2 f + lo), sqrt(2) erfinv(u)
+// jax.random.normal from raw bits: u = max(lo, 2 f + lo), sqrt(2) erfinv(u).
+// 2 f is exact, so one fused rounding of 2 f + lo equals jax's two-step
+// rounding, and u >= lo always (f >= 0), so the max is the identity.
 __device__ __forceinline__ float bits_to_normal(uint32_t b) {
   const float lo = -0x1.fffffep-1f;
-  const float u = fmaxf(__fadd_rn(__fmul_rn(bits_to_unit(b), 2.0f), lo), lo);
+  const float u = __fmaf_rn(bits_to_unit(b), 2.0f, lo);
   return __fmul_rn(0x1.6a09e6p+0f, erfinv_(u));
 }
 
@@ -193,8 +229,16 @@ MGB_HD int weight_shift(int64_t n) { return 61 - ceil_log2_u64((uint64_t)n); }
 // exponential spacings (< 16) quantised with 2^exp_shift(n) over n + 1 draws: total < 2^60
 MGB_HD int exp_shift(int64_t n) { return 56 - ceil_log2_u64((uint64_t)n + 1); }
 
+// trunc(expf(lw - M) * 2^S) from the float's bits (integer ops only; equals
+// __float2ull_rz of the exactly scaled value).  `scale` is 2^S.
 __device__ __forceinline__ uint64_t quantise_weight(float lw, float M, float scale) {
-  return __float2ull_rz(__fmul_rn(expf_(__fsub_rn(lw, M)), scale));
+  const uint32_t b = __float_as_uint(expf_(__fsub_rn(lw, M)));
+  const int ex = (int)((b >> 23) & 0xffu);
+  if (ex == 0 || ex == 255 || (b >> 31)) return 0ull;  // zero / subnormal, NaN / inf, negative
+  const int S = (int)((__float_as_uint(scale) >> 23) & 0xffu) - 127;
+  const uint64_t mant = (uint64_t)((b & 0x007fffffu) | 0x00800000u);
+  const int sh = ex - 150 + S;
+  return sh >= 0 ? (mant << sh) : (sh > -64 ? (mant >> -sh) : 0ull);
 }
 
 // 128-bit product comparison a*b <= c*d (all < 2^64)

@@ -27,36 +27,10 @@
 #include "mgb_internal.cuh"
 #include "mgb_resample.cuh"
 #include "mgb_kernels.cuh"
+#include "mgb_lg.cuh"
+#include "mgb_persist.cuh"
 
 namespace mgb {
-
-template <int D, int DY>
-struct LGP {
-  float F[D * D], Lq[D * D], H[DY * D], P[DY * DY], C0[D * D], m0[D];
-  float c;
-};
-
-struct PFState {
-  double logz;
-  double lse_prev;
-  float M;
-  int pad;
-};
-
-// per-run control block passed by value to the fused kernels
-struct PFCtl {
-  LsePartial *parts;
-  unsigned int *counter;
-  PFState *st;
-  float *ess_hist;     // (T,)
-  int32_t *res_hist;   // (T+1,): entry t = 1 if step t resamples
-  ResampleCtl *rctl;   // cleared by the finalising block for the next step
-  uint64_t *rstatus, *rstatus2;
-  int ntiles;
-  float thr_n;         // ess_threshold * n (float32, as the reference compares)
-  double logn;
-  double *logz_out;
-};
 
 constexpr int PF_TPB = 256;
 
@@ -84,37 +58,7 @@ __device__ __forceinline__ void pf_finalize(const PFCtl &ctl, int64_t t, float *
     ctl.rstatus[j] = 0ull;
     ctl.rstatus2[j] = 0ull;
   }
-}
-
-template <int D, int DY>
-__device__ __forceinline__ float lg_potential(const LGP<D, DY> &p, const float (&x)[D], const float (&y)[DY]) {
-  float diff[DY];
-#pragma unroll
-  for (int j = 0; j < DY; ++j) {
-    float hx = __fmul_rn(p.H[j * D], x[0]);
-#pragma unroll
-    for (int k = 1; k < D; ++k) hx = __fmaf_rn(p.H[j * D + k], x[k], hx);
-    diff[j] = __fsub_rn(y[j], hx);
-  }
-  float quad = 0.0f;
-#pragma unroll
-  for (int k = 0; k < DY; ++k) {
-    float v = __fmul_rn(diff[0], p.P[k]);
-#pragma unroll
-    for (int j = 1; j < DY; ++j) v = __fmaf_rn(diff[j], p.P[j * DY + k], v);
-    quad = k == 0 ? __fmul_rn(v, v) : __fmaf_rn(v, v, quad);
-  }
-  return __fadd_rn(__fmul_rn(0.5f, quad), p.c);
-}
-
-template <int D>
-__device__ __forceinline__ void particle_normals(uint32_t k0, uint32_t k1, int64_t n, int64_t i, float (&e)[D]) {
-  uint32_t a0, a1;
-  split_at(k0, k1, (uint64_t)n, (uint64_t)i, a0, a1);
-  uint32_t b[D];
-  bits_vec<D>(a0, a1, b);
-#pragma unroll
-  for (int j = 0; j < D; ++j) e[j] = bits_to_normal(b[j]);
+  if (threadIdx.x == 0) ctl.rctl->units = 0u;
 }
 
 // block partial + (optionally) last-block finalize
@@ -143,9 +87,9 @@ __global__ void __launch_bounds__(PF_TPB) k_lg_init(const __grid_constant__ LGP<
                                                      float *__restrict__ lw, PFCtl ctl) {
   const int64_t i = blockIdx.x * (int64_t)PF_TPB + threadIdx.x;
   const uint32_t k0 = key[0], k1 = key[1];
-  float y[DY];
-#pragma unroll
-  for (int j = 0; j < DY; ++j) y[j] = y0 ? y0[j] : 0.0f;
+  __shared__ float y[DY];
+  if (threadIdx.x < DY) y[threadIdx.x] = y0 ? y0[threadIdx.x] : 0.0f;
+  __syncthreads();
   float l = -INFINITY;
   const bool active = i < n;
   if (active) {
@@ -176,9 +120,9 @@ __global__ void __launch_bounds__(PF_TPB) k_lg_step(const __grid_constant__ LGP<
   const int64_t i = blockIdx.x * (int64_t)PF_TPB + threadIdx.x;
   const bool res = res_flag ? (*res_flag != 0) : (anc != nullptr);
   const uint32_t k0 = key[0], k1 = key[1];
-  float y[DY];
-#pragma unroll
-  for (int j = 0; j < DY; ++j) y[j] = y_t[j];
+  __shared__ float y[DY];
+  if (threadIdx.x < DY) y[threadIdx.x] = y_t[threadIdx.x];
+  __syncthreads();
   float l = -INFINITY;
   const bool active = i < n;
   if (active) {
@@ -187,17 +131,9 @@ __global__ void __launch_bounds__(PF_TPB) k_lg_step(const __grid_constant__ LGP<
     const int64_t src = res ? (int64_t)anc[i] : i;
 #pragma unroll
     for (int j = 0; j < D; ++j) xs[j] = __ldg(&x_prev[j * n + src]);
+    lg_transition<D, DY>(p, xs, e, xn);
 #pragma unroll
-    for (int r = 0; r < D; ++r) {
-      float fx = __fmul_rn(p.F[r * D], xs[0]);
-#pragma unroll
-      for (int k = 1; k < D; ++k) fx = __fmaf_rn(p.F[r * D + k], xs[k], fx);
-      float le = __fmul_rn(p.Lq[r * D], e[0]);
-#pragma unroll
-      for (int k = 1; k < D; ++k) le = __fmaf_rn(p.Lq[r * D + k], e[k], le);
-      xn[r] = __fadd_rn(fx, le);
-      x_new[r * n + i] = xn[r];
-    }
+    for (int r = 0; r < D; ++r) x_new[r * n + i] = xn[r];
     // run mode (res_flag set): lw_res = 0 after a resample (filtering.py:292);
     // standalone mode: lw_prev as given (NULL = 0)
     const float *lws = res_flag ? (res ? nullptr : lw_prev) : lw_prev;
@@ -206,6 +142,59 @@ __global__ void __launch_bounds__(PF_TPB) k_lg_step(const __grid_constant__ LGP<
     lw_new[i] = l;
   }
   if (FUSED) pf_reduce<PF_TPB>(l, active, ctl, t);
+}
+
+// Two particles per thread, i and i + n/2 (n even).  In jax's split layout the
+// key of particle i is (T(2i, 2i+n).x0, T(2i+1, 2i+1+n).x0) and the key of
+// particle i + n/2 is the .x1 halves of the same two cipher calls, so the
+// pair costs two key-split evaluations instead of four.
+template <int TPB>
+__device__ __forceinline__ void pf_reduce_online(float m, float s1, float s2, int nanf, const PFCtl &ctl, int64_t t) {
+  __shared__ float smf[TPB / 32];
+  __shared__ double smd[TPB / 32];
+  __shared__ bool last;
+  const LsePartial part = block_online_partial<TPB>(m, s1, s2, nanf, smf);
+  if (threadIdx.x == 0) {
+    ctl.parts[blockIdx.x] = part;
+    __threadfence();
+    last = atomicAdd(ctl.counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  pf_finalize<TPB>(ctl, t, smf, smd);
+}
+
+template <int D, int DY, bool FUSED>
+__global__ void __launch_bounds__(PF_TPB, 2) k_lg_step2(const __grid_constant__ LGP<D, DY> p, int64_t n,
+                                                         const uint32_t *key, const float *y_t,
+                                                         const float *__restrict__ x_prev, const int32_t *anc,
+                                                         const float *lw_prev, const int32_t *res_flag,
+                                                         float *__restrict__ x_new, float *__restrict__ lw_new,
+                                                         PFCtl ctl, int64_t t) {
+  const int64_t h = n >> 1;
+  const int64_t i = blockIdx.x * (int64_t)PF_TPB + threadIdx.x;
+  const bool res = res_flag ? (*res_flag != 0) : (anc != nullptr);
+  const float *lws = res_flag ? (res ? nullptr : lw_prev) : lw_prev;
+  const uint32_t k0 = key[0], k1 = key[1];
+  __shared__ float y[DY];
+  if (threadIdx.x < DY) y[threadIdx.x] = y_t[threadIdx.x];
+  __syncthreads();
+  float m = -INFINITY, a1 = 0.0f, a2 = 0.0f;
+  int nanf = 0;
+  if (i < h) {
+    uint32_t r0, r1, s0, s1;
+    threefry2x32_m(k0, k1, (uint32_t)(2 * i), (uint32_t)(2 * i + n), p.one, r0, r1);
+    threefry2x32_m(k0, k1, (uint32_t)(2 * i + 1), (uint32_t)(2 * i + 1 + n), p.one, s0, s1);
+    // two-trip loop, not unrolled: one copy of the particle code (instruction cache)
+#pragma unroll 1
+    for (int s = 0; s < 2; ++s) {
+      const float l = lg_particle<D, DY>(p, n, s ? r1 : r0, s ? s1 : s0, s ? i + h : i, res, x_prev, anc, lws, y,
+                                         x_new, lw_new);
+      online_acc(l, m, a1, a2, nanf);
+    }
+  }
+  if (FUSED) pf_reduce_online<PF_TPB>(m, a1, a2, nanf, ctl, t);
 }
 
 // key schedule of run_particle_filter_for_marginals: (random_key, sub_key) =
@@ -236,21 +225,6 @@ __global__ void k_finish(const PFState *st, const int32_t *res_hist, int64_t T, 
 }
 
 // ------------------------------------------------------------- host side
-template <int D, int DY>
-static LGP<D, DY> pack_lg(const mgb_lg_model *m) {
-  LGP<D, DY> p;
-  for (int i = 0; i < D * D; ++i) {
-    p.F[i] = m->F[i];
-    p.Lq[i] = m->Lq[i];
-    p.C0[i] = m->C0[i];
-  }
-  for (int i = 0; i < DY * D; ++i) p.H[i] = m->H[i];
-  for (int i = 0; i < DY * DY; ++i) p.P[i] = m->P[i];
-  for (int i = 0; i < D; ++i) p.m0[i] = m->m0[i];
-  p.c = m->c;
-  return p;
-}
-
 struct RunWs {
   uint32_t *keys;
   PFState *st;
@@ -280,13 +254,43 @@ static RunWs carve_run(Carver &c, int64_t n, int64_t T, int d, int scheme, bool 
   return w;
 }
 
+// Persistent path: systematic resampling, even n, n <= 2^21 (tile prefixes in smem).
+static bool persistent_ok(int64_t n, int scheme) {
+  return scheme == MGB_RESAMPLE_SYSTEMATIC && n % 2 == 0 && (n + SCAN_TILE - 1) / SCAN_TILE <= PP_MAX_TILES;
+}
+
+struct PersistWs {
+  LsePartial *parts;
+  int *chunk_ctr;
+  uint64_t *cloc;
+  uint64_t *tile_sum;
+  int *degen;
+  GridBar *bar;
+  int32_t *res;
+  int *err;
+};
+static PersistWs carve_persist(Carver &c, int64_t n, int64_t T) {
+  PersistWs w;
+  w.parts = c.take<LsePartial>(2 * PP_MAX_CHUNKS);
+  w.chunk_ctr = c.take<int>((size_t)T);
+  w.cloc = c.take<uint64_t>((size_t)n);
+  w.tile_sum = c.take<uint64_t>((size_t)((n + SCAN_TILE - 1) / SCAN_TILE));
+  w.degen = c.take<int>((size_t)T);
+  w.bar = c.take<GridBar>(1);
+  w.res = c.take<int32_t>((size_t)T);
+  w.err = c.take<int>(1);
+  return w;
+}
+
 template <int D, int DY>
 static int run_lg(const mgb_lg_model *m, int64_t n, int64_t T, const uint32_t *key, const float *y, float thr,
-                  int scheme, void *ws, size_t ws_bytes, const mgb_pf_outputs *out, cudaStream_t s) {
+                  int scheme, bool persistent, void *ws, size_t ws_bytes, const mgb_pf_outputs *out,
+                  cudaStream_t s) {
   const LGP<D, DY> p = pack_lg<D, DY>(m);
   const bool hx = out && out->x_hist, hl = out && out->lw_hist;
   Carver c(ws);
   RunWs w = carve_run(c, n, T, D, scheme, !hx, !hl, !(out && out->ess));
+  PersistWs pw = carve_persist(c, n, T);
   if (c.bytes() > ws_bytes) return ERR_WORKSPACE;
   float *ess = (out && out->ess) ? out->ess : w.ess_hist;
   int *err = out ? out->err : nullptr;
@@ -296,6 +300,50 @@ static int run_lg(const mgb_lg_model *m, int64_t n, int64_t T, const uint32_t *k
   int st = reset_resample(w.rws, s);
   if (st) return st;
   k_setup_keys<<<grid_for(T, 256), 256, 0, s>>>(key, T, w.keys);
+
+  if (persistent && persistent_ok(n, scheme)) {
+    if (cudaMemsetAsync(pw.degen, 0, sizeof(int) * T, s) != cudaSuccess) return ERR_CUDA;
+    if (cudaMemsetAsync(pw.bar, 0, sizeof(GridBar), s) != cudaSuccess) return ERR_CUDA;
+    if (cudaMemsetAsync(pw.err, 0, sizeof(int), s) != cudaSuccess) return ERR_CUDA;
+    if (cudaMemsetAsync(pw.chunk_ctr, 0, sizeof(int) * T, s) != cudaSuccess) return ERR_CUDA;
+    PersistArgs a;
+    a.n = n;
+    a.T = T;
+    a.keys = w.keys;
+    a.y = y;
+    a.thr_n = thr * (float)n;
+    a.logn = log((double)n);
+    a.xa = w.xa;
+    a.xb = w.xb;
+    a.la = w.la;
+    a.lb = w.lb;
+    a.x_hist = hx ? out->x_hist : nullptr;
+    a.lw_hist = hl ? out->lw_hist : nullptr;
+    a.anc = w.anc;
+    a.parts = pw.parts;
+    a.chunk_ctr = pw.chunk_ctr;
+    a.cloc = pw.cloc;
+    a.tile_sum = pw.tile_sum;
+    a.degen = pw.degen;
+    a.bar = pw.bar;
+    a.ess = ess;
+    a.res = (out && out->resampled) ? out->resampled : pw.res;
+    a.logz = out ? out->log_z : nullptr;
+    a.err = pw.err;
+    a.user_err = err;
+    a.magic = ~0ull / (unsigned long long)n;
+    a.trace = out ? out->trace : nullptr;
+    if ((st = run_lg_persistent(m, a, s))) return st;
+    const float *xl = hx ? out->x_hist + (size_t)(T - 1) * D * n : ((T - 1) & 1 ? w.xb : w.xa);
+    const float *ll = hl ? out->lw_hist + (size_t)(T - 1) * n : ((T - 1) & 1 ? w.lb : w.la);
+    if (out && out->x_final &&
+        cudaMemcpyAsync(out->x_final, xl, sizeof(float) * D * n, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+      return ERR_CUDA;
+    if (out && out->lw_final &&
+        cudaMemcpyAsync(out->lw_final, ll, sizeof(float) * n, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+      return ERR_CUDA;
+    return launch_status();
+  }
 
   PFCtl ctl;
   ctl.parts = w.parts;
@@ -312,6 +360,7 @@ static int run_lg(const mgb_lg_model *m, int64_t n, int64_t T, const uint32_t *k
   ctl.logz_out = nullptr;
 
   const unsigned grid = (unsigned)((n + PF_TPB - 1) / PF_TPB);
+  const unsigned grid2 = (unsigned)((n / 2 + PF_TPB - 1) / PF_TPB);
   auto xbuf = [&](int64_t t) -> float * { return hx ? out->x_hist + (size_t)t * D * n : (t & 1 ? w.xb : w.xa); };
   auto lbuf = [&](int64_t t) -> float * { return hl ? out->lw_hist + (size_t)t * n : (t & 1 ? w.lb : w.la); };
   k_lg_init<D, DY, true><<<grid, PF_TPB, 0, s>>>(p, n, w.keys, y, xbuf(0), lbuf(0), ctl);
@@ -320,8 +369,12 @@ static int run_lg(const mgb_lg_model *m, int64_t n, int64_t T, const uint32_t *k
     st = launch_resample(lbuf(t - 1), n, scheme, &w.st->M, w.keys + 2 * t, 0, 0u, w.res_hist + t, w.rws, w.anc,
                          err, s);
     if (st) return st;
-    k_lg_step<D, DY, true><<<grid, PF_TPB, 0, s>>>(p, n, w.keys + 2 * t, y + (size_t)t * DY, xbuf(t - 1), w.anc,
-                                                    lbuf(t - 1), w.res_hist + t, xbuf(t), lbuf(t), ctl, t);
+    if (n % 2 == 0)
+      k_lg_step2<D, DY, true><<<grid2, PF_TPB, 0, s>>>(p, n, w.keys + 2 * t, y + (size_t)t * DY, xbuf(t - 1),
+                                                        w.anc, lbuf(t - 1), w.res_hist + t, xbuf(t), lbuf(t), ctl, t);
+    else
+      k_lg_step<D, DY, true><<<grid, PF_TPB, 0, s>>>(p, n, w.keys + 2 * t, y + (size_t)t * DY, xbuf(t - 1), w.anc,
+                                                      lbuf(t - 1), w.res_hist + t, xbuf(t), lbuf(t), ctl, t);
     if ((st = launch_status())) return st;
   }
   k_finish<<<grid_for(T, 256), 256, 0, s>>>(w.st, w.res_hist, T, out ? out->log_z : nullptr,
@@ -349,8 +402,12 @@ static int step_lg(const mgb_lg_model *m, int64_t n, const uint32_t *key, const 
                    const int32_t *anc, const float *lwp, float *xn, float *lwn, cudaStream_t s) {
   const LGP<D, DY> p = pack_lg<D, DY>(m);
   PFCtl ctl{};
-  k_lg_step<D, DY, false><<<(unsigned)((n + PF_TPB - 1) / PF_TPB), PF_TPB, 0, s>>>(p, n, key, y, xp, anc, lwp,
-                                                                                    nullptr, xn, lwn, ctl, 0);
+  if (n % 2 == 0)
+    k_lg_step2<D, DY, false><<<(unsigned)((n / 2 + PF_TPB - 1) / PF_TPB), PF_TPB, 0, s>>>(p, n, key, y, xp, anc, lwp,
+                                                                                          nullptr, xn, lwn, ctl, 0);
+  else
+    k_lg_step<D, DY, false><<<(unsigned)((n + PF_TPB - 1) / PF_TPB), PF_TPB, 0, s>>>(p, n, key, y, xp, anc, lwp,
+                                                                                      nullptr, xn, lwn, ctl, 0);
   return launch_status();
 }
 
@@ -395,7 +452,8 @@ extern "C" {
 
 size_t mgb_pf_lg_workspace(int64_t n, int64_t T, int32_t d, int scheme) {
   Carver c(nullptr);
-  carve_run(c, n, T < 1 ? 1 : T, d, scheme, true, true, true);
+  carve_run(c, n, T < 1 ? 1 : T, d, scheme & 0xff, true, true, true);
+  carve_persist(c, n, T < 1 ? 1 : T);
   return c.bytes();
 }
 
@@ -414,10 +472,12 @@ int mgb_pf_lg_propagate(const mgb_lg_model *m, int64_t n, const uint32_t *key, c
 int mgb_pf_lg_run(const mgb_lg_model *m, int64_t n, int64_t T, const uint32_t *key, const float *y, float thr,
                   int scheme, void *ws, size_t ws_bytes, const mgb_pf_outputs *out, void *stream) {
   if (!lg_model_ok(m) || n < 1 || n > 0x7FFFFFFFll || T < 1 || !key || !y || !ws) return ERR_BAD_ARG;
+  const bool persistent = !(scheme & MGB_RUN_LAUNCH_PER_STEP);
+  scheme &= ~MGB_RUN_LAUNCH_PER_STEP;
   if (scheme < 0 || scheme > 2) return ERR_BAD_ARG;
   if (scheme == MGB_RESAMPLE_CATEGORICAL && n > 46340) return ERR_UNSUPPORTED;
   if (ws_bytes < mgb_pf_lg_workspace(n, T, m->d, scheme)) return ERR_WORKSPACE;
-  MGB_LG_DISPATCH(run_lg, m, n, T, key, y, thr, scheme, ws, ws_bytes, out, (cudaStream_t)stream);
+  MGB_LG_DISPATCH(run_lg, m, n, T, key, y, thr, scheme, persistent, ws, ws_bytes, out, (cudaStream_t)stream);
 }
 
 }  // extern "C"

@@ -1,0 +1,400 @@
+// Whole-filter persistent kernel: the bootstrap linear-Gaussian particle
+// filter with ESS-triggered systematic resampling, all T steps in one
+// cooperative launch (one CTA group resident on every SM).
+//
+// Per step the grid runs
+//   P1  propagate + weight, two particles per thread (i, i + n/2), grid-stride;
+//       each block folds its log-weights into an online (max, sum e, sum e^2)
+//       partial                                                  -> barrier
+//   P2  every block combines all partials identically (same data, same order,
+//       so every block reaches the same logsumexp / ESS / resample decision);
+//       block 0 records ESS, the resample flag and log Z
+//   and, when the next step resamples,
+//   P3  exact fixed-point tile sums of the new log-weights           -> barrier
+//   P4  every block scans the tile sums in shared memory, places each tile's
+//       output range, cuts it into units of <= 2048 outputs and fills the
+//       units assigned to it (grid-stride)                           -> barrier
+// A non-resampling step costs one grid barrier, a resampling step three; no
+// kernel launches, no host round trips.  Data written inside the kernel is
+// read back through L2 (__ldcg): L1 is not coherent across SMs.  The grid
+// barrier is a sense-reversing counter with a bounded wait (on expiry the
+// error word gets EB_TIMEOUT and the kernel runs to completion).
+//
+// Results are identical to the multi-kernel path (same float op sequence per
+// particle, integer resampling); only the float64 LSE reduction is grouped
+// differently.
+#include "mgb_internal.cuh"
+#include "mgb_kernels.cuh"
+#include "mgb_lg.cuh"
+#include "mgb_persist.cuh"
+
+namespace mgb {
+
+// err is the kernel's own (never null) error word: once a wait has run out,
+// later barriers stop waiting and the step loop exits, so a fault can cost at
+// most one bounded wait.
+__device__ __forceinline__ void grid_sync(GridBar *bar, unsigned nblocks, int *err) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned int *vgen = &bar->gen;
+    const unsigned int g = *vgen;
+    __threadfence();
+    if (atomicAdd(&bar->count, 1u) == nblocks - 1) {
+      bar->count = 0u;
+      __threadfence();
+      atomicAdd(&bar->gen, 1u);
+    } else {
+      int polls = 0;
+      while (*vgen == g && !(*(volatile int *)err & EB_TIMEOUT)) {
+        if (++polls > BAR_SPIN_LIMIT) {
+          atomicOr(err, EB_TIMEOUT);
+          break;
+        }
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// phase boundary stamp (block 0, thread 0 only)
+__device__ __forceinline__ void stamp(const PersistArgs &a, int64_t t, int k) {
+  if (a.trace && blockIdx.x == 0 && threadIdx.x == 0) a.trace[t * 10 + k] = globaltimer_ns();
+}
+
+__device__ __forceinline__ bool timed_out(const int *err) { return (*(volatile const int *)err & EB_TIMEOUT) != 0; }
+
+// Fixed-order combine of the chunk partials (identical in every block): float
+// shuffle trees only -- FP64 throughput is low on this part and this runs in
+// every block every step.  Logarithms in float; log Z accumulates in float64.
+template <int TPB>
+__device__ __forceinline__ LseOut combine_chunks(const LsePartial *parts, int np, float *smf, LseOut *res_s) {
+  // up to 8 partials per thread stay in registers between the max and the sums
+  // (one L2 round trip); more chunks than that are read twice
+  constexpr int PER = 8;
+  const bool one_pass = np <= PER * TPB;
+  float4 q[PER];
+  float m = -INFINITY;
+  int nan = 0;
+  if (one_pass) {
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+      const int b = threadIdx.x + j * TPB;
+      q[j] = b < np ? __ldcg((const float4 *)&parts[b]) : make_float4(-INFINITY, 0.0f, 0.0f, 0.0f);
+      m = fmaxf(m, q[j].x);
+      nan |= __float_as_int(q[j].w);
+    }
+  } else {
+    for (int b = threadIdx.x; b < np; b += TPB) {
+      m = fmaxf(m, __ldcg(&parts[b].m));
+      nan |= __ldcg(&parts[b].nan);
+    }
+  }
+  const float M = block_max<TPB>(m, smf);
+  const int anynan = __syncthreads_or(nan);
+  float s1 = 0.0f, s2 = 0.0f;
+  if (M > -INFINITY && M < INFINITY) {
+    if (one_pass) {
+#pragma unroll
+      for (int j = 0; j < PER; ++j) {
+        if (q[j].x > -INFINITY) {
+          const float f = expf(q[j].x - M);
+          s1 += q[j].y * f;
+          s2 += q[j].z * (f * f);
+        }
+      }
+    } else {
+      for (int b = threadIdx.x; b < np; b += TPB) {
+        const float4 v = __ldcg((const float4 *)&parts[b]);
+        if (v.x > -INFINITY) {
+          const float f = expf(v.x - M);
+          s1 += v.y * f;
+          s2 += v.z * (f * f);
+        }
+      }
+    }
+  }
+  s1 = block_sum<TPB, float>(s1, smf);
+  s2 = block_sum<TPB, float>(s2, smf);
+  if (threadIdx.x == 0) {
+    LseOut o;
+    o.M = M;
+    o.flags = anynan ? 1 : 0;
+    if (anynan) {
+      o.lse = o.lse2 = o.ess = __longlong_as_double(0x7ff8000000000000ll);
+    } else if (M == INFINITY) {
+      o.lse = o.lse2 = __longlong_as_double(0x7ff0000000000000ll);
+      o.ess = __longlong_as_double(0x7ff8000000000000ll);
+    } else if (M == -INFINITY) {
+      o.lse = o.lse2 = -__longlong_as_double(0x7ff0000000000000ll);
+      o.ess = __longlong_as_double(0x7ff8000000000000ll);
+    } else {
+      o.lse = (double)M + (double)logf(s1);
+      o.lse2 = 2.0 * (double)M + (double)logf(s2);
+      o.ess = (double)s1 * (double)s1 / (double)s2;
+    }
+    *res_s = o;
+  }
+  __syncthreads();
+  const LseOut o = *res_s;
+  __syncthreads();
+  return o;
+}
+
+template <int D, int DY>
+__global__ void __launch_bounds__(PP_TPB, 2) k_pf_lg_persist(const __grid_constant__ LGP<D, DY> p,
+                                                              const __grid_constant__ PersistArgs a) {
+  __shared__ float smf[PP_TPB / 32];
+  __shared__ unsigned long long smu[PP_TPB / 32];
+  __shared__ uint64_t sP[PP_MAX_TILES + 1];
+  __shared__ int32_t sK[PP_MAX_TILES + 1];
+  __shared__ int32_t sU[PP_MAX_TILES + 1];
+  __shared__ LseOut res_s;
+  __shared__ int chunk_s;
+  __shared__ float y_s[DY];
+  __shared__ uint64_t sC[SCAN_TILE];
+  __shared__ ResampleCtl sc;
+  const unsigned G = gridDim.x;
+  const int64_t n = a.n, h = n >> 1;
+  const int nchunks = (int)((h + PP_TPB - 1) / PP_TPB);
+  const int ntiles = (int)((n + SCAN_TILE - 1) / SCAN_TILE);
+  const float scale = __int_as_float((weight_shift(n) + 127) << 23);
+  int res_cur = 0;
+  double logz = 0.0, lse_prev = 0.0;
+
+  for (int64_t t = 0; t < a.T; ++t) {
+    if (timed_out(a.err)) break;
+    stamp(a, t, 0);
+    float *xo = a.x_hist ? a.x_hist + (size_t)t * D * n : ((t & 1) ? a.xb : a.xa);
+    float *lo = a.lw_hist ? a.lw_hist + (size_t)t * n : ((t & 1) ? a.lb : a.la);
+    const float *xi = t == 0 ? nullptr : (a.x_hist ? a.x_hist + (size_t)(t - 1) * D * n : ((t & 1) ? a.xa : a.xb));
+    const float *li = t == 0 ? nullptr : (a.lw_hist ? a.lw_hist + (size_t)(t - 1) * n : ((t & 1) ? a.la : a.lb));
+    const uint32_t k0 = __ldg(&a.keys[2 * t]), k1 = __ldg(&a.keys[2 * t + 1]);
+    // observation of the step in shared memory (broadcast reads; keeps DY
+    // registers free in the particle loop)
+    if (threadIdx.x < DY) y_s[threadIdx.x] = __ldg(&a.y[t * DY + threadIdx.x]);
+    const float *y = y_s;
+    LsePartial *parts = a.parts + (t & 1) * PP_MAX_CHUNKS;
+
+    // ---- P1: propagate + weight, 256-pair chunks taken from a per-step
+    // counter (SMs that run ahead take more chunks); one partial per chunk, so
+    // the combine does not depend on which block ran which chunk
+    const uint64_t t0 = (a.trace && t == 1 && threadIdx.x == 0) ? globaltimer_ns() : 0;
+    for (;;) {
+      if (threadIdx.x == 0) chunk_s = atomicAdd(&a.chunk_ctr[t], 1);
+      __syncthreads();
+      const int c = chunk_s;
+      if (c >= nchunks) break;
+      const int64_t i = (int64_t)c * PP_TPB + threadIdx.x;
+      float m = -INFINITY, s1 = 0.0f, s2 = 0.0f;
+      int nanf = 0;
+      if (i < h) {
+        uint32_t r0, r1, q0, q1;
+        threefry2x32_m(k0, k1, (uint32_t)(2 * i), (uint32_t)(2 * i + n), p.one, r0, r1);
+        threefry2x32_m(k0, k1, (uint32_t)(2 * i + 1), (uint32_t)(2 * i + 1 + n), p.one, q0, q1);
+        // the pair runs as a two-trip loop (not unrolled): one copy of the
+        // particle code keeps the hot loop inside the instruction cache
+#pragma unroll 1
+        for (int s = 0; s < 2; ++s) {
+          const uint32_t ka = s ? r1 : r0, kb = s ? q1 : q0;
+          const int64_t ii = s ? i + h : i;
+          const float l = t == 0 ? lg_init_particle<D, DY>(p, n, ka, kb, ii, y, xo, lo)
+                                 : lg_particle<D, DY, true>(p, n, ka, kb, ii, res_cur, xi, a.anc,
+                                                            res_cur ? nullptr : li, y, xo, lo);
+          online_acc(l, m, s1, s2, nanf);
+        }
+      }
+      const LsePartial part = block_online_partial<PP_TPB>(m, s1, s2, nanf, smf);
+      if (threadIdx.x == 0) parts[c] = part;
+    }
+    if (a.trace && t == 1 && threadIdx.x == 0) a.trace[a.T * 10 + blockIdx.x] = globaltimer_ns() - t0;
+    stamp(a, t, 1);
+    grid_sync(a.bar, G, a.err);
+    stamp(a, t, 2);
+
+    // ---- P2: combine (identical in every block)
+    const LseOut o = combine_chunks<PP_TPB>(parts, nchunks, smf, &res_s);
+    logz = t == 0 ? o.lse - a.logn : logz + o.lse - (res_cur ? a.logn : lse_prev);
+    lse_prev = o.lse;
+    const int res_next = ((float)o.ess < a.thr_n) ? 1 : 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      a.ess[t] = (float)o.ess;
+      a.res[t] = res_cur;
+      if (a.logz) *a.logz = logz;
+    }
+    stamp(a, t, 3);
+    if (t + 1 == a.T) break;
+
+    if (res_next) {
+      const float M = o.M;
+      // ---- P3: per tile, exact fixed-point weights, their within-tile
+      // inclusive prefixes (stored) and the tile sum
+      for (int tile = blockIdx.x; tile < ntiles; tile += G) {
+        const int64_t i0 = (int64_t)tile * SCAN_TILE + (int64_t)threadIdx.x * SCAN_IPT;
+        uint64_t q[SCAN_IPT];
+        int bad = !(M > -INFINITY && M < INFINITY);
+        uint64_t tsum = 0;
+#pragma unroll
+        for (int j = 0; j < SCAN_IPT; ++j) {
+          const float v = i0 + j < n ? __ldcg(&lo[i0 + j]) : -INFINITY;
+          bad |= (v != v) || (v == INFINITY);
+          q[j] = quantise_weight(v, M, scale);
+          tsum += q[j];
+        }
+        unsigned long long btot;
+        uint64_t c = block_excl_scan_u64(tsum, smu, btot);
+#pragma unroll
+        for (int j = 0; j < SCAN_IPT; ++j) {
+          c += q[j];
+          q[j] = c;
+        }
+        if (i0 + SCAN_IPT <= n) {
+          ulonglong2 *dst = (ulonglong2 *)&a.cloc[i0];
+#pragma unroll
+          for (int j = 0; j < SCAN_IPT / 2; ++j) dst[j] = make_ulonglong2(q[2 * j], q[2 * j + 1]);
+        } else {
+#pragma unroll
+          for (int j = 0; j < SCAN_IPT; ++j)
+            if (i0 + j < n) a.cloc[i0 + j] = q[j];
+        }
+        bad = __syncthreads_or(bad);
+        if (threadIdx.x == 0) {
+          a.tile_sum[tile] = btot;
+          if (bad) atomicOr(&a.degen[t], 1);
+        }
+      }
+      stamp(a, t, 4);
+      grid_sync(a.bar, G, a.err);
+      stamp(a, t, 5);
+
+      // ---- P4: scan tile sums, place outputs, fill units
+      const int per = (ntiles + PP_TPB - 1) / PP_TPB;
+      const int b0 = threadIdx.x * per, b1 = min(b0 + per, ntiles);
+      unsigned long long ts[4];
+      unsigned long long run = 0;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        ts[j] = (j < per && b0 + j < b1) ? __ldcg(&a.tile_sum[b0 + j]) : 0ull;
+        run += ts[j];
+      }
+      unsigned long long Q;
+      unsigned long long pre = block_excl_scan_u64(run, smu, Q);
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (j < per && b0 + j < b1) {
+          sP[b0 + j] = pre;
+          pre += ts[j];
+        }
+      if (threadIdx.x == 0) sP[ntiles] = Q;
+      const int degenerate = __ldcg(&a.degen[t]) || Q == 0;
+      if (degenerate) {
+        for (int64_t i = blockIdx.x * (int64_t)PP_TPB + threadIdx.x; i < n; i += (int64_t)G * PP_TPB) a.anc[i] = 0;
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(a.err, EB_DEGENERATE);
+      } else {
+        const uint32_t m23 = bits_at(__ldg(&a.keys[2 * (t + 1)]), __ldg(&a.keys[2 * (t + 1) + 1]), 1, 0) >> 9;
+        if (threadIdx.x == 0) sys_constants(Q, (uint64_t)n, m23, sc, a.magic);
+        const float n_over_q = __fdiv_rn((float)n, (float)Q);
+        for (int b = threadIdx.x; b <= ntiles; b += PP_TPB) sK[b] = (int32_t)sys_count(sP[b], n, m23, Q, n_over_q);
+        __syncthreads();
+        unsigned long long nu = 0;
+        for (int b = b0; b < b1; ++b) nu += (unsigned long long)((sK[b + 1] - sK[b] + SCAN_TILE - 1) / SCAN_TILE);
+        unsigned long long utot;
+        unsigned long long uo = block_excl_scan_u64(nu, smu, utot);
+        for (int b = b0; b < b1; ++b) {
+          sU[b] = (int32_t)uo;
+          uo += (unsigned long long)((sK[b + 1] - sK[b] + SCAN_TILE - 1) / SCAN_TILE);
+        }
+        if (threadIdx.x == 0) sU[ntiles] = (int32_t)utot;
+        __syncthreads();
+        stamp(a, t, 6);
+        const ResampleCtl c = sc;
+        if (a.trace && blockIdx.x == 0 && threadIdx.x == 0) a.trace[t * 10 + 9] = utot;
+        for (int u = blockIdx.x; u < (int)utot; u += G) {
+          int lo_b = 0, hi_b = ntiles;  // largest tile b with sU[b] <= u
+          while (hi_b - lo_b > 1) {
+            const int mid = (lo_b + hi_b) >> 1;
+            if (sU[mid] <= u) lo_b = mid;
+            else hi_b = mid;
+          }
+          const int tile = lo_b;
+          const int64_t kb = sK[tile] + (int64_t)(u - sU[tile]) * SCAN_TILE;
+          const int64_t ke = kb + SCAN_TILE < (int64_t)sK[tile + 1] ? kb + SCAN_TILE : (int64_t)sK[tile + 1];
+          const int64_t base = (int64_t)tile * SCAN_TILE;
+          const int cnt_valid = (int)(n - base < SCAN_TILE ? n - base : SCAN_TILE);
+          const uint64_t P = sP[tile];
+          {
+            uint64_t v[SCAN_IPT];
+#pragma unroll
+            for (int j = 0; j < SCAN_IPT; ++j) {
+              const int jj = threadIdx.x + j * PP_TPB;
+              v[j] = jj < cnt_valid ? __ldcg(&a.cloc[base + jj]) : 0ull;
+            }
+#pragma unroll
+            for (int j = 0; j < SCAN_IPT; ++j) {
+              const int jj = threadIdx.x + j * PP_TPB;
+              if (jj < cnt_valid) sC[jj] = P + v[j];
+            }
+          }
+          __syncthreads();
+          merge_fill(sC, cnt_valid, c, kb, (int)(ke - kb), base, n, a.anc);
+          __syncthreads();
+        }
+      }
+      stamp(a, t, 7);
+      grid_sync(a.bar, G, a.err);
+      stamp(a, t, 8);
+    }
+    res_cur = res_next;
+  }
+}
+
+__global__ void k_or_err(const int *src, int *dst) {
+  if (dst && *src) atomicOr(dst, *src);
+}
+
+// host: occupancy-sized cooperative launch
+template <int D, int DY>
+int launch_persist(const mgb_lg_model *m, const PersistArgs &args, cudaStream_t s) {
+  const LGP<D, DY> p = pack_lg<D, DY>(m);
+  int dev = 0, sms = 0, per_sm = 0, coop = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return ERR_CUDA;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return ERR_CUDA;
+  if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop) return ERR_UNSUPPORTED;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pf_lg_persist<D, DY>, PP_TPB, 0) != cudaSuccess ||
+      per_sm < 1)
+    return ERR_UNSUPPORTED;
+  PersistArgs a = args;
+  void *kargs[] = {(void *)&p, (void *)&a};
+  const dim3 grid((unsigned)(sms * per_sm)), block(PP_TPB);
+  if (cudaLaunchCooperativeKernel((void *)k_pf_lg_persist<D, DY>, grid, block, kargs, 0, s) != cudaSuccess)
+    return ERR_LAUNCH;
+  k_or_err<<<1, 1, 0, s>>>(args.err, args.user_err);
+  return launch_status();
+}
+
+#define MGB_PERSIST_CASE(D_, DY_) \
+  if (m->d == D_ && m->dy == DY_) return launch_persist<D_, DY_>(m, a, s);
+
+int run_lg_persistent(const mgb_lg_model *m, const PersistArgs &a, cudaStream_t s) {
+  MGB_PERSIST_CASE(1, 1)
+  MGB_PERSIST_CASE(2, 1)
+  MGB_PERSIST_CASE(3, 1)
+  MGB_PERSIST_CASE(4, 1)
+  MGB_PERSIST_CASE(5, 1)
+  MGB_PERSIST_CASE(8, 1)
+  MGB_PERSIST_CASE(10, 1)
+  MGB_PERSIST_CASE(2, 2)
+  MGB_PERSIST_CASE(3, 3)
+  MGB_PERSIST_CASE(4, 4)
+  MGB_PERSIST_CASE(5, 5)
+  MGB_PERSIST_CASE(8, 8)
+  MGB_PERSIST_CASE(10, 10)
+  return ERR_UNSUPPORTED;
+}
+
+}  // namespace mgb

@@ -13,10 +13,14 @@
 //    prefix); its first warp sums predecessors' words until it meets an
 //    inclusive prefix.  Waits are bounded: on expiry the kernel raises
 //    EB_TIMEOUT and continues.
-//  * Systematic: thresholds (k + u) n^-1 Q form an arithmetic progression, so
-//    particle i's offspring are the k in [K(C_{i-1}), K(C_i)) with
-//    K(X) = #{k : (k 2^23 + m) Q < X n 2^23}; each tile fills its output range
-//    cooperatively (binary search over the tile's K values in shared memory).
+//  * Systematic: reduce-then-scan.  Pass 1 sums each 2048-particle tile and
+//    its last block scans the tile sums (the total Q must be known before any
+//    threshold can be placed).  Thresholds (k + u) Q / n form an arithmetic
+//    progression, so particle i's offspring are the k in [K(C_{i-1}), K(C_i))
+//    with K(X) = #{k : (k 2^23 + m) Q < X n 2^23}; pass 1 also cuts each tile's
+//    output range into units of <= 2048 outputs, and pass 2 runs one block per
+//    unit (heavy tiles are split across blocks, so no block does more than one
+//    tile of scan work plus 2048 outputs).
 //  * Multinomial: sorted uniforms S_k / S_n from n+1 exponential spacings
 //    (exact integer scan); ancestors by a merge-path merge of the weight
 //    prefix C with S (A_i precedes B_k iff C_i S_n <= S_k Q).
@@ -35,8 +39,69 @@ struct ResampleCtl {
   int degenerate;
   unsigned long long total;  // exact sum of q_i
   unsigned int tile_counter2;
-  int pad;
+  unsigned int units;        // systematic fill units
+  unsigned int m23;          // systematic uniform's mantissa
+  // systematic thresholds T_k = floor((k 2^23 + m) Q / (n 2^23))
+  //                          = k qn + a + floor((k rn + bh) / n)
+  unsigned long long qn, rn, a, bh, magic;  // magic = floor((2^64 - 1) / n)
 };
+
+// Threshold constants from Q, n and the uniform's mantissa m:
+//   Q = qn n + rn;  m qn = a1 2^23 + r1;  V = r1 n + m rn < 2^24 n
+//   m Q / (n 2^23) = a1 + V / (n 2^23),  a = a1 + [V >= n 2^23],  bh = (V mod n 2^23) >> 23
+__device__ __forceinline__ void sys_constants(uint64_t Q, uint64_t n, uint32_t m, ResampleCtl &c,
+                                              uint64_t magic) {
+  uint64_t qn = __umul64hi(Q, magic), rn = Q - qn * n;  // magic = floor((2^64 - 1) / n)
+  if (rn >= n) {
+    ++qn;
+    rn -= n;
+  }
+  c.qn = qn;
+  c.rn = rn;
+  const uint64_t lo = (uint64_t)m * c.qn, hi = __umul64hi((uint64_t)m, c.qn);
+  const uint64_t a1 = (hi << 41) | (lo >> 23), r1 = lo & ((1ull << 23) - 1);
+  uint64_t V = r1 * n + (uint64_t)m * c.rn;
+  const uint64_t den = n << 23;
+  uint64_t a2 = 0;
+  if (V >= den) { V -= den; a2 = 1; }
+  c.a = a1 + a2;
+  c.bh = V >> 23;
+  c.magic = magic;
+}
+
+// #{j < cnt : c[j] <= T} for sorted c, given the answer is >= from:
+// galloping steps 1, 2, 4, ... from `from`, then a binary search, so the cost is
+// O(log gap) even across long runs of zero-weight particles.
+__device__ __forceinline__ int count_le_from(const uint64_t *c, int cnt, uint64_t T, int from) {
+  if (from >= cnt || c[from] > T) return from;
+  int lo = from + 1, step = 1;  // c[lo - 1] <= T
+  int hi = lo;
+  while (true) {
+    hi = lo + step;
+    if (hi >= cnt) {
+      hi = cnt;
+      break;
+    }
+    if (c[hi - 1] > T) break;
+    lo = hi;
+    step <<= 1;
+  }
+  // answer in [lo, hi]: c[lo - 1] <= T, c[hi - 1] > T or hi == cnt
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (c[mid] <= T) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// T_k from the constants above (exact; one 64-bit high multiply + one fix-up)
+__device__ __forceinline__ uint64_t sys_threshold(const ResampleCtl &c, uint64_t k, uint64_t n) {
+  const uint64_t num = k * c.rn + c.bh;
+  uint64_t q = __umul64hi(num, c.magic);
+  if (num - q * n >= n) ++q;
+  return k * c.qn + c.a + q;
+}
 
 struct LsePartial {
   float m, s1, s2;
@@ -52,67 +117,113 @@ struct LseOut {
 
 // ------------------------------------------------------- LSE partials
 // Block-level reduction of (max, sums) over a set of values, one per thread
-// slot; inactive slots pass -inf.
+// slot; inactive slots pass -inf.  The sums are float shuffle trees (pairwise,
+// error O(log2 TPB) ulp); float64 is used only across blocks, where there are
+// few terms -- FP64 runs at a small fraction of the FP32 rate on this part.
 template <int TPB>
 __device__ __forceinline__ LsePartial block_lse_partial(float v, bool nan_in, float *smf, double *smd) {
+  (void)smd;
   const float m = block_max<TPB>(v, smf);
   float e = 0.0f;
   if (m > -INFINITY && m < INFINITY && v == v) e = expf(v - m);
-  const double s1 = block_sum<TPB, double>((double)e, smd);
-  const double s2 = block_sum<TPB, double>((double)e * (double)e, smd);
+  const float s1 = block_sum<TPB, float>(e, smf);
+  const float s2 = block_sum<TPB, float>(e * e, smf);
   const int nn = __syncthreads_or(nan_in ? 1 : 0);
   LsePartial p;
   p.m = m;
-  p.s1 = (float)s1;
-  p.s2 = (float)s2;
+  p.s1 = s1;
+  p.s2 = s2;
   p.nan = nn;
   return p;
 }
 
-// Combine all partials (called by the last block, TPB threads). Returns LseOut
-// in every thread.
+// Combine all partials (TPB threads of one block).  The max is a block
+// reduction; the float64 sums run in warp 0 only and the logarithms /
+// exponential in its lane 0, then the result is broadcast through shared
+// memory (FP64 throughput is low on this part, so it is kept off the other
+// warps).
 template <int TPB>
 __device__ __forceinline__ LseOut combine_lse(const LsePartial *parts, int nparts, float *smf, double *smd) {
+  (void)smd;
+  __shared__ LseOut res_s;
   float m = -INFINITY;
   int nan = 0;
   for (int b = threadIdx.x; b < nparts; b += TPB) {
-    const float mb = __ldcg(&parts[b].m);
-    const int nb = __ldcg(&parts[b].nan);
-    m = fmaxf(m, mb);
-    nan |= nb;
+    m = fmaxf(m, __ldcg(&parts[b].m));
+    nan |= __ldcg(&parts[b].nan);
   }
   const float M = block_max<TPB>(m, smf);
   const int anynan = __syncthreads_or(nan);
-  double s1 = 0.0, s2 = 0.0;
-  if (M > -INFINITY && M < INFINITY) {
-    for (int b = threadIdx.x; b < nparts; b += TPB) {
-      const float mb = __ldcg(&parts[b].m);
-      if (mb > -INFINITY) {
-        const float f = expf(mb - M);
-        s1 += (double)(__ldcg(&parts[b].s1) * f);
-        s2 += (double)(__ldcg(&parts[b].s2) * (f * f));
+  if (threadIdx.x < 32) {
+    double s1 = 0.0, s2 = 0.0;
+    if (M > -INFINITY && M < INFINITY) {
+      for (int b = threadIdx.x; b < nparts; b += 32) {
+        const float mb = __ldcg(&parts[b].m);
+        if (mb > -INFINITY) {
+          const float f = expf(mb - M);
+          s1 += (double)(__ldcg(&parts[b].s1) * f);
+          s2 += (double)(__ldcg(&parts[b].s2) * (f * f));
+        }
       }
     }
+    s1 = warp_sum<double>(s1);
+    s2 = warp_sum<double>(s2);
+    if (threadIdx.x == 0) {
+      LseOut o;
+      o.M = M;
+      o.flags = anynan ? 1 : 0;
+      if (anynan) {
+        o.lse = o.lse2 = o.ess = __longlong_as_double(0x7ff8000000000000ll);
+      } else if (M == INFINITY) {
+        o.lse = o.lse2 = __longlong_as_double(0x7ff0000000000000ll);
+        o.ess = __longlong_as_double(0x7ff8000000000000ll);
+      } else if (M == -INFINITY) {
+        o.lse = o.lse2 = -__longlong_as_double(0x7ff0000000000000ll);
+        o.ess = __longlong_as_double(0x7ff8000000000000ll);
+      } else {
+        // float logarithms of the float64 sums (relative error ~1e-7 of
+        // log S, i.e. ~1e-7 absolute on the logsumexp); the ESS S1^2 / S2 in float64
+        o.lse = (double)M + (double)logf((float)s1);
+        o.lse2 = 2.0 * (double)M + (double)logf((float)s2);
+        o.ess = s1 * s1 / s2;
+      }
+      res_s = o;
+    }
   }
-  s1 = block_sum<TPB, double>(s1, smd);
-  s2 = block_sum<TPB, double>(s2, smd);
-  LseOut o;
-  o.M = M;
-  o.flags = anynan ? 1 : 0;
-  if (anynan) {
-    o.lse = o.lse2 = o.ess = __longlong_as_double(0x7ff8000000000000ll);
-  } else if (M == INFINITY) {
-    o.lse = o.lse2 = __longlong_as_double(0x7ff0000000000000ll);
-    o.ess = __longlong_as_double(0x7ff8000000000000ll);
-  } else if (M == -INFINITY) {
-    o.lse = o.lse2 = -__longlong_as_double(0x7ff0000000000000ll);
-    o.ess = __longlong_as_double(0x7ff8000000000000ll);
-  } else {
-    o.lse = (double)M + log(s1);
-    o.lse2 = 2.0 * (double)M + log(s2);
-    o.ess = exp(2.0 * o.lse - o.lse2);
-  }
+  __syncthreads();
+  const LseOut o = res_s;
+  __syncthreads();
   return o;
+}
+
+// online (max, sum exp(l - max), sum exp(2 (l - max))) of a stream of values
+__device__ __forceinline__ void online_acc(float l, float &m, float &s1, float &s2, int &nanf) {
+  if (l != l) {
+    nanf = 1;
+    return;
+  }
+  if (l == -INFINITY || m == INFINITY) return;
+  if (l > m) {
+    const float sc = m == -INFINITY ? 0.0f : expf(m - l);
+    s1 = s1 * sc + 1.0f;
+    s2 = s2 * (sc * sc) + 1.0f;
+    m = l;
+  } else {
+    const float e = expf(l - m);
+    s1 += e;
+    s2 += e * e;
+  }
+}
+
+// block partial of per-thread online accumulators
+template <int TPB>
+__device__ __forceinline__ LsePartial block_online_partial(float m, float s1, float s2, int nanf, float *smf) {
+  const float Mb = block_max<TPB>(m, smf);
+  const float f = (m > -INFINITY && Mb < INFINITY) ? expf(m - Mb) : 0.0f;
+  const float b1 = block_sum<TPB, float>(s1 * f, smf);
+  const float b2 = block_sum<TPB, float>(s2 * (f * f), smf);
+  const int bn = __syncthreads_or(nanf);
+  return LsePartial{Mb, b1, b2, bn};
 }
 
 // ------------------------------------------------------- scan helpers
@@ -189,14 +300,121 @@ __device__ __forceinline__ void tile_scan(uint64_t (&v)[SCAN_IPT], uint32_t tile
   for (int j = 0; j < SCAN_IPT; ++j) v[j] += add;
 }
 
+// Threshold cursor: T_k and the remainder of (k rn + bh) mod n, so that
+// T_{k+1} = T_k + qn + carry costs four integer operations.
+struct ThrCursor {
+  uint64_t T, rem;
+};
+__device__ __forceinline__ ThrCursor thr_at(const ResampleCtl &c, uint64_t k, uint64_t n) {
+  const uint64_t num = k * c.rn + c.bh;
+  uint64_t q = __umul64hi(num, c.magic);
+  uint64_t rem = num - q * n;
+  if (rem >= n) {
+    ++q;
+    rem -= n;
+  }
+  return ThrCursor{k * c.qn + c.a + q, rem};
+}
+__device__ __forceinline__ void thr_next(ThrCursor &t, const ResampleCtl &c, uint64_t n) {
+  t.rem += c.rn;
+  const uint64_t carry = t.rem >= n ? 1ull : 0ull;
+  t.rem -= carry * n;
+  t.T += c.qn + carry;
+}
+
+// Merge-path fill of one unit: sC[0..cnt) are the tile's sorted inclusive
+// prefixes, outputs k in [kb, kb + nout) have sorted thresholds T_k; output k
+// goes to particle base + #{j : sC[j] <= T_k}.  Thread t merges diagonal
+// [16 t, 16 t + 16) after one partition search, O(1) work per element.
+constexpr int MERGE_PER = 16;
+__device__ __forceinline__ void merge_fill(const uint64_t *sC, int cnt, const ResampleCtl &c, int64_t kb, int nout,
+                                           int64_t base, int64_t n, int32_t *anc) {
+  const int total = cnt + nout;
+  const int d0 = threadIdx.x * MERGE_PER;
+  if (d0 >= total) return;
+  int lo = d0 > nout ? d0 - nout : 0, hi = d0 < cnt ? d0 : cnt;
+  while (lo < hi) {  // split: A[mid] before B[d0 - 1 - mid] iff sC[mid] <= T
+    const int mid = (lo + hi) >> 1;
+    const uint64_t T = thr_at(c, (uint64_t)(kb + d0 - 1 - mid), (uint64_t)n).T;
+    if (sC[mid] <= T) lo = mid + 1;
+    else hi = mid;
+  }
+  int i = lo, kk = d0 - lo;
+  ThrCursor cur = thr_at(c, (uint64_t)(kb + (kk < nout ? kk : 0)), (uint64_t)n);
+  const int d1 = d0 + MERGE_PER < total ? d0 + MERGE_PER : total;
+  for (int d = d0; d < d1; ++d) {
+    if (i < cnt && (kk >= nout || sC[i] <= cur.T)) {
+      ++i;
+    } else {
+      anc[kb + kk] = (int32_t)(base + (i < cnt ? i : cnt - 1));
+      ++kk;
+      thr_next(cur, c, (uint64_t)n);
+    }
+  }
+}
+
+// Writes a particle's offspring run anc[lo, hi) = idx: short runs directly,
+// runs longer than RUN_DIRECT_MAX are queued in shared memory and filled by
+// whole warps afterwards (fill_queued_runs), so one heavy particle does not
+// serialise its warp.
+constexpr int RUN_DIRECT_MAX = 16;
+constexpr int RUN_QUEUE = 256;  // >= 2048 outputs / RUN_DIRECT_MAX
+__device__ __forceinline__ void write_run(int32_t *anc, int64_t lo, int64_t hi, int32_t idx, int4 *q, int *nq) {
+  if (hi - lo > RUN_DIRECT_MAX) {
+    const int slot = atomicAdd(nq, 1);
+    q[slot] = make_int4((int)lo, (int)hi, idx, 0);
+  } else {
+    for (int64_t k = lo; k < hi; ++k) anc[k] = idx;
+  }
+}
+template <int TPB>
+__device__ __forceinline__ void fill_queued_runs(int32_t *anc, const int4 *q, const int *nq) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int r = warp; r < *nq; r += TPB / 32) {
+    const int4 v = q[r];
+    for (int k = v.x + lane; k < v.y; k += 32) anc[k] = v.z;
+  }
+}
+
+// block-wide exclusive scan of one u64 per thread (returns the block total too)
+__device__ __forceinline__ unsigned long long block_excl_scan_u64(unsigned long long v, unsigned long long *sm,
+                                                                  unsigned long long &total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned long long x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  __syncthreads();
+  if (lane == 31) sm[warp] = x;
+  __syncthreads();
+  unsigned long long wpre = 0, tot = 0;
+#pragma unroll
+  for (int w = 0; w < SCAN_TPB / 32; ++w) {
+    if (w < warp) wpre += sm[w];
+    tot += sm[w];
+  }
+  total = tot;
+  return wpre + x - v;
+}
+
 // K(X) = #{k in [0, n) : (k 2^23 + m) Q < X n 2^23}  (systematic threshold count)
+// The float estimate is within one of K; both neighbours are tested
+// unconditionally (independent 128-bit products, no loop on the common path)
+// and a walk runs only if the estimate was further off.
 __device__ __forceinline__ int64_t sys_count(uint64_t X, int64_t n, uint64_t m, uint64_t Q, float n_over_q) {
   const uint64_t den = (uint64_t)n << 23;
-  float est = __fmul_rn((float)X, n_over_q) - (float)m * 0x1p-23f;
-  int64_t kk = (int64_t)ceilf(est);
-  if (kk < 0) kk = 0;
-  if (kk > n) kk = n;
-  // predicate f(k): (k 2^23 + m) Q < X den  (monotone: true then false)
+  const float xf = __fmaf_rn(__uint2float_rn((uint32_t)(X >> 32)), 0x1p32f, __uint2float_rn((uint32_t)X));
+  // the estimate lies in [-1, n] with n < 2^31: a 32-bit conversion (a float to
+  // 64-bit integer conversion is a slow path on this part)
+  const float est = fminf(fmaxf(__fmul_rn(xf, n_over_q) - (float)m * 0x1p-23f, -1.0f), 0x1.fffffep+30f);
+  int64_t kk = (int64_t)(int)ceilf(est);
+  kk = kk < 0 ? 0 : (kk > n ? n : kk);
+  // f(k) := (k 2^23 + m) Q < X den, true for k < K, false from K on
+  const bool f_lo = kk > 0 && !mul_le(X, den, (((uint64_t)(kk - 1)) << 23) + m, Q);
+  const bool f_hi = kk < n && !mul_le(X, den, (((uint64_t)kk) << 23) + m, Q);
+  if ((kk == 0 || f_lo) && !f_hi) return kk;
   while (kk > 0 && mul_le(X, den, (((uint64_t)(kk - 1)) << 23) + m, Q)) --kk;
   while (kk < n && !mul_le(X, den, (((uint64_t)kk) << 23) + m, Q)) ++kk;
   return kk;

@@ -25,6 +25,7 @@ from .metrics import ess_log_weight
 from .resampling import SCHEMES, resample
 
 LOG2PI = math.log(2.0 * math.pi)
+RUN_LAUNCH_PER_STEP = 0x100  # MGB_RUN_LAUNCH_PER_STEP
 LG_SUPPORTED = {(1, 1), (2, 1), (3, 1), (4, 1), (5, 1), (8, 1), (10, 1),
                 (2, 2), (3, 3), (4, 4), (5, 5), (8, 8), (10, 10)}
 
@@ -252,11 +253,14 @@ def propagate_particle_filter(ssm_scenario, particle_filter, particles, y_new, t
 
 
 def run_particle_filter_for_marginals(ssm_scenario, particle_filter, y, t, random_key, n=None, initial_sample=None,
-                                      ess_threshold=0.5, resampling="systematic", history=True):
+                                      ess_threshold=0.5, resampling="systematic", history=True, persistent=True):
     """filtering.py:255-324 on the GPU.
 
     Returns cdict(value (T, n, d), log_weight (T, n), ess (T,), t, y, log_z, resampled)
     (value/log_weight only the final step, shape (1, n, d) / (1, n), when history=False).
+    persistent=False forces one kernel launch per phase and step instead of the
+    single persistent launch (systematic resampling, even n <= 2^21); results
+    are the same.
     """
     _check_lg(ssm_scenario, particle_filter)
     particle_filter.startup(ssm_scenario)
@@ -278,8 +282,9 @@ def run_particle_filter_for_marginals(ssm_scenario, particle_filter, y, t, rando
     lh = torch.empty((T, n) if history else (1, n), dtype=torch.float32, device=dev)
     out = _lib.PFOutputs(logz.data_ptr(), ess.data_ptr(), res.data_ptr(), xh.data_ptr() if history else None,
                          lh.data_ptr() if history else None, None if history else xh.data_ptr(),
-                         None if history else lh.data_ptr(), err.data_ptr())
-    call("mgb_pf_lg_run", ctypes.byref(s), n, T, _dev.ptr(key), _dev.ptr(y2), float(ess_threshold), sc,
+                         None if history else lh.data_ptr(), err.data_ptr(), None)
+    flags = 0 if persistent else RUN_LAUNCH_PER_STEP
+    call("mgb_pf_lg_run", ctypes.byref(s), n, T, _dev.ptr(key), _dev.ptr(y2), float(ess_threshold), sc | flags,
          _dev.ptr(ws), ws.numel(), ctypes.byref(out), _dev.stream_ptr())
     e = int(err.item())
     if e & 1:

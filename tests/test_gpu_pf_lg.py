@@ -14,11 +14,11 @@ from oracle import kalman, models
 pytestmark = pytest.mark.gpu
 
 
-def _models(d, dy=None, seed=0, diag_r=True):
+def _models(d, dy=None, seed=0, diag_r=True, dense_q=True):
     dy = dy or d
     rng = np.random.default_rng(seed)
     F = models.random_stable_matrix(d, seed)
-    Q = 0.1 * np.eye(d) + (0.02 * np.ones((d, d)) if d > 1 else 0)
+    Q = 0.1 * np.eye(d) + (0.02 * np.ones((d, d)) if d > 1 and dense_q else 0)
     H = np.eye(d) if dy == d else rng.standard_normal((dy, d)) / np.sqrt(d)
     R = 0.5 * np.eye(dy) if diag_r else 0.5 * np.eye(dy) + 0.1 * np.ones((dy, dy))
     S0 = np.eye(d)
@@ -28,12 +28,13 @@ def _models(d, dy=None, seed=0, diag_r=True):
     return p, ssm
 
 
+@pytest.mark.parametrize("n", [3000, 3001])
 @pytest.mark.parametrize("d,dy", [(1, 1), (2, 1), (3, 3), (10, 10), (10, 1), (5, 5), (8, 8)])
-def test_init_and_step_bit_exact(cuda, d, dy):
+def test_init_and_step_bit_exact(cuda, d, dy, n):
+    """n even runs the two-particles-per-thread kernel, n odd the one-per-thread kernel."""
     import mocat_gb300 as mg
     from mocat_gb300.ssm import _step
     p, ssm = _models(d, dy, seed=d)
-    n = 3001
     _, y = models.simulate_lg(p, 3, O.PRNGKey(0))
     key = O.PRNGKey(1)
     x0, lw0 = O.lg_init(p, n, key, y[0])
@@ -53,22 +54,40 @@ def test_init_and_step_bit_exact(cuda, d, dy):
         assert np.array_equal(ln.cpu().numpy(), lr)
 
 
+@pytest.mark.parametrize("persistent", [True, False])
 @pytest.mark.parametrize("scheme", ["systematic", "multinomial", "categorical"])
 @pytest.mark.parametrize("d", [1, 3, 10])
-def test_run_matches_oracle(cuda, scheme, d):
+@pytest.mark.parametrize("odd", [False, True])
+def test_run_matches_oracle(cuda, scheme, d, odd, persistent):
+    """Even n with systematic resampling runs the persistent whole-filter kernel
+    (persistent=True); every other case runs one launch per phase and step."""
     import mocat_gb300 as mg
     p, ssm = _models(d, seed=10 + d)
-    T, n = 25, 1000 if scheme == "categorical" else 5003
+    T, n = 25, (1000 if scheme == "categorical" else 5002) + int(odd)
     _, y = models.simulate_lg(p, T, O.PRNGKey(0))
     ref = O.lg_run(p, n, O.PRNGKey(3), y, ess_threshold=0.5, scheme=scheme, history=True)
     out = mg.ssm.run_particle_filter_for_marginals(ssm, mg.ssm.BootstrapFilter(), y, np.arange(T), O.PRNGKey(3),
-                                                   n=n, ess_threshold=0.5, resampling=scheme)
+                                                   n=n, ess_threshold=0.5, resampling=scheme, persistent=persistent)
     assert np.array_equal(out.resampled.cpu().numpy(), ref["resampled"])
     assert ref["resampled"].sum() >= 2
     assert np.array_equal(out.value.cpu().numpy(), ref["value"])
     assert np.array_equal(out.log_weight.cpu().numpy(), ref["log_weight"])
     assert np.allclose(out.ess.cpu().numpy(), ref["ess"], rtol=1e-5)
     assert abs(float(out.log_z) - ref["log_z"]) <= 1e-5 * abs(ref["log_z"])
+
+
+@pytest.mark.parametrize("d", [3, 10])
+def test_structured_matrices_bit_exact(cuda, d):
+    """Diagonal Q and R, H = I take the specialised paths; values equal the dense oracle's."""
+    import mocat_gb300 as mg
+    p, ssm = _models(d, seed=20 + d, dense_q=False)
+    T, n = 12, 4096
+    _, y = models.simulate_lg(p, T, O.PRNGKey(0))
+    ref = O.lg_run(p, n, O.PRNGKey(4), y, ess_threshold=0.5, scheme="systematic", history=True)
+    out = mg.ssm.run_particle_filter_for_marginals(ssm, mg.ssm.BootstrapFilter(), y, np.arange(T), O.PRNGKey(4),
+                                                   n=n, ess_threshold=0.5)
+    assert np.array_equal(out.value.cpu().numpy(), ref["value"])
+    assert np.array_equal(out.log_weight.cpu().numpy(), ref["log_weight"])
 
 
 def test_config1_every_step_vs_kalman(cuda):
@@ -87,7 +106,8 @@ def test_config1_every_step_vs_kalman(cuda):
     assert abs(float(out.log_z) - kl) < 1.5, (float(out.log_z), kl)
 
 
-def test_config2_full_size_vs_kalman(cuda):
+@pytest.mark.parametrize("persistent", [True, False])
+def test_config2_full_size_vs_kalman(cuda, persistent):
     """d=10, n=2^20, T=200 (of 1000), ESS-triggered systematic at 0.5 n: log Z vs Kalman,
     a size-independent property (the estimator's error at this n is far below 1)."""
     import mocat_gb300 as mg
@@ -98,12 +118,30 @@ def test_config2_full_size_vs_kalman(cuda):
     _, y = models.simulate_lg(p, T, O.PRNGKey(0))
     kl = kalman.loglik(p["F64"], p["Q"], p["H64"], p["R"], p["m064"], p["S0"], y)
     out = mg.ssm.run_particle_filter_for_marginals(ssm, mg.ssm.BootstrapFilter(), y, np.arange(T),
-                                                   mg.random.PRNGKey(1), n=n, history=False)
+                                                   mg.random.PRNGKey(1), n=n, history=False, persistent=persistent)
     lz = float(out.log_z)
     assert abs(lz - kl) < 0.5, (lz, kl)
     ess = out.ess.cpu().numpy()
     assert (ess > 0).all() and (ess <= n * (1 + 1e-5)).all()
     assert 0 < out.resampled.cpu().numpy().sum() < T
+
+
+def test_persistent_matches_launch_per_step_full_size(cuda):
+    """n = 2^20, d = 10, T = 60: the persistent kernel and the launch-per-step path give the
+    same particles, log-weights and resample flags, and log Z within 1e-7 relative (the two
+    paths group the float logsumexp partials differently)."""
+    import mocat_gb300 as mg
+    d, T, n = 10, 60, 1 << 20
+    F = models.random_stable_matrix(d, 0)
+    ssm = mg.ssm.TimeHomogenousLinearGaussian(np.zeros(d), np.eye(d), F, 0.1 * np.eye(d), np.eye(d), 0.5 * np.eye(d))
+    sim = ssm.simulate(np.arange(T), mg.random.PRNGKey(0))
+    outs = [mg.ssm.run_particle_filter_for_marginals(ssm, mg.ssm.BootstrapFilter(), sim.y, np.arange(T),
+                                                     mg.random.PRNGKey(2), n=n, history=False, persistent=pp)
+            for pp in (True, False)]
+    a, b = outs
+    assert torch.equal(a.value, b.value) and torch.equal(a.log_weight, b.log_weight)
+    assert torch.equal(a.resampled, b.resampled)
+    assert abs(float(a.log_z) - float(b.log_z)) <= 1e-7 * abs(float(b.log_z))
 
 
 def test_online_propagate_matches_run(cuda):
