@@ -22,7 +22,8 @@
  *     ran out, bit 2 = every weight was zero / non-finite.
  * Thread-safety: calls on different streams with different workspaces are
  * independent; the only global mutable state is the fixed scratch array of
- * mgb_resample_systematic_u_noalloc.
+ * mgb_resample_systematic_u_noalloc and the mutex-guarded autotune cache of
+ * mgb_pf_sv_batch_autotune.
  */
 #ifndef MOCAT_GB300_H
 #define MOCAT_GB300_H
@@ -126,7 +127,7 @@ int mgb_gather_rows(const float *x_dev, int64_t width, const int32_t *ancestors_
  *   F, Lq, C0: d x d (transition_matrix, transition_covariance_sqrt,
  *   initial_covariance_sqrt); H: dy x d (likelihood_matrix); P: dy x dy
  *   (likelihood_precision_sqrt); m0: d; c = (dy log 2 pi - log det_prec) / 2.
- * Supported (d, dy): d in {1,2,3,4,5,6,8,10,12,16}, dy in {1, d}.
+ * Supported (d, dy): (d, 1) for d in {1,2,3,4,5,8,10}; (d, d) for d in {2,3,4,5,8,10}.
  */
 typedef struct {
   int32_t d, dy;
@@ -171,6 +172,66 @@ size_t mgb_pf_lg_workspace(int64_t n, int64_t T, int32_t d, int scheme);
 int mgb_pf_lg_run(const mgb_lg_model *model_host, int64_t n, int64_t T, const uint32_t *key_dev, const float *y_dev,
                   float ess_threshold, int scheme, void *ws_dev, size_t ws_bytes, const mgb_pf_outputs *out,
                   void *stream);
+
+/* ------------------------------- many stochastic-volatility filters at once
+ * B independent run_particle_filter_for_marginals calls (mocat/src/ssm/filtering.py:255-324)
+ * with BootstrapFilter on StochasticVolatility, d = 1
+ * (mocat/src/ssm/scenarios/stochastic_volatility.py:71-108), each with its own
+ * particle count n_b, length T_b, observations y[y_off_b : y_off_b + T_b] and key
+ * keys[2b : 2b + 2]; the reference runs them one after another.  All filters
+ * run in one persistent launch: each CTA takes bundles of filters of similar
+ * size and length from a work queue and keeps every filter's particles in
+ * shared memory for all of its steps.
+ *   x_t = phi x_{t-1} + bsig eps,  x_0 = c0 eps + m0,  eps = normal(split(k_t, n)[i], (1,))
+ *   potential(x, y) = (0.5 y^2 r2) exp(-x) + 0.5 x + cB
+ * Resampling is ESS-triggered (ess_{t-1} < ess_threshold * n_b), multinomial or
+ * systematic.  1 <= T_b, 2 <= n_b <= MGB_SV_BATCH_MAX_N.
+ */
+#define MGB_SV_BATCH_MAX_N 8192
+typedef struct {
+  float phi;  /* transition_matrix */
+  float bsig; /* transition_covariance_sqrt * sqrt(t_new - t_prev) */
+  float r2;   /* likelihood_precision_diag_sqrt ** 2 */
+  float cB;   /* (log 2 pi - log r2) / 2 */
+  float c0;   /* initial_covariance_sqrt */
+  float m0;   /* initial_mean */
+} mgb_sv_model;
+
+/* launch shape of a batched run (from mgb_pf_sv_batch_plan / _autotune) */
+typedef struct {
+  int32_t threads;     /* CTA size: 256, 512 or 1024 */
+  int32_t ppt;         /* particles per thread: a filter of slot size s runs on max(32, s / ppt) threads */
+  int32_t ctas_per_sm; /* CTAs per SM (0 = as many as fit) */
+  int32_t nbundles;    /* number of bundles (written by the planner) */
+  int64_t smem_bytes;  /* dynamic shared memory per CTA (written by the planner) */
+} mgb_sv_launch;
+
+/* Host-side planner: validates n/T, groups the filters into bundles (filters
+ * of one power-of-two slot size, similar T) and orders the bundles longest
+ * first.  Writes order_host (B,) and bundles_host (4 * B int32: first, count,
+ * slot, reserved) and fills launch->nbundles / smem_bytes.  threads / ppt /
+ * ctas_per_sm are read from *launch. */
+int mgb_pf_sv_batch_plan(int64_t B, const int32_t *n_host, const int32_t *T_host, mgb_sv_launch *launch,
+                         int32_t *order_host, int32_t *bundles_host);
+/* One launch over all filters.  order_dev / bundles_dev are the planner's
+ * arrays copied to the device; counter_dev is one int32 of scratch (reset by
+ * the call).  logz_dev (B,) receives log Z_b, nres_dev (B,) the number of
+ * resampling steps (may be NULL).  Graph-capturable. */
+int mgb_pf_sv_batch_run(const mgb_sv_model *model_host, int64_t B, const int32_t *n_dev, const int32_t *T_dev,
+                        const int64_t *y_off_dev, const float *y_dev, const uint32_t *keys_dev,
+                        const mgb_sv_launch *launch, const int32_t *order_dev, const int32_t *bundles_dev,
+                        float ess_threshold, int scheme, int32_t *counter_dev, double *logz_dev, int32_t *nres_dev,
+                        int32_t *err_dev, void *stream);
+/* Autotuner: times every candidate launch shape on this batch, each filter cut
+ * to probe_steps steps (<= 0: full length), and writes the fastest to *best.
+ * Results are cached per (device, scheme, batch signature) behind a mutex.
+ * Needs mgb_pf_sv_batch_autotune_workspace(B) bytes of device scratch;
+ * synchronises `stream`; not capturable. */
+size_t mgb_pf_sv_batch_autotune_workspace(int64_t B);
+int mgb_pf_sv_batch_autotune(const mgb_sv_model *model_host, int64_t B, const int32_t *n_host, const int32_t *T_host,
+                             const int32_t *n_dev, const int32_t *T_dev, const int64_t *y_off_dev, const float *y_dev,
+                             const uint32_t *keys_dev, float ess_threshold, int scheme, int32_t probe_steps,
+                             void *ws_dev, size_t ws_bytes, mgb_sv_launch *best, float *best_ms, void *stream);
 
 #ifdef __cplusplus
 }

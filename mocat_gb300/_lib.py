@@ -30,6 +30,16 @@ class PFOutputs(ctypes.Structure):
                 ("lw_final", ctypes.c_void_p), ("err", ctypes.c_void_p), ("trace", ctypes.c_void_p)]
 
 
+class SVModel(ctypes.Structure):
+    _fields_ = [("phi", ctypes.c_float), ("bsig", ctypes.c_float), ("r2", ctypes.c_float), ("cB", ctypes.c_float),
+                ("c0", ctypes.c_float), ("m0", ctypes.c_float)]
+
+
+class SVLaunch(ctypes.Structure):
+    _fields_ = [("threads", ctypes.c_int32), ("ppt", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32),
+                ("nbundles", ctypes.c_int32), ("smem_bytes", ctypes.c_int64)]
+
+
 _P = ctypes.c_void_p
 _I64 = ctypes.c_int64
 _I32 = ctypes.c_int
@@ -59,6 +69,12 @@ _SIGNATURES = {
     "mgb_pf_lg_workspace": ([_I64, _I64, ctypes.c_int32, _I32], _SZ),
     "mgb_pf_lg_run": ([ctypes.POINTER(LGModel), _I64, _I64, _P, _P, _F, _I32, _P, _SZ, ctypes.POINTER(PFOutputs), _P],
                       _I32),
+    "mgb_pf_sv_batch_plan": ([_I64, _P, _P, ctypes.POINTER(SVLaunch), _P, _P], _I32),
+    "mgb_pf_sv_batch_run": ([ctypes.POINTER(SVModel), _I64, _P, _P, _P, _P, _P, ctypes.POINTER(SVLaunch), _P, _P, _F,
+                             _I32, _P, _P, _P, _P, _P], _I32),
+    "mgb_pf_sv_batch_autotune_workspace": ([_I64], _SZ),
+    "mgb_pf_sv_batch_autotune": ([ctypes.POINTER(SVModel), _I64, _P, _P, _P, _P, _P, _P, _P, _F, _I32, ctypes.c_int32,
+                                  _P, _SZ, ctypes.POINTER(SVLaunch), ctypes.POINTER(ctypes.c_float), _P], _I32),
 }
 
 

@@ -142,6 +142,50 @@ class TimeHomogenousLinearGaussian(StateSpaceModel):
                      t=torch.as_tensor(np.asarray(t_all), device=dev), name=f"{self.name} simulation")
 
 
+class StochasticVolatility(StateSpaceModel):
+    """x_t ~ N(A x_{t-1}, Q dt), y_t ~ N(0, R exp(x_t)) elementwise
+    (mocat/src/ssm/scenarios/stochastic_volatility.py:15-108).  The GPU kernels
+    take dim = 1 (many independent series run as a batch)."""
+    name = "Stochastic Volatility"
+    _PARAMS = ("initial_mean", "initial_covariance", "transition_matrix", "transition_covariance",
+               "likelihood_covariance_diag")
+
+    def __init__(self, dim=1, initial_mean=None, initial_covariance=None, transition_matrix=None,
+                 transition_covariance=None, likelihood_covariance_diag=None, name=None):
+        super().__init__(name=name)
+        self.dim = dim
+        self.dim_obs = dim
+        self.initial_mean = np.zeros(dim) if initial_mean is None else _np(initial_mean).reshape(dim)
+        self.initial_covariance = np.eye(dim) if initial_covariance is None else _as_matrix(initial_covariance, dim)
+        self.transition_matrix = np.eye(dim) if transition_matrix is None else _as_matrix(transition_matrix, dim)
+        self.transition_covariance = (np.eye(dim) if transition_covariance is None
+                                      else _as_matrix(transition_covariance, dim))
+        lcd = np.ones(dim) if likelihood_covariance_diag is None else _np(likelihood_covariance_diag)
+        self.likelihood_covariance_diag = np.diag(lcd) if lcd.ndim == 2 else lcd.reshape(dim)
+
+    def __setattr__(self, key, value):
+        self.__dict__[key] = value
+        if key in self._PARAMS:
+            self.__dict__.pop("_derived", None)
+
+    def derived(self, dt=1.0):
+        """float32 constants of the d = 1 kernels and the C-ABI struct:
+        phi = A, bsig = sqrt(Q) sqrt(dt), r2 = 1 / R, cB = (log 2 pi - log r2) / 2,
+        c0 = sqrt(initial_covariance), m0 = initial_mean."""
+        if self.dim != 1:
+            raise NotImplementedError("StochasticVolatility: the GPU kernels take dim = 1")
+        if "_derived" not in self.__dict__ or self.__dict__["_derived"][0]["dt"] != dt:
+            r2 = np.float32(1.0 / float(self.likelihood_covariance_diag[0]))
+            p = dict(dt=dt, phi=np.float32(self.transition_matrix[0, 0]),
+                     bsig=np.float32(np.float32(np.sqrt(self.transition_covariance[0, 0])) * np.float32(np.sqrt(dt))),
+                     r2=r2, cB=np.float32(0.5 * (LOG2PI - np.log(r2))),
+                     c0=np.float32(np.sqrt(self.initial_covariance[0, 0])), m0=np.float32(self.initial_mean[0]),
+                     sqrtR=np.float32(np.sqrt(float(self.likelihood_covariance_diag[0]))))
+            s = _lib.SVModel(*(float(p[k]) for k in ("phi", "bsig", "r2", "cB", "c0", "m0")))
+            self.__dict__["_derived"] = (p, s)
+        return self.__dict__["_derived"]
+
+
 def _normal_keys(keys, d):
     keys = _dev.as_key(keys)
     out = torch.empty((keys.shape[0], d), dtype=torch.float32, device=keys.device)
