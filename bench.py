@@ -23,6 +23,12 @@ Metric: particle-steps/s (higher is better).
 JAX and is not installable here) on the same workload, all host threads.
 Multi-GPU (torchrun): independent replicas, one filter per rank, no
 collective on the data path; value = all ranks' particle-steps / max time.
+
+batched_sv -- a second workload in the same line: 4096 independent
+stochastic-volatility filters of uneven length and size in one persistent
+launch (graph replay; e2e with the observations copied from pinned host
+memory and log Z read back), with the oracle's C/OpenMP batch on a sample of
+the series as its CPU baseline.
 """
 import argparse
 import ctypes
@@ -127,6 +133,91 @@ def cpu_baseline(n, steps, threads=None):
     return n * steps / dt, oracle.num_threads(), dt
 
 
+SV_WORKLOAD = ("4096 independent stochastic-volatility bootstrap filters (phi=0.95, sigma=0.3, R=1, "
+               "x0~N(0, sigma^2/(1-phi^2))), T_b~U{50..2000}, N_b=2^U{9..13}, seeded; multinomial resampling at "
+               "ESS<0.5N_b; one persistent launch, CUDA-graph replay, autotuned launch shape")
+
+
+def sv_cpu_baseline(ns, y, T, keys, p, nfilt):
+    """oracle o_sv_batch (C/OpenMP, one filter per thread) on the first nfilt filters."""
+    import oracle
+    oracle.build()
+    off = np.concatenate([[0], np.cumsum(T.astype(np.int64))])
+    t0 = time.perf_counter()
+    oracle.sv_batch(p, ns[:nfilt], T[:nfilt], off[:nfilt], y[:off[nfilt]], keys[:nfilt], 0.5, "multinomial")
+    dt = time.perf_counter() - t0
+    return float((ns[:nfilt].astype(np.int64) * T[:nfilt]).sum()) / dt, oracle.num_threads(), dt
+
+
+def bench_sv_batch(args, flush, rank):
+    """The batched stochastic-volatility workload: device-resident graph replay,
+    end to end with host observations, and the oracle on a sample of the series."""
+    import torch
+    import mocat_gb300 as mg
+    ns, y, T, keys = mg.batched.synthetic_sv_batch(4096, seed=rank)
+    keys = keys.copy()
+    sc = mg.ssm.StochasticVolatility(dim=1, initial_covariance=0.3 ** 2 / (1 - 0.95 ** 2), transition_matrix=0.95,
+                                     transition_covariance=0.09, likelihood_covariance_diag=1.0)
+    t0 = time.perf_counter()
+    bf = mg.batched.BatchedFilters(sc, mg.ssm.BootstrapFilter(), ns, y, keys, lengths=T, resampling="multinomial",
+                                   tune=True, probe_steps=128, pin_y=True)
+    tune_s = time.perf_counter() - t0
+    work = bf.particle_steps
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        bf.enqueue()
+    torch.cuda.current_stream().wait_stream(side)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        bf.enqueue()
+    for _ in range(args.warmup):
+        flush.zero_()
+        g.replay()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        g.replay()
+        e1.record()
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+    t_dev = statistics.median(times)
+    lz = bf.log_z.cpu().numpy()
+    nres = bf.resampled_count.cpu().numpy()
+    e2e_t = []
+    for _ in range(max(2, args.steps // 2)):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        out = bf.run(copy_in=True)
+        lz_h = out.log_z.cpu()
+        e1.record()
+        torch.cuda.synchronize()
+        e2e_t.append(e0.elapsed_time(e1) / 1e3)
+    assert np.array_equal(lz_h.numpy(), lz)
+    res = {"workload": SV_WORKLOAD, "metric": METRIC, "value": work / t_dev, "unit": "particle-steps/s",
+           "ms_per_step": t_dev * 1e3, "particle_steps_per_run": work, "kernel": "k_sv_batch (one launch per run)",
+           "launch": bf.plan, "autotune_s": tune_s, "resample_fraction": float(nres.sum() / T.sum()),
+           "log_z_finite": bool(np.isfinite(lz).all()),
+           "e2e": {"value": work / statistics.median(e2e_t), "unit": "particle-steps/s",
+                   "h2d_bytes_per_step": int(y.nbytes), "d2h_bytes_per_step": int(lz.nbytes)},
+           "gpu_launches_per_step": 1,
+           "bound": "SM issue (threefry / erfinv / exp on-chip; particles live in shared memory, HBM traffic is "
+                    "the observations)"}
+    if rank == 0:
+        p, _ = sc.derived()
+        v_cpu, cores, dt = sv_cpu_baseline(ns, y, T, keys, p, args.sv_cpu_filters)
+        res["cpu_baseline"] = {"value": v_cpu, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+                               "sample": f"first {args.sv_cpu_filters} of the 4096 series ({dt:.1f} s), oracle "
+                                         "o_sv_batch C/OpenMP"}
+    return res
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
@@ -159,6 +250,8 @@ def main():
     ap.add_argument("--ref-steps", type=int, default=20)
     ap.add_argument("--cpu-steps", type=int, default=10)
     ap.add_argument("--kernel-iters", type=int, default=50)
+    ap.add_argument("--sv-cpu-filters", type=int, default=256)
+    ap.add_argument("--no-batched", action="store_true")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -321,6 +414,8 @@ def main():
                                               "frac": k_alg / k_t / 1e9 / peak}},
             "gpu_launches": args.steps * 3,  # k_setup_keys, k_pf_lg_persist, k_or_err per run
             "clocks": clk.summary()}
+    if not args.no_batched:
+        line["batched_sv"] = bench_sv_batch(args, flush, rank)
     if rank == 0:
         v_cpu, cores, dt = cpu_baseline(n, args.cpu_steps)
         line["cpu_baseline"] = {"value": v_cpu, "unit": "particle-steps/s", "cores": cores, "kind": "port",
