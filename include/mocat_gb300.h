@@ -173,6 +173,42 @@ int mgb_pf_lg_run(const mgb_lg_model *model_host, int64_t n, int64_t T, const ui
                   float ess_threshold, int scheme, void *ws_dev, size_t ws_bytes, const mgb_pf_outputs *out,
                   void *stream);
 
+/* ------------------------------------ particle filter, optimal proposal
+ * OptimalNonLinearGaussianParticleFilter (mocat/src/ssm/nonlinear_gaussian.py:134-281)
+ * for a linear transition f(x) = F x with linear-Gaussian observations:
+ *   init:  x_0 = (m0 + K0 (y_0 - H m0)) + eps C0c, lw_0 = 0
+ *   step:  mx = F x_prev[a_i], r = y_t - H mx,
+ *          x_new = (mx + K r) + S eps_i, lw_new = lw_res - (0.5 |r W|^2 + cw)
+ * with eps = normal(split(k, n)[0], (n, d)) -- one key for the whole (n, d)
+ * draw (nonlinear_gaussian.py:275).  Matrices are host pointers, row-major
+ * float32, computed as the reference's startup (:154-184) does:
+ *   F (d x d) transition matrix; H (dy x d) likelihood_matrix;
+ *   K (d x dy) proposal_kalman_gain; S (d x d) proposal_covariance_sqrt;
+ *   W (dy x dy) weight_precision_sqrt; cw = (dy log 2 pi - log weight_precision_det) / 2;
+ *   K0 (d x dy) initial_kalman_gain; C0c (d x d) initial_conditioned_covariance_sqrt;
+ *   m0 (d) initial_mean.
+ * Supported (d, dy) as for mgb_lg_model; n d < 2^32.
+ */
+typedef struct {
+  int32_t d, dy;
+  const float *F, *H, *K, *S, *W;
+  float cw;
+  const float *K0, *C0c, *m0;
+} mgb_opt_model;
+
+int mgb_pf_opt_init(const mgb_opt_model *model_host, int64_t n, const uint32_t *key_dev, const float *y0_dev,
+                    float *x_dev, float *lw_dev, void *stream);
+/* propose_and_intermediate_weight_vectorised (nonlinear_gaussian.py:264-281) for one step;
+ * ancestors_dev == NULL: no resampling; lw_prev_dev == NULL: 0 */
+int mgb_pf_opt_propagate(const mgb_opt_model *model_host, int64_t n, const uint32_t *key_t_dev, const float *y_t_dev,
+                         const float *x_prev_dev, const int32_t *ancestors_dev, const float *lw_prev_dev,
+                         float *x_new_dev, float *lw_new_dev, void *stream);
+/* run_particle_filter_for_marginals with this filter (launch per step; outputs as mgb_pf_lg_run) */
+size_t mgb_pf_opt_workspace(int64_t n, int64_t T, int32_t d, int scheme);
+int mgb_pf_opt_run(const mgb_opt_model *model_host, int64_t n, int64_t T, const uint32_t *key_dev, const float *y_dev,
+                   float ess_threshold, int scheme, void *ws_dev, size_t ws_bytes, const mgb_pf_outputs *out,
+                   void *stream);
+
 /* ------------------------------- many stochastic-volatility filters at once
  * B independent run_particle_filter_for_marginals calls (mocat/src/ssm/filtering.py:255-324)
  * with BootstrapFilter on StochasticVolatility, d = 1

@@ -30,6 +30,12 @@ class PFOutputs(ctypes.Structure):
                 ("lw_final", ctypes.c_void_p), ("err", ctypes.c_void_p), ("trace", ctypes.c_void_p)]
 
 
+class OptModel(ctypes.Structure):
+    _fields_ = [("d", ctypes.c_int32), ("dy", ctypes.c_int32), ("F", ctypes.c_void_p), ("H", ctypes.c_void_p),
+                ("K", ctypes.c_void_p), ("S", ctypes.c_void_p), ("W", ctypes.c_void_p), ("cw", ctypes.c_float),
+                ("K0", ctypes.c_void_p), ("C0c", ctypes.c_void_p), ("m0", ctypes.c_void_p)]
+
+
 class SVModel(ctypes.Structure):
     _fields_ = [("phi", ctypes.c_float), ("bsig", ctypes.c_float), ("r2", ctypes.c_float), ("cB", ctypes.c_float),
                 ("c0", ctypes.c_float), ("m0", ctypes.c_float)]
@@ -69,6 +75,11 @@ _SIGNATURES = {
     "mgb_pf_lg_workspace": ([_I64, _I64, ctypes.c_int32, _I32], _SZ),
     "mgb_pf_lg_run": ([ctypes.POINTER(LGModel), _I64, _I64, _P, _P, _F, _I32, _P, _SZ, ctypes.POINTER(PFOutputs), _P],
                       _I32),
+    "mgb_pf_opt_init": ([ctypes.POINTER(OptModel), _I64, _P, _P, _P, _P, _P], _I32),
+    "mgb_pf_opt_propagate": ([ctypes.POINTER(OptModel), _I64, _P, _P, _P, _P, _P, _P, _P, _P], _I32),
+    "mgb_pf_opt_workspace": ([_I64, _I64, ctypes.c_int32, _I32], _SZ),
+    "mgb_pf_opt_run": ([ctypes.POINTER(OptModel), _I64, _I64, _P, _P, _F, _I32, _P, _SZ, ctypes.POINTER(PFOutputs),
+                        _P], _I32),
     "mgb_pf_sv_batch_plan": ([_I64, _P, _P, ctypes.POINTER(SVLaunch), _P, _P], _I32),
     "mgb_pf_sv_batch_run": ([ctypes.POINTER(SVModel), _I64, _P, _P, _P, _P, _P, ctypes.POINTER(SVLaunch), _P, _P, _F,
                              _I32, _P, _P, _P, _P, _P], _I32),

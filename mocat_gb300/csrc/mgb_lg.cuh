@@ -19,28 +19,6 @@ struct LGP {
   uint32_t one;  // == 1: multiplier of the cipher's multiply-adds (see threefry2x32_m)
 };
 
-struct PFState {
-  double logz;
-  double lse_prev;
-  float M;
-  int pad;
-};
-
-// per-run control block passed by value to the fused kernels
-struct PFCtl {
-  LsePartial *parts;
-  unsigned int *counter;
-  PFState *st;
-  float *ess_hist;     // (T,)
-  int32_t *res_hist;   // (T+1,): entry t = 1 if step t resamples
-  ResampleCtl *rctl;   // cleared by the finalising block for the next step
-  uint64_t *rstatus, *rstatus2;
-  int ntiles;
-  float thr_n;         // ess_threshold * n (float32, as the reference compares)
-  double logn;
-  double *logz_out;
-};
-
 template <int D, int DY>
 __device__ __forceinline__ float lg_potential(const LGP<D, DY> &p, const float (&x)[D], const float *y) {
   float diff[DY];

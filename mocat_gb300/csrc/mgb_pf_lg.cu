@@ -29,56 +29,9 @@
 #include "mgb_kernels.cuh"
 #include "mgb_lg.cuh"
 #include "mgb_persist.cuh"
+#include "mgb_pf_common.cuh"
 
 namespace mgb {
-
-constexpr int PF_TPB = 256;
-
-// last block: combine partials, update the running state, clear scratch
-template <int TPB>
-__device__ __forceinline__ void pf_finalize(const PFCtl &ctl, int64_t t, float *smf, double *smd) {
-  const LseOut o = combine_lse<TPB>(ctl.parts, gridDim.x, smf, smd);
-  if (threadIdx.x == 0) {
-    PFState *st = ctl.st;
-    const int res_t = t == 0 ? 0 : ctl.res_hist[t];
-    const double logz = t == 0 ? o.lse - ctl.logn : st->logz + o.lse - (res_t ? ctl.logn : st->lse_prev);
-    st->logz = logz;
-    st->lse_prev = o.lse;
-    st->M = o.M;
-    ctl.ess_hist[t] = (float)o.ess;
-    ctl.res_hist[t + 1] = ((float)o.ess < ctl.thr_n) ? 1 : 0;
-    if (ctl.logz_out) *ctl.logz_out = logz;
-    *ctl.counter = 0u;
-    ctl.rctl->tile_counter = 0u;
-    ctl.rctl->tile_counter2 = 0u;
-    ctl.rctl->degenerate = 0;
-    ctl.rctl->total = 0ull;
-  }
-  for (int j = threadIdx.x; j < ctl.ntiles; j += TPB) {
-    ctl.rstatus[j] = 0ull;
-    ctl.rstatus2[j] = 0ull;
-  }
-  if (threadIdx.x == 0) ctl.rctl->units = 0u;
-}
-
-// block partial + (optionally) last-block finalize
-template <int TPB>
-__device__ __forceinline__ void pf_reduce(float lw, bool active, const PFCtl &ctl, int64_t t) {
-  __shared__ float smf[TPB / 32];
-  __shared__ double smd[TPB / 32];
-  __shared__ bool last;
-  const bool nan = active && lw != lw;
-  const LsePartial part = block_lse_partial<TPB>(active && !nan ? lw : -INFINITY, nan, smf, smd);
-  if (threadIdx.x == 0) {
-    ctl.parts[blockIdx.x] = part;
-    __threadfence();
-    last = atomicAdd(ctl.counter, 1u) == gridDim.x - 1;
-  }
-  __syncthreads();
-  if (!last) return;
-  __threadfence();
-  pf_finalize<TPB>(ctl, t, smf, smd);
-}
 
 // initiate_particles: x_0 = C0 eps + m0, lw_0 = -potential(x_0, y_0)
 template <int D, int DY, bool FUSED>
@@ -148,23 +101,6 @@ __global__ void __launch_bounds__(PF_TPB) k_lg_step(const __grid_constant__ LGP<
 // key of particle i is (T(2i, 2i+n).x0, T(2i+1, 2i+1+n).x0) and the key of
 // particle i + n/2 is the .x1 halves of the same two cipher calls, so the
 // pair costs two key-split evaluations instead of four.
-template <int TPB>
-__device__ __forceinline__ void pf_reduce_online(float m, float s1, float s2, int nanf, const PFCtl &ctl, int64_t t) {
-  __shared__ float smf[TPB / 32];
-  __shared__ double smd[TPB / 32];
-  __shared__ bool last;
-  const LsePartial part = block_online_partial<TPB>(m, s1, s2, nanf, smf);
-  if (threadIdx.x == 0) {
-    ctl.parts[blockIdx.x] = part;
-    __threadfence();
-    last = atomicAdd(ctl.counter, 1u) == gridDim.x - 1;
-  }
-  __syncthreads();
-  if (!last) return;
-  __threadfence();
-  pf_finalize<TPB>(ctl, t, smf, smd);
-}
-
 template <int D, int DY, bool FUSED>
 __global__ void __launch_bounds__(PF_TPB, 2) k_lg_step2(const __grid_constant__ LGP<D, DY> p, int64_t n,
                                                          const uint32_t *key, const float *y_t,
@@ -224,34 +160,16 @@ __global__ void k_finish(const PFState *st, const int32_t *res_hist, int64_t T, 
   }
 }
 
-// ------------------------------------------------------------- host side
-struct RunWs {
-  uint32_t *keys;
-  PFState *st;
-  LsePartial *parts;
-  unsigned int *counter;
-  int32_t *res_hist;
-  float *ess_hist;
-  float *xa, *xb, *la, *lb;
-  int32_t *anc;
-  ResampleWs rws;
-};
 
-static RunWs carve_run(Carver &c, int64_t n, int64_t T, int d, int scheme, bool need_x, bool need_lw, bool need_ess) {
-  RunWs w;
-  w.keys = c.take<uint32_t>(2 * (size_t)T);
-  w.st = c.take<PFState>(1);
-  w.parts = c.take<LsePartial>((size_t)((n + PF_TPB - 1) / PF_TPB));
-  w.counter = c.take<unsigned int>(1);
-  w.res_hist = c.take<int32_t>((size_t)T + 1);
-  w.ess_hist = need_ess ? c.take<float>((size_t)T) : nullptr;
-  w.xa = need_x ? c.take<float>((size_t)d * n) : nullptr;
-  w.xb = need_x ? c.take<float>((size_t)d * n) : nullptr;
-  w.la = need_lw ? c.take<float>((size_t)n) : nullptr;
-  w.lb = need_lw ? c.take<float>((size_t)n) : nullptr;
-  w.anc = c.take<int32_t>((size_t)n);
-  w.rws = carve_resample(c, n, scheme);
-  return w;
+int launch_setup_keys(const uint32_t *key, int64_t T, uint32_t *out, cudaStream_t s) {
+  k_setup_keys<<<grid_for(T, 256), 256, 0, s>>>(key, T, out);
+  return launch_status();
+}
+
+int launch_finish(const PFState *st, const int32_t *res_hist, int64_t T, double *logz, int32_t *resampled,
+                  cudaStream_t s) {
+  k_finish<<<grid_for(T, 256), 256, 0, s>>>(st, res_hist, T, logz, resampled);
+  return launch_status();
 }
 
 // Persistent path: systematic resampling, even n, n <= 2^21 (tile prefixes in smem).

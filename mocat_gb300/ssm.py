@@ -212,13 +212,71 @@ class BootstrapFilter(ParticleFilter):
     name = "Bootstrap Filter"
 
 
+class OptimalNonLinearGaussianParticleFilter(ParticleFilter):
+    """Optimal proposal for linear-Gaussian observations
+    (mocat/src/ssm/nonlinear_gaussian.py:134-281), on the GPU for a linear
+    transition f(x) = F x (a TimeHomogenousLinearGaussian scenario).  startup
+    computes the reference's constants (:154-184) in float64 and keeps float32
+    copies for the kernels."""
+    name = "Optimal Non-linear Gaussian Particle Filter"
+
+    def startup(self, ssm_scenario):
+        p, _ = ssm_scenario.derived()
+        S0 = ssm_scenario.initial_covariance
+        Q = ssm_scenario.transition_covariance
+        H = ssm_scenario.likelihood_matrix
+        R = ssm_scenario.likelihood_covariance
+        C0 = np.linalg.cholesky(S0)
+        init_prec_sqrt = np.linalg.inv(C0)
+        Lq = np.linalg.cholesky(Q)
+        LR = np.linalg.cholesky(R)
+        lik_prec_sqrt = np.linalg.inv(LR)
+
+        def kalman_gain(cov_sqrt, inv_mat=None):
+            if inv_mat is None:
+                hc = H @ cov_sqrt
+                inv_mat = np.linalg.inv(hc @ hc.T + LR @ LR.T)
+            return cov_sqrt @ cov_sqrt.T @ H.T @ inv_mat
+
+        self.initial_kalman_gain = kalman_gain(C0)
+        a = H.T @ lik_prec_sqrt
+        init_cond_prec = init_prec_sqrt @ init_prec_sqrt + a @ a.T
+        self.initial_conditioned_precision_sqrt = np.linalg.cholesky(init_cond_prec)
+        self.initial_conditioned_covariance_sqrt = np.linalg.inv(self.initial_conditioned_precision_sqrt)
+        hl = H @ Lq
+        weight_precision = np.linalg.inv(hl @ hl.T + LR @ LR.T)
+        self.proposal_kalman_gain = kalman_gain(Lq, weight_precision)
+        prop_cov = Q - self.proposal_kalman_gain @ H @ Q
+        self.proposal_covariance_sqrt = np.linalg.cholesky(prop_cov)
+        self.weight_precision_sqrt = np.linalg.cholesky(weight_precision)
+        self.weight_precision_det = np.linalg.det(weight_precision)
+        dy = H.shape[0]
+        c = dict(d=p["d"], dy=dy, F=p["F"], H=p["H"], K=_f32(self.proposal_kalman_gain),
+                 S=_f32(self.proposal_covariance_sqrt), W=_f32(self.weight_precision_sqrt),
+                 cw=np.float32((dy * LOG2PI - np.log(self.weight_precision_det)) / 2.0),
+                 K0=_f32(self.initial_kalman_gain), C0c=_f32(self.initial_conditioned_covariance_sqrt), m0=p["m0"])
+        self._consts = c
+        self._struct = _lib.OptModel(c["d"], c["dy"], c["F"].ctypes.data, c["H"].ctypes.data, c["K"].ctypes.data,
+                                     c["S"].ctypes.data, c["W"].ctypes.data, float(c["cw"]), c["K0"].ctypes.data,
+                                     c["C0c"].ctypes.data, c["m0"].ctypes.data)
+
+
 def _check_lg(ssm_scenario, particle_filter):
     if not isinstance(ssm_scenario, TimeHomogenousLinearGaussian):
         raise NotImplementedError(f"{ssm_scenario.__class__.__name__}: no fused GPU kernel for this model")
-    if not isinstance(particle_filter, BootstrapFilter):
+    if not isinstance(particle_filter, (BootstrapFilter, OptimalNonLinearGaussianParticleFilter)):
         raise NotImplementedError(f"{particle_filter.__class__.__name__}: no fused GPU kernel for this filter")
     if not ssm_scenario.gpu_supported():
         raise NotImplementedError(f"(d, dy) = ({ssm_scenario.dim}, {ssm_scenario.dim_obs}) not compiled")
+
+
+def _kernels(ssm_scenario, particle_filter):
+    """(C-ABI prefix, model struct) of the fused kernels for this scenario / filter pair."""
+    if isinstance(particle_filter, OptimalNonLinearGaussianParticleFilter):
+        if getattr(particle_filter, "_struct", None) is None:
+            particle_filter.startup(ssm_scenario)
+        return "mgb_pf_opt", particle_filter._struct
+    return "mgb_pf_lg", ssm_scenario.derived()[1]
 
 
 def _y2(y, dy):
@@ -230,14 +288,14 @@ def initiate_particles(ssm_scenario, particle_filter, n, random_key, y=None, t=N
     """filtering.py:173-193: particles (1, n, d), log-weights (1, n), ess (1,)."""
     _check_lg(ssm_scenario, particle_filter)
     particle_filter.startup(ssm_scenario)
-    _, s = ssm_scenario.derived()
+    prefix, s = _kernels(ssm_scenario, particle_filter)
     d = ssm_scenario.dim
     dev = _dev.device()
     key = _dev.as_key(random_key)
     x = torch.empty((d, n), dtype=torch.float32, device=dev)
     lw = torch.empty(n, dtype=torch.float32, device=dev)
     yd = None if y is None else _y2(y, ssm_scenario.dim_obs).reshape(-1)
-    call("mgb_pf_lg_init", ctypes.byref(s), n, _dev.ptr(key), _dev.ptr(yd), _dev.ptr(x), _dev.ptr(lw),
+    call(prefix + "_init", ctypes.byref(s), n, _dev.ptr(key), _dev.ptr(yd), _dev.ptr(x), _dev.ptr(lw),
          _dev.stream_ptr())
     return cdict(value=x.t().contiguous()[None], log_weight=lw[None],
                  t=torch.atleast_1d(torch.as_tensor(0.0 if t is None else t, device=dev)),
@@ -265,11 +323,10 @@ def resample_particles(particles, random_key, resample_full=True, resampling="sy
     return out
 
 
-def _step(s, n, key, y_t, x_prev_soa, anc, lw_prev):
-    d = x_prev_soa.shape[0]
+def _step(s, n, key, y_t, x_prev_soa, anc, lw_prev, prefix="mgb_pf_lg"):
     x_new = torch.empty_like(x_prev_soa)
     lw_new = torch.empty(n, dtype=torch.float32, device=x_prev_soa.device)
-    call("mgb_pf_lg_propagate", ctypes.byref(s), n, _dev.ptr(key), _dev.ptr(y_t), _dev.ptr(x_prev_soa),
+    call(prefix + "_propagate", ctypes.byref(s), n, _dev.ptr(key), _dev.ptr(y_t), _dev.ptr(x_prev_soa),
          _dev.ptr(anc), _dev.ptr(lw_prev), _dev.ptr(x_new), _dev.ptr(lw_new), _dev.stream_ptr())
     return x_new, lw_new
 
@@ -278,7 +335,7 @@ def propagate_particle_filter(ssm_scenario, particle_filter, particles, y_new, t
                               ess_threshold=0.5, resample_full=True, resampling="systematic"):
     """filtering.py:220-252: resample if ess < threshold n, then propagate and append."""
     _check_lg(ssm_scenario, particle_filter)
-    _, s = ssm_scenario.derived()
+    prefix, s = _kernels(ssm_scenario, particle_filter)
     n = particles.value.shape[1]
     key = _dev.as_key(random_key)
     if float(particles.ess[-1]) < ess_threshold * n:
@@ -286,7 +343,7 @@ def propagate_particle_filter(ssm_scenario, particle_filter, particles, y_new, t
     x_prev = particles.value[-1].t().contiguous()
     lw_prev = particles.log_weight[-1].contiguous()
     y_t = _y2(y_new, ssm_scenario.dim_obs).reshape(-1)
-    x_new, lw_new = _step(s, n, key, y_t, x_prev, None, lw_prev)
+    x_new, lw_new = _step(s, n, key, y_t, x_prev, None, lw_prev, prefix)
     out = particles.copy()
     out.value = torch.cat([particles.value, x_new.t()[None]], 0)
     out.log_weight = torch.cat([particles.log_weight, lw_new[None]], 0)
@@ -308,16 +365,16 @@ def run_particle_filter_for_marginals(ssm_scenario, particle_filter, y, t, rando
     """
     _check_lg(ssm_scenario, particle_filter)
     particle_filter.startup(ssm_scenario)
-    _, s = ssm_scenario.derived()
+    prefix, s = _kernels(ssm_scenario, particle_filter)
     d, dy = ssm_scenario.dim, ssm_scenario.dim_obs
     dev = _dev.device()
     y2 = _y2(y, dy)
     key = _dev.as_key(random_key)
     sc = SCHEMES[resampling]
     if initial_sample is not None:
-        return _run_from(ssm_scenario, s, initial_sample, y2, t, key, ess_threshold, resampling)
+        return _run_from(ssm_scenario, s, initial_sample, y2, t, key, ess_threshold, resampling, prefix)
     T = y2.shape[0]
-    ws = _dev.workspace(_lib.lib().mgb_pf_lg_workspace(n, T, d, sc), dev)
+    ws = _dev.workspace(getattr(_lib.lib(), prefix + "_workspace")(n, T, d, sc), dev)
     logz = torch.empty(1, dtype=torch.float64, device=dev)
     ess = torch.empty(T, dtype=torch.float32, device=dev)
     res = torch.empty(T, dtype=torch.int32, device=dev)
@@ -327,8 +384,8 @@ def run_particle_filter_for_marginals(ssm_scenario, particle_filter, y, t, rando
     out = _lib.PFOutputs(logz.data_ptr(), ess.data_ptr(), res.data_ptr(), xh.data_ptr() if history else None,
                          lh.data_ptr() if history else None, None if history else xh.data_ptr(),
                          None if history else lh.data_ptr(), err.data_ptr(), None)
-    flags = 0 if persistent else RUN_LAUNCH_PER_STEP
-    call("mgb_pf_lg_run", ctypes.byref(s), n, T, _dev.ptr(key), _dev.ptr(y2), float(ess_threshold), sc | flags,
+    flags = 0 if (persistent or prefix != "mgb_pf_lg") else RUN_LAUNCH_PER_STEP
+    call(prefix + "_run", ctypes.byref(s), n, T, _dev.ptr(key), _dev.ptr(y2), float(ess_threshold), sc | flags,
          _dev.ptr(ws), ws.numel(), ctypes.byref(out), _dev.stream_ptr())
     e = int(err.item())
     if e & 1:
@@ -338,7 +395,7 @@ def run_particle_filter_for_marginals(ssm_scenario, particle_filter, y, t, rando
                  resampled=res.bool(), degenerate=bool(e & 2))
 
 
-def _run_from(ssm_scenario, s, initial_sample, y2, t, key, ess_threshold, resampling):
+def _run_from(ssm_scenario, s, initial_sample, y2, t, key, ess_threshold, resampling, prefix="mgb_pf_lg"):
     """Resume from given particles (filtering.py:266-275 with initial_sample set)."""
     x = initial_sample.value[-1].t().contiguous()
     lw = initial_sample.log_weight[-1].contiguous()
@@ -352,7 +409,7 @@ def _run_from(ssm_scenario, s, initial_sample, y2, t, key, ess_threshold, resamp
     for i in range(T):
         res = ess < ess_threshold * n
         anc = resample(lw, keys[i], resampling) if res else None
-        x, lw = _step(s, n, keys[i], y2[i], x, anc, None if res else lw)
+        x, lw = _step(s, n, keys[i], y2[i], x, anc, None if res else lw, prefix)
         lse = float(torch.logsumexp(lw.double(), 0))
         logz += lse - (math.log(n) if res else lse_prev)
         lse_prev = lse

@@ -296,6 +296,29 @@ def _opt_struct(p):
     return s, keep
 
 
+def opt_init(params, n, key, y0):
+    """initial_sample of the optimal-proposal filter (nonlinear_gaussian.py:198-209); weights 0."""
+    s, keep = _opt_struct(params)
+    x = np.empty((n, params["d"]), np.float32)
+    lw = np.empty(n, np.float32)
+    lib().o_opt_init(ctypes.byref(s), n, _u32(key), _f32(y0), x.reshape(-1), lw)
+    return x, lw
+
+
+def opt_propagate(params, key_t, y, x_prev, anc=None, lw_prev=None):
+    """propose_and_intermediate_weight_vectorised (nonlinear_gaussian.py:264-281)."""
+    s, keep = _opt_struct(params)
+    x_prev = _f32(x_prev)
+    n = x_prev.shape[0]
+    x_new = np.empty_like(x_prev)
+    lw_new = np.empty(n, np.float32)
+    anc = None if anc is None else np.ascontiguousarray(anc, dtype=np.int32)
+    lw_prev = None if lw_prev is None else _f32(lw_prev)
+    lib().o_opt_propagate(ctypes.byref(s), n, _u32(key_t), _f32(y), x_prev.reshape(-1), _ptr(anc), _ptr(lw_prev),
+                          x_new.reshape(-1), lw_new)
+    return x_new, lw_new
+
+
 def opt_run(params, n, key, y, ess_threshold=0.5, scheme="systematic", history=False):
     s, keep = _opt_struct(params)
     y = _f32(y).reshape(len(y), -1)
