@@ -173,6 +173,22 @@ int mgb_pf_lg_run(const mgb_lg_model *model_host, int64_t n, int64_t T, const ui
                   float ess_threshold, int scheme, void *ws_dev, size_t ws_bytes, const mgb_pf_outputs *out,
                   void *stream);
 
+/* ----------------------------------------------- adjoint: d log Z / d theta
+ * Gradient of the bootstrap filter's log Z (run_particle_filter_for_marginals,
+ * mocat/src/ssm/filtering.py:255-324, as mgb_pf_lg_run) with the ancestors and
+ * resampling decisions held fixed, for a model with H = I and diagonal Lq, P:
+ * theta = (A = F, log q, log r) with q_k = Lq_kk^2, r_k = P_kk^-2.  One call
+ * runs the taped forward filter (ancestors of every step, (x, lw) every
+ * ckpt_every steps), then the backward pass, recomputing each segment of
+ * ckpt_every steps from its checkpoint.
+ * grad_dev (d*d + 2d floats): dA row-major, then d/dlog q_k, then d/dlog r_k.
+ * log_z_dev (1 double) and resampled_dev (T int32) may be NULL.  scheme:
+ * systematic or multinomial.  Synchronises `stream` once, between the passes. */
+size_t mgb_pf_lg_grad_workspace(int64_t n, int64_t T, int32_t d, int32_t ckpt_every);
+int mgb_pf_lg_grad(const mgb_lg_model *model_host, int64_t n, int64_t T, const uint32_t *key_dev, const float *y_dev,
+                   float ess_threshold, int scheme, int32_t ckpt_every, void *ws_dev, size_t ws_bytes,
+                   double *log_z_dev, float *grad_dev, int32_t *resampled_dev, void *stream);
+
 /* ------------------------------------ particle filter, optimal proposal
  * OptimalNonLinearGaussianParticleFilter (mocat/src/ssm/nonlinear_gaussian.py:134-281)
  * for a linear transition f(x) = F x with linear-Gaussian observations:

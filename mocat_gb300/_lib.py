@@ -75,6 +75,9 @@ _SIGNATURES = {
     "mgb_pf_lg_workspace": ([_I64, _I64, ctypes.c_int32, _I32], _SZ),
     "mgb_pf_lg_run": ([ctypes.POINTER(LGModel), _I64, _I64, _P, _P, _F, _I32, _P, _SZ, ctypes.POINTER(PFOutputs), _P],
                       _I32),
+    "mgb_pf_lg_grad_workspace": ([_I64, _I64, ctypes.c_int32, ctypes.c_int32], _SZ),
+    "mgb_pf_lg_grad": ([ctypes.POINTER(LGModel), _I64, _I64, _P, _P, _F, _I32, ctypes.c_int32, _P, _SZ, _P, _P, _P, _P],
+                       _I32),
     "mgb_pf_opt_init": ([ctypes.POINTER(OptModel), _I64, _P, _P, _P, _P, _P], _I32),
     "mgb_pf_opt_propagate": ([ctypes.POINTER(OptModel), _I64, _P, _P, _P, _P, _P, _P, _P, _P], _I32),
     "mgb_pf_opt_workspace": ([_I64, _I64, ctypes.c_int32, _I32], _SZ),

@@ -1,0 +1,119 @@
+"""d log Z / d theta of the bootstrap particle filter by a hand-written adjoint.
+
+mocat obtains parameter gradients by jax.grad through
+run_particle_filter_for_marginals (mocat/src/ssm/filtering.py:255-324); here the
+gradient of the log Z estimate with the ancestors and resampling decisions
+held fixed comes from one call into the C library (mgb_pf_lg_grad): a taped
+forward filter, then a backward pass that recomputes segments of
+``ckpt_every`` steps from checkpoints.
+
+The model is TimeHomogenousLinearGaussian with the identity likelihood matrix
+and diagonal transition / likelihood covariances; theta = (A, log diag Q,
+log diag R).
+
+* ``log_z_and_grad(ssm_scenario, y, random_key, n, ...)``: log Z and the three
+  gradient blocks for a scenario object.
+* ``ParticleFilterLogZ``: a torch.autograd.Function whose forward is the
+  filter's log Z and whose backward is the adjoint, so that
+  ``particle_filter_log_z(A, log_q, log_r, ...)`` composes with torch code.
+"""
+import ctypes
+import math
+
+import numpy as np
+import torch
+
+from . import _dev, _lib
+from ._lib import call
+from .core import cdict
+from .resampling import SCHEMES
+from .ssm import TimeHomogenousLinearGaussian, _f32
+
+LOG2PI = math.log(2.0 * math.pi)
+SUPPORTED_D = (1, 2, 3, 4, 5, 8, 10)
+
+
+def _diag_model(A, log_q, log_r, C0, m0):
+    """(float32 arrays kept alive, C-ABI struct) for theta = (A, log q, log r)."""
+    A = np.asarray(A, np.float64)
+    d = A.shape[0]
+    lq = np.asarray(log_q, np.float64).reshape(d)
+    lr = np.asarray(log_r, np.float64).reshape(d)
+    keep = dict(F=_f32(A), Lq=_f32(np.diag(np.exp(0.5 * lq))), H=_f32(np.eye(d)), P=_f32(np.diag(np.exp(-0.5 * lr))),
+                C0=_f32(C0), m0=_f32(np.asarray(m0, np.float64).reshape(d)))
+    c = np.float32(0.5 * (d * LOG2PI + lr.sum()))
+    s = _lib.LGModel(d, d, keep["F"].ctypes.data, keep["Lq"].ctypes.data, keep["H"].ctypes.data,
+                     keep["P"].ctypes.data, keep["C0"].ctypes.data, keep["m0"].ctypes.data, float(c))
+    return keep, s
+
+
+def _grad_call(s, d, y, key, n, ess_threshold, resampling, ckpt_every):
+    dev = _dev.device()
+    y2 = _dev.as_f32(y).reshape(-1, d).contiguous()
+    T = y2.shape[0]
+    key = _dev.as_key(key)
+    if d not in SUPPORTED_D:
+        raise NotImplementedError(f"adjoint for d = {d} not compiled (supported {SUPPORTED_D})")
+    ws = _dev.workspace(_lib.lib().mgb_pf_lg_grad_workspace(n, T, d, ckpt_every), dev)
+    logz = torch.empty(1, dtype=torch.float64, device=dev)
+    grad = torch.empty(d * d + 2 * d, dtype=torch.float32, device=dev)
+    res = torch.empty(T, dtype=torch.int32, device=dev)
+    call("mgb_pf_lg_grad", ctypes.byref(s), n, T, _dev.ptr(key), _dev.ptr(y2), float(ess_threshold),
+         SCHEMES[resampling], int(ckpt_every), _dev.ptr(ws), ws.numel(), _dev.ptr(logz), _dev.ptr(grad),
+         _dev.ptr(res), _dev.stream_ptr())
+    return logz[0], grad, res
+
+
+def log_z_and_grad(ssm_scenario, y, random_key, n, ess_threshold=0.5, resampling="systematic", ckpt_every=32):
+    """log Z of run_particle_filter_for_marginals(ssm_scenario, BootstrapFilter(), y, ..., n=n)
+    and its gradient with respect to (transition_matrix, log diag transition_covariance,
+    log diag likelihood_covariance), ancestors held fixed.
+
+    Returns cdict(log_z, grad_transition_matrix (d, d), grad_log_transition_covariance_diag (d,),
+    grad_log_likelihood_covariance_diag (d,), resampled (T,))."""
+    if not isinstance(ssm_scenario, TimeHomogenousLinearGaussian):
+        raise NotImplementedError(f"{ssm_scenario.__class__.__name__}: no adjoint kernel for this model")
+    _, s = ssm_scenario.derived()
+    d = ssm_scenario.dim
+    lz, g, res = _grad_call(s, d, y, random_key, n, ess_threshold, resampling, ckpt_every)
+    return cdict(log_z=lz, grad_transition_matrix=g[:d * d].reshape(d, d),
+                 grad_log_transition_covariance_diag=g[d * d:d * d + d],
+                 grad_log_likelihood_covariance_diag=g[d * d + d:], resampled=res.bool())
+
+
+class ParticleFilterLogZ(torch.autograd.Function):
+    """forward: log Z of the bootstrap filter for theta = (A, log q, log r);
+    backward: the adjoint (ancestors held fixed), computed in the same library call."""
+
+    @staticmethod
+    def forward(ctx, A, log_q, log_r, y, random_key, n, C0, m0, ess_threshold, resampling, ckpt_every):
+        d = A.shape[0]
+        _, s = _diag_model(A.detach().cpu().numpy(), log_q.detach().cpu().numpy(), log_r.detach().cpu().numpy(),
+                           C0, m0)
+        lz, g, _ = _grad_call(s, d, y, random_key, n, ess_threshold, resampling, ckpt_every)
+        ctx.save_for_backward(g)
+        ctx.d = d
+        ctx.devs = (A.device, log_q.device, log_r.device)
+        return lz.to(A.device)
+
+    @staticmethod
+    def backward(ctx, gout):
+        (g,) = ctx.saved_tensors
+        d = ctx.d
+        gout = gout.to(g.device, torch.float32)
+        gA = (gout * g[:d * d]).reshape(d, d).to(ctx.devs[0])
+        gq = (gout * g[d * d:d * d + d]).to(ctx.devs[1])
+        gr = (gout * g[d * d + d:]).to(ctx.devs[2])
+        return gA, gq, gr, None, None, None, None, None, None, None, None
+
+
+def particle_filter_log_z(A, log_q, log_r, y, random_key, n, initial_covariance=None, initial_mean=None,
+                          ess_threshold=0.5, resampling="systematic", ckpt_every=32):
+    """Differentiable log Z (torch) of the bootstrap filter for
+    x_t = A x_{t-1} + N(0, diag(exp(log_q))), y_t = x_t + N(0, diag(exp(log_r)))."""
+    d = A.shape[0]
+    S0 = np.eye(d) if initial_covariance is None else np.asarray(initial_covariance, np.float64)
+    C0 = np.linalg.cholesky(S0)
+    m0 = np.zeros(d) if initial_mean is None else np.asarray(initial_mean, np.float64)
+    return ParticleFilterLogZ.apply(A, log_q, log_r, y, random_key, int(n), C0, m0, float(ess_threshold), resampling,
+                                    int(ckpt_every))

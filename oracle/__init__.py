@@ -92,6 +92,11 @@ def lib():
         L.o_lg_run.argtypes = [ctypes.POINTER(_LGModel), i64, i64, u32p, f32p, ctypes.c_float, ctypes.c_int,
                                f32p, i32p, vp, vp]
         L.o_lg_run.restype = ctypes.c_double
+        L.o_lg_run_tape.argtypes = [ctypes.POINTER(_LGModel), i64, i64, u32p, f32p, ctypes.c_float, ctypes.c_int,
+                                    f32p, i32p, i32p]
+        L.o_lg_run_tape.restype = ctypes.c_double
+        L.o_lg_step_keys.argtypes = [u32p, i64, u32p]
+        L.o_lg_normals.argtypes = [u32p, i64, ctypes.c_int, f32p]
         L.o_opt_init.argtypes = [ctypes.POINTER(_OptModel), i64, u32p, f32p, f32p, f32p]
         L.o_opt_propagate.argtypes = [ctypes.POINTER(_OptModel), i64, u32p, f32p, f32p, vp, vp, f32p, f32p]
         L.o_opt_run.argtypes = [ctypes.POINTER(_OptModel), i64, i64, u32p, f32p, ctypes.c_float, ctypes.c_int,
@@ -287,6 +292,33 @@ def lg_run(params, n, key, y, ess_threshold=0.5, scheme="systematic", history=Fa
     logZ = lib().o_lg_run(ctypes.byref(s), n, T, _u32(key), y.reshape(-1), float(ess_threshold), SCHEMES[scheme],
                           ess, res, _ptr(xh), _ptr(lh))
     return dict(log_z=logZ, ess=ess, resampled=res.astype(bool), value=xh, log_weight=lh)
+
+
+def lg_run_tape(params, n, key, y, ess_threshold=0.5, scheme="systematic"):
+    """lg_run returning also the ancestors of every resampled step (T, n) (other rows -1)."""
+    s, keep = _lg_struct(params)
+    y = _f32(y).reshape(len(y), -1)
+    T = y.shape[0]
+    ess = np.empty(T, np.float32)
+    res = np.empty(T, np.int32)
+    anc = np.full((T, n), -1, np.int32)
+    logZ = lib().o_lg_run_tape(ctypes.byref(s), n, T, _u32(key), y.reshape(-1), float(ess_threshold),
+                               SCHEMES[scheme], ess, res, anc.reshape(-1))
+    return dict(log_z=logZ, ess=ess, resampled=res.astype(bool), ancestors=anc)
+
+
+def lg_step_keys(key, T):
+    """(T, 2): row 0 the initial draw's key, row t the key of step t (filtering.py:267-278)."""
+    out = np.empty((T, 2), np.uint32)
+    lib().o_lg_step_keys(_u32(key), T, out.reshape(-1))
+    return out
+
+
+def lg_normals(key_t, n, d):
+    """(n, d) bootstrap draws normal(split(k_t, n)[i], (d,))."""
+    e = np.empty((n, d), np.float32)
+    lib().o_lg_normals(_u32(key_t), n, d, e.reshape(-1))
+    return e
 
 
 def _opt_struct(p):

@@ -323,9 +323,50 @@ void o_lg_propagate(const o_lg_model *md, int64_t n, const uint32_t *kt, const f
  * Outputs: logZ (log-marginal-likelihood built from the log-weights),
  * ess[T], resampled[T] (resampled[t] = 1 when step t started with a resample),
  * optional histories x_hist (T, n, d) and lw_hist (T, n) (NULL to skip). */
+static double o_lg_run_impl(const o_lg_model *md, int64_t n, int64_t T, const uint32_t *key, const float *y,
+                            float ess_threshold, int scheme, float *ess_out, int32_t *resampled_out,
+                            float *x_hist, float *lw_hist, int32_t *anc_hist);
+
 double o_lg_run(const o_lg_model *md, int64_t n, int64_t T, const uint32_t *key, const float *y,
                 float ess_threshold, int scheme, float *ess_out, int32_t *resampled_out,
                 float *x_hist, float *lw_hist)
+{
+    return o_lg_run_impl(md, n, T, key, y, ess_threshold, scheme, ess_out, resampled_out, x_hist, lw_hist, NULL);
+}
+
+/* o_lg_run that also records the ancestors: anc_hist (T, n), row t written
+ * when step t resampled (the rows of the other steps are left as they are). */
+double o_lg_run_tape(const o_lg_model *md, int64_t n, int64_t T, const uint32_t *key, const float *y,
+                     float ess_threshold, int scheme, float *ess_out, int32_t *resampled_out, int32_t *anc_hist)
+{
+    return o_lg_run_impl(md, n, T, key, y, ess_threshold, scheme, ess_out, resampled_out, NULL, NULL, anc_hist);
+}
+
+/* Key schedule of run_particle_filter_for_marginals (filtering.py:267-278):
+ * out[0..1] = split(key)[1] (the initial draw), out[2t..2t+1] = split(split(key)[0], T-1)[t-1]. */
+void o_lg_step_keys(const uint32_t *key, int64_t T, uint32_t *out)
+{
+    uint32_t keys2[4];
+    o_split(key, 2, keys2);
+    out[0] = keys2[2];
+    out[1] = keys2[3];
+    if (T > 1) o_split(keys2, T - 1, out + 2);
+}
+
+/* eps (n, d): eps[i] = normal(split(k, n)[i], (d,)), the bootstrap draws of one step */
+void o_lg_normals(const uint32_t *kt, int64_t n, int d, float *e)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        uint32_t a0, a1;
+        o_split_at(kt[0], kt[1], (uint64_t)n, (uint64_t)i, &a0, &a1);
+        o_normal_vec(a0, a1, d, e + i * d);
+    }
+}
+
+static double o_lg_run_impl(const o_lg_model *md, int64_t n, int64_t T, const uint32_t *key, const float *y,
+                            float ess_threshold, int scheme, float *ess_out, int32_t *resampled_out,
+                            float *x_hist, float *lw_hist, int32_t *anc_hist)
 {
     const int d = md->d, dy = md->dy;
     float *xa = (float *)malloc(sizeof(float) * (size_t)(n * d));
@@ -365,6 +406,7 @@ double o_lg_run(const o_lg_model *md, int64_t n, int64_t T, const uint32_t *key,
                 o_resample_gumbel(la, n, n, kt, anc);
             }
         }
+        if (res && anc_hist) memcpy(anc_hist + t * n, anc, sizeof(int32_t) * (size_t)n);
         o_lg_propagate(md, n, kt, y + t * dy, xa, res ? anc : NULL, res ? NULL : la, xb, lb);
         o_lse_ess(lb, n, st);
         logZ += st[1] - (res ? logn : lse_prev);
