@@ -24,6 +24,10 @@ JAX and is not installable here) on the same workload, all host threads.
 Multi-GPU (torchrun): independent replicas, one filter per rank, no
 collective on the data path; value = all ranks' particle-steps / max time.
 
+adjoint -- gradient evaluations per second of log Z with respect to
+(A, log diag Q, log diag R) at N = 65536, T = 1000 (checkpoint every 32
+steps), next to finite differences of the plain filter.
+
 batched_sv -- a second workload in the same line: 4096 independent
 stochastic-volatility filters of uneven length and size in one persistent
 launch (graph replay; e2e with the observations copied from pinned host
@@ -218,6 +222,51 @@ def bench_sv_batch(args, flush, rank):
     return res
 
 
+def bench_adjoint(args, flush, rank):
+    """d log Z / d theta (theta = A, log diag Q, log diag R: 120 parameters) of the d = 10
+    filter at N = 65536, T = 1000, checkpoint every 32 steps: gradient evaluations per
+    second through the public call, against finite differences of the plain filter
+    (2 x 120 forward runs per gradient)."""
+    import torch
+    import mocat_gb300 as mg
+    n, T = args.adj_n, args.adj_T
+    a = model_arrays()
+    ssm = mg.ssm.TimeHomogenousLinearGaussian(**a)
+    y = ssm.simulate(np.arange(T), mg.random.PRNGKey(0)).y.contiguous()
+    key = mg.random.PRNGKey(1 + rank)
+    o = mg.adjoint.log_z_and_grad(ssm, y, key, n, ckpt_every=32)
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(max(3, args.steps)):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        o = mg.adjoint.log_z_and_grad(ssm, y, key, n, ckpt_every=32)
+        torch.cat([o.grad_transition_matrix.reshape(-1), o.grad_log_transition_covariance_diag,
+                   o.grad_log_likelihood_covariance_diag]).cpu()
+        ts.append(time.perf_counter() - t0)
+    t_grad = statistics.median(ts)
+    # plain form: one forward filter run (persistent kernel) per finite-difference point
+    fw = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        f = mg.ssm.run_particle_filter_for_marginals(ssm, mg.ssm.BootstrapFilter(), y, np.arange(T), key, n=n,
+                                                     history=False)
+        float(f.log_z)
+        fw.append(time.perf_counter() - t0)
+    t_fwd = statistics.median(fw)
+    npar = D * D + 2 * D
+    res = {"workload": f"d={D} linear-Gaussian (bench model), N={n}, T={T}, theta=(A, log diag Q, log diag R) "
+                       f"= {npar} parameters, ancestors held fixed, checkpoint every 32 steps",
+           "metric": "grad-evals/s", "value": 1.0 / t_grad, "unit": "grad-evals/s", "s_per_grad": t_grad,
+           "particle_steps_per_s_forward_plus_backward": n * T / t_grad,
+           "plain_fd": {"forward_s": t_fwd, "runs_per_grad": 2 * npar, "value": 1.0 / (2 * npar * t_fwd),
+                        "unit": "grad-evals/s"},
+           "speedup_vs_plain_fd": 2 * npar * t_fwd / t_grad}
+    return res
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
@@ -252,6 +301,9 @@ def main():
     ap.add_argument("--kernel-iters", type=int, default=50)
     ap.add_argument("--sv-cpu-filters", type=int, default=256)
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adj-n", type=int, default=65536)
+    ap.add_argument("--adj-T", type=int, default=1000)
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -416,6 +468,8 @@ def main():
             "clocks": clk.summary()}
     if not args.no_batched:
         line["batched_sv"] = bench_sv_batch(args, flush, rank)
+    if not args.no_adjoint:
+        line["adjoint"] = bench_adjoint(args, flush, rank)
     if rank == 0:
         v_cpu, cores, dt = cpu_baseline(n, args.cpu_steps)
         line["cpu_baseline"] = {"value": v_cpu, "unit": "particle-steps/s", "cores": cores, "kind": "port",
