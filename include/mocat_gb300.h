@@ -285,6 +285,73 @@ int mgb_pf_sv_batch_autotune(const mgb_sv_model *model_host, int64_t B, const in
                              const uint32_t *keys_dev, float ess_threshold, int scheme, int32_t probe_steps,
                              void *ws_dev, size_t ws_bytes, mgb_sv_launch *best, float *best_ms, void *stream);
 
+/* ----------------------- tempered SMC on Bayesian logistic regression
+ * MetropolisedSMCSampler (mocat/src/transport/smc.py:229-373) with MALA moves
+ * (Underdamped(leapfrog_steps=1, friction=inf), mocat/src/mcmc/standard_mcmc.py:72-153,
+ * Metropolis correction mocat/src/mcmc/metropolis.py:48-70), adaptive
+ * temperatures by regula falsi on the ESS (smc.py:311-326, utils.py:205-237),
+ * driven as mocat.run does (sample.py:110-148), for B independent posteriors
+ * (one key each) advanced in lockstep.  Scenario: beta ~ N(0, s^2 I),
+ * y_i ~ Bernoulli(sigmoid(x_i . beta)); prior potential |beta|^2 / (2 s^2),
+ * likelihood potential sum_i softplus(x_i . beta) - y_i x_i . beta.
+ * Resampling (ess <= ess_threshold_resample N) is systematic.
+ * N <= MGB_SMC_MAX_N; d in {2, 3, 5, 10, 20, 50}.
+ */
+#define MGB_SMC_MAX_N 24576
+enum { MGB_PREC_FP32 = 0, MGB_PREC_BF16 = 1 };
+
+/* logistic potential and gradient for P parameter rows beta (P, d):
+ * lik[p] = sum_i softplus(x_i . beta_p) - y_i x_i . beta_p, grad[p] = X^T (sigmoid(X beta_p) - y).
+ * X (n_data, d) row-major float32; precision MGB_PREC_BF16 also needs Xbf16, the
+ * (n_data, 64) bf16 zero-padded copy of X. */
+size_t mgb_logreg_workspace(int64_t P, int64_t n_data, int32_t d, int precision);
+int mgb_logreg_potential_grad(const float *X_dev, const float *y_dev, int64_t n_data, int32_t d, const float *beta_dev,
+                              int64_t P, float *lik_dev, float *grad_dev, int precision, const void *Xbf16_dev,
+                              void *ws_dev, size_t ws_bytes, void *stream);
+
+typedef struct {
+  int32_t B, N, d;              /* posteriors, particles per posterior, dimension */
+  int32_t mcmc_steps;           /* MALA moves per temperature */
+  float stepsize;               /* Underdamped stepsize */
+  float prior_scale;            /* s */
+  float ess_threshold_retain;   /* target ESS fraction of the temperature bisection */
+  float ess_threshold_resample; /* resample when ess <= this * N */
+  float bisection_tol;
+  int32_t max_bisection_iter;
+  float max_temperature;
+  int32_t max_iter;             /* SMC iterations (also the history length - 1) */
+  int32_t precision;            /* MGB_PREC_FP32 or MGB_PREC_BF16 (potential on the tensor cores) */
+} mgb_smc_logreg_config;
+
+/* device pointers into the sampler's workspace */
+typedef struct {
+  float *value;                 /* (B N, d) particles */
+  float *log_weight;            /* (B N) */
+  float *likelihood_potential;  /* (B N) */
+  float *temperature;           /* (B) */
+  float *ess;                   /* (B) */
+  double *log_norm_constant;    /* (B) */
+  int32_t *iter;                /* (B) iterations done */
+  int32_t *active;              /* (B) 1 while the posterior has not terminated */
+  float *hist_temperature;      /* (B, hist_len) entry 0 = after startup, i = after iteration i */
+  double *hist_log_norm_constant;
+  float *hist_ess;
+  float *hist_alpha;            /* mean acceptance probability of the iteration's moves */
+  int32_t *hist_resampled;
+  int32_t hist_len;
+} mgb_smc_views;
+
+size_t mgb_smc_logreg_workspace(const mgb_smc_logreg_config *cfg, int64_t n_data);
+int mgb_smc_logreg_views(const mgb_smc_logreg_config *cfg, void *ws_dev, mgb_smc_views *out);
+/* startup (prior draws, potentials, first temperature); keys_dev (B, 2) */
+int mgb_smc_logreg_init(const mgb_smc_logreg_config *cfg, const float *X_dev, const float *y_dev,
+                        const void *Xbf16_dev, int64_t n_data, const uint32_t *keys_dev, void *ws_dev,
+                        size_t ws_bytes, void *stream);
+/* one SMC iteration of every active posterior (the caller loops while any
+ * views.active[b] is set) */
+int mgb_smc_logreg_step(const mgb_smc_logreg_config *cfg, const float *X_dev, const float *y_dev,
+                        const void *Xbf16_dev, int64_t n_data, void *ws_dev, size_t ws_bytes, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

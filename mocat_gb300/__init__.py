@@ -7,6 +7,7 @@ PyTorch supplies device memory and streams only.
 """
 from . import adjoint
 from . import batched
+from . import smc
 from . import random
 from . import ssm
 from .core import Scenario, cdict, load_cdict, save_cdict, static_cdict
@@ -15,5 +16,5 @@ from .resampling import gather_rows, lse_ess, resample
 
 __version__ = "0.1.0"
 
-__all__ = ["adjoint", "batched", "random", "ssm", "Scenario", "cdict", "static_cdict", "save_cdict", "load_cdict", "ess_log_weight",
+__all__ = ["adjoint", "batched", "smc", "random", "ssm", "Scenario", "cdict", "static_cdict", "save_cdict", "load_cdict", "ess_log_weight",
            "log_ess_log_weight", "resample", "gather_rows", "lse_ess"]

@@ -46,6 +46,21 @@ class SVLaunch(ctypes.Structure):
                 ("nbundles", ctypes.c_int32), ("smem_bytes", ctypes.c_int64)]
 
 
+class SMCConfig(ctypes.Structure):
+    _fields_ = [("B", ctypes.c_int32), ("N", ctypes.c_int32), ("d", ctypes.c_int32), ("mcmc_steps", ctypes.c_int32),
+                ("stepsize", ctypes.c_float), ("prior_scale", ctypes.c_float),
+                ("ess_threshold_retain", ctypes.c_float), ("ess_threshold_resample", ctypes.c_float),
+                ("bisection_tol", ctypes.c_float), ("max_bisection_iter", ctypes.c_int32),
+                ("max_temperature", ctypes.c_float), ("max_iter", ctypes.c_int32), ("precision", ctypes.c_int32)]
+
+
+class SMCViews(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_void_p) for k in ("value", "log_weight", "likelihood_potential", "temperature", "ess",
+                                               "log_norm_constant", "iter", "active", "hist_temperature",
+                                               "hist_log_norm_constant", "hist_ess", "hist_alpha",
+                                               "hist_resampled")] + [("hist_len", ctypes.c_int32)]
+
+
 _P = ctypes.c_void_p
 _I64 = ctypes.c_int64
 _I32 = ctypes.c_int
@@ -83,6 +98,12 @@ _SIGNATURES = {
     "mgb_pf_opt_workspace": ([_I64, _I64, ctypes.c_int32, _I32], _SZ),
     "mgb_pf_opt_run": ([ctypes.POINTER(OptModel), _I64, _I64, _P, _P, _F, _I32, _P, _SZ, ctypes.POINTER(PFOutputs),
                         _P], _I32),
+    "mgb_logreg_workspace": ([_I64, _I64, ctypes.c_int32, _I32], _SZ),
+    "mgb_logreg_potential_grad": ([_P, _P, _I64, ctypes.c_int32, _P, _I64, _P, _P, _I32, _P, _P, _SZ, _P], _I32),
+    "mgb_smc_logreg_workspace": ([ctypes.POINTER(SMCConfig), _I64], _SZ),
+    "mgb_smc_logreg_views": ([ctypes.POINTER(SMCConfig), _P, ctypes.POINTER(SMCViews)], _I32),
+    "mgb_smc_logreg_init": ([ctypes.POINTER(SMCConfig), _P, _P, _P, _I64, _P, _P, _SZ, _P], _I32),
+    "mgb_smc_logreg_step": ([ctypes.POINTER(SMCConfig), _P, _P, _P, _I64, _P, _SZ, _P], _I32),
     "mgb_pf_sv_batch_plan": ([_I64, _P, _P, ctypes.POINTER(SVLaunch), _P, _P], _I32),
     "mgb_pf_sv_batch_run": ([ctypes.POINTER(SVModel), _I64, _P, _P, _P, _P, _P, ctypes.POINTER(SVLaunch), _P, _P, _F,
                              _I32, _P, _P, _P, _P, _P], _I32),

@@ -36,6 +36,7 @@
 
 #include "mgb_internal.cuh"
 #include "mgb_resample.cuh"
+#include "mgb_group.cuh"
 
 namespace mgb {
 
@@ -69,50 +70,6 @@ __host__ __device__ inline size_t sv_slot_bytes(int s) { return (size_t)s * 24 +
 __device__ __forceinline__ float sv_potential(const SVParams &p, float x, float y) {
   const float a = __fmul_rn(__fmul_rn(0.5f, __fmul_rn(y, y)), p.r2);
   return __fmaf_rn(a, expf_(-x), __fmaf_rn(0.5f, x, p.cB));
-}
-
-// group barrier: named barrier `id` over `nthr` threads, or the warp
-__device__ __forceinline__ void gbar(int id, int nthr) {
-  if (nthr <= 32) {
-    __syncwarp();
-  } else {
-    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthr) : "memory");
-  }
-}
-
-// In-place inclusive scan of V[0..cnt) by the group's W warps (warp wg owns a
-// contiguous segment, processed 32 items at a time); item j is load(j) on
-// entry.  Returns the total.  Two group barriers.
-template <class Load>
-__device__ __forceinline__ uint64_t group_scan(uint64_t *V, int cnt, int W, int wg, int lane, int wcta,
-                                               unsigned long long *wtot, int bar, int G, Load load) {
-  const int seg = ((cnt + 32 * W - 1) / (32 * W)) * 32;
-  const int s0 = wg * seg, s1 = min(s0 + seg, cnt);
-  uint64_t carry = 0;
-  for (int c = s0; c < s1; c += 32) {
-    const int j = c + lane;
-    uint64_t v = j < s1 ? load(j) : 0ull;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint64_t u = __shfl_up_sync(0xffffffffu, v, o);
-      if (lane >= o) v += u;
-    }
-    v += carry;
-    if (j < s1) V[j] = v;
-    carry = __shfl_sync(0xffffffffu, v, 31);
-  }
-  if (lane == 0) wtot[wcta] = carry;
-  gbar(bar, G);
-  uint64_t off = 0, tot = 0;
-  for (int w = 0; w < W; ++w) {
-    const uint64_t x = wtot[wcta - wg + w];
-    off += w < wg ? x : 0ull;
-    tot += x;
-  }
-  if (off)
-    for (int j = s0 + lane; j < s1; j += 32) V[j] += off;
-  gbar(bar, G);
-  return tot;
 }
 
 // One filter on one thread group (tg = thread in group, wg = warp in group,
@@ -207,33 +164,9 @@ __device__ __forceinline__ void sv_filter(const SVParams &p, const SVBatch &a, i
         }
       } else {
         // systematic: T_k = floor((k 2^23 + m) Q / (n 2^23)), m = bits(k_t) >> 9
-        ResampleCtl c;
         uint32_t r0, r1;
         threefry2x32_m(k0, k1, 0u, 0u, p.one, r0, r1);
-        sys_constants(Q, (uint64_t)n, r0 >> 9, c, magic);
-        const int total = 2 * n, per = (total + G - 1) / G, d0 = tg * per;
-        if (d0 < total) {
-          int lo = d0 > n ? d0 - n : 0, hi = d0 < n ? d0 : n;
-          while (lo < hi) {
-            const int mid = (lo + hi) >> 1;
-            if (C[mid] <= thr_at(c, (uint64_t)(d0 - 1 - mid), (uint64_t)n).T) lo = mid + 1;
-            else hi = mid;
-          }
-          int i = lo, kk = d0 - lo;
-          ThrCursor cur = thr_at(c, (uint64_t)(kk < n ? kk : 0), (uint64_t)n);
-          const int d1 = min(d0 + per, total);
-          uint64_t ci = i < n ? C[i] : 0ull;
-          for (int d = d0; d < d1; ++d) {
-            if (i < n && (kk >= n || ci <= cur.T)) {
-              ++i;
-              ci = i < n ? C[i] : 0ull;
-            } else {
-              A[kk] = i < n ? i : n - 1;
-              ++kk;
-              thr_next(cur, c, (uint64_t)n);
-            }
-          }
-        }
+        group_systematic_fill(C, n, Q, r0 >> 9, magic, A, tg, G);
       }
       gbar(bar, G);
       for (int k = tg; k < n; k += G) XR[k] = X[A[k]];

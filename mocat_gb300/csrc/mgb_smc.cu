@@ -1,0 +1,711 @@
+// Tempered SMC sampler with MALA moves on Bayesian logistic regression, many
+// independent posteriors advanced in lockstep.
+//
+// Reference path: mocat.run (mocat/src/sample.py:110-148) with
+// MetropolisedSMCSampler (mocat/src/transport/smc.py:229-373) over
+// Underdamped(leapfrog_steps=1, friction=inf) = MALA
+// (mocat/src/mcmc/standard_mcmc.py:72-153, utils.leapfrog :108-156) with the
+// Metropolis correction (mocat/src/mcmc/metropolis.py:48-70):
+//   startup  (smc.py:128-164, :267-296; transport/sampler.py:17-31):
+//            (key, sub) = split(key); beta_j = s normal(split(sub, N)[j], (d,));
+//            key = split(key, 2N + 1)[-1]; tau_1 by bisection from 0;
+//            lw = -tau_1 l; log Z = LSE(lw) - log N; key = split(key, 3)[0]
+//   update   (smc.py:73-99, :219-225): resample when ess <= thr N (keys_all =
+//            split(key, N + 2): particle keys [:N], resample key [N], next key
+//            [N + 1]); per particle k = split(k_j, 3)[0], then mcmc_steps MALA moves:
+//            (k, ka) = split(k); p = normal(ka, (d,)); p_h = p - eps/2 grad U;
+//            beta' = beta + eps p_h; p' = p_h - eps/2 grad U(beta');
+//            alpha = min(1, exp(-U' + U - |p'|^2/2 + |p|^2/2)); k = split(k, 2)[0];
+//            (k, ku) = split(k); accept if uniform(ku) < alpha;
+//            then l = (U - prior) / tau (smc.py:355-358)
+//   adapt    (smc.py:193-217, :311-326; utils.bisect :205-237): regula falsi on
+//            log ESS(lw_res - (tau' - tau) l) = log(ess retain); lw = lw_res - (tau' - tau) l;
+//            log Z += LSE(lw) - LSE(lw_res)
+// Scenario: prior N(0, s^2 I): prior potential |beta|^2 / (2 s^2); likelihood
+// potential l(beta) = sum_i softplus(x_i beta) - y_i x_i beta, gradient
+// X^T (sigmoid(X beta) - y).
+//
+// Differences by design: resampling is systematic (O(N), in shared memory per
+// posterior) instead of random.categorical; potentials are not re-evaluated at
+// the start of each MCMC block (they are deterministic, the stored values are
+// the same numbers).
+//
+// Layout: particle-major rows beta[(b N + j) d + k] (the K-major operand of the
+// potential's GEMMs); per-posterior scalars in (B,) arrays.
+#include <cmath>
+#include <vector>
+
+#include "mgb_internal.cuh"
+#include "mgb_resample.cuh"
+#include "mgb_group.cuh"
+#include "mgb_smc.cuh"
+
+namespace mgb {
+
+constexpr int SMC_TPB = 256;
+constexpr int ADAPT_TPB = 1024;
+constexpr int LR_TPB = 128;
+constexpr int LR_ROWS = 64;
+
+// ------------------------------------------------------------ potential, FP32
+// One thread per particle; X rows staged through shared memory in tiles of
+// LR_ROWS; blockIdx.y selects a chunk of the data (partials summed afterwards).
+template <int D>
+__global__ void __launch_bounds__(LR_TPB) k_logreg_f32(const float *__restrict__ X, const float *__restrict__ y,
+                                                        int64_t n_data, int64_t chunk,
+                                                        const float *__restrict__ beta, int64_t P,
+                                                        const int32_t *active, int N,
+                                                        float *__restrict__ part_lik,
+                                                        float *__restrict__ part_grad) {
+  __shared__ float xs[LR_ROWS * D];
+  __shared__ float ys[LR_ROWS];
+  const int64_t p = blockIdx.x * (int64_t)LR_TPB + threadIdx.x;
+  const int64_t r0 = blockIdx.y * chunk, r1 = min(r0 + chunk, n_data);
+  const int64_t pb = blockIdx.x * (int64_t)LR_TPB;
+  // whole block inactive: the posteriors of its particles have finished
+  bool any = false;
+  if (active) {
+    const int64_t plast = min(pb + LR_TPB, P) - 1;
+    for (int64_t b = pb / N; b <= plast / N; ++b) any |= active[b] != 0;
+  } else {
+    any = true;
+  }
+  if (!any) return;
+  const bool mine = p < P && (!active || active[p / N]);
+  float bt[D], g[D];
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    bt[k] = mine ? beta[p * D + k] : 0.0f;
+    g[k] = 0.0f;
+  }
+  float acc = 0.0f;
+  for (int64_t t0 = r0; t0 < r1; t0 += LR_ROWS) {
+    const int rows = (int)min((int64_t)LR_ROWS, r1 - t0);
+    __syncthreads();
+    for (int u = threadIdx.x; u < rows * D; u += LR_TPB) xs[u] = X[t0 * D + u];
+    for (int u = threadIdx.x; u < rows; u += LR_TPB) ys[u] = y[t0 + u];
+    __syncthreads();
+    if (mine) {
+      for (int i = 0; i < rows; ++i) {
+        float z = 0.0f;
+#pragma unroll
+        for (int k = 0; k < D; ++k) z = fmaf(bt[k], xs[i * D + k], z);
+        const float yi = ys[i];
+        const float sp = fmaxf(z, 0.0f) + log1pf(expf(-fabsf(z)));
+        acc += sp - yi * z;
+        const float r = 1.0f / (1.0f + expf(-z)) - yi;
+#pragma unroll
+        for (int k = 0; k < D; ++k) g[k] = fmaf(r, xs[i * D + k], g[k]);
+      }
+    }
+  }
+  if (p < P) {
+    part_lik[blockIdx.y * P + p] = acc;
+#pragma unroll
+    for (int k = 0; k < D; ++k) part_grad[(blockIdx.y * P + p) * D + k] = g[k];
+  }
+}
+
+__global__ void k_logreg_reduce(const float *part_lik, const float *part_grad, int64_t P, int D, int chunks,
+                                float *lik, float *grad) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < P; p += (int64_t)gridDim.x * blockDim.x) {
+    float a = 0.0f;
+    for (int c = 0; c < chunks; ++c) a += part_lik[c * P + p];
+    lik[p] = a;
+    for (int k = 0; k < D; ++k) {
+      float s = 0.0f;
+      for (int c = 0; c < chunks; ++c) s += part_grad[(c * P + p) * D + k];
+      grad[p * D + k] = s;
+    }
+  }
+}
+
+int logreg_chunks(int64_t P, int64_t n_data) {
+  const int64_t bx = (P + LR_TPB - 1) / LR_TPB;
+  int64_t c = (4 * kNumSMs + bx - 1) / bx;
+  if (c < 1) c = 1;
+  if (c > 64) c = 64;
+  const int64_t max_c = (n_data + LR_ROWS - 1) / LR_ROWS;
+  return (int)(c < max_c ? c : max_c);
+}
+
+size_t logreg_f32_workspace(int64_t P, int64_t n_data, int d) {
+  const int c = logreg_chunks(P, n_data);
+  Carver cv(nullptr);
+  cv.take<float>((size_t)c * P);
+  cv.take<float>((size_t)c * P * d);
+  return cv.bytes();
+}
+
+template <int D>
+int logreg_f32(const float *X, const float *y, int64_t n_data, const float *beta, int64_t P, const int32_t *active,
+               int N, float *lik, float *grad, void *ws, size_t ws_bytes, cudaStream_t s) {
+  const int chunks = logreg_chunks(P, n_data);
+  Carver cv(ws);
+  float *pl = cv.take<float>((size_t)chunks * P);
+  float *pg = cv.take<float>((size_t)chunks * P * D);
+  if (cv.bytes() > ws_bytes) return ERR_WORKSPACE;
+  const int64_t chunk = (((n_data + chunks - 1) / chunks + LR_ROWS - 1) / LR_ROWS) * LR_ROWS;
+  const dim3 grid((unsigned)((P + LR_TPB - 1) / LR_TPB), (unsigned)((n_data + chunk - 1) / chunk));
+  k_logreg_f32<D><<<grid, LR_TPB, 0, s>>>(X, y, n_data, chunk, beta, P, active, N ? N : (int)P, pl, pg);
+  int st = launch_status();
+  if (st) return st;
+  k_logreg_reduce<<<grid_for(P, 256), 256, 0, s>>>(pl, pg, P, D, (int)grid.y, lik, grad);
+  return launch_status();
+}
+
+#define MGB_SMC_D_DISPATCH(FN, ...)          \
+  switch (d) {                                \
+    case 2: return FN<2>(__VA_ARGS__);        \
+    case 3: return FN<3>(__VA_ARGS__);        \
+    case 5: return FN<5>(__VA_ARGS__);        \
+    case 10: return FN<10>(__VA_ARGS__);      \
+    case 20: return FN<20>(__VA_ARGS__);      \
+    case 50: return FN<50>(__VA_ARGS__);      \
+    default: return ERR_UNSUPPORTED;          \
+  }
+
+// ------------------------------------------------------------ SMC kernels
+// jax's split(k)[i] for a 2-way split
+__device__ __forceinline__ void split2(uint32_t k0, uint32_t k1, int i, uint32_t &o0, uint32_t &o1) {
+  split_at(k0, k1, 2, (uint64_t)i, o0, o1);
+}
+
+// normal(key, (D,)) in jax's counter layout
+template <int D>
+__device__ __forceinline__ void normal_vec(uint32_t k0, uint32_t k1, float (&e)[D]) {
+  uint32_t b[D];
+  bits_vec<D>(k0, k1, b);
+#pragma unroll
+  for (int j = 0; j < D; ++j) e[j] = bits_to_normal(b[j]);
+}
+
+// prior draws and the key schedule of the sampler's startup
+template <int D>
+__global__ void __launch_bounds__(SMC_TPB) k_smc_prior(SMCView v, const uint32_t *keys_in, float scale) {
+  const int64_t P = (int64_t)v.B * v.N;
+  const int64_t p = blockIdx.x * (int64_t)SMC_TPB + threadIdx.x;
+  if (p >= P) return;
+  const int b = (int)(p / v.N), j = (int)(p % v.N);
+  const uint32_t k0 = keys_in[2 * b], k1 = keys_in[2 * b + 1];
+  uint32_t e0, e1, s0, s1, a0, a1;
+  split2(k0, k1, 0, e0, e1);
+  split2(k0, k1, 1, s0, s1);
+  split_at(s0, s1, (uint64_t)v.N, (uint64_t)j, a0, a1);
+  float e[D];
+  normal_vec<D>(a0, a1, e);
+#pragma unroll
+  for (int k = 0; k < D; ++k) v.beta[p * D + k] = __fmul_rn(e[k], scale);
+  if (j == 0) {
+    uint32_t f0, f1, g0, g1;
+    split_at(e0, e1, 2 * (uint64_t)v.N + 1, 2 * (uint64_t)v.N, f0, f1);  // split(key, 2N + 1)[-1]
+    split_at(f0, f1, 3, 0, g0, g1);                                      // Underdamped.startup
+    v.key[2 * b] = g0;
+    v.key[2 * b + 1] = g1;
+    v.tau[b] = 0.0f;
+    v.ess[b] = (float)v.N;
+    v.logz[b] = 0.0;
+    v.iter[b] = 0;
+    v.active[b] = 1;
+    v.resampled[b] = 1;  // the first adapt starts from zero log-weights
+  }
+}
+
+// iteration start: resampling decision, particle keys, the next sampler key
+__global__ void __launch_bounds__(SMC_TPB) k_smc_keys(SMCView v, float thr_resample) {
+  const int64_t P = (int64_t)v.B * v.N;
+  const int64_t p = blockIdx.x * (int64_t)SMC_TPB + threadIdx.x;
+  if (p >= P) return;
+  const int b = (int)(p / v.N), j = (int)(p % v.N);
+  if (!v.active[b]) return;
+  const uint32_t k0 = v.key[2 * b], k1 = v.key[2 * b + 1];
+  const uint64_t nk = (uint64_t)v.N + 2;
+  uint32_t a0, a1, c0, c1;
+  split_at(k0, k1, nk, (uint64_t)j, a0, a1);
+  split_at(a0, a1, 3, 0, c0, c1);  // Underdamped.startup of forward_proposal
+  v.pkey[2 * p] = c0;
+  v.pkey[2 * p + 1] = c1;
+  v.alpha[p] = 0.0f;
+  if (j == 0) {
+    v.resampled[b] = v.ess[b] <= __fmul_rn(thr_resample, (float)v.N) ? 1 : 0;
+    uint32_t r0, r1, n0, n1;
+    split_at(k0, k1, nk, (uint64_t)v.N, r0, r1);
+    split_at(k0, k1, nk, (uint64_t)v.N + 1, n0, n1);
+    v.rkey[2 * b] = r0;
+    v.rkey[2 * b + 1] = r1;
+    v.key_next[2 * b] = n0;
+    v.key_next[2 * b + 1] = n1;
+  }
+}
+
+// systematic ancestors per posterior, fixed-point prefixes in shared memory
+__global__ void __launch_bounds__(ADAPT_TPB) k_smc_resample(SMCView v) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ float red[ADAPT_TPB / 32];
+  __shared__ unsigned long long wtot[ADAPT_TPB / 32];
+  const int b = blockIdx.x, N = v.N, tg = threadIdx.x;
+  int32_t *anc = v.anc + (int64_t)b * N;
+  if (!v.active[b] || !v.resampled[b]) {
+    for (int k = tg; k < N; k += ADAPT_TPB) anc[k] = k;
+    return;
+  }
+  const float *lw = v.lw + (int64_t)b * N;
+  float m = -INFINITY;
+  int bad = 0;
+  for (int k = tg; k < N; k += ADAPT_TPB) {
+    const float x = lw[k];
+    bad |= (x != x) || (x == INFINITY);
+    m = fmaxf(m, x);
+  }
+  const float M = block_max<ADAPT_TPB>(m, red);
+  bad = __syncthreads_or(bad) || !(M > -INFINITY);
+  if (bad) {
+    for (int k = tg; k < N; k += ADAPT_TPB) anc[k] = 0;
+    return;
+  }
+  uint64_t *C = (uint64_t *)smem;
+  const float wscale = __int_as_float((weight_shift(N) + 127) << 23);
+  const int lane = tg & 31, wcta = tg >> 5;
+  const uint64_t Q = group_scan(C, N, ADAPT_TPB / 32, wcta, lane, wcta, wtot, 1, ADAPT_TPB,
+                                [&](int j) { return quantise_weight(lw[j], M, wscale); });
+  const uint32_t r = bits_at(v.rkey[2 * b], v.rkey[2 * b + 1], 1, 0);
+  group_systematic_fill(C, N, Q, r >> 9, ~0ull / (uint64_t)N, anc, tg, ADAPT_TPB);
+}
+
+// rows of every posterior gathered by its ancestors (identity when it did not resample)
+template <int D>
+__global__ void __launch_bounds__(SMC_TPB) k_smc_gather(SMCView v) {
+  const int64_t P = (int64_t)v.B * v.N;
+  const int64_t p = blockIdx.x * (int64_t)SMC_TPB + threadIdx.x;
+  if (p >= P) return;
+  const int64_t b = p / v.N;
+  const int64_t src = b * v.N + v.anc[p];
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    v.beta_p[p * D + k] = v.beta[src * D + k];
+    v.glik_p[p * D + k] = v.glik[src * D + k];
+  }
+  v.lik_p[p] = v.lik[src];
+}
+
+// MALA, first half: fresh momentum, half step, position step
+template <int D>
+__global__ void __launch_bounds__(SMC_TPB) k_mala_pre(SMCView v, float eps, float inv_s2) {
+  const int64_t P = (int64_t)v.B * v.N;
+  const int64_t p = blockIdx.x * (int64_t)SMC_TPB + threadIdx.x;
+  if (p >= P || !v.active[p / v.N]) return;
+  const float tau = v.tau[p / v.N];
+  const uint32_t k0 = v.pkey[2 * p], k1 = v.pkey[2 * p + 1];
+  uint32_t n0, n1, a0, a1;
+  split2(k0, k1, 0, n0, n1);
+  split2(k0, k1, 1, a0, a1);
+  float mom[D];
+  normal_vec<D>(a0, a1, mom);
+  const float he = eps / 2.0f;
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    const float bk = v.beta[p * D + k];
+    const float gu = __fadd_rn(__fmul_rn(bk, inv_s2), __fmul_rn(tau, v.glik[p * D + k]));
+    const float ph = __fsub_rn(mom[k], __fmul_rn(he, gu));
+    v.mom[p * D + k] = mom[k];
+    v.phalf[p * D + k] = ph;
+    v.beta_p[p * D + k] = __fadd_rn(bk, __fmul_rn(eps, ph));
+  }
+  v.pkey[2 * p] = n0;
+  v.pkey[2 * p + 1] = n1;
+}
+
+template <int D>
+__device__ __forceinline__ float prior_pot(const float *bt, float inv_s2) {
+  float q = 0.0f;
+#pragma unroll
+  for (int k = 0; k < D; ++k) q = __fmaf_rn(bt[k], bt[k], q);
+  return __fmul_rn(__fmul_rn(0.5f, q), inv_s2);
+}
+
+// MALA, second half: half step at the proposal, Metropolis correction
+template <int D>
+__global__ void __launch_bounds__(SMC_TPB) k_mala_post(SMCView v, float eps, float inv_s2) {
+  const int64_t P = (int64_t)v.B * v.N;
+  const int64_t p = blockIdx.x * (int64_t)SMC_TPB + threadIdx.x;
+  if (p >= P || !v.active[p / v.N]) return;
+  const float tau = v.tau[p / v.N];
+  float bo[D], bn[D];
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    bo[k] = v.beta[p * D + k];
+    bn[k] = v.beta_p[p * D + k];
+  }
+  const float U = __fadd_rn(prior_pot<D>(bo, inv_s2), __fmul_rn(tau, v.lik[p]));
+  const float Un = __fadd_rn(prior_pot<D>(bn, inv_s2), __fmul_rn(tau, v.lik_p[p]));
+  const float he = eps / 2.0f;
+  float K = 0.0f, Kn = 0.0f;
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    const float gu = __fadd_rn(__fmul_rn(bn[k], inv_s2), __fmul_rn(tau, v.glik_p[p * D + k]));
+    const float pn = __fsub_rn(v.phalf[p * D + k], __fmul_rn(he, gu));
+    const float pm = v.mom[p * D + k];
+    K = __fmaf_rn(pm, pm, K);
+    Kn = __fmaf_rn(pn, pn, Kn);
+  }
+  K = __fmul_rn(0.5f, K);
+  Kn = __fmul_rn(0.5f, Kn);
+  float alpha = fminf(1.0f, expf(__fadd_rn(__fsub_rn(__fadd_rn(-Un, U), Kn), K)));
+  if (alpha != alpha) alpha = 0.0f;
+  // proposal: key = split(key, 2)[0]; correct: (key, sub) = split(key)
+  const uint32_t k0 = v.pkey[2 * p], k1 = v.pkey[2 * p + 1];
+  uint32_t q0, q1, n0, n1, u0, u1;
+  split2(k0, k1, 0, q0, q1);
+  split2(q0, q1, 0, n0, n1);
+  split2(q0, q1, 1, u0, u1);
+  const float u = bits_to_unit(bits_at(u0, u1, 1, 0));
+  if (u < alpha) {
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      v.beta[p * D + k] = bn[k];
+      v.glik[p * D + k] = v.glik_p[p * D + k];
+    }
+    v.lik[p] = v.lik_p[p];
+  }
+  v.alpha[p] += alpha;
+  v.pkey[2 * p] = n0;
+  v.pkey[2 * p + 1] = n1;
+}
+
+// after the moves: likelihood potential as the sampler derives it, (U - prior) / tau
+template <int D>
+__global__ void __launch_bounds__(SMC_TPB) k_smc_after(SMCView v, float inv_s2) {
+  const int64_t P = (int64_t)v.B * v.N;
+  const int64_t p = blockIdx.x * (int64_t)SMC_TPB + threadIdx.x;
+  if (p >= P || !v.active[p / v.N]) return;
+  const float tau = v.tau[p / v.N];
+  float bt[D];
+#pragma unroll
+  for (int k = 0; k < D; ++k) bt[k] = v.beta[p * D + k];
+  const float pr = prior_pot<D>(bt, inv_s2);
+  const float U = __fadd_rn(pr, __fmul_rn(tau, v.lik[p]));
+  v.lik_w[p] = __fdiv_rn(__fsub_rn(U, pr), tau);
+}
+
+// block-wide (max, sum e, sum e^2) of v_k = base_k - dt * l_k over one posterior
+struct Lse3 {
+  float lse, logess;
+  int nan;
+};
+__device__ __forceinline__ Lse3 block_lse3(const float *base, const float *l, float dt, int N, float *red) {
+  float m = -INFINITY, s1 = 0.0f, s2 = 0.0f;
+  int nanf = 0;
+  for (int k = threadIdx.x; k < N; k += ADAPT_TPB) {
+    const float b0 = base ? base[k] : 0.0f;
+    const float x = dt == 0.0f ? b0 : __fsub_rn(b0, __fmul_rn(dt, l[k]));
+    online_acc(x, m, s1, s2, nanf);
+  }
+  const LsePartial part = block_online_partial<ADAPT_TPB>(m, s1, s2, nanf, red);
+  Lse3 o;
+  o.nan = part.nan;
+  o.lse = part.m + logf(part.s1);
+  o.logess = 2.0f * logf(part.s1) - logf(part.s2);
+  if (part.nan) o.lse = o.logess = __int_as_float(0x7fc00000);
+  return o;
+}
+
+// next temperature (regula falsi), log-weights, ESS, log Z; one CTA per posterior
+__global__ void __launch_bounds__(ADAPT_TPB) k_smc_adapt(SMCView v, const float *ell_all, SMCParams sp, int startup) {
+  __shared__ float red[ADAPT_TPB / 32];
+  __shared__ int nan_count;
+  const int b = blockIdx.x, N = v.N;
+  if (!v.active[b]) return;
+  const float *ell = ell_all + (int64_t)b * N;
+  float *lw = v.lw + (int64_t)b * N;
+  const int res = v.resampled[b];
+  const float *base = res ? nullptr : lw;
+  const float ess_res = res ? (float)N : v.ess[b];
+  const float tau0 = v.tau[b];
+  const float target = logf(__fmul_rn(ess_res, sp.retain));
+  auto f = [&](float x) { return block_lse3(base, ell, __fsub_rn(x, tau0), N, red).logess - target; };
+  // utils.bisect on [tau0, max_temperature]
+  float b0 = tau0, b1 = sp.max_temp;
+  float e0 = f(b0), e1 = f(b1);
+  const bool incr = e1 > e0;
+  for (int it = 0; it < sp.max_bisect; ++it) {
+    const bool conv = fminf(fabsf(e0), fabsf(e1)) < sp.tol || (e0 < 0.0f && e1 < 0.0f) || (e0 > 0.0f && e1 > 0.0f);
+    if (conv) break;
+    const float np = __fsub_rn(b0, __fdiv_rn(__fmul_rn(e0, __fsub_rn(b1, b0)), __fsub_rn(e1, e0)));
+    const float ne = f(np);
+    const bool up = incr ? ne > 0.0f : ne < 0.0f;
+    if (up) {
+      b1 = np;
+      e1 = ne;
+    } else {
+      b0 = np;
+      e0 = ne;
+    }
+  }
+  const float tau1 = fabsf(e1) < fabsf(e0) ? b1 : b0;
+  const float dt = __fsub_rn(tau1, tau0);
+  // LSE of the log-weights the step started from, then the new log-weights (in place)
+  float lse_res = logf((float)N);
+  if (!res) lse_res = block_lse3(base, ell, 0.0f, N, red).lse;
+  for (int k = threadIdx.x; k < N; k += ADAPT_TPB) {
+    const float b0 = base ? base[k] : 0.0f;
+    lw[k] = dt == 0.0f ? b0 : __fsub_rn(b0, __fmul_rn(dt, ell[k]));
+  }
+  __syncthreads();
+  const Lse3 nw = block_lse3(lw, ell, 0.0f, N, red);
+  // NaN entries of the particles (termination when more than 10 %)
+  if (threadIdx.x == 0) nan_count = 0;
+  __syncthreads();
+  int cnt = 0;
+  for (int64_t u = threadIdx.x; u < (int64_t)N * v.D; u += ADAPT_TPB) {
+    const float x = v.beta[(int64_t)b * N * v.D + u];
+    cnt += x != x;
+  }
+  cnt = warp_sum(cnt);
+  if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(&nan_count, cnt);
+  float asum = 0.0f;
+  for (int k = threadIdx.x; k < N; k += ADAPT_TPB) asum += v.alpha[(int64_t)b * N + k];
+  asum = block_sum<ADAPT_TPB, float>(asum, red);
+  if (threadIdx.x == 0) {
+    const int it = startup ? 0 : v.iter[b] + 1;
+    const double lz = startup ? (double)nw.lse - (double)lse_res : v.logz[b] + (double)nw.lse - (double)lse_res;
+    const float ess = expf(nw.logess);
+    v.tau[b] = tau1;
+    v.ess[b] = ess;
+    v.logz[b] = lz;
+    v.iter[b] = it;
+    if (!startup) {
+      v.key[2 * b] = v.key_next[2 * b];
+      v.key[2 * b + 1] = v.key_next[2 * b + 1];
+    }
+    const bool nan_stop = (float)nan_count / ((float)N * (float)v.D) > 0.1f;
+    v.active[b] = !(tau1 >= sp.max_temp || it >= sp.max_iter || nan_stop);
+    if (it < v.H) {
+      v.h_tau[(int64_t)b * v.H + it] = tau1;
+      v.h_logz[(int64_t)b * v.H + it] = lz;
+      v.h_ess[(int64_t)b * v.H + it] = ess;
+      v.h_alpha[(int64_t)b * v.H + it] = startup ? 1.0f : asum / ((float)N * (float)sp.mcmc_steps);
+      v.h_res[(int64_t)b * v.H + it] = startup ? 0 : res;
+    }
+  }
+}
+
+// ------------------------------------------------------------ host side
+SMCView carve_smc(Carver &c, int B, int N, int d, int H) {
+  const size_t P = (size_t)B * N;
+  SMCView v{};
+  v.B = B;
+  v.N = N;
+  v.D = d;
+  v.H = H;
+  v.beta = c.take<float>(P * d);
+  v.beta_p = c.take<float>(P * d);
+  v.glik = c.take<float>(P * d);
+  v.glik_p = c.take<float>(P * d);
+  v.mom = c.take<float>(P * d);
+  v.phalf = c.take<float>(P * d);
+  v.lik = c.take<float>(P);
+  v.lik_p = c.take<float>(P);
+  v.lik_w = c.take<float>(P);
+  v.lw = c.take<float>(P);
+  v.alpha = c.take<float>(P);
+  v.pkey = c.take<uint32_t>(2 * P);
+  v.anc = c.take<int32_t>(P);
+  v.tau = c.take<float>(B);
+  v.ess = c.take<float>(B);
+  v.logz = c.take<double>(B);
+  v.key = c.take<uint32_t>(2 * (size_t)B);
+  v.key_next = c.take<uint32_t>(2 * (size_t)B);
+  v.rkey = c.take<uint32_t>(2 * (size_t)B);
+  v.iter = c.take<int32_t>(B);
+  v.active = c.take<int32_t>(B);
+  v.resampled = c.take<int32_t>(B);
+  v.h_tau = c.take<float>((size_t)B * H);
+  v.h_logz = c.take<double>((size_t)B * H);
+  v.h_ess = c.take<float>((size_t)B * H);
+  v.h_alpha = c.take<float>((size_t)B * H);
+  v.h_res = c.take<int32_t>((size_t)B * H);
+  return v;
+}
+
+static bool smc_cfg_ok(const mgb_smc_logreg_config *cfg) {
+  return cfg && cfg->B >= 1 && cfg->N >= 2 && cfg->N <= MGB_SMC_MAX_N && cfg->d >= 1 && cfg->mcmc_steps >= 1 &&
+         cfg->max_iter >= 1 && cfg->max_bisection_iter >= 0 && cfg->prior_scale > 0.0f && cfg->stepsize > 0.0f &&
+         (cfg->precision == MGB_PREC_FP32 || cfg->precision == MGB_PREC_BF16);
+}
+
+static size_t smc_pot_ws(const mgb_smc_logreg_config *cfg, int64_t n_data) {
+  const int64_t P = (int64_t)cfg->B * cfg->N;
+  size_t a = logreg_f32_workspace(P, n_data, cfg->d);
+  if (cfg->precision == MGB_PREC_BF16) {
+    const size_t b = logreg_tc_workspace(P, n_data, cfg->d);
+    if (b > a) a = b;
+  }
+  return a;
+}
+
+static int smc_potential(const mgb_smc_logreg_config *cfg, const SMCData &dat, const float *beta, float *lik,
+                         float *grad, const int32_t *active, void *ws, size_t ws_bytes, cudaStream_t s) {
+  const int64_t P = (int64_t)cfg->B * cfg->N;
+  const int d = cfg->d;
+  if (cfg->precision == MGB_PREC_BF16)
+    return logreg_tc(dat, beta, P, active, cfg->N, lik, grad, ws, ws_bytes, s);
+  MGB_SMC_D_DISPATCH(logreg_f32, dat.X, dat.y, dat.n_data, beta, P, active, cfg->N, lik, grad, ws, ws_bytes, s);
+}
+
+template <int D>
+static int smc_init_t(const mgb_smc_logreg_config *cfg, const SMCData &dat, const uint32_t *keys, SMCView v,
+                      void *pws, size_t pws_bytes, cudaStream_t s) {
+  const int64_t P = (int64_t)cfg->B * cfg->N;
+  const unsigned g = (unsigned)((P + SMC_TPB - 1) / SMC_TPB);
+  k_smc_prior<D><<<g, SMC_TPB, 0, s>>>(v, keys, cfg->prior_scale);
+  int st = launch_status();
+  if (st) return st;
+  if ((st = smc_potential(cfg, dat, v.beta, v.lik, v.glik, nullptr, pws, pws_bytes, s))) return st;
+  SMCParams sp{cfg->ess_threshold_retain, cfg->max_temperature, cfg->bisection_tol, cfg->max_bisection_iter,
+               cfg->max_iter, cfg->mcmc_steps};
+  if (cudaMemsetAsync(v.alpha, 0, sizeof(float) * P, s) != cudaSuccess) return ERR_CUDA;
+  k_smc_adapt<<<cfg->B, ADAPT_TPB, 0, s>>>(v, v.lik, sp, 1);
+  return launch_status();
+}
+
+template <int D>
+static int smc_step_t(const mgb_smc_logreg_config *cfg, const SMCData &dat, SMCView v, void *pws, size_t pws_bytes,
+                      cudaStream_t s) {
+  const int64_t P = (int64_t)cfg->B * cfg->N;
+  const unsigned g = (unsigned)((P + SMC_TPB - 1) / SMC_TPB);
+  const float inv_s2 = (float)(1.0 / ((double)cfg->prior_scale * (double)cfg->prior_scale));
+  int st;
+  k_smc_keys<<<g, SMC_TPB, 0, s>>>(v, cfg->ess_threshold_resample);
+  if ((st = launch_status())) return st;
+  const size_t rs_smem = sizeof(uint64_t) * (size_t)cfg->N;
+  if (cudaFuncSetAttribute(k_smc_resample, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rs_smem) != cudaSuccess)
+    return ERR_UNSUPPORTED;
+  k_smc_resample<<<cfg->B, ADAPT_TPB, rs_smem, s>>>(v);
+  if ((st = launch_status())) return st;
+  k_smc_gather<D><<<g, SMC_TPB, 0, s>>>(v);
+  if ((st = launch_status())) return st;
+  // the gathered rows become the state (pointer swap inside the view copy)
+  SMCView w = v;
+  std::swap(w.beta, w.beta_p);
+  std::swap(w.glik, w.glik_p);
+  std::swap(w.lik, w.lik_p);
+  for (int m = 0; m < cfg->mcmc_steps; ++m) {
+    k_mala_pre<D><<<g, SMC_TPB, 0, s>>>(w, cfg->stepsize, inv_s2);
+    if ((st = launch_status())) return st;
+    if ((st = smc_potential(cfg, dat, w.beta_p, w.lik_p, w.glik_p, w.active, pws, pws_bytes, s))) return st;
+    k_mala_post<D><<<g, SMC_TPB, 0, s>>>(w, cfg->stepsize, inv_s2);
+    if ((st = launch_status())) return st;
+  }
+  k_smc_after<D><<<g, SMC_TPB, 0, s>>>(w, inv_s2);
+  if ((st = launch_status())) return st;
+  SMCParams sp{cfg->ess_threshold_retain, cfg->max_temperature, cfg->bisection_tol, cfg->max_bisection_iter,
+               cfg->max_iter, cfg->mcmc_steps};
+  k_smc_adapt<<<cfg->B, ADAPT_TPB, 0, s>>>(w, w.lik_w, sp, 0);
+  if ((st = launch_status())) return st;
+  // the state lives in the swapped buffers now: copy back so the layout stays fixed
+  if (cudaMemcpyAsync(v.beta, w.beta, sizeof(float) * P * D, cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
+      cudaMemcpyAsync(v.glik, w.glik, sizeof(float) * P * D, cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
+      cudaMemcpyAsync(v.lik, w.lik, sizeof(float) * P, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+    return ERR_CUDA;
+  return OK;
+}
+
+}  // namespace mgb
+
+using namespace mgb;
+
+extern "C" {
+
+size_t mgb_logreg_workspace(int64_t P, int64_t n_data, int32_t d, int precision) {
+  if (P < 1 || n_data < 1 || d < 1) return 0;
+  size_t a = logreg_f32_workspace(P, n_data, d);
+  if (precision == MGB_PREC_BF16) {
+    const size_t b = logreg_tc_workspace(P, n_data, d);
+    if (b > a) a = b;
+  }
+  return a;
+}
+
+int mgb_logreg_potential_grad(const float *X, const float *y, int64_t n_data, int32_t d, const float *beta,
+                              int64_t P, float *lik, float *grad, int precision, const void *Xbf16, void *ws,
+                              size_t ws_bytes, void *stream) {
+  if (!X || !y || !beta || !lik || !grad || n_data < 1 || d < 1 || P < 1 || !ws) return ERR_BAD_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (precision == MGB_PREC_BF16) {
+    if (!Xbf16) return ERR_BAD_ARG;
+    SMCData dat{X, y, (const uint16_t *)Xbf16, n_data, d};
+    return logreg_tc(dat, beta, P, nullptr, (int)P, lik, grad, ws, ws_bytes, s);
+  }
+  if (precision != MGB_PREC_FP32) return ERR_BAD_ARG;
+  MGB_SMC_D_DISPATCH(logreg_f32, X, y, n_data, beta, P, nullptr, 0, lik, grad, ws, ws_bytes, s);
+}
+
+size_t mgb_smc_logreg_workspace(const mgb_smc_logreg_config *cfg, int64_t n_data) {
+  if (!smc_cfg_ok(cfg) || n_data < 1) return 0;
+  Carver c(nullptr);
+  carve_smc(c, cfg->B, cfg->N, cfg->d, cfg->max_iter + 1);
+  c.take<unsigned char>(smc_pot_ws(cfg, n_data));
+  return c.bytes();
+}
+
+int mgb_smc_logreg_views(const mgb_smc_logreg_config *cfg, void *ws, mgb_smc_views *out) {
+  if (!smc_cfg_ok(cfg) || !ws || !out) return ERR_BAD_ARG;
+  Carver c(ws);
+  const SMCView v = carve_smc(c, cfg->B, cfg->N, cfg->d, cfg->max_iter + 1);
+  out->value = v.beta;
+  out->log_weight = v.lw;
+  out->likelihood_potential = v.lik;
+  out->temperature = v.tau;
+  out->ess = v.ess;
+  out->log_norm_constant = v.logz;
+  out->iter = v.iter;
+  out->active = v.active;
+  out->hist_temperature = v.h_tau;
+  out->hist_log_norm_constant = v.h_logz;
+  out->hist_ess = v.h_ess;
+  out->hist_alpha = v.h_alpha;
+  out->hist_resampled = v.h_res;
+  out->hist_len = v.H;
+  return OK;
+}
+
+static int smc_setup(const mgb_smc_logreg_config *cfg, const float *X, const float *y, const void *Xbf16,
+                     int64_t n_data, void *ws, size_t ws_bytes, SMCData &dat, SMCView &v, void *&pws,
+                     size_t &pws_bytes) {
+  if (!smc_cfg_ok(cfg) || !X || !y || n_data < 1 || !ws) return ERR_BAD_ARG;
+  if (cfg->precision == MGB_PREC_BF16 && !Xbf16) return ERR_BAD_ARG;
+  if (ws_bytes < mgb_smc_logreg_workspace(cfg, n_data)) return ERR_WORKSPACE;
+  Carver c(ws);
+  v = carve_smc(c, cfg->B, cfg->N, cfg->d, cfg->max_iter + 1);
+  pws_bytes = smc_pot_ws(cfg, n_data);
+  pws = c.take<unsigned char>(pws_bytes);
+  dat = SMCData{X, y, (const uint16_t *)Xbf16, n_data, cfg->d};
+  return OK;
+}
+
+int mgb_smc_logreg_init(const mgb_smc_logreg_config *cfg, const float *X, const float *y, const void *Xbf16,
+                        int64_t n_data, const uint32_t *keys, void *ws, size_t ws_bytes, void *stream) {
+  SMCData dat;
+  SMCView v;
+  void *pws;
+  size_t pb;
+  int st = smc_setup(cfg, X, y, Xbf16, n_data, ws, ws_bytes, dat, v, pws, pb);
+  if (st) return st;
+  if (!keys) return ERR_BAD_ARG;
+  const int d = cfg->d;
+  MGB_SMC_D_DISPATCH(smc_init_t, cfg, dat, keys, v, pws, pb, (cudaStream_t)stream);
+}
+
+int mgb_smc_logreg_step(const mgb_smc_logreg_config *cfg, const float *X, const float *y, const void *Xbf16,
+                        int64_t n_data, void *ws, size_t ws_bytes, void *stream) {
+  SMCData dat;
+  SMCView v;
+  void *pws;
+  size_t pb;
+  int st = smc_setup(cfg, X, y, Xbf16, n_data, ws, ws_bytes, dat, v, pws, pb);
+  if (st) return st;
+  const int d = cfg->d;
+  MGB_SMC_D_DISPATCH(smc_step_t, cfg, dat, v, pws, pb, (cudaStream_t)stream);
+}
+
+}  // extern "C"
