@@ -1,15 +1,384 @@
-// Logistic-regression potential and gradient on the tensor cores (bf16
-// operands, fp32 accumulation): not built yet; the entry reports
-// MGB_ERR_UNSUPPORTED.
+// Logistic-regression likelihood potential and its gradient for many
+// parameter rows on the 5th-generation tensor cores (tcgen05, bf16 operands,
+// fp32 accumulation in tensor memory), fused so that the (n_data x P) matrix
+// of linear predictors never reaches HBM.
+//
+// For 128 parameter rows beta (one CTA) and the data streamed in 128-row tiles:
+//   MMA1  Z = beta X_t^T          M = 128 rows, N = 128 data rows, K = 64 features
+//   epi   pot += sum softplus(z) - y z;   R = sigmoid(Z) - y  (bf16, into smem)
+//   MMA2  G += R X_t              M = 128 rows, N = 64 features, K = 128 data rows
+// Reference computation: the vmapped likelihood_potential_and_grad that
+// mocat's MALA moves call (mocat/src/mcmc/standard_mcmc.py:121-131,
+// mocat/src/utils.py:121-131) for the logistic scenario.
+//
+// Warp roles (192 threads): warp 0 issues the TMA loads of X tiles (128B
+// swizzle) into a 4-stage ring; warp 1 owns tensor memory and issues the MMAs
+// from one thread; warps 2-5 are the epilogue, each reading its 32-lane
+// quarter of the accumulators with tcgen05.ld.  Z is double-buffered in
+// tensor memory (2 x 128 columns) so MMA1 of tile t+1 overlaps the epilogue of
+// tile t; G takes 64 more columns.  Every mbarrier wait is bounded: a wait that
+// runs out sets an error bit, raises a CTA-wide abort flag and the CTA drains.
+// Operand layouts (K-major / MN-major, SWIZZLE_128B, 1024-byte aligned tiles):
+//   beta tile  128 x 64 bf16 K-major    (written by the CTA from fp32 rows)
+//   X tile     128 x 64 bf16 row-major: K-major B of MMA1, MN-major B of MMA2
+//   R tile     128 x 128 bf16 K-major   (two 64-column sub-tiles)
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+
 #include "mgb_smc.cuh"
 
 namespace mgb {
 
+constexpr int TC_ROWS = 128;     // parameter rows per CTA (MMA M)
+constexpr int TC_DT = 128;       // data rows per tile
+constexpr int TC_K = 64;         // padded feature count
+constexpr int TC_STAGES = 4;
+constexpr int TC_THREADS = 192;
+constexpr uint32_t TC_TMEM_COLS = 512;
+constexpr uint32_t TILE_BYTES = TC_DT * TC_K * 2;  // 16 KB
+// alignment slack + beta tile + X ring + R double buffer + one tile of guard space
+constexpr size_t TC_SMEM = 1024 + TILE_BYTES + TC_STAGES * TILE_BYTES + 2 * 2 * TILE_BYTES + TILE_BYTES;
+constexpr uint32_t TC_WAIT_LIMIT = 1u << 24;
+
+// ---------------------------------------------------------------- PTX helpers
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *b, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint64_t *b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait; false when it ran out or the CTA aborted
+__device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, volatile int *abort) {
+  for (uint32_t i = 0; i < TC_WAIT_LIMIT; ++i) {
+    if (mbar_try(b, parity)) return true;
+    if (*abort) return false;
+  }
+  *abort = 1;
+  return false;
+}
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_u32(dst)),
+      "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// shared-memory matrix descriptor, SWIZZLE_128B, both byte offsets 1024
+// (8-row group stride; the other offset is unused for a 128-byte-wide atom)
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
+  uint64_t d = (uint64_t)((addr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)(1024u >> 4) << 16;
+  d |= (uint64_t)(1024u >> 4) << 32;
+  d |= (uint64_t)1 << 46;  // descriptor version
+  d |= (uint64_t)2 << 61;  // SWIZZLE_128B
+  return d;
+}
+// instruction descriptor, kind::f16: bf16 A/B, fp32 D, M x N, operand majorness
+__host__ __device__ constexpr uint32_t bf16_idesc(int M, int N, bool a_mn, bool b_mn) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((a_mn ? 1u : 0u) << 15) | ((b_mn ? 1u : 0u) << 16) |
+         ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+          d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+#define MGB_TMEM_LD32(taddr, v)                                                                                    \
+  asm volatile(                                                                                                    \
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, " \
+      "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"              \
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),          \
+        "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),    \
+        "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),  \
+        "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])   \
+      : "r"(taddr))
+__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// byte offset of element (row, col) of a 64-column bf16 K-major SWIZZLE_128B tile
+__device__ __forceinline__ uint32_t sw128_off(int row, int col) {
+  return (uint32_t)row * 128u + ((((uint32_t)col >> 3) ^ ((uint32_t)row & 7u)) << 4) + (((uint32_t)col & 7u) << 1);
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  return *(const uint32_t *)&h;
+}
+
+struct TCArgs {
+  const float *beta;
+  const float *y;
+  const int32_t *active;
+  float *lik, *grad;
+  int *err;
+  int64_t P, n_data;
+  int d, N;
+};
+
+__global__ void __launch_bounds__(TC_THREADS, 1) k_logreg_tc(const __grid_constant__ CUtensorMap xmap,
+                                                             const __grid_constant__ TCArgs a) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bar_xfull[TC_STAGES], bar_xempty[TC_STAGES];
+  __shared__ __align__(8) uint64_t bar_zfull[2], bar_zempty[2], bar_rfull[2], bar_rempty[2], bar_gdone;
+  __shared__ uint32_t tmem_slot;
+  __shared__ volatile int abort_flag;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t row0 = (int64_t)blockIdx.x * TC_ROWS;
+
+  // nothing to do when every posterior of this tile has finished
+  if (a.active) {
+    bool any = false;
+    const int64_t last = min(row0 + TC_ROWS, a.P) - 1;
+    for (int64_t b = row0 / a.N; b <= last / a.N; ++b) any |= a.active[b] != 0;
+    if (!any) return;
+  }
+
+  unsigned char *base = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  unsigned char *sA = base;                        // beta tile
+  unsigned char *sX = sA + TILE_BYTES;             // X ring
+  unsigned char *sR = sX + TC_STAGES * TILE_BYTES;  // R double buffer, 2 sub-tiles each
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < TC_STAGES; ++s) {
+      mbar_init(&bar_xfull[s], 1);
+      mbar_init(&bar_xempty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&bar_zfull[b], 1);
+      mbar_init(&bar_zempty[b], 128);
+      mbar_init(&bar_rfull[b], 128);
+      mbar_init(&bar_rempty[b], 1);
+    }
+    mbar_init(&bar_gdone, 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                 "r"(TC_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  // beta rows -> bf16 K-major swizzled tile (zero rows past P / of finished posteriors, zero columns past d)
+  for (int u = threadIdx.x; u < TC_ROWS * (TC_K / 8); u += TC_THREADS) {
+    const int r = u >> 3, ch = u & 7;
+    const int64_t p = row0 + r;
+    const bool live = p < a.P && (!a.active || a.active[p / a.N]);
+    float v[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int c = ch * 8 + e;
+      v[e] = (live && c < a.d) ? a.beta[p * a.d + c] : 0.0f;
+    }
+    uint4 q;
+    q.x = pack_bf16(v[0], v[1]);
+    q.y = pack_bf16(v[2], v[3]);
+    q.z = pack_bf16(v[4], v[5]);
+    q.w = pack_bf16(v[6], v[7]);
+    *(uint4 *)(sA + sw128_off(r, ch * 8)) = q;
+  }
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  const uint32_t tg = tmem + 256u;  // Z buffers at columns 0 and 128, G at 256
+  const int nt = (int)((a.n_data + TC_DT - 1) / TC_DT);
+
+  if (warp == 0) {
+    // ---------------------------------------------------------------- TMA producer
+    if (lane == 0) {
+      for (int t = 0; t < nt; ++t) {
+        const int s = t % TC_STAGES;
+        if (!mbar_wait(&bar_xempty[s], ((t / TC_STAGES) & 1) ^ 1, &abort_flag)) break;
+        mbar_expect_tx(&bar_xfull[s], TILE_BYTES);
+        tma_load_2d(sX + s * TILE_BYTES, &xmap, 0, t * TC_DT, &bar_xfull[s]);
+      }
+    }
+  } else if (warp == 1) {
+    // ---------------------------------------------------------------- MMA issuer
+    if (lane == 0) {
+      const uint32_t id1 = bf16_idesc(128, 128, false, false);
+      const uint32_t id2 = bf16_idesc(128, 64, false, true);
+      const uint32_t aA = smem_u32(sA);
+      bool ok = true;
+      for (int t = 0; t <= nt && ok; ++t) {
+        if (t < nt) {
+          const int s = t % TC_STAGES, zb = t & 1;
+          ok = mbar_wait(&bar_xfull[s], (t / TC_STAGES) & 1, &abort_flag) &&
+               mbar_wait(&bar_zempty[zb], ((t >> 1) & 1) ^ 1, &abort_flag);
+          if (!ok) break;
+          tc_fence_after();
+          const uint32_t aX = smem_u32(sX + s * TILE_BYTES);
+#pragma unroll
+          for (int k = 0; k < TC_K / 16; ++k)
+            mma_bf16(tmem + zb * 128u, sw128_desc(aA + k * 32), sw128_desc(aX + k * 32), id1, k > 0 ? 1u : 0u);
+          mma_commit(&bar_zfull[zb]);
+        }
+        if (t >= 1) {
+          const int u = t - 1, rb = u & 1, s = u % TC_STAGES;
+          ok = mbar_wait(&bar_rfull[rb], (u >> 1) & 1, &abort_flag);
+          if (!ok) break;
+          tc_fence_after();
+          const uint32_t aR = smem_u32(sR + rb * 2 * TILE_BYTES);
+          const uint32_t aX = smem_u32(sX + s * TILE_BYTES);
+#pragma unroll
+          for (int k = 0; k < TC_DT / 16; ++k)
+            mma_bf16(tg, sw128_desc(aR + (k >> 2) * TILE_BYTES + (k & 3) * 32), sw128_desc(aX + k * 2048), id2,
+                     (u > 0 || k > 0) ? 1u : 0u);
+          mma_commit(&bar_xempty[s]);
+          mma_commit(&bar_rempty[rb]);
+        }
+      }
+      mma_commit(&bar_gdone);
+    }
+  } else {
+    // ---------------------------------------------------------------- epilogue
+    const int q = warp & 3;             // tensor-memory lane quarter of this warp
+    const int row = q * 32 + lane;      // parameter row within the tile
+    const uint32_t lane_off = (uint32_t)(q * 32) << 16;
+    double pot = 0.0;
+    bool ok = true;
+    for (int t = 0; t < nt && ok; ++t) {
+      const int zb = t & 1, rb = t & 1;
+      ok = mbar_wait(&bar_zfull[zb], (t >> 1) & 1, &abort_flag) &&
+           mbar_wait(&bar_rempty[rb], ((t >> 1) & 1) ^ 1, &abort_flag);
+      if (!ok) break;
+      tc_fence_after();
+      unsigned char *R = sR + rb * 2 * TILE_BYTES;
+      float tsum = 0.0f;
+#pragma unroll 1
+      for (int c = 0; c < TC_DT / 32; ++c) {
+        uint32_t v[32];
+        MGB_TMEM_LD32(tmem + zb * 128u + lane_off + (uint32_t)(c * 32), v);
+        tmem_ld_wait();
+        uint32_t packed[16];
+#pragma unroll
+        for (int j = 0; j < 32; j += 2) {
+          float r2[2];
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const int64_t i = (int64_t)t * TC_DT + c * 32 + j + h;
+            float r = 0.0f;
+            if (i < a.n_data) {
+              const float z = __uint_as_float(v[j + h]);
+              const float yi = __ldg(&a.y[i]);
+              const float e = __expf(-fabsf(z));
+              const float inv = __fdividef(1.0f, 1.0f + e);
+              tsum += fmaxf(z, 0.0f) + __logf(1.0f + e) - yi * z;
+              r = (z >= 0.0f ? inv : e * inv) - yi;
+            }
+            r2[h] = r;
+          }
+          packed[j >> 1] = pack_bf16(r2[0], r2[1]);
+        }
+        unsigned char *sub = R + (c >> 1) * TILE_BYTES;
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+          const int col = (c & 1) * 32 + m * 8;
+          *(uint4 *)(sub + sw128_off(row, col)) =
+              make_uint4(packed[4 * m], packed[4 * m + 1], packed[4 * m + 2], packed[4 * m + 3]);
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(&bar_zempty[zb]);
+      fence_async_smem();
+      mbar_arrive(&bar_rfull[rb]);
+      pot += (double)tsum;
+    }
+    if (ok && mbar_wait(&bar_gdone, 0, &abort_flag)) {
+      tc_fence_after();
+      uint32_t g0[32], g1[32];
+      MGB_TMEM_LD32(tg + lane_off, g0);
+      MGB_TMEM_LD32(tg + lane_off + 32u, g1);
+      tmem_ld_wait();
+      const int64_t p = row0 + row;
+      if (p < a.P && (!a.active || a.active[p / a.N])) {
+#pragma unroll
+        for (int k = 0; k < 32; ++k) {
+          if (k < a.d) a.grad[p * a.d + k] = __uint_as_float(g0[k]);
+          if (k + 32 < a.d) a.grad[p * a.d + k + 32] = __uint_as_float(g1[k]);
+        }
+        a.lik[p] = (float)pot;
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (abort_flag && threadIdx.x == 0 && a.err) atomicOr(a.err, 1);
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
+  }
+}
+
+// ---------------------------------------------------------------- host side
+static int encode_xmap(CUtensorMap *map, const uint16_t *Xb, int64_t n_data) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (!encode) {
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn)
+      return ERR_UNSUPPORTED;
+    encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+  }
+  const cuuint64_t dims[2] = {(cuuint64_t)TC_K, (cuuint64_t)n_data};
+  const cuuint64_t strides[1] = {(cuuint64_t)TC_K * 2};
+  const cuuint32_t box[2] = {(cuuint32_t)TC_K, (cuuint32_t)TC_DT};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void *)Xb, dims, strides, box, estr,
+                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? OK : ERR_BAD_ARG;
+}
+
 size_t logreg_tc_workspace(int64_t, int64_t, int) { return 256; }
 
-int logreg_tc(const SMCData &, const float *, int64_t, const int32_t *, int, float *, float *, void *, size_t,
-              cudaStream_t) {
-  return ERR_UNSUPPORTED;
+int logreg_tc(const SMCData &dat, const float *beta, int64_t P, const int32_t *active, int N, float *lik, float *grad,
+              void *ws, size_t ws_bytes, cudaStream_t s) {
+  if (dat.d > TC_K || !dat.Xb || ((uintptr_t)dat.Xb & 15u) || ws_bytes < 256) return ERR_BAD_ARG;
+  CUtensorMap map;
+  int st = encode_xmap(&map, dat.Xb, dat.n_data);
+  if (st) return st;
+  static bool attr = false;
+  if (!attr) {
+    if (cudaFuncSetAttribute(k_logreg_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM) != cudaSuccess)
+      return ERR_UNSUPPORTED;
+    attr = true;
+  }
+  int *err = (int *)ws;
+  if (cudaMemsetAsync(err, 0, sizeof(int), s) != cudaSuccess) return ERR_CUDA;
+  TCArgs a{beta, dat.y, active, lik, grad, err, P, dat.n_data, dat.d, N > 0 ? N : (int)P};
+  const unsigned grid = (unsigned)((P + TC_ROWS - 1) / TC_ROWS);
+  k_logreg_tc<<<grid, TC_THREADS, TC_SMEM, s>>>(map, a);
+  return launch_status();
 }
 
 }  // namespace mgb

@@ -83,3 +83,38 @@ def test_single_posterior_run(cuda):
     assert float(out.temperature[-1]) == 1.0
     assert out.value.shape == (512, 5)
     assert np.isfinite(out.log_norm_constant.cpu().numpy()).all()
+
+
+@pytest.mark.parametrize("d,n_data,P", [(5, 1000, 256), (50, 3000, 700), (50, 20000, 4096), (2, 333, 130)])
+def test_potential_bf16_tensor_cores(cuda, d, n_data, P):
+    """tcgen05 path (bf16 X and beta, fp32 accumulation) against the fp32 kernel: the
+    potential within 1e-2 relative plus bf16 rounding of the linear predictors,
+    the gradient rows within 3e-2 (relative 2-norm)."""
+    import mocat_gb300 as mg
+    X, y = _data(n_data, d, seed=d)
+    sc = mg.smc.LogisticRegression(X, y)
+    beta = (np.random.default_rng(5).standard_normal((P, d)) * 0.3).astype(np.float32)
+    bt = torch.from_numpy(beta).cuda()
+    l32, g32 = sc.likelihood_potential_and_grad(bt, precision="fp32")
+    l16, g16 = sc.likelihood_potential_and_grad(bt, precision="bf16")
+    l32, g32, l16, g16 = (t.double().cpu().numpy() for t in (l32, g32, l16, g16))
+    assert np.isfinite(l16).all() and np.isfinite(g16).all()
+    rel = np.abs(l16 - l32) / np.abs(l32)
+    assert rel.max() < 1e-2, rel.max()
+    gr = np.linalg.norm(g16 - g32, axis=1) / np.linalg.norm(g32, axis=1)
+    assert np.median(gr) < 3e-2 and gr.max() < 0.1, (np.median(gr), gr.max())
+
+
+def test_sampler_bf16_close_to_fp32(cuda):
+    import mocat_gb300 as mg
+    X, y = _data(2000, 5)
+    sc = mg.smc.LogisticRegression(X, y)
+    sampler = mg.smc.MetropolisedSMCSampler(mg.smc.Underdamped(stepsize=0.02), mcmc_steps=3,
+                                            ess_threshold_retain=0.5)
+    keys = np.stack([O.PRNGKey(s) for s in range(8)])
+    z32 = mg.smc.run_batched(sc, sampler, 1024, keys, precision="fp32")
+    z16 = mg.smc.run_batched(sc, sampler, 1024, keys, precision="bf16")
+    a = np.array([float(z32.log_norm_constant[b, int(z32.iterations[b])]) for b in range(8)])
+    c = np.array([float(z16.log_norm_constant[b, int(z16.iterations[b])]) for b in range(8)])
+    assert np.isfinite(c).all()
+    assert abs(a.mean() - c.mean()) < 0.5 + 4 * (a.std() + c.std()) / np.sqrt(8), (a.mean(), c.mean())
