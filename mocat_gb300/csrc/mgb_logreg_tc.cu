@@ -11,10 +11,11 @@
 // mocat's MALA moves call (mocat/src/mcmc/standard_mcmc.py:121-131,
 // mocat/src/utils.py:121-131) for the logistic scenario.
 //
-// Warp roles (192 threads): warp 0 issues the TMA loads of X tiles (128B
+// Warp roles (576 threads): warp 0 issues the TMA loads of X tiles (128B
 // swizzle) into a 4-stage ring; warp 1 owns tensor memory and issues the MMAs
-// from one thread; warps 2-5 are the epilogue, each reading its 32-lane
-// quarter of the accumulators with tcgen05.ld.  Z is double-buffered in
+// from one thread; warps 2-17 are the epilogue: warp w reads lane quarter
+// w % 4 and one 32-column group of each Z tile with tcgen05.ld, so four warps
+// per scheduler hide the latency of the transcendental epilogue.  Z is double-buffered in
 // tensor memory (2 x 128 columns) so MMA1 of tile t+1 overlaps the epilogue of
 // tile t; G takes 64 more columns.  Every mbarrier wait is bounded: a wait that
 // runs out sets an error bit, raises a CTA-wide abort flag and the CTA drains.
@@ -34,7 +35,8 @@ constexpr int TC_ROWS = 128;     // parameter rows per CTA (MMA M)
 constexpr int TC_DT = 128;       // data rows per tile
 constexpr int TC_K = 64;         // padded feature count
 constexpr int TC_STAGES = 4;
-constexpr int TC_THREADS = 192;
+constexpr int TC_EPI_WARPS = 16;  // 4 column groups x 4 tensor-memory lane quarters
+constexpr int TC_THREADS = 64 + 32 * TC_EPI_WARPS;
 constexpr uint32_t TC_TMEM_COLS = 512;
 constexpr uint32_t TILE_BYTES = TC_DT * TC_K * 2;  // 16 KB
 // alignment slack + beta tile + X ring + R double buffer + one tile of guard space
@@ -125,9 +127,41 @@ __device__ __forceinline__ uint32_t sw128_off(int row, int col) {
   return (uint32_t)row * 128u + ((((uint32_t)col >> 3) ^ ((uint32_t)row & 7u)) << 4) + (((uint32_t)col & 7u) << 1);
 }
 
+__device__ __forceinline__ float exp2f_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float log2f_approx(float x) {
+  float y;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
   const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
   return *(const uint32_t *)&h;
+}
+
+// Epilogue of one pair of linear predictors z (labels y in {0, 1}):
+//   potential term softplus(z) - y z = max(w, 0) + log(1 + exp(-|z|)), w = (1 - 2y) z:
+//   s_lin += max(w, 0); prod *= (1 + exp(-|z|)) (one log2 of the product per 32 columns);
+//   gradient operand r = sigmoid(z) - y = tanh(z / 2) / 2 + (1/2 - y), packed bf16x2.
+// A padding column passes z = -inf, y = 0: it adds 0 to both sums.
+__device__ __forceinline__ void epi_pair(float z0, float z1, uint32_t y0, uint32_t y1, float &s_lin, float &prod,
+                                         uint32_t &packed) {
+  const float w0 = __uint_as_float(__float_as_uint(z0) ^ (y0 << 31));
+  const float w1 = __uint_as_float(__float_as_uint(z1) ^ (y1 << 31));
+  s_lin += fmaxf(w0, 0.0f) + fmaxf(w1, 0.0f);
+  const float e0 = exp2f_approx(-1.4426950408889634f * fabsf(z0));
+  const float e1 = exp2f_approx(-1.4426950408889634f * fabsf(z1));
+  prod = fmaf(prod, e0, prod);
+  prod = fmaf(prod, e1, prod);
+  uint32_t zh = pack_bf16(z0, z1), h;
+  asm("mul.rn.bf16x2 %0, %1, %2;" : "=r"(zh) : "r"(zh), "r"(0x3F003F00u));  // z / 2 (exact)
+  asm("tanh.approx.bf16x2 %0, %1;" : "=r"(h) : "r"(zh));
+  const uint32_t c = 0x3F003F00u | (y0 << 15) | (y1 << 31);  // (0.5 - y0, 0.5 - y1)
+  asm("fma.rn.bf16x2 %0, %1, %2, %3;" : "=r"(packed) : "r"(h), "r"(0x3F003F00u), "r"(c));
 }
 
 struct TCArgs {
@@ -147,6 +181,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_logreg_tc(const __grid_consta
   __shared__ __align__(8) uint64_t bar_zfull[2], bar_zempty[2], bar_rfull[2], bar_rempty[2], bar_gdone;
   __shared__ uint32_t tmem_slot;
   __shared__ volatile int abort_flag;
+  __shared__ double pot_s[4][TC_ROWS];
+  __shared__ int grad_ok_s;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t row0 = (int64_t)blockIdx.x * TC_ROWS;
 
@@ -170,12 +206,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_logreg_tc(const __grid_consta
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&bar_zfull[b], 1);
-      mbar_init(&bar_zempty[b], 128);
-      mbar_init(&bar_rfull[b], 128);
+      mbar_init(&bar_zempty[b], 32 * TC_EPI_WARPS);
+      mbar_init(&bar_rfull[b], 32 * TC_EPI_WARPS);
       mbar_init(&bar_rempty[b], 1);
     }
     mbar_init(&bar_gdone, 1);
     abort_flag = 0;
+    grad_ok_s = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
@@ -259,64 +296,76 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_logreg_tc(const __grid_consta
     }
   } else {
     // ---------------------------------------------------------------- epilogue
-    const int q = warp & 3;             // tensor-memory lane quarter of this warp
+    // warp w reads lane quarter w % 4 (the hardware's rule) and column group
+    // (w - 2) / 4 of 32 columns of every tile
+    const int q = warp & 3;
+    const int cg = (warp - 2) >> 2;
     const int row = q * 32 + lane;      // parameter row within the tile
     const uint32_t lane_off = (uint32_t)(q * 32) << 16;
     double pot = 0.0;
     bool ok = true;
+    float ynext = 0.0f;
+    {
+      const int64_t i = (int64_t)cg * 32 + lane;
+      if (i < a.n_data) ynext = __ldg(&a.y[i]);
+    }
     for (int t = 0; t < nt && ok; ++t) {
       const int zb = t & 1, rb = t & 1;
+      const float ycur = ynext;  // y of column cg*32 + lane of this tile (gathered into a bit mask below)
+      {
+        const int64_t i = (int64_t)(t + 1) * TC_DT + cg * 32 + lane;
+        ynext = (i < a.n_data) ? __ldg(&a.y[i]) : 0.0f;
+      }
       ok = mbar_wait(&bar_zfull[zb], (t >> 1) & 1, &abort_flag) &&
            mbar_wait(&bar_rempty[rb], ((t >> 1) & 1) ^ 1, &abort_flag);
       if (!ok) break;
       tc_fence_after();
-      unsigned char *R = sR + rb * 2 * TILE_BYTES;
-      float tsum = 0.0f;
-#pragma unroll 1
-      for (int c = 0; c < TC_DT / 32; ++c) {
-        uint32_t v[32];
-        MGB_TMEM_LD32(tmem + zb * 128u + lane_off + (uint32_t)(c * 32), v);
-        tmem_ld_wait();
-        uint32_t packed[16];
-#pragma unroll
-        for (int j = 0; j < 32; j += 2) {
-          float r2[2];
-#pragma unroll
-          for (int h = 0; h < 2; ++h) {
-            const int64_t i = (int64_t)t * TC_DT + c * 32 + j + h;
-            float r = 0.0f;
-            if (i < a.n_data) {
-              const float z = __uint_as_float(v[j + h]);
-              const float yi = __ldg(&a.y[i]);
-              const float e = __expf(-fabsf(z));
-              const float inv = __fdividef(1.0f, 1.0f + e);
-              tsum += fmaxf(z, 0.0f) + __logf(1.0f + e) - yi * z;
-              r = (z >= 0.0f ? inv : e * inv) - yi;
-            }
-            r2[h] = r;
-          }
-          packed[j >> 1] = pack_bf16(r2[0], r2[1]);
-        }
-        unsigned char *sub = R + (c >> 1) * TILE_BYTES;
-#pragma unroll
-        for (int m = 0; m < 4; ++m) {
-          const int col = (c & 1) * 32 + m * 8;
-          *(uint4 *)(sub + sw128_off(row, col)) =
-              make_uint4(packed[4 * m], packed[4 * m + 1], packed[4 * m + 2], packed[4 * m + 3]);
-        }
-      }
+      uint32_t v[32];
+      MGB_TMEM_LD32(tmem + zb * 128u + lane_off + (uint32_t)(cg * 32), v);
+      tmem_ld_wait();
       tc_fence_before();
       mbar_arrive(&bar_zempty[zb]);
+      const int64_t i0 = (int64_t)t * TC_DT + cg * 32;
+      const int nvalid = (int)min((int64_t)32, a.n_data - i0);
+      // labels of this warp's 32 columns as a bit mask; columns past n_data count as y = 0 with z = 0
+      const uint32_t ymask = __ballot_sync(0xffffffffu, ycur != 0.0f);
+      float s_lin = 0.0f, prod = 1.0f;
+      uint32_t packed[16];
+      if (nvalid == 32) {
+#pragma unroll
+        for (int j = 0; j < 32; j += 2)
+          epi_pair(__uint_as_float(v[j]), __uint_as_float(v[j + 1]), (ymask >> j) & 1u, (ymask >> (j + 1)) & 1u,
+                   s_lin, prod, packed[j >> 1]);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 32; j += 2) {
+          const bool ok0 = j < nvalid, ok1 = j + 1 < nvalid;
+          epi_pair(ok0 ? __uint_as_float(v[j]) : -INFINITY, ok1 ? __uint_as_float(v[j + 1]) : -INFINITY,
+                   ok0 ? (ymask >> j) & 1u : 0u, ok1 ? (ymask >> (j + 1)) & 1u : 0u, s_lin, prod, packed[j >> 1]);
+          if (!ok1) packed[j >> 1] &= ok0 ? 0x0000FFFFu : 0u;
+        }
+      }
+      const float s_l2 = log2f_approx(prod);
+      const float tsum = fmaf(0.69314718055994531f, s_l2, s_lin);
+      unsigned char *sub = sR + rb * 2 * TILE_BYTES + (cg >> 1) * TILE_BYTES;
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        const int col = (cg & 1) * 32 + m * 8;
+        *(uint4 *)(sub + sw128_off(row, col)) =
+            make_uint4(packed[4 * m], packed[4 * m + 1], packed[4 * m + 2], packed[4 * m + 3]);
+      }
       fence_async_smem();
       mbar_arrive(&bar_rfull[rb]);
       pot += (double)tsum;
     }
-    if (ok && mbar_wait(&bar_gdone, 0, &abort_flag)) {
+    pot_s[cg][row] = pot;
+    if (cg == 0 && ok && mbar_wait(&bar_gdone, 0, &abort_flag)) {
       tc_fence_after();
       uint32_t g0[32], g1[32];
       MGB_TMEM_LD32(tg + lane_off, g0);
       MGB_TMEM_LD32(tg + lane_off + 32u, g1);
       tmem_ld_wait();
+      grad_ok_s = 1;
       const int64_t p = row0 + row;
       if (p < a.P && (!a.active || a.active[p / a.N])) {
 #pragma unroll
@@ -324,13 +373,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_logreg_tc(const __grid_consta
           if (k < a.d) a.grad[p * a.d + k] = __uint_as_float(g0[k]);
           if (k + 32 < a.d) a.grad[p * a.d + k + 32] = __uint_as_float(g1[k]);
         }
-        a.lik[p] = (float)pot;
       }
     }
   }
   tc_fence_before();
   __syncthreads();
   if (abort_flag && threadIdx.x == 0 && a.err) atomicOr(a.err, 1);
+  // potential: the four column groups of each row
+  if (threadIdx.x < TC_ROWS && grad_ok_s) {
+    const int64_t p = row0 + threadIdx.x;
+    if (p < a.P && (!a.active || a.active[p / a.N]))
+      a.lik[p] = (float)(pot_s[0][threadIdx.x] + pot_s[1][threadIdx.x] + pot_s[2][threadIdx.x] +
+                         pot_s[3][threadIdx.x]);
+  }
   if (warp == 1) {
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
