@@ -28,6 +28,11 @@ adjoint -- gradient evaluations per second of log Z with respect to
 (A, log diag Q, log diag R) at N = 65536, T = 1000 (checkpoint every 32
 steps), next to finite differences of the plain filter.
 
+smc_logreg -- the tempered SMC sampler on Bayesian logistic regression
+(1e5 x 50 data, 16384 particles per posterior, 16 posteriors): particle
+potential+gradient evaluations per second over timed SMC iterations, and the
+tcgen05 potential kernel's tensor roofline next to the fp32 kernel.
+
 batched_sv -- a second workload in the same line: 4096 independent
 stochastic-volatility filters of uneven length and size in one persistent
 launch (graph replay; e2e with the observations copied from pinned host
@@ -267,6 +272,98 @@ def bench_adjoint(args, flush, rank):
     return res
 
 
+SMC_WORKLOAD = ("tempered SMC (MetropolisedSMCSampler, MALA moves, adaptive temperatures, ESS retain 0.5) on "
+                "Bayesian logistic regression, X 1e5 x 50 iid N(0,1), beta_true ~ N(0, I), y ~ Bernoulli(sigmoid(X "
+                "beta_true)), prior N(0, I), N = 16384 particles per posterior, 5 MALA moves per temperature")
+
+
+def smc_data(n_data=100000, d=50, seed=0):
+    rng = np.random.default_rng(seed)
+    X = rng.standard_normal((n_data, d)).astype(np.float32)
+    bt = rng.standard_normal(d)
+    y = (rng.random(n_data) < 1.0 / (1.0 + np.exp(-(X @ bt)))).astype(np.float32)
+    return X, y
+
+
+def smc_cpu_baseline(X, y, P, d):
+    """oracle float64 potential and gradient (numpy, BLAS threads) for P parameter rows."""
+    from oracle import smc as osmc
+    beta = np.random.default_rng(3).standard_normal((P, d)) * 0.1
+    osmc.potential_grad(X[:1000], y[:1000], beta)
+    t0 = time.perf_counter()
+    osmc.potential_grad(X, y, beta)
+    dt = time.perf_counter() - t0
+    return X.shape[0] * P / dt, dt
+
+
+def bench_smc(args, flush, rank):
+    """B posteriors of the logistic-regression SMC workload: timed SMC iterations on the
+    tensor-core path, and the potential+gradient kernel alone (bf16 tcgen05 and fp32)."""
+    import torch
+    import mocat_gb300 as mg
+    X, y = smc_data()
+    n_data, d = X.shape
+    N, B, steps = 16384, args.smc_B, 5
+    sc = mg.smc.LogisticRegression(X, y, prior_scale=1.0)
+    sampler = mg.smc.MetropolisedSMCSampler(mg.smc.Underdamped(stepsize=1e-3), mcmc_steps=steps,
+                                            ess_threshold_retain=0.5)
+    keys = np.stack([np.array([0, s], np.uint32) for s in range(B)])
+    run = mg.smc.BatchedSMC(sc, sampler, N, keys, precision="bf16", max_iter=args.smc_iters + 2)
+    run.init()
+    run.step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.smc_iters):
+        run.step()
+    e1.record()
+    torch.cuda.synchronize()
+    t_it = e0.elapsed_time(e1) / 1e3 / args.smc_iters
+    moves = B * N * steps
+    res = {"workload": SMC_WORKLOAD + f", {B} posteriors (of 256), {args.smc_iters} timed SMC iterations",
+           "metric": "grad-evals/s", "value": moves / t_it, "unit": "particle potential+gradient evaluations/s",
+           "s_per_smc_iteration": t_it, "tflops_algorithmic": 4.0 * n_data * d * moves / t_it / 1e12,
+           "temperature_after": [float(x) for x in run._tensor("temperature", (B,), torch.float32)[:4].cpu()]}
+    # the potential kernel alone at the batch's parameter-row count
+    P = B * N
+    beta = torch.randn((P, d), device="cuda") * 0.1
+    kt = {}
+    for prec in ("bf16", "fp32"):
+        sc.likelihood_potential_and_grad(beta, precision=prec)
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(3):
+            flush.zero_()
+            a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a0.record()
+            sc.likelihood_potential_and_grad(beta, precision=prec)
+            a1.record()
+            torch.cuda.synchronize()
+            ts.append(a0.elapsed_time(a1) / 1e3)
+        kt[prec] = min(ts)
+    flops = 4.0 * n_data * d * P
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = float(peaks.get("bf16_tflops", 1900.0))
+    res["roofline"] = {"bound": "tensor", "kernel": "k_logreg_tc (tcgen05 bf16, fused two MMAs + epilogue)",
+                       "achieved": flops / kt["bf16"] / 1e12, "peak": peak, "unit": "TFLOP/s",
+                       "frac": flops / kt["bf16"] / 1e12 / peak, "launch_ms": kt["bf16"] * 1e3,
+                       "alg_flops_per_launch": flops,
+                       "peak_source": "MEASURED_PEAKS.json bf16_tflops (measured)" if peaks else "fallback",
+                       "note": "issue-bound in the softplus/sigmoid epilogue (K = d = 50 is short)"}
+    res["fp32_kernel"] = {"kernel": "k_logreg_f32 (CUDA cores)", "launch_ms": kt["fp32"] * 1e3,
+                          "tflops_algorithmic": flops / kt["fp32"] / 1e12}
+    if rank == 0:
+        v, dt = smc_cpu_baseline(X, y, 256, d)
+        res["cpu_baseline"] = {"value": v, "unit": "potential+gradient (parameter row, data row) pairs/s",
+                               "gpu_value": n_data * P / kt["bf16"], "cores": os.cpu_count(), "kind": "port",
+                               "sample": f"256 parameter rows x 1e5 data rows, oracle float64 numpy ({dt:.2f} s)"}
+    return res
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
@@ -302,6 +399,9 @@ def main():
     ap.add_argument("--sv-cpu-filters", type=int, default=256)
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-smc", action="store_true")
+    ap.add_argument("--smc-B", type=int, default=16)
+    ap.add_argument("--smc-iters", type=int, default=3)
     ap.add_argument("--adj-n", type=int, default=65536)
     ap.add_argument("--adj-T", type=int, default=1000)
     args = ap.parse_args()
@@ -470,6 +570,8 @@ def main():
         line["batched_sv"] = bench_sv_batch(args, flush, rank)
     if not args.no_adjoint:
         line["adjoint"] = bench_adjoint(args, flush, rank)
+    if not args.no_smc:
+        line["smc_logreg"] = bench_smc(args, flush, rank)
     if rank == 0:
         v_cpu, cores, dt = cpu_baseline(n, args.cpu_steps)
         line["cpu_baseline"] = {"value": v_cpu, "unit": "particle-steps/s", "cores": cores, "kind": "port",

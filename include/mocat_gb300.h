@@ -347,6 +347,11 @@ int mgb_smc_logreg_views(const mgb_smc_logreg_config *cfg, void *ws_dev, mgb_smc
 int mgb_smc_logreg_init(const mgb_smc_logreg_config *cfg, const float *X_dev, const float *y_dev,
                         const void *Xbf16_dev, int64_t n_data, const uint32_t *keys_dev, void *ws_dev,
                         size_t ws_bytes, void *stream);
+/* d log Z / d prior_scale of each posterior (out_dev (B) doubles) from the
+ * current weighted particles by the Fisher identity,
+ * E_post[|beta|^2 / s^3 - d / s]; meaningful once the posterior is reached
+ * (temperature 1). */
+int mgb_smc_logreg_prior_scale_grad(const mgb_smc_logreg_config *cfg, void *ws_dev, double *out_dev, void *stream);
 /* one SMC iteration of every active posterior (the caller loops while any
  * views.active[b] is set) */
 int mgb_smc_logreg_step(const mgb_smc_logreg_config *cfg, const float *X_dev, const float *y_dev,

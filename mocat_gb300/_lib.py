@@ -103,6 +103,7 @@ _SIGNATURES = {
     "mgb_smc_logreg_workspace": ([ctypes.POINTER(SMCConfig), _I64], _SZ),
     "mgb_smc_logreg_views": ([ctypes.POINTER(SMCConfig), _P, ctypes.POINTER(SMCViews)], _I32),
     "mgb_smc_logreg_init": ([ctypes.POINTER(SMCConfig), _P, _P, _P, _I64, _P, _P, _SZ, _P], _I32),
+    "mgb_smc_logreg_prior_scale_grad": ([ctypes.POINTER(SMCConfig), _P, _P, _P], _I32),
     "mgb_smc_logreg_step": ([ctypes.POINTER(SMCConfig), _P, _P, _P, _I64, _P, _SZ, _P], _I32),
     "mgb_pf_sv_batch_plan": ([_I64, _P, _P, ctypes.POINTER(SVLaunch), _P, _P], _I32),
     "mgb_pf_sv_batch_run": ([ctypes.POINTER(SVModel), _I64, _P, _P, _P, _P, _P, ctypes.POINTER(SVLaunch), _P, _P, _F,

@@ -489,6 +489,45 @@ __global__ void __launch_bounds__(ADAPT_TPB) k_smc_adapt(SMCView v, const float 
   }
 }
 
+// d log Z / d s (prior scale) by the Fisher identity over the final weighted
+// particles: E_post[|beta|^2 / s^3 - d / s], one CTA per posterior
+__global__ void __launch_bounds__(ADAPT_TPB) k_smc_prior_scale_grad(SMCView v, float s, double *out) {
+  __shared__ float red[ADAPT_TPB / 32];
+  __shared__ double dsum[ADAPT_TPB / 32][2];
+  const int b = blockIdx.x, N = v.N, D = v.D;
+  const float *lw = v.lw + (int64_t)b * N;
+  float m = -INFINITY;
+  for (int k = threadIdx.x; k < N; k += ADAPT_TPB) m = fmaxf(m, lw[k]);
+  const float M = block_max<ADAPT_TPB>(m, red);
+  double w = 0.0, wq = 0.0;
+  for (int k = threadIdx.x; k < N; k += ADAPT_TPB) {
+    const double e = exp((double)(lw[k] - M));
+    double q = 0.0;
+    for (int j = 0; j < D; ++j) {
+      const double x = v.beta[((int64_t)b * N + k) * D + j];
+      q += x * x;
+    }
+    w += e;
+    wq += e * q;
+  }
+  w = warp_sum(w);
+  wq = warp_sum(wq);
+  if ((threadIdx.x & 31) == 0) {
+    dsum[threadIdx.x >> 5][0] = w;
+    dsum[threadIdx.x >> 5][1] = wq;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double W = 0.0, WQ = 0.0;
+    for (int i = 0; i < ADAPT_TPB / 32; ++i) {
+      W += dsum[i][0];
+      WQ += dsum[i][1];
+    }
+    const double sd = (double)s;
+    out[b] = WQ / W / (sd * sd * sd) - (double)D / sd;
+  }
+}
+
 // ------------------------------------------------------------ host side
 SMCView carve_smc(Carver &c, int B, int N, int d, int H) {
   const size_t P = (size_t)B * N;
@@ -638,6 +677,14 @@ int mgb_logreg_potential_grad(const float *X, const float *y, int64_t n_data, in
   }
   if (precision != MGB_PREC_FP32) return ERR_BAD_ARG;
   MGB_SMC_D_DISPATCH(logreg_f32, X, y, n_data, beta, P, nullptr, 0, lik, grad, ws, ws_bytes, s);
+}
+
+int mgb_smc_logreg_prior_scale_grad(const mgb_smc_logreg_config *cfg, void *ws, double *out, void *stream) {
+  if (!smc_cfg_ok(cfg) || !ws || !out) return ERR_BAD_ARG;
+  Carver c(ws);
+  const SMCView v = carve_smc(c, cfg->B, cfg->N, cfg->d, cfg->max_iter + 1);
+  k_smc_prior_scale_grad<<<cfg->B, ADAPT_TPB, 0, (cudaStream_t)stream>>>(v, cfg->prior_scale, out);
+  return launch_status();
 }
 
 size_t mgb_smc_logreg_workspace(const mgb_smc_logreg_config *cfg, int64_t n_data) {

@@ -181,6 +181,13 @@ class BatchedSMC:
             self.step()
         return self.result()
 
+    def prior_scale_grad(self):
+        """(B,) d log Z / d prior_scale at the current particles (Fisher identity)."""
+        out = torch.empty(self.B, dtype=torch.float64, device=self.ws.device)
+        call("mgb_smc_logreg_prior_scale_grad", ctypes.byref(self.cfg), _dev.ptr(self.ws), _dev.ptr(out),
+             _dev.stream_ptr())
+        return out
+
     def result(self):
         B, n, d, H = self.B, self.n, self.cfg.d, self.views.hist_len
         it = self._tensor("iter", (B,), torch.int32).clone()
@@ -193,7 +200,7 @@ class BatchedSMC:
                      ess=self._tensor("hist_ess", (B, H), torch.float32)[:, :L].clone(),
                      alpha=self._tensor("hist_alpha", (B, H), torch.float32)[:, :L].clone(),
                      resampled=self._tensor("hist_resampled", (B, H), torch.int32)[:, :L].bool(),
-                     iterations=it)
+                     iterations=it, grad_log_norm_constant_prior_scale=self.prior_scale_grad())
 
 
 def run_batched(scenario, sampler, n, random_keys, precision="fp32"):

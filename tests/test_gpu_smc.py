@@ -118,3 +118,20 @@ def test_sampler_bf16_close_to_fp32(cuda):
     c = np.array([float(z16.log_norm_constant[b, int(z16.iterations[b])]) for b in range(8)])
     assert np.isfinite(c).all()
     assert abs(a.mean() - c.mean()) < 0.5 + 4 * (a.std() + c.std()) / np.sqrt(8), (a.mean(), c.mean())
+
+
+def test_prior_scale_gradient_matches_quadrature(cuda):
+    """d log Z / d s from the final weighted particles against central differences
+    of the exact d = 2 log evidence."""
+    import mocat_gb300 as mg
+    X, y = _data(100, 2)
+    h = 1e-3
+    exact = (osmc.log_evidence_2d(X, y, 1.0 + h) - osmc.log_evidence_2d(X, y, 1.0 - h)) / (2 * h)
+    sc = mg.smc.LogisticRegression(X, y)
+    sampler = mg.smc.MetropolisedSMCSampler(mg.smc.Underdamped(stepsize=0.2), mcmc_steps=5,
+                                            ess_threshold_retain=0.5)
+    keys = np.stack([O.PRNGKey(100 + s) for s in range(16)])
+    out = mg.smc.run_batched(sc, sampler, 4096, keys)
+    g = out.grad_log_norm_constant_prior_scale.cpu().numpy()
+    se = g.std() / np.sqrt(len(g))
+    assert abs(g.mean() - exact) < 4 * se + 0.01, (g.mean(), exact, se)
