@@ -195,6 +195,8 @@ def bench_sv_batch(args, flush, rank):
         torch.cuda.synchronize()
         times.append(e0.elapsed_time(e1) / 1e3)
     t_dev = statistics.median(times)
+    from mocat_gb300 import replicas
+    value, _, _ = replicas.aggregate(work, t_dev)
     lz = bf.log_z.cpu().numpy()
     nres = bf.resampled_count.cpu().numpy()
     e2e_t = []
@@ -209,7 +211,7 @@ def bench_sv_batch(args, flush, rank):
         torch.cuda.synchronize()
         e2e_t.append(e0.elapsed_time(e1) / 1e3)
     assert np.array_equal(lz_h.numpy(), lz)
-    res = {"workload": SV_WORKLOAD, "metric": METRIC, "value": work / t_dev, "unit": "particle-steps/s",
+    res = {"workload": SV_WORKLOAD, "metric": METRIC, "value": value, "unit": "particle-steps/s",
            "ms_per_step": t_dev * 1e3, "particle_steps_per_run": work, "kernel": "k_sv_batch (one launch per run)",
            "launch": bf.plan, "autotune_s": tune_s, "resample_fraction": float(nres.sum() / T.sum()),
            "log_z_finite": bool(np.isfinite(lz).all()),
@@ -415,7 +417,7 @@ def main():
     import torch
     import torch.distributed as dist
     import mocat_gb300 as mg
-    from mocat_gb300 import _dev, _lib
+    from mocat_gb300 import _dev, _lib, replicas
     from mocat_gb300.ssm import _step
 
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -475,11 +477,9 @@ def main():
     if int(err.item()) != 0:
         raise RuntimeError(f"device error word {int(err.item())}")
     t_dev = sum(times)
-    tmax = torch.tensor([t_dev], dtype=torch.float64, device=dev)
-    if world > 1:
-        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
-    value = world * n * T * args.steps / float(tmax)
-    ms_per_step = float(tmax) / args.steps * 1e3
+    # replicas: all ranks' particle-steps over the slowest rank's time
+    value, tmax, _ = replicas.aggregate(n * T * args.steps, t_dev)
+    ms_per_step = tmax / args.steps * 1e3
     log_z = float(logz.item())
 
     # ---- end to end through the public API (host observations and key, host read-back)
@@ -537,7 +537,7 @@ def main():
     # dominant kernel of the timed region: the persistent whole-filter kernel
     # (one launch per run); algorithmic bytes per particle-step 8 d + 16 (state
     # read + write, log-weight write + read, ancestor write + read)
-    run_s = float(tmax) / args.steps
+    run_s = tmax / args.steps
     alg_run = n * T * (8 * D + 16)
     achieved = alg_run / run_s / 1e9
     # the propagate kernel alone (standalone launch, rotating buffers > L2)
