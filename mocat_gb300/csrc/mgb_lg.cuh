@@ -89,6 +89,25 @@ __device__ __forceinline__ T ld(const T *p) {
   return __ldg(p);
 }
 
+// the arithmetic of lg_particle for a particle whose source state xs and
+// log-weight lres are already in registers (callers that prefetch them)
+template <int D, int DY>
+__device__ __forceinline__ float lg_particle_regs(const LGP<D, DY> &p, int64_t n, uint32_t ka, uint32_t kb, int64_t i,
+                                                  const float (&xs)[D], float lres, const float *y,
+                                                  float *__restrict__ x_new, float *__restrict__ lw_new) {
+  uint32_t b[D];
+  bits_vec<D>(ka, kb, b, p.one);
+  float e[D], xn[D];
+#pragma unroll
+  for (int j = 0; j < D; ++j) e[j] = bits_to_normal(b[j]);
+  lg_transition<D, DY>(p, xs, e, xn);
+#pragma unroll
+  for (int r = 0; r < D; ++r) x_new[r * n + i] = xn[r];
+  const float l = __fsub_rn(lres, lg_potential<D, DY>(p, xn, y));
+  lw_new[i] = l;
+  return l;
+}
+
 template <int D, int DY, bool CG = false>
 __device__ __forceinline__ float lg_particle(const LGP<D, DY> &p, int64_t n, uint32_t ka, uint32_t kb, int64_t i,
                                              bool res, const float *__restrict__ x_prev, const int32_t *anc,

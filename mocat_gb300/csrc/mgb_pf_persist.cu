@@ -193,7 +193,28 @@ __global__ void __launch_bounds__(PP_TPB, 2) k_pf_lg_persist(const __grid_consta
       const int64_t i = (int64_t)c * PP_TPB + threadIdx.x;
       float m = -INFINITY, s1 = 0.0f, s2 = 0.0f;
       int nanf = 0;
-      if (i < h) {
+      if (i < h && t == 0) {
+        uint32_t r0, r1, q0, q1;
+        threefry2x32_m(k0, k1, (uint32_t)(2 * i), (uint32_t)(2 * i + n), p.one, r0, r1);
+        threefry2x32_m(k0, k1, (uint32_t)(2 * i + 1), (uint32_t)(2 * i + 1 + n), p.one, q0, q1);
+#pragma unroll 1
+        for (int s = 0; s < 2; ++s) {
+          const float l = lg_init_particle<D, DY>(p, n, s ? r1 : r0, s ? q1 : q0, s ? i + h : i, y, xo, lo);
+          online_acc(l, m, s1, s2, nanf);
+        }
+      } else if (i < h) {
+        // both particles' ancestors and source states are requested before the
+        // key-split ciphers run, so the cipher arithmetic hides the gather latency
+        const int64_t sa = res_cur ? (int64_t)__ldcg(&a.anc[i]) : i;
+        const int64_t sb = res_cur ? (int64_t)__ldcg(&a.anc[i + h]) : i + h;
+        float xa_[D], xb_[D];
+#pragma unroll
+        for (int j = 0; j < D; ++j) {
+          xa_[j] = __ldcg(&xi[j * n + sa]);
+          xb_[j] = __ldcg(&xi[j * n + sb]);
+        }
+        const float la_ = res_cur ? 0.0f : __ldcg(&li[i]);
+        const float lb_ = res_cur ? 0.0f : __ldcg(&li[i + h]);
         uint32_t r0, r1, q0, q1;
         threefry2x32_m(k0, k1, (uint32_t)(2 * i), (uint32_t)(2 * i + n), p.one, r0, r1);
         threefry2x32_m(k0, k1, (uint32_t)(2 * i + 1), (uint32_t)(2 * i + 1 + n), p.one, q0, q1);
@@ -201,11 +222,11 @@ __global__ void __launch_bounds__(PP_TPB, 2) k_pf_lg_persist(const __grid_consta
         // particle code keeps the hot loop inside the instruction cache
 #pragma unroll 1
         for (int s = 0; s < 2; ++s) {
-          const uint32_t ka = s ? r1 : r0, kb = s ? q1 : q0;
-          const int64_t ii = s ? i + h : i;
-          const float l = t == 0 ? lg_init_particle<D, DY>(p, n, ka, kb, ii, y, xo, lo)
-                                 : lg_particle<D, DY, true>(p, n, ka, kb, ii, res_cur, xi, a.anc,
-                                                            res_cur ? nullptr : li, y, xo, lo);
+          float xs[D];
+#pragma unroll
+          for (int j = 0; j < D; ++j) xs[j] = s ? xb_[j] : xa_[j];
+          const float l = lg_particle_regs<D, DY>(p, n, s ? r1 : r0, s ? q1 : q0, s ? i + h : i, xs,
+                                                  s ? lb_ : la_, y, xo, lo);
           online_acc(l, m, s1, s2, nanf);
         }
       }
