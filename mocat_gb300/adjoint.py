@@ -81,6 +81,58 @@ def log_z_and_grad(ssm_scenario, y, random_key, n, ess_threshold=0.5, resampling
                  grad_log_likelihood_covariance_diag=g[d * d + d:], resampled=res.bool())
 
 
+def log_z_and_grad_many(ssm_scenario, y, random_keys, n, ess_threshold=0.5, resampling="systematic",
+                        ckpt_every=32, max_concurrent=8):
+    """log_z_and_grad for B keys at once: each evaluation runs on its own CUDA stream,
+    enqueued from its own host thread (the C library releases the interpreter lock),
+    so the kernels of different evaluations overlap on the GPU.
+
+    Returns cdict(log_z (B,), grad (B, d*d + 2d)) in the layout of mgb_pf_lg_grad."""
+    import threading
+    if not isinstance(ssm_scenario, TimeHomogenousLinearGaussian):
+        raise NotImplementedError(f"{ssm_scenario.__class__.__name__}: no adjoint kernel for this model")
+    keys = np.asarray(random_keys.cpu() if isinstance(random_keys, torch.Tensor) else random_keys,
+                      np.uint32).reshape(-1, 2)
+    B, d = keys.shape[0], ssm_scenario.dim
+    _, s = ssm_scenario.derived()
+    dev = _dev.device()
+    y2 = _dev.as_f32(y).reshape(-1, d).contiguous()
+    T = y2.shape[0]
+    nws = _lib.lib().mgb_pf_lg_grad_workspace(n, T, d, ckpt_every)
+    logz = torch.empty(B, dtype=torch.float64, device=dev)
+    grad = torch.empty((B, d * d + 2 * d), dtype=torch.float32, device=dev)
+    keys_dev = torch.from_numpy(keys.view(np.int32).copy()).to(dev).view(torch.uint32)
+    lanes = min(B, max_concurrent)
+    ws = [_dev.workspace(nws, dev) for _ in range(lanes)]
+    streams = [torch.cuda.Stream(dev) for _ in range(lanes)]
+    cur = torch.cuda.current_stream(dev)
+    for st in streams:
+        st.wait_stream(cur)
+    errors = []
+
+    def lane(j):
+        try:
+            with torch.cuda.stream(streams[j]):
+                for b in range(j, B, lanes):
+                    call("mgb_pf_lg_grad", ctypes.byref(s), n, T, _dev.ptr(keys_dev[b]), _dev.ptr(y2),
+                         float(ess_threshold), SCHEMES[resampling], int(ckpt_every), _dev.ptr(ws[j]), ws[j].numel(),
+                         _dev.ptr(logz[b:b + 1]), _dev.ptr(grad[b]), None,
+                         ctypes.c_void_p(streams[j].cuda_stream))
+        except Exception as e:  # re-raised on the calling thread
+            errors.append(e)
+
+    threads = [threading.Thread(target=lane, args=(j,)) for j in range(lanes)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    if errors:
+        raise errors[0]
+    for st in streams:
+        cur.wait_stream(st)
+    return cdict(log_z=logz, grad=grad)
+
+
 class ParticleFilterLogZ(torch.autograd.Function):
     """forward: log Z of the bootstrap filter for theta = (A, log q, log r);
     backward: the adjoint (ancestors held fixed), computed in the same library call."""

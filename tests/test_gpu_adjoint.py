@@ -120,3 +120,16 @@ def test_full_size_gradient_vs_kalman(cuda):
     rel = np.linalg.norm(got - g) / np.linalg.norm(g)
     cos = got @ g / np.linalg.norm(got) / np.linalg.norm(g)
     assert rel < 0.6 and cos > 0.9, (rel, cos)
+
+
+def test_many_concurrent_evaluations_equal_single_calls(cuda):
+    import mocat_gb300 as mg
+    A, q, r, p, y, ssm = _setup(10, 4096, 60, seed=3)
+    keys = np.stack([O.PRNGKey(s) for s in range(5)])
+    many = mg.adjoint.log_z_and_grad_many(ssm, y, keys, 4096, max_concurrent=3)
+    for b in range(5):
+        o = mg.adjoint.log_z_and_grad(ssm, y, keys[b], 4096)
+        g = torch.cat([o.grad_transition_matrix.reshape(-1), o.grad_log_transition_covariance_diag,
+                       o.grad_log_likelihood_covariance_diag])
+        assert float(o.log_z) == float(many.log_z[b])
+        assert torch.equal(g, many.grad[b])
