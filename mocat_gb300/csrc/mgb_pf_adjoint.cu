@@ -22,7 +22,10 @@
 // from its checkpoint (x_t, lw_t and the draws eps_t, bit-identical to the
 // forward), then walks it backwards.  Children of parent j are the index range
 // [starts_j, starts_{j+1}) of the sorted ancestor vector (systematic and
-// multinomial resampling both give non-decreasing ancestors).  Parameter
+// multinomial resampling both give non-decreasing ancestors); the kernel that
+// produces lambda of a resampled step stores it as warp-chunk prefixes
+// restarted at each new ancestor, so a parent with many children sums one
+// value per 32 of them (the order is fixed: results do not depend on timing).  Parameter
 // partials accumulate per block across all steps (float32) and are summed at
 // the end, so the result does not depend on scheduling.
 #include <cmath>
@@ -85,10 +88,12 @@ __global__ void k_adj_starts(const int32_t *anc, int64_t n, int32_t *starts) {
 
 struct AdjStep {
   const float *x, *lw, *eps, *y;  // step t
-  const float *lam_next;          // lambda_{t+1} (d, n), null at the last step
+  const float *lam_next;          // from step t+1 (d, n): lambda_{t+1}, or its segmented warp prefixes
+                                  // when t+1 resampled; null at the last step
   const int32_t *starts;          // children of a_{t+1}, null when t+1 did not resample
   const double *lse;              // LSE(lw_t) at a segment end, else null
-  float *lam;                     // lambda_t (d, n)
+  const int32_t *anc;             // a_t when step t resampled (lam then holds segmented prefixes), else null
+  float *lam;                     // out (d, n)
   float *W;                       // normalised weights of the current segment (n)
   float *partial;                 // (gridDim.x, d d + 2 d), accumulated
   int has_eps;                    // t >= 1
@@ -110,10 +115,18 @@ __global__ void __launch_bounds__(ADJ_TPB) k_adj_back(const __grid_constant__ LG
   if (j < n) {
     if (s.lam_next) {
       if (s.starts) {
+        // children [c0, c1) of parent j: lam_next holds, per warp-aligned chunk of 32
+        // children, prefixes restarted at each new parent, so the sum over the range is
+        // the prefix at c1 - 1 plus the chunk-end prefixes of the earlier chunks it covers
         const int32_t c0 = s.starts[j], c1 = s.starts[j + 1];
-        for (int32_t c = c0; c < c1; ++c) {
+        if (c1 > c0) {
+          const int32_t k0 = c0 >> 5, k1 = (c1 - 1) >> 5;
 #pragma unroll
-          for (int k = 0; k < D; ++k) mu[k] += __ldg(&s.lam_next[k * n + c]);
+          for (int k = 0; k < D; ++k) mu[k] = __ldg(&s.lam_next[k * n + c1 - 1]);
+          for (int32_t ch = k0; ch < k1; ++ch) {
+#pragma unroll
+            for (int k = 0; k < D; ++k) mu[k] += __ldg(&s.lam_next[k * n + ch * 32 + 31]);
+          }
         }
       } else {
 #pragma unroll
@@ -139,10 +152,32 @@ __global__ void __launch_bounds__(ADJ_TPB) k_adj_back(const __grid_constant__ LG
       float lam = -g * diff * (P * P);
 #pragma unroll
       for (int r = 0; r < D; ++r) lam = fmaf(p.F[r * D + k], mu[r], lam);
-      s.lam[k * n + j] = lam;
+      lq[k] = lam;  // lambda_t, kept for the eps term below
       lr[k] = g * (0.5f - 0.5f * dp * dp);
-      lq[k] = s.has_eps ? lam * __ldg(&s.eps[k * n + j]) * (0.5f * p.Lq[k * D + k]) : 0.0f;
     }
+  }
+  // lambda_t out: raw, or (step t resampled) warp prefixes restarted at each new ancestor
+  {
+    const int32_t key = (j < n && s.anc) ? s.anc[j] : -1;
+    const unsigned full = 0xffffffffu;
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      float v = lq[k];
+      if (s.anc) {
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const float u = __shfl_up_sync(full, v, o);
+          const int32_t ku = __shfl_up_sync(full, key, o);
+          if ((threadIdx.x & 31) >= o && ku == key) v += u;
+        }
+      }
+      if (j < n) s.lam[k * n + j] = v;
+    }
+  }
+  if (j < n) {
+#pragma unroll
+    for (int k = 0; k < D; ++k)
+      lq[k] = s.has_eps ? lq[k] * __ldg(&s.eps[k * n + j]) * (0.5f * p.Lq[k * D + k]) : 0.0f;
   }
 #pragma unroll
   for (int k = 0; k < D; ++k) {
@@ -152,20 +187,25 @@ __global__ void __launch_bounds__(ADJ_TPB) k_adj_back(const __grid_constant__ LG
     lr_s[tid * D + k] = lr[k];
   }
   __syncthreads();
-  for (int q = tid; q < G; q += ADJ_TPB) {
+  // block sums of the G parameter partials: two threads per output, half the particles each
+  __shared__ float half_s[2 * G];
+  for (int q2 = tid; q2 < 2 * G; q2 += ADJ_TPB) {
+    const int q = q2 % G, u0 = (q2 / G) * (ADJ_TPB / 2), u1 = u0 + ADJ_TPB / 2;
     float acc = 0.0f;
     if (q < D * D) {
       const int r = q / D, c = q % D;
-      for (int u = 0; u < ADJ_TPB; ++u) acc = fmaf(mu_s[u * D + r], x_s[u * D + c], acc);
+      for (int u = u0; u < u1; ++u) acc = fmaf(mu_s[u * D + r], x_s[u * D + c], acc);
     } else if (q < D * D + D) {
       const int k = q - D * D;
-      for (int u = 0; u < ADJ_TPB; ++u) acc += lq_s[u * D + k];
+      for (int u = u0; u < u1; ++u) acc += lq_s[u * D + k];
     } else {
       const int k = q - D * D - D;
-      for (int u = 0; u < ADJ_TPB; ++u) acc += lr_s[u * D + k];
+      for (int u = u0; u < u1; ++u) acc += lr_s[u * D + k];
     }
-    s.partial[(size_t)blockIdx.x * G + q] += acc;
+    half_s[q2] = acc;
   }
+  __syncthreads();
+  for (int q = tid; q < G; q += ADJ_TPB) s.partial[(size_t)blockIdx.x * G + q] += half_s[q] + half_s[q + G];
 }
 
 // grad[q] = sum over blocks of partial[b][q] (float64 sum, float32 result)
@@ -302,6 +342,7 @@ static int grad_lg(const mgb_lg_model *m, int64_t n, int64_t T, const uint32_t *
       a.starts = nullptr;
       a.lse = nullptr;
       a.lam = w.lam + (size_t)(t & 1) * D * n;
+      a.anc = (t >= 1 && res[t]) ? w.anc_hist + (size_t)t * n : nullptr;
       a.W = w.W;
       a.partial = w.partial;
       a.has_eps = t >= 1;
