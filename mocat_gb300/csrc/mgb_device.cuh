@@ -134,14 +134,18 @@ __device__ __forceinline__ float logf_(float x) {
   uint32_t mb = (ix & 0x007fffffu) | 0x3f800000u;
   if (mb > 0x3fb504f3u) { mb -= 0x00800000u; e += 1; }
   const float m = asf(mb);
-  const float s = __fdiv_rn(__fsub_rn(m, 1.0f), __fadd_rn(m, 1.0f));
-  const float z = __fmul_rn(s, s);
-  float p = __fmaf_rn(z, 0x1.745d18p-3f, 0x1.c71c72p-3f);
-  p = __fmaf_rn(z, p, 0x1.24924ap-2f);
-  p = __fmaf_rn(z, p, 0x1.99999ap-2f);
-  p = __fmaf_rn(z, p, 0x1.555556p-1f);
-  p = __fmaf_rn(z, p, 2.0f);
-  const float lm = __fmul_rn(s, p);
+  // log(1 + f) = f - f^2/2 + f^3 q(f), f = m - 1 (exact) in [sqrt(1/2) - 1, sqrt(2) - 1];
+  // q: degree-7 weighted least-squares fit (no division on the path)
+  const float f = __fsub_rn(m, 1.0f);
+  const float f2 = __fmul_rn(f, f);
+  float q = __fmaf_rn(f, -0x1.38b582p-4f, 0x1.055b72p-3f);
+  q = __fmaf_rn(f, q, -0x1.0d8544p-3f);
+  q = __fmaf_rn(f, q, 0x1.22da1cp-3f);
+  q = __fmaf_rn(f, q, -0x1.547244p-3f);
+  q = __fmaf_rn(f, q, 0x1.99a008p-3f);
+  q = __fmaf_rn(f, q, -0x1.000226p-2f);
+  q = __fmaf_rn(f, q, 0x1.555554p-2f);
+  const float lm = __fadd_rn(f, __fmaf_rn(__fmul_rn(f2, f), q, __fmul_rn(-0.5f, f2)));
   const float ef = (float)e;
   return __fmaf_rn(ef, 0x1.63p-1f, __fmaf_rn(ef, -0x1.bd0106p-13f, lm));
 }

@@ -93,14 +93,18 @@ static inline float o_logf(float x)
     uint32_t mb = (ix & 0x007fffffu) | 0x3f800000u;
     if (mb > 0x3fb504f3u) { mb -= 0x00800000u; e += 1; }   /* m > sqrt(2): halve */
     float m = o_asf(mb);
-    float s = (m - 1.0f) / (m + 1.0f);
-    float z = s * s;
-    float p = fmaf(z, 0x1.745d18p-3f, 0x1.c71c72p-3f);     /* 2/11, 2/9 */
-    p = fmaf(z, p, 0x1.24924ap-2f);                        /* 2/7 */
-    p = fmaf(z, p, 0x1.99999ap-2f);                        /* 2/5 */
-    p = fmaf(z, p, 0x1.555556p-1f);                        /* 2/3 */
-    p = fmaf(z, p, 2.0f);
-    float lm = s * p;
+    /* log(1 + f) = f - f^2/2 + f^3 q(f), f = m - 1 (exact) in [sqrt(1/2) - 1, sqrt(2) - 1];
+     * q: degree-7 weighted least-squares fit (relative error of the sum < 6e-9) */
+    float f = m - 1.0f;
+    float f2 = f * f;
+    float q = fmaf(f, -0x1.38b582p-4f, 0x1.055b72p-3f);
+    q = fmaf(f, q, -0x1.0d8544p-3f);
+    q = fmaf(f, q, 0x1.22da1cp-3f);
+    q = fmaf(f, q, -0x1.547244p-3f);
+    q = fmaf(f, q, 0x1.99a008p-3f);
+    q = fmaf(f, q, -0x1.000226p-2f);
+    q = fmaf(f, q, 0x1.555554p-2f);
+    float lm = f + fmaf(f2 * f, q, -0.5f * f2);
     float ef = (float)e;
     return fmaf(ef, 0x1.63p-1f, fmaf(ef, -0x1.bd0106p-13f, lm));   /* e*ln2 split hi/lo */
 }
