@@ -378,6 +378,70 @@ def bench_smc(args, flush, rank):
     return res
 
 
+def bench_config1(args, rank):
+    """The reference's CPU-runnable case: 1-D linear-Gaussian SSM (F = 0.9, Q = 1, H = 1, R = 0.25),
+    T = 100, N = 1000, systematic resampling every step.  Latency-bound: microseconds per step
+    through the public call (whole filter in one persistent launch) and as a device-resident
+    graph replay."""
+    import torch
+    import mocat_gb300 as mg
+    from mocat_gb300 import _dev, _lib
+    n, T = 1000, 100
+    ssm = mg.ssm.TimeHomogenousLinearGaussian(initial_mean=np.zeros(1), initial_covariance=np.eye(1),
+                                              transition_matrix=[[0.9]], transition_covariance=np.eye(1),
+                                              likelihood_matrix=np.eye(1), likelihood_covariance=[[0.25]])
+    y = ssm.simulate(np.arange(T), mg.random.PRNGKey(0)).y
+    y_host = y.cpu().pin_memory()
+    key = np.array([0, 1 + rank], np.uint32)
+    for _ in range(3):
+        float(mg.ssm.run_particle_filter_for_marginals(ssm, mg.ssm.BootstrapFilter(), y_host, np.arange(T), key,
+                                                       n=n, ess_threshold=2.0, history=False).log_z)
+    ts = []
+    for _ in range(10):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        o = mg.ssm.run_particle_filter_for_marginals(ssm, mg.ssm.BootstrapFilter(), y_host, np.arange(T), key, n=n,
+                                                     ess_threshold=2.0, history=False)
+        float(o.log_z)
+        ts.append(time.perf_counter() - t0)
+    t_e2e = statistics.median(ts)
+    _, s = ssm.derived()
+    dev = y.device
+    ws = _dev.workspace(_lib.lib().mgb_pf_lg_workspace(n, T, 1, 0), dev)
+    kd = mg.random.PRNGKey(1 + rank)
+    logz = torch.empty(1, dtype=torch.float64, device=dev)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    out = _lib.PFOutputs(logz.data_ptr(), None, None, None, None, None, None, err.data_ptr(), None)
+    yd = y.contiguous()
+
+    def enqueue():
+        _lib.call("mgb_pf_lg_run", ctypes.byref(s), n, T, _dev.ptr(kd), _dev.ptr(yd), 2.0, 0, _dev.ptr(ws),
+                  ws.numel(), ctypes.byref(out), _dev.stream_ptr())
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        enqueue()
+    torch.cuda.current_stream().wait_stream(side)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        enqueue()
+    for _ in range(3):
+        g.replay()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(20):
+        g.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    t_dev = e0.elapsed_time(e1) / 1e3 / 20
+    return {"workload": "1-D linear-Gaussian SSM (F=0.9, Q=1, H=1, R=0.25), T=100, N=1000, systematic resampling "
+                        "every step", "us_per_step_device": t_dev / T * 1e6, "us_per_step_e2e": t_e2e / T * 1e6,
+            "particle_steps_per_s_device": n * T / t_dev, "bound": "latency (one persistent launch, 3 grid "
+            "barriers per step)", "log_z": float(logz.item())}
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
@@ -578,6 +642,7 @@ def main():
                                               "frac": k_alg / k_t / 1e9 / peak}},
             "gpu_launches": args.steps * 3,  # k_setup_keys, k_pf_lg_persist, k_or_err per run
             "clocks": clk.summary()}
+    line["config1"] = bench_config1(args, rank)
     if not args.no_batched:
         line["batched_sv"] = bench_sv_batch(args, flush, rank)
     if not args.no_adjoint:

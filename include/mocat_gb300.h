@@ -189,6 +189,27 @@ int mgb_pf_lg_grad(const mgb_lg_model *model_host, int64_t n, int64_t T, const u
                    float ess_threshold, int scheme, int32_t ckpt_every, void *ws_dev, size_t ws_bytes,
                    double *log_z_dev, float *grad_dev, int32_t *resampled_dev, void *stream);
 
+/* --------------------------------------------- backward simulation (FFBSi)
+ * backward_simulation with maximum_rejections = 0, i.e. backward_simulation_full
+ * (mocat/src/ssm/backward.py:217-245, full_resampling :20-40), for a linear-Gaussian
+ * transition: t_keys = split(key, T); the M samples at T-1 are
+ * categorical(t_keys[T-1], lw_{T-1}, (M,)); for t = T-2 .. 0 sample j takes
+ * argmax_i gumbel(split(t_keys[t], M)[j], (N,))_i + lw_{t,i} - transition_potential(x_t^i -> xs_{t+1}^j),
+ * transition_potential(x0 -> x1) = 0.5 |(x1 - F x0) @ Pq|^2 + cq.
+ * x_hist (T, d, N) dimension-major (the filter's history), lw_hist (T, N);
+ * out (T, d, M) sampled trajectories, idx (T, M) the chosen particle indices.
+ * d in {1,2,3,4,5,8,10}; M N < 2^32. */
+typedef struct {
+  int32_t d;
+  const float *F;  /* d x d transition_matrix (host) */
+  const float *Pq; /* d x d transition_precision_sqrt (host) */
+  float cq;        /* (d log 2 pi - log transition_precision_det) / 2 */
+} mgb_lg_transition;
+size_t mgb_ffbsi_workspace(int64_t N, int64_t T, int32_t d);
+int mgb_ffbsi_lg(const mgb_lg_transition *transition_host, int64_t T, int64_t N, int64_t M, const float *x_hist_dev,
+                 const float *lw_hist_dev, const uint32_t *key_dev, float *out_dev, int32_t *idx_dev, void *ws_dev,
+                 size_t ws_bytes, void *stream);
+
 /* ------------------------------------ particle filter, optimal proposal
  * OptimalNonLinearGaussianParticleFilter (mocat/src/ssm/nonlinear_gaussian.py:134-281)
  * for a linear transition f(x) = F x with linear-Gaussian observations:

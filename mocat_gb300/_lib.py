@@ -36,6 +36,10 @@ class OptModel(ctypes.Structure):
                 ("K0", ctypes.c_void_p), ("C0c", ctypes.c_void_p), ("m0", ctypes.c_void_p)]
 
 
+class LGTransition(ctypes.Structure):
+    _fields_ = [("d", ctypes.c_int32), ("F", ctypes.c_void_p), ("Pq", ctypes.c_void_p), ("cq", ctypes.c_float)]
+
+
 class SVModel(ctypes.Structure):
     _fields_ = [("phi", ctypes.c_float), ("bsig", ctypes.c_float), ("r2", ctypes.c_float), ("cB", ctypes.c_float),
                 ("c0", ctypes.c_float), ("m0", ctypes.c_float)]
@@ -93,6 +97,8 @@ _SIGNATURES = {
     "mgb_pf_lg_grad_workspace": ([_I64, _I64, ctypes.c_int32, ctypes.c_int32], _SZ),
     "mgb_pf_lg_grad": ([ctypes.POINTER(LGModel), _I64, _I64, _P, _P, _F, _I32, ctypes.c_int32, _P, _SZ, _P, _P, _P, _P],
                        _I32),
+    "mgb_ffbsi_workspace": ([_I64, _I64, ctypes.c_int32], _SZ),
+    "mgb_ffbsi_lg": ([ctypes.POINTER(LGTransition), _I64, _I64, _I64, _P, _P, _P, _P, _P, _P, _SZ, _P], _I32),
     "mgb_pf_opt_init": ([ctypes.POINTER(OptModel), _I64, _P, _P, _P, _P, _P], _I32),
     "mgb_pf_opt_propagate": ([ctypes.POINTER(OptModel), _I64, _P, _P, _P, _P, _P, _P, _P, _P], _I32),
     "mgb_pf_opt_workspace": ([_I64, _I64, ctypes.c_int32, _I32], _SZ),

@@ -1,0 +1,234 @@
+// Backward simulation (forward filtering, backward simulation) for a
+// linear-Gaussian transition: the full O(N M) version.
+//
+// Reference: backward_simulation_full (mocat/src/ssm/backward.py:217-245),
+// full_resampling / full_resample_single (:20-40):
+//   t_keys = split(key, T)
+//   samples at T-1:  categorical(t_keys[T-1], lw_{T-1}, (M,))  -- one (M, N) Gumbel draw
+//   for t = T-2 .. 0, sample j (keys = split(t_keys[t], M)):
+//     index_j = argmax_i gumbel(keys[j], (N,))_i + lw_{t,i} - transition_potential(x_t^i -> xs_{t+1}^j)
+// transition_potential(x0 -> x1) = 0.5 |(x1 - F x0) @ Pq|^2 + cq (linear_gaussian.py,
+// gaussian_potential utils.py:49-105).  First maximum wins, NaN entries are skipped.
+//
+// One CTA per sample: F x_t^i is computed once per step by a separate kernel
+// (dimension-major, read through L2 by every CTA); the Gumbel bits of element
+// i and i + ceil(N/2) come from the two halves of one cipher call.  The
+// argmax is reduced in the fixed order (value, then smaller index), so the
+// result does not depend on scheduling.
+#include "mgb_internal.cuh"
+
+namespace mgb {
+
+constexpr int FB_TPB = 256;
+
+template <int D>
+struct FBP {
+  float F[D * D], Pq[D * D];
+  float cq;
+  uint32_t one;
+};
+
+// F x_t^i for all i (dimension-major in and out)
+template <int D>
+__global__ void __launch_bounds__(FB_TPB) k_ffbsi_fx(const __grid_constant__ FBP<D> p, int64_t N,
+                                                      const float *__restrict__ x, float *__restrict__ fx) {
+  const int64_t i = blockIdx.x * (int64_t)FB_TPB + threadIdx.x;
+  if (i >= N) return;
+  float xv[D];
+#pragma unroll
+  for (int k = 0; k < D; ++k) xv[k] = x[k * N + i];
+#pragma unroll
+  for (int r = 0; r < D; ++r) {
+    float v = __fmul_rn(p.F[r * D], xv[0]);
+#pragma unroll
+    for (int k = 1; k < D; ++k) v = __fmaf_rn(p.F[r * D + k], xv[k], v);
+    fx[r * N + i] = v;
+  }
+}
+
+struct Best {
+  float v;
+  int32_t i;
+  int have;
+};
+__device__ __forceinline__ void best_take(Best &b, float v, int32_t i) {
+  if (v != v) return;
+  if (!b.have || v > b.v || (v == b.v && i < b.i)) {
+    b.v = v;
+    b.i = i;
+    b.have = 1;
+  }
+}
+__device__ __forceinline__ void best_merge(Best &b, const Best &o) {
+  if (!o.have) return;
+  if (!b.have || o.v > b.v || (o.v == b.v && o.i < b.i)) b = o;
+}
+
+template <int TPB>
+__device__ __forceinline__ int32_t block_argmax(Best b, Best *sm) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    Best o;
+    o.v = __shfl_down_sync(0xffffffffu, b.v, off);
+    o.i = __shfl_down_sync(0xffffffffu, b.i, off);
+    o.have = __shfl_down_sync(0xffffffffu, b.have, off);
+    best_merge(b, o);
+  }
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = b;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    Best r = sm[0];
+    for (int w = 1; w < TPB / 32; ++w) best_merge(r, sm[w]);
+    sm[0] = r;
+  }
+  __syncthreads();
+  return sm[0].have ? sm[0].i : 0;
+}
+
+// last step: sample j draws over the (M, N) Gumbel array of t_key
+__global__ void __launch_bounds__(FB_TPB) k_ffbsi_last(int64_t N, int64_t M, const float *__restrict__ lw,
+                                                        const uint32_t *tkey, int32_t *__restrict__ idx) {
+  __shared__ Best sm[FB_TPB / 32];
+  const int64_t j = blockIdx.x;
+  const uint32_t k0 = tkey[0], k1 = tkey[1];
+  const uint64_t tot = (uint64_t)M * (uint64_t)N;
+  Best b{-INFINITY, 0, 0};
+  for (int64_t i = threadIdx.x; i < N; i += FB_TPB) {
+    const float g = bits_to_gumbel(bits_at(k0, k1, tot, (uint64_t)j * N + i));
+    best_take(b, __fadd_rn(g, lw[i]), (int32_t)i);
+  }
+  const int32_t bi = block_argmax<FB_TPB>(b, sm);
+  if (threadIdx.x == 0) idx[j] = bi;
+}
+
+// step t: sample j conditions on its state at t + 1
+template <int D>
+__global__ void __launch_bounds__(FB_TPB) k_ffbsi_step(const __grid_constant__ FBP<D> p, int64_t N, int64_t M,
+                                                        const float *__restrict__ fx, const float *__restrict__ lw,
+                                                        const float *__restrict__ x_next_samples,
+                                                        const uint32_t *tkey, int32_t *__restrict__ idx) {
+  __shared__ Best sm[FB_TPB / 32];
+  __shared__ float x1[D];
+  __shared__ uint32_t kj[2];
+  const int64_t j = blockIdx.x;
+  if (threadIdx.x < D) x1[threadIdx.x] = x_next_samples[threadIdx.x * M + j];
+  if (threadIdx.x == 0) {
+    uint32_t a0, a1;
+    split_at(tkey[0], tkey[1], (uint64_t)M, (uint64_t)j, a0, a1);
+    kj[0] = a0;
+    kj[1] = a1;
+  }
+  __syncthreads();
+  const uint32_t k0 = kj[0], k1 = kj[1];
+  const int64_t h = (N + 1) >> 1;
+  Best b{-INFINITY, 0, 0};
+  for (int64_t q = threadIdx.x; q < h; q += FB_TPB) {
+    uint32_t r0, r1;
+    threefry2x32_m(k0, k1, (uint32_t)q, q + h < N ? (uint32_t)(q + h) : 0u, p.one, r0, r1);
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      const int64_t i = s ? q + h : q;
+      if (i >= N) break;
+      const float g = bits_to_gumbel(s ? r1 : r0);
+      float diff[D];
+#pragma unroll
+      for (int r = 0; r < D; ++r) diff[r] = __fsub_rn(x1[r], fx[r * N + i]);
+      float quad = 0.0f;
+#pragma unroll
+      for (int k = 0; k < D; ++k) {
+        float v = __fmul_rn(diff[0], p.Pq[k]);
+#pragma unroll
+        for (int r = 1; r < D; ++r) v = __fmaf_rn(diff[r], p.Pq[r * D + k], v);
+        quad = k == 0 ? __fmul_rn(v, v) : __fmaf_rn(v, v, quad);
+      }
+      const float pot = __fadd_rn(__fmul_rn(0.5f, quad), p.cq);
+      best_take(b, __fadd_rn(g, __fsub_rn(lw[i], pot)), (int32_t)i);
+    }
+  }
+  const int32_t bi = block_argmax<FB_TPB>(b, sm);
+  if (threadIdx.x == 0) idx[j] = bi;
+}
+
+// xs_t[:, j] = x_t[:, idx_j]
+template <int D>
+__global__ void k_ffbsi_take(int64_t N, int64_t M, const float *__restrict__ x, const int32_t *__restrict__ idx,
+                             float *__restrict__ out) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < M; j += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = idx[j];
+#pragma unroll
+    for (int k = 0; k < D; ++k) out[k * M + j] = x[k * N + i];
+  }
+}
+
+template <int D>
+static int ffbsi_lg(const mgb_lg_transition *tr, int64_t T, int64_t N, int64_t M, const float *x_hist,
+                    const float *lw_hist, const uint32_t *key, float *out, int32_t *idx, void *ws, size_t ws_bytes,
+                    cudaStream_t s) {
+  FBP<D> p;
+  for (int i = 0; i < D * D; ++i) {
+    p.F[i] = tr->F[i];
+    p.Pq[i] = tr->Pq[i];
+  }
+  p.cq = tr->cq;
+  p.one = 1u;
+  Carver c(ws);
+  float *fx = c.take<float>((size_t)D * N);
+  uint32_t *tkeys = c.take<uint32_t>(2 * (size_t)T);
+  if (c.bytes() > ws_bytes) return ERR_WORKSPACE;
+  int st = mgb_split(key, T, tkeys, s);
+  if (st) return st;
+  const size_t xs = (size_t)D * N;
+  k_ffbsi_last<<<(unsigned)M, FB_TPB, 0, s>>>(N, M, lw_hist + (size_t)(T - 1) * N, tkeys + 2 * (T - 1),
+                                              idx + (size_t)(T - 1) * M);
+  if ((st = launch_status())) return st;
+  k_ffbsi_take<D><<<grid_for(M, 256), 256, 0, s>>>(N, M, x_hist + (size_t)(T - 1) * xs, idx + (size_t)(T - 1) * M,
+                                                   out + (size_t)(T - 1) * D * M);
+  if ((st = launch_status())) return st;
+  for (int64_t t = T - 2; t >= 0; --t) {
+    k_ffbsi_fx<D><<<(unsigned)((N + FB_TPB - 1) / FB_TPB), FB_TPB, 0, s>>>(p, N, x_hist + (size_t)t * xs, fx);
+    if ((st = launch_status())) return st;
+    k_ffbsi_step<D><<<(unsigned)M, FB_TPB, 0, s>>>(p, N, M, fx, lw_hist + (size_t)t * N,
+                                                   out + (size_t)(t + 1) * D * M, tkeys + 2 * t,
+                                                   idx + (size_t)t * M);
+    if ((st = launch_status())) return st;
+    k_ffbsi_take<D><<<grid_for(M, 256), 256, 0, s>>>(N, M, x_hist + (size_t)t * xs, idx + (size_t)t * M,
+                                                     out + (size_t)t * D * M);
+    if ((st = launch_status())) return st;
+  }
+  return OK;
+}
+
+}  // namespace mgb
+
+using namespace mgb;
+
+extern "C" {
+
+size_t mgb_ffbsi_workspace(int64_t N, int64_t T, int32_t d) {
+  if (N < 1 || T < 1 || d < 1) return 0;
+  Carver c(nullptr);
+  c.take<float>((size_t)d * N);
+  c.take<uint32_t>(2 * (size_t)T);
+  return c.bytes();
+}
+
+int mgb_ffbsi_lg(const mgb_lg_transition *tr, int64_t T, int64_t N, int64_t M, const float *x_hist,
+                 const float *lw_hist, const uint32_t *key, float *out, int32_t *idx, void *ws, size_t ws_bytes,
+                 void *stream) {
+  if (!tr || !tr->F || !tr->Pq || T < 1 || N < 1 || N > 0x7FFFFFFFll || M < 1 || M > 0x7FFFFFFFll ||
+      (uint64_t)M * (uint64_t)N >= (1ull << 32) || !x_hist || !lw_hist || !key || !out || !idx || !ws)
+    return ERR_BAD_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  switch (tr->d) {
+    case 1: return ffbsi_lg<1>(tr, T, N, M, x_hist, lw_hist, key, out, idx, ws, ws_bytes, s);
+    case 2: return ffbsi_lg<2>(tr, T, N, M, x_hist, lw_hist, key, out, idx, ws, ws_bytes, s);
+    case 3: return ffbsi_lg<3>(tr, T, N, M, x_hist, lw_hist, key, out, idx, ws, ws_bytes, s);
+    case 4: return ffbsi_lg<4>(tr, T, N, M, x_hist, lw_hist, key, out, idx, ws, ws_bytes, s);
+    case 5: return ffbsi_lg<5>(tr, T, N, M, x_hist, lw_hist, key, out, idx, ws, ws_bytes, s);
+    case 8: return ffbsi_lg<8>(tr, T, N, M, x_hist, lw_hist, key, out, idx, ws, ws_bytes, s);
+    case 10: return ffbsi_lg<10>(tr, T, N, M, x_hist, lw_hist, key, out, idx, ws, ws_bytes, s);
+    default: return ERR_UNSUPPORTED;
+  }
+}
+
+}  // extern "C"

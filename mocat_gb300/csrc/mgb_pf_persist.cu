@@ -391,7 +391,11 @@ int launch_persist(const mgb_lg_model *m, const PersistArgs &args, cudaStream_t 
     return ERR_UNSUPPORTED;
   PersistArgs a = args;
   void *kargs[] = {(void *)&p, (void *)&a};
-  const dim3 grid((unsigned)(sms * per_sm)), block(PP_TPB);
+  // no more blocks than there are 256-pair propagate chunks: a small filter's grid
+  // barriers then span a few blocks instead of every co-resident one
+  const int64_t chunks = (args.n / 2 + PP_TPB - 1) / PP_TPB;
+  const int64_t cap = (int64_t)sms * per_sm;
+  const dim3 grid((unsigned)(chunks < cap ? (chunks > 0 ? chunks : 1) : cap)), block(PP_TPB);
   if (cudaLaunchCooperativeKernel((void *)k_pf_lg_persist<D, DY>, grid, block, kargs, 0, s) != cudaSuccess)
     return ERR_LAUNCH;
   k_or_err<<<1, 1, 0, s>>>(args.err, args.user_err);

@@ -102,6 +102,7 @@ class TimeHomogenousLinearGaussian(StateSpaceModel):
         self.__dict__[key] = value
         if key in self._PARAMS:
             self.__dict__.pop("_derived", None)
+            self.__dict__.pop("_transition", None)
 
     # derived float32 parameters and the C-ABI model struct
     def derived(self):
@@ -423,3 +424,62 @@ def _run_from(ssm_scenario, s, initial_sample, y2, t, key, ess_threshold, resamp
                  t=torch.as_tensor(np.asarray(t if not isinstance(t, torch.Tensor) else t.cpu()), device=dev),
                  y=y2, log_z=torch.tensor(logz, dtype=torch.float64, device=dev),
                  resampled=torch.tensor(resd, device=dev))
+
+
+def _transition_struct(ssm_scenario):
+    """F, transition_precision_sqrt = inv(chol(Q)), and the normaliser of the transition
+    potential, computed as reset_covariance does (mocat/src/utils.py:247-262)."""
+    if "_transition" not in ssm_scenario.__dict__:
+        Q = ssm_scenario.transition_covariance
+        Pq = np.linalg.inv(np.linalg.cholesky(Q))
+        det_prec = 1.0 / np.linalg.det(Q)
+        d = ssm_scenario.dim
+        keep = dict(F=_f32(ssm_scenario.transition_matrix), Pq=_f32(Pq),
+                    cq=np.float32((d * LOG2PI - np.log(det_prec)) / 2.0))
+        s = _lib.LGTransition(d, keep["F"].ctypes.data, keep["Pq"].ctypes.data, float(keep["cq"]))
+        ssm_scenario.__dict__["_transition"] = (keep, s)
+    return ssm_scenario.__dict__["_transition"]
+
+
+def backward_simulation(ssm_scenario, marginal_particles, random_key, n_samps=None, maximum_rejections=0,
+                        transition_dens_bound_parameter=0.0, bound_inflation=1.01):
+    """backward.py:248-270 with maximum_rejections = 0 (backward_simulation_full, :217-245):
+    n_samps trajectories drawn backwards through the filter's particles.  Returns
+    cdict(value (T, n_samps, d), t, num_transition_evals (T,))."""
+    if maximum_rejections > 0:
+        raise NotImplementedError("backward simulation by rejection sampling is not built (maximum_rejections=0)")
+    if not isinstance(ssm_scenario, TimeHomogenousLinearGaussian):
+        raise NotImplementedError(f"{ssm_scenario.__class__.__name__}: no backward-simulation kernel for this model")
+    if not ssm_scenario.gpu_supported():
+        raise NotImplementedError(f"d = {ssm_scenario.dim} not compiled")
+    value = marginal_particles.value
+    T, n, d = value.shape
+    M = n if n_samps is None else int(n_samps)
+    x = _dev.as_f32(value).permute(0, 2, 1).contiguous()
+    lw = _dev.as_f32(marginal_particles.log_weight).reshape(T, n).contiguous()
+    key = _dev.as_key(random_key)
+    _, s = _transition_struct(ssm_scenario)
+    dev = x.device
+    ws = _dev.workspace(_lib.lib().mgb_ffbsi_workspace(n, T, d), dev)
+    out = torch.empty((T, d, M), dtype=torch.float32, device=dev)
+    idx = torch.empty((T, M), dtype=torch.int32, device=dev)
+    call("mgb_ffbsi_lg", ctypes.byref(s), T, n, M, _dev.ptr(x), _dev.ptr(lw), _dev.ptr(key), _dev.ptr(out),
+         _dev.ptr(idx), _dev.ptr(ws), ws.numel(), _dev.stream_ptr())
+    evals = torch.full((T,), float(n * M), device=dev)
+    evals[0] = 0.0
+    return cdict(value=out.permute(0, 2, 1), t=marginal_particles.t, num_transition_evals=evals, indices=idx)
+
+
+def forward_filtering_backward_simulation(ssm_scenario, particle_filter, y, t, n_samps, random_key, n_pf=None,
+                                          ess_threshold=0.5, maximum_rejections=0, transition_dens_bound_parameter=0.0,
+                                          bound_inflation=1.01, resampling="systematic"):
+    """backward.py:272-315: (pf_key, bsi_key) = split(key); filter with n_pf particles, then
+    backward_simulation of n_samps trajectories."""
+    keys = mrandom.split(_dev.as_key(random_key), 2)
+    n_pf = n_samps if n_pf is None else n_pf
+    pf = run_particle_filter_for_marginals(ssm_scenario, particle_filter, y, t, keys[0], n=n_pf,
+                                           ess_threshold=ess_threshold, resampling=resampling)
+    out = backward_simulation(ssm_scenario, pf, keys[1], n_samps, maximum_rejections,
+                              transition_dens_bound_parameter, bound_inflation)
+    out.log_z = pf.log_z
+    return out

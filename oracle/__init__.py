@@ -62,6 +62,10 @@ class _SVModel(ctypes.Structure):
                 ("cB", ctypes.c_float), ("c0", ctypes.c_float), ("m0", ctypes.c_float)]
 
 
+class _FFBSiModel(ctypes.Structure):
+    _fields_ = [("d", ctypes.c_int), ("F", ctypes.c_void_p), ("Pq", ctypes.c_void_p), ("cq", ctypes.c_float)]
+
+
 def lib():
     global _lib
     if _lib is None:
@@ -107,6 +111,7 @@ def lib():
         L.o_sv_run.restype = ctypes.c_double
         L.o_sv_batch.argtypes = [ctypes.POINTER(_SVModel), i64, i64p, i64p, i64p, f32p, u32p, ctypes.c_float,
                                  ctypes.c_int, f64p]
+        L.o_ffbsi_lg.argtypes = [ctypes.POINTER(_FFBSiModel), i64, i64, i64, f32p, f32p, u32p, f32p, i32p]
         L.o_num_threads.restype = ctypes.c_int
         L.o_set_num_threads.argtypes = [ctypes.c_int]
         _lib = L
@@ -388,6 +393,20 @@ def sv_batch(params, n, T, y_off, y, keys, ess_threshold=0.5, scheme="multinomia
     lib().o_sv_batch(ctypes.byref(s), n.size, n, T, y_off, _f32(y), _u32(keys).reshape(-1), float(ess_threshold),
                      SCHEMES[scheme], out)
     return out
+
+
+def ffbsi_lg(F, Pq, cq, x_hist, lw_hist, key, M):
+    """backward_simulation_full (backward.py:217-245) for a linear-Gaussian transition:
+    x_hist (T, N, d), lw_hist (T, N) -> (samples (T, M, d), indices (T, M))."""
+    F, Pq = _f32(F), _f32(Pq)
+    x_hist = _f32(x_hist)
+    T, N, d = x_hist.shape
+    s = _FFBSiModel(d, _ptr(F), _ptr(Pq), float(cq))
+    out = np.empty((T, M, d), np.float32)
+    idx = np.empty((T, M), np.int32)
+    lib().o_ffbsi_lg(ctypes.byref(s), T, N, M, x_hist.reshape(-1), _f32(lw_hist).reshape(-1), _u32(key),
+                     out.reshape(-1), idx.reshape(-1))
+    return out, idx
 
 
 def num_threads():

@@ -652,6 +652,74 @@ void o_sv_batch(const o_sv_model *md, int64_t B, const int64_t *n, const int64_t
         logZ[b] = o_sv_run(md, n[b], T[b], keys + 2 * b, y + y_off[b], ess_threshold, scheme, NULL, NULL);
 }
 
+/* ------------------------------------------- backward simulation (full FFBSi) */
+
+typedef struct {
+    int d;
+    const float *F;    /* d x d transition_matrix */
+    const float *Pq;   /* d x d transition_precision_sqrt */
+    float cq;          /* (d log 2pi - log transition_precision_det) / 2 */
+} o_ffbsi_model;
+
+/* transition_potential(x0 -> x1) = 0.5 |(x1 - F x0) @ Pq|^2 + cq
+ * (linear_gaussian.py transition_potential via gaussian_potential, utils.py:49-105) */
+static inline float o_transition_potential(const o_ffbsi_model *md, const float *x0, const float *x1)
+{
+    const int d = md->d;
+    float diff[64];
+    for (int r = 0; r < d; ++r) {
+        const float *f = md->F + r * d;
+        float fx = f[0] * x0[0];
+        for (int k = 1; k < d; ++k) fx = fmaf(f[k], x0[k], fx);
+        diff[r] = x1[r] - fx;
+    }
+    float quad = 0.0f;
+    for (int k = 0; k < d; ++k) {
+        float v = diff[0] * md->Pq[k];
+        for (int r = 1; r < d; ++r) v = fmaf(diff[r], md->Pq[r * d + k], v);
+        quad = k == 0 ? v * v : fmaf(v, v, quad);
+    }
+    return 0.5f * quad + md->cq;
+}
+
+/* backward_simulation_full (backward.py:217-245): t_keys = split(key, T);
+ * samples at T-1: categorical(t_keys[T-1], lw_{T-1}, (M,)) (Gumbel-max over the (M, N) draw);
+ * for t = T-2 .. 0, sample j: keys = split(t_keys[t], M);
+ *   index_j = argmax_i gumbel(keys[j], (N,))_i + lw_{t,i} - transition_potential(x_t^i -> xs_{t+1}^j)
+ * (first maximum wins, NaN skipped).  x_hist (T, N, d), lw_hist (T, N); out (T, M, d), idx (T, M). */
+void o_ffbsi_lg(const o_ffbsi_model *md, int64_t T, int64_t N, int64_t M, const float *x_hist, const float *lw_hist,
+                const uint32_t *key, float *out, int32_t *idx)
+{
+    const int d = md->d;
+    uint32_t *tkeys = (uint32_t *)malloc(sizeof(uint32_t) * 2 * (size_t)T);
+    o_split(key, T, tkeys);
+    o_resample_gumbel(lw_hist + (T - 1) * N, N, M, tkeys + 2 * (T - 1), idx + (T - 1) * M);
+    for (int64_t j = 0; j < M; ++j)
+        memcpy(out + ((T - 1) * M + j) * d, x_hist + ((T - 1) * N + idx[(T - 1) * M + j]) * d, sizeof(float) * d);
+    uint32_t *skeys = (uint32_t *)malloc(sizeof(uint32_t) * 2 * (size_t)M);
+    for (int64_t t = T - 2; t >= 0; --t) {
+        o_split(tkeys + 2 * t, M, skeys);
+        const float *xt = x_hist + t * N * d;
+        const float *lw = lw_hist + t * N;
+#pragma omp parallel for schedule(static)
+        for (int64_t j = 0; j < M; ++j) {
+            const float *x1 = out + ((t + 1) * M + j) * d;
+            float best = -INFINITY;
+            int32_t bi = 0;
+            int have = 0;
+            for (int64_t i = 0; i < N; ++i) {
+                float g = o_bits_to_gumbel(o_bits_at(skeys[2 * j], skeys[2 * j + 1], (uint64_t)N, (uint64_t)i));
+                float v = g + (lw[i] - o_transition_potential(md, xt + i * d, x1));
+                if (v == v && (!have || v > best)) { best = v; bi = (int32_t)i; have = 1; }
+            }
+            idx[t * M + j] = bi;
+            memcpy(out + (t * M + j) * d, xt + (int64_t)bi * d, sizeof(float) * d);
+        }
+    }
+    free(skeys);
+    free(tkeys);
+}
+
 int o_num_threads(void)
 {
 #ifdef _OPENMP
