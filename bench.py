@@ -619,11 +619,14 @@ def main():
     # the propagate kernel alone (standalone launch, rotating buffers > L2)
     k_alg = n * (8 * D + 8)
     traffic = None
+    issue = None
     prof = os.path.join(ROOT, "profiles", "k_pf_lg_persist_d10_n1M.md")
     if os.path.exists(prof):
         for ln in open(prof):
             if ln.startswith("dram_bytes_per_launch_T1000:"):
                 traffic = float(ln.split(":")[1])
+            if ln.startswith("| warp instructions |"):
+                issue = ln.split("|")[2].strip()
 
     line = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -637,6 +640,9 @@ def main():
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "alg_bytes_per_launch": alg_run, "launch_us": run_s * 1e6,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback",
+                         "issue_bound_note": "the step is bound by instruction issue (jax threefry layout: 6 "
+                                             "cipher calls and 10 erfinv per particle at d=10), not by HBM; ncu "
+                                             "(T=20 capture): " + str(issue),
                          "propagate_kernel": {"kernel": "k_lg_step2<10,10> alone", "launch_us": k_t * 1e6,
                                               "alg_bytes": k_alg, "achieved": k_alg / k_t / 1e9,
                                               "frac": k_alg / k_t / 1e9 / peak}},
