@@ -205,6 +205,15 @@ typedef struct {
   const float *Pq; /* d x d transition_precision_sqrt (host) */
   float cq;        /* (d log 2 pi - log transition_precision_det) / 2 */
 } mgb_lg_transition;
+/* full_stitch (mocat/src/ssm/online_smoothing.py:21-41): keys = split(key, M0);
+ * idx_j = argmax_i gumbel(keys[j], (M1,))_i + lw1_i - transition_potential(x0_j -> x1_i);
+ * x0 (d, M0), x1 (d, M1) dimension-major. */
+int mgb_stitch_lg(const mgb_lg_transition *transition_host, int64_t M0, int64_t M1, const float *x0_dev,
+                  const float *x1_dev, const float *lw1_dev, const uint32_t *key_dev, int32_t *idx_dev, void *stream);
+/* out_i = lw_i + transition_potential(x0_i -> x1_i) (lw_dev NULL: the potential alone) --
+ * the non-interacting log-weight of fixed_lag_stitching (online_smoothing.py:191-193) */
+int mgb_transition_potential_pairs(const mgb_lg_transition *transition_host, int64_t M, const float *x0_dev,
+                                   const float *x1_dev, const float *lw_dev, float *out_dev, void *stream);
 size_t mgb_ffbsi_workspace(int64_t N, int64_t T, int32_t d);
 int mgb_ffbsi_lg(const mgb_lg_transition *transition_host, int64_t T, int64_t N, int64_t M, const float *x_hist_dev,
                  const float *lw_hist_dev, const uint32_t *key_dev, float *out_dev, int32_t *idx_dev, void *ws_dev,

@@ -97,6 +97,8 @@ _SIGNATURES = {
     "mgb_pf_lg_grad_workspace": ([_I64, _I64, ctypes.c_int32, ctypes.c_int32], _SZ),
     "mgb_pf_lg_grad": ([ctypes.POINTER(LGModel), _I64, _I64, _P, _P, _F, _I32, ctypes.c_int32, _P, _SZ, _P, _P, _P, _P],
                        _I32),
+    "mgb_stitch_lg": ([ctypes.POINTER(LGTransition), _I64, _I64, _P, _P, _P, _P, _P, _P], _I32),
+    "mgb_transition_potential_pairs": ([ctypes.POINTER(LGTransition), _I64, _P, _P, _P, _P, _P], _I32),
     "mgb_ffbsi_workspace": ([_I64, _I64, ctypes.c_int32], _SZ),
     "mgb_ffbsi_lg": ([ctypes.POINTER(LGTransition), _I64, _I64, _I64, _P, _P, _P, _P, _P, _P, _SZ, _P], _I32),
     "mgb_pf_opt_init": ([ctypes.POINTER(OptModel), _I64, _P, _P, _P, _P, _P], _I32),

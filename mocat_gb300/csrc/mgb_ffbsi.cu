@@ -160,10 +160,95 @@ __global__ void k_ffbsi_take(int64_t N, int64_t M, const float *__restrict__ x, 
   }
 }
 
+// transition potential of particle pairs (x0_i -> x1_i), plus lw_i when given
+// (non_interacting_log_weight of fixed_lag_stitching, online_smoothing.py:191-193)
 template <int D>
-static int ffbsi_lg(const mgb_lg_transition *tr, int64_t T, int64_t N, int64_t M, const float *x_hist,
-                    const float *lw_hist, const uint32_t *key, float *out, int32_t *idx, void *ws, size_t ws_bytes,
-                    cudaStream_t s) {
+__global__ void __launch_bounds__(FB_TPB) k_pair_potential(const __grid_constant__ FBP<D> p, int64_t M,
+                                                            const float *__restrict__ x0, const float *__restrict__ x1,
+                                                            const float *__restrict__ lw, float *__restrict__ out) {
+  const int64_t i = blockIdx.x * (int64_t)FB_TPB + threadIdx.x;
+  if (i >= M) return;
+  float xv[D], diff[D];
+#pragma unroll
+  for (int k = 0; k < D; ++k) xv[k] = x0[k * M + i];
+#pragma unroll
+  for (int r = 0; r < D; ++r) {
+    float v = __fmul_rn(p.F[r * D], xv[0]);
+#pragma unroll
+    for (int k = 1; k < D; ++k) v = __fmaf_rn(p.F[r * D + k], xv[k], v);
+    diff[r] = __fsub_rn(x1[r * M + i], v);
+  }
+  float quad = 0.0f;
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    float v = __fmul_rn(diff[0], p.Pq[k]);
+#pragma unroll
+    for (int r = 1; r < D; ++r) v = __fmaf_rn(diff[r], p.Pq[r * D + k], v);
+    quad = k == 0 ? __fmul_rn(v, v) : __fmaf_rn(v, v, quad);
+  }
+  const float pot = __fadd_rn(__fmul_rn(0.5f, quad), p.cq);
+  out[i] = lw ? __fadd_rn(lw[i], pot) : pot;
+}
+
+// full_stitch (online_smoothing.py:21-41): CTA j conditions on x0_j and draws among the x1_i
+template <int D>
+__global__ void __launch_bounds__(FB_TPB) k_stitch(const __grid_constant__ FBP<D> p, int64_t M0, int64_t M1,
+                                                    const float *__restrict__ x0, const float *__restrict__ x1,
+                                                    const float *__restrict__ lw1, const uint32_t *key,
+                                                    int32_t *__restrict__ idx) {
+  __shared__ Best sm[FB_TPB / 32];
+  __shared__ float fx0[D];
+  __shared__ uint32_t kj[2];
+  const int64_t j = blockIdx.x;
+  if (threadIdx.x == 0) {
+    float xv[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) xv[k] = x0[k * M0 + j];
+#pragma unroll
+    for (int r = 0; r < D; ++r) {
+      float v = __fmul_rn(p.F[r * D], xv[0]);
+#pragma unroll
+      for (int k = 1; k < D; ++k) v = __fmaf_rn(p.F[r * D + k], xv[k], v);
+      fx0[r] = v;
+    }
+    uint32_t a0, a1;
+    split_at(key[0], key[1], (uint64_t)M0, (uint64_t)j, a0, a1);
+    kj[0] = a0;
+    kj[1] = a1;
+  }
+  __syncthreads();
+  const uint32_t k0 = kj[0], k1 = kj[1];
+  const int64_t h = (M1 + 1) >> 1;
+  Best b{-INFINITY, 0, 0};
+  for (int64_t q = threadIdx.x; q < h; q += FB_TPB) {
+    uint32_t r0, r1;
+    threefry2x32_m(k0, k1, (uint32_t)q, q + h < M1 ? (uint32_t)(q + h) : 0u, p.one, r0, r1);
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      const int64_t i = s ? q + h : q;
+      if (i >= M1) break;
+      const float g = bits_to_gumbel(s ? r1 : r0);
+      float diff[D];
+#pragma unroll
+      for (int r = 0; r < D; ++r) diff[r] = __fsub_rn(x1[r * M1 + i], fx0[r]);
+      float quad = 0.0f;
+#pragma unroll
+      for (int k = 0; k < D; ++k) {
+        float v = __fmul_rn(diff[0], p.Pq[k]);
+#pragma unroll
+        for (int r = 1; r < D; ++r) v = __fmaf_rn(diff[r], p.Pq[r * D + k], v);
+        quad = k == 0 ? __fmul_rn(v, v) : __fmaf_rn(v, v, quad);
+      }
+      const float pot = __fadd_rn(__fmul_rn(0.5f, quad), p.cq);
+      best_take(b, __fadd_rn(g, __fsub_rn(lw1[i], pot)), (int32_t)i);
+    }
+  }
+  const int32_t bi = block_argmax<FB_TPB>(b, sm);
+  if (threadIdx.x == 0) idx[j] = bi;
+}
+
+template <int D>
+static FBP<D> pack_fb(const mgb_lg_transition *tr) {
   FBP<D> p;
   for (int i = 0; i < D * D; ++i) {
     p.F[i] = tr->F[i];
@@ -171,6 +256,28 @@ static int ffbsi_lg(const mgb_lg_transition *tr, int64_t T, int64_t N, int64_t M
   }
   p.cq = tr->cq;
   p.one = 1u;
+  return p;
+}
+
+template <int D>
+static int stitch_lg(const mgb_lg_transition *tr, int64_t M0, int64_t M1, const float *x0, const float *x1,
+                     const float *lw1, const uint32_t *key, int32_t *idx, cudaStream_t s) {
+  k_stitch<D><<<(unsigned)M0, FB_TPB, 0, s>>>(pack_fb<D>(tr), M0, M1, x0, x1, lw1, key, idx);
+  return launch_status();
+}
+
+template <int D>
+static int pair_potential(const mgb_lg_transition *tr, int64_t M, const float *x0, const float *x1, const float *lw,
+                          float *out, cudaStream_t s) {
+  k_pair_potential<D><<<(unsigned)((M + FB_TPB - 1) / FB_TPB), FB_TPB, 0, s>>>(pack_fb<D>(tr), M, x0, x1, lw, out);
+  return launch_status();
+}
+
+template <int D>
+static int ffbsi_lg(const mgb_lg_transition *tr, int64_t T, int64_t N, int64_t M, const float *x_hist,
+                    const float *lw_hist, const uint32_t *key, float *out, int32_t *idx, void *ws, size_t ws_bytes,
+                    cudaStream_t s) {
+  const FBP<D> p = pack_fb<D>(tr);
   Carver c(ws);
   float *fx = c.take<float>((size_t)D * N);
   uint32_t *tkeys = c.take<uint32_t>(2 * (size_t)T);
@@ -229,6 +336,32 @@ int mgb_ffbsi_lg(const mgb_lg_transition *tr, int64_t T, int64_t N, int64_t M, c
     case 10: return ffbsi_lg<10>(tr, T, N, M, x_hist, lw_hist, key, out, idx, ws, ws_bytes, s);
     default: return ERR_UNSUPPORTED;
   }
+}
+
+#define MGB_FB_DISPATCH(FN, ...)                 \
+  switch (tr->d) {                               \
+    case 1: return FN<1>(__VA_ARGS__);           \
+    case 2: return FN<2>(__VA_ARGS__);           \
+    case 3: return FN<3>(__VA_ARGS__);           \
+    case 4: return FN<4>(__VA_ARGS__);           \
+    case 5: return FN<5>(__VA_ARGS__);           \
+    case 8: return FN<8>(__VA_ARGS__);           \
+    case 10: return FN<10>(__VA_ARGS__);         \
+    default: return ERR_UNSUPPORTED;             \
+  }
+
+int mgb_stitch_lg(const mgb_lg_transition *tr, int64_t M0, int64_t M1, const float *x0, const float *x1,
+                  const float *lw1, const uint32_t *key, int32_t *idx, void *stream) {
+  if (!tr || !tr->F || !tr->Pq || M0 < 1 || M1 < 1 || M0 > 0x7FFFFFFFll || M1 > 0x7FFFFFFFll || !x0 || !x1 ||
+      !lw1 || !key || !idx)
+    return ERR_BAD_ARG;
+  MGB_FB_DISPATCH(stitch_lg, tr, M0, M1, x0, x1, lw1, key, idx, (cudaStream_t)stream);
+}
+
+int mgb_transition_potential_pairs(const mgb_lg_transition *tr, int64_t M, const float *x0, const float *x1,
+                                   const float *lw, float *out, void *stream) {
+  if (!tr || !tr->F || !tr->Pq || M < 1 || !x0 || !x1 || !out) return ERR_BAD_ARG;
+  MGB_FB_DISPATCH(pair_potential, tr, M, x0, x1, lw, out, (cudaStream_t)stream);
 }
 
 }  // extern "C"

@@ -310,7 +310,8 @@ def resample_particles(particles, random_key, resample_full=True, resampling="sy
     n = lw.numel()
     anc = resample(lw, random_key, resampling).long()
     if particles.log_weight.dim() == 1:
-        out.value = particles.value[anc]
+        # x[..., idx, :]: every time slice of a (T, n, d) value along the particle axis
+        out.value = particles.value[..., anc, :]
         out.log_weight = torch.zeros(n, device=lw.device)
     elif resample_full:
         out.value = particles.value[:, anc]
@@ -483,3 +484,137 @@ def forward_filtering_backward_simulation(ssm_scenario, particle_filter, y, t, n
                               transition_dens_bound_parameter, bound_inflation)
     out.log_z = pf.log_z
     return out
+
+
+def _pair_potential(ssm_scenario, x0, x1, lw=None):
+    """lw_i + transition_potential(x0_i -> x1_i) for particle-major (M, d) rows."""
+    _, s = _transition_struct(ssm_scenario)
+    x0t = _dev.as_f32(x0).t().contiguous()
+    x1t = _dev.as_f32(x1).t().contiguous()
+    M = x0t.shape[1]
+    out = torch.empty(M, dtype=torch.float32, device=x0t.device)
+    lwd = None if lw is None else _dev.as_f32(lw).reshape(-1).contiguous()
+    call("mgb_transition_potential_pairs", ctypes.byref(s), M, _dev.ptr(x0t), _dev.ptr(x1t), _dev.ptr(lwd),
+         _dev.ptr(out), _dev.stream_ptr())
+    return out
+
+
+def full_stitch(ssm_scenario, x0_all, t, x1_all, tplus1, x1_log_weight, random_key):
+    """online_smoothing.py:33-41: for each x0_j a categorical draw over the x1_i with
+    log-weights x1_log_weight - transition_potential(x0_j -> x1_i); keys split(key, len(x0))."""
+    _, s = _transition_struct(ssm_scenario)
+    x0t = _dev.as_f32(x0_all).t().contiguous()
+    x1t = _dev.as_f32(x1_all).t().contiguous()
+    M0, M1 = x0t.shape[1], x1t.shape[1]
+    lw = _dev.as_f32(x1_log_weight).reshape(-1).contiguous()
+    idx = torch.empty(M0, dtype=torch.int32, device=x0t.device)
+    call("mgb_stitch_lg", ctypes.byref(s), M0, M1, _dev.ptr(x0t), _dev.ptr(x1t), _dev.ptr(lw),
+         _dev.ptr(_dev.as_key(random_key)), _dev.ptr(idx), _dev.stream_ptr())
+    return idx
+
+
+def fixed_lag_stitching(ssm_scenario, early_block, t, recent_block, recent_block_log_weight, tplus1, random_key,
+                        maximum_rejections=0, init_bound_param=0.0, bound_inflation=1.01):
+    """online_smoothing.py:178-209 (full stitching): returns (stitched value, transition evaluations)."""
+    if maximum_rejections > 0:
+        raise NotImplementedError("stitching by rejection sampling is not built (maximum_rejections=0)")
+    x0_fixed_all = early_block[-1]
+    x0_vary_all, x1_vary_all = recent_block[0], recent_block[1]
+    nilw = _pair_potential(ssm_scenario, x0_vary_all, x1_vary_all, recent_block_log_weight)
+    inds = full_stitch(ssm_scenario, x0_fixed_all, t, x1_vary_all, tplus1, nilw, random_key).long()
+    return torch.cat([early_block, recent_block[1:, inds]], 0), len(x0_fixed_all) ** 2
+
+
+def _check_smoother(ssm_scenario, particle_filter):
+    _check_lg(ssm_scenario, particle_filter)
+    if not isinstance(particle_filter, BootstrapFilter):
+        raise NotImplementedError("the online smoother runs the bootstrap filter")
+
+
+def propagate_particle_smoother_pf(ssm_scenario, particle_filter, particles, y_new, t_new, random_key, lag,
+                                   maximum_rejections=0, init_bound_param=0.0, bound_inflation=1.01,
+                                   resampling="systematic"):
+    """online_smoothing.py:212-282: resample unless unweighted, propagate, append, then
+    stitch the block that leaves the lag window.  The same key drives the resampling,
+    the proposal and the stitch, as in the reference."""
+    _check_smoother(ssm_scenario, particle_filter)
+    prefix, s = _kernels(ssm_scenario, particle_filter)
+    key = _dev.as_key(random_key)
+    n = particles.value.shape[1]
+    out = particles.copy()
+    if not hasattr(out, "num_transition_evals"):
+        out.num_transition_evals = torch.zeros(1, device=particles.value.device)
+    lw_last = particles.log_weight if particles.log_weight.dim() == 1 else particles.log_weight[-1]
+    if float(ess_log_weight(lw_last)) < n - 1e-3:
+        out = resample_particles(out, key, True, resampling)
+    x_prev = out.value[-1].t().contiguous()
+    y_t = _y2(y_new, ssm_scenario.dim_obs).reshape(-1)
+    x_new, lw = _step(s, n, key, y_t, x_prev, None, None, prefix)
+    dev = x_new.device
+    out.value = torch.cat([out.value, x_new.t()[None]], 0)
+    out.y = torch.cat([out.y, y_t[None]], 0) if getattr(out, "y", None) is not None else y_t[None]
+    out.t = torch.cat([out.t, torch.atleast_1d(torch.as_tensor(t_new, device=dev)).to(out.t.dtype)])
+    out.ess = ess_log_weight(lw).reshape(1).float()
+    len_t = out.t.numel()
+    s1 = len_t - lag - 1
+    nte = 0
+    if s1 >= 0:
+        out.value, nte = fixed_lag_stitching(ssm_scenario, out.value[:s1 + 1], out.t[s1], out.value[s1:], lw,
+                                             out.t[s1 + 1], key, maximum_rejections, init_bound_param,
+                                             bound_inflation)
+    out.num_transition_evals = torch.cat([out.num_transition_evals,
+                                          torch.tensor([float(nte)], device=dev)])
+    out.log_weight = torch.zeros(n, device=dev) if s1 >= 0 else lw
+    return out
+
+
+def propagate_particle_smoother_bs(ssm_scenario, particle_filter, particles, y_new, t_new, random_key, lag,
+                                   ess_threshold=0.5, maximum_rejections=0, init_bound_param=0.0,
+                                   bound_inflation=1.01, resampling="systematic"):
+    """online_smoothing.py:285-366: propagate the marginal filter, then backward-simulate
+    the last lag + 1 steps and stitch them onto the fixed block."""
+    _check_smoother(ssm_scenario, particle_filter)
+    key = _dev.as_key(random_key)
+    n = particles.value.shape[1]
+    out = particles.copy()
+    if not hasattr(out, "num_transition_evals"):
+        out.num_transition_evals = torch.zeros(1, device=particles.value.device)
+    if not hasattr(out, "marginal_filter"):
+        out.marginal_filter = cdict(value=particles.value, log_weight=particles.log_weight, y=particles.y,
+                                    t=particles.t, ess=particles.ess)
+    split_keys = mrandom.split(key, 4)
+    out.marginal_filter = propagate_particle_filter(ssm_scenario, particle_filter, out.marginal_filter, y_new, t_new,
+                                                    split_keys[1], ess_threshold, False, resampling)
+    dev = out.marginal_filter.value.device
+    y_t = _y2(y_new, ssm_scenario.dim_obs).reshape(-1)
+    out.y = torch.cat([out.y, y_t[None]], 0) if getattr(out, "y", None) is not None else y_t[None]
+    out.t = torch.cat([out.t, torch.atleast_1d(torch.as_tensor(t_new, device=dev)).to(out.t.dtype)])
+    out.log_weight = torch.zeros(n, device=dev)
+    out.ess = out.marginal_filter.ess[-1:]
+    len_t = out.t.numel()
+    s1 = len_t - lag - 1
+    if s1 >= 0:
+        bsim = backward_simulation(ssm_scenario, out.marginal_filter[s1:], split_keys[2], n, maximum_rejections,
+                                   init_bound_param, bound_inflation)
+        out.value, snte = fixed_lag_stitching(ssm_scenario, out.value[:s1 + 1], out.t[s1], bsim.value,
+                                              torch.zeros(n, device=dev), out.t[s1 + 1], key, maximum_rejections,
+                                              init_bound_param, bound_inflation)
+        nte = snte + float(bsim.num_transition_evals.sum())
+    else:
+        bsim = backward_simulation(ssm_scenario, out.marginal_filter, split_keys[2], n, maximum_rejections,
+                                   init_bound_param, bound_inflation)
+        out.value, nte = bsim.value, float(bsim.num_transition_evals.sum())
+    out.num_transition_evals = torch.cat([out.num_transition_evals, torch.tensor([float(nte)], device=dev)])
+    return out
+
+
+def propagate_particle_smoother(ssm_scenario, particle_filter, particles, y_new, t_new, random_key, lag,
+                                backward_sim=True, ess_threshold=0.5, maximum_rejections=0, init_bound_param=0.0,
+                                bound_inflation=1.01, resampling="systematic"):
+    """Online fixed-lag particle smoothing (online_smoothing.py:369-386)."""
+    if backward_sim:
+        return propagate_particle_smoother_bs(ssm_scenario, particle_filter, particles, y_new, t_new, random_key,
+                                              lag, ess_threshold, maximum_rejections, init_bound_param,
+                                              bound_inflation, resampling)
+    return propagate_particle_smoother_pf(ssm_scenario, particle_filter, particles, y_new, t_new, random_key, lag,
+                                          maximum_rejections, init_bound_param, bound_inflation, resampling)

@@ -112,6 +112,8 @@ def lib():
         L.o_sv_batch.argtypes = [ctypes.POINTER(_SVModel), i64, i64p, i64p, i64p, f32p, u32p, ctypes.c_float,
                                  ctypes.c_int, f64p]
         L.o_ffbsi_lg.argtypes = [ctypes.POINTER(_FFBSiModel), i64, i64, i64, f32p, f32p, u32p, f32p, i32p]
+        L.o_stitch_lg.argtypes = [ctypes.POINTER(_FFBSiModel), i64, i64, f32p, f32p, f32p, u32p, i32p]
+        L.o_transition_potential_pairs.argtypes = [ctypes.POINTER(_FFBSiModel), i64, f32p, f32p, f32p]
         L.o_num_threads.restype = ctypes.c_int
         L.o_set_num_threads.argtypes = [ctypes.c_int]
         _lib = L
@@ -407,6 +409,24 @@ def ffbsi_lg(F, Pq, cq, x_hist, lw_hist, key, M):
     lib().o_ffbsi_lg(ctypes.byref(s), T, N, M, x_hist.reshape(-1), _f32(lw_hist).reshape(-1), _u32(key),
                      out.reshape(-1), idx.reshape(-1))
     return out, idx
+
+
+def stitch_lg(F, Pq, cq, x0, x1, lw1, key):
+    """full_stitch (online_smoothing.py:21-41): x0 (M0, d), x1 (M1, d) -> indices (M0,)."""
+    F, Pq, x0, x1 = _f32(F), _f32(Pq), _f32(x0), _f32(x1)
+    s = _FFBSiModel(x0.shape[1], _ptr(F), _ptr(Pq), float(cq))
+    idx = np.empty(x0.shape[0], np.int32)
+    lib().o_stitch_lg(ctypes.byref(s), x0.shape[0], x1.shape[0], x0.reshape(-1), x1.reshape(-1), _f32(lw1), _u32(key),
+                      idx)
+    return idx
+
+
+def transition_potential_pairs(F, Pq, cq, x0, x1):
+    F, Pq, x0, x1 = _f32(F), _f32(Pq), _f32(x0), _f32(x1)
+    s = _FFBSiModel(x0.shape[1], _ptr(F), _ptr(Pq), float(cq))
+    out = np.empty(x0.shape[0], np.float32)
+    lib().o_transition_potential_pairs(ctypes.byref(s), x0.shape[0], x0.reshape(-1), x1.reshape(-1), out)
+    return out
 
 
 def num_threads():

@@ -720,6 +720,36 @@ void o_ffbsi_lg(const o_ffbsi_model *md, int64_t T, int64_t N, int64_t M, const 
     free(tkeys);
 }
 
+/* full_stitch (online_smoothing.py:21-41): keys = split(key, M0); for each x0_j,
+ * idx_j = argmax_i gumbel(keys[j], (M1,))_i + lw1_i - transition_potential(x0_j -> x1_i)
+ * (first maximum wins, NaN skipped).  x0 (M0, d), x1 (M1, d) particle-major. */
+void o_stitch_lg(const o_ffbsi_model *md, int64_t M0, int64_t M1, const float *x0, const float *x1,
+                 const float *lw1, const uint32_t *key, int32_t *idx)
+{
+    const int d = md->d;
+    uint32_t *skeys = (uint32_t *)malloc(sizeof(uint32_t) * 2 * (size_t)M0);
+    o_split(key, M0, skeys);
+#pragma omp parallel for schedule(static)
+    for (int64_t j = 0; j < M0; ++j) {
+        float best = -INFINITY;
+        int32_t bi = 0;
+        int have = 0;
+        for (int64_t i = 0; i < M1; ++i) {
+            float g = o_bits_to_gumbel(o_bits_at(skeys[2 * j], skeys[2 * j + 1], (uint64_t)M1, (uint64_t)i));
+            float v = g + (lw1[i] - o_transition_potential(md, x0 + j * d, x1 + i * d));
+            if (v == v && (!have || v > best)) { best = v; bi = (int32_t)i; have = 1; }
+        }
+        idx[j] = bi;
+    }
+    free(skeys);
+}
+
+/* transition_potential(x0_i -> x1_i) for each i (vmap over pairs) */
+void o_transition_potential_pairs(const o_ffbsi_model *md, int64_t M, const float *x0, const float *x1, float *out)
+{
+    for (int64_t i = 0; i < M; ++i) out[i] = o_transition_potential(md, x0 + i * md->d, x1 + i * md->d);
+}
+
 int o_num_threads(void)
 {
 #ifdef _OPENMP
