@@ -255,6 +255,34 @@ int mgb_pf_opt_run(const mgb_opt_model *model_host, int64_t n, int64_t T, const 
                    float ess_threshold, int scheme, void *ws_dev, size_t ws_bytes, const mgb_pf_outputs *out,
                    void *stream);
 
+/* ------------------------------------- one-dimensional non-linear benchmark
+ * BootstrapFilter on NonLinear1DBenchmark (mocat/src/ssm/scenarios/nonlinear1d.py:16-80):
+ *   x_0 = normal(key_i, (1,)) initial_sd
+ *   x_t = 0.5 x + 25 x / (1 + x^2) + 8 cos(1.2 t_prev) + normal(key_i, (1,)) transition_sd
+ *   potential(x, y) = 0.5 ((y - x^2 / 20) / likelihood_sd)^2 + c,  c = log(2 pi) / 2 in float32
+ * key_i = split(k, n)[i]; particles and log-weights are (n) float32.
+ * 8 cos(1.2 t) is 8 * float(cos(double(1.2f * t))).
+ */
+typedef struct {
+  float initial_sd, transition_sd, likelihood_sd;
+  float c;
+} mgb_nl1d_model;
+
+/* initiate_particles (filtering.py:173-193); y0_dev == NULL: zero weights */
+int mgb_pf_nl1d_init(const mgb_nl1d_model *model_host, int64_t n, const uint32_t *key_dev, const float *y0_dev,
+                     float *x_dev, float *lw_dev, void *stream);
+/* propose_and_intermediate_weight_vectorised (filtering.py:124-139) for one step from
+ * t_previous; ancestors_dev == NULL: no resampling; lw_prev_dev == NULL: 0 */
+int mgb_pf_nl1d_propagate(const mgb_nl1d_model *model_host, int64_t n, const uint32_t *key_t_dev, const float *y_t_dev,
+                          float t_previous, const float *x_prev_dev, const int32_t *ancestors_dev,
+                          const float *lw_prev_dev, float *x_new_dev, float *lw_new_dev, void *stream);
+/* run_particle_filter_for_marginals (filtering.py:255-324); t_dev holds the T times
+ * (step t uses t_dev[t-1] as t_previous); outputs as mgb_pf_lg_run with d = 1 */
+size_t mgb_pf_nl1d_workspace(int64_t n, int64_t T, int scheme);
+int mgb_pf_nl1d_run(const mgb_nl1d_model *model_host, int64_t n, int64_t T, const uint32_t *key_dev, const float *y_dev,
+                    const float *t_dev, float ess_threshold, int scheme, void *ws_dev, size_t ws_bytes,
+                    const mgb_pf_outputs *out, void *stream);
+
 /* ------------------------------- many stochastic-volatility filters at once
  * B independent run_particle_filter_for_marginals calls (mocat/src/ssm/filtering.py:255-324)
  * with BootstrapFilter on StochasticVolatility, d = 1

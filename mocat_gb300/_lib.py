@@ -36,6 +36,11 @@ class OptModel(ctypes.Structure):
                 ("K0", ctypes.c_void_p), ("C0c", ctypes.c_void_p), ("m0", ctypes.c_void_p)]
 
 
+class NL1DModel(ctypes.Structure):
+    _fields_ = [("initial_sd", ctypes.c_float), ("transition_sd", ctypes.c_float), ("likelihood_sd", ctypes.c_float),
+                ("c", ctypes.c_float)]
+
+
 class LGTransition(ctypes.Structure):
     _fields_ = [("d", ctypes.c_int32), ("F", ctypes.c_void_p), ("Pq", ctypes.c_void_p), ("cq", ctypes.c_float)]
 
@@ -106,6 +111,11 @@ _SIGNATURES = {
     "mgb_pf_opt_workspace": ([_I64, _I64, ctypes.c_int32, _I32], _SZ),
     "mgb_pf_opt_run": ([ctypes.POINTER(OptModel), _I64, _I64, _P, _P, _F, _I32, _P, _SZ, ctypes.POINTER(PFOutputs),
                         _P], _I32),
+    "mgb_pf_nl1d_init": ([ctypes.POINTER(NL1DModel), _I64, _P, _P, _P, _P, _P], _I32),
+    "mgb_pf_nl1d_propagate": ([ctypes.POINTER(NL1DModel), _I64, _P, _P, _F, _P, _P, _P, _P, _P, _P], _I32),
+    "mgb_pf_nl1d_workspace": ([_I64, _I64, _I32], _SZ),
+    "mgb_pf_nl1d_run": ([ctypes.POINTER(NL1DModel), _I64, _I64, _P, _P, _P, _F, _I32, _P, _SZ,
+                         ctypes.POINTER(PFOutputs), _P], _I32),
     "mgb_logreg_workspace": ([_I64, _I64, ctypes.c_int32, _I32], _SZ),
     "mgb_logreg_potential_grad": ([_P, _P, _I64, ctypes.c_int32, _P, _I64, _P, _P, _I32, _P, _P, _SZ, _P], _I32),
     "mgb_smc_logreg_workspace": ([ctypes.POINTER(SMCConfig), _I64], _SZ),

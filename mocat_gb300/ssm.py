@@ -187,6 +187,69 @@ class StochasticVolatility(StateSpaceModel):
         return self.__dict__["_derived"]
 
 
+class NonLinear1DBenchmark(StateSpaceModel):
+    """x_0 ~ N(0, initial_sd^2), x_t ~ N(0.5 x + 25 x / (1 + x^2) + 8 cos(1.2 t_prev), transition_sd^2),
+    y_t ~ N(x_t^2 / 20, likelihood_sd^2) (mocat/src/ssm/scenarios/nonlinear1d.py:16-80).
+    The likelihood potential's normaliser is log(2 pi) / 2 whatever likelihood_sd is, as in
+    the reference (gaussian_potential of the standardised residual)."""
+    name = "1D Non-linear Benchmark"
+    dim = 1
+    dim_obs = 1
+    _PARAMS = ("initial_sd", "transition_sd", "likelihood_sd")
+
+    def __init__(self, initial_sd=math.sqrt(2.0), transition_sd=math.sqrt(10.0), likelihood_sd=1.0, name=None):
+        super().__init__(name=name)
+        self.initial_sd = float(initial_sd)
+        self.transition_sd = float(transition_sd)
+        self.likelihood_sd = float(likelihood_sd)
+
+    def __setattr__(self, key, value):
+        self.__dict__[key] = value
+        if key in self._PARAMS:
+            self.__dict__.pop("_derived", None)
+
+    def derived(self):
+        if "_derived" not in self.__dict__:
+            p = dict(s0=np.float32(self.initial_sd), tsd=np.float32(self.transition_sd),
+                     lsd=np.float32(self.likelihood_sd),
+                     c=np.float32(np.float32(np.log(np.float32(2.0 * math.pi))) / np.float32(2.0)))
+            s = _lib.NL1DModel(float(p["s0"]), float(p["tsd"]), float(p["lsd"]), float(p["c"]))
+            self.__dict__["_derived"] = (p, s)
+        return self.__dict__["_derived"]
+
+    def gpu_supported(self):
+        return True
+
+    @staticmethod
+    def drift(t):
+        """8 cos(1.2 t) as the kernels form it: 8 * float32(cos(float64(1.2f * t)))."""
+        a = np.float32(1.2) * np.asarray(t, np.float32)
+        return (np.float32(8.0) * np.cos(a.astype(np.float64)).astype(np.float32)).astype(np.float32)
+
+    def transition_mean(self, x, t_previous):
+        x = np.asarray(x, np.float32)
+        f = np.float32
+        return (f(0.5) * x + (f(25.0) * x) / (f(1.0) + x * x)) + self.drift(t_previous)
+
+    def simulate(self, t_all, random_key):
+        """StateSpaceModel.simulate (ssm.py:138-163): split(key, 2T); the first T keys
+        drive the latent chain, the last T the observations."""
+        p, _ = self.derived()
+        t_np = np.asarray(t_all.cpu() if isinstance(t_all, torch.Tensor) else t_all, np.float32).reshape(-1)
+        T = t_np.size
+        keys = mrandom.split(random_key, 2 * T)
+        ex = _normal_keys(keys[:T], 1).cpu().numpy()[:, 0]
+        ey = _normal_keys(keys[T:], 1).cpu().numpy()[:, 0]
+        x = np.empty(T, np.float32)
+        x[0] = ex[0] * p["s0"]
+        for i in range(1, T):
+            x[i] = self.transition_mean(x[i - 1], t_np[i - 1]) + ex[i] * p["tsd"]
+        y = (x * x) / np.float32(20.0) + ey * p["lsd"]
+        dev = _dev.device()
+        return cdict(x=torch.from_numpy(x[:, None].copy()).to(dev), y=torch.from_numpy(y[:, None].copy()).to(dev),
+                     t=torch.as_tensor(t_np, device=dev), name=f"{self.name} simulation")
+
+
 def _normal_keys(keys, d):
     keys = _dev.as_key(keys)
     out = torch.empty((keys.shape[0], d), dtype=torch.float32, device=keys.device)
@@ -263,6 +326,10 @@ class OptimalNonLinearGaussianParticleFilter(ParticleFilter):
 
 
 def _check_lg(ssm_scenario, particle_filter):
+    if isinstance(ssm_scenario, NonLinear1DBenchmark):
+        if type(particle_filter) is not BootstrapFilter:
+            raise NotImplementedError(f"{particle_filter.__class__.__name__}: no fused GPU kernel for this model")
+        return
     if not isinstance(ssm_scenario, TimeHomogenousLinearGaussian):
         raise NotImplementedError(f"{ssm_scenario.__class__.__name__}: no fused GPU kernel for this model")
     if not isinstance(particle_filter, (BootstrapFilter, OptimalNonLinearGaussianParticleFilter)):
@@ -273,6 +340,8 @@ def _check_lg(ssm_scenario, particle_filter):
 
 def _kernels(ssm_scenario, particle_filter):
     """(C-ABI prefix, model struct) of the fused kernels for this scenario / filter pair."""
+    if isinstance(ssm_scenario, NonLinear1DBenchmark):
+        return "mgb_pf_nl1d", ssm_scenario.derived()[1]
     if isinstance(particle_filter, OptimalNonLinearGaussianParticleFilter):
         if getattr(particle_filter, "_struct", None) is None:
             particle_filter.startup(ssm_scenario)
@@ -325,10 +394,12 @@ def resample_particles(particles, random_key, resample_full=True, resampling="sy
     return out
 
 
-def _step(s, n, key, y_t, x_prev_soa, anc, lw_prev, prefix="mgb_pf_lg"):
+def _step(s, n, key, y_t, x_prev_soa, anc, lw_prev, prefix="mgb_pf_lg", t_prev=None):
     x_new = torch.empty_like(x_prev_soa)
     lw_new = torch.empty(n, dtype=torch.float32, device=x_prev_soa.device)
-    call(prefix + "_propagate", ctypes.byref(s), n, _dev.ptr(key), _dev.ptr(y_t), _dev.ptr(x_prev_soa),
+    # the non-linear model's transition depends on t_previous
+    tp = (float(t_prev),) if prefix == "mgb_pf_nl1d" else ()
+    call(prefix + "_propagate", ctypes.byref(s), n, _dev.ptr(key), _dev.ptr(y_t), *tp, _dev.ptr(x_prev_soa),
          _dev.ptr(anc), _dev.ptr(lw_prev), _dev.ptr(x_new), _dev.ptr(lw_new), _dev.stream_ptr())
     return x_new, lw_new
 
@@ -345,7 +416,7 @@ def propagate_particle_filter(ssm_scenario, particle_filter, particles, y_new, t
     x_prev = particles.value[-1].t().contiguous()
     lw_prev = particles.log_weight[-1].contiguous()
     y_t = _y2(y_new, ssm_scenario.dim_obs).reshape(-1)
-    x_new, lw_new = _step(s, n, key, y_t, x_prev, None, lw_prev, prefix)
+    x_new, lw_new = _step(s, n, key, y_t, x_prev, None, lw_prev, prefix, t_prev=particles.t[-1])
     out = particles.copy()
     out.value = torch.cat([particles.value, x_new.t()[None]], 0)
     out.log_weight = torch.cat([particles.log_weight, lw_new[None]], 0)
@@ -376,7 +447,14 @@ def run_particle_filter_for_marginals(ssm_scenario, particle_filter, y, t, rando
     if initial_sample is not None:
         return _run_from(ssm_scenario, s, initial_sample, y2, t, key, ess_threshold, resampling, prefix)
     T = y2.shape[0]
-    ws = _dev.workspace(getattr(_lib.lib(), prefix + "_workspace")(n, T, d, sc), dev)
+    nl = prefix == "mgb_pf_nl1d"
+    if nl:
+        t32 = _dev.as_f32(t).reshape(-1).contiguous()
+        if t32.numel() != T:
+            raise ValueError(f"t has {t32.numel()} entries for {T} observations")
+        ws = _dev.workspace(_lib.lib().mgb_pf_nl1d_workspace(n, T, sc), dev)
+    else:
+        ws = _dev.workspace(getattr(_lib.lib(), prefix + "_workspace")(n, T, d, sc), dev)
     logz = torch.empty(1, dtype=torch.float64, device=dev)
     ess = torch.empty(T, dtype=torch.float32, device=dev)
     res = torch.empty(T, dtype=torch.int32, device=dev)
@@ -386,9 +464,13 @@ def run_particle_filter_for_marginals(ssm_scenario, particle_filter, y, t, rando
     out = _lib.PFOutputs(logz.data_ptr(), ess.data_ptr(), res.data_ptr(), xh.data_ptr() if history else None,
                          lh.data_ptr() if history else None, None if history else xh.data_ptr(),
                          None if history else lh.data_ptr(), err.data_ptr(), None)
-    flags = 0 if (persistent or prefix != "mgb_pf_lg") else RUN_LAUNCH_PER_STEP
-    call(prefix + "_run", ctypes.byref(s), n, T, _dev.ptr(key), _dev.ptr(y2), float(ess_threshold), sc | flags,
-         _dev.ptr(ws), ws.numel(), ctypes.byref(out), _dev.stream_ptr())
+    if nl:
+        call("mgb_pf_nl1d_run", ctypes.byref(s), n, T, _dev.ptr(key), _dev.ptr(y2), _dev.ptr(t32),
+             float(ess_threshold), sc, _dev.ptr(ws), ws.numel(), ctypes.byref(out), _dev.stream_ptr())
+    else:
+        flags = 0 if (persistent or prefix != "mgb_pf_lg") else RUN_LAUNCH_PER_STEP
+        call(prefix + "_run", ctypes.byref(s), n, T, _dev.ptr(key), _dev.ptr(y2), float(ess_threshold), sc | flags,
+             _dev.ptr(ws), ws.numel(), ctypes.byref(out), _dev.stream_ptr())
     e = int(err.item())
     if e & 1:
         raise _lib.MGBError(5, "run_particle_filter_for_marginals")
@@ -408,10 +490,14 @@ def _run_from(ssm_scenario, s, initial_sample, y2, t, key, ess_threshold, resamp
     vals, lws, esss, resd = [], [], [], []
     logz = 0.0
     lse_prev = float(torch.logsumexp(lw.double(), 0))
+    # t_previous of step i: the initial sample's last time, then t[i - 1] (filtering.py:295-303)
+    t_np = np.asarray(t.cpu() if isinstance(t, torch.Tensor) else t, np.float32).reshape(-1)
+    t_prev = float(initial_sample.t[-1]) if initial_sample.t is not None else 0.0
     for i in range(T):
         res = ess < ess_threshold * n
         anc = resample(lw, keys[i], resampling) if res else None
-        x, lw = _step(s, n, keys[i], y2[i], x, anc, None if res else lw, prefix)
+        x, lw = _step(s, n, keys[i], y2[i], x, anc, None if res else lw, prefix, t_prev=t_prev)
+        t_prev = float(t_np[i]) if i < t_np.size else t_prev
         lse = float(torch.logsumexp(lw.double(), 0))
         logz += lse - (math.log(n) if res else lse_prev)
         lse_prev = lse

@@ -62,6 +62,10 @@ class _SVModel(ctypes.Structure):
                 ("cB", ctypes.c_float), ("c0", ctypes.c_float), ("m0", ctypes.c_float)]
 
 
+class _NLModel(ctypes.Structure):
+    _fields_ = [("s0", ctypes.c_float), ("tsd", ctypes.c_float), ("lsd", ctypes.c_float), ("c", ctypes.c_float)]
+
+
 class _FFBSiModel(ctypes.Structure):
     _fields_ = [("d", ctypes.c_int), ("F", ctypes.c_void_p), ("Pq", ctypes.c_void_p), ("cq", ctypes.c_float)]
 
@@ -111,6 +115,14 @@ def lib():
         L.o_sv_run.restype = ctypes.c_double
         L.o_sv_batch.argtypes = [ctypes.POINTER(_SVModel), i64, i64p, i64p, i64p, f32p, u32p, ctypes.c_float,
                                  ctypes.c_int, f64p]
+        L.o_nl_drift.argtypes = [ctypes.c_float]
+        L.o_nl_drift.restype = ctypes.c_float
+        L.o_nl_init.argtypes = [ctypes.POINTER(_NLModel), i64, u32p, vp, f32p, f32p]
+        L.o_nl_propagate.argtypes = [ctypes.POINTER(_NLModel), i64, u32p, ctypes.c_float, ctypes.c_float, f32p, vp,
+                                     vp, f32p, f32p]
+        L.o_nl_run.argtypes = [ctypes.POINTER(_NLModel), i64, i64, u32p, f32p, f32p, ctypes.c_float, ctypes.c_int,
+                               f32p, i32p, vp, vp]
+        L.o_nl_run.restype = ctypes.c_double
         L.o_ffbsi_lg.argtypes = [ctypes.POINTER(_FFBSiModel), i64, i64, i64, f32p, f32p, u32p, f32p, i32p]
         L.o_stitch_lg.argtypes = [ctypes.POINTER(_FFBSiModel), i64, i64, f32p, f32p, f32p, u32p, i32p]
         L.o_transition_potential_pairs.argtypes = [ctypes.POINTER(_FFBSiModel), i64, f32p, f32p, f32p]
@@ -395,6 +407,51 @@ def sv_batch(params, n, T, y_off, y, keys, ess_threshold=0.5, scheme="multinomia
     lib().o_sv_batch(ctypes.byref(s), n.size, n, T, y_off, _f32(y), _u32(keys).reshape(-1), float(ess_threshold),
                      SCHEMES[scheme], out)
     return out
+
+
+def _nl_struct(p):
+    return _NLModel(*(float(p[k]) for k in ("s0", "tsd", "lsd", "c")))
+
+
+def nl_drift(t):
+    """8 cos(1.2 t) as the filters compute it (nonlinear1d.py:41-46)."""
+    return np.float32(lib().o_nl_drift(float(np.float32(t))))
+
+
+def nl_init(params, n, key, y0=None):
+    """initiate_particles on NonLinear1DBenchmark: (x (n,), lw (n,))."""
+    x = np.empty(n, np.float32)
+    lw = np.empty(n, np.float32)
+    y0 = None if y0 is None else _f32(y0).reshape(1)
+    lib().o_nl_init(ctypes.byref(_nl_struct(params)), n, _u32(key), _ptr(y0), x, lw)
+    return x, lw
+
+
+def nl_propagate(params, key_t, y, t_prev, x_prev, anc=None, lw_prev=None):
+    """One bootstrap step from t_prev: (x_new (n,), lw_new (n,))."""
+    x_prev = _f32(x_prev).reshape(-1)
+    n = x_prev.size
+    x_new = np.empty(n, np.float32)
+    lw_new = np.empty(n, np.float32)
+    anc = None if anc is None else np.ascontiguousarray(anc, np.int32)
+    lw_prev = None if lw_prev is None else _f32(lw_prev)
+    lib().o_nl_propagate(ctypes.byref(_nl_struct(params)), n, _u32(key_t), float(np.float32(y)),
+                         float(np.float32(t_prev)), x_prev, _ptr(anc), _ptr(lw_prev), x_new, lw_new)
+    return x_new, lw_new
+
+
+def nl_run(params, n, key, y, t, ess_threshold=0.5, scheme="systematic", history=False):
+    """run_particle_filter_for_marginals with BootstrapFilter on NonLinear1DBenchmark."""
+    y = _f32(y).reshape(-1)
+    t = _f32(t).reshape(-1)
+    T = y.size
+    ess = np.empty(T, np.float32)
+    res = np.empty(T, np.int32)
+    xh = np.empty((T, n), np.float32) if history else None
+    lh = np.empty((T, n), np.float32) if history else None
+    logZ = lib().o_nl_run(ctypes.byref(_nl_struct(params)), n, T, _u32(key), y, t, float(ess_threshold),
+                          SCHEMES[scheme], ess, res, _ptr(xh), _ptr(lh))
+    return dict(log_z=logZ, ess=ess, resampled=res.astype(bool), value=xh, log_weight=lh)
 
 
 def ffbsi_lg(F, Pq, cq, x_hist, lw_hist, key, M):

@@ -13,6 +13,7 @@
  *       mocat/src/ssm/linear_gaussian/linear_gaussian.py:46-51, 86-94, 118-128;
  *       gaussian_potential mocat/src/utils.py:49-105 (vectorised branch :90-104);
  *   - StochasticVolatility: mocat/src/ssm/scenarios/stochastic_volatility.py:71-102;
+ *   - NonLinear1DBenchmark: mocat/src/ssm/scenarios/nonlinear1d.py:16-80;
  *   - OptimalNonLinearGaussianParticleFilter fused step:
  *       mocat/src/ssm/nonlinear_gaussian.py:198-209, 264-281;
  *   - ESS / logsumexp: mocat/src/metrics.py:69-78 (max-shifted logsumexp of
@@ -650,6 +651,112 @@ void o_sv_batch(const o_sv_model *md, int64_t B, const int64_t *n, const int64_t
 #pragma omp parallel for schedule(dynamic, 1)
     for (int64_t b = 0; b < B; ++b)
         logZ[b] = o_sv_run(md, n[b], T[b], keys + 2 * b, y + y_off[b], ess_threshold, scheme, NULL, NULL);
+}
+
+/* ------------------------------- one-dimensional non-linear benchmark model */
+
+typedef struct {
+    float s0;   /* initial_sd */
+    float tsd;  /* transition_sd */
+    float lsd;  /* likelihood_sd */
+    float c;    /* log(2 pi) / 2: gaussian_potential with unit precision (utils.py:49-105) */
+} o_nl_model;
+
+/* 8 cos(1.2 t) (nonlinear1d.py:41-46): the float32 product 1.2f t, a
+ * double-precision cosine rounded to float32, an exact scaling by 8 */
+float o_nl_drift(float t)
+{
+    return 8.0f * (float)cos((double)(1.2f * t));
+}
+
+/* _transition_mean (nonlinear1d.py:41-46), left to right in float32 */
+static inline float o_nl_mean(float x, float drift)
+{
+    return (0.5f * x + (25.0f * x) / (1.0f + x * x)) + drift;
+}
+
+/* likelihood_potential (nonlinear1d.py:63-75): 0.5 ((y - x^2 / 20) / lsd)^2 + c */
+static inline float o_nl_potential(const o_nl_model *md, float x, float y)
+{
+    float z = (y - (x * x) / 20.0f) / md->lsd;
+    return 0.5f * (z * z) + md->c;
+}
+
+/* initiate_particles with initial_sample (nonlinear1d.py:36-39):
+ * x_i = normal(split(key, n)[i], (1,)) s0, lw_i = -potential(x_i, y0) (0 without y0) */
+void o_nl_init(const o_nl_model *md, int64_t n, const uint32_t *key, const float *y0, float *x, float *lw)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        uint32_t a0, a1;
+        o_split_at(key[0], key[1], (uint64_t)n, (uint64_t)i, &a0, &a1);
+        x[i] = o_bits_to_normal(o_bits_at(a0, a1, 1, 0)) * md->s0;
+        lw[i] = y0 ? -o_nl_potential(md, x[i], y0[0]) : 0.0f;
+    }
+}
+
+/* bootstrap propagate + weight from t_previous (filtering.py:124-139, 160-170):
+ * x_new = mean(x_src, t_prev) + normal(split(k_t, n)[i], (1,)) tsd;
+ * lw_new = lw_res - potential(x_new, y).  anc NULL: no resampling; lw_prev NULL: 0. */
+void o_nl_propagate(const o_nl_model *md, int64_t n, const uint32_t *kt, float y, float t_prev, const float *x_prev,
+                    const int32_t *anc, const float *lw_prev, float *x_new, float *lw_new)
+{
+    const float drift = o_nl_drift(t_prev);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        uint32_t a0, a1;
+        o_split_at(kt[0], kt[1], (uint64_t)n, (uint64_t)i, &a0, &a1);
+        float e = o_bits_to_normal(o_bits_at(a0, a1, 1, 0));
+        float xn = o_nl_mean(x_prev[anc ? anc[i] : i], drift) + e * md->tsd;
+        x_new[i] = xn;
+        lw_new[i] = (lw_prev ? lw_prev[i] : 0.0f) - o_nl_potential(md, xn, y);
+    }
+}
+
+/* Whole bootstrap filter (filtering.py:255-324) on the model; t[T] are the
+ * times, step t propagating from t[t-1].  Outputs as o_lg_run (d = 1). */
+double o_nl_run(const o_nl_model *md, int64_t n, int64_t T, const uint32_t *key, const float *y, const float *t,
+                float ess_threshold, int scheme, float *ess_out, int32_t *resampled_out, float *x_hist,
+                float *lw_hist)
+{
+    float *xa = (float *)malloc(sizeof(float) * (size_t)n), *xb = (float *)malloc(sizeof(float) * (size_t)n);
+    float *la = (float *)malloc(sizeof(float) * (size_t)n), *lb = (float *)malloc(sizeof(float) * (size_t)n);
+    int32_t *anc = (int32_t *)malloc(sizeof(int32_t) * (size_t)n);
+    uint32_t *keys = (uint32_t *)malloc(sizeof(uint32_t) * 2 * (size_t)(T > 1 ? T : 2));
+    o_lg_step_keys(key, T, keys);
+    o_nl_init(md, n, keys, y, xa, la);
+    double st[4];
+    o_lse_ess(la, n, st);
+    const double logn = log((double)n);
+    double logZ = st[1] - logn, lse_prev = st[1];
+    float ess_prev = (float)st[3];
+    if (ess_out) ess_out[0] = ess_prev;
+    if (resampled_out) resampled_out[0] = 0;
+    if (x_hist) memcpy(x_hist, xa, sizeof(float) * (size_t)n);
+    if (lw_hist) memcpy(lw_hist, la, sizeof(float) * (size_t)n);
+    for (int64_t s = 1; s < T; ++s) {
+        const uint32_t *kt = keys + 2 * s;
+        int res = ess_prev < ess_threshold * (float)n;
+        if (res) {
+            if (scheme == 0) o_resample_systematic(la, n, o_bits_at(kt[0], kt[1], 1, 0) >> 9, anc);
+            else if (scheme == 1) o_resample_multinomial(la, n, kt, anc);
+            else o_resample_gumbel(la, n, n, kt, anc);
+        }
+        o_nl_propagate(md, n, kt, y[s], t[s - 1], xa, res ? anc : NULL, res ? NULL : la, xb, lb);
+        o_lse_ess(lb, n, st);
+        logZ += st[1] - (res ? logn : lse_prev);
+        lse_prev = st[1];
+        ess_prev = (float)st[3];
+        if (ess_out) ess_out[s] = ess_prev;
+        if (resampled_out) resampled_out[s] = res;
+        if (x_hist) memcpy(x_hist + s * n, xb, sizeof(float) * (size_t)n);
+        if (lw_hist) memcpy(lw_hist + s * n, lb, sizeof(float) * (size_t)n);
+        float *tp = xa; xa = xb; xb = tp;
+        tp = la; la = lb; lb = tp;
+    }
+    free(keys);
+    free(xa); free(xb); free(la); free(lb); free(anc);
+    return logZ;
 }
 
 /* ------------------------------------------- backward simulation (full FFBSi) */
