@@ -282,6 +282,21 @@ size_t mgb_pf_nl1d_workspace(int64_t n, int64_t T, int scheme);
 int mgb_pf_nl1d_run(const mgb_nl1d_model *model_host, int64_t n, int64_t T, const uint32_t *key_dev, const float *y_dev,
                     const float *t_dev, float ess_threshold, int scheme, void *ws_dev, size_t ws_bytes,
                     const mgb_pf_outputs *out, void *stream);
+/* Backward simulation and stitching with this model's transition
+ * (transition_potential, nonlinear1d.py:48-54):
+ *   transition_potential(x0 at t_prev -> x1) = 0.5 ((x1 - mean(x0, t_prev)) / transition_sd)^2 + c
+ * with the key flows of mgb_ffbsi_lg / mgb_stitch_lg / mgb_transition_potential_pairs.
+ * mgb_ffbsi_nl1d: x_hist (T, N), lw_hist (T, N), t_dev the T times (step t's
+ * transition leaves t_dev[t]); out (T, M), idx (T, M); workspace mgb_ffbsi_workspace(N, T, 1). */
+int mgb_ffbsi_nl1d(const mgb_nl1d_model *model_host, int64_t T, int64_t N, int64_t M, const float *x_hist_dev,
+                   const float *lw_hist_dev, const float *t_dev, const uint32_t *key_dev, float *out_dev,
+                   int32_t *idx_dev, void *ws_dev, size_t ws_bytes, void *stream);
+int mgb_stitch_nl1d(const mgb_nl1d_model *model_host, int64_t M0, int64_t M1, const float *x0_dev,
+                    const float *x1_dev, const float *lw1_dev, float t_previous, const uint32_t *key_dev,
+                    int32_t *idx_dev, void *stream);
+int mgb_transition_potential_pairs_nl1d(const mgb_nl1d_model *model_host, int64_t M, const float *x0_dev,
+                                        const float *x1_dev, float t_previous, const float *lw_dev, float *out_dev,
+                                        void *stream);
 
 /* ------------------------------- many stochastic-volatility filters at once
  * B independent run_particle_filter_for_marginals calls (mocat/src/ssm/filtering.py:255-324)

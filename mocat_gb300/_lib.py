@@ -116,6 +116,9 @@ _SIGNATURES = {
     "mgb_pf_nl1d_workspace": ([_I64, _I64, _I32], _SZ),
     "mgb_pf_nl1d_run": ([ctypes.POINTER(NL1DModel), _I64, _I64, _P, _P, _P, _F, _I32, _P, _SZ,
                          ctypes.POINTER(PFOutputs), _P], _I32),
+    "mgb_ffbsi_nl1d": ([ctypes.POINTER(NL1DModel), _I64, _I64, _I64, _P, _P, _P, _P, _P, _P, _P, _SZ, _P], _I32),
+    "mgb_stitch_nl1d": ([ctypes.POINTER(NL1DModel), _I64, _I64, _P, _P, _P, _F, _P, _P, _P], _I32),
+    "mgb_transition_potential_pairs_nl1d": ([ctypes.POINTER(NL1DModel), _I64, _P, _P, _F, _P, _P, _P], _I32),
     "mgb_logreg_workspace": ([_I64, _I64, ctypes.c_int32, _I32], _SZ),
     "mgb_logreg_potential_grad": ([_P, _P, _I64, ctypes.c_int32, _P, _I64, _P, _P, _I32, _P, _P, _SZ, _P], _I32),
     "mgb_smc_logreg_workspace": ([ctypes.POINTER(SMCConfig), _I64], _SZ),

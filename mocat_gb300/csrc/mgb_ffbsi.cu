@@ -1,5 +1,6 @@
-// Backward simulation (forward filtering, backward simulation) for a
-// linear-Gaussian transition: the full O(N M) version.
+// Backward simulation (forward filtering, backward simulation) and particle
+// stitching: the full O(N M) versions, for a linear-Gaussian transition and for
+// the one-dimensional non-linear benchmark transition.
 //
 // Reference: backward_simulation_full (mocat/src/ssm/backward.py:217-245),
 // full_resampling / full_resample_single (:20-40):
@@ -7,43 +8,99 @@
 //   samples at T-1:  categorical(t_keys[T-1], lw_{T-1}, (M,))  -- one (M, N) Gumbel draw
 //   for t = T-2 .. 0, sample j (keys = split(t_keys[t], M)):
 //     index_j = argmax_i gumbel(keys[j], (N,))_i + lw_{t,i} - transition_potential(x_t^i -> xs_{t+1}^j)
-// transition_potential(x0 -> x1) = 0.5 |(x1 - F x0) @ Pq|^2 + cq (linear_gaussian.py,
-// gaussian_potential utils.py:49-105).  First maximum wins, NaN entries are skipped.
+// transition_potential(x0 -> x1) = potential(x1 - mean(x0)):
+//   linear-Gaussian   mean = F x0, potential(diff) = 0.5 |diff @ Pq|^2 + cq
+//                     (linear_gaussian.py, gaussian_potential utils.py:49-105);
+//   non-linear 1-D    mean = 0.5 x + 25 x / (1 + x^2) + 8 cos(1.2 t_prev),
+//                     potential(diff) = 0.5 (diff / transition_sd)^2 + log(2 pi) / 2
+//                     (nonlinear1d.py:41-61).
+// The kernels are templates over a transition policy (LGT<D>, NLT) that supplies
+// the two.  First maximum wins, NaN entries are skipped.
 //
-// One CTA per sample: F x_t^i is computed once per step by a separate kernel
+// One CTA per sample: mean(x_t^i) is computed once per step by a separate kernel
 // (dimension-major, read through L2 by every CTA); the Gumbel bits of element
 // i and i + ceil(N/2) come from the two halves of one cipher call.  The
 // argmax is reduced in the fixed order (value, then smaller index), so the
 // result does not depend on scheduling.
 #include "mgb_internal.cuh"
+#include "mgb_nl1d.cuh"
 
 namespace mgb {
 
 constexpr int FB_TPB = 256;
 
+// linear-Gaussian transition
 template <int D>
-struct FBP {
+struct LGT {
+  static constexpr int DIM = D;
+  static constexpr bool kDrift = false;
   float F[D * D], Pq[D * D];
   float cq;
   uint32_t one;
+  __device__ __forceinline__ void mean(const float (&x)[D], float (&m)[D], float) const {
+#pragma unroll
+    for (int r = 0; r < D; ++r) {
+      float v = __fmul_rn(F[r * D], x[0]);
+#pragma unroll
+      for (int k = 1; k < D; ++k) v = __fmaf_rn(F[r * D + k], x[k], v);
+      m[r] = v;
+    }
+  }
+  __device__ __forceinline__ float potential(const float (&diff)[D]) const {
+    float quad = 0.0f;
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      float v = __fmul_rn(diff[0], Pq[k]);
+#pragma unroll
+      for (int r = 1; r < D; ++r) v = __fmaf_rn(diff[r], Pq[r * D + k], v);
+      quad = k == 0 ? __fmul_rn(v, v) : __fmaf_rn(v, v, quad);
+    }
+    return __fadd_rn(__fmul_rn(0.5f, quad), cq);
+  }
 };
 
-// F x_t^i for all i (dimension-major in and out)
-template <int D>
-__global__ void __launch_bounds__(FB_TPB) k_ffbsi_fx(const __grid_constant__ FBP<D> p, int64_t N,
+// non-linear 1-D benchmark transition; t_previous from *tp (device) or tv
+struct NLT {
+  static constexpr int DIM = 1;
+  static constexpr bool kDrift = true;
+  float tsd, c;
+  const float *tp;
+  float tv;
+  uint32_t one;
+  __device__ __forceinline__ void mean(const float (&x)[1], float (&m)[1], float drift) const {
+    m[0] = nl_mean(x[0], drift);
+  }
+  __device__ __forceinline__ float potential(const float (&diff)[1]) const { return nl_gauss(diff[0], tsd, c); }
+};
+
+// the policy's per-launch constant (8 cos(1.2 t_prev)), computed once per block
+// by thread 0; every thread of the block calls this
+template <class TP>
+__device__ __forceinline__ float block_drift(const TP &p, float *sm) {
+  if constexpr (TP::kDrift) {
+    if (threadIdx.x == 0) sm[0] = nl_drift(p.tp ? *p.tp : p.tv);
+    __syncthreads();
+    return sm[0];
+  } else {
+    return 0.0f;
+  }
+}
+
+// mean(x_t^i) for all i (dimension-major in and out)
+template <class TP>
+__global__ void __launch_bounds__(FB_TPB) k_ffbsi_fx(const __grid_constant__ TP p, int64_t N,
                                                       const float *__restrict__ x, float *__restrict__ fx) {
+  constexpr int D = TP::DIM;
+  __shared__ float sm[1];
+  const float drift = block_drift(p, sm);
   const int64_t i = blockIdx.x * (int64_t)FB_TPB + threadIdx.x;
   if (i >= N) return;
-  float xv[D];
+  float xv[D], m[D];
 #pragma unroll
   for (int k = 0; k < D; ++k) xv[k] = x[k * N + i];
+  p.mean(xv, m, drift);
 #pragma unroll
-  for (int r = 0; r < D; ++r) {
-    float v = __fmul_rn(p.F[r * D], xv[0]);
-#pragma unroll
-    for (int k = 1; k < D; ++k) v = __fmaf_rn(p.F[r * D + k], xv[k], v);
-    fx[r * N + i] = v;
-  }
+  for (int r = 0; r < D; ++r) fx[r * N + i] = m[r];
 }
 
 struct Best {
@@ -102,11 +159,12 @@ __global__ void __launch_bounds__(FB_TPB) k_ffbsi_last(int64_t N, int64_t M, con
 }
 
 // step t: sample j conditions on its state at t + 1
-template <int D>
-__global__ void __launch_bounds__(FB_TPB) k_ffbsi_step(const __grid_constant__ FBP<D> p, int64_t N, int64_t M,
+template <class TP>
+__global__ void __launch_bounds__(FB_TPB) k_ffbsi_step(const __grid_constant__ TP p, int64_t N, int64_t M,
                                                         const float *__restrict__ fx, const float *__restrict__ lw,
                                                         const float *__restrict__ x_next_samples,
                                                         const uint32_t *tkey, int32_t *__restrict__ idx) {
+  constexpr int D = TP::DIM;
   __shared__ Best sm[FB_TPB / 32];
   __shared__ float x1[D];
   __shared__ uint32_t kj[2];
@@ -133,16 +191,7 @@ __global__ void __launch_bounds__(FB_TPB) k_ffbsi_step(const __grid_constant__ F
       float diff[D];
 #pragma unroll
       for (int r = 0; r < D; ++r) diff[r] = __fsub_rn(x1[r], fx[r * N + i]);
-      float quad = 0.0f;
-#pragma unroll
-      for (int k = 0; k < D; ++k) {
-        float v = __fmul_rn(diff[0], p.Pq[k]);
-#pragma unroll
-        for (int r = 1; r < D; ++r) v = __fmaf_rn(diff[r], p.Pq[r * D + k], v);
-        quad = k == 0 ? __fmul_rn(v, v) : __fmaf_rn(v, v, quad);
-      }
-      const float pot = __fadd_rn(__fmul_rn(0.5f, quad), p.cq);
-      best_take(b, __fadd_rn(g, __fsub_rn(lw[i], pot)), (int32_t)i);
+      best_take(b, __fadd_rn(g, __fsub_rn(lw[i], p.potential(diff))), (int32_t)i);
     }
   }
   const int32_t bi = block_argmax<FB_TPB>(b, sm);
@@ -162,55 +211,45 @@ __global__ void k_ffbsi_take(int64_t N, int64_t M, const float *__restrict__ x, 
 
 // transition potential of particle pairs (x0_i -> x1_i), plus lw_i when given
 // (non_interacting_log_weight of fixed_lag_stitching, online_smoothing.py:191-193)
-template <int D>
-__global__ void __launch_bounds__(FB_TPB) k_pair_potential(const __grid_constant__ FBP<D> p, int64_t M,
+template <class TP>
+__global__ void __launch_bounds__(FB_TPB) k_pair_potential(const __grid_constant__ TP p, int64_t M,
                                                             const float *__restrict__ x0, const float *__restrict__ x1,
                                                             const float *__restrict__ lw, float *__restrict__ out) {
+  constexpr int D = TP::DIM;
+  __shared__ float sd[1];
+  const float drift = block_drift(p, sd);
   const int64_t i = blockIdx.x * (int64_t)FB_TPB + threadIdx.x;
   if (i >= M) return;
-  float xv[D], diff[D];
+  float xv[D], m[D], diff[D];
 #pragma unroll
   for (int k = 0; k < D; ++k) xv[k] = x0[k * M + i];
+  p.mean(xv, m, drift);
 #pragma unroll
-  for (int r = 0; r < D; ++r) {
-    float v = __fmul_rn(p.F[r * D], xv[0]);
-#pragma unroll
-    for (int k = 1; k < D; ++k) v = __fmaf_rn(p.F[r * D + k], xv[k], v);
-    diff[r] = __fsub_rn(x1[r * M + i], v);
-  }
-  float quad = 0.0f;
-#pragma unroll
-  for (int k = 0; k < D; ++k) {
-    float v = __fmul_rn(diff[0], p.Pq[k]);
-#pragma unroll
-    for (int r = 1; r < D; ++r) v = __fmaf_rn(diff[r], p.Pq[r * D + k], v);
-    quad = k == 0 ? __fmul_rn(v, v) : __fmaf_rn(v, v, quad);
-  }
-  const float pot = __fadd_rn(__fmul_rn(0.5f, quad), p.cq);
+  for (int r = 0; r < D; ++r) diff[r] = __fsub_rn(x1[r * M + i], m[r]);
+  const float pot = p.potential(diff);
   out[i] = lw ? __fadd_rn(lw[i], pot) : pot;
 }
 
 // full_stitch (online_smoothing.py:21-41): CTA j conditions on x0_j and draws among the x1_i
-template <int D>
-__global__ void __launch_bounds__(FB_TPB) k_stitch(const __grid_constant__ FBP<D> p, int64_t M0, int64_t M1,
+template <class TP>
+__global__ void __launch_bounds__(FB_TPB) k_stitch(const __grid_constant__ TP p, int64_t M0, int64_t M1,
                                                     const float *__restrict__ x0, const float *__restrict__ x1,
                                                     const float *__restrict__ lw1, const uint32_t *key,
                                                     int32_t *__restrict__ idx) {
+  constexpr int D = TP::DIM;
   __shared__ Best sm[FB_TPB / 32];
   __shared__ float fx0[D];
   __shared__ uint32_t kj[2];
+  __shared__ float sd[1];
+  const float drift = block_drift(p, sd);
   const int64_t j = blockIdx.x;
   if (threadIdx.x == 0) {
-    float xv[D];
+    float xv[D], m[D];
 #pragma unroll
     for (int k = 0; k < D; ++k) xv[k] = x0[k * M0 + j];
+    p.mean(xv, m, drift);
 #pragma unroll
-    for (int r = 0; r < D; ++r) {
-      float v = __fmul_rn(p.F[r * D], xv[0]);
-#pragma unroll
-      for (int k = 1; k < D; ++k) v = __fmaf_rn(p.F[r * D + k], xv[k], v);
-      fx0[r] = v;
-    }
+    for (int r = 0; r < D; ++r) fx0[r] = m[r];
     uint32_t a0, a1;
     split_at(key[0], key[1], (uint64_t)M0, (uint64_t)j, a0, a1);
     kj[0] = a0;
@@ -231,16 +270,7 @@ __global__ void __launch_bounds__(FB_TPB) k_stitch(const __grid_constant__ FBP<D
       float diff[D];
 #pragma unroll
       for (int r = 0; r < D; ++r) diff[r] = __fsub_rn(x1[r * M1 + i], fx0[r]);
-      float quad = 0.0f;
-#pragma unroll
-      for (int k = 0; k < D; ++k) {
-        float v = __fmul_rn(diff[0], p.Pq[k]);
-#pragma unroll
-        for (int r = 1; r < D; ++r) v = __fmaf_rn(diff[r], p.Pq[r * D + k], v);
-        quad = k == 0 ? __fmul_rn(v, v) : __fmaf_rn(v, v, quad);
-      }
-      const float pot = __fadd_rn(__fmul_rn(0.5f, quad), p.cq);
-      best_take(b, __fadd_rn(g, __fsub_rn(lw1[i], pot)), (int32_t)i);
+      best_take(b, __fadd_rn(g, __fsub_rn(lw1[i], p.potential(diff))), (int32_t)i);
     }
   }
   const int32_t bi = block_argmax<FB_TPB>(b, sm);
@@ -248,8 +278,8 @@ __global__ void __launch_bounds__(FB_TPB) k_stitch(const __grid_constant__ FBP<D
 }
 
 template <int D>
-static FBP<D> pack_fb(const mgb_lg_transition *tr) {
-  FBP<D> p;
+static LGT<D> pack_lgt(const mgb_lg_transition *tr) {
+  LGT<D> p;
   for (int i = 0; i < D * D; ++i) {
     p.F[i] = tr->F[i];
     p.Pq[i] = tr->Pq[i];
@@ -259,25 +289,48 @@ static FBP<D> pack_fb(const mgb_lg_transition *tr) {
   return p;
 }
 
+static NLT pack_nlt(const mgb_nl1d_model *m, const float *tp, float tv) {
+  NLT p;
+  p.tsd = m->transition_sd;
+  p.c = m->c;
+  p.tp = tp;
+  p.tv = tv;
+  p.one = 1u;
+  return p;
+}
+
+template <class TP>
+static int stitch_run(const TP &p, int64_t M0, int64_t M1, const float *x0, const float *x1, const float *lw1,
+                      const uint32_t *key, int32_t *idx, cudaStream_t s) {
+  k_stitch<TP><<<(unsigned)M0, FB_TPB, 0, s>>>(p, M0, M1, x0, x1, lw1, key, idx);
+  return launch_status();
+}
+
+template <class TP>
+static int pairs_run(const TP &p, int64_t M, const float *x0, const float *x1, const float *lw, float *out,
+                     cudaStream_t s) {
+  k_pair_potential<TP><<<(unsigned)((M + FB_TPB - 1) / FB_TPB), FB_TPB, 0, s>>>(p, M, x0, x1, lw, out);
+  return launch_status();
+}
+
 template <int D>
 static int stitch_lg(const mgb_lg_transition *tr, int64_t M0, int64_t M1, const float *x0, const float *x1,
                      const float *lw1, const uint32_t *key, int32_t *idx, cudaStream_t s) {
-  k_stitch<D><<<(unsigned)M0, FB_TPB, 0, s>>>(pack_fb<D>(tr), M0, M1, x0, x1, lw1, key, idx);
-  return launch_status();
+  return stitch_run(pack_lgt<D>(tr), M0, M1, x0, x1, lw1, key, idx, s);
 }
 
 template <int D>
 static int pair_potential(const mgb_lg_transition *tr, int64_t M, const float *x0, const float *x1, const float *lw,
                           float *out, cudaStream_t s) {
-  k_pair_potential<D><<<(unsigned)((M + FB_TPB - 1) / FB_TPB), FB_TPB, 0, s>>>(pack_fb<D>(tr), M, x0, x1, lw, out);
-  return launch_status();
+  return pairs_run(pack_lgt<D>(tr), M, x0, x1, lw, out, s);
 }
 
-template <int D>
-static int ffbsi_lg(const mgb_lg_transition *tr, int64_t T, int64_t N, int64_t M, const float *x_hist,
-                    const float *lw_hist, const uint32_t *key, float *out, int32_t *idx, void *ws, size_t ws_bytes,
-                    cudaStream_t s) {
-  const FBP<D> p = pack_fb<D>(tr);
+// t_all (device, T times): step t's transition leaves x_t at t_all[t] (policies with a drift)
+template <class TP>
+static int ffbsi_run(TP p, const float *t_all, int64_t T, int64_t N, int64_t M, const float *x_hist,
+                     const float *lw_hist, const uint32_t *key, float *out, int32_t *idx, void *ws, size_t ws_bytes,
+                     cudaStream_t s) {
+  constexpr int D = TP::DIM;
   Carver c(ws);
   float *fx = c.take<float>((size_t)D * N);
   uint32_t *tkeys = c.take<uint32_t>(2 * (size_t)T);
@@ -292,17 +345,30 @@ static int ffbsi_lg(const mgb_lg_transition *tr, int64_t T, int64_t N, int64_t M
                                                    out + (size_t)(T - 1) * D * M);
   if ((st = launch_status())) return st;
   for (int64_t t = T - 2; t >= 0; --t) {
-    k_ffbsi_fx<D><<<(unsigned)((N + FB_TPB - 1) / FB_TPB), FB_TPB, 0, s>>>(p, N, x_hist + (size_t)t * xs, fx);
+    if constexpr (TP::kDrift) p.tp = t_all + t;
+    k_ffbsi_fx<TP><<<(unsigned)((N + FB_TPB - 1) / FB_TPB), FB_TPB, 0, s>>>(p, N, x_hist + (size_t)t * xs, fx);
     if ((st = launch_status())) return st;
-    k_ffbsi_step<D><<<(unsigned)M, FB_TPB, 0, s>>>(p, N, M, fx, lw_hist + (size_t)t * N,
-                                                   out + (size_t)(t + 1) * D * M, tkeys + 2 * t,
-                                                   idx + (size_t)t * M);
+    k_ffbsi_step<TP><<<(unsigned)M, FB_TPB, 0, s>>>(p, N, M, fx, lw_hist + (size_t)t * N,
+                                                    out + (size_t)(t + 1) * D * M, tkeys + 2 * t,
+                                                    idx + (size_t)t * M);
     if ((st = launch_status())) return st;
     k_ffbsi_take<D><<<grid_for(M, 256), 256, 0, s>>>(N, M, x_hist + (size_t)t * xs, idx + (size_t)t * M,
                                                      out + (size_t)t * D * M);
     if ((st = launch_status())) return st;
   }
   return OK;
+}
+
+template <int D>
+static int ffbsi_lg(const mgb_lg_transition *tr, int64_t T, int64_t N, int64_t M, const float *x_hist,
+                    const float *lw_hist, const uint32_t *key, float *out, int32_t *idx, void *ws, size_t ws_bytes,
+                    cudaStream_t s) {
+  return ffbsi_run(pack_lgt<D>(tr), nullptr, T, N, M, x_hist, lw_hist, key, out, idx, ws, ws_bytes, s);
+}
+
+static bool ffbsi_sizes_ok(int64_t T, int64_t N, int64_t M) {
+  return T >= 1 && N >= 1 && N <= 0x7FFFFFFFll && M >= 1 && M <= 0x7FFFFFFFll &&
+         (uint64_t)M * (uint64_t)N < (1ull << 32);
 }
 
 }  // namespace mgb
@@ -322,8 +388,7 @@ size_t mgb_ffbsi_workspace(int64_t N, int64_t T, int32_t d) {
 int mgb_ffbsi_lg(const mgb_lg_transition *tr, int64_t T, int64_t N, int64_t M, const float *x_hist,
                  const float *lw_hist, const uint32_t *key, float *out, int32_t *idx, void *ws, size_t ws_bytes,
                  void *stream) {
-  if (!tr || !tr->F || !tr->Pq || T < 1 || N < 1 || N > 0x7FFFFFFFll || M < 1 || M > 0x7FFFFFFFll ||
-      (uint64_t)M * (uint64_t)N >= (1ull << 32) || !x_hist || !lw_hist || !key || !out || !idx || !ws)
+  if (!tr || !tr->F || !tr->Pq || !ffbsi_sizes_ok(T, N, M) || !x_hist || !lw_hist || !key || !out || !idx || !ws)
     return ERR_BAD_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   switch (tr->d) {
@@ -362,6 +427,27 @@ int mgb_transition_potential_pairs(const mgb_lg_transition *tr, int64_t M, const
                                    const float *lw, float *out, void *stream) {
   if (!tr || !tr->F || !tr->Pq || M < 1 || !x0 || !x1 || !out) return ERR_BAD_ARG;
   MGB_FB_DISPATCH(pair_potential, tr, M, x0, x1, lw, out, (cudaStream_t)stream);
+}
+
+int mgb_ffbsi_nl1d(const mgb_nl1d_model *m, int64_t T, int64_t N, int64_t M, const float *x_hist,
+                   const float *lw_hist, const float *t, const uint32_t *key, float *out, int32_t *idx, void *ws,
+                   size_t ws_bytes, void *stream) {
+  if (!m || !ffbsi_sizes_ok(T, N, M) || !x_hist || !lw_hist || !t || !key || !out || !idx || !ws) return ERR_BAD_ARG;
+  return ffbsi_run(pack_nlt(m, nullptr, 0.0f), t, T, N, M, x_hist, lw_hist, key, out, idx, ws, ws_bytes,
+                   (cudaStream_t)stream);
+}
+
+int mgb_stitch_nl1d(const mgb_nl1d_model *m, int64_t M0, int64_t M1, const float *x0, const float *x1,
+                    const float *lw1, float t_previous, const uint32_t *key, int32_t *idx, void *stream) {
+  if (!m || M0 < 1 || M1 < 1 || M0 > 0x7FFFFFFFll || M1 > 0x7FFFFFFFll || !x0 || !x1 || !lw1 || !key || !idx)
+    return ERR_BAD_ARG;
+  return stitch_run(pack_nlt(m, nullptr, t_previous), M0, M1, x0, x1, lw1, key, idx, (cudaStream_t)stream);
+}
+
+int mgb_transition_potential_pairs_nl1d(const mgb_nl1d_model *m, int64_t M, const float *x0, const float *x1,
+                                        float t_previous, const float *lw, float *out, void *stream) {
+  if (!m || M < 1 || !x0 || !x1 || !out) return ERR_BAD_ARG;
+  return pairs_run(pack_nlt(m, nullptr, t_previous), M, x0, x1, lw, out, (cudaStream_t)stream);
 }
 
 }  // extern "C"

@@ -26,6 +26,7 @@
 #include "mgb_resample.cuh"
 #include "mgb_kernels.cuh"
 #include "mgb_pf_common.cuh"
+#include "mgb_nl1d.cuh"
 
 namespace mgb {
 
@@ -34,22 +35,8 @@ struct NLP {
   uint32_t one;  // == 1, multiplier of the cipher's multiply-adds
 };
 
-__device__ __forceinline__ float nl_drift(float t) {
-  const float a = __fmul_rn(1.2f, t);
-  return __fmul_rn(8.0f, __double2float_rn(cos((double)a)));
-}
-
-// 0.5 x + 25 x / (1 + x^2) + drift, left to right
-__device__ __forceinline__ float nl_mean(float x, float drift) {
-  const float a = __fmul_rn(0.5f, x);
-  const float b = __fdiv_rn(__fmul_rn(25.0f, x), __fadd_rn(1.0f, __fmul_rn(x, x)));
-  return __fadd_rn(__fadd_rn(a, b), drift);
-}
-
 __device__ __forceinline__ float nl_potential(const NLP &p, float x, float y) {
-  const float m = __fdiv_rn(__fmul_rn(x, x), 20.0f);
-  const float z = __fdiv_rn(__fsub_rn(y, m), p.lsd);
-  return __fadd_rn(__fmul_rn(0.5f, __fmul_rn(z, z)), p.c);
+  return nl_lik_potential(x, y, p.lsd, p.c);
 }
 
 // normal(key, (1,)) for the particle key (ka, kb)

@@ -535,7 +535,8 @@ def backward_simulation(ssm_scenario, marginal_particles, random_key, n_samps=No
     cdict(value (T, n_samps, d), t, num_transition_evals (T,))."""
     if maximum_rejections > 0:
         raise NotImplementedError("backward simulation by rejection sampling is not built (maximum_rejections=0)")
-    if not isinstance(ssm_scenario, TimeHomogenousLinearGaussian):
+    nl = isinstance(ssm_scenario, NonLinear1DBenchmark)
+    if not nl and not isinstance(ssm_scenario, TimeHomogenousLinearGaussian):
         raise NotImplementedError(f"{ssm_scenario.__class__.__name__}: no backward-simulation kernel for this model")
     if not ssm_scenario.gpu_supported():
         raise NotImplementedError(f"d = {ssm_scenario.dim} not compiled")
@@ -545,13 +546,20 @@ def backward_simulation(ssm_scenario, marginal_particles, random_key, n_samps=No
     x = _dev.as_f32(value).permute(0, 2, 1).contiguous()
     lw = _dev.as_f32(marginal_particles.log_weight).reshape(T, n).contiguous()
     key = _dev.as_key(random_key)
-    _, s = _transition_struct(ssm_scenario)
     dev = x.device
     ws = _dev.workspace(_lib.lib().mgb_ffbsi_workspace(n, T, d), dev)
     out = torch.empty((T, d, M), dtype=torch.float32, device=dev)
     idx = torch.empty((T, M), dtype=torch.int32, device=dev)
-    call("mgb_ffbsi_lg", ctypes.byref(s), T, n, M, _dev.ptr(x), _dev.ptr(lw), _dev.ptr(key), _dev.ptr(out),
-         _dev.ptr(idx), _dev.ptr(ws), ws.numel(), _dev.stream_ptr())
+    if nl:
+        tt = _dev.as_f32(marginal_particles.t).reshape(-1).contiguous()
+        if tt.numel() != T:
+            raise ValueError(f"marginal_particles.t has {tt.numel()} entries for {T} steps")
+        call("mgb_ffbsi_nl1d", ctypes.byref(ssm_scenario.derived()[1]), T, n, M, _dev.ptr(x), _dev.ptr(lw),
+             _dev.ptr(tt), _dev.ptr(key), _dev.ptr(out), _dev.ptr(idx), _dev.ptr(ws), ws.numel(), _dev.stream_ptr())
+    else:
+        _, s = _transition_struct(ssm_scenario)
+        call("mgb_ffbsi_lg", ctypes.byref(s), T, n, M, _dev.ptr(x), _dev.ptr(lw), _dev.ptr(key), _dev.ptr(out),
+             _dev.ptr(idx), _dev.ptr(ws), ws.numel(), _dev.stream_ptr())
     evals = torch.full((T,), float(n * M), device=dev)
     evals[0] = 0.0
     return cdict(value=out.permute(0, 2, 1), t=marginal_particles.t, num_transition_evals=evals, indices=idx)
@@ -572,14 +580,18 @@ def forward_filtering_backward_simulation(ssm_scenario, particle_filter, y, t, n
     return out
 
 
-def _pair_potential(ssm_scenario, x0, x1, lw=None):
-    """lw_i + transition_potential(x0_i -> x1_i) for particle-major (M, d) rows."""
-    _, s = _transition_struct(ssm_scenario)
+def _pair_potential(ssm_scenario, x0, x1, lw=None, t_prev=0.0):
+    """lw_i + transition_potential(x0_i at t_prev -> x1_i) for particle-major (M, d) rows."""
     x0t = _dev.as_f32(x0).t().contiguous()
     x1t = _dev.as_f32(x1).t().contiguous()
     M = x0t.shape[1]
     out = torch.empty(M, dtype=torch.float32, device=x0t.device)
     lwd = None if lw is None else _dev.as_f32(lw).reshape(-1).contiguous()
+    if isinstance(ssm_scenario, NonLinear1DBenchmark):
+        call("mgb_transition_potential_pairs_nl1d", ctypes.byref(ssm_scenario.derived()[1]), M, _dev.ptr(x0t),
+             _dev.ptr(x1t), float(t_prev), _dev.ptr(lwd), _dev.ptr(out), _dev.stream_ptr())
+        return out
+    _, s = _transition_struct(ssm_scenario)
     call("mgb_transition_potential_pairs", ctypes.byref(s), M, _dev.ptr(x0t), _dev.ptr(x1t), _dev.ptr(lwd),
          _dev.ptr(out), _dev.stream_ptr())
     return out
@@ -588,12 +600,16 @@ def _pair_potential(ssm_scenario, x0, x1, lw=None):
 def full_stitch(ssm_scenario, x0_all, t, x1_all, tplus1, x1_log_weight, random_key):
     """online_smoothing.py:33-41: for each x0_j a categorical draw over the x1_i with
     log-weights x1_log_weight - transition_potential(x0_j -> x1_i); keys split(key, len(x0))."""
-    _, s = _transition_struct(ssm_scenario)
     x0t = _dev.as_f32(x0_all).t().contiguous()
     x1t = _dev.as_f32(x1_all).t().contiguous()
     M0, M1 = x0t.shape[1], x1t.shape[1]
     lw = _dev.as_f32(x1_log_weight).reshape(-1).contiguous()
     idx = torch.empty(M0, dtype=torch.int32, device=x0t.device)
+    if isinstance(ssm_scenario, NonLinear1DBenchmark):
+        call("mgb_stitch_nl1d", ctypes.byref(ssm_scenario.derived()[1]), M0, M1, _dev.ptr(x0t), _dev.ptr(x1t),
+             _dev.ptr(lw), float(t), _dev.ptr(_dev.as_key(random_key)), _dev.ptr(idx), _dev.stream_ptr())
+        return idx
+    _, s = _transition_struct(ssm_scenario)
     call("mgb_stitch_lg", ctypes.byref(s), M0, M1, _dev.ptr(x0t), _dev.ptr(x1t), _dev.ptr(lw),
          _dev.ptr(_dev.as_key(random_key)), _dev.ptr(idx), _dev.stream_ptr())
     return idx
@@ -606,7 +622,7 @@ def fixed_lag_stitching(ssm_scenario, early_block, t, recent_block, recent_block
         raise NotImplementedError("stitching by rejection sampling is not built (maximum_rejections=0)")
     x0_fixed_all = early_block[-1]
     x0_vary_all, x1_vary_all = recent_block[0], recent_block[1]
-    nilw = _pair_potential(ssm_scenario, x0_vary_all, x1_vary_all, recent_block_log_weight)
+    nilw = _pair_potential(ssm_scenario, x0_vary_all, x1_vary_all, recent_block_log_weight, t)
     inds = full_stitch(ssm_scenario, x0_fixed_all, t, x1_vary_all, tplus1, nilw, random_key).long()
     return torch.cat([early_block, recent_block[1:, inds]], 0), len(x0_fixed_all) ** 2
 
@@ -635,7 +651,7 @@ def propagate_particle_smoother_pf(ssm_scenario, particle_filter, particles, y_n
         out = resample_particles(out, key, True, resampling)
     x_prev = out.value[-1].t().contiguous()
     y_t = _y2(y_new, ssm_scenario.dim_obs).reshape(-1)
-    x_new, lw = _step(s, n, key, y_t, x_prev, None, None, prefix)
+    x_new, lw = _step(s, n, key, y_t, x_prev, None, None, prefix, t_prev=out.t[-1])
     dev = x_new.device
     out.value = torch.cat([out.value, x_new.t()[None]], 0)
     out.y = torch.cat([out.y, y_t[None]], 0) if getattr(out, "y", None) is not None else y_t[None]

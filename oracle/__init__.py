@@ -67,7 +67,8 @@ class _NLModel(ctypes.Structure):
 
 
 class _FFBSiModel(ctypes.Structure):
-    _fields_ = [("d", ctypes.c_int), ("F", ctypes.c_void_p), ("Pq", ctypes.c_void_p), ("cq", ctypes.c_float)]
+    _fields_ = [("d", ctypes.c_int), ("F", ctypes.c_void_p), ("Pq", ctypes.c_void_p), ("cq", ctypes.c_float),
+                ("nl", ctypes.c_int), ("tsd", ctypes.c_float), ("c", ctypes.c_float)]
 
 
 def lib():
@@ -123,6 +124,10 @@ def lib():
         L.o_nl_run.argtypes = [ctypes.POINTER(_NLModel), i64, i64, u32p, f32p, f32p, ctypes.c_float, ctypes.c_int,
                                f32p, i32p, vp, vp]
         L.o_nl_run.restype = ctypes.c_double
+        L.o_ffbsi_nl1d.argtypes = [ctypes.POINTER(_NLModel), i64, i64, i64, f32p, f32p, f32p, u32p, f32p, i32p]
+        L.o_stitch_nl1d.argtypes = [ctypes.POINTER(_NLModel), i64, i64, f32p, f32p, f32p, ctypes.c_float, u32p, i32p]
+        L.o_transition_potential_pairs_nl1d.argtypes = [ctypes.POINTER(_NLModel), i64, f32p, f32p, ctypes.c_float,
+                                                        f32p]
         L.o_ffbsi_lg.argtypes = [ctypes.POINTER(_FFBSiModel), i64, i64, i64, f32p, f32p, u32p, f32p, i32p]
         L.o_stitch_lg.argtypes = [ctypes.POINTER(_FFBSiModel), i64, i64, f32p, f32p, f32p, u32p, i32p]
         L.o_transition_potential_pairs.argtypes = [ctypes.POINTER(_FFBSiModel), i64, f32p, f32p, f32p]
@@ -452,6 +457,35 @@ def nl_run(params, n, key, y, t, ess_threshold=0.5, scheme="systematic", history
     logZ = lib().o_nl_run(ctypes.byref(_nl_struct(params)), n, T, _u32(key), y, t, float(ess_threshold),
                           SCHEMES[scheme], ess, res, _ptr(xh), _ptr(lh))
     return dict(log_z=logZ, ess=ess, resampled=res.astype(bool), value=xh, log_weight=lh)
+
+
+def ffbsi_nl1d(params, x_hist, lw_hist, t, key, M):
+    """backward_simulation_full on NonLinear1DBenchmark: x_hist, lw_hist (T, N), t (T,)
+    -> (samples (T, M), indices (T, M))."""
+    x_hist, lw_hist, t = _f32(x_hist), _f32(lw_hist), _f32(t).reshape(-1)
+    T, N = lw_hist.shape
+    out = np.empty((T, M), np.float32)
+    idx = np.empty((T, M), np.int32)
+    lib().o_ffbsi_nl1d(ctypes.byref(_nl_struct(params)), T, N, M, x_hist.reshape(-1), lw_hist.reshape(-1), t,
+                       _u32(key), out.reshape(-1), idx.reshape(-1))
+    return out, idx
+
+
+def stitch_nl1d(params, x0, x1, lw1, t_prev, key):
+    """full_stitch on NonLinear1DBenchmark, x0 (M0,) at t_prev, x1 (M1,) -> indices (M0,)."""
+    x0, x1, lw1 = _f32(x0).reshape(-1), _f32(x1).reshape(-1), _f32(lw1).reshape(-1)
+    idx = np.empty(x0.size, np.int32)
+    lib().o_stitch_nl1d(ctypes.byref(_nl_struct(params)), x0.size, x1.size, x0, x1, lw1, float(np.float32(t_prev)),
+                        _u32(key), idx)
+    return idx
+
+
+def transition_potential_pairs_nl1d(params, x0, x1, t_prev):
+    x0, x1 = _f32(x0).reshape(-1), _f32(x1).reshape(-1)
+    out = np.empty(x0.size, np.float32)
+    lib().o_transition_potential_pairs_nl1d(ctypes.byref(_nl_struct(params)), x0.size, x0, x1,
+                                            float(np.float32(t_prev)), out)
+    return out
 
 
 def ffbsi_lg(F, Pq, cq, x_hist, lw_hist, key, M):

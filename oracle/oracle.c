@@ -766,12 +766,21 @@ typedef struct {
     const float *F;    /* d x d transition_matrix */
     const float *Pq;   /* d x d transition_precision_sqrt */
     float cq;          /* (d log 2pi - log transition_precision_det) / 2 */
+    int nl;            /* 1: the non-linear benchmark transition (d = 1, F and Pq unused) */
+    float tsd, c;      /* its transition_sd and log(2 pi) / 2 */
 } o_ffbsi_model;
 
-/* transition_potential(x0 -> x1) = 0.5 |(x1 - F x0) @ Pq|^2 + cq
- * (linear_gaussian.py transition_potential via gaussian_potential, utils.py:49-105) */
-static inline float o_transition_potential(const o_ffbsi_model *md, const float *x0, const float *x1)
+/* transition_potential(x0 -> x1):
+ *   linear-Gaussian  0.5 |(x1 - F x0) @ Pq|^2 + cq
+ *                    (linear_gaussian.py transition_potential via gaussian_potential, utils.py:49-105);
+ *   non-linear 1-D   0.5 ((x1 - mean(x0, t_prev)) / tsd)^2 + c, drift = 8 cos(1.2 t_prev)
+ *                    (nonlinear1d.py:48-54). */
+static inline float o_transition_potential(const o_ffbsi_model *md, const float *x0, const float *x1, float drift)
 {
+    if (md->nl) {
+        float z = (x1[0] - o_nl_mean(x0[0], drift)) / md->tsd;
+        return 0.5f * (z * z) + md->c;
+    }
     const int d = md->d;
     float diff[64];
     for (int r = 0; r < d; ++r) {
@@ -794,8 +803,8 @@ static inline float o_transition_potential(const o_ffbsi_model *md, const float 
  * for t = T-2 .. 0, sample j: keys = split(t_keys[t], M);
  *   index_j = argmax_i gumbel(keys[j], (N,))_i + lw_{t,i} - transition_potential(x_t^i -> xs_{t+1}^j)
  * (first maximum wins, NaN skipped).  x_hist (T, N, d), lw_hist (T, N); out (T, M, d), idx (T, M). */
-void o_ffbsi_lg(const o_ffbsi_model *md, int64_t T, int64_t N, int64_t M, const float *x_hist, const float *lw_hist,
-                const uint32_t *key, float *out, int32_t *idx)
+static void o_ffbsi(const o_ffbsi_model *md, int64_t T, int64_t N, int64_t M, const float *x_hist,
+                    const float *lw_hist, const float *t_all, const uint32_t *key, float *out, int32_t *idx)
 {
     const int d = md->d;
     uint32_t *tkeys = (uint32_t *)malloc(sizeof(uint32_t) * 2 * (size_t)T);
@@ -806,6 +815,7 @@ void o_ffbsi_lg(const o_ffbsi_model *md, int64_t T, int64_t N, int64_t M, const 
     uint32_t *skeys = (uint32_t *)malloc(sizeof(uint32_t) * 2 * (size_t)M);
     for (int64_t t = T - 2; t >= 0; --t) {
         o_split(tkeys + 2 * t, M, skeys);
+        const float drift = md->nl ? o_nl_drift(t_all[t]) : 0.0f;
         const float *xt = x_hist + t * N * d;
         const float *lw = lw_hist + t * N;
 #pragma omp parallel for schedule(static)
@@ -816,7 +826,7 @@ void o_ffbsi_lg(const o_ffbsi_model *md, int64_t T, int64_t N, int64_t M, const 
             int have = 0;
             for (int64_t i = 0; i < N; ++i) {
                 float g = o_bits_to_gumbel(o_bits_at(skeys[2 * j], skeys[2 * j + 1], (uint64_t)N, (uint64_t)i));
-                float v = g + (lw[i] - o_transition_potential(md, xt + i * d, x1));
+                float v = g + (lw[i] - o_transition_potential(md, xt + i * d, x1, drift));
                 if (v == v && (!have || v > best)) { best = v; bi = (int32_t)i; have = 1; }
             }
             idx[t * M + j] = bi;
@@ -827,11 +837,32 @@ void o_ffbsi_lg(const o_ffbsi_model *md, int64_t T, int64_t N, int64_t M, const 
     free(tkeys);
 }
 
+void o_ffbsi_lg(const o_ffbsi_model *md, int64_t T, int64_t N, int64_t M, const float *x_hist, const float *lw_hist,
+                const uint32_t *key, float *out, int32_t *idx)
+{
+    o_ffbsi(md, T, N, M, x_hist, lw_hist, NULL, key, out, idx);
+}
+
+static o_ffbsi_model o_nl_transition(const o_nl_model *nm)
+{
+    o_ffbsi_model md = {1, NULL, NULL, 0.0f, 1, nm->tsd, nm->c};
+    return md;
+}
+
+/* backward_simulation_full on the non-linear benchmark model: t_all[T] are the
+ * filter's times (step t's transition leaves t_all[t]); x_hist (T, N), out (T, M) */
+void o_ffbsi_nl1d(const o_nl_model *nm, int64_t T, int64_t N, int64_t M, const float *x_hist, const float *lw_hist,
+                  const float *t_all, const uint32_t *key, float *out, int32_t *idx)
+{
+    o_ffbsi_model md = o_nl_transition(nm);
+    o_ffbsi(&md, T, N, M, x_hist, lw_hist, t_all, key, out, idx);
+}
+
 /* full_stitch (online_smoothing.py:21-41): keys = split(key, M0); for each x0_j,
  * idx_j = argmax_i gumbel(keys[j], (M1,))_i + lw1_i - transition_potential(x0_j -> x1_i)
  * (first maximum wins, NaN skipped).  x0 (M0, d), x1 (M1, d) particle-major. */
-void o_stitch_lg(const o_ffbsi_model *md, int64_t M0, int64_t M1, const float *x0, const float *x1,
-                 const float *lw1, const uint32_t *key, int32_t *idx)
+static void o_stitch(const o_ffbsi_model *md, int64_t M0, int64_t M1, const float *x0, const float *x1,
+                     const float *lw1, float drift, const uint32_t *key, int32_t *idx)
 {
     const int d = md->d;
     uint32_t *skeys = (uint32_t *)malloc(sizeof(uint32_t) * 2 * (size_t)M0);
@@ -843,7 +874,7 @@ void o_stitch_lg(const o_ffbsi_model *md, int64_t M0, int64_t M1, const float *x
         int have = 0;
         for (int64_t i = 0; i < M1; ++i) {
             float g = o_bits_to_gumbel(o_bits_at(skeys[2 * j], skeys[2 * j + 1], (uint64_t)M1, (uint64_t)i));
-            float v = g + (lw1[i] - o_transition_potential(md, x0 + j * d, x1 + i * d));
+            float v = g + (lw1[i] - o_transition_potential(md, x0 + j * d, x1 + i * d, drift));
             if (v == v && (!have || v > best)) { best = v; bi = (int32_t)i; have = 1; }
         }
         idx[j] = bi;
@@ -851,10 +882,32 @@ void o_stitch_lg(const o_ffbsi_model *md, int64_t M0, int64_t M1, const float *x
     free(skeys);
 }
 
+void o_stitch_lg(const o_ffbsi_model *md, int64_t M0, int64_t M1, const float *x0, const float *x1,
+                 const float *lw1, const uint32_t *key, int32_t *idx)
+{
+    o_stitch(md, M0, M1, x0, x1, lw1, 0.0f, key, idx);
+}
+
+/* full_stitch on the non-linear benchmark model, x0 at time t_prev */
+void o_stitch_nl1d(const o_nl_model *nm, int64_t M0, int64_t M1, const float *x0, const float *x1,
+                   const float *lw1, float t_prev, const uint32_t *key, int32_t *idx)
+{
+    o_ffbsi_model md = o_nl_transition(nm);
+    o_stitch(&md, M0, M1, x0, x1, lw1, o_nl_drift(t_prev), key, idx);
+}
+
 /* transition_potential(x0_i -> x1_i) for each i (vmap over pairs) */
 void o_transition_potential_pairs(const o_ffbsi_model *md, int64_t M, const float *x0, const float *x1, float *out)
 {
-    for (int64_t i = 0; i < M; ++i) out[i] = o_transition_potential(md, x0 + i * md->d, x1 + i * md->d);
+    for (int64_t i = 0; i < M; ++i) out[i] = o_transition_potential(md, x0 + i * md->d, x1 + i * md->d, 0.0f);
+}
+
+void o_transition_potential_pairs_nl1d(const o_nl_model *nm, int64_t M, const float *x0, const float *x1,
+                                       float t_prev, float *out)
+{
+    o_ffbsi_model md = o_nl_transition(nm);
+    const float drift = o_nl_drift(t_prev);
+    for (int64_t i = 0; i < M; ++i) out[i] = o_transition_potential(&md, x0 + i, x1 + i, drift);
 }
 
 int o_num_threads(void)

@@ -128,3 +128,94 @@ def test_bootstrap_brackets_truth(cuda):
     x = sim.x[:, 0]
     assert bool((x < pf.value.max(dim=1).values[:, 0]).all())
     assert bool((pf.value.min(dim=1).values[:, 0] < x).all())
+
+
+# ------------------------------------------------ backward simulation, stitching
+
+def test_ffbsi_bit_exact(cuda):
+    """backward_simulation (maximum_rejections = 0) on the non-linear model: samples and
+    indices equal the oracle's; times are non-integer so every step's drift differs"""
+    mg, ssm, p, _, _, _ = _setup(5, T=12)
+    T, n, M = 12, 700, 333
+    t = (np.arange(T) * 0.61 + 0.2).astype(np.float32)
+    y = (np.random.default_rng(5).standard_normal(T) * 3 + 3).astype(np.float32)
+    pf = mg.ssm.run_particle_filter_for_marginals(ssm, mg.ssm.BootstrapFilter(), y, t, O.PRNGKey(6), n=n)
+    key = O.PRNGKey(12)
+    bs = mg.ssm.backward_simulation(ssm, pf, key, M)
+    xs, idx = O.ffbsi_nl1d(p, pf.value[..., 0].cpu().numpy(), pf.log_weight.cpu().numpy(), t, key, M)
+    assert np.array_equal(bs.indices.cpu().numpy(), idx)
+    assert np.array_equal(bs.value[..., 0].cpu().numpy(), xs)
+    assert bs.value.shape == (T, M, 1)
+
+
+def test_stitch_and_pairs_bit_exact(cuda):
+    mg, ssm, p, _, _, _ = _setup(6)
+    rng = np.random.default_rng(6)
+    M0, M1 = 90, 301
+    x0 = (rng.standard_normal((M0, 1)) * 5).astype(np.float32)
+    x1 = (rng.standard_normal((M1, 1)) * 5).astype(np.float32)
+    lw = rng.standard_normal(M1).astype(np.float32)
+    key = O.PRNGKey(13)
+    for tp in (0.0, 3.0, 41.7):
+        idx = mg.ssm.full_stitch(ssm, torch.from_numpy(x0).cuda(), tp, torch.from_numpy(x1).cuda(), tp + 1.0,
+                                 torch.from_numpy(lw).cuda(), key)
+        assert np.array_equal(idx.cpu().numpy(), O.stitch_nl1d(p, x0, x1, lw, tp, key))
+        pp = mg.ssm._pair_potential(ssm, torch.from_numpy(x1[:M0]).cuda(), torch.from_numpy(x1[M1 - M0:]).cuda(),
+                                    None, tp)
+        assert np.array_equal(pp.cpu().numpy(), O.transition_potential_pairs_nl1d(p, x1[:M0], x1[M1 - M0:], tp))
+
+
+def test_smoother_pf_variant_matches_oracle(cuda):
+    """propagate_particle_smoother(backward_sim=False), lag 3, against an oracle-driven
+    restatement (propagate from t_previous, systematic resampling, stitching at t)"""
+    mg, ssm, p, t, y, _ = _setup(7, T=12)
+    T, lag, n = 12, 3, 500
+    keys = O.split(O.PRNGKey(8), T)
+    bf = mg.ssm.BootstrapFilter()
+    parts = mg.ssm.initiate_particles(ssm, bf, n, keys[0], y[0], t=float(t[0]))
+    for s in range(1, T):
+        parts = mg.ssm.propagate_particle_smoother(ssm, bf, parts, y[s], float(t[s]), keys[s], lag,
+                                                   backward_sim=False)
+    x0, lw = O.nl_init(p, n, keys[0], y[0])
+    value = [x0]
+    for s in range(1, T):
+        key = keys[s]
+        if O.lse_ess(lw)[3] < n - 1e-3:
+            anc = O.resample_systematic(lw, O.systematic_u_bits(key))[0]
+            value = [v[anc] for v in value]
+        x_new, lw = O.nl_propagate(p, key, y[s], t[s - 1], value[-1])
+        value.append(x_new)
+        s1 = len(value) - lag - 1
+        if s1 >= 0:
+            nilw = lw + O.transition_potential_pairs_nl1d(p, value[s1], value[s1 + 1], t[s1])
+            idx = O.stitch_nl1d(p, value[s1], value[s1 + 1], nilw, t[s1], key)
+            value = value[:s1 + 1] + [v[idx] for v in value[s1 + 1:]]
+            lw = np.zeros(n, np.float32)
+    assert np.array_equal(parts.value[..., 0].cpu().numpy(), np.stack(value))
+
+
+def test_backward_and_smoothers_bracket_truth(cuda):
+    """the reference's checks (tests/test_ssm.py _test_ffbsi_full, online smoothing):
+    backward samples and fixed-lag smoothed particles bracket the simulated states"""
+    import mocat_gb300 as mg
+    ssm = mg.ssm.NonLinear1DBenchmark()
+    t = np.arange(20, dtype=np.float32)
+    sim = ssm.simulate(t, mg.random.PRNGKey(0))
+    x = sim.x[:, 0]
+    pf = mg.ssm.run_particle_filter_for_marginals(ssm, mg.ssm.BootstrapFilter(), sim.y, t, mg.random.PRNGKey(0),
+                                                  n=10000)
+    bs = mg.ssm.backward_simulation(ssm, pf, mg.random.PRNGKey(0), 2000)
+    assert not hasattr(bs, "log_weight")
+    assert bool((x < bs.value.max(dim=1).values[:, 0]).all())
+    assert bool((bs.value.min(dim=1).values[:, 0] < x).all())
+    for backward_sim in (False, True):
+        bf = mg.ssm.BootstrapFilter()
+        parts = mg.ssm.initiate_particles(ssm, bf, 2000, mg.random.PRNGKey(1), sim.y[0], t=0.0)
+        for s in range(1, 20):
+            parts = mg.ssm.propagate_particle_smoother(ssm, bf, parts, sim.y[s], float(t[s]),
+                                                       mg.random.split(mg.random.PRNGKey(2), 20)[s], 5,
+                                                       backward_sim=backward_sim)
+        assert parts.value.shape == (20, 2000, 1)
+        assert bool(torch.isfinite(parts.value).all())
+        assert bool((x < parts.value.max(dim=1).values[:, 0]).all())
+        assert bool((parts.value.min(dim=1).values[:, 0] < x).all())

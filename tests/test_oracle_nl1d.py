@@ -104,3 +104,25 @@ def test_drift_matches_facade_formula():
     got = np.array([O.nl_drift(v) for v in t], np.float32)
     assert np.array_equal(got, NonLinear1DBenchmark.drift(t))
     assert np.array_equal(got, np.array([_drift(v) for v in t], np.float32))
+
+
+def test_oracle_backward_pieces_match_numpy():
+    """the oracle's non-linear transition potential and stitch follow the numpy arithmetic
+    (Gumbel-max over split(key, M0)[j], first maximum)"""
+    rng = np.random.default_rng(2)
+    x0 = (rng.standard_normal(50) * 4).astype(np.float32)
+    x1 = (rng.standard_normal(50) * 4).astype(np.float32)
+    tp = 2.5
+    want = []
+    for a, b in zip(x0, x1):
+        z = (b - _mean(a, _drift(tp))) / PARAMS["tsd"]
+        want.append(F(0.5) * (z * z) + PARAMS["c"])
+    assert np.array_equal(O.transition_potential_pairs_nl1d(PARAMS, x0, x1, tp), np.array(want, np.float32))
+    lw1 = rng.standard_normal(50).astype(np.float32)
+    key = O.PRNGKey(3)
+    idx = O.stitch_nl1d(PARAMS, x0[:7], x1, lw1, tp, key)
+    for j, k in enumerate(O.split(key, 7)):
+        gum = O.gumbel(k, (50,))
+        pot = O.transition_potential_pairs_nl1d(PARAMS, np.full(50, x0[j], np.float32), x1, tp)
+        v = gum + (lw1 - pot)
+        assert idx[j] == int(np.argmax(v))
