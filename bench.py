@@ -33,6 +33,10 @@ smc_logreg -- the tempered SMC sampler on Bayesian logistic regression
 potential+gradient evaluations per second over timed SMC iterations, and the
 tcgen05 potential kernel's tensor roofline next to the fp32 kernel.
 
+nl1d -- the bootstrap filter on the one-dimensional non-linear benchmark
+model at N = 2^20, T = 1000 (graph replay), its fused step kernel alone, and
+the oracle's C/OpenMP filter on a sample of steps.
+
 batched_sv -- a second workload in the same line: 4096 independent
 stochastic-volatility filters of uneven length and size in one persistent
 launch (graph replay; e2e with the observations copied from pinned host
@@ -442,6 +446,105 @@ def bench_config1(args, rank):
             "barriers per step)", "log_z": float(logz.item())}
 
 
+def bench_nl1d(args, flush, rank):
+    """Bootstrap filter on the one-dimensional non-linear benchmark model (initial_sd = sqrt 2,
+    transition_sd = sqrt 10, likelihood_sd = 1), N = 2^20, T = 1000, ESS-triggered systematic
+    resampling at 0.5 N: whole runs replayed from a CUDA graph (two fused kernels per step plus
+    the resampling kernels), the step kernel alone, and the oracle's C/OpenMP filter on a
+    sample of steps."""
+    import torch
+    import mocat_gb300 as mg
+    import oracle
+    from mocat_gb300 import _dev, _lib
+    n, T = 1 << 20, 1000
+    ssm = mg.ssm.NonLinear1DBenchmark()
+    p, s = ssm.derived()
+    t_all = np.arange(T, dtype=np.float32)
+    sim = ssm.simulate(t_all, mg.random.PRNGKey(0))
+    dev = sim.y.device
+    yd = sim.y.reshape(-1).contiguous()
+    td = torch.from_numpy(t_all).to(dev)
+    kd = mg.random.PRNGKey(1 + rank)
+    ws = _dev.workspace(_lib.lib().mgb_pf_nl1d_workspace(n, T, 0), dev)
+    logz = torch.empty(1, dtype=torch.float64, device=dev)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    xf = torch.empty(n, device=dev)
+    out = _lib.PFOutputs(logz.data_ptr(), None, None, None, None, xf.data_ptr(), None, err.data_ptr(), None)
+
+    def enqueue():
+        _lib.call("mgb_pf_nl1d_run", ctypes.byref(s), n, T, _dev.ptr(kd), _dev.ptr(yd), _dev.ptr(td), 0.5, 0,
+                  _dev.ptr(ws), ws.numel(), ctypes.byref(out), _dev.stream_ptr())
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        enqueue()
+    torch.cuda.current_stream().wait_stream(side)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        enqueue()
+    for _ in range(max(3, args.warmup)):
+        g.replay()
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(max(2, args.steps // 2)):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        g.replay()
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1) / 1e3)
+    t_run = statistics.median(ts)
+    # the fused step kernel alone, gathering through sorted ancestors (rotating buffers > L2)
+    nbuf = 8
+    xs = [torch.randn(n, device=dev) * 5 for _ in range(nbuf)]
+    xo = [torch.empty(n, device=dev) for _ in range(nbuf)]
+    lo = [torch.empty(n, device=dev) for _ in range(nbuf)]
+    anc = mg.resample(torch.randn(n, device=dev), mg.random.PRNGKey(7), "systematic")
+    kt = mg.random.split(mg.random.PRNGKey(9), 1)[0].contiguous()
+    y0 = yd[1:2].contiguous()
+
+    def step(i):
+        _lib.call("mgb_pf_nl1d_propagate", ctypes.byref(s), n, _dev.ptr(kt), _dev.ptr(y0), 3.0,
+                  _dev.ptr(xs[i % nbuf]), _dev.ptr(anc), None, _dev.ptr(xo[i % nbuf]), _dev.ptr(lo[i % nbuf]),
+                  _dev.stream_ptr())
+    for i in range(3):
+        step(i)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for i in range(args.kernel_iters):
+        step(i)
+    e1.record()
+    torch.cuda.synchronize()
+    k_t = e0.elapsed_time(e1) / 1e3 / args.kernel_iters
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    k_alg = n * 16  # x[a_i] read, a_i read, x and lw written
+    res = {"workload": "bootstrap particle filter, NonLinear1DBenchmark (initial_sd=sqrt2, transition_sd=sqrt10, "
+                       "likelihood_sd=1), N=2^20, T=1000, t=0..999, ESS-triggered systematic resampling at 0.5N, "
+                       "observations simulated from seed 0",
+           "metric": "particle-steps/s", "value": n * T / t_run, "unit": "particle-steps/s",
+           "ms_per_run": t_run * 1e3, "log_z": float(logz.item()),
+           "step_kernel": {"kernel": "k_nl_step<false> alone (resampled step)", "launch_us": k_t * 1e6,
+                           "alg_bytes": k_alg, "achieved_gbs": k_alg / k_t / 1e9,
+                           "frac_of_measured_hbm": k_alg / k_t / 1e9 / peak}}
+    if rank == 0:
+        yh = sim.y.reshape(-1).cpu().numpy()[:args.cpu_steps + 1]
+        t0 = time.perf_counter()
+        oracle.nl_run(p, n, np.array([0, 1], np.uint32), yh, t_all[:yh.size])
+        dt = time.perf_counter() - t0
+        res["cpu_baseline"] = {"value": n * yh.size / dt, "unit": "particle-steps/s",
+                               "cores": oracle.num_threads(), "kind": "port",
+                               "sample": f"N={n}, {yh.size} steps ({dt:.1f} s), oracle C/OpenMP"}
+    return res
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
@@ -478,6 +581,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-smc", action="store_true")
+    ap.add_argument("--no-nl1d", action="store_true")
     ap.add_argument("--smc-B", type=int, default=16)
     ap.add_argument("--smc-iters", type=int, default=3)
     ap.add_argument("--adj-n", type=int, default=65536)
@@ -655,6 +759,8 @@ def main():
         line["adjoint"] = bench_adjoint(args, flush, rank)
     if not args.no_smc:
         line["smc_logreg"] = bench_smc(args, flush, rank)
+    if not args.no_nl1d:
+        line["nl1d"] = bench_nl1d(args, flush, rank)
     if rank == 0:
         v_cpu, cores, dt = cpu_baseline(n, args.cpu_steps)
         line["cpu_baseline"] = {"value": v_cpu, "unit": "particle-steps/s", "cores": cores, "kind": "port",

@@ -195,8 +195,9 @@ def test_smoother_pf_variant_matches_oracle(cuda):
 
 
 def test_backward_and_smoothers_bracket_truth(cuda):
-    """the reference's checks (tests/test_ssm.py _test_ffbsi_full, online smoothing):
-    backward samples and fixed-lag smoothed particles bracket the simulated states"""
+    """the reference's checks (tests/test_ssm.py _test_ffbsi_full, _test_online_smoothing_*_full):
+    backward samples bracket every simulated state; for the fixed-lag smoothers (lag 3,
+    keys split(PRNGKey(0), 20)) the truth lies outside the particle range at under 10% of times"""
     import mocat_gb300 as mg
     ssm = mg.ssm.NonLinear1DBenchmark()
     t = np.arange(20, dtype=np.float32)
@@ -208,14 +209,14 @@ def test_backward_and_smoothers_bracket_truth(cuda):
     assert not hasattr(bs, "log_weight")
     assert bool((x < bs.value.max(dim=1).values[:, 0]).all())
     assert bool((bs.value.min(dim=1).values[:, 0] < x).all())
+    rkeys = mg.random.split(mg.random.PRNGKey(0), 20)
     for backward_sim in (False, True):
         bf = mg.ssm.BootstrapFilter()
-        parts = mg.ssm.initiate_particles(ssm, bf, 2000, mg.random.PRNGKey(1), sim.y[0], t=0.0)
+        parts = mg.ssm.initiate_particles(ssm, bf, 2000, rkeys[0], sim.y[0], t=float(t[0]))
         for s in range(1, 20):
-            parts = mg.ssm.propagate_particle_smoother(ssm, bf, parts, sim.y[s], float(t[s]),
-                                                       mg.random.split(mg.random.PRNGKey(2), 20)[s], 5,
+            parts = mg.ssm.propagate_particle_smoother(ssm, bf, parts, sim.y[s], float(t[s]), rkeys[s], 3,
                                                        backward_sim=backward_sim)
         assert parts.value.shape == (20, 2000, 1)
         assert bool(torch.isfinite(parts.value).all())
-        assert bool((x < parts.value.max(dim=1).values[:, 0]).all())
-        assert bool((parts.value.min(dim=1).values[:, 0] < x).all())
+        assert float((x > parts.value.max(dim=1).values[:, 0]).float().mean()) < 0.1
+        assert float((x < parts.value.min(dim=1).values[:, 0]).float().mean()) < 0.1
