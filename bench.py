@@ -16,6 +16,9 @@ Metric: particle-steps/s (higher is better).
                read + write, log-weight write + read, ancestor write + read).
                The propagate kernel is also timed alone (rotating buffers larger
                than L2; 8 d + 8 bytes per particle).
+  --profile-run / --phase-trace (with --profile-model lg|nl1d, --n, --T): one
+               run for an ncu capture of a small case, or the whole-filter
+               kernel's per-phase times; no bench line.
   cpu_baseline -- the oracle's C/OpenMP restatement of the same filter on the
                host cores, on a bounded sample (N = 2^20, a few steps).
 
@@ -545,6 +548,70 @@ def bench_nl1d(args, flush, rank):
     return res
 
 
+def _profile_model(name):
+    """(scenario, d, C-ABI run prefix) of the model a profiling mode runs"""
+    import mocat_gb300 as mg
+    if name == "nl1d":
+        return mg.ssm.NonLinear1DBenchmark(), 1, "mgb_pf_nl1d"
+    return mg.ssm.TimeHomogenousLinearGaussian(**model_arrays()), D, "mgb_pf_lg"
+
+
+def profile_main(args):
+    """Profiling modes (no JSON bench line).
+    --profile-run: one filter run of --profile-model at (--n, --T) through the public call, for
+      an ncu capture of the whole-filter kernel (k_pf_persist) on a small case.
+    --phase-trace: the whole-filter kernel's per-phase times from block 0's globaltimer stamps
+      (mgb_pf_outputs.trace), medians over the steady steps, with ESS threshold 0.5 (resampling
+      steps) and 0 (no resampling)."""
+    import torch
+    import mocat_gb300 as mg
+    from mocat_gb300 import _dev, _lib
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    ssm, d, prefix = _profile_model(args.profile_model)
+    n, T = args.n, args.T
+    t_all = np.arange(T, dtype=np.float32)
+    y = ssm.simulate(t_all, mg.random.PRNGKey(0)).y.contiguous()
+    if args.profile_run:
+        o = mg.ssm.run_particle_filter_for_marginals(ssm, mg.ssm.BootstrapFilter(), y, t_all, mg.random.PRNGKey(1),
+                                                     n=n, history=False)
+        print(json.dumps({"model": args.profile_model, "n": n, "T": T, "log_z": float(o.log_z),
+                          "resampled_steps": int(o.resampled.sum())}))
+        return
+    _, s = ssm.derived()
+    td = torch.from_numpy(t_all).to(dev)
+    for thr in (0.5, 0.0):
+        if prefix == "mgb_pf_nl1d":
+            ws = _dev.workspace(_lib.lib().mgb_pf_nl1d_workspace(n, T, 0), dev)
+        else:
+            ws = _dev.workspace(_lib.lib().mgb_pf_lg_workspace(n, T, d, 0), dev)
+        key = mg.random.PRNGKey(1)
+        logz = torch.empty(1, dtype=torch.float64, device=dev)
+        err = torch.zeros(1, dtype=torch.int32, device=dev)
+        tr = torch.zeros(T * 10 + 4096, dtype=torch.int64, device=dev)
+        out = _lib.PFOutputs(logz.data_ptr(), None, None, None, None, None, None, err.data_ptr(), tr.data_ptr())
+        for _ in range(2):
+            tr.zero_()
+            if prefix == "mgb_pf_nl1d":
+                _lib.call(prefix + "_run", ctypes.byref(s), n, T, _dev.ptr(key), _dev.ptr(y), _dev.ptr(td), thr, 0,
+                          _dev.ptr(ws), ws.numel(), ctypes.byref(out), _dev.stream_ptr())
+            else:
+                _lib.call(prefix + "_run", ctypes.byref(s), n, T, _dev.ptr(key), _dev.ptr(y), thr, 0, _dev.ptr(ws),
+                          ws.numel(), ctypes.byref(out), _dev.stream_ptr())
+            torch.cuda.synchronize()
+        st = tr.cpu().numpy().astype(np.float64)[:T * 10].reshape(T, 10)[1:-1]
+
+        def med(a, b):
+            return float(np.median(st[:, b] - st[:, a]) / 1e3)
+        res = {"model": args.profile_model, "n": n, "T": T, "ess_threshold": thr, "us_propagate": med(0, 1),
+               "us_barrier1": med(1, 2), "us_combine": med(2, 3)}
+        if thr > 0:
+            res.update({"us_tile_sums": med(3, 4), "us_barrier2": med(4, 5), "us_fill_setup": med(5, 6),
+                        "us_fill_units": med(6, 7), "us_barrier3": med(7, 8)})
+        res["us_step"] = float(np.median(np.diff(st[:, 0])) / 1e3)
+        print(json.dumps(res))
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
@@ -582,11 +649,17 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-smc", action="store_true")
     ap.add_argument("--no-nl1d", action="store_true")
+    ap.add_argument("--profile-run", action="store_true")
+    ap.add_argument("--phase-trace", action="store_true")
+    ap.add_argument("--profile-model", default="lg", choices=["lg", "nl1d"])
     ap.add_argument("--smc-B", type=int, default=16)
     ap.add_argument("--smc-iters", type=int, default=3)
     ap.add_argument("--adj-n", type=int, default=65536)
     ap.add_argument("--adj-T", type=int, default=1000)
     args = ap.parse_args()
+    if args.profile_run or args.phase_trace:
+        profile_main(args)
+        return
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -740,7 +813,7 @@ def main():
                        "log_z": log_z},
             "e2e": {"value": e2e_val, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "roofline": {"bound": "hbm", "kernel": "k_pf_lg_persist<10,10> (whole filter, one launch per run)",
+            "roofline": {"bound": "hbm", "kernel": "k_pf_persist<LGModelP<10,10>> (whole filter, one launch per run)",
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "alg_bytes_per_launch": alg_run, "launch_us": run_s * 1e6,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback",
@@ -750,7 +823,7 @@ def main():
                          "propagate_kernel": {"kernel": "k_lg_step2<10,10> alone", "launch_us": k_t * 1e6,
                                               "alg_bytes": k_alg, "achieved": k_alg / k_t / 1e9,
                                               "frac": k_alg / k_t / 1e9 / peak}},
-            "gpu_launches": args.steps * 3,  # k_setup_keys, k_pf_lg_persist, k_or_err per run
+            "gpu_launches": args.steps * 3,  # k_setup_keys, k_pf_persist, k_or_err per run
             "clocks": clk.summary()}
     line["config1"] = bench_config1(args, rank)
     if not args.no_batched:

@@ -33,4 +33,55 @@ __device__ __forceinline__ float nl_lik_potential(float x, float y, float lsd, f
   return nl_gauss(__fsub_rn(y, __fdiv_rn(__fmul_rn(x, x), 20.0f)), lsd, c);
 }
 
+struct NLP {
+  float s0, tsd, lsd, c;
+  uint32_t one;  // == 1, multiplier of the cipher's multiply-adds
+};
+
+inline NLP pack_nl(const mgb_nl1d_model *m) {
+  NLP p;
+  p.s0 = m->initial_sd;
+  p.tsd = m->transition_sd;
+  p.lsd = m->likelihood_sd;
+  p.c = m->c;
+  p.one = 1u;
+  return p;
+}
+
+__device__ __forceinline__ float nl_potential(const NLP &p, float x, float y) {
+  return nl_lik_potential(x, y, p.lsd, p.c);
+}
+
+// normal(key, (1,)) for the particle key (ka, kb)
+__device__ __forceinline__ float nl_normal(uint32_t ka, uint32_t kb, uint32_t one) {
+  uint32_t b[1];
+  bits_vec<1>(ka, kb, b, one);
+  return bits_to_normal(b[0]);
+}
+
+// the model as a particle policy of the persistent whole-filter kernel; aux is
+// the step's drift 8 cos(1.2 t_prev)
+struct NLModelP {
+  static constexpr int kD = 1, kDY = 1;
+  NLP p;
+  __device__ __forceinline__ uint32_t one() const { return p.one; }
+  __device__ __forceinline__ float init(int64_t, uint32_t ka, uint32_t kb, int64_t i, const float *y,
+                                        float *__restrict__ x, float *__restrict__ lw) const {
+    const float xv = __fmul_rn(nl_normal(ka, kb, p.one), p.s0);
+    x[i] = xv;
+    const float l = -nl_potential(p, xv, y[0]);
+    lw[i] = l;
+    return l;
+  }
+  __device__ __forceinline__ float step(int64_t, uint32_t ka, uint32_t kb, int64_t i, const float (&xs)[1],
+                                        float lres, const float *y, float aux, float *__restrict__ x,
+                                        float *__restrict__ lw) const {
+    const float xn = __fadd_rn(nl_mean(xs[0], aux), __fmul_rn(nl_normal(ka, kb, p.one), p.tsd));
+    x[i] = xn;
+    const float l = __fsub_rn(lres, nl_potential(p, xn, y[0]));
+    lw[i] = l;
+    return l;
+  }
+};
+
 }  // namespace mgb

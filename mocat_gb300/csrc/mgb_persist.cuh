@@ -1,6 +1,9 @@
-// Whole-filter persistent kernel: arguments shared with the driver.
+// Whole-filter persistent kernel: arguments and workspace shared with the
+// drivers of the models that run on it.
 #pragma once
 #include "mgb_internal.cuh"
+#include "mgb_resample.cuh"
+#include "mgb_pf_common.cuh"
 
 namespace mgb {
 
@@ -36,8 +39,93 @@ struct PersistArgs {
   int *user_err;                  // caller's error word (may be null): err is OR-ed into it
   unsigned long long magic;       // floor((2^64 - 1) / n)
   uint64_t *trace;                // (T, 8) phase timestamps from block 0, or null
+  const float *aux;               // (T,) per-step constant of the model (may be null)
 };
 
+// Persistent path: systematic resampling, even n, n <= 2^21 (tile prefixes in smem).
+inline bool persistent_ok(int64_t n, int scheme) {
+  return scheme == MGB_RESAMPLE_SYSTEMATIC && n % 2 == 0 && (n + SCAN_TILE - 1) / SCAN_TILE <= PP_MAX_TILES;
+}
+
+struct PersistWs {
+  LsePartial *parts;
+  int *chunk_ctr;
+  uint64_t *cloc;
+  uint64_t *tile_sum;
+  int *degen;
+  GridBar *bar;
+  int32_t *res;
+  int *err;
+};
+
+inline PersistWs carve_persist(Carver &c, int64_t n, int64_t T) {
+  PersistWs w;
+  w.parts = c.take<LsePartial>(2 * PP_MAX_CHUNKS);
+  w.chunk_ctr = c.take<int>((size_t)T);
+  w.cloc = c.take<uint64_t>((size_t)n);
+  w.tile_sum = c.take<uint64_t>((size_t)((n + SCAN_TILE - 1) / SCAN_TILE));
+  w.degen = c.take<int>((size_t)T);
+  w.bar = c.take<GridBar>(1);
+  w.res = c.take<int32_t>((size_t)T);
+  w.err = c.take<int>(1);
+  return w;
+}
+
+// zeroes the per-run state and fills the arguments every model shares; x_hist /
+// lw_hist are used when the caller asked for histories
+inline int persist_setup(const RunWs &w, const PersistWs &pw, int64_t n, int64_t T, const float *y, float thr,
+                         float *ess, const mgb_pf_outputs *out, PersistArgs &a, cudaStream_t s) {
+  if (cudaMemsetAsync(pw.degen, 0, sizeof(int) * T, s) != cudaSuccess) return ERR_CUDA;
+  if (cudaMemsetAsync(pw.bar, 0, sizeof(GridBar), s) != cudaSuccess) return ERR_CUDA;
+  if (cudaMemsetAsync(pw.err, 0, sizeof(int), s) != cudaSuccess) return ERR_CUDA;
+  if (cudaMemsetAsync(pw.chunk_ctr, 0, sizeof(int) * T, s) != cudaSuccess) return ERR_CUDA;
+  const bool hx = out && out->x_hist, hl = out && out->lw_hist;
+  a.n = n;
+  a.T = T;
+  a.keys = w.keys;
+  a.y = y;
+  a.thr_n = thr * (float)n;
+  a.logn = log((double)n);
+  a.xa = w.xa;
+  a.xb = w.xb;
+  a.la = w.la;
+  a.lb = w.lb;
+  a.x_hist = hx ? out->x_hist : nullptr;
+  a.lw_hist = hl ? out->lw_hist : nullptr;
+  a.anc = w.anc;
+  a.parts = pw.parts;
+  a.chunk_ctr = pw.chunk_ctr;
+  a.cloc = pw.cloc;
+  a.tile_sum = pw.tile_sum;
+  a.degen = pw.degen;
+  a.bar = pw.bar;
+  a.ess = ess;
+  a.res = (out && out->resampled) ? out->resampled : pw.res;
+  a.logz = out ? out->log_z : nullptr;
+  a.err = pw.err;
+  a.user_err = out ? out->err : nullptr;
+  a.magic = ~0ull / (unsigned long long)n;
+  a.trace = out ? out->trace : nullptr;
+  a.aux = nullptr;
+  return OK;
+}
+
+// copies the last step's particles / log-weights to x_final / lw_final when asked
+inline int persist_finish(const PersistArgs &a, int d, const mgb_pf_outputs *out, cudaStream_t s) {
+  const int64_t n = a.n, T = a.T;
+  const float *xl = a.x_hist ? a.x_hist + (size_t)(T - 1) * d * n : ((T - 1) & 1 ? a.xb : a.xa);
+  const float *ll = a.lw_hist ? a.lw_hist + (size_t)(T - 1) * n : ((T - 1) & 1 ? a.lb : a.la);
+  if (out && out->x_final &&
+      cudaMemcpyAsync(out->x_final, xl, sizeof(float) * d * n, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+    return ERR_CUDA;
+  if (out && out->lw_final &&
+      cudaMemcpyAsync(out->lw_final, ll, sizeof(float) * n, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+    return ERR_CUDA;
+  return OK;
+}
+
 int run_lg_persistent(const mgb_lg_model *m, const PersistArgs &a, cudaStream_t s);
+// the one-dimensional non-linear benchmark model; a.aux = 8 cos(1.2 t_{t-1}) per step
+int run_nl_persistent(const mgb_nl1d_model *m, const PersistArgs &a, cudaStream_t s);
 
 }  // namespace mgb

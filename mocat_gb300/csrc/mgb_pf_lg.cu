@@ -73,34 +73,6 @@ int launch_finish(const PFState *st, const int32_t *res_hist, int64_t T, double 
   return launch_status();
 }
 
-// Persistent path: systematic resampling, even n, n <= 2^21 (tile prefixes in smem).
-static bool persistent_ok(int64_t n, int scheme) {
-  return scheme == MGB_RESAMPLE_SYSTEMATIC && n % 2 == 0 && (n + SCAN_TILE - 1) / SCAN_TILE <= PP_MAX_TILES;
-}
-
-struct PersistWs {
-  LsePartial *parts;
-  int *chunk_ctr;
-  uint64_t *cloc;
-  uint64_t *tile_sum;
-  int *degen;
-  GridBar *bar;
-  int32_t *res;
-  int *err;
-};
-static PersistWs carve_persist(Carver &c, int64_t n, int64_t T) {
-  PersistWs w;
-  w.parts = c.take<LsePartial>(2 * PP_MAX_CHUNKS);
-  w.chunk_ctr = c.take<int>((size_t)T);
-  w.cloc = c.take<uint64_t>((size_t)n);
-  w.tile_sum = c.take<uint64_t>((size_t)((n + SCAN_TILE - 1) / SCAN_TILE));
-  w.degen = c.take<int>((size_t)T);
-  w.bar = c.take<GridBar>(1);
-  w.res = c.take<int32_t>((size_t)T);
-  w.err = c.take<int>(1);
-  return w;
-}
-
 template <int D, int DY>
 static int run_lg(const mgb_lg_model *m, int64_t n, int64_t T, const uint32_t *key, const float *y, float thr,
                   int scheme, bool persistent, void *ws, size_t ws_bytes, const mgb_pf_outputs *out,
@@ -121,46 +93,10 @@ static int run_lg(const mgb_lg_model *m, int64_t n, int64_t T, const uint32_t *k
   k_setup_keys<<<grid_for(T, 256), 256, 0, s>>>(key, T, w.keys);
 
   if (persistent && persistent_ok(n, scheme)) {
-    if (cudaMemsetAsync(pw.degen, 0, sizeof(int) * T, s) != cudaSuccess) return ERR_CUDA;
-    if (cudaMemsetAsync(pw.bar, 0, sizeof(GridBar), s) != cudaSuccess) return ERR_CUDA;
-    if (cudaMemsetAsync(pw.err, 0, sizeof(int), s) != cudaSuccess) return ERR_CUDA;
-    if (cudaMemsetAsync(pw.chunk_ctr, 0, sizeof(int) * T, s) != cudaSuccess) return ERR_CUDA;
     PersistArgs a;
-    a.n = n;
-    a.T = T;
-    a.keys = w.keys;
-    a.y = y;
-    a.thr_n = thr * (float)n;
-    a.logn = log((double)n);
-    a.xa = w.xa;
-    a.xb = w.xb;
-    a.la = w.la;
-    a.lb = w.lb;
-    a.x_hist = hx ? out->x_hist : nullptr;
-    a.lw_hist = hl ? out->lw_hist : nullptr;
-    a.anc = w.anc;
-    a.parts = pw.parts;
-    a.chunk_ctr = pw.chunk_ctr;
-    a.cloc = pw.cloc;
-    a.tile_sum = pw.tile_sum;
-    a.degen = pw.degen;
-    a.bar = pw.bar;
-    a.ess = ess;
-    a.res = (out && out->resampled) ? out->resampled : pw.res;
-    a.logz = out ? out->log_z : nullptr;
-    a.err = pw.err;
-    a.user_err = err;
-    a.magic = ~0ull / (unsigned long long)n;
-    a.trace = out ? out->trace : nullptr;
+    if ((st = persist_setup(w, pw, n, T, y, thr, ess, out, a, s))) return st;
     if ((st = run_lg_persistent(m, a, s))) return st;
-    const float *xl = hx ? out->x_hist + (size_t)(T - 1) * D * n : ((T - 1) & 1 ? w.xb : w.xa);
-    const float *ll = hl ? out->lw_hist + (size_t)(T - 1) * n : ((T - 1) & 1 ? w.lb : w.la);
-    if (out && out->x_final &&
-        cudaMemcpyAsync(out->x_final, xl, sizeof(float) * D * n, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
-      return ERR_CUDA;
-    if (out && out->lw_final &&
-        cudaMemcpyAsync(out->lw_final, ll, sizeof(float) * n, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
-      return ERR_CUDA;
+    if ((st = persist_finish(a, D, out, s))) return st;
     return launch_status();
   }
 

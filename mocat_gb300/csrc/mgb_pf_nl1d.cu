@@ -15,9 +15,15 @@
 // each rounded to float32 (IEEE division, no contraction), so every particle and
 // log-weight equals the oracle's.
 //
-// 8 cos(1.2 t) is a per-step constant: thread 0 of each block computes it once
-// as 8 * float(cos(double(1.2f * t))), the float32 product the reference forms,
-// a double-precision cosine rounded to float32, and an exact scaling by 8.
+// 8 cos(1.2 t) is a per-step constant, 8 * float(cos(double(1.2f * t))): the
+// float32 product the reference forms, a double-precision cosine rounded to
+// float32, and an exact scaling by 8.  A whole run computes it for every step
+// once (k_nl_drifts); a single propagate call computes it in thread 0 of each block.
+//
+// A run with systematic resampling and even n <= 2^21 is one persistent
+// cooperative launch (k_pf_persist<NLModelP>, the same kernel as the
+// linear-Gaussian filter's); otherwise each step launches the resampling
+// kernels and the fused step kernel.
 //
 // Layout: particles (n) float32, log-weights (n) float32, ancestors (n) int32.
 // One step reads x_prev[a_i] (4 B), the previous log-weight when the step did
@@ -27,24 +33,9 @@
 #include "mgb_kernels.cuh"
 #include "mgb_pf_common.cuh"
 #include "mgb_nl1d.cuh"
+#include "mgb_persist.cuh"
 
 namespace mgb {
-
-struct NLP {
-  float s0, tsd, lsd, c;
-  uint32_t one;  // == 1, multiplier of the cipher's multiply-adds
-};
-
-__device__ __forceinline__ float nl_potential(const NLP &p, float x, float y) {
-  return nl_lik_potential(x, y, p.lsd, p.c);
-}
-
-// normal(key, (1,)) for the particle key (ka, kb)
-__device__ __forceinline__ float nl_normal(uint32_t ka, uint32_t kb, uint32_t one) {
-  uint32_t b[1];
-  bits_vec<1>(ka, kb, b, one);
-  return bits_to_normal(b[0]);
-}
 
 __device__ __forceinline__ float nl_particle(const NLP &p, int64_t i, float e, bool res,
                                              const float *__restrict__ x_prev, const int32_t *anc, const float *lws,
@@ -78,19 +69,26 @@ __global__ void __launch_bounds__(PF_TPB) k_nl_init(const NLP p, int64_t n, cons
   if (FUSED) pf_reduce_online<PF_TPB>(m, a1, a2, nanf, ctl, 0);
 }
 
+// aux[t] = 8 cos(1.2 t_all[t - 1]), the drift of step t (aux[0] = 0)
+__global__ void k_nl_drifts(const float *t_all, int64_t T, float *aux) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < T; t += (int64_t)gridDim.x * blockDim.x)
+    aux[t] = t == 0 ? 0.0f : nl_drift(t_all[t - 1]);
+}
+
 // One bootstrap step.  Even n: a thread takes particles i and i + n/2, whose
-// keys are the two halves of the same two cipher calls.  tp (nullable) points
-// at t_previous, else t_prev is used; res_flag (nullable) decides resampled vs
-// identity at run time (run mode: lw_res = 0 after a resample, filtering.py:292).
+// keys are the two halves of the same two cipher calls.  dp (nullable) points
+// at the step's precomputed drift, else it is computed from t_prev; res_flag
+// (nullable) decides resampled vs identity at run time (run mode: lw_res = 0
+// after a resample, filtering.py:292).
 template <bool FUSED>
 __global__ void __launch_bounds__(PF_TPB) k_nl_step(const NLP p, int64_t n, const uint32_t *key, const float *y_t,
-                                                     const float *tp, float t_prev, const float *__restrict__ x_prev,
+                                                     const float *dp, float t_prev, const float *__restrict__ x_prev,
                                                      const int32_t *anc, const float *lw_prev,
                                                      const int32_t *res_flag, float *__restrict__ x_new,
                                                      float *__restrict__ lw_new, PFCtl ctl, int64_t t) {
   __shared__ float sh[2];
   if (threadIdx.x == 0) {
-    sh[0] = nl_drift(tp ? *tp : t_prev);
+    sh[0] = dp ? *dp : nl_drift(t_prev);
     sh[1] = *y_t;
   }
   __syncthreads();
@@ -125,23 +123,26 @@ inline unsigned nl_grid(int64_t n) {
   return (unsigned)((work + PF_TPB - 1) / PF_TPB);
 }
 
-inline NLP pack_nl(const mgb_nl1d_model *m) {
-  NLP p;
-  p.s0 = m->initial_sd;
-  p.tsd = m->transition_sd;
-  p.lsd = m->likelihood_sd;
-  p.c = m->c;
-  p.one = 1u;
-  return p;
+static void carve_nl(Carver &c, int64_t n, int64_t T, int scheme, bool need_x, bool need_lw, bool need_ess,
+                     RunWs *w, PersistWs *pw, float **aux) {
+  RunWs rw = carve_run(c, n, T, 1, scheme, need_x, need_lw, need_ess);
+  PersistWs p = carve_persist(c, n, T);
+  float *a = c.take<float>((size_t)T);
+  if (w) *w = rw;
+  if (pw) *pw = p;
+  if (aux) *aux = a;
 }
 
 static int run_nl(const mgb_nl1d_model *m, int64_t n, int64_t T, const uint32_t *key, const float *y,
-                  const float *t_all, float thr, int scheme, void *ws, size_t ws_bytes, const mgb_pf_outputs *out,
-                  cudaStream_t s) {
+                  const float *t_all, float thr, int scheme, bool persistent, void *ws, size_t ws_bytes,
+                  const mgb_pf_outputs *out, cudaStream_t s) {
   const NLP p = pack_nl(m);
   const bool hx = out && out->x_hist, hl = out && out->lw_hist;
   Carver c(ws);
-  RunWs w = carve_run(c, n, T, 1, scheme, !hx, !hl, !(out && out->ess));
+  RunWs w;
+  PersistWs pw;
+  float *aux;
+  carve_nl(c, n, T, scheme, !hx, !hl, !(out && out->ess), &w, &pw, &aux);
   if (c.bytes() > ws_bytes) return ERR_WORKSPACE;
   float *ess = (out && out->ess) ? out->ess : w.ess_hist;
   int *err = out ? out->err : nullptr;
@@ -151,6 +152,18 @@ static int run_nl(const mgb_nl1d_model *m, int64_t n, int64_t T, const uint32_t 
   int st = reset_resample(w.rws, s);
   if (st) return st;
   if ((st = launch_setup_keys(key, T, w.keys, s))) return st;
+  k_nl_drifts<<<grid_for(T, 256), 256, 0, s>>>(t_all, T, aux);
+  if ((st = launch_status())) return st;
+
+  if (persistent && persistent_ok(n, scheme)) {
+    PersistArgs a;
+    if ((st = persist_setup(w, pw, n, T, y, thr, ess, out, a, s))) return st;
+    a.aux = aux;
+    if ((st = run_nl_persistent(m, a, s))) return st;
+    if ((st = persist_finish(a, 1, out, s))) return st;
+    return launch_status();
+  }
+
   PFCtl ctl;
   ctl.parts = w.parts;
   ctl.counter = w.counter;
@@ -173,7 +186,7 @@ static int run_nl(const mgb_nl1d_model *m, int64_t n, int64_t T, const uint32_t 
     st = launch_resample(lbuf(t - 1), n, scheme, &w.st->M, w.keys + 2 * t, 0, 0u, w.res_hist + t, w.rws, w.anc,
                          err, s);
     if (st) return st;
-    k_nl_step<true><<<grid, PF_TPB, 0, s>>>(p, n, w.keys + 2 * t, y + t, t_all + (t - 1), 0.0f, xbuf(t - 1), w.anc,
+    k_nl_step<true><<<grid, PF_TPB, 0, s>>>(p, n, w.keys + 2 * t, y + t, aux + t, 0.0f, xbuf(t - 1), w.anc,
                                             lbuf(t - 1), w.res_hist + t, xbuf(t), lbuf(t), ctl, t);
     if ((st = launch_status())) return st;
   }
@@ -218,7 +231,7 @@ int mgb_pf_nl1d_propagate(const mgb_nl1d_model *m, int64_t n, const uint32_t *ke
 size_t mgb_pf_nl1d_workspace(int64_t n, int64_t T, int scheme) {
   if (n < 1 || T < 1) return 0;
   Carver c(nullptr);
-  carve_run(c, n, T, 1, scheme & 0xff, true, true, true);
+  carve_nl(c, n, T, scheme & 0xff, true, true, true, nullptr, nullptr, nullptr);
   return c.bytes();
 }
 
@@ -226,11 +239,13 @@ int mgb_pf_nl1d_run(const mgb_nl1d_model *m, int64_t n, int64_t T, const uint32_
                     const float *t, float ess_threshold, int scheme, void *ws, size_t ws_bytes,
                     const mgb_pf_outputs *out, void *stream) {
   if (!nl_model_ok(m) || n < 1 || n > 0x7FFFFFFFll || T < 1 || !key || !y || !t || !ws) return ERR_BAD_ARG;
+  const bool persistent = !(scheme & MGB_RUN_LAUNCH_PER_STEP);
+  scheme &= ~MGB_RUN_LAUNCH_PER_STEP;
   if (scheme != MGB_RESAMPLE_SYSTEMATIC && scheme != MGB_RESAMPLE_MULTINOMIAL && scheme != MGB_RESAMPLE_CATEGORICAL)
     return ERR_UNSUPPORTED;
   if (scheme == MGB_RESAMPLE_CATEGORICAL && n > 46340) return ERR_UNSUPPORTED;
   if (ws_bytes < mgb_pf_nl1d_workspace(n, T, scheme)) return ERR_WORKSPACE;
-  return run_nl(m, n, T, key, y, t, ess_threshold, scheme, ws, ws_bytes, out, (cudaStream_t)stream);
+  return run_nl(m, n, T, key, y, t, ess_threshold, scheme, persistent, ws, ws_bytes, out, (cudaStream_t)stream);
 }
 
 }  // extern "C"

@@ -1,6 +1,10 @@
-// Whole-filter persistent kernel: the bootstrap linear-Gaussian particle
-// filter with ESS-triggered systematic resampling, all T steps in one
-// cooperative launch (one CTA group resident on every SM).
+// Whole-filter persistent kernel: a bootstrap particle filter with
+// ESS-triggered systematic resampling, all T steps in one cooperative launch
+// (one CTA group resident on every SM).  The model enters as a particle policy
+// (the GPU counterpart of the reference's StateSpaceModel plugin): kD, kDY,
+// init() for the initial draw and weight, step() for one propagate + weight
+// from a source state and a carried log-weight; LGModelP (linear-Gaussian) and
+// NLModelP (one-dimensional non-linear benchmark) are the two compiled here.
 //
 // Per step the grid runs
 //   P1  propagate + weight, two particles per thread (i, i + n/2), grid-stride;
@@ -27,6 +31,7 @@
 #include "mgb_kernels.cuh"
 #include "mgb_lg.cuh"
 #include "mgb_persist.cuh"
+#include "mgb_nl1d.cuh"
 
 namespace mgb {
 
@@ -146,9 +151,27 @@ __device__ __forceinline__ LseOut combine_chunks(const LsePartial *parts, int np
   return o;
 }
 
+// the linear-Gaussian model as a particle policy
 template <int D, int DY>
-__global__ void __launch_bounds__(PP_TPB, 2) k_pf_lg_persist(const __grid_constant__ LGP<D, DY> p,
-                                                              const __grid_constant__ PersistArgs a) {
+struct LGModelP {
+  static constexpr int kD = D, kDY = DY;
+  LGP<D, DY> p;
+  __device__ __forceinline__ uint32_t one() const { return p.one; }
+  __device__ __forceinline__ float init(int64_t n, uint32_t ka, uint32_t kb, int64_t i, const float *y,
+                                        float *__restrict__ x, float *__restrict__ lw) const {
+    return lg_init_particle<D, DY>(p, n, ka, kb, i, y, x, lw);
+  }
+  __device__ __forceinline__ float step(int64_t n, uint32_t ka, uint32_t kb, int64_t i, const float (&xs)[D],
+                                        float lres, const float *y, float, float *__restrict__ x,
+                                        float *__restrict__ lw) const {
+    return lg_particle_regs<D, DY>(p, n, ka, kb, i, xs, lres, y, x, lw);
+  }
+};
+
+template <class MP>
+__global__ void __launch_bounds__(PP_TPB, 2) k_pf_persist(const __grid_constant__ MP p,
+                                                           const __grid_constant__ PersistArgs a) {
+  constexpr int D = MP::kD, DY = MP::kDY;
   __shared__ float smf[PP_TPB / 32];
   __shared__ unsigned long long smu[PP_TPB / 32];
   __shared__ uint64_t sP[PP_MAX_TILES + 1];
@@ -175,6 +198,7 @@ __global__ void __launch_bounds__(PP_TPB, 2) k_pf_lg_persist(const __grid_consta
     const float *xi = t == 0 ? nullptr : (a.x_hist ? a.x_hist + (size_t)(t - 1) * D * n : ((t & 1) ? a.xa : a.xb));
     const float *li = t == 0 ? nullptr : (a.lw_hist ? a.lw_hist + (size_t)(t - 1) * n : ((t & 1) ? a.la : a.lb));
     const uint32_t k0 = __ldg(&a.keys[2 * t]), k1 = __ldg(&a.keys[2 * t + 1]);
+    const float aux = a.aux ? __ldg(&a.aux[t]) : 0.0f;
     // observation of the step in shared memory (broadcast reads; keeps DY
     // registers free in the particle loop)
     if (threadIdx.x < DY) y_s[threadIdx.x] = __ldg(&a.y[t * DY + threadIdx.x]);
@@ -195,11 +219,11 @@ __global__ void __launch_bounds__(PP_TPB, 2) k_pf_lg_persist(const __grid_consta
       int nanf = 0;
       if (i < h && t == 0) {
         uint32_t r0, r1, q0, q1;
-        threefry2x32_m(k0, k1, (uint32_t)(2 * i), (uint32_t)(2 * i + n), p.one, r0, r1);
-        threefry2x32_m(k0, k1, (uint32_t)(2 * i + 1), (uint32_t)(2 * i + 1 + n), p.one, q0, q1);
+        threefry2x32_m(k0, k1, (uint32_t)(2 * i), (uint32_t)(2 * i + n), p.one(), r0, r1);
+        threefry2x32_m(k0, k1, (uint32_t)(2 * i + 1), (uint32_t)(2 * i + 1 + n), p.one(), q0, q1);
 #pragma unroll 1
         for (int s = 0; s < 2; ++s) {
-          const float l = lg_init_particle<D, DY>(p, n, s ? r1 : r0, s ? q1 : q0, s ? i + h : i, y, xo, lo);
+          const float l = p.init(n, s ? r1 : r0, s ? q1 : q0, s ? i + h : i, y, xo, lo);
           online_acc(l, m, s1, s2, nanf);
         }
       } else if (i < h) {
@@ -216,8 +240,8 @@ __global__ void __launch_bounds__(PP_TPB, 2) k_pf_lg_persist(const __grid_consta
         const float la_ = res_cur ? 0.0f : __ldcg(&li[i]);
         const float lb_ = res_cur ? 0.0f : __ldcg(&li[i + h]);
         uint32_t r0, r1, q0, q1;
-        threefry2x32_m(k0, k1, (uint32_t)(2 * i), (uint32_t)(2 * i + n), p.one, r0, r1);
-        threefry2x32_m(k0, k1, (uint32_t)(2 * i + 1), (uint32_t)(2 * i + 1 + n), p.one, q0, q1);
+        threefry2x32_m(k0, k1, (uint32_t)(2 * i), (uint32_t)(2 * i + n), p.one(), r0, r1);
+        threefry2x32_m(k0, k1, (uint32_t)(2 * i + 1), (uint32_t)(2 * i + 1 + n), p.one(), q0, q1);
         // the pair runs as a two-trip loop (not unrolled): one copy of the
         // particle code keeps the hot loop inside the instruction cache
 #pragma unroll 1
@@ -225,8 +249,7 @@ __global__ void __launch_bounds__(PP_TPB, 2) k_pf_lg_persist(const __grid_consta
           float xs[D];
 #pragma unroll
           for (int j = 0; j < D; ++j) xs[j] = s ? xb_[j] : xa_[j];
-          const float l = lg_particle_regs<D, DY>(p, n, s ? r1 : r0, s ? q1 : q0, s ? i + h : i, xs,
-                                                  s ? lb_ : la_, y, xo, lo);
+          const float l = p.step(n, s ? r1 : r0, s ? q1 : q0, s ? i + h : i, xs, s ? lb_ : la_, y, aux, xo, lo);
           online_acc(l, m, s1, s2, nanf);
         }
       }
@@ -379,31 +402,31 @@ __global__ void k_or_err(const int *src, int *dst) {
 }
 
 // host: occupancy-sized cooperative launch
-template <int D, int DY>
-int launch_persist(const mgb_lg_model *m, const PersistArgs &args, cudaStream_t s) {
-  const LGP<D, DY> p = pack_lg<D, DY>(m);
+template <class MP>
+static int launch_persist(const MP &p, const PersistArgs &args, cudaStream_t s) {
   int dev = 0, sms = 0, per_sm = 0, coop = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return ERR_CUDA;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return ERR_CUDA;
   if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop) return ERR_UNSUPPORTED;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pf_lg_persist<D, DY>, PP_TPB, 0) != cudaSuccess ||
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pf_persist<MP>, PP_TPB, 0) != cudaSuccess ||
       per_sm < 1)
     return ERR_UNSUPPORTED;
+  MP pc = p;
   PersistArgs a = args;
-  void *kargs[] = {(void *)&p, (void *)&a};
+  void *kargs[] = {(void *)&pc, (void *)&a};
   // no more blocks than there are 256-pair propagate chunks: a small filter's grid
   // barriers then span a few blocks instead of every co-resident one
   const int64_t chunks = (args.n / 2 + PP_TPB - 1) / PP_TPB;
   const int64_t cap = (int64_t)sms * per_sm;
   const dim3 grid((unsigned)(chunks < cap ? (chunks > 0 ? chunks : 1) : cap)), block(PP_TPB);
-  if (cudaLaunchCooperativeKernel((void *)k_pf_lg_persist<D, DY>, grid, block, kargs, 0, s) != cudaSuccess)
+  if (cudaLaunchCooperativeKernel((void *)k_pf_persist<MP>, grid, block, kargs, 0, s) != cudaSuccess)
     return ERR_LAUNCH;
   k_or_err<<<1, 1, 0, s>>>(args.err, args.user_err);
   return launch_status();
 }
 
 #define MGB_PERSIST_CASE(D_, DY_) \
-  if (m->d == D_ && m->dy == DY_) return launch_persist<D_, DY_>(m, a, s);
+  if (m->d == D_ && m->dy == DY_) return launch_persist(LGModelP<D_, DY_>{pack_lg<D_, DY_>(m)}, a, s);
 
 int run_lg_persistent(const mgb_lg_model *m, const PersistArgs &a, cudaStream_t s) {
   MGB_PERSIST_CASE(1, 1)
@@ -420,6 +443,10 @@ int run_lg_persistent(const mgb_lg_model *m, const PersistArgs &a, cudaStream_t 
   MGB_PERSIST_CASE(8, 8)
   MGB_PERSIST_CASE(10, 10)
   return ERR_UNSUPPORTED;
+}
+
+int run_nl_persistent(const mgb_nl1d_model *m, const PersistArgs &a, cudaStream_t s) {
+  return launch_persist(NLModelP{pack_nl(m)}, a, s);
 }
 
 }  // namespace mgb

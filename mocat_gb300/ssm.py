@@ -433,7 +433,8 @@ def run_particle_filter_for_marginals(ssm_scenario, particle_filter, y, t, rando
     Returns cdict(value (T, n, d), log_weight (T, n), ess (T,), t, y, log_z, resampled)
     (value/log_weight only the final step, shape (1, n, d) / (1, n), when history=False).
     persistent=False forces one kernel launch per phase and step instead of the
-    single persistent launch (systematic resampling, even n <= 2^21); results
+    single persistent launch (bootstrap filter on the linear-Gaussian or the
+    non-linear benchmark model, systematic resampling, even n <= 2^21); results
     are the same.
     """
     _check_lg(ssm_scenario, particle_filter)
@@ -466,7 +467,8 @@ def run_particle_filter_for_marginals(ssm_scenario, particle_filter, y, t, rando
                          None if history else lh.data_ptr(), err.data_ptr(), None)
     if nl:
         call("mgb_pf_nl1d_run", ctypes.byref(s), n, T, _dev.ptr(key), _dev.ptr(y2), _dev.ptr(t32),
-             float(ess_threshold), sc, _dev.ptr(ws), ws.numel(), ctypes.byref(out), _dev.stream_ptr())
+             float(ess_threshold), sc | (0 if persistent else RUN_LAUNCH_PER_STEP), _dev.ptr(ws), ws.numel(),
+             ctypes.byref(out), _dev.stream_ptr())
     else:
         flags = 0 if (persistent or prefix != "mgb_pf_lg") else RUN_LAUNCH_PER_STEP
         call(prefix + "_run", ctypes.byref(s), n, T, _dev.ptr(key), _dev.ptr(y2), float(ess_threshold), sc | flags,

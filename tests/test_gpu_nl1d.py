@@ -220,3 +220,22 @@ def test_backward_and_smoothers_bracket_truth(cuda):
         assert bool(torch.isfinite(parts.value).all())
         assert float((x > parts.value.max(dim=1).values[:, 0]).float().mean()) < 0.1
         assert float((x < parts.value.min(dim=1).values[:, 0]).float().mean()) < 0.1
+
+
+@pytest.mark.parametrize("thr", [0.5, 2.0, 0.0])
+def test_persistent_equals_launch_per_step(cuda, thr):
+    """the persistent whole-filter kernel (k_pf_persist<NLModelP>) and the launch-per-step
+    path give identical particles, log-weights and decisions; both equal the oracle"""
+    mg, ssm, p, t, y, _ = _setup(8, T=25)
+    n = 1 << 16
+    key = O.PRNGKey(21)
+    a = mg.ssm.run_particle_filter_for_marginals(ssm, mg.ssm.BootstrapFilter(), y, t, key, n=n, ess_threshold=thr)
+    b = mg.ssm.run_particle_filter_for_marginals(ssm, mg.ssm.BootstrapFilter(), y, t, key, n=n, ess_threshold=thr,
+                                                 persistent=False)
+    ref = O.nl_run(p, n, key, y, t, ess_threshold=thr, scheme="systematic", history=True)
+    for o in (a, b):
+        assert np.array_equal(o.resampled.cpu().numpy(), ref["resampled"])
+        assert np.array_equal(o.value[..., 0].cpu().numpy(), ref["value"])
+        assert np.array_equal(o.log_weight.cpu().numpy(), ref["log_weight"])
+        np.testing.assert_allclose(float(o.log_z), ref["log_z"], rtol=1e-6)
+    np.testing.assert_allclose(a.ess.cpu().numpy(), b.ess.cpu().numpy(), rtol=1e-5)
