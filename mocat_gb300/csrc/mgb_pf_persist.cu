@@ -151,6 +151,41 @@ __device__ __forceinline__ LseOut combine_chunks(const LsePartial *parts, int np
   return o;
 }
 
+// log-weights lw[i0 .. i0 + SCAN_IPT) through L2 (written by other blocks this
+// step); -inf past n
+__device__ __forceinline__ void load_tile_lw(const float *lw, int64_t i0, int64_t n, float (&v)[SCAN_IPT]) {
+  static_assert(SCAN_IPT == 8, "two float4 loads per thread");
+  if (i0 + SCAN_IPT <= n && (((uintptr_t)(lw + i0)) & 15) == 0) {
+    const float4 a = __ldcg((const float4 *)(lw + i0));
+    const float4 b = __ldcg((const float4 *)(lw + i0) + 1);
+    v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w, v[4] = b.x, v[5] = b.y, v[6] = b.z, v[7] = b.w;
+  } else {
+#pragma unroll
+    for (int j = 0; j < SCAN_IPT; ++j) v[j] = i0 + j < n ? __ldcg(&lw[i0 + j]) : -INFINITY;
+  }
+}
+
+// tile of the u-th unit of a numbering whose per-tile prefix is sU (the largest
+// tile b with sU[b] <= u), its particle count and its within-tile prefixes
+// (thread's elements threadIdx.x + j PP_TPB) into v
+__device__ __forceinline__ void unit_load(int u, int ntiles, int64_t n, const int32_t *sU, const uint64_t *cloc,
+                                          int &tile, int &cnt_valid, uint64_t (&v)[SCAN_IPT]) {
+  int lo_b = 0, hi_b = ntiles;
+  while (hi_b - lo_b > 1) {
+    const int mid = (lo_b + hi_b) >> 1;
+    if (sU[mid] <= u) lo_b = mid;
+    else hi_b = mid;
+  }
+  tile = lo_b;
+  const int64_t base = (int64_t)tile * SCAN_TILE;
+  cnt_valid = (int)(n - base < SCAN_TILE ? n - base : SCAN_TILE);
+#pragma unroll
+  for (int j = 0; j < SCAN_IPT; ++j) {
+    const int jj = threadIdx.x + j * PP_TPB;
+    v[j] = jj < cnt_valid ? __ldcg(&cloc[base + jj]) : 0ull;
+  }
+}
+
 // the linear-Gaussian model as a particle policy
 template <int D, int DY>
 struct LGModelP {
@@ -277,17 +312,22 @@ __global__ void __launch_bounds__(PP_TPB, 2) k_pf_persist(const __grid_constant_
     if (res_next) {
       const float M = o.M;
       // ---- P3: per tile, exact fixed-point weights, their within-tile
-      // inclusive prefixes (stored) and the tile sum
+      // inclusive prefixes (stored) and the tile sum.  The next tile's
+      // log-weights are requested before this tile's scan, so a block with two
+      // tiles waits for one L2 round trip instead of two.
+      float v[SCAN_IPT];
+      if ((int)blockIdx.x < ntiles) load_tile_lw(lo, (int64_t)blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_IPT, n, v);
       for (int tile = blockIdx.x; tile < ntiles; tile += G) {
         const int64_t i0 = (int64_t)tile * SCAN_TILE + (int64_t)threadIdx.x * SCAN_IPT;
+        float w[SCAN_IPT];
+        if (tile + (int)G < ntiles) load_tile_lw(lo, i0 + (int64_t)G * SCAN_TILE, n, w);
         uint64_t q[SCAN_IPT];
         int bad = !(M > -INFINITY && M < INFINITY);
         uint64_t tsum = 0;
 #pragma unroll
         for (int j = 0; j < SCAN_IPT; ++j) {
-          const float v = i0 + j < n ? __ldcg(&lo[i0 + j]) : -INFINITY;
-          bad |= (v != v) || (v == INFINITY);
-          q[j] = quantise_weight(v, M, scale);
+          bad |= (v[j] != v[j]) || (v[j] == INFINITY);
+          q[j] = quantise_weight(v[j], M, scale);
           tsum += q[j];
         }
         unsigned long long btot;
@@ -311,6 +351,8 @@ __global__ void __launch_bounds__(PP_TPB, 2) k_pf_persist(const __grid_constant_
           a.tile_sum[tile] = btot;
           if (bad) atomicOr(&a.degen[t], 1);
         }
+#pragma unroll
+        for (int j = 0; j < SCAN_IPT; ++j) v[j] = w[j];
       }
       stamp(a, t, 4);
       grid_sync(a.bar, G, a.err);
@@ -356,37 +398,36 @@ __global__ void __launch_bounds__(PP_TPB, 2) k_pf_persist(const __grid_constant_
         if (threadIdx.x == 0) sU[ntiles] = (int32_t)utot;
         __syncthreads();
         stamp(a, t, 6);
-        const ResampleCtl c = sc;
         if (a.trace && blockIdx.x == 0 && threadIdx.x == 0) a.trace[t * 10 + 9] = utot;
-        for (int u = blockIdx.x; u < (int)utot; u += G) {
-          int lo_b = 0, hi_b = ntiles;  // largest tile b with sU[b] <= u
-          while (hi_b - lo_b > 1) {
-            const int mid = (lo_b + hi_b) >> 1;
-            if (sU[mid] <= u) lo_b = mid;
-            else hi_b = mid;
-          }
-          const int tile = lo_b;
+        const ResampleCtl c = sc;
+        // units run round robin, one after another per block; the next unit's
+        // prefixes are requested into registers while the current one merges
+        // from shared memory
+        int u = blockIdx.x;
+        int tile = 0, cnt_valid = 0;
+        uint64_t cv[SCAN_IPT];
+        if (u < (int)utot) unit_load(u, ntiles, n, sU, a.cloc, tile, cnt_valid, cv);
+        int done = 0;
+        while (u < (int)utot) {
           const int64_t kb = sK[tile] + (int64_t)(u - sU[tile]) * SCAN_TILE;
           const int64_t ke = kb + SCAN_TILE < (int64_t)sK[tile + 1] ? kb + SCAN_TILE : (int64_t)sK[tile + 1];
           const int64_t base = (int64_t)tile * SCAN_TILE;
-          const int cnt_valid = (int)(n - base < SCAN_TILE ? n - base : SCAN_TILE);
           const uint64_t P = sP[tile];
-          {
-            uint64_t v[SCAN_IPT];
 #pragma unroll
-            for (int j = 0; j < SCAN_IPT; ++j) {
-              const int jj = threadIdx.x + j * PP_TPB;
-              v[j] = jj < cnt_valid ? __ldcg(&a.cloc[base + jj]) : 0ull;
-            }
-#pragma unroll
-            for (int j = 0; j < SCAN_IPT; ++j) {
-              const int jj = threadIdx.x + j * PP_TPB;
-              if (jj < cnt_valid) sC[jj] = P + v[j];
-            }
+          for (int j = 0; j < SCAN_IPT; ++j) {
+            const int jj = threadIdx.x + j * PP_TPB;
+            if (jj < cnt_valid) sC[jj] = P + cv[j];
           }
           __syncthreads();
-          merge_fill(sC, cnt_valid, c, kb, (int)(ke - kb), base, n, a.anc);
+          const int cnt = cnt_valid;
+          const int un = u + (int)G;
+          if (un < (int)utot) unit_load(un, ntiles, n, sU, a.cloc, tile, cnt_valid, cv);
+          merge_fill(sC, cnt, c, kb, (int)(ke - kb), base, n, a.anc);
           __syncthreads();
+          if (a.trace && t == 1 && blockIdx.x == 0 && threadIdx.x == 0 && done < 1024)
+            a.trace[a.T * 10 + 1024 + done] = globaltimer_ns() - a.trace[t * 10 + 6];
+          ++done;
+          u = un;
         }
       }
       stamp(a, t, 7);
