@@ -16,9 +16,10 @@ Metric: particle-steps/s (higher is better).
                read + write, log-weight write + read, ancestor write + read).
                The propagate kernel is also timed alone (rotating buffers larger
                than L2; 8 d + 8 bytes per particle).
-  --profile-run / --phase-trace (with --profile-model lg|nl1d, --n, --T): one
-               run for an ncu capture of a small case, or the whole-filter
-               kernel's per-phase times; no bench line.
+  --profile-run / --phase-trace (with --profile-model, --n, --T): one run of
+               a small case for an ncu capture (models lg, nl1d, adjoint, lgstep,
+               logreg, svbatch), or the whole-filter kernel's per-phase times (lg,
+               nl1d); no bench line.
   cpu_baseline -- the oracle's C/OpenMP restatement of the same filter on the
                host cores, on a bounded sample (N = 2^20, a few steps).
 
@@ -568,6 +569,8 @@ def profile_main(args):
     from mocat_gb300 import _dev, _lib
     torch.cuda.set_device(0)
     dev = torch.device("cuda", 0)
+    if args.profile_model in ("adjoint", "lgstep", "logreg", "svbatch"):
+        return profile_other(args)
     ssm, d, prefix = _profile_model(args.profile_model)
     n, T = args.n, args.T
     t_all = np.arange(T, dtype=np.float32)
@@ -620,6 +623,65 @@ def profile_main(args):
         print(json.dumps(res))
 
 
+def profile_other(args):
+    """--profile-run for the other kernels' captures (one call of the public API each):
+      adjoint  mocat_gb300.adjoint.log_z_and_grad on the headline model, n = --n, T = --T;
+      lgstep   the headline filter on the launch-per-step path (k_lg_step2 per step), n = --n, T = --T;
+      logreg   LogisticRegression.likelihood_potential_and_grad, 1e5 x 50 seeded data, P = --n
+               parameter rows, --profile-precision bf16 | fp32 (three timed calls);
+      svbatch  BatchedFilters over synthetic_sv_batch(--n series, seed 0, T in [50, --T]), launch
+               shape (512, 16)."""
+    import torch
+    import mocat_gb300 as mg
+    m, n, T = args.profile_model, args.n, args.T
+    out = {"model": m, "n": n, "T": T}
+    if m in ("adjoint", "lgstep"):
+        ssm = mg.ssm.TimeHomogenousLinearGaussian(**model_arrays())
+        y = ssm.simulate(np.arange(T), mg.random.PRNGKey(0)).y.contiguous()
+        if m == "adjoint":
+            o = mg.adjoint.log_z_and_grad(ssm, y, mg.random.PRNGKey(1), n, ckpt_every=32)
+        else:
+            o = mg.ssm.run_particle_filter_for_marginals(ssm, mg.ssm.BootstrapFilter(), y, np.arange(T),
+                                                         mg.random.PRNGKey(1), n=n, history=False, persistent=False)
+        out["log_z"] = float(o.log_z)
+    elif m == "logreg":
+        d, n_data = 50, 100000
+        rng = np.random.default_rng(0)
+        X = rng.standard_normal((n_data, d)).astype(np.float32)
+        y = (rng.random(n_data) < 1 / (1 + np.exp(-X @ rng.standard_normal(d)))).astype(np.float32)
+        sc = mg.smc.LogisticRegression(X, y)
+        beta = torch.from_numpy((rng.standard_normal((n, d)) * 0.1).astype(np.float32)).cuda()
+        sc.likelihood_potential_and_grad(beta, precision=args.profile_precision)
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            sc.likelihood_potential_and_grad(beta, precision=args.profile_precision)
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1) / 1e3)
+        t = min(ts)
+        out.update(precision=args.profile_precision, n_data=n_data, d=d, ms=t * 1e3,
+                   tflops_alg=4.0 * n_data * d * n / t / 1e12)
+    else:
+        ns, y, Tb, keys = mg.batched.synthetic_sv_batch(n, seed=0, t_range=(50, T))
+        sc = mg.ssm.StochasticVolatility(dim=1, initial_covariance=0.3 ** 2 / (1 - 0.95 ** 2),
+                                         transition_matrix=0.95, transition_covariance=0.09,
+                                         likelihood_covariance_diag=1.0)
+        bf = mg.batched.BatchedFilters(sc, mg.ssm.BootstrapFilter(), ns, y, keys, lengths=Tb, launch=(512, 16))
+        bf.run()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        bf.enqueue()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        out.update(particle_steps=int(bf.particle_steps), ms=ms, g_per_s=bf.particle_steps / ms / 1e6)
+    print(json.dumps(out))
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
@@ -659,7 +721,9 @@ def main():
     ap.add_argument("--no-nl1d", action="store_true")
     ap.add_argument("--profile-run", action="store_true")
     ap.add_argument("--phase-trace", action="store_true")
-    ap.add_argument("--profile-model", default="lg", choices=["lg", "nl1d"])
+    ap.add_argument("--profile-model", default="lg",
+                    choices=["lg", "nl1d", "adjoint", "lgstep", "logreg", "svbatch"])
+    ap.add_argument("--profile-precision", default="bf16", choices=["bf16", "fp32"])
     ap.add_argument("--smc-B", type=int, default=16)
     ap.add_argument("--smc-iters", type=int, default=3)
     ap.add_argument("--adj-n", type=int, default=65536)
@@ -805,7 +869,7 @@ def main():
     k_alg = n * (8 * D + 8)
     traffic = None
     issue = None
-    prof = os.path.join(ROOT, "profiles", "k_pf_lg_persist_d10_n1M.md")
+    prof = os.path.join(ROOT, "profiles", "k_pf_persist_lg_d10_n1M.md")
     if os.path.exists(prof):
         for ln in open(prof):
             if ln.startswith("dram_bytes_per_launch_T1000:"):
