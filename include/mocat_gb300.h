@@ -432,6 +432,73 @@ int mgb_smc_logreg_prior_scale_grad(const mgb_smc_logreg_config *cfg, void *ws_d
 int mgb_smc_logreg_step(const mgb_smc_logreg_config *cfg, const float *X_dev, const float *y_dev,
                         const void *Xbf16_dev, int64_t n_data, void *ws_dev, size_t ws_bytes, void *stream);
 
+/* ------------------------------------------------ ABC-SMC (likelihood-free)
+ * MetropolisedABCSMCSampler (mocat/src/abc/smc.py:101-245) with RandomWalkABC moves and the
+ * Metropolis correction (mocat/src/abc/mcmc.py:59-103, mocat/src/mcmc/metropolis.py:48-70),
+ * driven as mocat.run (mocat/src/sample.py:110-148), on the ABC LinearGaussian scenario
+ * (mocat/src/abc/scenarios/linear_gaussian.py): prior N(m0, C0 C0^T), simulated data
+ * H x + L eps, distance |sim - data|_2 (mocat/src/abc/abc.py:36-39).  B posteriors with keys
+ * (B, 2), N particles each.
+ *   weights 0 / -inf (distance <= threshold), ESS = exp(log #alive);
+ *   thresholds: schedule[iter] (index clamped) or jnp.quantile(distances,
+ *     ess_threshold_retain ess / N) with linear interpolation;
+ *   resampling when ess < ess_threshold_resample N: systematic (the reference: random.categorical);
+ *   moves: mcmc_steps random-walk proposals x + sqrt(stepsize) eps per alive particle, stepsize
+ *     the per-dimension variance (ddof 1) of the particles / d * 2.38^2 after every iteration
+ *     (adapt_stepsize = 1, the reference's default) or fixed;
+ *   termination: mean acceptance of the moves <= termination_alpha, or iter >= max_iter.
+ * Supported (d, dy): (1,1) (2,1) (2,2) (3,2) (3,3) (5,5) (10,10); 2 <= N <= MGB_ABC_MAX_N. */
+#define MGB_ABC_MAX_N 65536
+typedef struct {
+  int32_t d, dy;
+  const float *m0;   /* (d) prior_mean (host) */
+  const float *C0;   /* d x d prior_covariance_sqrt */
+  const float *P0;   /* d x d prior_precision_sqrt */
+  float c0;          /* (d log 2 pi - log prior_precision_det) / 2 */
+  const float *H;    /* dy x d likelihood_matrix */
+  const float *L;    /* dy x dy likelihood_covariance_sqrt */
+  const float *data; /* (dy) observed data */
+} mgb_abc_lg_model;
+
+typedef struct {
+  int32_t B, N, mcmc_steps, max_iter;
+  float ess_threshold_retain, ess_threshold_resample, termination_alpha;
+  int32_t adapt_stepsize; /* 1: variance-scaled stepsize (default sampler); 0: `stepsize` fixed */
+  float stepsize;
+  int32_t n_schedule;     /* 0: adaptive thresholds */
+  const float *schedule;  /* (n_schedule) thresholds (host); max_iter = n_schedule in the reference */
+} mgb_abc_smc_config;
+
+/* device pointers into the sampler's workspace */
+typedef struct {
+  float *value;           /* (B N, d) particle-major */
+  float *distance;        /* (B N) */
+  float *log_weight;      /* (B N) 0 or -inf */
+  float *prior_potential; /* (B N) */
+  float *alpha;           /* (B N) each particle's mean acceptance over its last moves */
+  float *stepsize;        /* (B, d) */
+  float *threshold;       /* (B) */
+  float *ess;             /* (B) */
+  float *alpha_mean;      /* (B) */
+  int32_t *iter;          /* (B) */
+  int32_t *active;        /* (B) 1 while the posterior has not terminated */
+  float *hist_threshold;  /* (B, hist_len) entry 0 = after startup, i = after iteration i */
+  float *hist_ess;
+  float *hist_alpha;
+  int32_t *hist_resampled;
+  int32_t hist_len;
+} mgb_abc_views;
+
+size_t mgb_abc_smc_workspace(const mgb_abc_smc_config *cfg, int32_t d);
+int mgb_abc_smc_views(const mgb_abc_smc_config *cfg, int32_t d, void *ws_dev, mgb_abc_views *out);
+/* startup (ABCSMCSampler.startup, abc/smc.py:44-85 and :129-149): prior draws, potentials,
+ * simulations, distances, first threshold; the schedule is copied into the workspace */
+int mgb_abc_smc_init(const mgb_abc_smc_config *cfg, const mgb_abc_lg_model *model_host, const uint32_t *keys_dev,
+                     void *ws_dev, size_t ws_bytes, void *stream);
+/* one SMCSampler.update of every active posterior (the caller loops while any views.active[b]) */
+int mgb_abc_smc_step(const mgb_abc_smc_config *cfg, const mgb_abc_lg_model *model_host, void *ws_dev,
+                     size_t ws_bytes, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

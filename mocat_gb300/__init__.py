@@ -5,6 +5,7 @@ CUDA kernels behind a C ABI (include/mocat_gb300.h, libmocatgb.so), with
 Python classes and functions that keep mocat's names and call signatures.
 PyTorch supplies device memory and streams only.
 """
+from . import abc
 from . import adjoint
 from . import batched
 from . import smc
@@ -16,5 +17,5 @@ from .resampling import gather_rows, lse_ess, resample
 
 __version__ = "0.1.0"
 
-__all__ = ["adjoint", "batched", "smc", "random", "ssm", "Scenario", "cdict", "static_cdict", "save_cdict", "load_cdict", "ess_log_weight",
+__all__ = ["abc", "adjoint", "batched", "smc", "random", "ssm", "Scenario", "cdict", "static_cdict", "save_cdict", "load_cdict", "ess_log_weight",
            "log_ess_log_weight", "resample", "gather_rows", "lse_ess"]

@@ -41,6 +41,27 @@ class NL1DModel(ctypes.Structure):
                 ("c", ctypes.c_float)]
 
 
+class ABCModel(ctypes.Structure):
+    _fields_ = [("d", ctypes.c_int32), ("dy", ctypes.c_int32), ("m0", ctypes.c_void_p), ("C0", ctypes.c_void_p),
+                ("P0", ctypes.c_void_p), ("c0", ctypes.c_float), ("H", ctypes.c_void_p), ("L", ctypes.c_void_p),
+                ("data", ctypes.c_void_p)]
+
+
+class ABCConfig(ctypes.Structure):
+    _fields_ = [("B", ctypes.c_int32), ("N", ctypes.c_int32), ("mcmc_steps", ctypes.c_int32),
+                ("max_iter", ctypes.c_int32), ("ess_threshold_retain", ctypes.c_float),
+                ("ess_threshold_resample", ctypes.c_float), ("termination_alpha", ctypes.c_float),
+                ("adapt_stepsize", ctypes.c_int32), ("stepsize", ctypes.c_float), ("n_schedule", ctypes.c_int32),
+                ("schedule", ctypes.c_void_p)]
+
+
+class ABCViews(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_void_p) for k in ("value", "distance", "log_weight", "prior_potential", "alpha",
+                                                "stepsize", "threshold", "ess", "alpha_mean", "iter", "active",
+                                                "hist_threshold", "hist_ess", "hist_alpha", "hist_resampled")] + \
+               [("hist_len", ctypes.c_int32)]
+
+
 class LGTransition(ctypes.Structure):
     _fields_ = [("d", ctypes.c_int32), ("F", ctypes.c_void_p), ("Pq", ctypes.c_void_p), ("cq", ctypes.c_float)]
 
@@ -119,6 +140,10 @@ _SIGNATURES = {
     "mgb_ffbsi_nl1d": ([ctypes.POINTER(NL1DModel), _I64, _I64, _I64, _P, _P, _P, _P, _P, _P, _P, _SZ, _P], _I32),
     "mgb_stitch_nl1d": ([ctypes.POINTER(NL1DModel), _I64, _I64, _P, _P, _P, _F, _P, _P, _P], _I32),
     "mgb_transition_potential_pairs_nl1d": ([ctypes.POINTER(NL1DModel), _I64, _P, _P, _F, _P, _P, _P], _I32),
+    "mgb_abc_smc_workspace": ([ctypes.POINTER(ABCConfig), ctypes.c_int32], _SZ),
+    "mgb_abc_smc_views": ([ctypes.POINTER(ABCConfig), ctypes.c_int32, _P, ctypes.POINTER(ABCViews)], _I32),
+    "mgb_abc_smc_init": ([ctypes.POINTER(ABCConfig), ctypes.POINTER(ABCModel), _P, _P, _SZ, _P], _I32),
+    "mgb_abc_smc_step": ([ctypes.POINTER(ABCConfig), ctypes.POINTER(ABCModel), _P, _SZ, _P], _I32),
     "mgb_logreg_workspace": ([_I64, _I64, ctypes.c_int32, _I32], _SZ),
     "mgb_logreg_potential_grad": ([_P, _P, _I64, ctypes.c_int32, _P, _I64, _P, _P, _I32, _P, _P, _SZ, _P], _I32),
     "mgb_smc_logreg_workspace": ([ctypes.POINTER(SMCConfig), _I64], _SZ),

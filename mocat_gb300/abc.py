@@ -1,0 +1,217 @@
+"""Likelihood-free SMC (ABC-SMC) on the GPU with mocat's names
+(mocat/src/abc/abc.py, abc/mcmc.py, abc/smc.py, abc/scenarios/linear_gaussian.py).
+
+    scenario = LinearGaussian(prior_mean, prior_covariance, data, likelihood_matrix, likelihood_covariance)
+    sampler = MetropolisedABCSMCSampler(ess_threshold_retain=0.8)           # RandomWalkABC moves
+    out = run(scenario, sampler, n=1000, random_key=PRNGKey(0))             # one posterior
+    outs = run_batched(scenario, sampler, n=1000, random_keys=keys)         # B posteriors
+
+Differences from the reference, by design:
+  * resampling (ess < ess_threshold_resample n) is systematic, O(n), instead of
+    random.categorical;
+  * the output keeps the final particles and per-iteration scalars (threshold,
+    ess, alpha, resampled) rather than the stacked (iterations, n, d) chain;
+  * the stepsize variance and the mean acceptance are float64 sums in a fixed
+    order.
+"""
+import ctypes
+import math
+
+import numpy as np
+import torch
+
+from . import _dev, _lib
+from ._lib import call
+from .core import Scenario, cdict
+
+SUPPORTED = {(1, 1), (2, 1), (2, 2), (3, 2), (3, 3), (5, 5), (10, 10)}
+MAX_N = 65536  # MGB_ABC_MAX_N
+
+
+def _arr(a, shape=None):
+    a = np.asarray(a.cpu() if isinstance(a, torch.Tensor) else a, np.float64)
+    return a if shape is None else a.reshape(shape)
+
+
+class ABCScenario(Scenario):
+    """Scenario whose likelihood can be simulated but not evaluated (abc/abc.py:15-39)."""
+    data = None
+
+    def potential(self, x, random_key=None):
+        raise TypeError(f"{self.name} abc_scenario potential is intractable")
+
+    def likelihood_potential(self, x, random_key=None):
+        raise TypeError(f"{self.name} abc_scenario likelihood_potential is intractable")
+
+    def distance_function(self, simulated_data):
+        d = torch.as_tensor(simulated_data) - torch.as_tensor(np.asarray(self.data, np.float32),
+                                                                 device=torch.as_tensor(simulated_data).device)
+        return torch.sqrt((d * d).sum(-1))
+
+
+class LinearGaussian(ABCScenario):
+    """x ~ N(prior_mean, prior_covariance), data ~ N(likelihood_matrix x, likelihood_covariance)
+    (abc/scenarios/linear_gaussian.py).  Square roots follow reset_covariance
+    (mocat/src/utils.py:247-262): Cholesky factors and their inverses."""
+    name = "Linear Gaussian"
+
+    def __init__(self, prior_mean=0.0, prior_covariance=1.0, data=0.0, likelihood_matrix=1.0,
+                 likelihood_covariance=1.0, name=None):
+        super().__init__(name=name)
+        m0 = _arr(prior_mean)
+        self.dim = m0.size if m0.ndim else None
+        for a in (prior_covariance, likelihood_matrix, likelihood_covariance):
+            if self.dim is None and np.ndim(_arr(a)) > 0:
+                self.dim = _arr(a).shape[-1]
+        if self.dim is None:
+            raise AttributeError(f"Could not find dimension for {self.__class__.__name__}")
+        d = self.dim
+        self.prior_mean = np.ones(d) * m0 if m0.ndim == 0 else m0.reshape(d)
+        S0 = _arr(prior_covariance)
+        self.prior_covariance = np.eye(d) * S0 if S0.ndim == 0 else S0
+        H = _arr(likelihood_matrix)
+        self.likelihood_matrix = np.eye(d) * H if H.ndim == 0 else H
+        self.dim_obs = self.likelihood_matrix.shape[0]
+        R = _arr(likelihood_covariance)
+        self.likelihood_covariance = np.eye(self.dim_obs) * R if R.ndim == 0 else R
+        self.data = np.ones(self.dim_obs) * _arr(data) if np.ndim(data) == 0 else _arr(data).reshape(self.dim_obs)
+
+    def derived(self):
+        """float32 constants of the kernels and the C-ABI model struct"""
+        d = self.dim
+        C0 = np.linalg.cholesky(self.prior_covariance)
+        keep = dict(m0=self.prior_mean, C0=C0, P0=np.linalg.inv(C0), H=self.likelihood_matrix,
+                    L=np.linalg.cholesky(self.likelihood_covariance), data=self.data)
+        keep = {k: np.ascontiguousarray(np.asarray(v, np.float32)) for k, v in keep.items()}
+        keep["c0"] = np.float32((d * math.log(2 * math.pi) + math.log(np.linalg.det(self.prior_covariance))) / 2)
+        s = _lib.ABCModel(d, self.dim_obs, keep["m0"].ctypes.data, keep["C0"].ctypes.data, keep["P0"].ctypes.data,
+                          float(keep["c0"]), keep["H"].ctypes.data, keep["L"].ctypes.data, keep["data"].ctypes.data)
+        return keep, s
+
+    def prior_sample(self, random_key):
+        from . import random as mrandom
+        e = mrandom.normal(random_key, (self.dim,)).cpu().numpy().astype(np.float64)
+        return self.prior_mean + np.linalg.cholesky(self.prior_covariance) @ e
+
+
+class RandomWalkABC:
+    """Random-walk ABC MCMC kernel (abc/mcmc.py:59-103): x + sqrt(stepsize) eps, accepted with
+    probability min(1, exp(prior_potential_old - prior_potential_new) [distance_new < threshold])."""
+    name = "Random Walk ABC"
+
+    def __init__(self, threshold=None, stepsize=None):
+        self.threshold = threshold
+        self.stepsize = stepsize
+
+
+class MetropolisedABCSMCSampler:
+    """ABC-SMC with MCMC moves (abc/smc.py:101-245).  mcmc_sampler=None is the reference's
+    default: RandomWalkABC with the stepsize re-set after every iteration to the particles'
+    per-dimension variance / d * 2.38^2; RandomWalkABC(stepsize=s) keeps s fixed."""
+    name = "ABC SMC"
+
+    def __init__(self, mcmc_sampler=None, mcmc_correction="sampler_default", mcmc_steps=1, threshold_schedule=None,
+                 max_iter=int(1e4), ess_threshold_retain=0.9, ess_threshold_resample=0.5, termination_alpha=0.01):
+        if isinstance(mcmc_sampler, type):
+            mcmc_sampler = mcmc_sampler()
+        if mcmc_sampler is not None and not isinstance(mcmc_sampler, RandomWalkABC):
+            raise NotImplementedError("the GPU sampler moves with RandomWalkABC")
+        if mcmc_correction not in ("sampler_default", "Metropolis"):
+            raise NotImplementedError("the GPU sampler uses the Metropolis correction")
+        if mcmc_sampler is not None and mcmc_sampler.stepsize is None:
+            raise NotImplementedError("RandomWalkABC needs a stepsize when given explicitly")
+        self.mcmc_sampler = mcmc_sampler
+        self.mcmc_steps = int(mcmc_steps)
+        self.threshold_schedule = None if threshold_schedule is None else _arr(threshold_schedule).reshape(-1)
+        self.max_iter = len(self.threshold_schedule) if self.threshold_schedule is not None else int(max_iter)
+        self.ess_threshold_retain = float(ess_threshold_retain)
+        self.ess_threshold_resample = float(ess_threshold_resample)
+        self.termination_alpha = float(termination_alpha)
+
+
+class BatchedABCSMC:
+    """B posteriors of one ABC scenario advanced together on the GPU; ``init()`` then
+    ``step()`` until ``done()``, or ``run()``."""
+
+    def __init__(self, scenario, sampler, n, random_keys):
+        if not isinstance(scenario, LinearGaussian):
+            raise NotImplementedError(f"{scenario.__class__.__name__}: no GPU ABC kernel for this scenario")
+        if (scenario.dim, scenario.dim_obs) not in SUPPORTED:
+            raise NotImplementedError(f"(d, dy) = ({scenario.dim}, {scenario.dim_obs}) not compiled")
+        if not 2 <= n <= MAX_N:
+            raise NotImplementedError(f"n must be in [2, {MAX_N}]")
+        keys = _dev.as_key(random_keys).reshape(-1, 2).contiguous()
+        self.scenario, self.sampler = scenario, sampler
+        self.keys = keys
+        self.B, self.n = keys.shape[0], int(n)
+        self._keep, self.model = scenario.derived()
+        sch = sampler.threshold_schedule
+        self._sch = None if sch is None else np.ascontiguousarray(sch, np.float32)
+        fixed = sampler.mcmc_sampler is not None
+        self.cfg = _lib.ABCConfig(self.B, self.n, sampler.mcmc_steps, min(sampler.max_iter, 100000),
+                                  sampler.ess_threshold_retain, sampler.ess_threshold_resample,
+                                  sampler.termination_alpha, 0 if fixed else 1,
+                                  float(sampler.mcmc_sampler.stepsize) if fixed else 0.0,
+                                  0 if self._sch is None else self._sch.size,
+                                  None if self._sch is None else self._sch.ctypes.data)
+        d = scenario.dim
+        self.ws = _dev.workspace(_lib.lib().mgb_abc_smc_workspace(ctypes.byref(self.cfg), d))
+        self.views = _lib.ABCViews()
+        call("mgb_abc_smc_views", ctypes.byref(self.cfg), d, _dev.ptr(self.ws), ctypes.byref(self.views))
+        self.iterations = 0
+
+    def _tensor(self, name, shape, dtype):
+        n = int(np.prod(shape))
+        off = getattr(self.views, name) - self.ws.data_ptr()
+        nbytes = n * torch.tensor([], dtype=dtype).element_size()
+        return self.ws.view(torch.uint8)[off:off + nbytes].view(dtype).reshape(shape)
+
+    def init(self):
+        call("mgb_abc_smc_init", ctypes.byref(self.cfg), ctypes.byref(self.model), _dev.ptr(self.keys),
+             _dev.ptr(self.ws), self.ws.numel(), _dev.stream_ptr())
+        self.iterations = 0
+
+    def step(self):
+        call("mgb_abc_smc_step", ctypes.byref(self.cfg), ctypes.byref(self.model), _dev.ptr(self.ws),
+             self.ws.numel(), _dev.stream_ptr())
+        self.iterations += 1
+
+    def done(self):
+        return not bool(self._tensor("active", (self.B,), torch.int32).any())
+
+    def run(self):
+        self.init()
+        while not self.done() and self.iterations < self.cfg.max_iter:
+            self.step()
+        return self.result()
+
+    def result(self):
+        B, n, d, H = self.B, self.n, self.scenario.dim, self.views.hist_len
+        it = self._tensor("iter", (B,), torch.int32).clone()
+        L = int(it.max()) + 1
+        return cdict(value=self._tensor("value", (B, n, d), torch.float32).clone(),
+                     log_weight=self._tensor("log_weight", (B, n), torch.float32).clone(),
+                     distance=self._tensor("distance", (B, n), torch.float32).clone(),
+                     prior_potential=self._tensor("prior_potential", (B, n), torch.float32).clone(),
+                     stepsize=self._tensor("stepsize", (B, d), torch.float32).clone(),
+                     threshold=self._tensor("hist_threshold", (B, H), torch.float32)[:, :L].clone(),
+                     ess=self._tensor("hist_ess", (B, H), torch.float32)[:, :L].clone(),
+                     alpha=self._tensor("hist_alpha", (B, H), torch.float32)[:, :L].clone(),
+                     resampled=self._tensor("hist_resampled", (B, H), torch.int32)[:, :L].bool(),
+                     iterations=it)
+
+
+def run_batched(scenario, sampler, n, random_keys):
+    """mocat.run(scenario, sampler, n, key) for each of B keys, in one batch.  Per-iteration
+    arrays are padded past each posterior's last iteration."""
+    return BatchedABCSMC(scenario, sampler, n, random_keys).run()
+
+
+def run(scenario, sampler, n, random_key):
+    """mocat.run (sample.py:110-148) for MetropolisedABCSMCSampler on an ABC scenario."""
+    out = run_batched(scenario, sampler, n, _dev.as_key(random_key).reshape(1, 2))
+    L = int(out.iterations[0]) + 1
+    return cdict(value=out.value[0], log_weight=out.log_weight[0], distance=out.distance[0],
+                 prior_potential=out.prior_potential[0], stepsize=out.stepsize[0], threshold=out.threshold[0, :L],
+                 ess=out.ess[0, :L], alpha=out.alpha[0, :L], resampled=out.resampled[0, :L],
+                 iterations=int(out.iterations[0]))

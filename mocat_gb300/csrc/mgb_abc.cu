@@ -1,0 +1,614 @@
+// ABC-SMC: MetropolisedABCSMCSampler with random-walk ABC moves on the ABC
+// linear-Gaussian scenario, B posteriors at once.
+//
+// Reference: MetropolisedABCSMCSampler (mocat/src/abc/smc.py:101-245) driven as
+// mocat.run (mocat/src/sample.py:110-148) through SMCSampler.update
+// (mocat/src/transport/smc.py:61-100); RandomWalkABC (mocat/src/abc/mcmc.py:59-103)
+// with the Metropolis correction (mocat/src/mcmc/metropolis.py:48-70); scenario
+// LinearGaussian (mocat/src/abc/scenarios/linear_gaussian.py):
+//   prior_sample       m0 + C0 normal(key, (d,))
+//   prior_potential    0.5 |(x - m0) P0|^2 + c0
+//   likelihood_sample  H x + L normal(key, (dy,))
+//   distance           sqrt(sum((sim - data)^2))            (abc/abc.py:36-39)
+// Weights are 0 / -inf (distance <= threshold); ESS = exp(log(#alive)).
+//
+// Key flow (per posterior, extra.random_key = e):
+//   startup   (e, sub) = split(e); x_i from split(sub, N)[i]; prior potentials
+//             consume split(e, N + 1) (e <- last); simulations use
+//             split(e, N + 1)[i] (e <- last)
+//   iteration keys = split(e, N + 2): keys[N] resamples, keys[i] drives particle
+//             i's moves, e <- keys[N + 1]; per move k <- split(k)[0];
+//             (k, k1, k2, k3) = split(k, 4); proposal x + sqrt(s) normal(k1, (d,)),
+//             simulation with k3; (k, ku) = split(k); accept if uniform(ku) < alpha,
+//             alpha = min(1, exp(pp_old - pp_new) [dist_new < threshold]).
+// Differences from the reference, by design: resampling is systematic (the
+// reference draws random.categorical); the stepsize variance and the mean
+// acceptance are float64 sums in a fixed order (the reference: float32 in XLA's
+// order), so the oracle can mirror them exactly.
+//
+// Layout: per posterior b, particles particle-major value[(b N + i) d + j];
+// distance, prior potential, alpha, log-weight (B N).  Per iteration three
+// launches: k_abc_resample (one block per posterior), k_abc_move (one thread per
+// particle), k_abc_adapt (one block per posterior: quantile by radix select,
+// ESS, mean acceptance, stepsize, termination, history).
+#include "mgb_internal.cuh"
+
+namespace mgb {
+
+constexpr int ABC_TPB = 1024;
+constexpr int ABC_MOVE_TPB = 256;
+
+template <int D, int DY>
+struct ABCP {
+  float m0[D], C0[D * D], P0[D * D], H[DY * D], L[DY * DY], data[DY];
+  float c0;
+  uint32_t one;
+};
+
+struct ABCCtl {
+  int32_t N, mcmc_steps, max_iter, n_schedule, adapt_stepsize, hist_len;
+  float retain, resample_thr, term_alpha, fixed_stepsize;
+};
+
+// workspace views of one sampler (all arrays cover the B posteriors)
+struct ABCWs {
+  float *value, *value_tmp;       // (B N, d)
+  float *dist, *dist_tmp;         // (B N)
+  float *pp, *pp_tmp;             // (B N) prior potentials
+  float *alpha, *alpha_tmp;       // (B N)
+  float *lw;                      // (B N) 0 / -inf
+  int32_t *rank_idx;              // (B N) index of the alive particle of each rank
+  uint32_t *key;                  // (B, 2) extra.random_key
+  float *stepsize;                // (B, d)
+  float *threshold, *ess, *alpha_mean;  // (B)
+  int32_t *iter, *active, *resampled;   // (B)
+  float *hist_thr, *hist_ess, *hist_alpha;  // (B, hist_len)
+  int32_t *hist_res;              // (B, hist_len)
+  float *schedule;                // (n_schedule)
+};
+
+inline ABCWs carve_abc(Carver &c, int64_t B, int64_t N, int d, int hist_len, int n_schedule) {
+  ABCWs w;
+  const size_t BN = (size_t)(B * N);
+  w.value = c.take<float>(BN * d);
+  w.value_tmp = c.take<float>(BN * d);
+  w.dist = c.take<float>(BN);
+  w.dist_tmp = c.take<float>(BN);
+  w.pp = c.take<float>(BN);
+  w.pp_tmp = c.take<float>(BN);
+  w.alpha = c.take<float>(BN);
+  w.alpha_tmp = c.take<float>(BN);
+  w.lw = c.take<float>(BN);
+  w.rank_idx = c.take<int32_t>(BN);
+  w.key = c.take<uint32_t>(2 * (size_t)B);
+  w.stepsize = c.take<float>((size_t)B * d);
+  w.threshold = c.take<float>((size_t)B);
+  w.ess = c.take<float>((size_t)B);
+  w.alpha_mean = c.take<float>((size_t)B);
+  w.iter = c.take<int32_t>((size_t)B);
+  w.active = c.take<int32_t>((size_t)B);
+  w.resampled = c.take<int32_t>((size_t)B);
+  w.hist_thr = c.take<float>((size_t)B * hist_len);
+  w.hist_ess = c.take<float>((size_t)B * hist_len);
+  w.hist_alpha = c.take<float>((size_t)B * hist_len);
+  w.hist_res = c.take<int32_t>((size_t)B * hist_len);
+  w.schedule = c.take<float>((size_t)(n_schedule > 0 ? n_schedule : 1));
+  return w;
+}
+
+template <int D, int DY>
+__device__ __forceinline__ float abc_prior_potential(const ABCP<D, DY> &p, const float (&x)[D]) {
+  float diff[D];
+#pragma unroll
+  for (int j = 0; j < D; ++j) diff[j] = __fsub_rn(x[j], p.m0[j]);
+  float quad = 0.0f;
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    float v = __fmul_rn(diff[0], p.P0[k]);
+#pragma unroll
+    for (int j = 1; j < D; ++j) v = __fmaf_rn(diff[j], p.P0[j * D + k], v);
+    quad = k == 0 ? __fmul_rn(v, v) : __fmaf_rn(v, v, quad);
+  }
+  return __fadd_rn(__fmul_rn(0.5f, quad), p.c0);
+}
+
+// distance of a simulation H x + L normal(key, (dy,)) to the data
+template <int D, int DY>
+__device__ __forceinline__ float abc_sim_distance(const ABCP<D, DY> &p, const float (&x)[D], uint32_t k0,
+                                                  uint32_t k1) {
+  uint32_t b[DY];
+  bits_vec<DY>(k0, k1, b, p.one);
+  float e[DY];
+#pragma unroll
+  for (int j = 0; j < DY; ++j) e[j] = bits_to_normal(b[j]);
+  float s = 0.0f;
+#pragma unroll
+  for (int r = 0; r < DY; ++r) {
+    float hx = __fmul_rn(p.H[r * D], x[0]);
+#pragma unroll
+    for (int k = 1; k < D; ++k) hx = __fmaf_rn(p.H[r * D + k], x[k], hx);
+    float le = __fmul_rn(p.L[r * DY], e[0]);
+#pragma unroll
+    for (int k = 1; k < DY; ++k) le = __fmaf_rn(p.L[r * DY + k], e[k], le);
+    const float dv = __fsub_rn(__fadd_rn(hx, le), p.data[r]);
+    s = r == 0 ? __fmul_rn(dv, dv) : __fadd_rn(s, __fmul_rn(dv, dv));
+  }
+  return __fsqrt_rn(s);
+}
+
+// ---------------------------------------------------------------- startup
+// one thread per particle: prior draw, prior potential, simulation, distance
+template <int D, int DY>
+__global__ void __launch_bounds__(ABC_MOVE_TPB) k_abc_init(const __grid_constant__ ABCP<D, DY> p, int64_t B,
+                                                            int64_t N, const uint32_t *keys, ABCWs w) {
+  const int64_t g = blockIdx.x * (int64_t)ABC_MOVE_TPB + threadIdx.x;
+  if (g >= B * N) return;
+  const int64_t b = g / N, i = g - b * N;
+  uint32_t e0, e1, s0, s1;
+  split_at(keys[2 * b], keys[2 * b + 1], 2, 0, e0, e1);  // extra.random_key
+  split_at(keys[2 * b], keys[2 * b + 1], 2, 1, s0, s1);  // sub_key of the prior draws
+  uint32_t a0, a1;
+  split_at(s0, s1, (uint64_t)N, (uint64_t)i, a0, a1);
+  uint32_t bits[D];
+  bits_vec<D>(a0, a1, bits, p.one);
+  float e[D], x[D];
+#pragma unroll
+  for (int j = 0; j < D; ++j) e[j] = bits_to_normal(bits[j]);
+#pragma unroll
+  for (int r = 0; r < D; ++r) {
+    float v = __fmul_rn(p.C0[r * D], e[0]);
+#pragma unroll
+    for (int k = 1; k < D; ++k) v = __fmaf_rn(p.C0[r * D + k], e[k], v);
+    x[r] = __fadd_rn(p.m0[r], v);
+    w.value[g * D + r] = x[r];
+  }
+  w.pp[g] = abc_prior_potential<D, DY>(p, x);
+  // the prior potentials consume split(e, N + 1); the simulations use split(e', N + 1)[i]
+  uint32_t f0, f1, k0, k1;
+  split_at(e0, e1, (uint64_t)N + 1, (uint64_t)N, f0, f1);
+  split_at(f0, f1, (uint64_t)N + 1, (uint64_t)i, k0, k1);
+  w.dist[g] = abc_sim_distance<D, DY>(p, x, k0, k1);
+  w.alpha[g] = 1.0f;
+  w.lw[g] = 0.0f;
+  if (i == 0) {
+    uint32_t z0, z1;
+    split_at(f0, f1, (uint64_t)N + 1, (uint64_t)N, z0, z1);
+    w.key[2 * b] = z0;
+    w.key[2 * b + 1] = z1;
+  }
+}
+
+// ------------------------------------------------------- block primitives
+// fixed-order float64 block sum: per-thread partials, a shuffle-down tree per
+// warp, warp results added in warp order by thread 0 (the oracle mirrors it)
+__device__ __forceinline__ double abc_block_sum(double v, double *sm) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = sm[0];
+    for (int k = 1; k < ABC_TPB / 32; ++k) s += sm[k];
+    sm[32] = s;
+  }
+  __syncthreads();
+  const double r = sm[32];
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ int abc_block_count(int v, int *sm) {
+  v = __reduce_add_sync(0xffffffffu, (unsigned)v);
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int s = 0;
+    for (int k = 0; k < ABC_TPB / 32; ++k) s += sm[k];
+    sm[32] = s;
+  }
+  __syncthreads();
+  const int r = sm[32];
+  __syncthreads();
+  return r;
+}
+
+// the rank-th smallest (0-based) of the non-negative floats v[0..n) (bit order
+// = value order; NaN sorts last, as jnp.sort places it): 4 passes of 8-bit digits
+__device__ __forceinline__ float abc_block_select(const float *v, int64_t n, int64_t rank, unsigned *hist,
+                                                  unsigned *res) {
+  unsigned prefix = 0u, mask = 0u;
+  int64_t r = rank;
+#pragma unroll 1
+  for (int pass = 0; pass < 4; ++pass) {
+    const int shift = 24 - 8 * pass;
+    for (int k = threadIdx.x; k < 256; k += ABC_TPB) hist[k] = 0u;
+    __syncthreads();
+    for (int64_t i = threadIdx.x; i < n; i += ABC_TPB) {
+      const unsigned u = __float_as_uint(v[i]);
+      if ((u & mask) == prefix) atomicAdd(&hist[(u >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int64_t cum = 0;
+      unsigned bin = 255u;
+      for (unsigned k = 0; k < 256u; ++k) {
+        if (r < cum + (int64_t)hist[k]) {
+          bin = k;
+          break;
+        }
+        cum += hist[k];
+      }
+      res[0] = bin;
+      res[1] = (unsigned)(r - cum);
+    }
+    __syncthreads();
+    prefix |= res[0] << shift;
+    mask |= 255u << shift;
+    r = res[1];
+    __syncthreads();
+  }
+  return __uint_as_float(prefix);
+}
+
+// --------------------------------------------------------------- adapt
+// MetropolisedABCSMCSampler.adapt (abc/smc.py:226-245) after startup (startup = 1)
+// or after an iteration's moves
+template <int D>
+__global__ void __launch_bounds__(ABC_TPB) k_abc_adapt(ABCCtl ctl, ABCWs w, int startup) {
+  __shared__ double smd[33];
+  __shared__ int smi[33];
+  __shared__ unsigned hist[256], res[2];
+  const int64_t b = blockIdx.x, N = ctl.N;
+  if (!startup && !w.active[b]) return;
+  const int64_t off = b * N;
+  const int iter = startup ? 0 : w.iter[b] + 1;
+  // mean acceptance over the particles alive before the moves
+  double as = 0.0;
+  int ac = 0;
+  for (int64_t i = threadIdx.x; i < N; i += ABC_TPB)
+    if (w.lw[off + i] > -INFINITY) {
+      as += (double)w.alpha[off + i];
+      ++ac;
+    }
+  as = abc_block_sum(as, smd);
+  ac = abc_block_count(ac, smi);
+  const float alpha_mean = (float)(as / (double)ac);
+  // next threshold: the schedule (index clamped, as jax indexing is) or the quantile
+  // of the distances at retain * ess / N (jnp.quantile, linear interpolation)
+  float thr;
+  if (ctl.n_schedule > 0) {
+    thr = w.schedule[iter < ctl.n_schedule ? iter : ctl.n_schedule - 1];
+  } else {
+    const float ess_prev = startup ? (float)N : w.ess[b];
+    const float q = __fdiv_rn(__fmul_rn(ctl.retain, ess_prev), (float)N);
+    const float pos = __fmul_rn(q, (float)(N - 1));
+    const float lo = floorf(pos), hi = ceilf(pos);
+    const float hw = __fsub_rn(pos, lo), lwt = __fsub_rn(1.0f, hw);
+    int64_t ilo = (int64_t)fminf(fmaxf(lo, 0.0f), (float)(N - 1));
+    int64_t ihi = (int64_t)fminf(fmaxf(hi, 0.0f), (float)(N - 1));
+    const float vlo = abc_block_select(w.dist + off, N, ilo, hist, res);
+    const float vhi = ihi == ilo ? vlo : abc_block_select(w.dist + off, N, ihi, hist, res);
+    thr = __fadd_rn(__fmul_rn(vlo, lwt), __fmul_rn(vhi, hw));
+  }
+  // log-weights and ESS
+  int alive = 0;
+  for (int64_t i = threadIdx.x; i < N; i += ABC_TPB) {
+    const bool a = !(w.dist[off + i] > thr);
+    w.lw[off + i] = a ? 0.0f : -INFINITY;
+    alive += a;
+  }
+  alive = abc_block_count(alive, smi);
+  const float ess = alive > 0 ? expf_(logf_((float)alive)) : __int_as_float(0x7fc00000);
+  // stepsize: per-dimension variance (ddof 1) of all particles / d * 2.38^2
+  if (ctl.adapt_stepsize) {
+#pragma unroll 1
+    for (int j = 0; j < D; ++j) {
+      double s1 = 0.0;
+      for (int64_t i = threadIdx.x; i < N; i += ABC_TPB) s1 += (double)w.value[(off + i) * D + j];
+      const double mean = abc_block_sum(s1, smd) / (double)N;
+      double s2 = 0.0;
+      for (int64_t i = threadIdx.x; i < N; i += ABC_TPB) {
+        const double dv = (double)w.value[(off + i) * D + j] - mean;
+        s2 += dv * dv;
+      }
+      const double var = abc_block_sum(s2, smd) / (double)(N - 1);
+      if (threadIdx.x == 0) w.stepsize[b * D + j] = __fmul_rn(__fdiv_rn((float)var, (float)D), 5.6644f);
+    }
+  } else if (threadIdx.x < D) {
+    w.stepsize[b * D + threadIdx.x] = ctl.fixed_stepsize;
+  }
+  if (threadIdx.x == 0) {
+    w.threshold[b] = thr;
+    w.ess[b] = ess;
+    w.alpha_mean[b] = alpha_mean;
+    w.iter[b] = iter;
+    const int done = alive == 0 || alpha_mean <= ctl.term_alpha || iter >= ctl.max_iter;
+    w.active[b] = !done;
+    if (iter < ctl.hist_len) {
+      w.hist_thr[b * ctl.hist_len + iter] = thr;
+      w.hist_ess[b * ctl.hist_len + iter] = ess;
+      w.hist_alpha[b * ctl.hist_len + iter] = alpha_mean;
+      w.hist_res[b * ctl.hist_len + iter] = startup ? 0 : w.resampled[b];
+    }
+    if (!startup) {
+      // e <- split(e, N + 2)[N + 1], after the moves have used the old e
+      uint32_t z0, z1;
+      split_at(w.key[2 * b], w.key[2 * b + 1], (uint64_t)N + 2, (uint64_t)N + 1, z0, z1);
+      w.key[2 * b] = z0;
+      w.key[2 * b + 1] = z1;
+    }
+  }
+}
+
+// -------------------------------------------------------------- resample
+// systematic resampling of 0 / -inf weights: output k takes the alive particle
+// of rank floor((k 2^23 + m) A / (N 2^23)) (A alive, m the uniform's mantissa),
+// the ancestor the 62-bit fixed-point systematic fill gives for these weights
+template <int D>
+__global__ void __launch_bounds__(ABC_TPB) k_abc_resample(ABCCtl ctl, ABCWs w) {
+  __shared__ int smi[33];
+  __shared__ int wsum[ABC_TPB / 32];
+  const int64_t b = blockIdx.x, N = ctl.N;
+  if (!w.active[b]) return;
+  const int64_t off = b * N;
+  const int res = w.ess[b] < __fmul_rn(ctl.resample_thr, (float)N);
+  if (threadIdx.x == 0) w.resampled[b] = res;
+  if (!res) return;
+  // ranks of the alive particles: each thread scans a contiguous chunk
+  const int64_t per = (N + ABC_TPB - 1) / ABC_TPB;
+  const int64_t i0 = threadIdx.x * per, i1 = i0 + per < N ? i0 + per : N;
+  int cnt = 0;
+  for (int64_t i = i0; i < i1; ++i) cnt += w.lw[off + i] > -INFINITY;
+  // block exclusive scan of cnt
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (lane == 31) wsum[warp] = incl;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int s = 0;
+    for (int k = 0; k < ABC_TPB / 32; ++k) {
+      const int t = wsum[k];
+      wsum[k] = s;
+      s += t;
+    }
+    smi[32] = s;
+  }
+  __syncthreads();
+  int rank = wsum[warp] + incl - cnt;
+  const int A = smi[32];
+  if (A == 0) return;  // nothing alive: the posterior is inactive (adapt), kept as a guard
+  for (int64_t i = i0; i < i1; ++i)
+    if (w.lw[off + i] > -INFINITY) w.rank_idx[off + rank++] = (int32_t)i;
+  __syncthreads();
+  const uint32_t *kb = w.key + 2 * b;
+  uint32_t r0, r1;
+  split_at(kb[0], kb[1], (uint64_t)N + 2, (uint64_t)N, r0, r1);
+  const uint64_t m23 = bits_at(r0, r1, 1, 0) >> 9;
+  const uint64_t den = (uint64_t)N << 23;
+  for (int64_t k = threadIdx.x; k < N; k += ABC_TPB) {
+    const uint64_t rk = ((((uint64_t)k) << 23) + m23) * (uint64_t)A / den;
+    const int64_t src = off + w.rank_idx[off + rk];
+#pragma unroll
+    for (int j = 0; j < D; ++j) w.value_tmp[(off + k) * D + j] = w.value[src * D + j];
+    w.dist_tmp[off + k] = w.dist[src];
+    w.pp_tmp[off + k] = w.pp[src];
+    w.alpha_tmp[off + k] = w.alpha[src];
+  }
+  __syncthreads();
+  for (int64_t k = threadIdx.x; k < N; k += ABC_TPB) {
+#pragma unroll
+    for (int j = 0; j < D; ++j) w.value[(off + k) * D + j] = w.value_tmp[(off + k) * D + j];
+    w.dist[off + k] = w.dist_tmp[off + k];
+    w.pp[off + k] = w.pp_tmp[off + k];
+    w.alpha[off + k] = w.alpha_tmp[off + k];
+    w.lw[off + k] = 0.0f;
+  }
+  if (threadIdx.x == 0) w.ess[b] = (float)N;
+}
+
+// ------------------------------------------------------------------ moves
+// forward_proposal (abc/smc.py:172-209): mcmc_steps random-walk ABC moves of
+// every alive particle with key split(e, N + 2)[i]; dead particles are kept
+template <int D, int DY>
+__global__ void __launch_bounds__(ABC_MOVE_TPB) k_abc_move(const __grid_constant__ ABCP<D, DY> p, ABCCtl ctl,
+                                                            int64_t B, ABCWs w) {
+  const int64_t N = ctl.N;
+  const int64_t g = blockIdx.x * (int64_t)ABC_MOVE_TPB + threadIdx.x;
+  if (g >= B * N) return;
+  const int64_t b = g / N, i = g - b * N;
+  if (!w.active[b] || !(w.lw[g] > -INFINITY)) return;
+  const float thr = w.threshold[b];
+  float sq[D], x[D];
+#pragma unroll
+  for (int j = 0; j < D; ++j) {
+    sq[j] = __fsqrt_rn(w.stepsize[b * D + j]);
+    x[j] = w.value[g * D + j];
+  }
+  float pp = w.pp[g], dist = w.dist[g];
+  uint32_t k0, k1;
+  split_at(w.key[2 * b], w.key[2 * b + 1], (uint64_t)N + 2, (uint64_t)i, k0, k1);
+  float asum = 0.0f;
+#pragma unroll 1
+  for (int s = 0; s < ctl.mcmc_steps; ++s) {
+    uint32_t t0, t1;
+    split_at(k0, k1, 2, 0, t0, t1);  // always(): key <- split(key)[0]
+    uint32_t n0, n1, a0, a1, c0, c1;
+    split_at(t0, t1, 4, 0, n0, n1);  // new extra key
+    split_at(t0, t1, 4, 1, a0, a1);  // proposal normals
+    split_at(t0, t1, 4, 3, c0, c1);  // simulation
+    uint32_t bits[D];
+    bits_vec<D>(a0, a1, bits, p.one);
+    float xp[D];
+#pragma unroll
+    for (int j = 0; j < D; ++j) xp[j] = __fadd_rn(x[j], __fmul_rn(sq[j], bits_to_normal(bits[j])));
+    const float ppn = abc_prior_potential<D, DY>(p, xp);
+    const float dn = abc_sim_distance<D, DY>(p, xp, c0, c1);
+    // min(1, exp(pp - ppn) [dn < thr]) with NaN (inf * 0) mapped to 0 (metropolis.py:58)
+    float a = __fmul_rn(expf_(__fsub_rn(pp, ppn)), dn < thr ? 1.0f : 0.0f);
+    a = a != a ? 0.0f : fminf(1.0f, a);
+    uint32_t u0, u1, v0, v1;
+    split_at(n0, n1, 2, 0, u0, u1);
+    split_at(n0, n1, 2, 1, v0, v1);
+    const float u = bits_to_unit(bits_at(v0, v1, 1, 0));
+    if (u < a) {
+#pragma unroll
+      for (int j = 0; j < D; ++j) x[j] = xp[j];
+      pp = ppn;
+      dist = dn;
+    }
+    asum = s == 0 ? a : __fadd_rn(asum, a);
+    k0 = u0;
+    k1 = u1;
+  }
+#pragma unroll
+  for (int j = 0; j < D; ++j) w.value[g * D + j] = x[j];
+  w.pp[g] = pp;
+  w.dist[g] = dist;
+  w.alpha[g] = __fdiv_rn(asum, (float)ctl.mcmc_steps);
+}
+
+template <int D, int DY>
+static ABCP<D, DY> pack_abc(const mgb_abc_lg_model *m) {
+  ABCP<D, DY> p;
+  for (int i = 0; i < D; ++i) p.m0[i] = m->m0[i];
+  for (int i = 0; i < D * D; ++i) {
+    p.C0[i] = m->C0[i];
+    p.P0[i] = m->P0[i];
+  }
+  for (int i = 0; i < DY * D; ++i) p.H[i] = m->H[i];
+  for (int i = 0; i < DY * DY; ++i) p.L[i] = m->L[i];
+  for (int i = 0; i < DY; ++i) p.data[i] = m->data[i];
+  p.c0 = m->c0;
+  p.one = 1u;
+  return p;
+}
+
+static int abc_hist_len(const mgb_abc_smc_config *cfg) { return cfg->max_iter + 1; }
+
+static ABCCtl abc_ctl(const mgb_abc_smc_config *cfg) {
+  ABCCtl c;
+  c.N = cfg->N;
+  c.mcmc_steps = cfg->mcmc_steps;
+  c.max_iter = cfg->max_iter;
+  c.n_schedule = cfg->n_schedule;
+  c.adapt_stepsize = cfg->adapt_stepsize;
+  c.hist_len = abc_hist_len(cfg);
+  c.retain = cfg->ess_threshold_retain;
+  c.resample_thr = cfg->ess_threshold_resample;
+  c.term_alpha = cfg->termination_alpha;
+  c.fixed_stepsize = cfg->stepsize;
+  return c;
+}
+
+static ABCWs abc_ws(const mgb_abc_smc_config *cfg, int d, void *ws) {
+  Carver c(ws);
+  return carve_abc(c, cfg->B, cfg->N, d, abc_hist_len(cfg), cfg->n_schedule);
+}
+
+template <int D, int DY>
+static int abc_init(const mgb_abc_smc_config *cfg, const mgb_abc_lg_model *m, const uint32_t *keys, void *ws,
+                    cudaStream_t s) {
+  const ABCWs w = abc_ws(cfg, D, ws);
+  const ABCCtl ctl = abc_ctl(cfg);
+  if (cfg->n_schedule > 0 &&
+      cudaMemcpyAsync(w.schedule, cfg->schedule, sizeof(float) * cfg->n_schedule, cudaMemcpyHostToDevice, s) !=
+          cudaSuccess)
+    return ERR_CUDA;
+  const int64_t BN = (int64_t)cfg->B * cfg->N;
+  k_abc_init<D, DY><<<(unsigned)((BN + ABC_MOVE_TPB - 1) / ABC_MOVE_TPB), ABC_MOVE_TPB, 0, s>>>(
+      pack_abc<D, DY>(m), cfg->B, cfg->N, keys, w);
+  int st = launch_status();
+  if (st) return st;
+  k_abc_adapt<D><<<(unsigned)cfg->B, ABC_TPB, 0, s>>>(ctl, w, 1);
+  return launch_status();
+}
+
+template <int D, int DY>
+static int abc_step(const mgb_abc_smc_config *cfg, const mgb_abc_lg_model *m, void *ws, cudaStream_t s) {
+  const ABCWs w = abc_ws(cfg, D, ws);
+  const ABCCtl ctl = abc_ctl(cfg);
+  k_abc_resample<D><<<(unsigned)cfg->B, ABC_TPB, 0, s>>>(ctl, w);
+  int st = launch_status();
+  if (st) return st;
+  const int64_t BN = (int64_t)cfg->B * cfg->N;
+  k_abc_move<D, DY><<<(unsigned)((BN + ABC_MOVE_TPB - 1) / ABC_MOVE_TPB), ABC_MOVE_TPB, 0, s>>>(
+      pack_abc<D, DY>(m), ctl, cfg->B, w);
+  if ((st = launch_status())) return st;
+  k_abc_adapt<D><<<(unsigned)cfg->B, ABC_TPB, 0, s>>>(ctl, w, 0);
+  return launch_status();
+}
+
+#define MGB_ABC_DISPATCH(FN, ...)                                     \
+  do {                                                                \
+    const int d_ = m->d, dy_ = m->dy;                                 \
+    if (d_ == 1 && dy_ == 1) return FN<1, 1>(__VA_ARGS__);            \
+    if (d_ == 2 && dy_ == 1) return FN<2, 1>(__VA_ARGS__);            \
+    if (d_ == 2 && dy_ == 2) return FN<2, 2>(__VA_ARGS__);            \
+    if (d_ == 3 && dy_ == 2) return FN<3, 2>(__VA_ARGS__);            \
+    if (d_ == 3 && dy_ == 3) return FN<3, 3>(__VA_ARGS__);            \
+    if (d_ == 5 && dy_ == 5) return FN<5, 5>(__VA_ARGS__);            \
+    if (d_ == 10 && dy_ == 10) return FN<10, 10>(__VA_ARGS__);        \
+    return ERR_UNSUPPORTED;                                           \
+  } while (0)
+
+static bool abc_ok(const mgb_abc_smc_config *cfg, const mgb_abc_lg_model *m) {
+  return cfg && m && m->m0 && m->C0 && m->P0 && m->H && m->L && m->data && cfg->B >= 1 && cfg->N >= 2 &&
+         cfg->N <= MGB_ABC_MAX_N && cfg->mcmc_steps >= 1 && cfg->max_iter >= 0 && cfg->max_iter <= 100000 &&
+         cfg->n_schedule >= 0 && (cfg->n_schedule == 0 || cfg->schedule);
+}
+
+}  // namespace mgb
+
+using namespace mgb;
+
+extern "C" {
+
+size_t mgb_abc_smc_workspace(const mgb_abc_smc_config *cfg, int32_t d) {
+  if (!cfg || d < 1) return 0;
+  Carver c(nullptr);
+  carve_abc(c, cfg->B, cfg->N, d, abc_hist_len(cfg), cfg->n_schedule);
+  return c.bytes();
+}
+
+int mgb_abc_smc_views(const mgb_abc_smc_config *cfg, int32_t d, void *ws, mgb_abc_views *out) {
+  if (!cfg || !ws || !out || d < 1) return ERR_BAD_ARG;
+  const ABCWs w = abc_ws(cfg, d, ws);
+  out->value = w.value;
+  out->distance = w.dist;
+  out->log_weight = w.lw;
+  out->prior_potential = w.pp;
+  out->alpha = w.alpha;
+  out->stepsize = w.stepsize;
+  out->threshold = w.threshold;
+  out->ess = w.ess;
+  out->alpha_mean = w.alpha_mean;
+  out->iter = w.iter;
+  out->active = w.active;
+  out->hist_threshold = w.hist_thr;
+  out->hist_ess = w.hist_ess;
+  out->hist_alpha = w.hist_alpha;
+  out->hist_resampled = w.hist_res;
+  out->hist_len = abc_hist_len(cfg);
+  return OK;
+}
+
+int mgb_abc_smc_init(const mgb_abc_smc_config *cfg, const mgb_abc_lg_model *m, const uint32_t *keys, void *ws,
+                     size_t ws_bytes, void *stream) {
+  if (!abc_ok(cfg, m) || !keys || !ws) return ERR_BAD_ARG;
+  if (ws_bytes < mgb_abc_smc_workspace(cfg, m->d)) return ERR_WORKSPACE;
+  MGB_ABC_DISPATCH(abc_init, cfg, m, keys, ws, (cudaStream_t)stream);
+}
+
+int mgb_abc_smc_step(const mgb_abc_smc_config *cfg, const mgb_abc_lg_model *m, void *ws, size_t ws_bytes,
+                     void *stream) {
+  if (!abc_ok(cfg, m) || !ws) return ERR_BAD_ARG;
+  if (ws_bytes < mgb_abc_smc_workspace(cfg, m->d)) return ERR_WORKSPACE;
+  MGB_ABC_DISPATCH(abc_step, cfg, m, ws, (cudaStream_t)stream);
+}
+
+}  // extern "C"

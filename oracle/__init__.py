@@ -66,6 +66,18 @@ class _NLModel(ctypes.Structure):
     _fields_ = [("s0", ctypes.c_float), ("tsd", ctypes.c_float), ("lsd", ctypes.c_float), ("c", ctypes.c_float)]
 
 
+class _ABCModel(ctypes.Structure):
+    _fields_ = [("d", ctypes.c_int), ("dy", ctypes.c_int), ("m0", vp), ("C0", vp), ("P0", vp),
+                ("c0", ctypes.c_float), ("H", vp), ("L", vp), ("data", vp)]
+
+
+class _ABCConfig(ctypes.Structure):
+    _fields_ = [("N", ctypes.c_int), ("mcmc_steps", ctypes.c_int), ("max_iter", ctypes.c_int),
+                ("n_schedule", ctypes.c_int), ("adapt_stepsize", ctypes.c_int), ("retain", ctypes.c_float),
+                ("resample_thr", ctypes.c_float), ("term_alpha", ctypes.c_float), ("stepsize", ctypes.c_float),
+                ("schedule", vp)]
+
+
 class _FFBSiModel(ctypes.Structure):
     _fields_ = [("d", ctypes.c_int), ("F", ctypes.c_void_p), ("Pq", ctypes.c_void_p), ("cq", ctypes.c_float),
                 ("nl", ctypes.c_int), ("tsd", ctypes.c_float), ("c", ctypes.c_float)]
@@ -124,6 +136,9 @@ def lib():
         L.o_nl_run.argtypes = [ctypes.POINTER(_NLModel), i64, i64, u32p, f32p, f32p, ctypes.c_float, ctypes.c_int,
                                f32p, i32p, vp, vp]
         L.o_nl_run.restype = ctypes.c_double
+        L.o_abc_lg_run.argtypes = [ctypes.POINTER(_ABCModel), ctypes.POINTER(_ABCConfig), u32p, f32p, f32p, f32p,
+                                   f32p, f32p, f32p, f32p, i32p]
+        L.o_abc_lg_run.restype = ctypes.c_int
         L.o_ffbsi_nl1d.argtypes = [ctypes.POINTER(_NLModel), i64, i64, i64, f32p, f32p, f32p, u32p, f32p, i32p]
         L.o_stitch_nl1d.argtypes = [ctypes.POINTER(_NLModel), i64, i64, f32p, f32p, f32p, ctypes.c_float, u32p, i32p]
         L.o_transition_potential_pairs_nl1d.argtypes = [ctypes.POINTER(_NLModel), i64, f32p, f32p, ctypes.c_float,
@@ -486,6 +501,37 @@ def transition_potential_pairs_nl1d(params, x0, x1, t_prev):
     lib().o_transition_potential_pairs_nl1d(ctypes.byref(_nl_struct(params)), x0.size, x0, x1,
                                             float(np.float32(t_prev)), out)
     return out
+
+
+def abc_lg_run(params, N, key, mcmc_steps=1, max_iter=10000, retain=0.9, resample_thr=0.5, term_alpha=0.01,
+               schedule=None, stepsize=None):
+    """mocat.run(LinearGaussian ABC scenario, MetropolisedABCSMCSampler(...), N, key) restated with
+    systematic resampling (one posterior).  params: m0, C0, P0, c0, H, L, data (float32).
+    stepsize=None: the default sampler's variance-scaled stepsize; a float: fixed.
+    Returns dict(value (N, d), log_weight, distance, stepsize, threshold, ess, alpha, resampled
+    (iterations + 1 entries), iterations)."""
+    keep = {k: _f32(params[k]) for k in ("m0", "C0", "P0", "H", "L", "data")}
+    d, dy = keep["m0"].size, keep["data"].size
+    md = _ABCModel(d, dy, keep["m0"].ctypes.data, keep["C0"].ctypes.data, keep["P0"].ctypes.data,
+                   float(params["c0"]), keep["H"].ctypes.data, keep["L"].ctypes.data, keep["data"].ctypes.data)
+    sch = None if schedule is None else _f32(schedule)
+    if sch is not None:
+        max_iter = sch.size
+    cf = _ABCConfig(N, mcmc_steps, max_iter, 0 if sch is None else sch.size, 1 if stepsize is None else 0,
+                    float(retain), float(resample_thr), float(term_alpha), 0.0 if stepsize is None else float(stepsize),
+                    _ptr(sch))
+    x = np.empty((N, d), np.float32)
+    lw = np.empty(N, np.float32)
+    dist = np.empty(N, np.float32)
+    st = np.empty(d, np.float32)
+    H = max_iter + 1
+    ht, he, ha = np.zeros(H, np.float32), np.zeros(H, np.float32), np.zeros(H, np.float32)
+    hr = np.zeros(H, np.int32)
+    it = lib().o_abc_lg_run(ctypes.byref(md), ctypes.byref(cf), _u32(key), x.reshape(-1), lw, dist, st, ht, he, ha,
+                            hr)
+    L = it + 1
+    return dict(value=x, log_weight=lw, distance=dist, stepsize=st, threshold=ht[:L], ess=he[:L], alpha=ha[:L],
+                resampled=hr[:L].astype(bool), iterations=it)
 
 
 def ffbsi_lg(F, Pq, cq, x_hist, lw_hist, key, M):

@@ -910,6 +910,258 @@ void o_transition_potential_pairs_nl1d(const o_nl_model *nm, int64_t M, const fl
     for (int64_t i = 0; i < M; ++i) out[i] = o_transition_potential(&md, x0 + i, x1 + i, drift);
 }
 
+/* ---------------------------------------------------------------- ABC-SMC */
+
+typedef struct {
+    int d, dy;
+    const float *m0, *C0, *P0;  /* prior mean, covariance sqrt, precision sqrt */
+    float c0;                   /* prior potential normaliser */
+    const float *H, *L, *data;  /* likelihood matrix, covariance sqrt, observed data */
+} o_abc_model;
+
+typedef struct {
+    int N, mcmc_steps, max_iter, n_schedule, adapt_stepsize;
+    float retain, resample_thr, term_alpha, stepsize;
+    const float *schedule;
+} o_abc_config;
+
+/* prior_potential of the ABC LinearGaussian scenario: 0.5 |(x - m0) P0|^2 + c0
+ * (vectorised gaussian_potential, utils.py:90-104) */
+static float o_abc_prior_pot(const o_abc_model *md, const float *x)
+{
+    const int d = md->d;
+    float diff[16];
+    for (int j = 0; j < d; ++j) diff[j] = x[j] - md->m0[j];
+    float quad = 0.0f;
+    for (int k = 0; k < d; ++k) {
+        float v = diff[0] * md->P0[k];
+        for (int j = 1; j < d; ++j) v = fmaf(diff[j], md->P0[j * d + k], v);
+        quad = k == 0 ? v * v : fmaf(v, v, quad);
+    }
+    return 0.5f * quad + md->c0;
+}
+
+/* |H x + L normal(key, (dy,)) - data|_2 (likelihood_sample, distance_function) */
+static float o_abc_sim_dist(const o_abc_model *md, const float *x, uint32_t k0, uint32_t k1)
+{
+    const int d = md->d, dy = md->dy;
+    float e[16];
+    o_normal_vec(k0, k1, dy, e);
+    float s = 0.0f;
+    for (int r = 0; r < dy; ++r) {
+        float hx = md->H[r * d] * x[0];
+        for (int k = 1; k < d; ++k) hx = fmaf(md->H[r * d + k], x[k], hx);
+        float le = md->L[r * dy] * e[0];
+        for (int k = 1; k < dy; ++k) le = fmaf(md->L[r * dy + k], e[k], le);
+        float dv = (hx + le) - md->data[r];
+        s = r == 0 ? dv * dv : s + dv * dv;
+    }
+    return sqrtf(s);
+}
+
+/* the GPU's fixed-order float64 block sum over 1024 thread partials: a
+ * shuffle-down tree (16, 8, 4, 2, 1) inside each warp, then the 32 warp results
+ * in warp order */
+#define O_ABC_TPB 1024
+static double o_abc_block_sum(const double *part)
+{
+    double warp_res[O_ABC_TPB / 32];
+    for (int w = 0; w < O_ABC_TPB / 32; ++w) {
+        double v[32], t[32];
+        for (int l = 0; l < 32; ++l) v[l] = part[32 * w + l];
+        for (int off = 16; off > 0; off >>= 1) {
+            for (int l = 0; l < 32; ++l) t[l] = v[l] + (l + off < 32 ? v[l + off] : v[l]);
+            memcpy(v, t, sizeof(v));
+        }
+        warp_res[w] = v[0];
+    }
+    double s = warp_res[0];
+    for (int w = 1; w < O_ABC_TPB / 32; ++w) s += warp_res[w];
+    return s;
+}
+
+static int o_cmp_u32(const void *a, const void *b)
+{
+    uint32_t x = *(const uint32_t *)a, y = *(const uint32_t *)b;
+    return x < y ? -1 : (x > y);
+}
+
+/* k-th smallest of non-negative floats by bit order (NaN last) */
+static float o_abc_select(const float *v, int n, int k, uint32_t *scratch)
+{
+    memcpy(scratch, v, sizeof(float) * (size_t)n);
+    qsort(scratch, (size_t)n, sizeof(uint32_t), o_cmp_u32);
+    float r;
+    memcpy(&r, &scratch[k], sizeof(float));
+    return r;
+}
+
+/* MetropolisedABCSMCSampler adapt (abc/smc.py:226-245); returns 1 while active.
+ * iter: the iteration just completed (0 = startup); ess_prev: the state's ess field */
+static int o_abc_adapt(const o_abc_model *md, const o_abc_config *cf, int iter, float ess_prev, float *x, float *lw,
+                       const float *dist, const float *alpha, float *stepsize, float *thr_out, float *ess_out,
+                       float *alpha_mean_out, uint32_t *scratch)
+{
+    const int N = cf->N, d = md->d;
+    double part[O_ABC_TPB];
+    int cnt = 0;
+    for (int t = 0; t < O_ABC_TPB; ++t) {
+        double s = 0.0;
+        for (int i = t; i < N; i += O_ABC_TPB)
+            if (lw[i] > -INFINITY) { s += (double)alpha[i]; ++cnt; }
+        part[t] = s;
+    }
+    const float alpha_mean = (float)(o_abc_block_sum(part) / (double)cnt);
+    float thr;
+    if (cf->n_schedule > 0) {
+        thr = cf->schedule[iter < cf->n_schedule ? iter : cf->n_schedule - 1];
+    } else {
+        const float q = (cf->retain * ess_prev) / (float)N;
+        const float pos = q * (float)(N - 1);
+        const float lo = floorf(pos), hi = ceilf(pos);
+        const float hw = pos - lo, lwt = 1.0f - hw;
+        const int ilo = (int)fminf(fmaxf(lo, 0.0f), (float)(N - 1));
+        const int ihi = (int)fminf(fmaxf(hi, 0.0f), (float)(N - 1));
+        const float vlo = o_abc_select(dist, N, ilo, scratch);
+        const float vhi = ihi == ilo ? vlo : o_abc_select(dist, N, ihi, scratch);
+        thr = vlo * lwt + vhi * hw;
+    }
+    int alive = 0;
+    for (int i = 0; i < N; ++i) {
+        const int a = !(dist[i] > thr);
+        lw[i] = a ? 0.0f : -INFINITY;
+        alive += a;
+    }
+    const float ess = alive > 0 ? o_expf(o_logf((float)alive)) : NAN;
+    for (int j = 0; j < d; ++j) {
+        if (!cf->adapt_stepsize) { stepsize[j] = cf->stepsize; continue; }
+        for (int t = 0; t < O_ABC_TPB; ++t) {
+            double s = 0.0;
+            for (int i = t; i < N; i += O_ABC_TPB) s += (double)x[(size_t)i * d + j];
+            part[t] = s;
+        }
+        const double mean = o_abc_block_sum(part) / (double)N;
+        for (int t = 0; t < O_ABC_TPB; ++t) {
+            double s = 0.0;
+            for (int i = t; i < N; i += O_ABC_TPB) {
+                const double dv = (double)x[(size_t)i * d + j] - mean;
+                s += dv * dv;
+            }
+            part[t] = s;
+        }
+        const double var = o_abc_block_sum(part) / (double)(N - 1);
+        stepsize[j] = ((float)var / (float)d) * 5.6644f;
+    }
+    *thr_out = thr;
+    *ess_out = ess;
+    *alpha_mean_out = alpha_mean;
+    return !(alive == 0 || alpha_mean <= cf->term_alpha || iter >= cf->max_iter);
+}
+
+/* mocat.run of MetropolisedABCSMCSampler with RandomWalkABC moves on the ABC
+ * LinearGaussian scenario (abc/smc.py:101-245, abc/mcmc.py:59-103,
+ * metropolis.py:48-70, transport/smc.py:61-100, sample.py:110-148), one
+ * posterior, systematic resampling.  x (N, d) receives the final particles,
+ * lw / dist (N) the final log-weights and distances; hist_* (max_iter + 1)
+ * entry 0 = after startup.  Returns the number of iterations. */
+int o_abc_lg_run(const o_abc_model *md, const o_abc_config *cf, const uint32_t *key, float *x, float *lw,
+                 float *dist, float *stepsize, float *hist_thr, float *hist_ess, float *hist_alpha, int32_t *hist_res)
+{
+    const int N = cf->N, d = md->d;
+    float *pp = (float *)malloc(sizeof(float) * (size_t)N), *alpha = (float *)malloc(sizeof(float) * (size_t)N);
+    float *x2 = (float *)malloc(sizeof(float) * (size_t)N * d), *f2 = (float *)malloc(sizeof(float) * (size_t)N * 3);
+    int32_t *anc = (int32_t *)malloc(sizeof(int32_t) * (size_t)N);
+    uint32_t *scratch = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)N);
+    uint32_t e0, e1, s0, s1, f0, f1;
+    o_split_at(key[0], key[1], 2, 0, &e0, &e1);
+    o_split_at(key[0], key[1], 2, 1, &s0, &s1);
+    o_split_at(e0, e1, (uint64_t)N + 1, (uint64_t)N, &f0, &f1);
+    for (int i = 0; i < N; ++i) {
+        uint32_t a0, a1, k0, k1;
+        float e[16];
+        o_split_at(s0, s1, (uint64_t)N, (uint64_t)i, &a0, &a1);
+        o_normal_vec(a0, a1, d, e);
+        float *xi = x + (size_t)i * d;
+        for (int r = 0; r < d; ++r) {
+            float v = md->C0[r * d] * e[0];
+            for (int k = 1; k < d; ++k) v = fmaf(md->C0[r * d + k], e[k], v);
+            xi[r] = md->m0[r] + v;
+        }
+        pp[i] = o_abc_prior_pot(md, xi);
+        o_split_at(f0, f1, (uint64_t)N + 1, (uint64_t)i, &k0, &k1);
+        dist[i] = o_abc_sim_dist(md, xi, k0, k1);
+        alpha[i] = 1.0f;
+        lw[i] = 0.0f;
+    }
+    uint32_t k[2];
+    o_split_at(f0, f1, (uint64_t)N + 1, (uint64_t)N, &k[0], &k[1]);
+    float thr, ess, am;
+    int active = o_abc_adapt(md, cf, 0, (float)N, x, lw, dist, alpha, stepsize, &thr, &ess, &am, scratch);
+    hist_thr[0] = thr; hist_ess[0] = ess; hist_alpha[0] = am; hist_res[0] = 0;
+    int iter = 0;
+    while (active) {
+        ++iter;
+        const int res = ess < cf->resample_thr * (float)N;
+        if (res) {
+            uint32_t r0, r1;
+            o_split_at(k[0], k[1], (uint64_t)N + 2, (uint64_t)N, &r0, &r1);
+            o_resample_systematic(lw, N, o_bits_at(r0, r1, 1, 0) >> 9, anc);
+            for (int i = 0; i < N; ++i) {
+                memcpy(x2 + (size_t)i * d, x + (size_t)anc[i] * d, sizeof(float) * d);
+                f2[3 * i] = dist[anc[i]]; f2[3 * i + 1] = pp[anc[i]]; f2[3 * i + 2] = alpha[anc[i]];
+            }
+            memcpy(x, x2, sizeof(float) * (size_t)N * d);
+            for (int i = 0; i < N; ++i) {
+                dist[i] = f2[3 * i]; pp[i] = f2[3 * i + 1]; alpha[i] = f2[3 * i + 2]; lw[i] = 0.0f;
+            }
+            ess = (float)N;
+        }
+        float sq[16];
+        for (int j = 0; j < d; ++j) sq[j] = sqrtf(stepsize[j]);
+        for (int i = 0; i < N; ++i) {
+            if (!(lw[i] > -INFINITY)) continue;
+            float *xi = x + (size_t)i * d;
+            uint32_t k0, k1;
+            o_split_at(k[0], k[1], (uint64_t)N + 2, (uint64_t)i, &k0, &k1);
+            float asum = 0.0f;
+            for (int st = 0; st < cf->mcmc_steps; ++st) {
+                uint32_t t0, t1, n0, n1, a0, a1, c0, c1, u0, u1, v0, v1;
+                o_split_at(k0, k1, 2, 0, &t0, &t1);
+                o_split_at(t0, t1, 4, 0, &n0, &n1);
+                o_split_at(t0, t1, 4, 1, &a0, &a1);
+                o_split_at(t0, t1, 4, 3, &c0, &c1);
+                float e[16], xp[16];
+                o_normal_vec(a0, a1, d, e);
+                for (int j = 0; j < d; ++j) xp[j] = xi[j] + sq[j] * e[j];
+                const float ppn = o_abc_prior_pot(md, xp);
+                const float dn = o_abc_sim_dist(md, xp, c0, c1);
+                float a = o_expf(pp[i] - ppn) * (dn < thr ? 1.0f : 0.0f);
+                a = a != a ? 0.0f : fminf(1.0f, a);
+                o_split_at(n0, n1, 2, 0, &u0, &u1);
+                o_split_at(n0, n1, 2, 1, &v0, &v1);
+                const float u = o_bits_to_unit(o_bits_at(v0, v1, 1, 0));
+                if (u < a) {
+                    memcpy(xi, xp, sizeof(float) * d);
+                    pp[i] = ppn;
+                    dist[i] = dn;
+                }
+                asum = st == 0 ? a : asum + a;
+                k0 = u0; k1 = u1;
+            }
+            alpha[i] = asum / (float)cf->mcmc_steps;
+        }
+        active = o_abc_adapt(md, cf, iter, ess, x, lw, dist, alpha, stepsize, &thr, &ess, &am, scratch);
+        uint32_t z0, z1;
+        o_split_at(k[0], k[1], (uint64_t)N + 2, (uint64_t)N + 1, &z0, &z1);
+        k[0] = z0; k[1] = z1;
+        if (iter <= cf->max_iter) {
+            hist_thr[iter] = thr; hist_ess[iter] = ess; hist_alpha[iter] = am; hist_res[iter] = res;
+        }
+    }
+    free(pp); free(alpha); free(x2); free(f2); free(anc); free(scratch);
+    return iter;
+}
+
 int o_num_threads(void)
 {
 #ifdef _OPENMP
