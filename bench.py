@@ -37,6 +37,10 @@ smc_logreg -- the tempered SMC sampler on Bayesian logistic regression
 potential+gradient evaluations per second over timed SMC iterations, and the
 tcgen05 potential kernel's tensor roofline next to the fp32 kernel.
 
+abc_smc -- ABC-SMC on the reference's ABC linear-Gaussian test model, 64
+posteriors of 16384 particles to termination: likelihood simulations per
+second, next to the oracle on one posterior.
+
 nl1d -- the bootstrap filter on the one-dimensional non-linear benchmark
 model at N = 2^20, T = 1000 (graph replay), its fused step kernel alone, and
 the oracle's C/OpenMP filter on a sample of steps.
@@ -450,6 +454,54 @@ def bench_config1(args, rank):
             "barriers per step)", "log_z": float(logz.item())}
 
 
+def bench_abc(args, rank):
+    """ABC-SMC (MetropolisedABCSMCSampler, RandomWalkABC moves, adaptive thresholds at retain
+    0.8) on the reference's ABC linear-Gaussian test model (d = 3, dy = 2), 64 posteriors of
+    16384 particles run to termination in one batch; throughput = likelihood simulations
+    (one per move of an alive particle) per second of the whole run; the oracle runs one
+    posterior of the same size on the host cores."""
+    import torch
+    import mocat_gb300 as mg
+    import oracle
+    S0 = np.array([[1.0, -0.6, 0.5], [-0.6, 0.7, 0.1], [0.5, -0.6, 3.0]])
+    H = np.array([[1.0, 0.5, 0.], [0.2, 0.3, 1.5]])
+    R = np.array([[0.02, -0.01], [-0.01, 0.05]])
+    data = np.array([1.4, -2.5])
+    sc = mg.abc.LinearGaussian(np.zeros(3), S0, data, H, R)
+    smp = mg.abc.MetropolisedABCSMCSampler(ess_threshold_retain=0.8)
+    B, n = 64, 16384
+    keys = np.stack([np.array([0, 2000 + 64 * rank + b], np.uint32) for b in range(B)])
+    mg.abc.run_batched(sc, smp, n, keys[:2])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out = mg.abc.run_batched(sc, smp, n, keys)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    ess, res, it = out.ess.cpu().numpy(), out.resampled.cpu().numpy(), out.iterations.cpu().numpy()
+    sims = 0.0
+    for b in range(B):
+        for k in range(1, int(it[b]) + 1):
+            sims += n if res[b, k] else round(float(ess[b, k - 1]))
+    r = {"workload": "ABC-SMC, ABC LinearGaussian (d=3, dy=2, the reference's test model), MetropolisedABCSMCSampler "
+                     "(RandomWalkABC, retain 0.8, 1 move per iteration), 64 posteriors x 16384 particles to "
+                     "termination, seeded keys",
+         "metric": "simulations/s", "value": sims / dt, "unit": "simulations/s", "s_per_batch": dt,
+         "iterations_mean": float(it.mean())}
+    if rank == 0:
+        keep, _ = sc.derived()
+        p = {k: keep[k] for k in ("m0", "C0", "P0", "H", "L", "data")}
+        p["c0"] = keep["c0"]
+        t0 = time.perf_counter()
+        ref = oracle.abc_lg_run(p, n, keys[0], retain=0.8)
+        dtc = time.perf_counter() - t0
+        simc = sum(n if ref["resampled"][k] else round(float(ref["ess"][k - 1]))
+                   for k in range(1, ref["iterations"] + 1))
+        r["cpu_baseline"] = {"value": simc / dtc, "unit": "simulations/s", "cores": 1, "kind": "port",
+                             "sample": f"one posterior, N={n}, {ref['iterations']} iterations ({dtc:.1f} s), "
+                                       "oracle C (one thread)"}
+    return r
+
+
 def bench_nl1d(args, flush, rank):
     """Bootstrap filter on the one-dimensional non-linear benchmark model (initial_sd = sqrt 2,
     transition_sd = sqrt 10, likelihood_sd = 1), N = 2^20, T = 1000, ESS-triggered systematic
@@ -719,6 +771,7 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-smc", action="store_true")
     ap.add_argument("--no-nl1d", action="store_true")
+    ap.add_argument("--no-abc", action="store_true")
     ap.add_argument("--profile-run", action="store_true")
     ap.add_argument("--phase-trace", action="store_true")
     ap.add_argument("--profile-model", default="lg",
@@ -906,6 +959,8 @@ def main():
         line["smc_logreg"] = bench_smc(args, flush, rank)
     if not args.no_nl1d:
         line["nl1d"] = bench_nl1d(args, flush, rank)
+    if not args.no_abc:
+        line["abc_smc"] = bench_abc(args, rank)
     if rank == 0:
         v_cpu, cores, dt = cpu_baseline(n, args.cpu_steps)
         line["cpu_baseline"] = {"value": v_cpu, "unit": "particle-steps/s", "cores": cores, "kind": "port",
