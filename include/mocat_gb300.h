@@ -185,7 +185,11 @@ int mgb_pf_lg_run(const mgb_lg_model *model_host, int64_t n, int64_t T, const ui
  * ckpt_every steps from its checkpoint.
  * grad_dev (d*d + 2d floats): dA row-major, then d/dlog q_k, then d/dlog r_k.
  * log_z_dev (1 double) and resampled_dev (T int32) may be NULL.  scheme:
- * systematic or multinomial.  Synchronises `stream` once, between the passes. */
+ * systematic or multinomial.  Synchronises `stream` once, between the passes.
+ * The forward pass is one persistent cooperative launch (the whole GPU) for
+ * systematic resampling with even n <= 2^21; OR-ing MGB_RUN_LAUNCH_PER_STEP into
+ * `scheme` runs it one launch per phase instead, which lets gradients on
+ * several streams overlap (same results, log Z within 1e-6). */
 size_t mgb_pf_lg_grad_workspace(int64_t n, int64_t T, int32_t d, int32_t ckpt_every);
 int mgb_pf_lg_grad(const mgb_lg_model *model_host, int64_t n, int64_t T, const uint32_t *key_dev, const float *y_dev,
                    float ess_threshold, int scheme, int32_t ckpt_every, void *ws_dev, size_t ws_bytes,

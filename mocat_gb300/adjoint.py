@@ -27,7 +27,7 @@ from . import _dev, _lib
 from ._lib import call
 from .core import cdict
 from .resampling import SCHEMES
-from .ssm import TimeHomogenousLinearGaussian, _f32
+from .ssm import RUN_LAUNCH_PER_STEP, TimeHomogenousLinearGaussian, _f32
 
 LOG2PI = math.log(2.0 * math.pi)
 SUPPORTED_D = (1, 2, 3, 4, 5, 8, 10)
@@ -47,7 +47,7 @@ def _diag_model(A, log_q, log_r, C0, m0):
     return keep, s
 
 
-def _grad_call(s, d, y, key, n, ess_threshold, resampling, ckpt_every):
+def _grad_call(s, d, y, key, n, ess_threshold, resampling, ckpt_every, persistent=True):
     dev = _dev.device()
     y2 = _dev.as_f32(y).reshape(-1, d).contiguous()
     T = y2.shape[0]
@@ -59,15 +59,19 @@ def _grad_call(s, d, y, key, n, ess_threshold, resampling, ckpt_every):
     grad = torch.empty(d * d + 2 * d, dtype=torch.float32, device=dev)
     res = torch.empty(T, dtype=torch.int32, device=dev)
     call("mgb_pf_lg_grad", ctypes.byref(s), n, T, _dev.ptr(key), _dev.ptr(y2), float(ess_threshold),
-         SCHEMES[resampling], int(ckpt_every), _dev.ptr(ws), ws.numel(), _dev.ptr(logz), _dev.ptr(grad),
+         SCHEMES[resampling] | (0 if persistent else RUN_LAUNCH_PER_STEP), int(ckpt_every), _dev.ptr(ws),
+         ws.numel(), _dev.ptr(logz), _dev.ptr(grad),
          _dev.ptr(res), _dev.stream_ptr())
     return logz[0], grad, res
 
 
-def log_z_and_grad(ssm_scenario, y, random_key, n, ess_threshold=0.5, resampling="systematic", ckpt_every=32):
+def log_z_and_grad(ssm_scenario, y, random_key, n, ess_threshold=0.5, resampling="systematic", ckpt_every=32,
+                   persistent=True):
     """log Z of run_particle_filter_for_marginals(ssm_scenario, BootstrapFilter(), y, ..., n=n)
     and its gradient with respect to (transition_matrix, log diag transition_covariance,
-    log diag likelihood_covariance), ancestors held fixed.
+    log diag likelihood_covariance), ancestors held fixed.  persistent=False runs the taped
+    forward pass one launch per phase instead of one persistent launch (same gradient;
+    log Z within 1e-6, its float partial sums grouped differently).
 
     Returns cdict(log_z, grad_transition_matrix (d, d), grad_log_transition_covariance_diag (d,),
     grad_log_likelihood_covariance_diag (d,), resampled (T,))."""
@@ -75,7 +79,7 @@ def log_z_and_grad(ssm_scenario, y, random_key, n, ess_threshold=0.5, resampling
         raise NotImplementedError(f"{ssm_scenario.__class__.__name__}: no adjoint kernel for this model")
     _, s = ssm_scenario.derived()
     d = ssm_scenario.dim
-    lz, g, res = _grad_call(s, d, y, random_key, n, ess_threshold, resampling, ckpt_every)
+    lz, g, res = _grad_call(s, d, y, random_key, n, ess_threshold, resampling, ckpt_every, persistent)
     return cdict(log_z=lz, grad_transition_matrix=g[:d * d].reshape(d, d),
                  grad_log_transition_covariance_diag=g[d * d:d * d + d],
                  grad_log_likelihood_covariance_diag=g[d * d + d:], resampled=res.bool())
@@ -85,7 +89,8 @@ def log_z_and_grad_many(ssm_scenario, y, random_keys, n, ess_threshold=0.5, resa
                         ckpt_every=32, max_concurrent=8):
     """log_z_and_grad for B keys at once: each evaluation runs on its own CUDA stream,
     enqueued from its own host thread (the C library releases the interpreter lock),
-    so the kernels of different evaluations overlap on the GPU.
+    so the kernels of different evaluations overlap on the GPU.  The forward passes run
+    one launch per phase (log_z_and_grad(..., persistent=False) gives the same values).
 
     Returns cdict(log_z (B,), grad (B, d*d + 2d)) in the layout of mgb_pf_lg_grad."""
     import threading
@@ -114,8 +119,11 @@ def log_z_and_grad_many(ssm_scenario, y, random_keys, n, ess_threshold=0.5, resa
         try:
             with torch.cuda.stream(streams[j]):
                 for b in range(j, B, lanes):
+                    # launch per phase: the concurrent gradients overlap on the GPU, which one
+                    # whole-GPU persistent forward launch per gradient would prevent
                     call("mgb_pf_lg_grad", ctypes.byref(s), n, T, _dev.ptr(keys_dev[b]), _dev.ptr(y2),
-                         float(ess_threshold), SCHEMES[resampling], int(ckpt_every), _dev.ptr(ws[j]), ws[j].numel(),
+                         float(ess_threshold), SCHEMES[resampling] | RUN_LAUNCH_PER_STEP, int(ckpt_every),
+                         _dev.ptr(ws[j]), ws[j].numel(),
                          _dev.ptr(logz[b:b + 1]), _dev.ptr(grad[b]), None,
                          ctypes.c_void_p(streams[j].cuda_stream))
         except Exception as e:  # re-raised on the calling thread

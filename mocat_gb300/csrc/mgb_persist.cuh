@@ -40,7 +40,25 @@ struct PersistArgs {
   unsigned long long magic;       // floor((2^64 - 1) / n)
   uint64_t *trace;                // (T, 8) phase timestamps from block 0, or null
   const float *aux;               // (T,) per-step constant of the model (may be null)
+  // taped runs (the adjoint's forward pass): ancestors of every step into anc_hist
+  // (T, n) instead of anc, and (x, lw) of every ck_every-th step into the
+  // checkpoint slots ckx (T / ck_every, d, n) / ckl instead of the ping-pong buffers
+  int32_t *anc_hist;
+  int64_t ck_every;
+  float *ckx, *ckl;
 };
+
+// particles / log-weights of step s: the history, a checkpoint slot, or a ping-pong buffer
+__host__ __device__ inline float *persist_xbuf(const PersistArgs &a, int64_t s, int d) {
+  if (a.x_hist) return a.x_hist + (size_t)s * d * a.n;
+  if (a.ck_every && s % a.ck_every == 0) return a.ckx + (size_t)(s / a.ck_every) * d * a.n;
+  return (s & 1) ? a.xb : a.xa;
+}
+__host__ __device__ inline float *persist_lbuf(const PersistArgs &a, int64_t s) {
+  if (a.lw_hist) return a.lw_hist + (size_t)s * a.n;
+  if (a.ck_every && s % a.ck_every == 0) return a.ckl + (size_t)(s / a.ck_every) * a.n;
+  return (s & 1) ? a.lb : a.la;
+}
 
 // Persistent path: systematic resampling, even n, n <= 2^21 (tile prefixes in smem).
 inline bool persistent_ok(int64_t n, int scheme) {
@@ -107,14 +125,17 @@ inline int persist_setup(const RunWs &w, const PersistWs &pw, int64_t n, int64_t
   a.magic = ~0ull / (unsigned long long)n;
   a.trace = out ? out->trace : nullptr;
   a.aux = nullptr;
+  a.anc_hist = nullptr;
+  a.ck_every = 0;
+  a.ckx = a.ckl = nullptr;
   return OK;
 }
 
 // copies the last step's particles / log-weights to x_final / lw_final when asked
 inline int persist_finish(const PersistArgs &a, int d, const mgb_pf_outputs *out, cudaStream_t s) {
   const int64_t n = a.n, T = a.T;
-  const float *xl = a.x_hist ? a.x_hist + (size_t)(T - 1) * d * n : ((T - 1) & 1 ? a.xb : a.xa);
-  const float *ll = a.lw_hist ? a.lw_hist + (size_t)(T - 1) * n : ((T - 1) & 1 ? a.lb : a.la);
+  const float *xl = persist_xbuf(a, T - 1, d);
+  const float *ll = persist_lbuf(a, T - 1);
   if (out && out->x_final &&
       cudaMemcpyAsync(out->x_final, xl, sizeof(float) * d * n, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
     return ERR_CUDA;

@@ -37,6 +37,7 @@
 #include "mgb_lg.cuh"
 #include "mgb_pf_common.cuh"
 #include "mgb_lg_kernels.cuh"
+#include "mgb_persist.cuh"
 
 namespace mgb {
 
@@ -219,6 +220,7 @@ __global__ void k_adj_sum(const float *partial, int nb, int G, float *grad) {
 
 struct AdjWs {
   RunWs run;
+  PersistWs pw;
   int32_t *anc_hist;
   float *ckx, *ckl;
   float *segx, *segl, *sege;
@@ -234,6 +236,7 @@ struct AdjWs {
 static AdjWs carve_adj(Carver &c, int64_t n, int64_t T, int d, int scheme, int k) {
   AdjWs w;
   w.run = carve_run(c, n, T, d, scheme, true, true, true);
+  w.pw = carve_persist(c, n, T);
   const int64_t nck = (T + k - 1) / k;
   const int64_t nb = (n + ADJ_TPB - 1) / ADJ_TPB;
   w.anc_hist = c.take<int32_t>((size_t)T * n);
@@ -254,7 +257,7 @@ static AdjWs carve_adj(Carver &c, int64_t n, int64_t T, int d, int scheme, int k
 
 template <int D>
 static int grad_lg(const mgb_lg_model *m, int64_t n, int64_t T, const uint32_t *key, const float *y, float thr,
-                   int scheme, int k, void *ws, size_t ws_bytes, double *logz_out, float *grad_out,
+                   int scheme, bool persistent, int k, void *ws, size_t ws_bytes, double *logz_out, float *grad_out,
                    int32_t *resampled_out, cudaStream_t s) {
   const LGP<D, D> p = pack_lg<D, D>(m);
   if (!p.lq_diag || !p.p_diag || !p.h_eye) return ERR_UNSUPPORTED;
@@ -283,33 +286,54 @@ static int grad_lg(const mgb_lg_model *m, int64_t n, int64_t T, const uint32_t *
   ctl.thr_n = thr * (float)n;
   ctl.logn = log((double)n);
   ctl.logz_out = nullptr;
-  auto xbuf = [&](int64_t t) -> float * {
-    return t % k == 0 ? w.ckx + (size_t)(t / k) * D * n : (t & 1 ? r.xb : r.xa);
-  };
-  auto lbuf = [&](int64_t t) -> float * { return t % k == 0 ? w.ckl + (size_t)(t / k) * n : (t & 1 ? r.lb : r.la); };
-  const unsigned grid = (unsigned)((n + PF_TPB - 1) / PF_TPB);
-  const unsigned grid2 = (unsigned)((n / 2 + PF_TPB - 1) / PF_TPB);
-  k_lg_init<D, D, true><<<grid, PF_TPB, 0, s>>>(p, n, r.keys, y, xbuf(0), lbuf(0), ctl);
-  if ((st = launch_status())) return st;
-  for (int64_t t = 1; t < T; ++t) {
-    int32_t *anc = w.anc_hist + (size_t)t * n;
-    if ((st = launch_resample(lbuf(t - 1), n, scheme, &r.st->M, r.keys + 2 * t, 0, 0u, r.res_hist + t, r.rws, anc,
-                              nullptr, s)))
-      return st;
-    if (n % 2 == 0)
-      k_lg_step2<D, D, true><<<grid2, PF_TPB, 0, s>>>(p, n, r.keys + 2 * t, y + (size_t)t * D, xbuf(t - 1), anc,
-                                                      lbuf(t - 1), r.res_hist + t, xbuf(t), lbuf(t), ctl, t);
-    else
-      k_lg_step<D, D, true><<<grid, PF_TPB, 0, s>>>(p, n, r.keys + 2 * t, y + (size_t)t * D, xbuf(t - 1), anc,
-                                                    lbuf(t - 1), r.res_hist + t, xbuf(t), lbuf(t), ctl, t);
+  std::vector<int32_t> res((size_t)T + 1, 0);
+  if (persistent && persistent_ok(n, scheme)) {
+    // one persistent launch (k_pf_persist) writing the ancestor tape and the checkpoints
+    mgb_pf_outputs o = {};
+    o.log_z = logz_out;
+    PersistArgs a;
+    if ((st = persist_setup(r, w.pw, n, T, y, thr, r.ess_hist, &o, a, s))) return st;
+    a.anc_hist = w.anc_hist;
+    a.ck_every = k;
+    a.ckx = w.ckx;
+    a.ckl = w.ckl;
+    if ((st = run_lg_persistent(m, a, s))) return st;
+    if (resampled_out &&
+        cudaMemcpyAsync(resampled_out, a.res, sizeof(int32_t) * T, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+      return ERR_CUDA;
+    // the backward pass is laid out on the host from the resampling decisions
+    if (cudaMemcpyAsync(res.data(), a.res, sizeof(int32_t) * T, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+      return ERR_CUDA;
+  } else {
+    auto xbuf = [&](int64_t t) -> float * {
+      return t % k == 0 ? w.ckx + (size_t)(t / k) * D * n : (t & 1 ? r.xb : r.xa);
+    };
+    auto lbuf = [&](int64_t t) -> float * {
+      return t % k == 0 ? w.ckl + (size_t)(t / k) * n : (t & 1 ? r.lb : r.la);
+    };
+    const unsigned grid = (unsigned)((n + PF_TPB - 1) / PF_TPB);
+    const unsigned grid2 = (unsigned)((n / 2 + PF_TPB - 1) / PF_TPB);
+    k_lg_init<D, D, true><<<grid, PF_TPB, 0, s>>>(p, n, r.keys, y, xbuf(0), lbuf(0), ctl);
     if ((st = launch_status())) return st;
+    for (int64_t t = 1; t < T; ++t) {
+      int32_t *anc = w.anc_hist + (size_t)t * n;
+      if ((st = launch_resample(lbuf(t - 1), n, scheme, &r.st->M, r.keys + 2 * t, 0, 0u, r.res_hist + t, r.rws,
+                                anc, nullptr, s)))
+        return st;
+      if (n % 2 == 0)
+        k_lg_step2<D, D, true><<<grid2, PF_TPB, 0, s>>>(p, n, r.keys + 2 * t, y + (size_t)t * D, xbuf(t - 1), anc,
+                                                        lbuf(t - 1), r.res_hist + t, xbuf(t), lbuf(t), ctl, t);
+      else
+        k_lg_step<D, D, true><<<grid, PF_TPB, 0, s>>>(p, n, r.keys + 2 * t, y + (size_t)t * D, xbuf(t - 1), anc,
+                                                      lbuf(t - 1), r.res_hist + t, xbuf(t), lbuf(t), ctl, t);
+      if ((st = launch_status())) return st;
+    }
+    if ((st = launch_finish(r.st, r.res_hist, T, logz_out, resampled_out, s))) return st;
+    if (cudaMemcpyAsync(res.data(), r.res_hist, sizeof(int32_t) * (T + 1), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+      return ERR_CUDA;
   }
-  if ((st = launch_finish(r.st, r.res_hist, T, logz_out, resampled_out, s))) return st;
-  // the backward pass is laid out on the host from the resampling decisions
-  std::vector<int32_t> res((size_t)T + 1);
-  if (cudaMemcpyAsync(res.data(), r.res_hist, sizeof(int32_t) * (T + 1), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-      cudaStreamSynchronize(s) != cudaSuccess)
-    return ERR_CUDA;
 
   // ---- backward, segment by segment from the end
   const int G = D * D + 2 * D;
@@ -382,16 +406,25 @@ int mgb_pf_lg_grad(const mgb_lg_model *m, int64_t n, int64_t T, const uint32_t *
       !y || !ws || !grad || ckpt_every < 1)
     return ERR_BAD_ARG;
   if (m->dy != m->d) return ERR_UNSUPPORTED;
+  const bool persistent = !(scheme & MGB_RUN_LAUNCH_PER_STEP);
+  scheme &= ~MGB_RUN_LAUNCH_PER_STEP;
   if (scheme != MGB_RESAMPLE_SYSTEMATIC && scheme != MGB_RESAMPLE_MULTINOMIAL) return ERR_UNSUPPORTED;
   cudaStream_t s = (cudaStream_t)stream;
   switch (m->d) {
-    case 1: return grad_lg<1>(m, n, T, key, y, ess_threshold, scheme, ckpt_every, ws, ws_bytes, log_z, grad, resampled, s);
-    case 2: return grad_lg<2>(m, n, T, key, y, ess_threshold, scheme, ckpt_every, ws, ws_bytes, log_z, grad, resampled, s);
-    case 3: return grad_lg<3>(m, n, T, key, y, ess_threshold, scheme, ckpt_every, ws, ws_bytes, log_z, grad, resampled, s);
-    case 4: return grad_lg<4>(m, n, T, key, y, ess_threshold, scheme, ckpt_every, ws, ws_bytes, log_z, grad, resampled, s);
-    case 5: return grad_lg<5>(m, n, T, key, y, ess_threshold, scheme, ckpt_every, ws, ws_bytes, log_z, grad, resampled, s);
-    case 8: return grad_lg<8>(m, n, T, key, y, ess_threshold, scheme, ckpt_every, ws, ws_bytes, log_z, grad, resampled, s);
-    case 10: return grad_lg<10>(m, n, T, key, y, ess_threshold, scheme, ckpt_every, ws, ws_bytes, log_z, grad, resampled, s);
+    case 1: return grad_lg<1>(m, n, T, key, y, ess_threshold, scheme, persistent, ckpt_every, ws, ws_bytes, log_z, grad,
+                                    resampled, s);
+    case 2: return grad_lg<2>(m, n, T, key, y, ess_threshold, scheme, persistent, ckpt_every, ws, ws_bytes, log_z, grad,
+                                    resampled, s);
+    case 3: return grad_lg<3>(m, n, T, key, y, ess_threshold, scheme, persistent, ckpt_every, ws, ws_bytes, log_z, grad,
+                                    resampled, s);
+    case 4: return grad_lg<4>(m, n, T, key, y, ess_threshold, scheme, persistent, ckpt_every, ws, ws_bytes, log_z, grad,
+                                    resampled, s);
+    case 5: return grad_lg<5>(m, n, T, key, y, ess_threshold, scheme, persistent, ckpt_every, ws, ws_bytes, log_z, grad,
+                                    resampled, s);
+    case 8: return grad_lg<8>(m, n, T, key, y, ess_threshold, scheme, persistent, ckpt_every, ws, ws_bytes, log_z, grad,
+                                    resampled, s);
+    case 10: return grad_lg<10>(m, n, T, key, y, ess_threshold, scheme, persistent, ckpt_every, ws, ws_bytes, log_z, grad,
+                                    resampled, s);
     default: return ERR_UNSUPPORTED;
   }
 }

@@ -228,10 +228,11 @@ __global__ void __launch_bounds__(PP_TPB, 2) k_pf_persist(const __grid_constant_
   for (int64_t t = 0; t < a.T; ++t) {
     if (timed_out(a.err)) break;
     stamp(a, t, 0);
-    float *xo = a.x_hist ? a.x_hist + (size_t)t * D * n : ((t & 1) ? a.xb : a.xa);
-    float *lo = a.lw_hist ? a.lw_hist + (size_t)t * n : ((t & 1) ? a.lb : a.la);
-    const float *xi = t == 0 ? nullptr : (a.x_hist ? a.x_hist + (size_t)(t - 1) * D * n : ((t & 1) ? a.xa : a.xb));
-    const float *li = t == 0 ? nullptr : (a.lw_hist ? a.lw_hist + (size_t)(t - 1) * n : ((t & 1) ? a.la : a.lb));
+    float *xo = persist_xbuf(a, t, D);
+    float *lo = persist_lbuf(a, t);
+    const float *xi = t == 0 ? nullptr : persist_xbuf(a, t - 1, D);
+    const float *li = t == 0 ? nullptr : persist_lbuf(a, t - 1);
+
     const uint32_t k0 = __ldg(&a.keys[2 * t]), k1 = __ldg(&a.keys[2 * t + 1]);
     const float aux = a.aux ? __ldg(&a.aux[t]) : 0.0f;
     // observation of the step in shared memory (broadcast reads; keeps DY
@@ -264,8 +265,10 @@ __global__ void __launch_bounds__(PP_TPB, 2) k_pf_persist(const __grid_constant_
       } else if (i < h) {
         // both particles' ancestors and source states are requested before the
         // key-split ciphers run, so the cipher arithmetic hides the gather latency
-        const int64_t sa = res_cur ? (int64_t)__ldcg(&a.anc[i]) : i;
-        const int64_t sb = res_cur ? (int64_t)__ldcg(&a.anc[i + h]) : i + h;
+        // ancestors of this step (from the tape when one is recorded)
+        const int32_t *anc_t = a.anc_hist ? a.anc_hist + (size_t)t * n : a.anc;
+        const int64_t sa = res_cur ? (int64_t)__ldcg(&anc_t[i]) : i;
+        const int64_t sb = res_cur ? (int64_t)__ldcg(&anc_t[i + h]) : i + h;
         float xa_[D], xb_[D];
 #pragma unroll
         for (int j = 0; j < D; ++j) {
@@ -311,6 +314,8 @@ __global__ void __launch_bounds__(PP_TPB, 2) k_pf_persist(const __grid_constant_
 
     if (res_next) {
       const float M = o.M;
+      // ancestors filled for the next step (into the tape when one is recorded)
+      int32_t *anc_n = a.anc_hist ? a.anc_hist + (size_t)(t + 1) * n : a.anc;
       // ---- P3: per tile, exact fixed-point weights, their within-tile
       // inclusive prefixes (stored) and the tile sum.  The next tile's
       // log-weights are requested before this tile's scan, so a block with two
@@ -379,7 +384,7 @@ __global__ void __launch_bounds__(PP_TPB, 2) k_pf_persist(const __grid_constant_
       if (threadIdx.x == 0) sP[ntiles] = Q;
       const int degenerate = __ldcg(&a.degen[t]) || Q == 0;
       if (degenerate) {
-        for (int64_t i = blockIdx.x * (int64_t)PP_TPB + threadIdx.x; i < n; i += (int64_t)G * PP_TPB) a.anc[i] = 0;
+        for (int64_t i = blockIdx.x * (int64_t)PP_TPB + threadIdx.x; i < n; i += (int64_t)G * PP_TPB) anc_n[i] = 0;
         if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(a.err, EB_DEGENERATE);
       } else {
         const uint32_t m23 = bits_at(__ldg(&a.keys[2 * (t + 1)]), __ldg(&a.keys[2 * (t + 1) + 1]), 1, 0) >> 9;
@@ -422,7 +427,7 @@ __global__ void __launch_bounds__(PP_TPB, 2) k_pf_persist(const __grid_constant_
           const int cnt = cnt_valid;
           const int un = u + (int)G;
           if (un < (int)utot) unit_load(un, ntiles, n, sU, a.cloc, tile, cnt_valid, cv);
-          merge_fill(sC, cnt, c, kb, (int)(ke - kb), base, n, a.anc);
+          merge_fill(sC, cnt, c, kb, (int)(ke - kb), base, n, anc_n);
           __syncthreads();
           if (a.trace && t == 1 && blockIdx.x == 0 && threadIdx.x == 0 && done < 1024)
             a.trace[a.T * 10 + 1024 + done] = globaltimer_ns() - a.trace[t * 10 + 6];
