@@ -677,7 +677,8 @@ def profile_main(args):
 
 def profile_other(args):
     """--profile-run for the other kernels' captures (one call of the public API each):
-      adjoint  mocat_gb300.adjoint.log_z_and_grad on the headline model, n = --n, T = --T;
+      adjoint  mocat_gb300.adjoint.log_z_and_grad on the headline model, n = --n, T = --T
+               (--launch-per-step: the forward pass one launch per phase);
       lgstep   the headline filter on the launch-per-step path (k_lg_step2 per step), n = --n, T = --T;
       logreg   LogisticRegression.likelihood_potential_and_grad, 1e5 x 50 seeded data, P = --n
                parameter rows, --profile-precision bf16 | fp32 (three timed calls);
@@ -691,7 +692,8 @@ def profile_other(args):
         ssm = mg.ssm.TimeHomogenousLinearGaussian(**model_arrays())
         y = ssm.simulate(np.arange(T), mg.random.PRNGKey(0)).y.contiguous()
         if m == "adjoint":
-            o = mg.adjoint.log_z_and_grad(ssm, y, mg.random.PRNGKey(1), n, ckpt_every=32)
+            o = mg.adjoint.log_z_and_grad(ssm, y, mg.random.PRNGKey(1), n, ckpt_every=32,
+                                          persistent=not args.launch_per_step)
         else:
             o = mg.ssm.run_particle_filter_for_marginals(ssm, mg.ssm.BootstrapFilter(), y, np.arange(T),
                                                          mg.random.PRNGKey(1), n=n, history=False, persistent=False)
@@ -777,6 +779,7 @@ def main():
     ap.add_argument("--profile-model", default="lg",
                     choices=["lg", "nl1d", "adjoint", "lgstep", "logreg", "svbatch"])
     ap.add_argument("--profile-precision", default="bf16", choices=["bf16", "fp32"])
+    ap.add_argument("--launch-per-step", action="store_true")
     ap.add_argument("--smc-B", type=int, default=16)
     ap.add_argument("--smc-iters", type=int, default=3)
     ap.add_argument("--adj-n", type=int, default=65536)
