@@ -953,6 +953,21 @@ def main():
                                               "frac": k_alg / k_t / 1e9 / peak}},
             "gpu_launches": args.steps * 3,  # k_setup_keys, k_pf_persist, k_or_err per run
             "clocks": clk.summary()}
+    # the binding resource: instruction issue.  Warp instructions per step from the committed
+    # ncu capture (T = 20, the per-step count does not depend on T) against 4 issue slots per
+    # SM per cycle at the sampled SM clock.
+    if issue and "per step" in issue:
+        import re
+        mt = re.search(r"~([0-9.]+e[0-9]+) per step", issue)
+        if mt:
+            clk_mhz = line["clocks"]["sm_mhz"] or 2070.0
+            props = torch.cuda.get_device_properties(dev)
+            ipeak = props.multi_processor_count * 4 * clk_mhz * 1e6
+            iach = float(mt.group(1)) * T / run_s
+            line["roofline"]["issue"] = {"achieved": iach, "peak": ipeak, "unit": "warp-instructions/s",
+                                         "frac": iach / ipeak,
+                                         "source": "warp instructions per step from profiles/"
+                                                   "k_pf_persist_lg_d10_n1M.md; peak = SMs x 4 x SM clock"}
     line["config1"] = bench_config1(args, rank)
     if not args.no_batched:
         line["batched_sv"] = bench_sv_batch(args, flush, rank)
