@@ -148,11 +148,12 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
 //   s_lin += max(w, 0); prod *= (1 + exp(-|z|)) (one log2 of the product per 32 columns);
 //   gradient operand r = sigmoid(z) - y = tanh(z / 2) / 2 + (1/2 - y), packed bf16x2.
 // A padding column passes z = -inf, y = 0: it adds 0 to both sums.
-__device__ __forceinline__ void epi_pair(float z0, float z1, uint32_t y0, uint32_t y1, float &s_lin, float &prod,
-                                         uint32_t &packed) {
-  const float w0 = __uint_as_float(__float_as_uint(z0) ^ (y0 << 31));
-  const float w1 = __uint_as_float(__float_as_uint(z1) ^ (y1 << 31));
-  s_lin += fmaxf(w0, 0.0f) + fmaxf(w1, 0.0f);
+// softplus(w) = max(w, 0) + log(1 + e^-|z|) with w = (1 - 2y) z, and sum_j max(w_j, 0) =
+// (sum_j w_j + sum_j |z_j|) / 2 where sum_j w_j = beta . u, u = X^T (1 - 2y) (added once per
+// row): per element only |z| is accumulated (a0, a1: |z| of valid columns, 0 past n_data)
+__device__ __forceinline__ void epi_pair(float z0, float z1, float a0, float a1, uint32_t y0, uint32_t y1,
+                                         float &s_abs, float &prod, uint32_t &packed) {
+  s_abs += a0 + a1;
   const float e0 = exp2f_approx(-1.4426950408889634f * fabsf(z0));
   const float e1 = exp2f_approx(-1.4426950408889634f * fabsf(z1));
   prod = fmaf(prod, e0, prod);
@@ -167,6 +168,7 @@ __device__ __forceinline__ void epi_pair(float z0, float z1, uint32_t y0, uint32
 struct TCArgs {
   const float *beta;
   const float *y;
+  const float *u;  // (TC_K) X^T (1 - 2y) from the bf16 rows
   const int32_t *active;
   float *lik, *grad;
   int *err;
@@ -329,24 +331,27 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_logreg_tc(const __grid_consta
       const int nvalid = (int)min((int64_t)32, a.n_data - i0);
       // labels of this warp's 32 columns as a bit mask; columns past n_data count as y = 0 with z = 0
       const uint32_t ymask = __ballot_sync(0xffffffffu, ycur != 0.0f);
-      float s_lin = 0.0f, prod = 1.0f;
+      float s_abs = 0.0f, prod = 1.0f;
       uint32_t packed[16];
       if (nvalid == 32) {
 #pragma unroll
-        for (int j = 0; j < 32; j += 2)
-          epi_pair(__uint_as_float(v[j]), __uint_as_float(v[j + 1]), (ymask >> j) & 1u, (ymask >> (j + 1)) & 1u,
-                   s_lin, prod, packed[j >> 1]);
+        for (int j = 0; j < 32; j += 2) {
+          const float z0 = __uint_as_float(v[j]), z1 = __uint_as_float(v[j + 1]);
+          epi_pair(z0, z1, fabsf(z0), fabsf(z1), (ymask >> j) & 1u, (ymask >> (j + 1)) & 1u, s_abs, prod,
+                   packed[j >> 1]);
+        }
       } else {
 #pragma unroll
         for (int j = 0; j < 32; j += 2) {
           const bool ok0 = j < nvalid, ok1 = j + 1 < nvalid;
-          epi_pair(ok0 ? __uint_as_float(v[j]) : -INFINITY, ok1 ? __uint_as_float(v[j + 1]) : -INFINITY,
-                   ok0 ? (ymask >> j) & 1u : 0u, ok1 ? (ymask >> (j + 1)) & 1u : 0u, s_lin, prod, packed[j >> 1]);
+          const float z0 = __uint_as_float(v[j]), z1 = __uint_as_float(v[j + 1]);
+          epi_pair(ok0 ? z0 : -INFINITY, ok1 ? z1 : -INFINITY, ok0 ? fabsf(z0) : 0.0f, ok1 ? fabsf(z1) : 0.0f,
+                   ok0 ? (ymask >> j) & 1u : 0u, ok1 ? (ymask >> (j + 1)) & 1u : 0u, s_abs, prod, packed[j >> 1]);
           if (!ok1) packed[j >> 1] &= ok0 ? 0x0000FFFFu : 0u;
         }
       }
       const float s_l2 = log2f_approx(prod);
-      const float tsum = fmaf(0.69314718055994531f, s_l2, s_lin);
+      const float tsum = fmaf(0.69314718055994531f, s_l2, 0.5f * s_abs);
       unsigned char *sub = sR + rb * 2 * TILE_BYTES + (cg >> 1) * TILE_BYTES;
 #pragma unroll
       for (int m = 0; m < 4; ++m) {
@@ -382,9 +387,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_logreg_tc(const __grid_consta
   // potential: the four column groups of each row
   if (threadIdx.x < TC_ROWS && grad_ok_s) {
     const int64_t p = row0 + threadIdx.x;
-    if (p < a.P && (!a.active || a.active[p / a.N]))
+    if (p < a.P && (!a.active || a.active[p / a.N])) {
+      // 0.5 sum_j w_j = 0.5 bf16(beta_p) . u (the MMA's operands)
+      float bu = 0.0f;
+      for (int k = 0; k < a.d; ++k) bu = fmaf(__bfloat162float(__float2bfloat16_rn(a.beta[p * a.d + k])), a.u[k], bu);
       a.lik[p] = (float)(pot_s[0][threadIdx.x] + pot_s[1][threadIdx.x] + pot_s[2][threadIdx.x] +
-                         pot_s[3][threadIdx.x]);
+                         pot_s[3][threadIdx.x] + 0.5 * (double)bu);
+    }
   }
   if (warp == 1) {
     tc_fence_after();
@@ -414,11 +423,37 @@ static int encode_xmap(CUtensorMap *map, const uint16_t *Xb, int64_t n_data) {
   return r == CUDA_SUCCESS ? OK : ERR_BAD_ARG;
 }
 
-size_t logreg_tc_workspace(int64_t, int64_t, int) { return 256; }
+// u = X^T (1 - 2y) over the bf16 rows, in a fixed order: block b sums rows of its chunk
+// (4 row lanes per feature, then the lanes in order), a second kernel sums the blocks in order
+constexpr int TC_UBLOCKS = 64;
+__global__ void __launch_bounds__(256) k_logreg_u_part(const uint16_t *Xb, const float *y, int64_t n_data,
+                                                        float *partial) {
+  __shared__ float sm[4][TC_K];
+  const int k = threadIdx.x & (TC_K - 1), r = threadIdx.x / TC_K;
+  const int64_t chunk = (n_data + TC_UBLOCKS - 1) / TC_UBLOCKS;
+  const int64_t j0 = blockIdx.x * chunk, j1 = j0 + chunk < n_data ? j0 + chunk : n_data;
+  float acc = 0.0f;
+  for (int64_t j = j0 + r; j < j1; j += 4) {
+    const float x = __uint_as_float((uint32_t)Xb[j * TC_K + k] << 16);
+    acc = __ldg(&y[j]) != 0.0f ? acc - x : acc + x;
+  }
+  sm[r][k] = acc;
+  __syncthreads();
+  if (threadIdx.x < TC_K) partial[blockIdx.x * TC_K + k] = ((sm[0][k] + sm[1][k]) + sm[2][k]) + sm[3][k];
+}
+__global__ void k_logreg_u_sum(const float *partial, float *u) {
+  float s = 0.0f;
+  for (int b = 0; b < TC_UBLOCKS; ++b) s += partial[b * TC_K + threadIdx.x];
+  u[threadIdx.x] = s;
+}
+
+// err word, block partials of u, u
+size_t logreg_tc_workspace(int64_t, int64_t, int) { return 256 + sizeof(float) * (TC_UBLOCKS + 1) * TC_K; }
 
 int logreg_tc(const SMCData &dat, const float *beta, int64_t P, const int32_t *active, int N, float *lik, float *grad,
               void *ws, size_t ws_bytes, cudaStream_t s) {
-  if (dat.d > TC_K || !dat.Xb || ((uintptr_t)dat.Xb & 15u) || ws_bytes < 256) return ERR_BAD_ARG;
+  if (dat.d > TC_K || !dat.Xb || ((uintptr_t)dat.Xb & 15u) || ws_bytes < logreg_tc_workspace(P, dat.n_data, dat.d))
+    return ERR_BAD_ARG;
   CUtensorMap map;
   int st = encode_xmap(&map, dat.Xb, dat.n_data);
   if (st) return st;
@@ -429,8 +464,12 @@ int logreg_tc(const SMCData &dat, const float *beta, int64_t P, const int32_t *a
     attr = true;
   }
   int *err = (int *)ws;
+  float *partial = (float *)((char *)ws + 256), *u = partial + TC_UBLOCKS * TC_K;
   if (cudaMemsetAsync(err, 0, sizeof(int), s) != cudaSuccess) return ERR_CUDA;
-  TCArgs a{beta, dat.y, active, lik, grad, err, P, dat.n_data, dat.d, N > 0 ? N : (int)P};
+  k_logreg_u_part<<<TC_UBLOCKS, 256, 0, s>>>(dat.Xb, dat.y, dat.n_data, partial);
+  k_logreg_u_sum<<<1, TC_K, 0, s>>>(partial, u);
+  if ((st = launch_status())) return st;
+  TCArgs a{beta, dat.y, u, active, lik, grad, err, P, dat.n_data, dat.d, N > 0 ? N : (int)P};
   const unsigned grid = (unsigned)((P + TC_ROWS - 1) / TC_ROWS);
   k_logreg_tc<<<grid, TC_THREADS, TC_SMEM, s>>>(map, a);
   return launch_status();
