@@ -436,6 +436,32 @@ int mgb_smc_logreg_prior_scale_grad(const mgb_smc_logreg_config *cfg, void *ws_d
 int mgb_smc_logreg_step(const mgb_smc_logreg_config *cfg, const float *X_dev, const float *y_dev,
                         const void *Xbf16_dev, int64_t n_data, void *ws_dev, size_t ws_bytes, void *stream);
 
+/* ---------------------------------------------- Kalman filter and smoother
+ * run_kalman_filter_for_marginals / run_kalman_smoother_for_marginals
+ * (mocat/src/ssm/linear_gaussian/kalman.py:16-57, 60-104) for B observation sequences of the
+ * same time-homogeneous model at once, float32 as the reference computes:
+ *   t = 0: K = C0 H' (H C0 H' + R)^-1, mean = m0 + K (y_0 - H m0), cov = C0 - K H C0, where C0 is
+ *          the initial covariance square root (the reference uses it as the covariance at t = 0);
+ *   t > 0: predict F mean, F cov F' + Q, then the same update;
+ *   smoother: A = F P_t F' + Q, G = P_t F' A^-1, mean_t += G (mean_{t+1}^s - F mean_t),
+ *             cov_t += G (cov_{t+1}^s - A) G'.
+ * Matrices are host pointers, row-major float32: F, Q (d x d), H (dy x d), R (dy x dy), m0 (d),
+ * C0 (d x d).  y (B, T, dy); means (B, T, d); covs (B, T, d, d).  loglik (B doubles, may be NULL):
+ * the prediction-error log-likelihood sum_t log N(y_t; H mean_{t|t-1}, S_t) (new).
+ * lag_ones (B, T-1, d, d; may be NULL) replaces run_kalman_smoother_for_marginals_and_lag_ones
+ * (kalman.py:60-94): <mean_t^f, mean_{t+1}^s> + G (cov_{t+1}^s + <mean_{t+1}^s - mean_{t+1}^f,
+ * mean_{t+1}^s>), the reference's 1-D `@` products being dot products.
+ * (d, dy) as for mgb_lg_model. */
+typedef struct {
+  int32_t d, dy;
+  const float *F, *Q, *H, *R, *m0, *C0;
+} mgb_kalman_model;
+int mgb_kalman_filter(const mgb_kalman_model *model_host, int64_t B, int64_t T, const float *y_dev,
+                      float *means_dev, float *covs_dev, double *loglik_dev, void *stream);
+int mgb_kalman_smoother(const mgb_kalman_model *model_host, int64_t B, int64_t T, const float *filter_means_dev,
+                        const float *filter_covs_dev, float *means_dev, float *covs_dev, float *lag_ones_dev,
+                        void *stream);
+
 /* ------------------------------------------------ ABC-SMC (likelihood-free)
  * MetropolisedABCSMCSampler (mocat/src/abc/smc.py:101-245) with RandomWalkABC moves and the
  * Metropolis correction (mocat/src/abc/mcmc.py:59-103, mocat/src/mcmc/metropolis.py:48-70),

@@ -62,6 +62,11 @@ class ABCViews(ctypes.Structure):
                [("hist_len", ctypes.c_int32)]
 
 
+class KalmanModel(ctypes.Structure):
+    _fields_ = [("d", ctypes.c_int32), ("dy", ctypes.c_int32)] + \
+               [(k, ctypes.c_void_p) for k in ("F", "Q", "H", "R", "m0", "C0")]
+
+
 class LGTransition(ctypes.Structure):
     _fields_ = [("d", ctypes.c_int32), ("F", ctypes.c_void_p), ("Pq", ctypes.c_void_p), ("cq", ctypes.c_float)]
 
@@ -144,6 +149,8 @@ _SIGNATURES = {
     "mgb_abc_smc_views": ([ctypes.POINTER(ABCConfig), ctypes.c_int32, _P, ctypes.POINTER(ABCViews)], _I32),
     "mgb_abc_smc_init": ([ctypes.POINTER(ABCConfig), ctypes.POINTER(ABCModel), _P, _P, _SZ, _P], _I32),
     "mgb_abc_smc_step": ([ctypes.POINTER(ABCConfig), ctypes.POINTER(ABCModel), _P, _SZ, _P], _I32),
+    "mgb_kalman_filter": ([ctypes.POINTER(KalmanModel), _I64, _I64, _P, _P, _P, _P, _P], _I32),
+    "mgb_kalman_smoother": ([ctypes.POINTER(KalmanModel), _I64, _I64, _P, _P, _P, _P, _P, _P], _I32),
     "mgb_logreg_workspace": ([_I64, _I64, ctypes.c_int32, _I32], _SZ),
     "mgb_logreg_potential_grad": ([_P, _P, _I64, ctypes.c_int32, _P, _I64, _P, _P, _I32, _P, _P, _SZ, _P], _I32),
     "mgb_smc_logreg_workspace": ([ctypes.POINTER(SMCConfig), _I64], _SZ),

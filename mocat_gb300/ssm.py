@@ -515,6 +515,83 @@ def _run_from(ssm_scenario, s, initial_sample, y2, t, key, ess_threshold, resamp
                  resampled=torch.tensor(resd, device=dev))
 
 
+def _kalman_struct(ssm_scenario):
+    """float32 F, Q, H, R, m0 and the initial covariance square root (the reference's t = 0 covariance)"""
+    keep = dict(F=_f32(ssm_scenario.transition_matrix), Q=_f32(ssm_scenario.transition_covariance),
+                H=_f32(ssm_scenario.likelihood_matrix), R=_f32(ssm_scenario.likelihood_covariance),
+                m0=_f32(ssm_scenario.initial_mean), C0=_f32(np.linalg.cholesky(ssm_scenario.initial_covariance)))
+    s = _lib.KalmanModel(ssm_scenario.dim, ssm_scenario.dim_obs,
+                         *[keep[k].ctypes.data for k in ("F", "Q", "H", "R", "m0", "C0")])
+    return keep, s
+
+
+def _check_kalman(ssm_scenario):
+    if not isinstance(ssm_scenario, TimeHomogenousLinearGaussian):
+        raise NotImplementedError(f"{ssm_scenario.__class__.__name__}: the Kalman filter takes a linear-Gaussian model")
+    if not ssm_scenario.gpu_supported():
+        raise NotImplementedError(f"(d, dy) = ({ssm_scenario.dim}, {ssm_scenario.dim_obs}) not compiled")
+
+
+def run_kalman_filter_for_marginals(lgssm_scenario, y, t=None, return_log_likelihood=False):
+    """kalman.py:16-57 on the GPU: (means (T, d), covs (T, d, d)) filtered marginals.  y may carry a
+    leading batch axis (B, T, dy): B sequences of the same model in one launch, outputs (B, T, ...).
+    return_log_likelihood=True appends the prediction-error log-likelihood (float64, (B,) or scalar)."""
+    _check_kalman(lgssm_scenario)
+    d, dy = lgssm_scenario.dim, lgssm_scenario.dim_obs
+    yy = _dev.as_f32(y)
+    if yy.dim() == 1:
+        yy = yy.reshape(-1, dy)
+    batched = yy.dim() == 3
+    yy = (yy if batched else yy[None]).contiguous()
+    B, T = yy.shape[0], yy.shape[1]
+    dev = yy.device
+    means = torch.empty((B, T, d), dtype=torch.float32, device=dev)
+    covs = torch.empty((B, T, d, d), dtype=torch.float32, device=dev)
+    ll = torch.empty(B, dtype=torch.float64, device=dev)
+    _, s = _kalman_struct(lgssm_scenario)
+    call("mgb_kalman_filter", ctypes.byref(s), B, T, _dev.ptr(yy), _dev.ptr(means), _dev.ptr(covs), _dev.ptr(ll),
+         _dev.stream_ptr())
+    out = (means, covs, ll) if batched else (means[0], covs[0], ll[0])
+    return out if return_log_likelihood else out[:2]
+
+
+def run_kalman_smoother_for_marginals_and_lag_ones(lgssm_scenario, y, t=None, filter_output=None):
+    """kalman.py:60-94 on the GPU: (means, covs, lag_ones) smoothed marginals and the lag-one
+    terms (T-1, d, d), in the batched form of run_kalman_filter_for_marginals."""
+    _check_kalman(lgssm_scenario)
+    if filter_output is None:
+        filter_output = run_kalman_filter_for_marginals(lgssm_scenario, y, t)
+    fm, fc = (_dev.as_f32(a) for a in filter_output[:2])
+    batched = fm.dim() == 3
+    fm = (fm if batched else fm[None]).contiguous()
+    fc = (fc if batched else fc[None]).contiguous()
+    B, T, d = fm.shape
+    sm, sc = torch.empty_like(fm), torch.empty_like(fc)
+    lag = torch.empty((B, max(T - 1, 0), d, d), dtype=torch.float32, device=fm.device)
+    _, s = _kalman_struct(lgssm_scenario)
+    call("mgb_kalman_smoother", ctypes.byref(s), B, T, _dev.ptr(fm), _dev.ptr(fc), _dev.ptr(sm), _dev.ptr(sc),
+         _dev.ptr(lag) if T > 1 else None, _dev.stream_ptr())
+    return (sm, sc, lag) if batched else (sm[0], sc[0], lag[0])
+
+
+def run_kalman_smoother_for_marginals(lgssm_scenario, y, t=None, filter_output=None):
+    """kalman.py:97-104 on the GPU: (means, covs) smoothed marginals (the batched form as
+    run_kalman_filter_for_marginals)."""
+    _check_kalman(lgssm_scenario)
+    if filter_output is None:
+        filter_output = run_kalman_filter_for_marginals(lgssm_scenario, y, t)
+    fm, fc = (_dev.as_f32(a) for a in filter_output[:2])
+    batched = fm.dim() == 3
+    fm = (fm if batched else fm[None]).contiguous()
+    fc = (fc if batched else fc[None]).contiguous()
+    B, T = fm.shape[0], fm.shape[1]
+    sm, sc = torch.empty_like(fm), torch.empty_like(fc)
+    _, s = _kalman_struct(lgssm_scenario)
+    call("mgb_kalman_smoother", ctypes.byref(s), B, T, _dev.ptr(fm), _dev.ptr(fc), _dev.ptr(sm), _dev.ptr(sc), None,
+         _dev.stream_ptr())
+    return (sm, sc) if batched else (sm[0], sc[0])
+
+
 def _transition_struct(ssm_scenario):
     """F, transition_precision_sqrt = inv(chol(Q)), and the normaliser of the transition
     potential, computed as reset_covariance does (mocat/src/utils.py:247-262)."""

@@ -16,6 +16,9 @@ propagates the tangents (dm, dP) of every parameter direction through the same
 recursion (forward-mode sensitivities), vectorised over directions.
 (The reference quirk of using the initial covariance *square root* as the
 covariance, kalman.py:20,26-28, only matters when S0 != I; this oracle uses S0.)
+
+filter_marginals / smoother_marginals restate the reference's marginal filter and RTS
+smoother as written, that quirk included, with the lag-one terms of kalman.py:60-94.
 """
 import numpy as np
 
@@ -96,3 +99,46 @@ def loglik_and_grad(F, logq, H, logr, m0, S0, y):
         P = P - K @ HP
         P = 0.5 * (P + P.T)
     return ll, g
+
+
+def filter_marginals(F, Q, H, R, m0, C0, y):
+    """run_kalman_filter_for_marginals (kalman.py:16-57) in float64, as the reference writes it:
+    at t = 0 the initial covariance *square root* C0 stands in for the covariance; no
+    symmetrisation.  Returns (means (T, d), covs (T, d, d), prediction-error log-likelihood)."""
+    F, Q, H, R, m0, C0 = (np.asarray(a, np.float64) for a in (F, Q, H, R, m0, C0))
+    y = np.asarray(y, np.float64).reshape(len(y), -1)
+    dy = H.shape[0]
+    mus, covs, ll = [], [], 0.0
+    m, P = m0, C0
+    for t in range(y.shape[0]):
+        if t > 0:
+            m = F @ m
+            P = F @ P @ F.T + Q
+        S = H @ P @ H.T + R
+        Si = np.linalg.inv(S)
+        e = y[t] - H @ m
+        ll += -0.5 * (dy * LOG2PI + np.linalg.slogdet(S)[1] + e @ Si @ e)
+        K = P @ H.T @ Si
+        m = m + K @ e
+        P = P - K @ H @ P
+        mus.append(m)
+        covs.append(P)
+    return np.stack(mus), np.stack(covs), ll
+
+
+def smoother_marginals(F, Q, means, covs, lag_ones=False):
+    """run_kalman_smoother_for_marginals (kalman.py:60-104) in float64 from filter output;
+    lag_ones=True also returns the lag-one terms of kalman.py:83, whose 1-D `@` products
+    are dot products."""
+    F, Q = np.asarray(F, np.float64), np.asarray(Q, np.float64)
+    means, covs = np.asarray(means, np.float64), np.asarray(covs, np.float64)
+    T, d = means.shape
+    sm, sc = means.copy(), covs.copy()
+    lag = np.zeros((max(T - 1, 0), d, d))
+    for t in range(T - 2, -1, -1):
+        A = F @ covs[t] @ F.T + Q
+        G = covs[t] @ F.T @ np.linalg.inv(A)
+        lag[t] = means[t] @ sm[t + 1] + G @ (sc[t + 1] + (sm[t + 1] - means[t + 1]) @ sm[t + 1])
+        sm[t] = means[t] + G @ (sm[t + 1] - F @ means[t])
+        sc[t] = covs[t] + G @ (sc[t + 1] - A) @ G.T
+    return (sm, sc, lag) if lag_ones else (sm, sc)
