@@ -304,6 +304,48 @@ int mgb_transition_potential_pairs_nl1d(const mgb_nl1d_model *model_host, int64_
                                         const float *x1_dev, float t_previous, const float *lw_dev, float *out_dev,
                                         void *stream);
 
+/* ------------------------------ backward simulation and stitching by rejection
+ * maximum_rejections > 0: backward_simulation_rejection (mocat/src/ssm/backward.py:172-214,
+ * rejection_resampling :54-169) and rejection_stitching (mocat/src/ssm/online_smoothing.py:59-175,
+ * called by fixed_lag_stitching :178-209).  n items with fixed states each draw an index into a pool
+ * of Np particles with log-weights lw, accepting pair (i, j) with probability
+ * exp(-transition_potential) / bound:
+ *   (c0, u0, k0) = split(key, 3); idx = categorical(c0, lw, (n,)); dens_i = exp(-potential(i, idx_i));
+ *   bound = max dens > init_bound_param ? max dens * bound_inflation : init_bound_param;
+ *   unaccepted_i = uniform(u0, (n,))_i > dens_i / bound; key_i = split(k0, n)_i; evals = n;
+ *   up to maximum_rejections - 1 rounds while any item is unaccepted: evals += #unaccepted; each
+ *   unaccepted item: (key_i, c, u) = split(key_i, 3), idx_i = categorical(c, lw), dens_i, accept
+ *   unless uniform(u) > dens_i / bound; if the round's max dens > bound: bound = max dens *
+ *   bound_inflation and every item is unaccepted again;
+ *   then each unaccepted item: idx_i = categorical(key_i, lw - potential(i, .)); evals += Np * #unaccepted.
+ * Backward simulation: items = the M samples at t+1, pool = the N filter particles at t, keys and
+ * the last step as mgb_ffbsi_lg; evals (T, int64, device): evals[0] = 0, evals[t+1] = step t's
+ * count (the reference's append(0, ...) layout).  Stitching: items = x0 (M), pool = x1 (M),
+ * evals (1, int64, device).  These entry points synchronise their stream (the host reads a
+ * device flag between groups of rounds); not for stream capture. */
+typedef struct {
+  int32_t maximum_rejections; /* >= 1 */
+  float init_bound_param;     /* transition_dens_bound_parameter */
+  float bound_inflation;
+} mgb_rejection_config;
+size_t mgb_ffbsi_rejection_workspace(int64_t N, int64_t M, int64_t T, int32_t d);
+size_t mgb_stitch_rejection_workspace(int64_t M, int32_t d);
+int mgb_ffbsi_rejection_lg(const mgb_lg_transition *transition_host, const mgb_rejection_config *cfg_host, int64_t T,
+                           int64_t N, int64_t M, const float *x_hist_dev, const float *lw_hist_dev,
+                           const uint32_t *key_dev, float *out_dev, int32_t *idx_dev, int64_t *evals_dev,
+                           void *ws_dev, size_t ws_bytes, void *stream);
+int mgb_ffbsi_rejection_nl1d(const mgb_nl1d_model *model_host, const mgb_rejection_config *cfg_host, int64_t T,
+                             int64_t N, int64_t M, const float *x_hist_dev, const float *lw_hist_dev,
+                             const float *t_dev, const uint32_t *key_dev, float *out_dev, int32_t *idx_dev,
+                             int64_t *evals_dev, void *ws_dev, size_t ws_bytes, void *stream);
+int mgb_stitch_rejection_lg(const mgb_lg_transition *transition_host, const mgb_rejection_config *cfg_host, int64_t M,
+                            const float *x0_dev, const float *x1_dev, const float *lw1_dev, const uint32_t *key_dev,
+                            int32_t *idx_dev, int64_t *evals_dev, void *ws_dev, size_t ws_bytes, void *stream);
+int mgb_stitch_rejection_nl1d(const mgb_nl1d_model *model_host, const mgb_rejection_config *cfg_host, int64_t M,
+                              const float *x0_dev, const float *x1_dev, const float *lw1_dev, float t_previous,
+                              const uint32_t *key_dev, int32_t *idx_dev, int64_t *evals_dev, void *ws_dev,
+                              size_t ws_bytes, void *stream);
+
 /* ------------------------------- many stochastic-volatility filters at once
  * B independent run_particle_filter_for_marginals calls (mocat/src/ssm/filtering.py:255-324)
  * with BootstrapFilter on StochasticVolatility, d = 1

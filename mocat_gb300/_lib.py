@@ -71,6 +71,11 @@ class LGTransition(ctypes.Structure):
     _fields_ = [("d", ctypes.c_int32), ("F", ctypes.c_void_p), ("Pq", ctypes.c_void_p), ("cq", ctypes.c_float)]
 
 
+class RejectionConfig(ctypes.Structure):
+    _fields_ = [("maximum_rejections", ctypes.c_int32), ("init_bound_param", ctypes.c_float),
+                ("bound_inflation", ctypes.c_float)]
+
+
 class SVModel(ctypes.Structure):
     _fields_ = [("phi", ctypes.c_float), ("bsig", ctypes.c_float), ("r2", ctypes.c_float), ("cB", ctypes.c_float),
                 ("c0", ctypes.c_float), ("m0", ctypes.c_float)]
@@ -144,6 +149,16 @@ _SIGNATURES = {
                          ctypes.POINTER(PFOutputs), _P], _I32),
     "mgb_ffbsi_nl1d": ([ctypes.POINTER(NL1DModel), _I64, _I64, _I64, _P, _P, _P, _P, _P, _P, _P, _SZ, _P], _I32),
     "mgb_stitch_nl1d": ([ctypes.POINTER(NL1DModel), _I64, _I64, _P, _P, _P, _F, _P, _P, _P], _I32),
+    "mgb_ffbsi_rejection_workspace": ([_I64, _I64, _I64, ctypes.c_int32], _SZ),
+    "mgb_stitch_rejection_workspace": ([_I64, ctypes.c_int32], _SZ),
+    "mgb_ffbsi_rejection_lg": ([ctypes.POINTER(LGTransition), ctypes.POINTER(RejectionConfig), _I64, _I64, _I64, _P,
+                                _P, _P, _P, _P, _P, _P, _SZ, _P], _I32),
+    "mgb_ffbsi_rejection_nl1d": ([ctypes.POINTER(NL1DModel), ctypes.POINTER(RejectionConfig), _I64, _I64, _I64, _P,
+                                  _P, _P, _P, _P, _P, _P, _P, _SZ, _P], _I32),
+    "mgb_stitch_rejection_lg": ([ctypes.POINTER(LGTransition), ctypes.POINTER(RejectionConfig), _I64, _P, _P, _P, _P,
+                                 _P, _P, _P, _SZ, _P], _I32),
+    "mgb_stitch_rejection_nl1d": ([ctypes.POINTER(NL1DModel), ctypes.POINTER(RejectionConfig), _I64, _P, _P, _P, _F,
+                                   _P, _P, _P, _P, _SZ, _P], _I32),
     "mgb_transition_potential_pairs_nl1d": ([ctypes.POINTER(NL1DModel), _I64, _P, _P, _F, _P, _P, _P], _I32),
     "mgb_abc_smc_workspace": ([ctypes.POINTER(ABCConfig), ctypes.c_int32], _SZ),
     "mgb_abc_smc_views": ([ctypes.POINTER(ABCConfig), ctypes.c_int32, _P, ctypes.POINTER(ABCViews)], _I32),

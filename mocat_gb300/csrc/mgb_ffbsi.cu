@@ -22,141 +22,9 @@
 // i and i + ceil(N/2) come from the two halves of one cipher call.  The
 // argmax is reduced in the fixed order (value, then smaller index), so the
 // result does not depend on scheduling.
-#include "mgb_internal.cuh"
-#include "mgb_nl1d.cuh"
+#include "mgb_transition.cuh"
 
 namespace mgb {
-
-constexpr int FB_TPB = 256;
-
-// linear-Gaussian transition
-template <int D>
-struct LGT {
-  static constexpr int DIM = D;
-  static constexpr bool kDrift = false;
-  float F[D * D], Pq[D * D];
-  float cq;
-  uint32_t one;
-  __device__ __forceinline__ void mean(const float (&x)[D], float (&m)[D], float) const {
-#pragma unroll
-    for (int r = 0; r < D; ++r) {
-      float v = __fmul_rn(F[r * D], x[0]);
-#pragma unroll
-      for (int k = 1; k < D; ++k) v = __fmaf_rn(F[r * D + k], x[k], v);
-      m[r] = v;
-    }
-  }
-  __device__ __forceinline__ float potential(const float (&diff)[D]) const {
-    float quad = 0.0f;
-#pragma unroll
-    for (int k = 0; k < D; ++k) {
-      float v = __fmul_rn(diff[0], Pq[k]);
-#pragma unroll
-      for (int r = 1; r < D; ++r) v = __fmaf_rn(diff[r], Pq[r * D + k], v);
-      quad = k == 0 ? __fmul_rn(v, v) : __fmaf_rn(v, v, quad);
-    }
-    return __fadd_rn(__fmul_rn(0.5f, quad), cq);
-  }
-};
-
-// non-linear 1-D benchmark transition; t_previous from *tp (device) or tv
-struct NLT {
-  static constexpr int DIM = 1;
-  static constexpr bool kDrift = true;
-  float tsd, c;
-  const float *tp;
-  float tv;
-  uint32_t one;
-  __device__ __forceinline__ void mean(const float (&x)[1], float (&m)[1], float drift) const {
-    m[0] = nl_mean(x[0], drift);
-  }
-  __device__ __forceinline__ float potential(const float (&diff)[1]) const { return nl_gauss(diff[0], tsd, c); }
-};
-
-// the policy's per-launch constant (8 cos(1.2 t_prev)), computed once per block
-// by thread 0; every thread of the block calls this
-template <class TP>
-__device__ __forceinline__ float block_drift(const TP &p, float *sm) {
-  if constexpr (TP::kDrift) {
-    if (threadIdx.x == 0) sm[0] = nl_drift(p.tp ? *p.tp : p.tv);
-    __syncthreads();
-    return sm[0];
-  } else {
-    return 0.0f;
-  }
-}
-
-// mean(x_t^i) for all i (dimension-major in and out)
-template <class TP>
-__global__ void __launch_bounds__(FB_TPB) k_ffbsi_fx(const __grid_constant__ TP p, int64_t N,
-                                                      const float *__restrict__ x, float *__restrict__ fx) {
-  constexpr int D = TP::DIM;
-  __shared__ float sm[1];
-  const float drift = block_drift(p, sm);
-  const int64_t i = blockIdx.x * (int64_t)FB_TPB + threadIdx.x;
-  if (i >= N) return;
-  float xv[D], m[D];
-#pragma unroll
-  for (int k = 0; k < D; ++k) xv[k] = x[k * N + i];
-  p.mean(xv, m, drift);
-#pragma unroll
-  for (int r = 0; r < D; ++r) fx[r * N + i] = m[r];
-}
-
-struct Best {
-  float v;
-  int32_t i;
-  int have;
-};
-__device__ __forceinline__ void best_take(Best &b, float v, int32_t i) {
-  if (v != v) return;
-  if (!b.have || v > b.v || (v == b.v && i < b.i)) {
-    b.v = v;
-    b.i = i;
-    b.have = 1;
-  }
-}
-__device__ __forceinline__ void best_merge(Best &b, const Best &o) {
-  if (!o.have) return;
-  if (!b.have || o.v > b.v || (o.v == b.v && o.i < b.i)) b = o;
-}
-
-template <int TPB>
-__device__ __forceinline__ int32_t block_argmax(Best b, Best *sm) {
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    Best o;
-    o.v = __shfl_down_sync(0xffffffffu, b.v, off);
-    o.i = __shfl_down_sync(0xffffffffu, b.i, off);
-    o.have = __shfl_down_sync(0xffffffffu, b.have, off);
-    best_merge(b, o);
-  }
-  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = b;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    Best r = sm[0];
-    for (int w = 1; w < TPB / 32; ++w) best_merge(r, sm[w]);
-    sm[0] = r;
-  }
-  __syncthreads();
-  return sm[0].have ? sm[0].i : 0;
-}
-
-// last step: sample j draws over the (M, N) Gumbel array of t_key
-__global__ void __launch_bounds__(FB_TPB) k_ffbsi_last(int64_t N, int64_t M, const float *__restrict__ lw,
-                                                        const uint32_t *tkey, int32_t *__restrict__ idx) {
-  __shared__ Best sm[FB_TPB / 32];
-  const int64_t j = blockIdx.x;
-  const uint32_t k0 = tkey[0], k1 = tkey[1];
-  const uint64_t tot = (uint64_t)M * (uint64_t)N;
-  Best b{-INFINITY, 0, 0};
-  for (int64_t i = threadIdx.x; i < N; i += FB_TPB) {
-    const float g = bits_to_gumbel(bits_at(k0, k1, tot, (uint64_t)j * N + i));
-    best_take(b, __fadd_rn(g, lw[i]), (int32_t)i);
-  }
-  const int32_t bi = block_argmax<FB_TPB>(b, sm);
-  if (threadIdx.x == 0) idx[j] = bi;
-}
 
 // step t: sample j conditions on its state at t + 1
 template <class TP>
@@ -196,17 +64,6 @@ __global__ void __launch_bounds__(FB_TPB) k_ffbsi_step(const __grid_constant__ T
   }
   const int32_t bi = block_argmax<FB_TPB>(b, sm);
   if (threadIdx.x == 0) idx[j] = bi;
-}
-
-// xs_t[:, j] = x_t[:, idx_j]
-template <int D>
-__global__ void k_ffbsi_take(int64_t N, int64_t M, const float *__restrict__ x, const int32_t *__restrict__ idx,
-                             float *__restrict__ out) {
-  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < M; j += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = idx[j];
-#pragma unroll
-    for (int k = 0; k < D; ++k) out[k * M + j] = x[k * N + i];
-  }
 }
 
 // transition potential of particle pairs (x0_i -> x1_i), plus lw_i when given
@@ -275,28 +132,6 @@ __global__ void __launch_bounds__(FB_TPB) k_stitch(const __grid_constant__ TP p,
   }
   const int32_t bi = block_argmax<FB_TPB>(b, sm);
   if (threadIdx.x == 0) idx[j] = bi;
-}
-
-template <int D>
-static LGT<D> pack_lgt(const mgb_lg_transition *tr) {
-  LGT<D> p;
-  for (int i = 0; i < D * D; ++i) {
-    p.F[i] = tr->F[i];
-    p.Pq[i] = tr->Pq[i];
-  }
-  p.cq = tr->cq;
-  p.one = 1u;
-  return p;
-}
-
-static NLT pack_nlt(const mgb_nl1d_model *m, const float *tp, float tv) {
-  NLT p;
-  p.tsd = m->transition_sd;
-  p.c = m->c;
-  p.tp = tp;
-  p.tv = tv;
-  p.one = 1u;
-  return p;
 }
 
 template <class TP>

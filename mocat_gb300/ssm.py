@@ -609,11 +609,10 @@ def _transition_struct(ssm_scenario):
 
 def backward_simulation(ssm_scenario, marginal_particles, random_key, n_samps=None, maximum_rejections=0,
                         transition_dens_bound_parameter=0.0, bound_inflation=1.01):
-    """backward.py:248-270 with maximum_rejections = 0 (backward_simulation_full, :217-245):
-    n_samps trajectories drawn backwards through the filter's particles.  Returns
-    cdict(value (T, n_samps, d), t, num_transition_evals (T,))."""
-    if maximum_rejections > 0:
-        raise NotImplementedError("backward simulation by rejection sampling is not built (maximum_rejections=0)")
+    """backward.py:248-270: n_samps trajectories drawn backwards through the filter's particles,
+    by the full categorical (maximum_rejections = 0, backward_simulation_full :217-245) or by
+    rejection sampling (backward_simulation_rejection :172-214).  Returns cdict(value
+    (T, n_samps, d), t, num_transition_evals (T,), indices)."""
     nl = isinstance(ssm_scenario, NonLinear1DBenchmark)
     if not nl and not isinstance(ssm_scenario, TimeHomogenousLinearGaussian):
         raise NotImplementedError(f"{ssm_scenario.__class__.__name__}: no backward-simulation kernel for this model")
@@ -626,13 +625,30 @@ def backward_simulation(ssm_scenario, marginal_particles, random_key, n_samps=No
     lw = _dev.as_f32(marginal_particles.log_weight).reshape(T, n).contiguous()
     key = _dev.as_key(random_key)
     dev = x.device
-    ws = _dev.workspace(_lib.lib().mgb_ffbsi_workspace(n, T, d), dev)
     out = torch.empty((T, d, M), dtype=torch.float32, device=dev)
     idx = torch.empty((T, M), dtype=torch.int32, device=dev)
+    tt = None
     if nl:
         tt = _dev.as_f32(marginal_particles.t).reshape(-1).contiguous()
         if tt.numel() != T:
             raise ValueError(f"marginal_particles.t has {tt.numel()} entries for {T} steps")
+    if maximum_rejections > 0:
+        cfg = _lib.RejectionConfig(int(maximum_rejections), float(transition_dens_bound_parameter),
+                                   float(bound_inflation))
+        ws = _dev.workspace(_lib.lib().mgb_ffbsi_rejection_workspace(n, M, T, d), dev)
+        evals = torch.empty(T, dtype=torch.int64, device=dev)
+        if nl:
+            call("mgb_ffbsi_rejection_nl1d", ctypes.byref(ssm_scenario.derived()[1]), ctypes.byref(cfg), T, n, M,
+                 _dev.ptr(x), _dev.ptr(lw), _dev.ptr(tt), _dev.ptr(key), _dev.ptr(out), _dev.ptr(idx), _dev.ptr(evals),
+                 _dev.ptr(ws), ws.numel(), _dev.stream_ptr())
+        else:
+            _, s = _transition_struct(ssm_scenario)
+            call("mgb_ffbsi_rejection_lg", ctypes.byref(s), ctypes.byref(cfg), T, n, M, _dev.ptr(x), _dev.ptr(lw),
+                 _dev.ptr(key), _dev.ptr(out), _dev.ptr(idx), _dev.ptr(evals), _dev.ptr(ws), ws.numel(),
+                 _dev.stream_ptr())
+        return cdict(value=out.permute(0, 2, 1), t=marginal_particles.t, num_transition_evals=evals, indices=idx)
+    ws = _dev.workspace(_lib.lib().mgb_ffbsi_workspace(n, T, d), dev)
+    if nl:
         call("mgb_ffbsi_nl1d", ctypes.byref(ssm_scenario.derived()[1]), T, n, M, _dev.ptr(x), _dev.ptr(lw),
              _dev.ptr(tt), _dev.ptr(key), _dev.ptr(out), _dev.ptr(idx), _dev.ptr(ws), ws.numel(), _dev.stream_ptr())
     else:
@@ -694,14 +710,46 @@ def full_stitch(ssm_scenario, x0_all, t, x1_all, tplus1, x1_log_weight, random_k
     return idx
 
 
+def rejection_stitching(ssm_scenario, x0_all, t, x1_all, tplus1, x1_log_weight, random_key, maximum_rejections,
+                        init_bound_param=0.0, bound_inflation=1.01):
+    """online_smoothing.py:129-175: for each x0_i an index into x1_all by rejection sampling
+    against exp(-transition_potential), the full categorical for those still unaccepted after
+    maximum_rejections rounds.  Returns (indices (M,), transition evaluations)."""
+    x0t = _dev.as_f32(x0_all).t().contiguous()
+    x1t = _dev.as_f32(x1_all).t().contiguous()
+    M, d = x1t.shape[1], x1t.shape[0]
+    if x0t.shape[1] != M:
+        raise ValueError(f"rejection stitching pairs x0_all ({x0t.shape[1]}) with x1_all ({M}) one to one")
+    lw = _dev.as_f32(x1_log_weight).reshape(-1).contiguous()
+    dev = x0t.device
+    idx = torch.empty(M, dtype=torch.int32, device=dev)
+    evals = torch.empty(1, dtype=torch.int64, device=dev)
+    cfg = _lib.RejectionConfig(int(maximum_rejections), float(init_bound_param), float(bound_inflation))
+    ws = _dev.workspace(_lib.lib().mgb_stitch_rejection_workspace(M, d), dev)
+    key = _dev.as_key(random_key)
+    if isinstance(ssm_scenario, NonLinear1DBenchmark):
+        call("mgb_stitch_rejection_nl1d", ctypes.byref(ssm_scenario.derived()[1]), ctypes.byref(cfg), M,
+             _dev.ptr(x0t), _dev.ptr(x1t), _dev.ptr(lw), float(t), _dev.ptr(key), _dev.ptr(idx), _dev.ptr(evals),
+             _dev.ptr(ws), ws.numel(), _dev.stream_ptr())
+    else:
+        _, s = _transition_struct(ssm_scenario)
+        call("mgb_stitch_rejection_lg", ctypes.byref(s), ctypes.byref(cfg), M, _dev.ptr(x0t), _dev.ptr(x1t),
+             _dev.ptr(lw), _dev.ptr(key), _dev.ptr(idx), _dev.ptr(evals), _dev.ptr(ws), ws.numel(),
+             _dev.stream_ptr())
+    return idx, int(evals.item())
+
+
 def fixed_lag_stitching(ssm_scenario, early_block, t, recent_block, recent_block_log_weight, tplus1, random_key,
                         maximum_rejections=0, init_bound_param=0.0, bound_inflation=1.01):
-    """online_smoothing.py:178-209 (full stitching): returns (stitched value, transition evaluations)."""
-    if maximum_rejections > 0:
-        raise NotImplementedError("stitching by rejection sampling is not built (maximum_rejections=0)")
+    """online_smoothing.py:178-209: returns (stitched value, transition evaluations); full
+    stitching for maximum_rejections = 0, rejection stitching otherwise."""
     x0_fixed_all = early_block[-1]
     x0_vary_all, x1_vary_all = recent_block[0], recent_block[1]
     nilw = _pair_potential(ssm_scenario, x0_vary_all, x1_vary_all, recent_block_log_weight, t)
+    if maximum_rejections > 0:
+        inds, evals = rejection_stitching(ssm_scenario, x0_fixed_all, t, x1_vary_all, tplus1, nilw, random_key,
+                                          maximum_rejections, init_bound_param, bound_inflation)
+        return torch.cat([early_block, recent_block[1:, inds.long()]], 0), evals
     inds = full_stitch(ssm_scenario, x0_fixed_all, t, x1_vary_all, tplus1, nilw, random_key).long()
     return torch.cat([early_block, recent_block[1:, inds]], 0), len(x0_fixed_all) ** 2
 

@@ -146,6 +146,17 @@ def lib():
         L.o_ffbsi_lg.argtypes = [ctypes.POINTER(_FFBSiModel), i64, i64, i64, f32p, f32p, u32p, f32p, i32p]
         L.o_stitch_lg.argtypes = [ctypes.POINTER(_FFBSiModel), i64, i64, f32p, f32p, f32p, u32p, i32p]
         L.o_transition_potential_pairs.argtypes = [ctypes.POINTER(_FFBSiModel), i64, f32p, f32p, f32p]
+        fl, i32 = ctypes.c_float, ctypes.c_int32
+        L.o_ffbsi_rejection_lg.argtypes = [ctypes.POINTER(_FFBSiModel), i64, i64, i64, f32p, f32p, u32p, i32, fl, fl,
+                                           f32p, i32p, i64p]
+        L.o_ffbsi_rejection_nl1d.argtypes = [ctypes.POINTER(_NLModel), i64, i64, i64, f32p, f32p, f32p, u32p, i32, fl,
+                                             fl, f32p, i32p, i64p]
+        L.o_stitch_rejection_lg.argtypes = [ctypes.POINTER(_FFBSiModel), i64, f32p, f32p, f32p, u32p, i32, fl, fl,
+                                            i32p]
+        L.o_stitch_rejection_lg.restype = i64
+        L.o_stitch_rejection_nl1d.argtypes = [ctypes.POINTER(_NLModel), i64, f32p, f32p, f32p, fl, u32p, i32, fl, fl,
+                                              i32p]
+        L.o_stitch_rejection_nl1d.restype = i64
         L.o_num_threads.restype = ctypes.c_int
         L.o_set_num_threads.argtypes = [ctypes.c_int]
         _lib = L
@@ -564,6 +575,60 @@ def transition_potential_pairs(F, Pq, cq, x0, x1):
     out = np.empty(x0.shape[0], np.float32)
     lib().o_transition_potential_pairs(ctypes.byref(s), x0.shape[0], x0.reshape(-1), x1.reshape(-1), out)
     return out
+
+
+def ffbsi_rejection_lg(F, Pq, cq, x_hist, lw_hist, key, M, maximum_rejections, init_bound_param=0.0,
+                       bound_inflation=1.01):
+    """backward_simulation_rejection (backward.py:172-214) for a linear-Gaussian transition:
+    x_hist (T, N, d), lw_hist (T, N) -> (samples (T, M, d), indices (T, M), evals (T,) int64)."""
+    F, Pq = _f32(F), _f32(Pq)
+    x_hist = _f32(x_hist)
+    T, N, d = x_hist.shape
+    s = _FFBSiModel(d, _ptr(F), _ptr(Pq), float(cq))
+    out = np.empty((T, M, d), np.float32)
+    idx = np.empty((T, M), np.int32)
+    ev = np.empty(T, np.int64)
+    lib().o_ffbsi_rejection_lg(ctypes.byref(s), T, N, M, x_hist.reshape(-1), _f32(lw_hist).reshape(-1), _u32(key),
+                               int(maximum_rejections), float(np.float32(init_bound_param)),
+                               float(np.float32(bound_inflation)), out.reshape(-1), idx.reshape(-1), ev)
+    return out, idx, ev
+
+
+def ffbsi_rejection_nl1d(params, x_hist, lw_hist, t, key, M, maximum_rejections, init_bound_param=0.0,
+                         bound_inflation=1.01):
+    """backward_simulation_rejection on NonLinear1DBenchmark: x_hist, lw_hist (T, N), t (T,)
+    -> (samples (T, M), indices (T, M), evals (T,) int64)."""
+    x_hist, lw_hist, t = _f32(x_hist), _f32(lw_hist), _f32(t).reshape(-1)
+    T, N = lw_hist.shape
+    out = np.empty((T, M), np.float32)
+    idx = np.empty((T, M), np.int32)
+    ev = np.empty(T, np.int64)
+    lib().o_ffbsi_rejection_nl1d(ctypes.byref(_nl_struct(params)), T, N, M, x_hist.reshape(-1), lw_hist.reshape(-1),
+                                 t, _u32(key), int(maximum_rejections), float(np.float32(init_bound_param)),
+                                 float(np.float32(bound_inflation)), out.reshape(-1), idx.reshape(-1), ev)
+    return out, idx, ev
+
+
+def stitch_rejection_lg(F, Pq, cq, x0, x1, lw1, key, maximum_rejections, init_bound_param=0.0, bound_inflation=1.01):
+    """rejection_stitching (online_smoothing.py:129-175): x0, x1 (M, d) -> (indices (M,), evals)."""
+    F, Pq, x0, x1 = _f32(F), _f32(Pq), _f32(x0), _f32(x1)
+    s = _FFBSiModel(x0.shape[1], _ptr(F), _ptr(Pq), float(cq))
+    idx = np.empty(x0.shape[0], np.int32)
+    ev = lib().o_stitch_rejection_lg(ctypes.byref(s), x0.shape[0], x0.reshape(-1), x1.reshape(-1), _f32(lw1),
+                                     _u32(key), int(maximum_rejections), float(np.float32(init_bound_param)),
+                                     float(np.float32(bound_inflation)), idx)
+    return idx, int(ev)
+
+
+def stitch_rejection_nl1d(params, x0, x1, lw1, t_prev, key, maximum_rejections, init_bound_param=0.0,
+                          bound_inflation=1.01):
+    """rejection_stitching on NonLinear1DBenchmark, x0 (M,) at t_prev, x1 (M,) -> (indices, evals)."""
+    x0, x1, lw1 = _f32(x0).reshape(-1), _f32(x1).reshape(-1), _f32(lw1).reshape(-1)
+    idx = np.empty(x0.size, np.int32)
+    ev = lib().o_stitch_rejection_nl1d(ctypes.byref(_nl_struct(params)), x0.size, x0, x1, lw1,
+                                       float(np.float32(t_prev)), _u32(key), int(maximum_rejections),
+                                       float(np.float32(init_bound_param)), float(np.float32(bound_inflation)), idx)
+    return idx, int(ev)
 
 
 def num_threads():

@@ -910,6 +910,172 @@ void o_transition_potential_pairs_nl1d(const o_nl_model *nm, int64_t M, const fl
     for (int64_t i = 0; i < M; ++i) out[i] = o_transition_potential(&md, x0 + i, x1 + i, drift);
 }
 
+/* -------------------------------- backward simulation and stitching by rejection */
+
+/* transition potential of item i against pool element j: back = 1 pool_j -> itm_i
+ * (backward simulation), back = 0 itm_i -> pool_j (stitching); rows particle-major */
+static inline float o_rej_pot(const o_ffbsi_model *md, int back, const float *itm, const float *pool, int64_t i,
+                              int64_t j, float drift)
+{
+    const int d = md->d;
+    return back ? o_transition_potential(md, pool + j * d, itm + i * d, drift)
+                : o_transition_potential(md, itm + i * d, pool + j * d, drift);
+}
+
+/* categorical(key, w) over Np logits: argmax_j gumbel(key, (Np,))_j + w_j, with
+ * w_j = lw_j - potential(i, j) when full (first maximum wins, NaN skipped) */
+static int32_t o_rej_categorical(const o_ffbsi_model *md, int back, int full, const float *itm, const float *pool,
+                                 int64_t i, int64_t Np, const float *lw, float drift, uint32_t k0, uint32_t k1)
+{
+    float best = -INFINITY;
+    int32_t bi = 0;
+    int have = 0;
+    for (int64_t j = 0; j < Np; ++j) {
+        float g = o_bits_to_gumbel(o_bits_at(k0, k1, (uint64_t)Np, (uint64_t)j));
+        float w = full ? lw[j] - o_rej_pot(md, back, itm, pool, i, j, drift) : lw[j];
+        float v = g + w;
+        if (v == v && (!have || v > best)) { best = v; bi = (int32_t)j; have = 1; }
+    }
+    return bi;
+}
+
+/* max with jnp.max's NaN propagation */
+static inline float o_nanmax(float m, float v) { return (v != v || v > m) ? v : m; }
+
+/* rejection_resampling (backward.py:126-169, proposals :54-123) and rejection_stitching
+ * (online_smoothing.py:129-175, proposals :59-126), one routine: n items with states itm
+ * (n, d), a pool (Np, d) with log-weights lw.
+ *   (c0, u0, k0) = split(key, 3); idx = categorical(c0, lw, (n,)) (one (n, Np) Gumbel draw);
+ *   dens_i = exp(-pot(i, idx_i)); bound = max dens > ibp ? max dens * infl : ibp;
+ *   nya_i = uniform(u0, (n,))_i > dens_i / bound; key_i = split(k0, n)_i; evals = n; iter = 1
+ *   while any(nya) and iter < max_rej:
+ *     evals += #nya; for nya_i: (key_i, c, u) = split(key_i, 3); idx_i = categorical(c, lw);
+ *       dens_i = exp(-pot(i, idx_i)); nya_i = uniform(u) > dens_i / bound   (others dens 0, nya 0)
+ *     if max dens > bound: bound = max dens * infl; nya = all; iter += 1
+ *   for nya_i: idx_i = categorical(key_i, lw - pot(i, .)); evals += Np * #nya.
+ * Returns evals. */
+static int64_t o_rejection(const o_ffbsi_model *md, int back, int64_t n, int64_t Np, const float *itm,
+                           const float *pool, const float *lw, float drift, const uint32_t *key, int32_t max_rej,
+                           float ibp, float infl, int32_t *idx)
+{
+    uint32_t k3[6];
+    o_split(key, 3, k3);
+    uint32_t *keys = (uint32_t *)malloc(sizeof(uint32_t) * 2 * (size_t)n);
+    float *dens = (float *)malloc(sizeof(float) * (size_t)n);
+    uint8_t *nya = (uint8_t *)malloc((size_t)n);
+    const uint64_t tot = (uint64_t)n * (uint64_t)Np;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        float best = -INFINITY;
+        int32_t bi = 0;
+        int have = 0;
+        for (int64_t j = 0; j < Np; ++j) {
+            float g = o_bits_to_gumbel(o_bits_at(k3[0], k3[1], tot, (uint64_t)i * (uint64_t)Np + (uint64_t)j));
+            float v = g + lw[j];
+            if (v == v && (!have || v > best)) { best = v; bi = (int32_t)j; have = 1; }
+        }
+        idx[i] = bi;
+        dens[i] = o_expf(-o_rej_pot(md, back, itm, pool, i, bi, drift));
+    }
+    float mx = dens[0];
+    for (int64_t i = 1; i < n; ++i) mx = o_nanmax(mx, dens[i]);
+    float bound = mx > ibp ? mx * infl : ibp;
+    int64_t cnt = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        float u = o_bits_to_unit(o_bits_at(k3[2], k3[3], (uint64_t)n, (uint64_t)i));
+        nya[i] = u > dens[i] / bound;
+        cnt += nya[i];
+        o_split_at(k3[4], k3[5], (uint64_t)n, (uint64_t)i, &keys[2 * i], &keys[2 * i + 1]);
+    }
+    int64_t evals = n;
+    for (int32_t it = 1; cnt > 0 && it < max_rej; ++it) {
+        evals += cnt;
+#pragma omp parallel for schedule(dynamic, 16)
+        for (int64_t i = 0; i < n; ++i) {
+            if (!nya[i]) { dens[i] = 0.0f; continue; }
+            uint32_t sk[6];
+            o_split(keys + 2 * i, 3, sk);
+            int32_t bi = o_rej_categorical(md, back, 0, itm, pool, i, Np, lw, drift, sk[2], sk[3]);
+            idx[i] = bi;
+            dens[i] = o_expf(-o_rej_pot(md, back, itm, pool, i, bi, drift));
+            float u = o_bits_to_unit(o_bits_at(sk[4], sk[5], 1, 0));
+            nya[i] = u > dens[i] / bound;
+            keys[2 * i] = sk[0];
+            keys[2 * i + 1] = sk[1];
+        }
+        mx = dens[0];
+        for (int64_t i = 1; i < n; ++i) mx = o_nanmax(mx, dens[i]);
+        if (mx > bound) {
+            bound = mx * infl;
+            memset(nya, 1, (size_t)n);
+        }
+        cnt = 0;
+        for (int64_t i = 0; i < n; ++i) cnt += nya[i];
+    }
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t i = 0; i < n; ++i)
+        if (nya[i]) idx[i] = o_rej_categorical(md, back, 1, itm, pool, i, Np, lw, drift, keys[2 * i], keys[2 * i + 1]);
+    evals += Np * cnt;
+    free(keys);
+    free(dens);
+    free(nya);
+    return evals;
+}
+
+/* backward_simulation_rejection (backward.py:172-214): t_keys = split(key, T); the last step as
+ * the full version; step t = T-2 .. 0 by o_rejection with items = samples at t+1, pool = x_t.
+ * evals (T): evals[0] = 0, evals[t+1] = step t's count. */
+static void o_ffbsi_rejection(const o_ffbsi_model *md, int64_t T, int64_t N, int64_t M, const float *x_hist,
+                              const float *lw_hist, const float *t_all, const uint32_t *key, int32_t max_rej,
+                              float ibp, float infl, float *out, int32_t *idx, int64_t *evals)
+{
+    const int d = md->d;
+    uint32_t *tkeys = (uint32_t *)malloc(sizeof(uint32_t) * 2 * (size_t)T);
+    o_split(key, T, tkeys);
+    o_resample_gumbel(lw_hist + (T - 1) * N, N, M, tkeys + 2 * (T - 1), idx + (T - 1) * M);
+    for (int64_t j = 0; j < M; ++j)
+        memcpy(out + ((T - 1) * M + j) * d, x_hist + ((T - 1) * N + idx[(T - 1) * M + j]) * d, sizeof(float) * d);
+    evals[0] = 0;
+    for (int64_t t = T - 2; t >= 0; --t) {
+        const float drift = md->nl ? o_nl_drift(t_all[t]) : 0.0f;
+        evals[t + 1] = o_rejection(md, 1, M, N, out + (t + 1) * M * d, x_hist + t * N * d, lw_hist + t * N, drift,
+                                   tkeys + 2 * t, max_rej, ibp, infl, idx + t * M);
+        for (int64_t j = 0; j < M; ++j)
+            memcpy(out + (t * M + j) * d, x_hist + (t * N + idx[t * M + j]) * d, sizeof(float) * d);
+    }
+    free(tkeys);
+}
+
+void o_ffbsi_rejection_lg(const o_ffbsi_model *md, int64_t T, int64_t N, int64_t M, const float *x_hist,
+                          const float *lw_hist, const uint32_t *key, int32_t max_rej, float ibp, float infl,
+                          float *out, int32_t *idx, int64_t *evals)
+{
+    o_ffbsi_rejection(md, T, N, M, x_hist, lw_hist, NULL, key, max_rej, ibp, infl, out, idx, evals);
+}
+
+void o_ffbsi_rejection_nl1d(const o_nl_model *nm, int64_t T, int64_t N, int64_t M, const float *x_hist,
+                            const float *lw_hist, const float *t_all, const uint32_t *key, int32_t max_rej,
+                            float ibp, float infl, float *out, int32_t *idx, int64_t *evals)
+{
+    o_ffbsi_model md = o_nl_transition(nm);
+    o_ffbsi_rejection(&md, T, N, M, x_hist, lw_hist, t_all, key, max_rej, ibp, infl, out, idx, evals);
+}
+
+/* rejection_stitching: items x0 (M, d) at t_prev, pool x1 (M, d) with lw1; returns evals */
+int64_t o_stitch_rejection_lg(const o_ffbsi_model *md, int64_t M, const float *x0, const float *x1, const float *lw1,
+                              const uint32_t *key, int32_t max_rej, float ibp, float infl, int32_t *idx)
+{
+    return o_rejection(md, 0, M, M, x0, x1, lw1, 0.0f, key, max_rej, ibp, infl, idx);
+}
+
+int64_t o_stitch_rejection_nl1d(const o_nl_model *nm, int64_t M, const float *x0, const float *x1, const float *lw1,
+                                float t_prev, const uint32_t *key, int32_t max_rej, float ibp, float infl,
+                                int32_t *idx)
+{
+    o_ffbsi_model md = o_nl_transition(nm);
+    return o_rejection(&md, 0, M, M, x0, x1, lw1, o_nl_drift(t_prev), key, max_rej, ibp, infl, idx);
+}
+
 /* ---------------------------------------------------------------- ABC-SMC */
 
 typedef struct {
