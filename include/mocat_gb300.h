@@ -417,7 +417,18 @@ int mgb_pf_sv_batch_autotune(const mgb_sv_model *model_host, int64_t B, const in
  * likelihood potential sum_i softplus(x_i . beta) - y_i x_i . beta.
  * Resampling (ess <= ess_threshold_resample N) is systematic.
  * N <= MGB_SMC_MAX_N; d in {2, 3, 5, 10, 20, 50}.
+ * The same sampler also takes (fields after `precision`; zero keeps the setting above):
+ *   RandomWalk moves (standard_mcmc.py:20-64): x' = x + sqrt(stepsize) e, alpha = min(1, exp(U - U'));
+ *   Underdamped with leapfrog_steps L and a finite friction f (standard_mcmc.py:72-153,
+ *     utils.leapfrog :108-156): p = -p exp(-f eps) + sqrt(1 - exp(-2 f eps)) e, L leapfrog steps, the
+ *     momenta kept per particle (resampled with it) between moves and iterations;
+ *   a temperature_schedule (smc.py:100-125, leading 0 removed): tau_i = schedule[i];
+ *   prior draws with their own scale (a scenario whose prior_sample and prior_potential differ);
+ *   the Gaussian likelihood of toy_examples.Gaussian (scenarios/toy_examples.py:17-51):
+ *     0.5 |(x - mean) @ prec_sqrt^T|^2, prec_sqrt = inv(chol(covariance)), X and y unused.
  */
+enum { MGB_MOVE_UNDERDAMPED = 0, MGB_MOVE_RANDOM_WALK = 1 };
+enum { MGB_LIK_LOGISTIC = 0, MGB_LIK_GAUSSIAN = 1 };
 #define MGB_SMC_MAX_N 24576
 enum { MGB_PREC_FP32 = 0, MGB_PREC_BF16 = 1 };
 
@@ -442,6 +453,15 @@ typedef struct {
   float max_temperature;
   int32_t max_iter;             /* SMC iterations (also the history length - 1) */
   int32_t precision;            /* MGB_PREC_FP32 or MGB_PREC_BF16 (potential on the tensor cores) */
+  int32_t move;                 /* MGB_MOVE_UNDERDAMPED or MGB_MOVE_RANDOM_WALK */
+  int32_t leapfrog_steps;       /* Underdamped leapfrog steps (0: 1) */
+  float friction;               /* Underdamped friction (<= 0 or infinite: fresh momenta, MALA / HMC) */
+  float prior_sample_scale;     /* prior draws prior_sample_scale * normal (0: prior_scale) */
+  int32_t n_schedule;           /* > 0: temperatures from schedule_dev; max_iter = n_schedule */
+  const float *schedule_dev;    /* (n_schedule) device */
+  int32_t likelihood;           /* MGB_LIK_LOGISTIC or MGB_LIK_GAUSSIAN */
+  const float *gauss_mean_dev;  /* (d) device, MGB_LIK_GAUSSIAN */
+  const float *gauss_prec_sqrt_dev; /* (d, d) row-major device, MGB_LIK_GAUSSIAN */
 } mgb_smc_logreg_config;
 
 /* device pointers into the sampler's workspace */

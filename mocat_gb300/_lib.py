@@ -91,7 +91,11 @@ class SMCConfig(ctypes.Structure):
                 ("stepsize", ctypes.c_float), ("prior_scale", ctypes.c_float),
                 ("ess_threshold_retain", ctypes.c_float), ("ess_threshold_resample", ctypes.c_float),
                 ("bisection_tol", ctypes.c_float), ("max_bisection_iter", ctypes.c_int32),
-                ("max_temperature", ctypes.c_float), ("max_iter", ctypes.c_int32), ("precision", ctypes.c_int32)]
+                ("max_temperature", ctypes.c_float), ("max_iter", ctypes.c_int32), ("precision", ctypes.c_int32),
+                ("move", ctypes.c_int32), ("leapfrog_steps", ctypes.c_int32), ("friction", ctypes.c_float),
+                ("prior_sample_scale", ctypes.c_float), ("n_schedule", ctypes.c_int32),
+                ("schedule_dev", ctypes.c_void_p), ("likelihood", ctypes.c_int32),
+                ("gauss_mean_dev", ctypes.c_void_p), ("gauss_prec_sqrt_dev", ctypes.c_void_p)]
 
 
 class SMCViews(ctypes.Structure):

@@ -180,9 +180,10 @@ __device__ __forceinline__ void normal_vec(uint32_t k0, uint32_t k1, float (&e)[
   for (int j = 0; j < D; ++j) e[j] = bits_to_normal(b[j]);
 }
 
-// prior draws and the key schedule of the sampler's startup
+// prior draws and the key schedule of the sampler's startup; msplit is the key
+// split of the MCMC sampler's startup (Underdamped 3, RandomWalk 2)
 template <int D>
-__global__ void __launch_bounds__(SMC_TPB) k_smc_prior(SMCView v, const uint32_t *keys_in, float scale) {
+__global__ void __launch_bounds__(SMC_TPB) k_smc_prior(SMCView v, const uint32_t *keys_in, float scale, int msplit) {
   const int64_t P = (int64_t)v.B * v.N;
   const int64_t p = blockIdx.x * (int64_t)SMC_TPB + threadIdx.x;
   if (p >= P) return;
@@ -195,11 +196,14 @@ __global__ void __launch_bounds__(SMC_TPB) k_smc_prior(SMCView v, const uint32_t
   float e[D];
   normal_vec<D>(a0, a1, e);
 #pragma unroll
-  for (int k = 0; k < D; ++k) v.beta[p * D + k] = __fmul_rn(e[k], scale);
+  for (int k = 0; k < D; ++k) {
+    v.beta[p * D + k] = __fmul_rn(e[k], scale);
+    v.ms[p * D + k] = 0.0f;  // Underdamped.startup: momenta = zeros(d)
+  }
   if (j == 0) {
     uint32_t f0, f1, g0, g1;
     split_at(e0, e1, 2 * (uint64_t)v.N + 1, 2 * (uint64_t)v.N, f0, f1);  // split(key, 2N + 1)[-1]
-    split_at(f0, f1, 3, 0, g0, g1);                                      // Underdamped.startup
+    split_at(f0, f1, (uint64_t)msplit, 0, g0, g1);                       // the MCMC sampler's startup
     v.key[2 * b] = g0;
     v.key[2 * b + 1] = g1;
     v.tau[b] = 0.0f;
@@ -212,7 +216,7 @@ __global__ void __launch_bounds__(SMC_TPB) k_smc_prior(SMCView v, const uint32_t
 }
 
 // iteration start: resampling decision, particle keys, the next sampler key
-__global__ void __launch_bounds__(SMC_TPB) k_smc_keys(SMCView v, float thr_resample) {
+__global__ void __launch_bounds__(SMC_TPB) k_smc_keys(SMCView v, float thr_resample, int msplit) {
   const int64_t P = (int64_t)v.B * v.N;
   const int64_t p = blockIdx.x * (int64_t)SMC_TPB + threadIdx.x;
   if (p >= P) return;
@@ -222,7 +226,7 @@ __global__ void __launch_bounds__(SMC_TPB) k_smc_keys(SMCView v, float thr_resam
   const uint64_t nk = (uint64_t)v.N + 2;
   uint32_t a0, a1, c0, c1;
   split_at(k0, k1, nk, (uint64_t)j, a0, a1);
-  split_at(a0, a1, 3, 0, c0, c1);  // Underdamped.startup of forward_proposal
+  split_at(a0, a1, (uint64_t)msplit, 0, c0, c1);  // the MCMC sampler's startup in forward_proposal
   v.pkey[2 * p] = c0;
   v.pkey[2 * p + 1] = c1;
   v.alpha[p] = 0.0f;
@@ -284,35 +288,15 @@ __global__ void __launch_bounds__(SMC_TPB) k_smc_gather(SMCView v) {
   for (int k = 0; k < D; ++k) {
     v.beta_p[p * D + k] = v.beta[src * D + k];
     v.glik_p[p * D + k] = v.glik[src * D + k];
+    v.ms_p[p * D + k] = v.ms[src * D + k];
   }
   v.lik_p[p] = v.lik[src];
 }
 
-// MALA, first half: fresh momentum, half step, position step
+// grad U = beta / s^2 + tau grad l
 template <int D>
-__global__ void __launch_bounds__(SMC_TPB) k_mala_pre(SMCView v, float eps, float inv_s2) {
-  const int64_t P = (int64_t)v.B * v.N;
-  const int64_t p = blockIdx.x * (int64_t)SMC_TPB + threadIdx.x;
-  if (p >= P || !v.active[p / v.N]) return;
-  const float tau = v.tau[p / v.N];
-  const uint32_t k0 = v.pkey[2 * p], k1 = v.pkey[2 * p + 1];
-  uint32_t n0, n1, a0, a1;
-  split2(k0, k1, 0, n0, n1);
-  split2(k0, k1, 1, a0, a1);
-  float mom[D];
-  normal_vec<D>(a0, a1, mom);
-  const float he = eps / 2.0f;
-#pragma unroll
-  for (int k = 0; k < D; ++k) {
-    const float bk = v.beta[p * D + k];
-    const float gu = __fadd_rn(__fmul_rn(bk, inv_s2), __fmul_rn(tau, v.glik[p * D + k]));
-    const float ph = __fsub_rn(mom[k], __fmul_rn(he, gu));
-    v.mom[p * D + k] = mom[k];
-    v.phalf[p * D + k] = ph;
-    v.beta_p[p * D + k] = __fadd_rn(bk, __fmul_rn(eps, ph));
-  }
-  v.pkey[2 * p] = n0;
-  v.pkey[2 * p + 1] = n1;
+__device__ __forceinline__ float grad_u(const float *bt, const float *gl, int k, float inv_s2, float tau) {
+  return __fadd_rn(__fmul_rn(bt[k], inv_s2), __fmul_rn(tau, gl[k]));
 }
 
 template <int D>
@@ -323,9 +307,134 @@ __device__ __forceinline__ float prior_pot(const float *bt, float inv_s2) {
   return __fmul_rn(__fmul_rn(0.5f, q), inv_s2);
 }
 
-// MALA, second half: half step at the proposal, Metropolis correction
+// Underdamped, always + first leapfrog half: (k, ka) = split(k); p0 = -m c1 + c2 normal(ka, (d,))
+// (c1 = exp(-f eps), c2 = sqrt(1 - exp(-2 f eps)); c1 = 0, c2 = 1 for infinite friction);
+// p_h = p0 - eps/2 grad U(beta); beta' = beta + eps p_h
 template <int D>
-__global__ void __launch_bounds__(SMC_TPB) k_mala_post(SMCView v, float eps, float inv_s2) {
+__global__ void __launch_bounds__(SMC_TPB) k_ud_pre(SMCView v, float eps, float c1, float c2, float inv_s2) {
+  const int64_t P = (int64_t)v.B * v.N;
+  const int64_t p = blockIdx.x * (int64_t)SMC_TPB + threadIdx.x;
+  if (p >= P || !v.active[p / v.N]) return;
+  const float tau = v.tau[p / v.N];
+  const uint32_t k0 = v.pkey[2 * p], k1 = v.pkey[2 * p + 1];
+  uint32_t n0, n1, a0, a1;
+  split2(k0, k1, 0, n0, n1);
+  split2(k0, k1, 1, a0, a1);
+  float e[D];
+  normal_vec<D>(a0, a1, e);
+  const float he = eps / 2.0f;
+  const float *bt = v.beta + p * D, *gl = v.glik + p * D;
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    const float p0 = __fadd_rn(__fmul_rn(-v.ms[p * D + k], c1), __fmul_rn(c2, e[k]));
+    const float ph = __fsub_rn(p0, __fmul_rn(he, grad_u<D>(bt, gl, k, inv_s2, tau)));
+    v.mom[p * D + k] = p0;
+    v.phalf[p * D + k] = ph;
+    v.beta_p[p * D + k] = __fadd_rn(bt[k], __fmul_rn(eps, ph));
+  }
+  v.pkey[2 * p] = n0;
+  v.pkey[2 * p + 1] = n1;
+}
+
+// between two leapfrog steps (utils.py:121-135): p = p_h - eps/2 grad U(beta');
+// p_h = p - eps/2 grad U(beta'); beta'' = beta' + eps p_h
+template <int D>
+__global__ void __launch_bounds__(SMC_TPB) k_lf_mid(SMCView v, float eps, float inv_s2) {
+  const int64_t P = (int64_t)v.B * v.N;
+  const int64_t p = blockIdx.x * (int64_t)SMC_TPB + threadIdx.x;
+  if (p >= P || !v.active[p / v.N]) return;
+  const float tau = v.tau[p / v.N];
+  const float he = eps / 2.0f;
+  const float *bt = v.beta_p + p * D, *gl = v.glik_p + p * D;
+  float nb[D];
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    const float g = grad_u<D>(bt, gl, k, inv_s2, tau);
+    const float pm = __fsub_rn(v.phalf[p * D + k], __fmul_rn(he, g));
+    const float ph = __fsub_rn(pm, __fmul_rn(he, g));
+    v.phalf[p * D + k] = ph;
+    nb[k] = __fadd_rn(bt[k], __fmul_rn(eps, ph));
+  }
+#pragma unroll
+  for (int k = 0; k < D; ++k) v.beta_p[p * D + k] = nb[k];
+}
+
+// Underdamped, last leapfrog half and the Metropolis correction: p_L = p_h - eps/2 grad U(beta_L);
+// alpha = min(1, exp(-U' + U - |p_L|^2/2 + |p0|^2/2)); k = split(k, L + 1)[0]; (k, ku) = split(k);
+// accept if uniform(ku) < alpha: the state takes beta_L and the momenta -p_L, else keeps p0
+template <int D>
+__global__ void __launch_bounds__(SMC_TPB) k_ud_post(SMCView v, float eps, int L, float inv_s2) {
+  const int64_t P = (int64_t)v.B * v.N;
+  const int64_t p = blockIdx.x * (int64_t)SMC_TPB + threadIdx.x;
+  if (p >= P || !v.active[p / v.N]) return;
+  const float tau = v.tau[p / v.N];
+  float bo[D], bn[D], pL[D];
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    bo[k] = v.beta[p * D + k];
+    bn[k] = v.beta_p[p * D + k];
+  }
+  const float U = __fadd_rn(prior_pot<D>(bo, inv_s2), __fmul_rn(tau, v.lik[p]));
+  const float Un = __fadd_rn(prior_pot<D>(bn, inv_s2), __fmul_rn(tau, v.lik_p[p]));
+  const float he = eps / 2.0f;
+  float K = 0.0f, Kn = 0.0f;
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    const float pn = __fsub_rn(v.phalf[p * D + k], __fmul_rn(he, grad_u<D>(bn, v.glik_p + p * D, k, inv_s2, tau)));
+    const float pm = v.mom[p * D + k];
+    pL[k] = pn;
+    K = __fmaf_rn(pm, pm, K);
+    Kn = __fmaf_rn(pn, pn, Kn);
+  }
+  K = __fmul_rn(0.5f, K);
+  Kn = __fmul_rn(0.5f, Kn);
+  float alpha = expf(__fadd_rn(__fsub_rn(__fadd_rn(-Un, U), Kn), K));
+  alpha = alpha != alpha ? 0.0f : fminf(1.0f, alpha);
+  const uint32_t k0 = v.pkey[2 * p], k1 = v.pkey[2 * p + 1];
+  uint32_t q0, q1, n0, n1, u0, u1;
+  split_at(k0, k1, (uint64_t)L + 1, 0, q0, q1);
+  split2(q0, q1, 0, n0, n1);
+  split2(q0, q1, 1, u0, u1);
+  const float u = bits_to_unit(bits_at(u0, u1, 1, 0));
+  if (u < alpha) {
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      v.beta[p * D + k] = bn[k];
+      v.glik[p * D + k] = v.glik_p[p * D + k];
+      v.ms[p * D + k] = -pL[k];
+    }
+    v.lik[p] = v.lik_p[p];
+  } else {
+#pragma unroll
+    for (int k = 0; k < D; ++k) v.ms[p * D + k] = v.mom[p * D + k];
+  }
+  v.alpha[p] += alpha;
+  v.pkey[2 * p] = n0;
+  v.pkey[2 * p + 1] = n1;
+}
+
+// RandomWalk proposal (standard_mcmc.py:44-57): (k, ks, _) = split(k, 3); beta' = beta + sq normal(ks, (d,)),
+// sq = sqrt(stepsize)
+template <int D>
+__global__ void __launch_bounds__(SMC_TPB) k_rw_pre(SMCView v, float sq) {
+  const int64_t P = (int64_t)v.B * v.N;
+  const int64_t p = blockIdx.x * (int64_t)SMC_TPB + threadIdx.x;
+  if (p >= P || !v.active[p / v.N]) return;
+  const uint32_t k0 = v.pkey[2 * p], k1 = v.pkey[2 * p + 1];
+  uint32_t n0, n1, a0, a1;
+  split_at(k0, k1, 3, 0, n0, n1);
+  split_at(k0, k1, 3, 1, a0, a1);
+  float e[D];
+  normal_vec<D>(a0, a1, e);
+#pragma unroll
+  for (int k = 0; k < D; ++k) v.beta_p[p * D + k] = __fadd_rn(v.beta[p * D + k], __fmul_rn(sq, e[k]));
+  v.pkey[2 * p] = n0;
+  v.pkey[2 * p + 1] = n1;
+}
+
+// RandomWalk correction: alpha = min(1, exp(-U' + U)); (k, ku) = split(k); accept if uniform(ku) < alpha
+template <int D>
+__global__ void __launch_bounds__(SMC_TPB) k_rw_post(SMCView v, float inv_s2) {
   const int64_t P = (int64_t)v.B * v.N;
   const int64_t p = blockIdx.x * (int64_t)SMC_TPB + threadIdx.x;
   if (p >= P || !v.active[p / v.N]) return;
@@ -338,26 +447,12 @@ __global__ void __launch_bounds__(SMC_TPB) k_mala_post(SMCView v, float eps, flo
   }
   const float U = __fadd_rn(prior_pot<D>(bo, inv_s2), __fmul_rn(tau, v.lik[p]));
   const float Un = __fadd_rn(prior_pot<D>(bn, inv_s2), __fmul_rn(tau, v.lik_p[p]));
-  const float he = eps / 2.0f;
-  float K = 0.0f, Kn = 0.0f;
-#pragma unroll
-  for (int k = 0; k < D; ++k) {
-    const float gu = __fadd_rn(__fmul_rn(bn[k], inv_s2), __fmul_rn(tau, v.glik_p[p * D + k]));
-    const float pn = __fsub_rn(v.phalf[p * D + k], __fmul_rn(he, gu));
-    const float pm = v.mom[p * D + k];
-    K = __fmaf_rn(pm, pm, K);
-    Kn = __fmaf_rn(pn, pn, Kn);
-  }
-  K = __fmul_rn(0.5f, K);
-  Kn = __fmul_rn(0.5f, Kn);
-  float alpha = fminf(1.0f, expf(__fadd_rn(__fsub_rn(__fadd_rn(-Un, U), Kn), K)));
-  if (alpha != alpha) alpha = 0.0f;
-  // proposal: key = split(key, 2)[0]; correct: (key, sub) = split(key)
+  float alpha = expf(__fadd_rn(-Un, U));
+  alpha = alpha != alpha ? 0.0f : fminf(1.0f, alpha);
   const uint32_t k0 = v.pkey[2 * p], k1 = v.pkey[2 * p + 1];
-  uint32_t q0, q1, n0, n1, u0, u1;
-  split2(k0, k1, 0, q0, q1);
-  split2(q0, q1, 0, n0, n1);
-  split2(q0, q1, 1, u0, u1);
+  uint32_t n0, n1, u0, u1;
+  split2(k0, k1, 0, n0, n1);
+  split2(k0, k1, 1, u0, u1);
   const float u = bits_to_unit(bits_at(u0, u1, 1, 0));
   if (u < alpha) {
 #pragma unroll
@@ -370,6 +465,35 @@ __global__ void __launch_bounds__(SMC_TPB) k_mala_post(SMCView v, float eps, flo
   v.alpha[p] += alpha;
   v.pkey[2 * p] = n0;
   v.pkey[2 * p + 1] = n1;
+}
+
+// Gaussian likelihood of toy_examples.Gaussian: z = (x - m) @ Ps^T, l = 0.5 |z|^2, grad = Ps^T z
+template <int D>
+__global__ void __launch_bounds__(SMC_TPB) k_gauss_lik(const float *__restrict__ beta, int64_t P,
+                                                        const int32_t *__restrict__ active, int N,
+                                                        const float *__restrict__ m, const float *__restrict__ Ps,
+                                                        float *__restrict__ lik, float *__restrict__ grad) {
+  const int64_t p = blockIdx.x * (int64_t)SMC_TPB + threadIdx.x;
+  if (p >= P || (active && !active[p / N])) return;
+  float x[D], g[D];
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    x[k] = __fsub_rn(beta[p * D + k], __ldg(&m[k]));
+    g[k] = 0.0f;
+  }
+  float q = 0.0f;
+#pragma unroll
+  for (int r = 0; r < D; ++r) {
+    float z = __fmul_rn(x[0], __ldg(&Ps[r * D]));
+#pragma unroll
+    for (int k = 1; k < D; ++k) z = __fmaf_rn(x[k], __ldg(&Ps[r * D + k]), z);
+    q = __fmaf_rn(z, z, q);
+#pragma unroll
+    for (int k = 0; k < D; ++k) g[k] = __fmaf_rn(__ldg(&Ps[r * D + k]), z, g[k]);
+  }
+  lik[p] = __fmul_rn(0.5f, q);
+#pragma unroll
+  for (int k = 0; k < D; ++k) grad[p * D + k] = g[k];
 }
 
 // after the moves: likelihood potential as the sampler derives it, (U - prior) / tau
@@ -423,25 +547,33 @@ __global__ void __launch_bounds__(ADAPT_TPB) k_smc_adapt(SMCView v, const float 
   const float tau0 = v.tau[b];
   const float target = logf(__fmul_rn(ess_res, sp.retain));
   auto f = [&](float x) { return block_lse3(base, ell, __fsub_rn(x, tau0), N, red).logess - target; };
-  // utils.bisect on [tau0, max_temperature]
-  float b0 = tau0, b1 = sp.max_temp;
-  float e0 = f(b0), e1 = f(b1);
-  const bool incr = e1 > e0;
-  for (int it = 0; it < sp.max_bisect; ++it) {
-    const bool conv = fminf(fabsf(e0), fabsf(e1)) < sp.tol || (e0 < 0.0f && e1 < 0.0f) || (e0 > 0.0f && e1 > 0.0f);
-    if (conv) break;
-    const float np = __fsub_rn(b0, __fdiv_rn(__fmul_rn(e0, __fsub_rn(b1, b0)), __fsub_rn(e1, e0)));
-    const float ne = f(np);
-    const bool up = incr ? ne > 0.0f : ne < 0.0f;
-    if (up) {
-      b1 = np;
-      e1 = ne;
-    } else {
-      b0 = np;
-      e0 = ne;
+  const int it = startup ? 0 : v.iter[b] + 1;
+  float tau1;
+  if (sp.sched) {
+    // temperature_schedule[extra.iter] (smc.py:118-121)
+    tau1 = sp.sched[it < sp.n_sched ? it : sp.n_sched - 1];
+  } else {
+    // utils.bisect on [tau0, max_temperature]
+    float b0 = tau0, b1 = sp.max_temp;
+    float e0 = f(b0), e1 = f(b1);
+    const bool incr = e1 > e0;
+    for (int k = 0; k < sp.max_bisect; ++k) {
+      const bool conv =
+          fminf(fabsf(e0), fabsf(e1)) < sp.tol || (e0 < 0.0f && e1 < 0.0f) || (e0 > 0.0f && e1 > 0.0f);
+      if (conv) break;
+      const float np = __fsub_rn(b0, __fdiv_rn(__fmul_rn(e0, __fsub_rn(b1, b0)), __fsub_rn(e1, e0)));
+      const float ne = f(np);
+      const bool up = incr ? ne > 0.0f : ne < 0.0f;
+      if (up) {
+        b1 = np;
+        e1 = ne;
+      } else {
+        b0 = np;
+        e0 = ne;
+      }
     }
+    tau1 = fabsf(e1) < fabsf(e0) ? b1 : b0;
   }
-  const float tau1 = fabsf(e1) < fabsf(e0) ? b1 : b0;
   const float dt = __fsub_rn(tau1, tau0);
   // LSE of the log-weights the step started from, then the new log-weights (in place)
   float lse_res = logf((float)N);
@@ -466,7 +598,6 @@ __global__ void __launch_bounds__(ADAPT_TPB) k_smc_adapt(SMCView v, const float 
   for (int k = threadIdx.x; k < N; k += ADAPT_TPB) asum += v.alpha[(int64_t)b * N + k];
   asum = block_sum<ADAPT_TPB, float>(asum, red);
   if (threadIdx.x == 0) {
-    const int it = startup ? 0 : v.iter[b] + 1;
     const double lz = startup ? (double)nw.lse - (double)lse_res : v.logz[b] + (double)nw.lse - (double)lse_res;
     const float ess = expf(nw.logess);
     v.tau[b] = tau1;
@@ -542,6 +673,8 @@ SMCView carve_smc(Carver &c, int B, int N, int d, int H) {
   v.glik_p = c.take<float>(P * d);
   v.mom = c.take<float>(P * d);
   v.phalf = c.take<float>(P * d);
+  v.ms = c.take<float>(P * d);
+  v.ms_p = c.take<float>(P * d);
   v.lik = c.take<float>(P);
   v.lik_p = c.take<float>(P);
   v.lik_w = c.take<float>(P);
@@ -567,12 +700,21 @@ SMCView carve_smc(Carver &c, int B, int N, int d, int H) {
 }
 
 static bool smc_cfg_ok(const mgb_smc_logreg_config *cfg) {
-  return cfg && cfg->B >= 1 && cfg->N >= 2 && cfg->N <= MGB_SMC_MAX_N && cfg->d >= 1 && cfg->mcmc_steps >= 1 &&
-         cfg->max_iter >= 1 && cfg->max_bisection_iter >= 0 && cfg->prior_scale > 0.0f && cfg->stepsize > 0.0f &&
-         (cfg->precision == MGB_PREC_FP32 || cfg->precision == MGB_PREC_BF16);
+  if (!(cfg && cfg->B >= 1 && cfg->N >= 2 && cfg->N <= MGB_SMC_MAX_N && cfg->d >= 1 && cfg->mcmc_steps >= 1 &&
+        cfg->max_iter >= 1 && cfg->max_bisection_iter >= 0 && cfg->prior_scale > 0.0f && cfg->stepsize > 0.0f &&
+        (cfg->precision == MGB_PREC_FP32 || cfg->precision == MGB_PREC_BF16)))
+    return false;
+  if (cfg->move != MGB_MOVE_UNDERDAMPED && cfg->move != MGB_MOVE_RANDOM_WALK) return false;
+  if (cfg->leapfrog_steps < 0 || cfg->prior_sample_scale < 0.0f || cfg->n_schedule < 0) return false;
+  if (cfg->n_schedule > 0 && !cfg->schedule_dev) return false;
+  if (cfg->likelihood == MGB_LIK_GAUSSIAN) return cfg->gauss_mean_dev && cfg->gauss_prec_sqrt_dev;
+  return cfg->likelihood == MGB_LIK_LOGISTIC;
 }
 
+static bool smc_gauss(const mgb_smc_logreg_config *cfg) { return cfg->likelihood == MGB_LIK_GAUSSIAN; }
+
 static size_t smc_pot_ws(const mgb_smc_logreg_config *cfg, int64_t n_data) {
+  if (smc_gauss(cfg)) return 0;
   const int64_t P = (int64_t)cfg->B * cfg->N;
   size_t a = logreg_f32_workspace(P, n_data, cfg->d);
   if (cfg->precision == MGB_PREC_BF16) {
@@ -582,28 +724,45 @@ static size_t smc_pot_ws(const mgb_smc_logreg_config *cfg, int64_t n_data) {
   return a;
 }
 
+template <int D>
+static int gauss_lik(const mgb_smc_logreg_config *cfg, const float *beta, int64_t P, const int32_t *active, int N,
+                     float *lik, float *grad, cudaStream_t s) {
+  k_gauss_lik<D><<<(unsigned)((P + SMC_TPB - 1) / SMC_TPB), SMC_TPB, 0, s>>>(
+      beta, P, active, N, cfg->gauss_mean_dev, cfg->gauss_prec_sqrt_dev, lik, grad);
+  return launch_status();
+}
+
 static int smc_potential(const mgb_smc_logreg_config *cfg, const SMCData &dat, const float *beta, float *lik,
                          float *grad, const int32_t *active, void *ws, size_t ws_bytes, cudaStream_t s) {
   const int64_t P = (int64_t)cfg->B * cfg->N;
   const int d = cfg->d;
+  if (smc_gauss(cfg)) MGB_SMC_D_DISPATCH(gauss_lik, cfg, beta, P, active, cfg->N, lik, grad, s);
   if (cfg->precision == MGB_PREC_BF16)
     return logreg_tc(dat, beta, P, active, cfg->N, lik, grad, ws, ws_bytes, s);
   MGB_SMC_D_DISPATCH(logreg_f32, dat.X, dat.y, dat.n_data, beta, P, active, cfg->N, lik, grad, ws, ws_bytes, s);
 }
+
+static SMCParams smc_params(const mgb_smc_logreg_config *cfg) {
+  return SMCParams{cfg->ess_threshold_retain, cfg->max_temperature, cfg->bisection_tol, cfg->max_bisection_iter,
+                   cfg->max_iter,           cfg->mcmc_steps,      cfg->n_schedule > 0 ? cfg->schedule_dev : nullptr,
+                   cfg->n_schedule};
+}
+
+// key split of the MCMC sampler's startup: Underdamped (key, prior, lik) = split(key, 3), RandomWalk 2
+static int smc_msplit(const mgb_smc_logreg_config *cfg) { return cfg->move == MGB_MOVE_RANDOM_WALK ? 2 : 3; }
 
 template <int D>
 static int smc_init_t(const mgb_smc_logreg_config *cfg, const SMCData &dat, const uint32_t *keys, SMCView v,
                       void *pws, size_t pws_bytes, cudaStream_t s) {
   const int64_t P = (int64_t)cfg->B * cfg->N;
   const unsigned g = (unsigned)((P + SMC_TPB - 1) / SMC_TPB);
-  k_smc_prior<D><<<g, SMC_TPB, 0, s>>>(v, keys, cfg->prior_scale);
+  const float sscale = cfg->prior_sample_scale > 0.0f ? cfg->prior_sample_scale : cfg->prior_scale;
+  k_smc_prior<D><<<g, SMC_TPB, 0, s>>>(v, keys, sscale, smc_msplit(cfg));
   int st = launch_status();
   if (st) return st;
   if ((st = smc_potential(cfg, dat, v.beta, v.lik, v.glik, nullptr, pws, pws_bytes, s))) return st;
-  SMCParams sp{cfg->ess_threshold_retain, cfg->max_temperature, cfg->bisection_tol, cfg->max_bisection_iter,
-               cfg->max_iter, cfg->mcmc_steps};
   if (cudaMemsetAsync(v.alpha, 0, sizeof(float) * P, s) != cudaSuccess) return ERR_CUDA;
-  k_smc_adapt<<<cfg->B, ADAPT_TPB, 0, s>>>(v, v.lik, sp, 1);
+  k_smc_adapt<<<cfg->B, ADAPT_TPB, 0, s>>>(v, v.lik, smc_params(cfg), 1);
   return launch_status();
 }
 
@@ -614,7 +773,7 @@ static int smc_step_t(const mgb_smc_logreg_config *cfg, const SMCData &dat, SMCV
   const unsigned g = (unsigned)((P + SMC_TPB - 1) / SMC_TPB);
   const float inv_s2 = (float)(1.0 / ((double)cfg->prior_scale * (double)cfg->prior_scale));
   int st;
-  k_smc_keys<<<g, SMC_TPB, 0, s>>>(v, cfg->ess_threshold_resample);
+  k_smc_keys<<<g, SMC_TPB, 0, s>>>(v, cfg->ess_threshold_resample, smc_msplit(cfg));
   if ((st = launch_status())) return st;
   const size_t rs_smem = sizeof(uint64_t) * (size_t)cfg->N;
   if (cudaFuncSetAttribute(k_smc_resample, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rs_smem) != cudaSuccess)
@@ -628,23 +787,46 @@ static int smc_step_t(const mgb_smc_logreg_config *cfg, const SMCData &dat, SMCV
   std::swap(w.beta, w.beta_p);
   std::swap(w.glik, w.glik_p);
   std::swap(w.lik, w.lik_p);
+  std::swap(w.ms, w.ms_p);
+  const float eps = cfg->stepsize;
+  const bool rw = cfg->move == MGB_MOVE_RANDOM_WALK;
+  const int L = cfg->leapfrog_steps > 0 ? cfg->leapfrog_steps : 1;
+  // OU refresh factors exp(-f eps), sqrt(1 - exp(-2 f eps)) in float32 (standard_mcmc.py:112-118)
+  float c1 = 0.0f, c2 = 1.0f;
+  if (!rw && cfg->friction > 0.0f && std::isfinite(cfg->friction)) {
+    c1 = std::exp(-cfg->friction * eps);
+    c2 = std::sqrt(1.0f - std::exp(-2.0f * cfg->friction * eps));
+  }
+  const float sq = std::sqrt(eps);
   for (int m = 0; m < cfg->mcmc_steps; ++m) {
-    k_mala_pre<D><<<g, SMC_TPB, 0, s>>>(w, cfg->stepsize, inv_s2);
+    if (rw) {
+      k_rw_pre<D><<<g, SMC_TPB, 0, s>>>(w, sq);
+    } else {
+      k_ud_pre<D><<<g, SMC_TPB, 0, s>>>(w, eps, c1, c2, inv_s2);
+    }
     if ((st = launch_status())) return st;
     if ((st = smc_potential(cfg, dat, w.beta_p, w.lik_p, w.glik_p, w.active, pws, pws_bytes, s))) return st;
-    k_mala_post<D><<<g, SMC_TPB, 0, s>>>(w, cfg->stepsize, inv_s2);
+    for (int l = 1; !rw && l < L; ++l) {
+      k_lf_mid<D><<<g, SMC_TPB, 0, s>>>(w, eps, inv_s2);
+      if ((st = launch_status())) return st;
+      if ((st = smc_potential(cfg, dat, w.beta_p, w.lik_p, w.glik_p, w.active, pws, pws_bytes, s))) return st;
+    }
+    if (rw) {
+      k_rw_post<D><<<g, SMC_TPB, 0, s>>>(w, inv_s2);
+    } else {
+      k_ud_post<D><<<g, SMC_TPB, 0, s>>>(w, eps, L, inv_s2);
+    }
     if ((st = launch_status())) return st;
   }
   k_smc_after<D><<<g, SMC_TPB, 0, s>>>(w, inv_s2);
   if ((st = launch_status())) return st;
-  SMCParams sp{cfg->ess_threshold_retain, cfg->max_temperature, cfg->bisection_tol, cfg->max_bisection_iter,
-               cfg->max_iter, cfg->mcmc_steps};
-  k_smc_adapt<<<cfg->B, ADAPT_TPB, 0, s>>>(w, w.lik_w, sp, 0);
+  k_smc_adapt<<<cfg->B, ADAPT_TPB, 0, s>>>(w, w.lik_w, smc_params(cfg), 0);
   if ((st = launch_status())) return st;
   // the state lives in the swapped buffers now: copy back so the layout stays fixed
   if (cudaMemcpyAsync(v.beta, w.beta, sizeof(float) * P * D, cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
       cudaMemcpyAsync(v.glik, w.glik, sizeof(float) * P * D, cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
-      cudaMemcpyAsync(v.lik, w.lik, sizeof(float) * P, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+      cudaMemcpyAsync(v.lik, w.lik, sizeof(float) * P, cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
+      cudaMemcpyAsync(v.ms, w.ms, sizeof(float) * P * D, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
     return ERR_CUDA;
   return OK;
 }
@@ -719,8 +901,8 @@ int mgb_smc_logreg_views(const mgb_smc_logreg_config *cfg, void *ws, mgb_smc_vie
 static int smc_setup(const mgb_smc_logreg_config *cfg, const float *X, const float *y, const void *Xbf16,
                      int64_t n_data, void *ws, size_t ws_bytes, SMCData &dat, SMCView &v, void *&pws,
                      size_t &pws_bytes) {
-  if (!smc_cfg_ok(cfg) || !X || !y || n_data < 1 || !ws) return ERR_BAD_ARG;
-  if (cfg->precision == MGB_PREC_BF16 && !Xbf16) return ERR_BAD_ARG;
+  if (!smc_cfg_ok(cfg) || (!smc_gauss(cfg) && (!X || !y)) || n_data < 1 || !ws) return ERR_BAD_ARG;
+  if (cfg->precision == MGB_PREC_BF16 && !smc_gauss(cfg) && !Xbf16) return ERR_BAD_ARG;
   if (ws_bytes < mgb_smc_logreg_workspace(cfg, n_data)) return ERR_WORKSPACE;
   Carver c(ws);
   v = carve_smc(c, cfg->B, cfg->N, cfg->d, cfg->max_iter + 1);

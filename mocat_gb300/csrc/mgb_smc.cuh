@@ -10,7 +10,8 @@ struct SMCView {
   int32_t B, N, D, H;
   float *beta, *beta_p;      // (B N, D) state / proposal rows
   float *glik, *glik_p;      // (B N, D) likelihood-potential gradients
-  float *mom, *phalf;        // (B N, D) momentum, half-step momentum
+  float *mom, *phalf;        // (B N, D) momentum at the move's start, half-step momentum of the proposal
+  float *ms, *ms_p;          // (B N, D) Underdamped momenta kept between moves (and their gathered copy)
   float *lik, *lik_p, *lik_w;  // (B N) likelihood potential: state, proposal, (U - prior) / tau
   float *lw, *alpha;         // (B N) log-weights, acceptance-probability sums
   uint32_t *pkey;            // (B N, 2) MCMC keys
@@ -27,6 +28,8 @@ struct SMCView {
 struct SMCParams {
   float retain, max_temp, tol;
   int32_t max_bisect, max_iter, mcmc_steps;
+  const float *sched;  // temperature schedule (nullptr: adaptive)
+  int32_t n_sched;
 };
 
 struct SMCData {

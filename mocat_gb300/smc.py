@@ -1,12 +1,15 @@
-"""Tempered SMC sampler with MALA moves on Bayesian logistic regression
-(mocat/src/transport/smc.py:229-373, mocat/src/mcmc/standard_mcmc.py:72-153,
-mocat/src/mcmc/metropolis.py:48-70, driven as mocat.run, mocat/src/sample.py:110-148),
-running on the GPU for B independent posteriors at once.
+"""Tempered SMC sampler (mocat/src/transport/smc.py:100-373) with Underdamped / MALA / HMC
+or RandomWalk moves (mocat/src/mcmc/standard_mcmc.py:20-153) and the Metropolis correction
+(mocat/src/mcmc/metropolis.py:48-70), adaptive or scheduled temperatures, driven as
+mocat.run (mocat/src/sample.py:110-148), running on the GPU for B independent posteriors
+at once, on Bayesian logistic regression or the Gaussian toy scenario.
 
     scenario = LogisticRegression(X, y, prior_scale=1.0)
     sampler = MetropolisedSMCSampler(Underdamped(stepsize=0.01), mcmc_steps=5, ess_threshold_retain=0.5)
     out = run(scenario, sampler, n=16384, random_key=PRNGKey(0))             # one posterior
     outs = run_batched(scenario, sampler, n=16384, random_keys=keys)          # B posteriors
+    run(Gaussian(covariance=S, prior_scale=49.0, prior_sample_scale=7.0),
+        MetropolisedSMCSampler(RandomWalk(stepsize=1.0)), 10000, key, temperature_schedule=sched)
 
 Differences from the reference, by design:
   * resampling (ess <= ess_threshold_resample n) is systematic, O(n), instead of
@@ -89,18 +92,66 @@ class LogisticRegression(Scenario):
 
 
 class Underdamped:
-    """Underdamped Langevin / HMC proposal (standard_mcmc.py:72-153).  The GPU sampler
-    takes the MALA setting leapfrog_steps=1, friction=inf."""
+    """Underdamped Langevin proposal (standard_mcmc.py:72-153): leapfrog_steps leapfrog steps of
+    the tempered potential, momenta refreshed by the OU solution with the given friction
+    (infinite friction: fresh momenta, i.e. HMC, and MALA for one leapfrog step)."""
     name = "Underdamped"
 
     def __init__(self, stepsize=None, leapfrog_steps=1, friction=math.inf):
         self.stepsize = stepsize
-        self.leapfrog_steps = leapfrog_steps
-        self.friction = friction
+        self.leapfrog_steps = int(leapfrog_steps)
+        self.friction = float(friction)
+
+
+class RandomWalk:
+    """Random-walk proposal x + sqrt(stepsize) N(0, I) (standard_mcmc.py:20-64)."""
+    name = "Random Walk"
+
+    def __init__(self, stepsize=None):
+        self.stepsize = stepsize
+
+
+class Gaussian(Scenario):
+    """toy_examples.Gaussian (mocat/src/scenarios/toy_examples.py:17-51): likelihood potential
+    0.5 |(x - mean) @ precision_sqrt^T|^2 with precision_sqrt = inv(chol(covariance)).  The GPU
+    sampler's prior is N(0, prior_scale^2 I) in the potential (prior_scale = inf: flat) and draws
+    prior_sample_scale N(0, I) (defaults to prior_scale), covering a scenario whose prior_sample
+    and prior_potential are set separately."""
+    name = "Gaussian"
+
+    def __init__(self, dim=None, mean=None, covariance=None, prior_scale=1.0, prior_sample_scale=None, name=None):
+        if covariance is not None:
+            cov = np.asarray(covariance.cpu() if isinstance(covariance, torch.Tensor) else covariance, np.float64)
+            d = cov.shape[-1] if cov.ndim else (int(dim) if dim is not None else 1)
+        else:
+            d = int(dim) if dim is not None else (np.asarray(mean).shape[-1] if mean is not None else 1)
+            cov = np.ones(d)
+        if cov.ndim < 2:
+            cov = np.diag(np.broadcast_to(cov, (d,)))
+        self.dim = d
+        self.mean = np.zeros(d) if mean is None else np.asarray(mean, np.float64).reshape(d)
+        self.covariance = cov
+        self.precision_sqrt = np.linalg.inv(np.linalg.cholesky(cov))
+        self.prior_scale = float(prior_scale)
+        self.prior_sample_scale = self.prior_scale if prior_sample_scale is None else float(prior_sample_scale)
+        dev = _dev.device()
+        self._m = torch.as_tensor(self.mean.astype(np.float32), device=dev).contiguous()
+        self._ps = torch.as_tensor(self.precision_sqrt.astype(np.float32), device=dev).contiguous()
+        super().__init__(name=name)
+
+    def prior_potential(self, x, random_key=None):
+        x = _dev.as_f32(x)
+        return 0.5 * (x * x).sum(-1) / self.prior_scale ** 2
+
+    def likelihood_potential(self, x, random_key=None):
+        z = (_dev.as_f32(x) - self._m) @ self._ps.T
+        return 0.5 * (z * z).sum(-1)
 
 
 class MetropolisedSMCSampler:
-    """Tempered SMC with MCMC moves and adaptive temperatures (smc.py:229-373)."""
+    """Tempered SMC with MCMC moves (smc.py:229-373), adaptive temperatures or a
+    temperature_schedule (its leading 0 removed; max_temperature and max_iter follow it,
+    smc.py:113-125, :243-245)."""
     name = "Metropolised SMC Sampler"
 
     def __init__(self, mcmc_sampler, mcmc_correction="sampler_default", mcmc_steps=1, max_iter=int(1e4),
@@ -108,13 +159,12 @@ class MetropolisedSMCSampler:
                  ess_threshold_resample=0.5, bisection_tol=1e-5, max_bisection_iter=1000):
         if isinstance(mcmc_sampler, type):
             mcmc_sampler = mcmc_sampler()
-        if temperature_schedule is not None:
-            raise NotImplementedError("the GPU sampler takes adaptive temperatures (temperature_schedule=None)")
         if mcmc_correction not in ("sampler_default", "Metropolis"):
             raise NotImplementedError("the GPU sampler uses the Metropolis correction")
-        if not isinstance(mcmc_sampler, Underdamped) or mcmc_sampler.leapfrog_steps != 1 \
-                or mcmc_sampler.friction != math.inf or mcmc_sampler.stepsize is None:
-            raise NotImplementedError("the GPU sampler moves with MALA: Underdamped(stepsize, 1, inf)")
+        if not isinstance(mcmc_sampler, (Underdamped, RandomWalk)) or mcmc_sampler.stepsize is None:
+            raise NotImplementedError("the GPU sampler moves with Underdamped(stepsize, ...) or RandomWalk(stepsize)")
+        if isinstance(mcmc_sampler, Underdamped) and mcmc_sampler.leapfrog_steps < 1:
+            raise ValueError("leapfrog_steps must be >= 1")
         self.mcmc_sampler = mcmc_sampler
         self.mcmc_steps = int(mcmc_steps)
         self.max_iter = int(max_iter)
@@ -123,6 +173,23 @@ class MetropolisedSMCSampler:
         self.ess_threshold_resample = float(ess_threshold_resample)
         self.bisection_tol = float(bisection_tol)
         self.max_bisection_iter = int(max_bisection_iter)
+        self.temperature_schedule = None
+        self.set_schedule(temperature_schedule)
+
+    def set_schedule(self, temperature_schedule):
+        """TemperedSMCSampler.__setattr__ (smc.py:113-125, :261-265)"""
+        if temperature_schedule is None:
+            self.temperature_schedule = None
+            return
+        sch = np.asarray(temperature_schedule.cpu() if isinstance(temperature_schedule, torch.Tensor)
+                         else temperature_schedule, np.float32).reshape(-1)
+        if sch.size and sch[0] == 0.0:
+            sch = sch[1:]
+        if sch.size == 0:
+            raise ValueError("empty temperature schedule")
+        self.temperature_schedule = sch
+        self.max_temperature = float(sch[-1])
+        self.max_iter = int(sch.size)
 
 
 class BatchedSMC:
@@ -130,7 +197,8 @@ class BatchedSMC:
     ``done()``, or ``run()``.  The workspace stays on the device between calls."""
 
     def __init__(self, scenario, sampler, n, random_keys, precision="fp32", max_iter=None):
-        if not isinstance(scenario, LogisticRegression):
+        gauss = isinstance(scenario, Gaussian)
+        if not gauss and not isinstance(scenario, LogisticRegression):
             raise NotImplementedError(f"{scenario.__class__.__name__}: no GPU SMC kernel for this scenario")
         if scenario.dim not in SUPPORTED_D:
             raise NotImplementedError(f"d = {scenario.dim} not compiled (supported {SUPPORTED_D})")
@@ -140,19 +208,33 @@ class BatchedSMC:
         self.scenario, self.sampler = scenario, sampler
         self.B, self.n = keys.shape[0], int(n)
         mi = sampler.max_iter if max_iter is None else int(max_iter)
-        self.cfg = _lib.SMCConfig(self.B, self.n, scenario.dim, sampler.mcmc_steps, sampler.mcmc_sampler.stepsize,
+        mv = sampler.mcmc_sampler
+        rw = isinstance(mv, RandomWalk)
+        sch = sampler.temperature_schedule
+        self._sched = None if sch is None else torch.as_tensor(sch, device=keys.device).contiguous()
+        fr = 0.0 if rw or not math.isfinite(mv.friction) else float(mv.friction)
+        self.cfg = _lib.SMCConfig(self.B, self.n, scenario.dim, sampler.mcmc_steps, mv.stepsize,
                                   scenario.prior_scale, sampler.ess_threshold_retain, sampler.ess_threshold_resample,
                                   sampler.bisection_tol, sampler.max_bisection_iter, sampler.max_temperature,
-                                  min(mi, 100000), PRECISIONS[precision])
+                                  min(mi, 100000), PRECISIONS[precision], 1 if rw else 0,
+                                  1 if rw else mv.leapfrog_steps, fr,
+                                  getattr(scenario, "prior_sample_scale", scenario.prior_scale),
+                                  0 if sch is None else len(sch), _dev.ptr(self._sched), 1 if gauss else 0,
+                                  _dev.ptr(scenario._m) if gauss else None, _dev.ptr(scenario._ps) if gauss else None)
         self.keys = keys
-        self.Xb = scenario.Xbf16() if precision == "bf16" else None
-        self.ws = _dev.workspace(_lib.lib().mgb_smc_logreg_workspace(ctypes.byref(self.cfg), scenario.n_data))
+        self.Xb = scenario.Xbf16() if precision == "bf16" and not gauss else None
+        self.ws = _dev.workspace(_lib.lib().mgb_smc_logreg_workspace(ctypes.byref(self.cfg), self._n_data()))
         self.views = _lib.SMCViews()
         call("mgb_smc_logreg_views", ctypes.byref(self.cfg), _dev.ptr(self.ws), ctypes.byref(self.views))
         self.iterations = 0
 
+    def _n_data(self):
+        return self.scenario.n_data if isinstance(self.scenario, LogisticRegression) else 1
+
     def _args(self):
         sc = self.scenario
+        if isinstance(sc, Gaussian):
+            return (ctypes.byref(self.cfg), None, None, None, 1)
         return (ctypes.byref(self.cfg), _dev.ptr(sc.X), _dev.ptr(sc.y), _dev.ptr(self.Xb), sc.n_data)
 
     def _tensor(self, name, shape, dtype):
@@ -203,15 +285,19 @@ class BatchedSMC:
                      iterations=it, grad_log_norm_constant_prior_scale=self.prior_scale_grad())
 
 
-def run_batched(scenario, sampler, n, random_keys, precision="fp32"):
+def run_batched(scenario, sampler, n, random_keys, precision="fp32", temperature_schedule=None):
     """mocat.run(scenario, sampler, n, key) for each of B keys, in one batch.  Fields carry a
-    leading B axis; per-iteration arrays are padded past each posterior's last iteration."""
+    leading B axis; per-iteration arrays are padded past each posterior's last iteration.
+    temperature_schedule (a run() keyword in the reference) sets the sampler's schedule."""
+    if temperature_schedule is not None:
+        sampler.set_schedule(temperature_schedule)
     return BatchedSMC(scenario, sampler, n, random_keys, precision).run()
 
 
-def run(scenario, sampler, n, random_key, precision="fp32"):
-    """mocat.run (sample.py:110-148) for MetropolisedSMCSampler on a LogisticRegression scenario."""
-    out = run_batched(scenario, sampler, n, _dev.as_key(random_key).reshape(1, 2), precision)
+def run(scenario, sampler, n, random_key, precision="fp32", temperature_schedule=None):
+    """mocat.run (sample.py:110-148) for MetropolisedSMCSampler on a LogisticRegression or
+    Gaussian scenario.  temperature: the per-iteration temperatures (entry 0 after startup)."""
+    out = run_batched(scenario, sampler, n, _dev.as_key(random_key).reshape(1, 2), precision, temperature_schedule)
     L = int(out.iterations[0]) + 1
     return cdict(value=out.value[0], log_weight=out.log_weight[0],
                  likelihood_potential=out.likelihood_potential[0], temperature=out.temperature[0, :L],

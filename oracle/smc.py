@@ -1,11 +1,12 @@
-"""Float64 restatement of the GPU tempered SMC sampler on logistic regression --
-test infrastructure only (the checker of mgb_smc_logreg_*, never the product).
+"""Float64 restatement of the GPU tempered SMC sampler on logistic regression and the
+Gaussian toy scenario -- test infrastructure only (the checker of mgb_smc_logreg_*,
+never the product).
 
 Follows mocat's MetropolisedSMCSampler (mocat/src/transport/smc.py:128-164,
-193-226, 267-373) with MALA moves (Underdamped(leapfrog_steps=1, friction=inf),
-mocat/src/mcmc/standard_mcmc.py:72-153; utils.leapfrog mocat/src/utils.py:108-156;
+193-226, 267-373) with Underdamped moves (any leapfrog_steps and friction; MALA for 1 and inf) or
+RandomWalk moves (mocat/src/mcmc/standard_mcmc.py:20-153; utils.leapfrog mocat/src/utils.py:108-156;
 Metropolis.correct mocat/src/mcmc/metropolis.py:48-70), regula-falsi
-temperatures (utils.bisect mocat/src/utils.py:205-237) and the key schedule of
+temperatures (utils.bisect mocat/src/utils.py:205-237) or a temperature schedule and the key schedule of
 mocat.run (mocat/src/sample.py:110-148), with the same two choices as the GPU
 sampler: systematic resampling and no re-evaluation of the (deterministic)
 potentials at the start of each MCMC block.  Draws come from the oracle's
@@ -68,30 +69,63 @@ def _bisect(f, b0, b1, tol, max_iter):
     return b1 if abs(e1) < abs(e0) else b0
 
 
+def gaussian_potential_grad(mean, prec_sqrt, beta):
+    """toy_examples.Gaussian likelihood (mocat/src/scenarios/toy_examples.py:40-44) in float64:
+    z = (x - mean) @ prec_sqrt^T, lik = |z|^2 / 2, grad = z @ prec_sqrt."""
+    z = (np.asarray(beta, np.float64) - np.asarray(mean, np.float64)) @ np.asarray(prec_sqrt, np.float64).T
+    return 0.5 * (z * z).sum(1), z @ np.asarray(prec_sqrt, np.float64)
+
+
 def run(X, y, prior_scale, N, key, stepsize, mcmc_steps=5, retain=0.5, resample_thr=0.5, tol=1e-5,
         max_bisect=1000, max_temp=1.0, max_iter=1000):
-    """Returns dict(temperature, log_norm_constant, ess, alpha, resampled (per iteration,
-    entry 0 = after startup), value (N, d) final particles, accepts (list of (N,) bool per move))."""
-    X = np.asarray(X, np.float64)
-    d = X.shape[1]
+    """Logistic regression with MALA moves; see run_general."""
+    return run_general(lambda b: potential_grad(X, y, b), np.asarray(X).shape[1], prior_scale, N, key, stepsize,
+                       mcmc_steps=mcmc_steps, retain=retain, resample_thr=resample_thr, tol=tol,
+                       max_bisect=max_bisect, max_temp=max_temp, max_iter=max_iter)
+
+
+def run_general(lik_fn, d, prior_scale, N, key, stepsize, mcmc_steps=5, retain=0.5, resample_thr=0.5, tol=1e-5,
+                max_bisect=1000, max_temp=1.0, max_iter=1000, move="underdamped", leapfrog_steps=1,
+                friction=math.inf, sample_scale=None, schedule=None):
+    """lik_fn(beta (P, d)) -> (lik (P,), grad (P, d)).  move "underdamped" (leapfrog_steps, friction;
+    standard_mcmc.py:72-153) or "random_walk" (standard_mcmc.py:20-64); schedule: the
+    temperature_schedule without its leading 0 (max_temp, max_iter follow it).  Returns
+    dict(temperature, log_norm_constant, ess, alpha, resampled (per iteration, entry 0 = after
+    startup), value (N, d) final particles, accepts (list of (N,) bool per move))."""
+    rw = move == "random_walk"
+    if schedule is not None:
+        schedule = np.asarray(schedule, np.float32)
+        max_temp, max_iter = float(schedule[-1]), len(schedule)
     s2inv = np.float64(np.float32(1.0 / (prior_scale * prior_scale)))
+    sscale = np.float32(prior_scale if sample_scale is None else sample_scale)
+    msplit = 2 if rw else 3
     ek = _split(key, 2)
     e, sub = ek[0], ek[1]
     pk = _split(sub, N)
-    beta = np.stack([(O.normal(pk[j], (d,)) * np.float32(prior_scale)).astype(np.float32) for j in range(N)])
+    beta = np.stack([(O.normal(pk[j], (d,)) * sscale).astype(np.float32) for j in range(N)])
     beta = beta.astype(np.float64)
     e = _split(e, 2 * N + 1)[2 * N]
-    e = _split(e, 3)[0]
-    lik, glik = potential_grad(X, y, beta)
+    e = _split(e, msplit)[0]
+    lik, glik = lik_fn(beta)
+    ms = np.zeros((N, d))
     prior = lambda b: 0.5 * (b * b).sum(1) * s2inv
+    gradU = lambda b, g, tau: b * s2inv + tau * g
+    if not rw and math.isfinite(friction) and friction > 0:
+        c1 = float(np.float32(math.exp(-friction * stepsize)))
+        c2 = float(np.float32(math.sqrt(1.0 - math.exp(-2.0 * friction * stepsize))))
+    else:
+        c1, c2 = 0.0, 1.0
 
-    def adapt(lw_res, ess_res, tau0, ell):
-        target = math.log(ess_res * retain)
-        f = lambda x: _logess(lw_res - (x - tau0) * ell) - target
-        tau1 = _bisect(f, tau0, max_temp, tol, max_bisect)
+    def adapt(lw_res, ess_res, tau0, ell, it):
+        if schedule is not None:
+            tau1 = float(schedule[min(it, len(schedule) - 1)])
+        else:
+            target = math.log(ess_res * retain)
+            f = lambda x: _logess(lw_res - (x - tau0) * ell) - target
+            tau1 = _bisect(f, tau0, max_temp, tol, max_bisect)
         return tau1, lw_res - (tau1 - tau0) * ell
 
-    tau, lw = adapt(np.zeros(N), float(N), 0.0, lik)
+    tau, lw = adapt(np.zeros(N), float(N), 0.0, lik, 0)
     ess = math.exp(_logess(lw))
     logz = _lse(lw) - math.log(N)
     hist = dict(temperature=[tau], log_norm_constant=[logz], ess=[ess], alpha=[1.0], resampled=[False],
@@ -100,35 +134,49 @@ def run(X, y, prior_scale, N, key, stepsize, mcmc_steps=5, retain=0.5, resample_
     while not (tau >= max_temp or it >= max_iter):
         res = ess <= resample_thr * N
         keys_all = _split(e, N + 2)
-        pkeys = [_split(keys_all[j], 3)[0] for j in range(N)]
+        pkeys = [_split(keys_all[j], msplit)[0] for j in range(N)]
         if res:
             m23 = int(O.random_bits(keys_all[N], 1)[0]) >> 9
             anc = O.resample_systematic(lw.astype(np.float32), m23)
-            beta, lik, glik = beta[anc], lik[anc], glik[anc]
+            beta, lik, glik, ms = beta[anc], lik[anc], glik[anc], ms[anc]
             lw_res, ess_res = np.zeros(N), float(N)
         else:
             lw_res, ess_res = lw, ess
         e = keys_all[N + 1]
         asum = np.zeros(N)
         for _ in range(mcmc_steps):
-            mom = np.empty((N, d))
-            for j in range(N):
-                kk = _split(pkeys[j], 2)
-                pkeys[j] = kk[0]
-                mom[j] = O.normal(kk[1], (d,))
-            gu = beta * s2inv + tau * glik
-            ph = mom - stepsize / 2.0 * gu
-            bn = beta + stepsize * ph
-            ln, gn = potential_grad(X, y, bn)
             U = prior(beta) + tau * lik
-            Un = prior(bn) + tau * ln
-            pn = ph - stepsize / 2.0 * (bn * s2inv + tau * gn)
-            with np.errstate(over="ignore", invalid="ignore"):
-                alpha = np.minimum(1.0, np.exp(-Un + U - 0.5 * (pn * pn).sum(1) + 0.5 * (mom * mom).sum(1)))
+            if rw:
+                noise = np.empty((N, d))
+                for j in range(N):
+                    kk = _split(pkeys[j], 3)
+                    pkeys[j] = kk[0]
+                    noise[j] = O.normal(kk[1], (d,))
+                bn = beta + float(np.float32(math.sqrt(stepsize))) * noise
+                ln, gn = lik_fn(bn)
+                Un = prior(bn) + tau * ln
+                with np.errstate(over="ignore", invalid="ignore"):
+                    alpha = np.minimum(1.0, np.exp(-Un + U))
+            else:
+                mom = np.empty((N, d))
+                for j in range(N):
+                    kk = _split(pkeys[j], 2)
+                    pkeys[j] = kk[0]
+                    mom[j] = -ms[j] * c1 + c2 * O.normal(kk[1], (d,))
+                p = mom
+                bn, gn = beta, glik
+                for _l in range(leapfrog_steps):
+                    ph = p - stepsize / 2.0 * gradU(bn, gn, tau)
+                    bn = bn + stepsize * ph
+                    ln, gn = lik_fn(bn)
+                    p = ph - stepsize / 2.0 * gradU(bn, gn, tau)
+                Un = prior(bn) + tau * ln
+                with np.errstate(over="ignore", invalid="ignore"):
+                    alpha = np.minimum(1.0, np.exp(-Un + U - 0.5 * (p * p).sum(1) + 0.5 * (mom * mom).sum(1)))
             alpha = np.where(np.isnan(alpha), 0.0, alpha)
             u = np.empty(N)
             for j in range(N):
-                k2 = _split(pkeys[j], 2)[0]
+                k2 = pkeys[j] if rw else _split(pkeys[j], leapfrog_steps + 1)[0]
                 kk = _split(k2, 2)
                 pkeys[j] = kk[0]
                 u[j] = O.uniform(kk[1], ())
@@ -137,10 +185,12 @@ def run(X, y, prior_scale, N, key, stepsize, mcmc_steps=5, retain=0.5, resample_
             beta = np.where(acc[:, None], bn, beta)
             lik = np.where(acc, ln, lik)
             glik = np.where(acc[:, None], gn, glik)
+            if not rw:
+                ms = np.where(acc[:, None], -p, mom)
             asum += alpha
         U = prior(beta) + tau * lik
         ell = (U - prior(beta)) / tau
-        tau1, lw = adapt(lw_res, ess_res, tau, ell)
+        tau1, lw = adapt(lw_res, ess_res, tau, ell, it + 1)
         logz += _lse(lw) - (math.log(N) if res else _lse(lw_res))
         ess = math.exp(_logess(lw))
         tau = tau1

@@ -135,3 +135,90 @@ def test_prior_scale_gradient_matches_quadrature(cuda):
     g = out.grad_log_norm_constant_prior_scale.cpu().numpy()
     se = g.std() / np.sqrt(len(g))
     assert abs(g.mean() - exact) < 4 * se + 0.01, (g.mean(), exact, se)
+
+
+COV = np.array([[1.0, 0.9], [0.9, 2.0]])
+
+
+def _general_case(name):
+    """(scenario, sampler, restatement kwargs, lik_fn, d) of the generalised moves"""
+    import mocat_gb300 as mg
+    if name.startswith("gauss"):
+        sc = mg.smc.Gaussian(covariance=COV, prior_scale=7.0)
+        ps = np.linalg.inv(np.linalg.cholesky(COV))
+        fn, d = (lambda b: osmc.gaussian_potential_grad(np.zeros(2), ps, b)), 2
+    else:
+        d = 3 if name == "logreg_hmc" else 5
+        X, y = _data(150, d, 7)
+        sc = mg.smc.LogisticRegression(X, y, prior_scale=1.0)
+        fn = (lambda X, y: (lambda b: osmc.potential_grad(X, y, b)))(X, y)
+    if name == "gauss_rw_schedule":
+        sch = np.arange(0.1, 1.01, 0.15).astype(np.float32)
+        smp = mg.smc.MetropolisedSMCSampler(mg.smc.RandomWalk(stepsize=1.0), mcmc_steps=2, temperature_schedule=sch)
+        kw = dict(stepsize=1.0, mcmc_steps=2, move="random_walk", schedule=sch)
+    elif name == "gauss_ud_friction":
+        smp = mg.smc.MetropolisedSMCSampler(mg.smc.Underdamped(stepsize=0.4, leapfrog_steps=3, friction=1.0),
+                                            mcmc_steps=2, ess_threshold_retain=0.6)
+        kw = dict(stepsize=0.4, mcmc_steps=2, retain=0.6, leapfrog_steps=3, friction=1.0)
+    elif name == "logreg_hmc":
+        smp = mg.smc.MetropolisedSMCSampler(mg.smc.Underdamped(stepsize=0.1, leapfrog_steps=2), mcmc_steps=2,
+                                            ess_threshold_retain=0.6)
+        kw = dict(stepsize=0.1, mcmc_steps=2, retain=0.6, leapfrog_steps=2)
+    else:
+        smp = mg.smc.MetropolisedSMCSampler(mg.smc.RandomWalk(stepsize=0.01), mcmc_steps=3, ess_threshold_retain=0.6)
+        kw = dict(stepsize=0.01, mcmc_steps=3, retain=0.6, move="random_walk")
+    return sc, smp, kw, fn, d
+
+
+@pytest.mark.parametrize("name", ["gauss_rw_schedule", "gauss_ud_friction", "logreg_hmc", "logreg_rw"])
+def test_general_moves_match_restatement(cuda, name):
+    """RandomWalk moves, Underdamped with several leapfrog steps and a finite friction (momenta
+    kept and resampled with the particles), temperature schedules and the Gaussian scenario,
+    against the float64 restatement with the same draws (tolerances as above)"""
+    import mocat_gb300 as mg
+    sc, smp, kw, fn, d = _general_case(name)
+    N = 64
+    keys = np.stack([O.PRNGKey(31), O.PRNGKey(32)])
+    out = mg.smc.run_batched(sc, smp, N, keys)
+    for b in range(2):
+        ref = osmc.run_general(fn, d, sc.prior_scale, N, keys[b], **kw)
+        L = int(out.iterations[b]) + 1
+        assert L == len(ref["temperature"]), (L, len(ref["temperature"]))
+        np.testing.assert_allclose(out.temperature[b, :L].cpu().numpy(), ref["temperature"], rtol=1e-4)
+        assert np.array_equal(out.resampled[b, :L].cpu().numpy(), ref["resampled"])
+        np.testing.assert_allclose(out.alpha[b, :L].cpu().numpy(), ref["alpha"], rtol=1e-4, atol=1e-5)
+        np.testing.assert_allclose(out.log_norm_constant[b, :L].cpu().numpy(), ref["log_norm_constant"], rtol=1e-4,
+                                   atol=1e-5)
+        np.testing.assert_allclose(out.value[b].cpu().numpy(), ref["value"], atol=1e-3)
+    if "schedule" in kw:
+        assert np.array_equal(out.temperature[0, :L].cpu().numpy(), kw["schedule"])
+
+
+@pytest.mark.parametrize("move,schedule", [("rw", True), ("ud", True), ("rw", False), ("ud10", False)])
+def test_reference_transport_checks(cuda, move, schedule):
+    """TestMetropolisedSMC (tests/test_transport.py:121-170): n = 1e4, the correlated Gaussian
+    with prior_sample 7 N(0, I) and prior_potential 0.5 |x / 49|^2; after a categorical resample
+    of the final particles (PRNGKey(1)) the mean is 0 to 0 decimals and the covariance the
+    posterior's to 1 decimal; log_norm_constant equals the tempered closed form to 0 decimals;
+    a preschedule comes back as the temperatures"""
+    import mocat_gb300 as mg
+    sc = mg.smc.Gaussian(covariance=COV, prior_scale=49.0, prior_sample_scale=7.0)
+    mv = {"rw": mg.smc.RandomWalk(stepsize=1.0), "ud": mg.smc.Underdamped(stepsize=1.0),
+          "ud10": mg.smc.Underdamped(stepsize=1.0, leapfrog_steps=10)}[move]
+    pre = np.arange(0.0, 1.1, 0.1).astype(np.float32)
+    n = 10000
+    out = mg.smc.run(sc, mg.smc.MetropolisedSMCSampler(mv), n, mg.random.PRNGKey(0),
+                     temperature_schedule=pre if schedule else None)
+    lw = out.log_weight.cpu().numpy()
+    idx = O.resample_gumbel(lw, O.PRNGKey(1), n)
+    x = out.value.cpu().numpy()[idx].astype(np.float64)
+    post = np.linalg.inv(np.linalg.inv(COV) + np.eye(2) / 49.0)
+    np.testing.assert_array_almost_equal(x.mean(0), np.zeros(2), decimal=0)
+    np.testing.assert_array_almost_equal(np.cov(x.T), post, decimal=1)
+    temps = out.temperature.cpu().numpy().astype(np.float64)
+    lik_prec = np.linalg.inv(COV)
+    dets = np.array([np.linalg.det(np.linalg.inv(lik_prec * t + np.eye(2) / 49.0)) for t in temps])
+    np.testing.assert_array_almost_equal(out.log_norm_constant.cpu().numpy(), 0.5 * (np.log(dets) - 4 * np.log(7.0)),
+                                         0)
+    if schedule:
+        assert np.array_equal(out.temperature.cpu().numpy(), pre[1:])
