@@ -370,6 +370,22 @@ typedef struct {
   float m0;   /* initial_mean */
 } mgb_sv_model;
 
+/* One series with the particle history: run_particle_filter_for_marginals
+ * (filtering.py:255-324) with BootstrapFilter on StochasticVolatility (dim 1),
+ * outputs as mgb_pf_lg_run with d = 1.  Here model->bsig is
+ * transition_covariance_sqrt (the dt = 1 value): step t scales it by
+ * sqrt(t_dev[t] - t_dev[t-1]) (propagate: by sqrt(dt)).  Systematic resampling
+ * with even n <= 2^21 runs as one persistent launch. */
+int mgb_pf_sv_init(const mgb_sv_model *model_host, int64_t n, const uint32_t *key_dev, const float *y0_dev,
+                   float *x_dev, float *lw_dev, void *stream);
+int mgb_pf_sv_propagate(const mgb_sv_model *model_host, int64_t n, const uint32_t *key_dev, const float *y_dev,
+                        float dt, const float *x_prev_dev, const int32_t *ancestors_dev, const float *lw_prev_dev,
+                        float *x_new_dev, float *lw_new_dev, void *stream);
+size_t mgb_pf_sv_workspace(int64_t n, int64_t T, int scheme);
+int mgb_pf_sv_run(const mgb_sv_model *model_host, int64_t n, int64_t T, const uint32_t *key_dev, const float *y_dev,
+                  const float *t_dev, float ess_threshold, int scheme, void *ws_dev, size_t ws_bytes,
+                  const mgb_pf_outputs *out, void *stream);
+
 /* launch shape of a batched run (from mgb_pf_sv_batch_plan / _autotune) */
 typedef struct {
   int32_t threads;     /* CTA size: 256, 512 or 1024 */

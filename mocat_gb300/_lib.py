@@ -146,6 +146,11 @@ _SIGNATURES = {
     "mgb_pf_opt_workspace": ([_I64, _I64, ctypes.c_int32, _I32], _SZ),
     "mgb_pf_opt_run": ([ctypes.POINTER(OptModel), _I64, _I64, _P, _P, _F, _I32, _P, _SZ, ctypes.POINTER(PFOutputs),
                         _P], _I32),
+    "mgb_pf_sv_init": ([ctypes.POINTER(SVModel), _I64, _P, _P, _P, _P, _P], _I32),
+    "mgb_pf_sv_propagate": ([ctypes.POINTER(SVModel), _I64, _P, _P, _F, _P, _P, _P, _P, _P, _P], _I32),
+    "mgb_pf_sv_workspace": ([_I64, _I64, ctypes.c_int], _SZ),
+    "mgb_pf_sv_run": ([ctypes.POINTER(SVModel), _I64, _I64, _P, _P, _P, _F, ctypes.c_int, _P, _SZ,
+                       ctypes.POINTER(PFOutputs), _P], _I32),
     "mgb_pf_nl1d_init": ([ctypes.POINTER(NL1DModel), _I64, _P, _P, _P, _P, _P], _I32),
     "mgb_pf_nl1d_propagate": ([ctypes.POINTER(NL1DModel), _I64, _P, _P, _F, _P, _P, _P, _P, _P, _P], _I32),
     "mgb_pf_nl1d_workspace": ([_I64, _I64, _I32], _SZ),

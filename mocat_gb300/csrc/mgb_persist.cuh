@@ -148,5 +148,7 @@ inline int persist_finish(const PersistArgs &a, int d, const mgb_pf_outputs *out
 int run_lg_persistent(const mgb_lg_model *m, const PersistArgs &a, cudaStream_t s);
 // the one-dimensional non-linear benchmark model; a.aux = 8 cos(1.2 t_{t-1}) per step
 int run_nl_persistent(const mgb_nl1d_model *m, const PersistArgs &a, cudaStream_t s);
+// stochastic volatility, dim 1; a.aux = transition_covariance_sqrt sqrt(t_t - t_{t-1}) per step
+int run_sv_persistent(const mgb_sv_model *m, const PersistArgs &a, cudaStream_t s);
 
 }  // namespace mgb

@@ -3,8 +3,9 @@
 // (one CTA group resident on every SM).  The model enters as a particle policy
 // (the GPU counterpart of the reference's StateSpaceModel plugin): kD, kDY,
 // init() for the initial draw and weight, step() for one propagate + weight
-// from a source state and a carried log-weight; LGModelP (linear-Gaussian) and
-// NLModelP (one-dimensional non-linear benchmark) are the two compiled here.
+// from a source state and a carried log-weight; LGModelP (linear-Gaussian),
+// NLModelP (one-dimensional non-linear benchmark) and SVModelP (stochastic
+// volatility, dim 1) are compiled here.
 //
 // Per step the grid runs
 //   P1  propagate + weight, two particles per thread (i, i + n/2), grid-stride;
@@ -32,6 +33,7 @@
 #include "mgb_lg.cuh"
 #include "mgb_persist.cuh"
 #include "mgb_nl1d.cuh"
+#include "mgb_sv.cuh"
 
 namespace mgb {
 
@@ -493,6 +495,10 @@ int run_lg_persistent(const mgb_lg_model *m, const PersistArgs &a, cudaStream_t 
 
 int run_nl_persistent(const mgb_nl1d_model *m, const PersistArgs &a, cudaStream_t s) {
   return launch_persist(NLModelP{pack_nl(m)}, a, s);
+}
+
+int run_sv_persistent(const mgb_sv_model *m, const PersistArgs &a, cudaStream_t s) {
+  return launch_persist(SVModelP{pack_sv(m)}, a, s);
 }
 
 }  // namespace mgb

@@ -37,17 +37,13 @@
 #include "mgb_internal.cuh"
 #include "mgb_resample.cuh"
 #include "mgb_group.cuh"
+#include "mgb_sv.cuh"
 
 namespace mgb {
 
 constexpr int SVB_MAX_GROUPS = 16;
 constexpr int SVB_MIN_SLOT = 64;
 constexpr size_t SVB_MAX_SMEM = 227 * 1024;
-
-struct SVParams {
-  float phi, bsig, r2, cB, c0, m0;
-  uint32_t one;
-};
 
 struct SVBatch {
   const int32_t *n, *T;
@@ -64,13 +60,6 @@ struct SVBatch {
 };
 
 __host__ __device__ inline size_t sv_slot_bytes(int s) { return (size_t)s * 24 + 16; }
-
-// likelihood_potential (stochastic_volatility.py:96-102) with s = r / exp(x/2):
-// 0.5 y^2 s^2 + 0.5 (log 2 pi - log s^2) = (0.5 y^2 r^2) exp(-x) + (0.5 x + cB)
-__device__ __forceinline__ float sv_potential(const SVParams &p, float x, float y) {
-  const float a = __fmul_rn(__fmul_rn(0.5f, __fmul_rn(y, y)), p.r2);
-  return __fmaf_rn(a, expf_(-x), __fmaf_rn(0.5f, x, p.cB));
-}
 
 // One filter on one thread group (tg = thread in group, wg = warp in group,
 // wcta = warp in CTA, bar = named barrier id, gi = group index).

@@ -186,6 +186,27 @@ class StochasticVolatility(StateSpaceModel):
             self.__dict__["_derived"] = (p, s)
         return self.__dict__["_derived"]
 
+    def simulate(self, t_all, random_key):
+        """StateSpaceModel.simulate (ssm.py:138-163) with this model's samplers
+        (stochastic_volatility.py:71-108): x_0 = e c0 + m0, x_t = phi x_{t-1} + (e sqrt(Q))
+        sqrt(t_t - t_{t-1}), y_t = sqrt(R) exp(x_t / 2) e; normals drawn on the GPU."""
+        p, _ = self.derived()
+        f = np.float32
+        t = np.asarray(t_all.cpu() if isinstance(t_all, torch.Tensor) else t_all, np.float32).reshape(-1)
+        T = t.size
+        keys = mrandom.split(random_key, 2 * T)
+        ex = _normal_keys(keys[:T], 1).cpu().numpy()[:, 0]
+        ey = _normal_keys(keys[T:], 1).cpu().numpy()[:, 0]
+        sq = f(np.sqrt(f(self.transition_covariance[0, 0])))
+        x = np.empty(T, np.float32)
+        x[0] = f(ex[0] * p["c0"]) + p["m0"]
+        for i in range(1, T):
+            x[i] = f(x[i - 1] * p["phi"]) + f(f(ex[i] * sq) * f(np.sqrt(f(t[i] - t[i - 1]))))
+        y = (f(p["sqrtR"]) * np.exp(f(0.5) * x).astype(np.float32) * ey).astype(np.float32)
+        dev = _dev.device()
+        return cdict(x=torch.from_numpy(x[:, None]).to(dev), y=torch.from_numpy(y[:, None]).to(dev),
+                     t=torch.as_tensor(t, device=dev), name=f"{self.name} simulation")
+
 
 class NonLinear1DBenchmark(StateSpaceModel):
     """x_0 ~ N(0, initial_sd^2), x_t ~ N(0.5 x + 25 x / (1 + x^2) + 8 cos(1.2 t_prev), transition_sd^2),
@@ -326,6 +347,12 @@ class OptimalNonLinearGaussianParticleFilter(ParticleFilter):
 
 
 def _check_lg(ssm_scenario, particle_filter):
+    if isinstance(ssm_scenario, StochasticVolatility):
+        if type(particle_filter) is not BootstrapFilter:
+            raise NotImplementedError(f"{particle_filter.__class__.__name__}: no fused GPU kernel for this model")
+        if ssm_scenario.dim != 1:
+            raise NotImplementedError("StochasticVolatility: the GPU kernels take dim = 1")
+        return
     if isinstance(ssm_scenario, NonLinear1DBenchmark):
         if type(particle_filter) is not BootstrapFilter:
             raise NotImplementedError(f"{particle_filter.__class__.__name__}: no fused GPU kernel for this model")
@@ -342,6 +369,9 @@ def _kernels(ssm_scenario, particle_filter):
     """(C-ABI prefix, model struct) of the fused kernels for this scenario / filter pair."""
     if isinstance(ssm_scenario, NonLinear1DBenchmark):
         return "mgb_pf_nl1d", ssm_scenario.derived()[1]
+    if isinstance(ssm_scenario, StochasticVolatility):
+        # bsig of the dt = 1 struct is transition_covariance_sqrt; the kernels scale it by sqrt(dt)
+        return "mgb_pf_sv", ssm_scenario.derived(1.0)[1]
     if isinstance(particle_filter, OptimalNonLinearGaussianParticleFilter):
         if getattr(particle_filter, "_struct", None) is None:
             particle_filter.startup(ssm_scenario)
@@ -394,11 +424,17 @@ def resample_particles(particles, random_key, resample_full=True, resampling="sy
     return out
 
 
-def _step(s, n, key, y_t, x_prev_soa, anc, lw_prev, prefix="mgb_pf_lg", t_prev=None):
+def _step(s, n, key, y_t, x_prev_soa, anc, lw_prev, prefix="mgb_pf_lg", t_prev=None, t_new=None):
     x_new = torch.empty_like(x_prev_soa)
     lw_new = torch.empty(n, dtype=torch.float32, device=x_prev_soa.device)
-    # the non-linear model's transition depends on t_previous
-    tp = (float(t_prev),) if prefix == "mgb_pf_nl1d" else ()
+    # the non-linear model's transition depends on t_previous, the stochastic-volatility
+    # model's on t_new - t_previous (float32, as the reference's time arrays)
+    if prefix == "mgb_pf_nl1d":
+        tp = (float(t_prev),)
+    elif prefix == "mgb_pf_sv":
+        tp = (float(np.float32(float(t_new)) - np.float32(float(t_prev))),)
+    else:
+        tp = ()
     call(prefix + "_propagate", ctypes.byref(s), n, _dev.ptr(key), _dev.ptr(y_t), *tp, _dev.ptr(x_prev_soa),
          _dev.ptr(anc), _dev.ptr(lw_prev), _dev.ptr(x_new), _dev.ptr(lw_new), _dev.stream_ptr())
     return x_new, lw_new
@@ -416,7 +452,7 @@ def propagate_particle_filter(ssm_scenario, particle_filter, particles, y_new, t
     x_prev = particles.value[-1].t().contiguous()
     lw_prev = particles.log_weight[-1].contiguous()
     y_t = _y2(y_new, ssm_scenario.dim_obs).reshape(-1)
-    x_new, lw_new = _step(s, n, key, y_t, x_prev, None, lw_prev, prefix, t_prev=particles.t[-1])
+    x_new, lw_new = _step(s, n, key, y_t, x_prev, None, lw_prev, prefix, t_prev=particles.t[-1], t_new=t_new)
     out = particles.copy()
     out.value = torch.cat([particles.value, x_new.t()[None]], 0)
     out.log_weight = torch.cat([particles.log_weight, lw_new[None]], 0)
@@ -448,12 +484,12 @@ def run_particle_filter_for_marginals(ssm_scenario, particle_filter, y, t, rando
     if initial_sample is not None:
         return _run_from(ssm_scenario, s, initial_sample, y2, t, key, ess_threshold, resampling, prefix)
     T = y2.shape[0]
-    nl = prefix == "mgb_pf_nl1d"
+    nl = prefix in ("mgb_pf_nl1d", "mgb_pf_sv")
     if nl:
         t32 = _dev.as_f32(t).reshape(-1).contiguous()
         if t32.numel() != T:
             raise ValueError(f"t has {t32.numel()} entries for {T} observations")
-        ws = _dev.workspace(_lib.lib().mgb_pf_nl1d_workspace(n, T, sc), dev)
+        ws = _dev.workspace(getattr(_lib.lib(), prefix + "_workspace")(n, T, sc), dev)
     else:
         ws = _dev.workspace(getattr(_lib.lib(), prefix + "_workspace")(n, T, d, sc), dev)
     logz = torch.empty(1, dtype=torch.float64, device=dev)
@@ -466,7 +502,7 @@ def run_particle_filter_for_marginals(ssm_scenario, particle_filter, y, t, rando
                          lh.data_ptr() if history else None, None if history else xh.data_ptr(),
                          None if history else lh.data_ptr(), err.data_ptr(), None)
     if nl:
-        call("mgb_pf_nl1d_run", ctypes.byref(s), n, T, _dev.ptr(key), _dev.ptr(y2), _dev.ptr(t32),
+        call(prefix + "_run", ctypes.byref(s), n, T, _dev.ptr(key), _dev.ptr(y2), _dev.ptr(t32),
              float(ess_threshold), sc | (0 if persistent else RUN_LAUNCH_PER_STEP), _dev.ptr(ws), ws.numel(),
              ctypes.byref(out), _dev.stream_ptr())
     else:
@@ -498,8 +534,9 @@ def _run_from(ssm_scenario, s, initial_sample, y2, t, key, ess_threshold, resamp
     for i in range(T):
         res = ess < ess_threshold * n
         anc = resample(lw, keys[i], resampling) if res else None
-        x, lw = _step(s, n, keys[i], y2[i], x, anc, None if res else lw, prefix, t_prev=t_prev)
-        t_prev = float(t_np[i]) if i < t_np.size else t_prev
+        t_new = float(t_np[i]) if i < t_np.size else t_prev
+        x, lw = _step(s, n, keys[i], y2[i], x, anc, None if res else lw, prefix, t_prev=t_prev, t_new=t_new)
+        t_prev = t_new
         lse = float(torch.logsumexp(lw.double(), 0))
         logz += lse - (math.log(n) if res else lse_prev)
         lse_prev = lse
@@ -778,7 +815,7 @@ def propagate_particle_smoother_pf(ssm_scenario, particle_filter, particles, y_n
         out = resample_particles(out, key, True, resampling)
     x_prev = out.value[-1].t().contiguous()
     y_t = _y2(y_new, ssm_scenario.dim_obs).reshape(-1)
-    x_new, lw = _step(s, n, key, y_t, x_prev, None, None, prefix, t_prev=out.t[-1])
+    x_new, lw = _step(s, n, key, y_t, x_prev, None, None, prefix, t_prev=out.t[-1], t_new=t_new)
     dev = x_new.device
     out.value = torch.cat([out.value, x_new.t()[None]], 0)
     out.y = torch.cat([out.y, y_t[None]], 0) if getattr(out, "y", None) is not None else y_t[None]

@@ -126,6 +126,9 @@ def lib():
         L.o_sv_run.argtypes = [ctypes.POINTER(_SVModel), i64, i64, u32p, f32p, ctypes.c_float, ctypes.c_int,
                                vp, vp]
         L.o_sv_run.restype = ctypes.c_double
+        L.o_sv_run_hist.argtypes = [ctypes.POINTER(_SVModel), i64, i64, u32p, f32p, vp, ctypes.c_float, ctypes.c_int,
+                                    f32p, i32p, vp, vp]
+        L.o_sv_run_hist.restype = ctypes.c_double
         L.o_sv_batch.argtypes = [ctypes.POINTER(_SVModel), i64, i64p, i64p, i64p, f32p, u32p, ctypes.c_float,
                                  ctypes.c_int, f64p]
         L.o_nl_drift.argtypes = [ctypes.c_float]
@@ -427,6 +430,22 @@ def sv_run(params, n, key, y, ess_threshold=0.5, scheme="multinomial"):
     logZ = lib().o_sv_run(ctypes.byref(s), n, T, _u32(key), y, float(ess_threshold), SCHEMES[scheme],
                           ess.ctypes.data, res.ctypes.data)
     return dict(log_z=logZ, ess=ess, resampled=res.astype(bool))
+
+
+def sv_run_hist(params, n, key, y, t=None, ess_threshold=0.5, scheme="systematic"):
+    """run_particle_filter_for_marginals on StochasticVolatility (dim 1) with the history; params
+    bsig is transition_covariance_sqrt and t (T,) the times (None: unit steps)."""
+    s = _sv_struct(params)
+    y = _f32(y).reshape(-1)
+    T = y.size
+    tt = None if t is None else _f32(t).reshape(-1)
+    ess = np.empty(T, np.float32)
+    res = np.empty(T, np.int32)
+    xh = np.empty((T, n), np.float32)
+    lh = np.empty((T, n), np.float32)
+    logZ = lib().o_sv_run_hist(ctypes.byref(s), n, T, _u32(key), y, _ptr(tt), float(ess_threshold),
+                               SCHEMES[scheme], ess, res, _ptr(xh), _ptr(lh))
+    return dict(log_z=logZ, ess=ess, resampled=res.astype(bool), value=xh, log_weight=lh)
 
 
 def sv_batch(params, n, T, y_off, y, keys, ess_threshold=0.5, scheme="multinomial"):

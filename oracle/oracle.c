@@ -585,9 +585,12 @@ static inline float o_sv_potential(const o_sv_model *md, float x, float y)
     return fmaf(a, o_expf(-x), fmaf(0.5f, x, md->cB));
 }
 
-/* One stochastic-volatility filter; scheme as in o_lg_run.  Returns logZ. */
-double o_sv_run(const o_sv_model *md, int64_t n, int64_t T, const uint32_t *key, const float *y,
-                float ess_threshold, int scheme, float *ess_out, int32_t *resampled_out)
+/* One stochastic-volatility filter; scheme as in o_lg_run.  t_all (nullable): the T
+ * times, step t then takes bsig_t = md->bsig sqrt(t_t - t_{t-1}) (md->bsig being the
+ * dt = 1 value), else md->bsig.  x_hist, lw_hist (nullable): (T, n).  Returns logZ. */
+static double o_sv_run_impl(const o_sv_model *md, int64_t n, int64_t T, const uint32_t *key, const float *y,
+                            const float *t_all, float ess_threshold, int scheme, float *ess_out,
+                            int32_t *resampled_out, float *x_hist, float *lw_hist)
 {
     float *xa = (float *)malloc(sizeof(float) * (size_t)n), *xb = (float *)malloc(sizeof(float) * (size_t)n);
     float *la = (float *)malloc(sizeof(float) * (size_t)n), *lb = (float *)malloc(sizeof(float) * (size_t)n);
@@ -603,6 +606,8 @@ double o_sv_run(const o_sv_model *md, int64_t n, int64_t T, const uint32_t *key,
         xa[i] = e * md->c0 + md->m0;
         la[i] = -o_sv_potential(md, xa[i], y[0]);
     }
+    if (x_hist) memcpy(x_hist, xa, sizeof(float) * (size_t)n);
+    if (lw_hist) memcpy(lw_hist, la, sizeof(float) * (size_t)n);
     double st[4];
     o_lse_ess(la, n, st);
     double logn = log((double)n);
@@ -620,12 +625,13 @@ double o_sv_run(const o_sv_model *md, int64_t n, int64_t T, const uint32_t *key,
             else if (scheme == 1) o_resample_multinomial(la, n, kt, anc);
             else o_resample_gumbel(la, n, n, kt, anc);
         }
+        const float bsig = t_all ? md->bsig * sqrtf(t_all[t] - t_all[t - 1]) : md->bsig;
         for (int64_t i = 0; i < n; ++i) {
             uint32_t a0, a1;
             o_split_at(kt[0], kt[1], (uint64_t)n, (uint64_t)i, &a0, &a1);
             float e = o_bits_to_normal(o_bits_at(a0, a1, 1, 0));
             float xs = xa[res ? anc[i] : i];
-            float xn = fmaf(xs, md->phi, e * md->bsig);
+            float xn = fmaf(xs, md->phi, e * bsig);
             xb[i] = xn;
             lb[i] = (res ? 0.0f : la[i]) - o_sv_potential(md, xn, y[t]);
         }
@@ -635,12 +641,28 @@ double o_sv_run(const o_sv_model *md, int64_t n, int64_t T, const uint32_t *key,
         ess_prev = (float)st[3];
         if (ess_out) ess_out[t] = ess_prev;
         if (resampled_out) resampled_out[t] = res;
+        if (x_hist) memcpy(x_hist + t * n, xb, sizeof(float) * (size_t)n);
+        if (lw_hist) memcpy(lw_hist + t * n, lb, sizeof(float) * (size_t)n);
         float *tp = xa; xa = xb; xb = tp;
         tp = la; la = lb; lb = tp;
     }
     free(tkeys);
     free(xa); free(xb); free(la); free(lb); free(anc);
     return logZ;
+}
+
+double o_sv_run(const o_sv_model *md, int64_t n, int64_t T, const uint32_t *key, const float *y,
+                float ess_threshold, int scheme, float *ess_out, int32_t *resampled_out)
+{
+    return o_sv_run_impl(md, n, T, key, y, NULL, ess_threshold, scheme, ess_out, resampled_out, NULL, NULL);
+}
+
+/* run_particle_filter_for_marginals on StochasticVolatility (dim 1) with the history */
+double o_sv_run_hist(const o_sv_model *md, int64_t n, int64_t T, const uint32_t *key, const float *y,
+                     const float *t_all, float ess_threshold, int scheme, float *ess_out, int32_t *resampled_out,
+                     float *x_hist, float *lw_hist)
+{
+    return o_sv_run_impl(md, n, T, key, y, t_all, ess_threshold, scheme, ess_out, resampled_out, x_hist, lw_hist);
 }
 
 /* Many independent SV filters (the batched workload), each with its own
