@@ -607,6 +607,32 @@ int mgb_abc_smc_init(const mgb_abc_smc_config *cfg, const mgb_abc_lg_model *mode
 int mgb_abc_smc_step(const mgb_abc_smc_config *cfg, const mgb_abc_lg_model *model_host, void *ws_dev,
                      size_t ws_bytes, void *stream);
 
+/* g-and-k scenarios (mocat/src/abc/scenarios/gk.py:81-175: GKTransformedUniformPrior, d = 4, and
+ * GKOnlyATransformedUniformPrior, d = 1) with the thinned-order-statistics summary of
+ * tests/test_abc_gk.py (sorted draws at ranks floor(j n_unsummarised / n_summary)) under the
+ * same sampler and config.  prior N(0, I); parameters constrained by prior_min + Phi(x)
+ * (prior_max - prior_min); a simulation draws n_unsummarised uniforms in [buffer, 1 - buffer],
+ * z = Phi^-1(u), v = A + B (1 + c (1 - e^{-g z}) / (1 + e^{-g z})) z (1 + z^2)^k (A-only: B = 1,
+ * g = 2 and the exponent c, as the reference writes it).  Phi uses the Numerical Recipes erfc
+ * fit and Phi^-1 the library's erfinv, so values are not XLA's bit for bit.
+ * mgb_abc_gk_simulate: summaries (P, n_summary) and/or distances (P) of parameter rows x (P, d)
+ * with keys (P, 2) (likelihood_sample then distance_function). */
+typedef struct {
+  int32_t d;               /* 4 or 1 */
+  int32_t n_unsummarised;  /* draws per simulation, <= 2048 */
+  int32_t n_summary;       /* thinned order statistics */
+  float c;                 /* 0.8 */
+  float prior_min, prior_max, buffer;  /* 0, 10, 1e-5 */
+  const float *data_dev;   /* (n_summary) observed summary */
+} mgb_abc_gk_model;
+size_t mgb_abc_gk_workspace(const mgb_abc_smc_config *cfg, int32_t d);
+int mgb_abc_gk_smc_init(const mgb_abc_smc_config *cfg, const mgb_abc_gk_model *model_host, const uint32_t *keys_dev,
+                        void *ws_dev, size_t ws_bytes, void *stream);
+int mgb_abc_gk_smc_step(const mgb_abc_smc_config *cfg, const mgb_abc_gk_model *model_host, void *ws_dev,
+                        size_t ws_bytes, void *stream);
+int mgb_abc_gk_simulate(const mgb_abc_gk_model *model_host, int64_t P, const float *x_dev, const uint32_t *keys_dev,
+                        float *summary_dev, float *dist_dev, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -47,6 +47,12 @@ class ABCModel(ctypes.Structure):
                 ("data", ctypes.c_void_p)]
 
 
+class GKModel(ctypes.Structure):
+    _fields_ = [("d", ctypes.c_int32), ("n_unsummarised", ctypes.c_int32), ("n_summary", ctypes.c_int32),
+                ("c", ctypes.c_float), ("prior_min", ctypes.c_float), ("prior_max", ctypes.c_float),
+                ("buffer", ctypes.c_float), ("data_dev", ctypes.c_void_p)]
+
+
 class ABCConfig(ctypes.Structure):
     _fields_ = [("B", ctypes.c_int32), ("N", ctypes.c_int32), ("mcmc_steps", ctypes.c_int32),
                 ("max_iter", ctypes.c_int32), ("ess_threshold_retain", ctypes.c_float),
@@ -169,6 +175,10 @@ _SIGNATURES = {
     "mgb_stitch_rejection_nl1d": ([ctypes.POINTER(NL1DModel), ctypes.POINTER(RejectionConfig), _I64, _P, _P, _P, _F,
                                    _P, _P, _P, _P, _SZ, _P], _I32),
     "mgb_transition_potential_pairs_nl1d": ([ctypes.POINTER(NL1DModel), _I64, _P, _P, _F, _P, _P, _P], _I32),
+    "mgb_abc_gk_workspace": ([ctypes.POINTER(ABCConfig), ctypes.c_int32], _SZ),
+    "mgb_abc_gk_smc_init": ([ctypes.POINTER(ABCConfig), ctypes.POINTER(GKModel), _P, _P, _SZ, _P], _I32),
+    "mgb_abc_gk_smc_step": ([ctypes.POINTER(ABCConfig), ctypes.POINTER(GKModel), _P, _SZ, _P], _I32),
+    "mgb_abc_gk_simulate": ([ctypes.POINTER(GKModel), _I64, _P, _P, _P, _P, _P], _I32),
     "mgb_abc_smc_workspace": ([ctypes.POINTER(ABCConfig), ctypes.c_int32], _SZ),
     "mgb_abc_smc_views": ([ctypes.POINTER(ABCConfig), ctypes.c_int32, _P, ctypes.POINTER(ABCViews)], _I32),
     "mgb_abc_smc_init": ([ctypes.POINTER(ABCConfig), ctypes.POINTER(ABCModel), _P, _P, _SZ, _P], _I32),

@@ -1,5 +1,5 @@
 """Likelihood-free SMC (ABC-SMC) on the GPU with mocat's names
-(mocat/src/abc/abc.py, abc/mcmc.py, abc/smc.py, abc/scenarios/linear_gaussian.py).
+(mocat/src/abc/abc.py, abc/mcmc.py, abc/smc.py, abc/scenarios/linear_gaussian.py, abc/scenarios/gk.py).
 
     scenario = LinearGaussian(prior_mean, prior_covariance, data, likelihood_matrix, likelihood_covariance)
     sampler = MetropolisedABCSMCSampler(ess_threshold_retain=0.8)           # RandomWalkABC moves
@@ -94,6 +94,69 @@ class LinearGaussian(ABCScenario):
         return self.prior_mean + np.linalg.cholesky(self.prior_covariance) @ e
 
 
+class GKTransformedUniformPrior(ABCScenario):
+    """g-and-k distribution with a N(0, I) prior on unconstrained parameters
+    (abc/scenarios/gk.py:81-116, constrain lo + Phi(x) (hi - lo)), summarised by thinned
+    order statistics as the reference's GK tests do (tests/test_abc_gk.py GKThinOrder):
+    the sorted n_unsummarised_data draws at ranks floor(j n / num_thin).  Simulations run
+    on the GPU, one CTA per parameter row (mgb_abc_gk_simulate)."""
+    name = "GK_fewN"
+    dim = 4
+    c = 0.8
+    prior_mins = 0.0
+    prior_maxs = 10.0
+    buffer = 1e-5
+
+    def __init__(self, n_unsummarised_data=1000, num_thin=100, data=None, name=None):
+        super().__init__(name=name)
+        self.n_unsummarised_data = int(n_unsummarised_data)
+        self.num_thin = int(num_thin)
+        self.data = None if data is None else _arr(data).reshape(-1)
+
+    def constrain(self, unconstrained_x):
+        x = torch.as_tensor(np.asarray(unconstrained_x, np.float64))
+        return (self.prior_mins + torch.special.ndtr(x) * (self.prior_maxs - self.prior_mins)).numpy()
+
+    def unconstrain(self, constrained_x):
+        x = torch.as_tensor(np.asarray(constrained_x, np.float64))
+        return torch.special.ndtri((x - self.prior_mins) / (self.prior_maxs - self.prior_mins)).numpy()
+
+    def model(self, data_dev=None):
+        return _lib.GKModel(self.dim, self.n_unsummarised_data, self.num_thin, self.c, self.prior_mins,
+                            self.prior_maxs, self.buffer, data_dev)
+
+    def prior_potential(self, x, random_key=None):
+        x = _arr(x)
+        return 0.5 * (x ** 2).sum(-1)
+
+    def prior_sample(self, random_key):
+        from . import random as mrandom
+        return mrandom.normal(random_key, (self.dim,)).cpu().numpy().astype(np.float64)
+
+    def simulate_summaries(self, x, random_keys):
+        """likelihood_sample for parameter rows x (P, d) with keys (P, 2): (P, num_thin) on the GPU"""
+        xs = _dev.as_f32(x).reshape(-1, self.dim).contiguous()
+        keys = _dev.as_key(random_keys).reshape(-1, 2).contiguous()
+        out = torch.empty((xs.shape[0], self.num_thin), dtype=torch.float32, device=xs.device)
+        call("mgb_abc_gk_simulate", ctypes.byref(self.model()), xs.shape[0], _dev.ptr(xs), _dev.ptr(keys),
+             _dev.ptr(out), None, _dev.stream_ptr())
+        return out
+
+    def likelihood_sample(self, x, random_key):
+        return self.simulate_summaries(_arr(x).reshape(1, -1), _dev.as_key(random_key).reshape(1, 2))[0]
+
+
+class GKOnlyATransformedUniformPrior(GKTransformedUniformPrior):
+    """the A-only g-and-k scenario (abc/scenarios/gk.py:138-175): B = 1, g = 2, and the exponent
+    of (1 + z^2) is c, as the reference writes it"""
+    name = "GK_fewN only A"
+    dim = 1
+
+
+GKThinOrder = GKTransformedUniformPrior
+GKOnlyAThinOrder = GKOnlyATransformedUniformPrior
+
+
 class RandomWalkABC:
     """Random-walk ABC MCMC kernel (abc/mcmc.py:59-103): x + sqrt(stepsize) eps, accepted with
     probability min(1, exp(prior_potential_old - prior_potential_new) [distance_new < threshold])."""
@@ -134,17 +197,24 @@ class BatchedABCSMC:
     ``step()`` until ``done()``, or ``run()``."""
 
     def __init__(self, scenario, sampler, n, random_keys):
-        if not isinstance(scenario, LinearGaussian):
+        self.gk = isinstance(scenario, GKTransformedUniformPrior)
+        if not self.gk and not isinstance(scenario, LinearGaussian):
             raise NotImplementedError(f"{scenario.__class__.__name__}: no GPU ABC kernel for this scenario")
-        if (scenario.dim, scenario.dim_obs) not in SUPPORTED:
+        if not self.gk and (scenario.dim, scenario.dim_obs) not in SUPPORTED:
             raise NotImplementedError(f"(d, dy) = ({scenario.dim}, {scenario.dim_obs}) not compiled")
+        if self.gk and (scenario.data is None or np.size(scenario.data) != scenario.num_thin):
+            raise ValueError("the g-and-k scenario needs data: num_thin summary values")
         if not 2 <= n <= MAX_N:
             raise NotImplementedError(f"n must be in [2, {MAX_N}]")
         keys = _dev.as_key(random_keys).reshape(-1, 2).contiguous()
         self.scenario, self.sampler = scenario, sampler
         self.keys = keys
         self.B, self.n = keys.shape[0], int(n)
-        self._keep, self.model = scenario.derived()
+        if self.gk:
+            self._data = torch.as_tensor(np.asarray(scenario.data, np.float32), device=keys.device).contiguous()
+            self.model = scenario.model(_dev.ptr(self._data))
+        else:
+            self._keep, self.model = scenario.derived()
         sch = sampler.threshold_schedule
         self._sch = None if sch is None else np.ascontiguousarray(sch, np.float32)
         fixed = sampler.mcmc_sampler is not None
@@ -155,7 +225,9 @@ class BatchedABCSMC:
                                   0 if self._sch is None else self._sch.size,
                                   None if self._sch is None else self._sch.ctypes.data)
         d = scenario.dim
-        self.ws = _dev.workspace(_lib.lib().mgb_abc_smc_workspace(ctypes.byref(self.cfg), d))
+        wsf = _lib.lib().mgb_abc_gk_workspace if self.gk else _lib.lib().mgb_abc_smc_workspace
+        self.ws = _dev.workspace(wsf(ctypes.byref(self.cfg), d))
+        self._pref = "mgb_abc_gk_smc" if self.gk else "mgb_abc_smc"
         self.views = _lib.ABCViews()
         call("mgb_abc_smc_views", ctypes.byref(self.cfg), d, _dev.ptr(self.ws), ctypes.byref(self.views))
         self.iterations = 0
@@ -167,12 +239,12 @@ class BatchedABCSMC:
         return self.ws.view(torch.uint8)[off:off + nbytes].view(dtype).reshape(shape)
 
     def init(self):
-        call("mgb_abc_smc_init", ctypes.byref(self.cfg), ctypes.byref(self.model), _dev.ptr(self.keys),
+        call(self._pref + "_init", ctypes.byref(self.cfg), ctypes.byref(self.model), _dev.ptr(self.keys),
              _dev.ptr(self.ws), self.ws.numel(), _dev.stream_ptr())
         self.iterations = 0
 
     def step(self):
-        call("mgb_abc_smc_step", ctypes.byref(self.cfg), ctypes.byref(self.model), _dev.ptr(self.ws),
+        call(self._pref + "_step", ctypes.byref(self.cfg), ctypes.byref(self.model), _dev.ptr(self.ws),
              self.ws.numel(), _dev.stream_ptr())
         self.iterations += 1
 

@@ -543,6 +543,346 @@ static int abc_step(const mgb_abc_smc_config *cfg, const mgb_abc_lg_model *m, vo
   return launch_status();
 }
 
+// ------------------------------------------------------------- g-and-k
+// GKTransformedUniformPrior / GKOnlyATransformedUniformPrior (abc/scenarios/gk.py:81-175)
+// with the thinned-order-statistics summary of the reference's GK tests
+// (tests/test_abc_gk.py GKThinOrder):
+//   prior_sample     normal(key, (d,)); prior_potential 0.5 sum x^2
+//   constrain        lo + Phi(x) (hi - lo)
+//   simulation       u = max(buffer, f (1 - 2 buffer) + buffer) from uniform bits f,
+//                    z = Phi^-1(u), e = exp(-g z),
+//                    v = A + ((B (1 + c (1 - e) / (1 + e))) z) (1 + z^2)^k
+//                    (the A-only scenario: B = 1, g = 2 and the exponent c, as the reference writes it)
+//   summary          sorted v at ranks floor(j n_raw / n_sum), j < n_sum; distance |summary - data|_2.
+// Phi(x) = 0.5 erfc(-x / sqrt 2) with the erfc of Numerical Recipes (erfcc, a Chebyshev
+// fit with fractional error below 1.2e-7); Phi^-1(u) = sqrt 2 erfinv(2u - 1) with the
+// library's own erfinv; (1 + z^2)^k = exp(k log(1 + z^2)) with its own exp and log.
+constexpr int GK_TPB = 256;
+constexpr int GK_MAX_RAW = 2048;
+
+struct GKP {
+  int32_t d, n_raw, n_sum, p2;  // p2: sort length, the power of two >= n_raw
+  float c, lo, hi, buffer;
+  const float *data;
+  uint32_t one;
+};
+
+__device__ __forceinline__ float gk_erfcc(float x) {
+  const float z = fabsf(x);
+  const float t = __fdiv_rn(1.0f, __fmaf_rn(0.5f, z, 1.0f));
+  float q = 0.17087277f;
+  q = __fmaf_rn(t, q, -0.82215223f);
+  q = __fmaf_rn(t, q, 1.48851587f);
+  q = __fmaf_rn(t, q, -1.13520398f);
+  q = __fmaf_rn(t, q, 0.27886807f);
+  q = __fmaf_rn(t, q, -0.18628806f);
+  q = __fmaf_rn(t, q, 0.09678418f);
+  q = __fmaf_rn(t, q, 0.37409196f);
+  q = __fmaf_rn(t, q, 1.00002368f);
+  const float arg = __fmaf_rn(t, q, __fsub_rn(-__fmul_rn(z, z), 1.26551223f));
+  const float ans = __fmul_rn(t, expf_(arg));
+  return x >= 0.0f ? ans : __fsub_rn(2.0f, ans);
+}
+
+__device__ __forceinline__ float gk_ncdf(float x) {
+  return __fmul_rn(0.5f, gk_erfcc(__fmul_rn(-x, 0.70710677f)));
+}
+
+__device__ __forceinline__ float gk_ppf(float u) {
+  return __fmul_rn(1.41421354f, erfinv_(__fsub_rn(__fmul_rn(2.0f, u), 1.0f)));
+}
+
+// (A, B, g, exponent) of a parameter row
+__device__ __forceinline__ void gk_params(const GKP &p, const float *x, float (&q)[4]) {
+  const float span = __fsub_rn(p.hi, p.lo);
+  if (p.d == 4) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) q[j] = __fadd_rn(p.lo, __fmul_rn(gk_ncdf(x[j]), span));
+  } else {
+    q[0] = __fadd_rn(p.lo, __fmul_rn(gk_ncdf(x[0]), span));
+    q[1] = 1.0f;
+    q[2] = 2.0f;
+    q[3] = p.c;
+  }
+}
+
+__device__ __forceinline__ float gk_value(const GKP &p, const float (&q)[4], uint32_t bits) {
+  const float range = __fsub_rn(__fsub_rn(1.0f, p.buffer), p.buffer);
+  const float u = fmaxf(p.buffer, __fadd_rn(__fmul_rn(bits_to_unit(bits), range), p.buffer));
+  const float z = gk_ppf(u);
+  const float e = expf_(-__fmul_rn(q[2], z));
+  const float term = __fadd_rn(1.0f, __fdiv_rn(__fmul_rn(p.c, __fsub_rn(1.0f, e)), __fadd_rn(1.0f, e)));
+  const float pw = expf_(__fmul_rn(q[3], logf_(__fadd_rn(1.0f, __fmul_rn(z, z)))));
+  return __fadd_rn(q[0], __fmul_rn(__fmul_rn(__fmul_rn(q[1], term), z), pw));
+}
+
+// ascending sort keys of floats (NaN of either sign after +inf, as jnp.sort)
+__device__ __forceinline__ uint32_t gk_key(float v) {
+  if (v != v) return 0xFFFFFFFEu;
+  const uint32_t b = __float_as_uint(v);
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float gk_unkey(uint32_t k) {
+  if (k == 0xFFFFFFFEu) return __uint_as_float(0x7fc00000u);
+  return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+// one CTA per parameter row: n_raw draws, sort, thinned order statistics, distance
+__global__ void __launch_bounds__(GK_TPB) k_gk_sim(const GKP p, int64_t P, const float *__restrict__ x,
+                                                    const uint32_t *__restrict__ keys, const int32_t *mask,
+                                                    float *__restrict__ dist, float *__restrict__ summary) {
+  __shared__ uint32_t sk[GK_MAX_RAW];
+  __shared__ float q[4];
+  const int64_t r = blockIdx.x;
+  if (r >= P || (mask && !mask[r])) return;
+  if (threadIdx.x == 0) {
+    float qq[4];
+    gk_params(p, x + r * p.d, qq);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) q[j] = qq[j];
+  }
+  __syncthreads();
+  const float qv[4] = {q[0], q[1], q[2], q[3]};
+  const uint32_t k0 = keys[2 * r], k1 = keys[2 * r + 1];
+  for (int i = threadIdx.x; i < p.p2; i += GK_TPB)
+    sk[i] = i < p.n_raw ? gk_key(gk_value(p, qv, bits_at(k0, k1, (uint64_t)p.n_raw, (uint64_t)i))) : 0xFFFFFFFFu;
+  __syncthreads();
+  for (int kk = 2; kk <= p.p2; kk <<= 1) {
+    for (int j = kk >> 1; j > 0; j >>= 1) {
+      for (int i = threadIdx.x; i < p.p2; i += GK_TPB) {
+        const int ixj = i ^ j;
+        if (ixj > i) {
+          const uint32_t a = sk[i], b = sk[ixj];
+          if ((a > b) == ((i & kk) == 0)) {
+            sk[i] = b;
+            sk[ixj] = a;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  if (summary)
+    for (int j = threadIdx.x; j < p.n_sum; j += GK_TPB)
+      summary[r * p.n_sum + j] = gk_unkey(sk[(int)(((int64_t)j * p.n_raw) / p.n_sum)]);
+  if (dist && threadIdx.x == 0) {
+    float acc = 0.0f;
+    for (int j = 0; j < p.n_sum; ++j) {
+      const float dv = __fsub_rn(gk_unkey(sk[(int)(((int64_t)j * p.n_raw) / p.n_sum)]), p.data[j]);
+      acc = j == 0 ? __fmul_rn(dv, dv) : __fadd_rn(acc, __fmul_rn(dv, dv));
+    }
+    dist[r] = __fsqrt_rn(acc);
+  }
+}
+
+template <int D>
+__device__ __forceinline__ float gk_prior_pot(const float (&x)[D]) {
+  float s = __fmul_rn(x[0], x[0]);
+#pragma unroll
+  for (int j = 1; j < D; ++j) s = __fadd_rn(s, __fmul_rn(x[j], x[j]));
+  return __fmul_rn(0.5f, s);
+}
+
+// per-particle state of the split moves (the simulation is a CTA per particle)
+struct GKWs {
+  float *xp;        // (B N, d) proposals
+  float *ppn, *dn;  // (B N) proposal prior potential, distance
+  float *asum;      // (B N) acceptance sums
+  uint32_t *skey;   // (B N, 2) simulation keys
+  uint32_t *mkey;   // (B N, 2) move keys
+  int32_t *mask;    // (B N) rows to simulate
+};
+
+inline GKWs carve_gk(Carver &c, int64_t B, int64_t N, int d) {
+  GKWs g;
+  const size_t BN = (size_t)(B * N);
+  g.xp = c.take<float>(BN * d);
+  g.ppn = c.take<float>(BN);
+  g.dn = c.take<float>(BN);
+  g.asum = c.take<float>(BN);
+  g.skey = c.take<uint32_t>(2 * BN);
+  g.mkey = c.take<uint32_t>(2 * BN);
+  g.mask = c.take<int32_t>(BN);
+  return g;
+}
+
+// startup: prior draw, prior potential, the simulation key (the simulation itself is k_gk_sim)
+template <int D>
+__global__ void __launch_bounds__(ABC_MOVE_TPB) k_gk_init(int64_t B, int64_t N, const uint32_t *keys, ABCWs w,
+                                                           GKWs g, uint32_t one) {
+  const int64_t i0 = blockIdx.x * (int64_t)ABC_MOVE_TPB + threadIdx.x;
+  if (i0 >= B * N) return;
+  const int64_t b = i0 / N, i = i0 - b * N;
+  uint32_t e0, e1, s0, s1, a0, a1;
+  split_at(keys[2 * b], keys[2 * b + 1], 2, 0, e0, e1);
+  split_at(keys[2 * b], keys[2 * b + 1], 2, 1, s0, s1);
+  split_at(s0, s1, (uint64_t)N, (uint64_t)i, a0, a1);
+  uint32_t bits[D];
+  bits_vec<D>(a0, a1, bits, one);
+  float x[D];
+#pragma unroll
+  for (int j = 0; j < D; ++j) {
+    x[j] = bits_to_normal(bits[j]);
+    w.value[i0 * D + j] = x[j];
+  }
+  w.pp[i0] = gk_prior_pot<D>(x);
+  uint32_t f0, f1, k0, k1;
+  split_at(e0, e1, (uint64_t)N + 1, (uint64_t)N, f0, f1);
+  split_at(f0, f1, (uint64_t)N + 1, (uint64_t)i, k0, k1);
+  g.skey[2 * i0] = k0;
+  g.skey[2 * i0 + 1] = k1;
+  g.mask[i0] = 1;
+  w.alpha[i0] = 1.0f;
+  w.lw[i0] = 0.0f;
+  if (i == 0) {
+    uint32_t z0, z1;
+    split_at(f0, f1, (uint64_t)N + 1, (uint64_t)N, z0, z1);
+    w.key[2 * b] = z0;
+    w.key[2 * b + 1] = z1;
+  }
+}
+
+// first move of an iteration: the particle's key split(e, N + 2)[i]; every move:
+// key <- split(key)[0]; (key, k1, k2, k3) = split(key, 4); proposal x + sqrt(s) normal(k1, (d,))
+template <int D>
+__global__ void __launch_bounds__(ABC_MOVE_TPB) k_gk_prop(ABCCtl ctl, int64_t B, ABCWs w, GKWs g, int first,
+                                                           uint32_t one) {
+  const int64_t N = ctl.N;
+  const int64_t i0 = blockIdx.x * (int64_t)ABC_MOVE_TPB + threadIdx.x;
+  if (i0 >= B * N) return;
+  const int64_t b = i0 / N, i = i0 - b * N;
+  const bool live = w.active[b] && (w.lw[i0] > -INFINITY);
+  g.mask[i0] = live;
+  if (!live) return;
+  uint32_t k0, k1;
+  if (first) {
+    split_at(w.key[2 * b], w.key[2 * b + 1], (uint64_t)N + 2, (uint64_t)i, k0, k1);
+  } else {
+    k0 = g.mkey[2 * i0];
+    k1 = g.mkey[2 * i0 + 1];
+  }
+  uint32_t t0, t1, n0, n1, a0, a1, c0, c1;
+  split_at(k0, k1, 2, 0, t0, t1);
+  split_at(t0, t1, 4, 0, n0, n1);
+  split_at(t0, t1, 4, 1, a0, a1);
+  split_at(t0, t1, 4, 3, c0, c1);
+  uint32_t bits[D];
+  bits_vec<D>(a0, a1, bits, one);
+  float xp[D];
+#pragma unroll
+  for (int j = 0; j < D; ++j) {
+    xp[j] = __fadd_rn(w.value[i0 * D + j], __fmul_rn(__fsqrt_rn(w.stepsize[b * D + j]), bits_to_normal(bits[j])));
+    g.xp[i0 * D + j] = xp[j];
+  }
+  g.ppn[i0] = gk_prior_pot<D>(xp);
+  g.skey[2 * i0] = c0;
+  g.skey[2 * i0 + 1] = c1;
+  g.mkey[2 * i0] = n0;
+  g.mkey[2 * i0 + 1] = n1;
+}
+
+// Metropolis correction of the move: alpha = min(1, exp(pp - ppn) [dn < threshold]) (NaN -> 0);
+// (key, ku) = split(key); accept if uniform(ku) < alpha
+template <int D>
+__global__ void __launch_bounds__(ABC_MOVE_TPB) k_gk_accept(ABCCtl ctl, int64_t B, ABCWs w, GKWs g, int step) {
+  const int64_t N = ctl.N;
+  const int64_t i0 = blockIdx.x * (int64_t)ABC_MOVE_TPB + threadIdx.x;
+  if (i0 >= B * N || !g.mask[i0]) return;
+  const int64_t b = i0 / N;
+  const float thr = w.threshold[b];
+  const float pp = w.pp[i0], ppn = g.ppn[i0], dn = g.dn[i0];
+  float a = __fmul_rn(expf_(__fsub_rn(pp, ppn)), dn < thr ? 1.0f : 0.0f);
+  a = a != a ? 0.0f : fminf(1.0f, a);
+  const uint32_t n0 = g.mkey[2 * i0], n1 = g.mkey[2 * i0 + 1];
+  uint32_t u0, u1, v0, v1;
+  split_at(n0, n1, 2, 0, u0, u1);
+  split_at(n0, n1, 2, 1, v0, v1);
+  const float u = bits_to_unit(bits_at(v0, v1, 1, 0));
+  if (u < a) {
+#pragma unroll
+    for (int j = 0; j < D; ++j) w.value[i0 * D + j] = g.xp[i0 * D + j];
+    w.pp[i0] = ppn;
+    w.dist[i0] = dn;
+  }
+  const float as = step == 0 ? a : __fadd_rn(g.asum[i0], a);
+  g.asum[i0] = as;
+  g.mkey[2 * i0] = u0;
+  g.mkey[2 * i0 + 1] = u1;
+  if (step == ctl.mcmc_steps - 1) w.alpha[i0] = __fdiv_rn(as, (float)ctl.mcmc_steps);
+}
+
+static GKP pack_gk(const mgb_abc_gk_model *m) {
+  GKP p;
+  p.d = m->d;
+  p.n_raw = m->n_unsummarised;
+  p.n_sum = m->n_summary;
+  int p2 = 1;
+  while (p2 < m->n_unsummarised) p2 <<= 1;
+  p.p2 = p2;
+  p.c = m->c;
+  p.lo = m->prior_min;
+  p.hi = m->prior_max;
+  p.buffer = m->buffer;
+  p.data = m->data_dev;
+  p.one = 1u;
+  return p;
+}
+
+static bool gk_ok(const mgb_abc_gk_model *m) {
+  return m && (m->d == 4 || m->d == 1) && m->n_unsummarised >= 1 && m->n_unsummarised <= GK_MAX_RAW &&
+         m->n_summary >= 1 && m->n_summary <= m->n_unsummarised;
+}
+
+static GKWs gk_ws(const mgb_abc_smc_config *cfg, int d, void *ws) {
+  Carver c(ws);
+  carve_abc(c, cfg->B, cfg->N, d, abc_hist_len(cfg), cfg->n_schedule);
+  return carve_gk(c, cfg->B, cfg->N, d);
+}
+
+template <int D>
+static int gk_init(const mgb_abc_smc_config *cfg, const mgb_abc_gk_model *m, const uint32_t *keys, void *ws,
+                   cudaStream_t s) {
+  const ABCWs w = abc_ws(cfg, D, ws);
+  const GKWs g = gk_ws(cfg, D, ws);
+  const ABCCtl ctl = abc_ctl(cfg);
+  if (cfg->n_schedule > 0 &&
+      cudaMemcpyAsync(w.schedule, cfg->schedule, sizeof(float) * cfg->n_schedule, cudaMemcpyHostToDevice, s) !=
+          cudaSuccess)
+    return ERR_CUDA;
+  const int64_t BN = (int64_t)cfg->B * cfg->N;
+  const unsigned grid = (unsigned)((BN + ABC_MOVE_TPB - 1) / ABC_MOVE_TPB);
+  k_gk_init<D><<<grid, ABC_MOVE_TPB, 0, s>>>(cfg->B, cfg->N, keys, w, g, 1u);
+  int st = launch_status();
+  if (st) return st;
+  k_gk_sim<<<(unsigned)BN, GK_TPB, 0, s>>>(pack_gk(m), BN, w.value, g.skey, nullptr, w.dist, nullptr);
+  if ((st = launch_status())) return st;
+  k_abc_adapt<D><<<(unsigned)cfg->B, ABC_TPB, 0, s>>>(ctl, w, 1);
+  return launch_status();
+}
+
+template <int D>
+static int gk_step(const mgb_abc_smc_config *cfg, const mgb_abc_gk_model *m, void *ws, cudaStream_t s) {
+  const ABCWs w = abc_ws(cfg, D, ws);
+  const GKWs g = gk_ws(cfg, D, ws);
+  const ABCCtl ctl = abc_ctl(cfg);
+  k_abc_resample<D><<<(unsigned)cfg->B, ABC_TPB, 0, s>>>(ctl, w);
+  int st = launch_status();
+  if (st) return st;
+  const int64_t BN = (int64_t)cfg->B * cfg->N;
+  const unsigned grid = (unsigned)((BN + ABC_MOVE_TPB - 1) / ABC_MOVE_TPB);
+  const GKP p = pack_gk(m);
+  for (int k = 0; k < cfg->mcmc_steps; ++k) {
+    k_gk_prop<D><<<grid, ABC_MOVE_TPB, 0, s>>>(ctl, cfg->B, w, g, k == 0, 1u);
+    if ((st = launch_status())) return st;
+    k_gk_sim<<<(unsigned)BN, GK_TPB, 0, s>>>(p, BN, g.xp, g.skey, g.mask, g.dn, nullptr);
+    if ((st = launch_status())) return st;
+    k_gk_accept<D><<<grid, ABC_MOVE_TPB, 0, s>>>(ctl, cfg->B, w, g, k);
+    if ((st = launch_status())) return st;
+  }
+  k_abc_adapt<D><<<(unsigned)cfg->B, ABC_TPB, 0, s>>>(ctl, w, 0);
+  return launch_status();
+}
+
 #define MGB_ABC_DISPATCH(FN, ...)                                     \
   do {                                                                \
     const int d_ = m->d, dy_ = m->dy;                                 \
@@ -609,6 +949,44 @@ int mgb_abc_smc_step(const mgb_abc_smc_config *cfg, const mgb_abc_lg_model *m, v
   if (!abc_ok(cfg, m) || !ws) return ERR_BAD_ARG;
   if (ws_bytes < mgb_abc_smc_workspace(cfg, m->d)) return ERR_WORKSPACE;
   MGB_ABC_DISPATCH(abc_step, cfg, m, ws, (cudaStream_t)stream);
+}
+
+size_t mgb_abc_gk_workspace(const mgb_abc_smc_config *cfg, int32_t d) {
+  if (!cfg || (d != 1 && d != 4)) return 0;
+  Carver c(nullptr);
+  carve_abc(c, cfg->B, cfg->N, d, abc_hist_len(cfg), cfg->n_schedule);
+  carve_gk(c, cfg->B, cfg->N, d);
+  return c.bytes();
+}
+
+static bool abc_cfg_ok(const mgb_abc_smc_config *cfg) {
+  return cfg && cfg->B >= 1 && cfg->N >= 2 && cfg->N <= MGB_ABC_MAX_N && cfg->mcmc_steps >= 1 &&
+         cfg->max_iter >= 0 && cfg->max_iter <= 100000 && cfg->n_schedule >= 0 &&
+         (cfg->n_schedule == 0 || cfg->schedule);
+}
+
+int mgb_abc_gk_smc_init(const mgb_abc_smc_config *cfg, const mgb_abc_gk_model *m, const uint32_t *keys, void *ws,
+                        size_t ws_bytes, void *stream) {
+  if (!abc_cfg_ok(cfg) || !gk_ok(m) || !m->data_dev || !keys || !ws) return ERR_BAD_ARG;
+  if (ws_bytes < mgb_abc_gk_workspace(cfg, m->d)) return ERR_WORKSPACE;
+  if (m->d == 4) return gk_init<4>(cfg, m, keys, ws, (cudaStream_t)stream);
+  return gk_init<1>(cfg, m, keys, ws, (cudaStream_t)stream);
+}
+
+int mgb_abc_gk_smc_step(const mgb_abc_smc_config *cfg, const mgb_abc_gk_model *m, void *ws, size_t ws_bytes,
+                        void *stream) {
+  if (!abc_cfg_ok(cfg) || !gk_ok(m) || !m->data_dev || !ws) return ERR_BAD_ARG;
+  if (ws_bytes < mgb_abc_gk_workspace(cfg, m->d)) return ERR_WORKSPACE;
+  if (m->d == 4) return gk_step<4>(cfg, m, ws, (cudaStream_t)stream);
+  return gk_step<1>(cfg, m, ws, (cudaStream_t)stream);
+}
+
+int mgb_abc_gk_simulate(const mgb_abc_gk_model *m, int64_t P, const float *x, const uint32_t *keys, float *summary,
+                        float *dist, void *stream) {
+  if (!gk_ok(m) || P < 1 || P > 0x7FFFFFFFll || !x || !keys || (!summary && !dist) || (dist && !m->data_dev))
+    return ERR_BAD_ARG;
+  k_gk_sim<<<(unsigned)P, GK_TPB, 0, (cudaStream_t)stream>>>(pack_gk(m), P, x, keys, nullptr, dist, summary);
+  return launch_status();
 }
 
 }  // extern "C"

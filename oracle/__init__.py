@@ -78,6 +78,11 @@ class _ABCConfig(ctypes.Structure):
                 ("schedule", vp)]
 
 
+class _GKModel(ctypes.Structure):
+    _fields_ = [("d", ctypes.c_int), ("n_raw", ctypes.c_int), ("n_sum", ctypes.c_int), ("c", ctypes.c_float),
+                ("lo", ctypes.c_float), ("hi", ctypes.c_float), ("buffer", ctypes.c_float), ("data", ctypes.c_void_p)]
+
+
 class _FFBSiModel(ctypes.Structure):
     _fields_ = [("d", ctypes.c_int), ("F", ctypes.c_void_p), ("Pq", ctypes.c_void_p), ("cq", ctypes.c_float),
                 ("nl", ctypes.c_int), ("tsd", ctypes.c_float), ("c", ctypes.c_float)]
@@ -142,6 +147,10 @@ def lib():
         L.o_abc_lg_run.argtypes = [ctypes.POINTER(_ABCModel), ctypes.POINTER(_ABCConfig), u32p, f32p, f32p, f32p,
                                    f32p, f32p, f32p, f32p, i32p]
         L.o_abc_lg_run.restype = ctypes.c_int
+        L.o_abc_gk_run.argtypes = [ctypes.POINTER(_GKModel), ctypes.POINTER(_ABCConfig), u32p, f32p, f32p, f32p,
+                                   f32p, f32p, f32p, f32p, i32p]
+        L.o_abc_gk_run.restype = ctypes.c_int
+        L.o_gk_simulate.argtypes = [ctypes.POINTER(_GKModel), i64, f32p, u32p, vp, vp]
         L.o_ffbsi_nl1d.argtypes = [ctypes.POINTER(_NLModel), i64, i64, i64, f32p, f32p, f32p, u32p, f32p, i32p]
         L.o_stitch_nl1d.argtypes = [ctypes.POINTER(_NLModel), i64, i64, f32p, f32p, f32p, ctypes.c_float, u32p, i32p]
         L.o_transition_potential_pairs_nl1d.argtypes = [ctypes.POINTER(_NLModel), i64, f32p, f32p, ctypes.c_float,
@@ -559,6 +568,47 @@ def abc_lg_run(params, N, key, mcmc_steps=1, max_iter=10000, retain=0.9, resampl
     hr = np.zeros(H, np.int32)
     it = lib().o_abc_lg_run(ctypes.byref(md), ctypes.byref(cf), _u32(key), x.reshape(-1), lw, dist, st, ht, he, ha,
                             hr)
+    L = it + 1
+    return dict(value=x, log_weight=lw, distance=dist, stepsize=st, threshold=ht[:L], ess=he[:L], alpha=ha[:L],
+                resampled=hr[:L].astype(bool), iterations=it)
+
+
+def _gk_struct(d, n_raw, n_sum, data=None, c=0.8, lo=0.0, hi=10.0, buffer=1e-5):
+    keep = None if data is None else _f32(data).reshape(-1)
+    return _GKModel(int(d), int(n_raw), int(n_sum), float(c), float(lo), float(hi), float(buffer), _ptr(keep)), keep
+
+
+def gk_simulate(x, keys, d, n_raw=1000, n_sum=100, data=None, **kw):
+    """thinned order statistics (P, n_sum) of g-and-k simulations of parameter rows x (P, d) with
+    keys (P, 2); with data also the distances (P,)."""
+    x = _f32(x).reshape(-1, d)
+    P = x.shape[0]
+    s, keep = _gk_struct(d, n_raw, n_sum, data, **kw)
+    summ = np.empty((P, n_sum), np.float32)
+    dist = np.empty(P, np.float32) if data is not None else None
+    lib().o_gk_simulate(ctypes.byref(s), P, x.reshape(-1), _u32(keys).reshape(-1), _ptr(summ), _ptr(dist))
+    return summ, dist
+
+
+def abc_gk_run(d, data, N, key, n_raw=1000, n_sum=100, mcmc_steps=1, max_iter=10000, retain=0.9, resample_thr=0.5,
+               term_alpha=0.01, schedule=None, stepsize=None):
+    """mocat.run of MetropolisedABCSMCSampler on a g-and-k scenario (d = 4 or 1), one posterior;
+    returns as abc_lg_run."""
+    s, keep = _gk_struct(d, n_raw, n_sum, data)
+    sch = None if schedule is None else _f32(schedule)
+    if sch is not None:
+        max_iter = sch.size
+    cf = _ABCConfig(N, mcmc_steps, max_iter, 0 if sch is None else sch.size, 1 if stepsize is None else 0,
+                    float(retain), float(resample_thr), float(term_alpha), 0.0 if stepsize is None else float(stepsize),
+                    _ptr(sch))
+    x = np.empty((N, d), np.float32)
+    lw = np.empty(N, np.float32)
+    dist = np.empty(N, np.float32)
+    st = np.empty(d, np.float32)
+    H = max_iter + 1
+    ht, he, ha = np.zeros(H, np.float32), np.zeros(H, np.float32), np.zeros(H, np.float32)
+    hr = np.zeros(H, np.int32)
+    it = lib().o_abc_gk_run(ctypes.byref(s), ctypes.byref(cf), _u32(key), x.reshape(-1), lw, dist, st, ht, he, ha, hr)
     L = it + 1
     return dict(value=x, log_weight=lw, distance=dist, stepsize=st, threshold=ht[:L], ess=he[:L], alpha=ha[:L],
                 resampled=hr[:L].astype(bool), iterations=it)

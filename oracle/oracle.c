@@ -1186,11 +1186,11 @@ static float o_abc_select(const float *v, int n, int k, uint32_t *scratch)
 
 /* MetropolisedABCSMCSampler adapt (abc/smc.py:226-245); returns 1 while active.
  * iter: the iteration just completed (0 = startup); ess_prev: the state's ess field */
-static int o_abc_adapt(const o_abc_model *md, const o_abc_config *cf, int iter, float ess_prev, float *x, float *lw,
+static int o_abc_adapt(int d, const o_abc_config *cf, int iter, float ess_prev, float *x, float *lw,
                        const float *dist, const float *alpha, float *stepsize, float *thr_out, float *ess_out,
                        float *alpha_mean_out, uint32_t *scratch)
 {
-    const int N = cf->N, d = md->d;
+    const int N = cf->N;
     double part[O_ABC_TPB];
     int cnt = 0;
     for (int t = 0; t < O_ABC_TPB; ++t) {
@@ -1246,16 +1246,130 @@ static int o_abc_adapt(const o_abc_model *md, const o_abc_config *cf, int iter, 
     return !(alive == 0 || alpha_mean <= cf->term_alpha || iter >= cf->max_iter);
 }
 
+
+/* ------------------------------------------------ g-and-k ABC scenarios */
+
+typedef struct {
+    int d;                  /* 4 (A, B, g, k) or 1 (A only) */
+    int n_raw, n_sum;       /* draws per simulation, thinned order statistics */
+    float c, lo, hi, buffer;
+    const float *data;      /* (n_sum) observed summary */
+} o_gk_model;
+
+/* erfc by Numerical Recipes' erfcc (Chebyshev fit, fractional error < 1.2e-7) */
+static float o_gk_erfcc(float x)
+{
+    const float z = fabsf(x);
+    const float t = 1.0f / fmaf(0.5f, z, 1.0f);
+    float q = 0.17087277f;
+    q = fmaf(t, q, -0.82215223f);
+    q = fmaf(t, q, 1.48851587f);
+    q = fmaf(t, q, -1.13520398f);
+    q = fmaf(t, q, 0.27886807f);
+    q = fmaf(t, q, -0.18628806f);
+    q = fmaf(t, q, 0.09678418f);
+    q = fmaf(t, q, 0.37409196f);
+    q = fmaf(t, q, 1.00002368f);
+    const float arg = fmaf(t, q, -(z * z) - 1.26551223f);
+    const float ans = t * o_expf(arg);
+    return x >= 0.0f ? ans : 2.0f - ans;
+}
+
+static float o_gk_ncdf(float x) { return 0.5f * o_gk_erfcc(-x * 0.70710677f); }
+static float o_gk_ppf(float u) { return 1.41421354f * o_erfinvf(2.0f * u - 1.0f); }
+
+/* constrained (A, B, g, exponent): lo + Phi(x) (hi - lo); the A-only scenario keeps
+ * B = 1, g = 2 and the exponent c (gk.py:146-156) */
+static void o_gk_params(const o_gk_model *md, const float *x, float q[4])
+{
+    const float span = md->hi - md->lo;
+    if (md->d == 4) {
+        for (int j = 0; j < 4; ++j) q[j] = md->lo + o_gk_ncdf(x[j]) * span;
+    } else {
+        q[0] = md->lo + o_gk_ncdf(x[0]) * span;
+        q[1] = 1.0f; q[2] = 2.0f; q[3] = md->c;
+    }
+}
+
+/* full_data_sample (gk.py:101-110): u = max(buffer, f (1 - 2 buffer) + buffer), z = Phi^-1(u),
+ * v = A + ((B (1 + c (1 - e) / (1 + e))) z) (1 + z^2)^k, e = exp(-g z), (.)^k = exp(k log(.)) */
+static float o_gk_value(const o_gk_model *md, const float q[4], uint32_t bits)
+{
+    const float range = (1.0f - md->buffer) - md->buffer;
+    const float u = fmaxf(md->buffer, o_bits_to_unit(bits) * range + md->buffer);
+    const float z = o_gk_ppf(u);
+    const float e = o_expf(-(q[2] * z));
+    const float term = 1.0f + (md->c * (1.0f - e)) / (1.0f + e);
+    const float pw = o_expf(q[3] * o_logf(1.0f + z * z));
+    return q[0] + ((q[1] * term) * z) * pw;
+}
+
+/* ascending order of floats with NaN last (jnp.sort) */
+static uint32_t o_gk_key(float v)
+{
+    if (v != v) return 0xFFFFFFFEu;
+    const uint32_t b = o_asu(v);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+static float o_gk_unkey(uint32_t k)
+{
+    if (k == 0xFFFFFFFEu) return NAN;
+    return o_asf((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+/* likelihood_sample of GKThinOrder (tests/test_abc_gk.py): n_sum sorted draws at ranks
+ * floor(j n_raw / n_sum); with data: the distance |summary - data|_2 summed in index order */
+static float o_gk_sim(const o_gk_model *md, const float *x, uint32_t k0, uint32_t k1, float *summary)
+{
+    float q[4];
+    o_gk_params(md, x, q);
+    uint32_t *keys = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)md->n_raw);
+    for (int i = 0; i < md->n_raw; ++i)
+        keys[i] = o_gk_key(o_gk_value(md, q, o_bits_at(k0, k1, (uint64_t)md->n_raw, (uint64_t)i)));
+    qsort(keys, (size_t)md->n_raw, sizeof(uint32_t), o_cmp_u32);
+    float acc = 0.0f;
+    for (int j = 0; j < md->n_sum; ++j) {
+        const float v = o_gk_unkey(keys[(int)(((int64_t)j * md->n_raw) / md->n_sum)]);
+        if (summary) summary[j] = v;
+        if (md->data) {
+            const float dv = v - md->data[j];
+            acc = j == 0 ? dv * dv : acc + dv * dv;
+        }
+    }
+    free(keys);
+    return sqrtf(acc);
+}
+
+void o_gk_simulate(const o_gk_model *md, int64_t P, const float *x, const uint32_t *keys, float *summary,
+                   float *dist)
+{
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int64_t r = 0; r < P; ++r) {
+        const float dv = o_gk_sim(md, x + r * md->d, keys[2 * r], keys[2 * r + 1],
+                                  summary ? summary + r * md->n_sum : NULL);
+        if (dist) dist[r] = dv;
+    }
+}
+
+static float o_gk_prior_pot(int d, const float *x)
+{
+    float s = x[0] * x[0];
+    for (int j = 1; j < d; ++j) s = s + x[j] * x[j];
+    return 0.5f * s;
+}
+
 /* mocat.run of MetropolisedABCSMCSampler with RandomWalkABC moves on the ABC
  * LinearGaussian scenario (abc/smc.py:101-245, abc/mcmc.py:59-103,
  * metropolis.py:48-70, transport/smc.py:61-100, sample.py:110-148), one
  * posterior, systematic resampling.  x (N, d) receives the final particles,
  * lw / dist (N) the final log-weights and distances; hist_* (max_iter + 1)
  * entry 0 = after startup.  Returns the number of iterations. */
-int o_abc_lg_run(const o_abc_model *md, const o_abc_config *cf, const uint32_t *key, float *x, float *lw,
-                 float *dist, float *stepsize, float *hist_thr, float *hist_ess, float *hist_alpha, int32_t *hist_res)
+static int o_abc_run(const o_abc_model *md, const o_gk_model *gk, const o_abc_config *cf, const uint32_t *key,
+                     float *x, float *lw, float *dist, float *stepsize, float *hist_thr, float *hist_ess,
+                     float *hist_alpha, int32_t *hist_res)
 {
-    const int N = cf->N, d = md->d;
+    const int N = cf->N, d = gk ? gk->d : md->d;
     float *pp = (float *)malloc(sizeof(float) * (size_t)N), *alpha = (float *)malloc(sizeof(float) * (size_t)N);
     float *x2 = (float *)malloc(sizeof(float) * (size_t)N * d), *f2 = (float *)malloc(sizeof(float) * (size_t)N * 3);
     int32_t *anc = (int32_t *)malloc(sizeof(int32_t) * (size_t)N);
@@ -1264,27 +1378,33 @@ int o_abc_lg_run(const o_abc_model *md, const o_abc_config *cf, const uint32_t *
     o_split_at(key[0], key[1], 2, 0, &e0, &e1);
     o_split_at(key[0], key[1], 2, 1, &s0, &s1);
     o_split_at(e0, e1, (uint64_t)N + 1, (uint64_t)N, &f0, &f1);
+#pragma omp parallel for schedule(dynamic, 8)
     for (int i = 0; i < N; ++i) {
         uint32_t a0, a1, k0, k1;
         float e[16];
         o_split_at(s0, s1, (uint64_t)N, (uint64_t)i, &a0, &a1);
         o_normal_vec(a0, a1, d, e);
         float *xi = x + (size_t)i * d;
-        for (int r = 0; r < d; ++r) {
-            float v = md->C0[r * d] * e[0];
-            for (int k = 1; k < d; ++k) v = fmaf(md->C0[r * d + k], e[k], v);
-            xi[r] = md->m0[r] + v;
+        if (gk) {
+            for (int r = 0; r < d; ++r) xi[r] = e[r];
+            pp[i] = o_gk_prior_pot(d, xi);
+        } else {
+            for (int r = 0; r < d; ++r) {
+                float v = md->C0[r * d] * e[0];
+                for (int k = 1; k < d; ++k) v = fmaf(md->C0[r * d + k], e[k], v);
+                xi[r] = md->m0[r] + v;
+            }
+            pp[i] = o_abc_prior_pot(md, xi);
         }
-        pp[i] = o_abc_prior_pot(md, xi);
         o_split_at(f0, f1, (uint64_t)N + 1, (uint64_t)i, &k0, &k1);
-        dist[i] = o_abc_sim_dist(md, xi, k0, k1);
+        dist[i] = gk ? o_gk_sim(gk, xi, k0, k1, NULL) : o_abc_sim_dist(md, xi, k0, k1);
         alpha[i] = 1.0f;
         lw[i] = 0.0f;
     }
     uint32_t k[2];
     o_split_at(f0, f1, (uint64_t)N + 1, (uint64_t)N, &k[0], &k[1]);
     float thr, ess, am;
-    int active = o_abc_adapt(md, cf, 0, (float)N, x, lw, dist, alpha, stepsize, &thr, &ess, &am, scratch);
+    int active = o_abc_adapt(d, cf, 0, (float)N, x, lw, dist, alpha, stepsize, &thr, &ess, &am, scratch);
     hist_thr[0] = thr; hist_ess[0] = ess; hist_alpha[0] = am; hist_res[0] = 0;
     int iter = 0;
     while (active) {
@@ -1306,6 +1426,7 @@ int o_abc_lg_run(const o_abc_model *md, const o_abc_config *cf, const uint32_t *
         }
         float sq[16];
         for (int j = 0; j < d; ++j) sq[j] = sqrtf(stepsize[j]);
+#pragma omp parallel for schedule(dynamic, 8)
         for (int i = 0; i < N; ++i) {
             if (!(lw[i] > -INFINITY)) continue;
             float *xi = x + (size_t)i * d;
@@ -1318,11 +1439,11 @@ int o_abc_lg_run(const o_abc_model *md, const o_abc_config *cf, const uint32_t *
                 o_split_at(t0, t1, 4, 0, &n0, &n1);
                 o_split_at(t0, t1, 4, 1, &a0, &a1);
                 o_split_at(t0, t1, 4, 3, &c0, &c1);
-                float e[16], xp[16];
+                float e[16], xp[16] = {0.0f};
                 o_normal_vec(a0, a1, d, e);
                 for (int j = 0; j < d; ++j) xp[j] = xi[j] + sq[j] * e[j];
-                const float ppn = o_abc_prior_pot(md, xp);
-                const float dn = o_abc_sim_dist(md, xp, c0, c1);
+                const float ppn = gk ? o_gk_prior_pot(d, xp) : o_abc_prior_pot(md, xp);
+                const float dn = gk ? o_gk_sim(gk, xp, c0, c1, NULL) : o_abc_sim_dist(md, xp, c0, c1);
                 float a = o_expf(pp[i] - ppn) * (dn < thr ? 1.0f : 0.0f);
                 a = a != a ? 0.0f : fminf(1.0f, a);
                 o_split_at(n0, n1, 2, 0, &u0, &u1);
@@ -1338,7 +1459,7 @@ int o_abc_lg_run(const o_abc_model *md, const o_abc_config *cf, const uint32_t *
             }
             alpha[i] = asum / (float)cf->mcmc_steps;
         }
-        active = o_abc_adapt(md, cf, iter, ess, x, lw, dist, alpha, stepsize, &thr, &ess, &am, scratch);
+        active = o_abc_adapt(d, cf, iter, ess, x, lw, dist, alpha, stepsize, &thr, &ess, &am, scratch);
         uint32_t z0, z1;
         o_split_at(k[0], k[1], (uint64_t)N + 2, (uint64_t)N + 1, &z0, &z1);
         k[0] = z0; k[1] = z1;
@@ -1348,6 +1469,19 @@ int o_abc_lg_run(const o_abc_model *md, const o_abc_config *cf, const uint32_t *
     }
     free(pp); free(alpha); free(x2); free(f2); free(anc); free(scratch);
     return iter;
+}
+
+int o_abc_lg_run(const o_abc_model *md, const o_abc_config *cf, const uint32_t *key, float *x, float *lw,
+                 float *dist, float *stepsize, float *hist_thr, float *hist_ess, float *hist_alpha, int32_t *hist_res)
+{
+    return o_abc_run(md, NULL, cf, key, x, lw, dist, stepsize, hist_thr, hist_ess, hist_alpha, hist_res);
+}
+
+/* the same sampler on a g-and-k scenario */
+int o_abc_gk_run(const o_gk_model *gk, const o_abc_config *cf, const uint32_t *key, float *x, float *lw,
+                 float *dist, float *stepsize, float *hist_thr, float *hist_ess, float *hist_alpha, int32_t *hist_res)
+{
+    return o_abc_run(NULL, gk, cf, key, x, lw, dist, stepsize, hist_thr, hist_ess, hist_alpha, hist_res);
 }
 
 int o_num_threads(void)

@@ -1,0 +1,77 @@
+"""g-and-k ABC on the GPU (mocat_gb300.abc.GKTransformedUniformPrior / GKOnlyATransformedUniformPrior,
+mgb_abc_gk_*) vs the oracle: summaries of the simulator bit for bit, and the whole
+MetropolisedABCSMCSampler run (particles, distances, log-weights, stepsizes, every
+iteration's threshold, ESS, acceptance and resampling flag) bit for bit for B posteriors;
+and the reference's own check (tests/test_abc_gk.py TestMetSMCGK / TestMetSMCGKOnlyA)."""
+import numpy as np
+import pytest
+import torch
+
+import oracle as O
+from test_oracle_abc_gk import TRUE1, TRUE4, _unconstrain
+
+pytestmark = pytest.mark.gpu
+
+
+def _scenario(onlyA, data=None, n_raw=1000, n_sum=100):
+    import mocat_gb300 as mg
+    cls = mg.abc.GKOnlyAThinOrder if onlyA else mg.abc.GKThinOrder
+    return cls(n_unsummarised_data=n_raw, num_thin=n_sum, data=data)
+
+
+@pytest.mark.parametrize("onlyA", [False, True])
+@pytest.mark.parametrize("n_raw,n_sum", [(1000, 100), (300, 17), (2048, 64)])
+def test_simulator_bit_exact(cuda, onlyA, n_raw, n_sum):
+    d = 1 if onlyA else 4
+    rng = np.random.default_rng(n_raw)
+    x = (rng.standard_normal((50, d)) * 0.8).astype(np.float32)
+    keys = np.stack([O.PRNGKey(s) for s in range(50)])
+    sc = _scenario(onlyA, n_raw=n_raw, n_sum=n_sum)
+    got = sc.simulate_summaries(torch.from_numpy(x).cuda(), keys).cpu().numpy()
+    ref, _ = O.gk_simulate(x, keys, d, n_raw=n_raw, n_sum=n_sum)
+    assert np.array_equal(got, ref)
+
+
+@pytest.mark.parametrize("onlyA", [False, True])
+@pytest.mark.parametrize("mode", ["schedule", "adaptive"])
+def test_smc_matches_oracle(cuda, onlyA, mode):
+    import mocat_gb300 as mg
+    d = 1 if onlyA else 4
+    true_u = _unconstrain(TRUE1 if onlyA else TRUE4).astype(np.float32)
+    data, _ = O.gk_simulate(true_u[None], O.PRNGKey(0)[None], d)
+    sc = _scenario(onlyA, data=data[0])
+    if mode == "schedule":
+        sch = np.linspace(100.0, 10.0, 6)
+        smp, kw = mg.abc.MetropolisedABCSMCSampler(threshold_schedule=sch, mcmc_steps=2), dict(schedule=sch,
+                                                                                              mcmc_steps=2)
+    else:
+        smp = mg.abc.MetropolisedABCSMCSampler(ess_threshold_retain=0.7, termination_alpha=0.1, max_iter=12)
+        kw = dict(retain=0.7, term_alpha=0.1, max_iter=12)
+    N = 300
+    keys = np.stack([O.PRNGKey(4), O.PRNGKey(77)])
+    out = mg.abc.run_batched(sc, smp, N, keys)
+    for b in range(2):
+        ref = O.abc_gk_run(d, data[0], N, keys[b], **kw)
+        L = ref["iterations"] + 1
+        assert int(out.iterations[b]) == ref["iterations"]
+        for k in ("threshold", "ess", "alpha", "resampled"):
+            assert np.array_equal(getattr(out, k)[b, :L].cpu().numpy(), ref[k]), k
+        for k in ("value", "distance", "log_weight", "stepsize"):
+            assert np.array_equal(getattr(out, k)[b].cpu().numpy(), ref[k]), k
+
+
+@pytest.mark.parametrize("onlyA", [False, True])
+@pytest.mark.parametrize("mode", ["schedule", "adaptive"])
+def test_reference_check(cuda, onlyA, mode):
+    """TestMetSMCGK / TestMetSMCGKOnlyA: n = 1e3, |true - mean(final particles)|_1 < 3"""
+    import mocat_gb300 as mg
+    d = 1 if onlyA else 4
+    true_u = _unconstrain(TRUE1 if onlyA else TRUE4).astype(np.float32)
+    sc = _scenario(onlyA)
+    sc.data = sc.likelihood_sample(true_u, mg.random.PRNGKey(0)).cpu().numpy()
+    if mode == "schedule":
+        smp = mg.abc.MetropolisedABCSMCSampler(threshold_schedule=np.linspace(100.0, 10.0, 10))
+    else:
+        smp = mg.abc.MetropolisedABCSMCSampler(ess_threshold_retain=0.8, termination_alpha=0.1)
+    out = mg.abc.run(sc, smp, 1000, mg.random.PRNGKey(0))
+    assert np.abs(true_u - out.value.double().cpu().numpy().mean(0)).sum() < 3.0
