@@ -633,6 +633,20 @@ int mgb_abc_gk_smc_step(const mgb_abc_smc_config *cfg, const mgb_abc_gk_model *m
 int mgb_abc_gk_simulate(const mgb_abc_gk_model *model_host, int64_t P, const float *x_dev, const uint32_t *keys_dev,
                         float *summary_dev, float *dist_dev, void *stream);
 
+/* VanillaABC (mocat/src/abc/importance.py:16-118) run as mocat.run does: a chain of n prior draws
+ * with sequential keys ((K, s) = split(K) for x_0, one split for its prior potential, one for its
+ * simulation; then (K, k1, k2, k3) = split(K, 4) per draw), log_weight = 0 where distance <
+ * threshold else -inf.  acceptance_rate >= 0 replaces the threshold by
+ * jnp.quantile(distance, acceptance_rate) (clean_chain_ar); threshold_out (device, 1 float)
+ * receives the threshold used.  x (n, d), pp, dist, lw (n) device outputs. */
+size_t mgb_abc_vanilla_workspace(int64_t n);
+int mgb_abc_vanilla_lg(const mgb_abc_lg_model *model_host, int64_t n, const uint32_t *key_dev, float threshold,
+                       float acceptance_rate, void *ws_dev, size_t ws_bytes, float *x_dev, float *prior_potential_dev,
+                       float *distance_dev, float *log_weight_dev, float *threshold_out_dev, void *stream);
+int mgb_abc_vanilla_gk(const mgb_abc_gk_model *model_host, int64_t n, const uint32_t *key_dev, float threshold,
+                       float acceptance_rate, void *ws_dev, size_t ws_bytes, float *x_dev, float *prior_potential_dev,
+                       float *distance_dev, float *log_weight_dev, float *threshold_out_dev, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

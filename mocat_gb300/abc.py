@@ -167,6 +167,53 @@ class RandomWalkABC:
         self.stepsize = stepsize
 
 
+class VanillaABC:
+    """Importance (rejection) ABC from the prior (abc/importance.py:97-118) run as mocat.run runs
+    it: a chain of n prior draws with sequential keys, log_weight 0 where the distance is below
+    the threshold, else -inf; with acceptance_rate the threshold becomes the acceptance_rate
+    quantile of the chain's distances (clean_chain_ar) and is written back to
+    parameters.threshold."""
+    name = "Vanilla ABC"
+
+    def __init__(self, threshold=math.inf, acceptance_rate=None):
+        self.parameters = cdict(threshold=float(threshold))
+        if acceptance_rate is not None:
+            self.parameters.acceptance_rate = float(acceptance_rate)
+
+
+def _run_vanilla(scenario, sampler, n, random_key):
+    gk = isinstance(scenario, GKTransformedUniformPrior)
+    if not gk and not isinstance(scenario, LinearGaussian):
+        raise NotImplementedError(f"{scenario.__class__.__name__}: no GPU ABC kernel for this scenario")
+    if not gk and (scenario.dim, scenario.dim_obs) not in SUPPORTED:
+        raise NotImplementedError(f"(d, dy) = ({scenario.dim}, {scenario.dim_obs}) not compiled")
+    if not 2 <= n <= 0x7FFFFFFF:
+        raise ValueError("n must be at least 2")
+    key = _dev.as_key(random_key).reshape(2).contiguous()
+    dev = key.device
+    d = scenario.dim
+    x = torch.empty((n, d), dtype=torch.float32, device=dev)
+    pp, dist, lw = (torch.empty(n, dtype=torch.float32, device=dev) for _ in range(3))
+    thr = torch.empty(1, dtype=torch.float32, device=dev)
+    ws = _dev.workspace(_lib.lib().mgb_abc_vanilla_workspace(n), dev)
+    rate = getattr(sampler.parameters, "acceptance_rate", None)
+    args = (n, _dev.ptr(key), float(sampler.parameters.threshold), -1.0 if rate is None else float(rate),
+            _dev.ptr(ws), ws.numel(), _dev.ptr(x), _dev.ptr(pp), _dev.ptr(dist), _dev.ptr(lw), _dev.ptr(thr),
+            _dev.stream_ptr())
+    if gk:
+        if scenario.data is None or np.size(scenario.data) != scenario.num_thin:
+            raise ValueError("the g-and-k scenario needs data: num_thin summary values")
+        data = torch.as_tensor(np.asarray(scenario.data, np.float32), device=dev).contiguous()
+        call("mgb_abc_vanilla_gk", ctypes.byref(scenario.model(_dev.ptr(data))), *args)
+    else:
+        _keep, model = scenario.derived()
+        call("mgb_abc_vanilla_lg", ctypes.byref(model), *args)
+    t = float(thr.item())
+    if rate is not None:
+        sampler.parameters.threshold = t
+    return cdict(value=x, log_weight=lw, distance=dist, prior_potential=pp, threshold=t)
+
+
 class MetropolisedABCSMCSampler:
     """ABC-SMC with MCMC moves (abc/smc.py:101-245).  mcmc_sampler=None is the reference's
     default: RandomWalkABC with the stepsize re-set after every iteration to the particles'
@@ -280,7 +327,9 @@ def run_batched(scenario, sampler, n, random_keys):
 
 
 def run(scenario, sampler, n, random_key):
-    """mocat.run (sample.py:110-148) for MetropolisedABCSMCSampler on an ABC scenario."""
+    """mocat.run (sample.py:110-148) for MetropolisedABCSMCSampler or VanillaABC on an ABC scenario."""
+    if isinstance(sampler, VanillaABC):
+        return _run_vanilla(scenario, sampler, n, random_key)
     out = run_batched(scenario, sampler, n, _dev.as_key(random_key).reshape(1, 2))
     L = int(out.iterations[0]) + 1
     return cdict(value=out.value[0], log_weight=out.log_weight[0], distance=out.distance[0],

@@ -883,6 +883,147 @@ static int gk_step(const mgb_abc_smc_config *cfg, const mgb_abc_gk_model *m, voi
   return launch_status();
 }
 
+// ------------------------------------------------------------ VanillaABC
+// mocat.run(scenario, VanillaABC(threshold | acceptance_rate), n, key) (abc/importance.py:16-118,
+// abc/abc.py:42-66, sample.py:110-148): a chain of n independent prior draws whose keys
+// are sequential:
+//   (K, s) = split(K): x_0 = prior_sample(s); (K, _) = split(K) (prior potential);
+//   (K, k) = split(K): simulation of x_0 with k;
+//   step i = 1..n-1: (K, k1, k2, k3) = split(K, 4): x_i = prior_sample(k1), simulation with k3;
+//   log_weight = 0 if distance < threshold else -inf; with acceptance_rate the threshold is
+//   jnp.quantile(distance, acceptance_rate) (linear interpolation) over the whole chain.
+// The key chain is one thread (a serial dependency); the draws and simulations are parallel.
+__global__ void k_vabc_keys(const uint32_t *key, int64_t n, uint32_t *__restrict__ pk, uint32_t *__restrict__ sk) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  uint32_t K0 = key[0], K1 = key[1], a0, a1, b0, b1;
+  split_at(K0, K1, 2, 1, a0, a1);
+  pk[0] = a0;
+  pk[1] = a1;
+  split_at(K0, K1, 2, 0, b0, b1);        // after the prior draw
+  split_at(b0, b1, 2, 0, K0, K1);        // after the prior potential
+  split_at(K0, K1, 2, 1, a0, a1);        // the simulation key of x_0
+  sk[0] = a0;
+  sk[1] = a1;
+  split_at(K0, K1, 2, 0, b0, b1);
+  K0 = b0;
+  K1 = b1;
+  for (int64_t i = 1; i < n; ++i) {
+    split_at(K0, K1, 4, 1, a0, a1);
+    pk[2 * i] = a0;
+    pk[2 * i + 1] = a1;
+    split_at(K0, K1, 4, 3, a0, a1);
+    sk[2 * i] = a0;
+    sk[2 * i + 1] = a1;
+    split_at(K0, K1, 4, 0, b0, b1);
+    K0 = b0;
+    K1 = b1;
+  }
+}
+
+// linear-Gaussian scenario: prior draw, prior potential, simulation distance, threshold weight
+template <int D, int DY>
+__global__ void __launch_bounds__(ABC_MOVE_TPB) k_vabc_lg(const __grid_constant__ ABCP<D, DY> p, int64_t n,
+                                                           const uint32_t *pk, const uint32_t *sk, float thr,
+                                                           int weigh, float *x, float *pp, float *dist, float *lw) {
+  const int64_t i = blockIdx.x * (int64_t)ABC_MOVE_TPB + threadIdx.x;
+  if (i >= n) return;
+  uint32_t bits[D];
+  bits_vec<D>(pk[2 * i], pk[2 * i + 1], bits, p.one);
+  float e[D], xv[D];
+#pragma unroll
+  for (int j = 0; j < D; ++j) e[j] = bits_to_normal(bits[j]);
+#pragma unroll
+  for (int r = 0; r < D; ++r) {
+    float v = __fmul_rn(p.C0[r * D], e[0]);
+#pragma unroll
+    for (int k = 1; k < D; ++k) v = __fmaf_rn(p.C0[r * D + k], e[k], v);
+    xv[r] = __fadd_rn(p.m0[r], v);
+    x[i * D + r] = xv[r];
+  }
+  pp[i] = abc_prior_potential<D, DY>(p, xv);
+  const float dv = abc_sim_distance<D, DY>(p, xv, sk[2 * i], sk[2 * i + 1]);
+  dist[i] = dv;
+  if (weigh) lw[i] = dv < thr ? 0.0f : -INFINITY;
+}
+
+// g-and-k scenario: prior draw and potential (the simulation is k_gk_sim)
+template <int D>
+__global__ void __launch_bounds__(ABC_MOVE_TPB) k_vabc_gk_prior(int64_t n, const uint32_t *pk, float *x, float *pp,
+                                                                 uint32_t one) {
+  const int64_t i = blockIdx.x * (int64_t)ABC_MOVE_TPB + threadIdx.x;
+  if (i >= n) return;
+  uint32_t bits[D];
+  bits_vec<D>(pk[2 * i], pk[2 * i + 1], bits, one);
+  float xv[D];
+#pragma unroll
+  for (int j = 0; j < D; ++j) {
+    xv[j] = bits_to_normal(bits[j]);
+    x[i * D + j] = xv[j];
+  }
+  pp[i] = gk_prior_pot<D>(xv);
+}
+
+// the threshold (given, or the acceptance-rate quantile of the distances) and the weights; one block
+__global__ void __launch_bounds__(ABC_TPB) k_vabc_weights(int64_t n, float thr_in, float rate, const float *dist,
+                                                          float *lw, float *thr_out) {
+  __shared__ unsigned hist[256], res[2];
+  float thr = thr_in;
+  if (rate >= 0.0f) {
+    const float pos = __fmul_rn(rate, (float)(n - 1));
+    const float lo = floorf(pos), hi = ceilf(pos);
+    const float hw = __fsub_rn(pos, lo), lwt = __fsub_rn(1.0f, hw);
+    const int64_t ilo = (int64_t)fminf(fmaxf(lo, 0.0f), (float)(n - 1));
+    const int64_t ihi = (int64_t)fminf(fmaxf(hi, 0.0f), (float)(n - 1));
+    const float vlo = abc_block_select(dist, n, ilo, hist, res);
+    const float vhi = ihi == ilo ? vlo : abc_block_select(dist, n, ihi, hist, res);
+    thr = __fadd_rn(__fmul_rn(vlo, lwt), __fmul_rn(vhi, hw));
+  }
+  for (int64_t i = threadIdx.x; i < n; i += ABC_TPB) lw[i] = dist[i] < thr ? 0.0f : -INFINITY;
+  if (threadIdx.x == 0) *thr_out = thr;
+}
+
+struct VABCWs {
+  uint32_t *pk, *sk;
+};
+
+static VABCWs carve_vabc(Carver &c, int64_t n) {
+  VABCWs v;
+  v.pk = c.take<uint32_t>(2 * (size_t)n);
+  v.sk = c.take<uint32_t>(2 * (size_t)n);
+  return v;
+}
+
+template <int D, int DY>
+static int vabc_lg(const mgb_abc_lg_model *m, int64_t n, const uint32_t *key, float thr, float rate, void *ws,
+                   float *x, float *pp, float *dist, float *lw, float *thr_out, cudaStream_t s) {
+  Carver c(ws);
+  const VABCWs v = carve_vabc(c, n);
+  k_vabc_keys<<<1, 32, 0, s>>>(key, n, v.pk, v.sk);
+  int st = launch_status();
+  if (st) return st;
+  k_vabc_lg<D, DY><<<(unsigned)((n + ABC_MOVE_TPB - 1) / ABC_MOVE_TPB), ABC_MOVE_TPB, 0, s>>>(
+      pack_abc<D, DY>(m), n, v.pk, v.sk, thr, 0, x, pp, dist, lw);
+  if ((st = launch_status())) return st;
+  k_vabc_weights<<<1, ABC_TPB, 0, s>>>(n, thr, rate, dist, lw, thr_out);
+  return launch_status();
+}
+
+template <int D>
+static int vabc_gk(const mgb_abc_gk_model *m, int64_t n, const uint32_t *key, float thr, float rate, void *ws,
+                   float *x, float *pp, float *dist, float *lw, float *thr_out, cudaStream_t s) {
+  Carver c(ws);
+  const VABCWs v = carve_vabc(c, n);
+  k_vabc_keys<<<1, 32, 0, s>>>(key, n, v.pk, v.sk);
+  int st = launch_status();
+  if (st) return st;
+  k_vabc_gk_prior<D><<<(unsigned)((n + ABC_MOVE_TPB - 1) / ABC_MOVE_TPB), ABC_MOVE_TPB, 0, s>>>(n, v.pk, x, pp, 1u);
+  if ((st = launch_status())) return st;
+  k_gk_sim<<<(unsigned)n, GK_TPB, 0, s>>>(pack_gk(m), n, x, v.sk, nullptr, dist, nullptr);
+  if ((st = launch_status())) return st;
+  k_vabc_weights<<<1, ABC_TPB, 0, s>>>(n, thr, rate, dist, lw, thr_out);
+  return launch_status();
+}
+
 #define MGB_ABC_DISPATCH(FN, ...)                                     \
   do {                                                                \
     const int d_ = m->d, dy_ = m->dy;                                 \
@@ -979,6 +1120,36 @@ int mgb_abc_gk_smc_step(const mgb_abc_smc_config *cfg, const mgb_abc_gk_model *m
   if (ws_bytes < mgb_abc_gk_workspace(cfg, m->d)) return ERR_WORKSPACE;
   if (m->d == 4) return gk_step<4>(cfg, m, ws, (cudaStream_t)stream);
   return gk_step<1>(cfg, m, ws, (cudaStream_t)stream);
+}
+
+size_t mgb_abc_vanilla_workspace(int64_t n) {
+  if (n < 1) return 0;
+  Carver c(nullptr);
+  carve_vabc(c, n);
+  return c.bytes();
+}
+
+int mgb_abc_vanilla_lg(const mgb_abc_lg_model *m, int64_t n, const uint32_t *key, float threshold,
+                       float acceptance_rate, void *ws, size_t ws_bytes, float *x, float *pp, float *dist, float *lw,
+                       float *threshold_out, void *stream) {
+  if (!m || !m->m0 || !m->C0 || !m->P0 || !m->H || !m->L || !m->data || n < 2 || n > 0x7FFFFFFFll || !key || !ws ||
+      !x || !pp || !dist || !lw || !threshold_out)
+    return ERR_BAD_ARG;
+  if (ws_bytes < mgb_abc_vanilla_workspace(n)) return ERR_WORKSPACE;
+  MGB_ABC_DISPATCH(vabc_lg, m, n, key, threshold, acceptance_rate, ws, x, pp, dist, lw, threshold_out,
+                   (cudaStream_t)stream);
+}
+
+int mgb_abc_vanilla_gk(const mgb_abc_gk_model *m, int64_t n, const uint32_t *key, float threshold,
+                       float acceptance_rate, void *ws, size_t ws_bytes, float *x, float *pp, float *dist, float *lw,
+                       float *threshold_out, void *stream) {
+  if (!gk_ok(m) || !m->data_dev || n < 2 || n > 0x7FFFFFFFll || !key || !ws || !x || !pp || !dist || !lw ||
+      !threshold_out)
+    return ERR_BAD_ARG;
+  if (ws_bytes < mgb_abc_vanilla_workspace(n)) return ERR_WORKSPACE;
+  if (m->d == 4)
+    return vabc_gk<4>(m, n, key, threshold, acceptance_rate, ws, x, pp, dist, lw, threshold_out, (cudaStream_t)stream);
+  return vabc_gk<1>(m, n, key, threshold, acceptance_rate, ws, x, pp, dist, lw, threshold_out, (cudaStream_t)stream);
 }
 
 int mgb_abc_gk_simulate(const mgb_abc_gk_model *m, int64_t P, const float *x, const uint32_t *keys, float *summary,

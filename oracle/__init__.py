@@ -151,6 +151,10 @@ def lib():
                                    f32p, f32p, f32p, f32p, i32p]
         L.o_abc_gk_run.restype = ctypes.c_int
         L.o_gk_simulate.argtypes = [ctypes.POINTER(_GKModel), i64, f32p, u32p, vp, vp]
+        for nm, mt in (("o_abc_vanilla_lg", _ABCModel), ("o_abc_vanilla_gk", _GKModel)):
+            getattr(L, nm).argtypes = [ctypes.POINTER(mt), ctypes.c_int, u32p, ctypes.c_float, ctypes.c_float, f32p,
+                                       f32p, f32p, f32p]
+            getattr(L, nm).restype = ctypes.c_float
         L.o_ffbsi_nl1d.argtypes = [ctypes.POINTER(_NLModel), i64, i64, i64, f32p, f32p, f32p, u32p, f32p, i32p]
         L.o_stitch_nl1d.argtypes = [ctypes.POINTER(_NLModel), i64, i64, f32p, f32p, f32p, ctypes.c_float, u32p, i32p]
         L.o_transition_potential_pairs_nl1d.argtypes = [ctypes.POINTER(_NLModel), i64, f32p, f32p, ctypes.c_float,
@@ -588,6 +592,31 @@ def gk_simulate(x, keys, d, n_raw=1000, n_sum=100, data=None, **kw):
     dist = np.empty(P, np.float32) if data is not None else None
     lib().o_gk_simulate(ctypes.byref(s), P, x.reshape(-1), _u32(keys).reshape(-1), _ptr(summ), _ptr(dist))
     return summ, dist
+
+
+def _abc_lg_struct(params):
+    keep = {k: _f32(params[k]) for k in ("m0", "C0", "P0", "H", "L", "data")}
+    md = _ABCModel(keep["m0"].size, keep["data"].size, keep["m0"].ctypes.data, keep["C0"].ctypes.data,
+                   keep["P0"].ctypes.data, float(params["c0"]), keep["H"].ctypes.data, keep["L"].ctypes.data,
+                   keep["data"].ctypes.data)
+    return md, keep
+
+
+def abc_vanilla(n, key, threshold=np.inf, acceptance_rate=None, lg_params=None, gk=None):
+    """mocat.run(scenario, VanillaABC(threshold | acceptance_rate), n, key) on the ABC linear-Gaussian
+    scenario (lg_params as abc_lg_run) or a g-and-k one (gk = dict(d, data, n_raw, n_sum)).
+    Returns dict(value (n, d), prior_potential, distance, log_weight, threshold)."""
+    if gk is not None:
+        s, keep = _gk_struct(gk["d"], gk.get("n_raw", 1000), gk.get("n_sum", 100), gk["data"])
+        fn, d = lib().o_abc_vanilla_gk, gk["d"]
+    else:
+        s, keep = _abc_lg_struct(lg_params)
+        fn, d = lib().o_abc_vanilla_lg, s.d
+    x = np.empty((n, d), np.float32)
+    pp, dist, lw = (np.empty(n, np.float32) for _ in range(3))
+    thr = fn(ctypes.byref(s), n, _u32(key), float(threshold), -1.0 if acceptance_rate is None else float(acceptance_rate),
+             x.reshape(-1), pp, dist, lw)
+    return dict(value=x, prior_potential=pp, distance=dist, log_weight=lw, threshold=np.float32(thr))
 
 
 def abc_gk_run(d, data, N, key, n_raw=1000, n_sum=100, mcmc_steps=1, max_iter=10000, retain=0.9, resample_thr=0.5,

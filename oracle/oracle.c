@@ -1477,6 +1477,78 @@ int o_abc_lg_run(const o_abc_model *md, const o_abc_config *cf, const uint32_t *
     return o_abc_run(md, NULL, cf, key, x, lw, dist, stepsize, hist_thr, hist_ess, hist_alpha, hist_res);
 }
 
+/* VanillaABC (abc/importance.py:16-118) run as mocat.run: n prior draws with the sequential
+ * key chain (K, s) = split(K) [x_0]; (K, _) = split(K) [prior potential]; (K, k) = split(K)
+ * [simulation of x_0]; then (K, k1, k2, k3) = split(K, 4) per draw (x_i from k1, simulation
+ * from k3).  lw = 0 where dist < threshold; rate >= 0: threshold = jnp.quantile(dist, rate)
+ * (linear interpolation).  Returns the threshold. */
+static float o_abc_vanilla(const o_abc_model *md, const o_gk_model *gk, int n, const uint32_t *key, float thr,
+                           float rate, float *x, float *pp, float *dist, float *lw)
+{
+    const int d = gk ? gk->d : md->d;
+    uint32_t *pk = (uint32_t *)malloc(sizeof(uint32_t) * 2 * (size_t)n);
+    uint32_t *sk = (uint32_t *)malloc(sizeof(uint32_t) * 2 * (size_t)n);
+    uint32_t K0, K1, b0, b1;
+    o_split_at(key[0], key[1], 2, 1, &pk[0], &pk[1]);
+    o_split_at(key[0], key[1], 2, 0, &b0, &b1);
+    o_split_at(b0, b1, 2, 0, &K0, &K1);
+    o_split_at(K0, K1, 2, 1, &sk[0], &sk[1]);
+    o_split_at(K0, K1, 2, 0, &b0, &b1);
+    K0 = b0; K1 = b1;
+    for (int i = 1; i < n; ++i) {
+        o_split_at(K0, K1, 4, 1, &pk[2 * i], &pk[2 * i + 1]);
+        o_split_at(K0, K1, 4, 3, &sk[2 * i], &sk[2 * i + 1]);
+        o_split_at(K0, K1, 4, 0, &b0, &b1);
+        K0 = b0; K1 = b1;
+    }
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int i = 0; i < n; ++i) {
+        float e[16];
+        float *xi = x + (size_t)i * d;
+        o_normal_vec(pk[2 * i], pk[2 * i + 1], d, e);
+        if (gk) {
+            for (int r = 0; r < d; ++r) xi[r] = e[r];
+            pp[i] = o_gk_prior_pot(d, xi);
+            dist[i] = o_gk_sim(gk, xi, sk[2 * i], sk[2 * i + 1], NULL);
+        } else {
+            for (int r = 0; r < d; ++r) {
+                float v = md->C0[r * d] * e[0];
+                for (int k = 1; k < d; ++k) v = fmaf(md->C0[r * d + k], e[k], v);
+                xi[r] = md->m0[r] + v;
+            }
+            pp[i] = o_abc_prior_pot(md, xi);
+            dist[i] = o_abc_sim_dist(md, xi, sk[2 * i], sk[2 * i + 1]);
+        }
+    }
+    if (rate >= 0.0f) {
+        uint32_t *scratch = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)n);
+        const float pos = rate * (float)(n - 1);
+        const float lo = floorf(pos), hi = ceilf(pos);
+        const float hw = pos - lo, lwt = 1.0f - hw;
+        const int ilo = (int)fminf(fmaxf(lo, 0.0f), (float)(n - 1));
+        const int ihi = (int)fminf(fmaxf(hi, 0.0f), (float)(n - 1));
+        const float vlo = o_abc_select(dist, n, ilo, scratch);
+        const float vhi = ihi == ilo ? vlo : o_abc_select(dist, n, ihi, scratch);
+        thr = vlo * lwt + vhi * hw;
+        free(scratch);
+    }
+    for (int i = 0; i < n; ++i) lw[i] = dist[i] < thr ? 0.0f : -INFINITY;
+    free(pk); free(sk);
+    return thr;
+}
+
+float o_abc_vanilla_lg(const o_abc_model *md, int n, const uint32_t *key, float thr, float rate, float *x, float *pp,
+                       float *dist, float *lw)
+{
+    return o_abc_vanilla(md, NULL, n, key, thr, rate, x, pp, dist, lw);
+}
+
+float o_abc_vanilla_gk(const o_gk_model *gk, int n, const uint32_t *key, float thr, float rate, float *x, float *pp,
+                       float *dist, float *lw)
+{
+    return o_abc_vanilla(NULL, gk, n, key, thr, rate, x, pp, dist, lw);
+}
+
 /* the same sampler on a g-and-k scenario */
 int o_abc_gk_run(const o_gk_model *gk, const o_abc_config *cf, const uint32_t *key, float *x, float *lw,
                  float *dist, float *stepsize, float *hist_thr, float *hist_ess, float *hist_alpha, int32_t *hist_res)
