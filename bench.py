@@ -41,6 +41,10 @@ abc_smc -- ABC-SMC on the reference's ABC linear-Gaussian test model, 64
 posteriors of 16384 particles to termination: likelihood simulations per
 second, next to the oracle on one posterior.
 
+abc_gk -- ABC-SMC on the reference's g-and-k test scenario (1000 draws per simulation,
+sorted and thinned), 16 posteriors of 4096 particles: simulations per second, next to the
+oracle on one posterior of 1024 particles.
+
 nl1d -- the bootstrap filter on the one-dimensional non-linear benchmark
 model at N = 2^20, T = 1000 (graph replay), its fused step kernel alone, and
 the oracle's C/OpenMP filter on a sample of steps.
@@ -502,6 +506,51 @@ def bench_abc(args, rank):
         r["cpu_baseline"] = {"value": simc / dtc, "unit": "simulations/s", "cores": 1, "kind": "port",
                              "sample": f"one posterior, N={n}, {ref['iterations']} iterations ({dtc:.1f} s), "
                                        "oracle C (one thread)"}
+    return r
+
+
+def bench_abc_gk(args, rank):
+    """ABC-SMC on the reference's g-and-k test scenario (4 parameters, 1000 draws per simulation
+    summarised by 100 thinned order statistics, retain 0.8, termination_alpha 0.1, at most 25
+    iterations), 16 posteriors of 4096 particles in one batch; throughput = simulations (one
+    per move of an alive particle, each 1000 draws and a 1024-key sort) per second; the oracle
+    runs one posterior of 1024 particles on the host cores."""
+    import torch
+    import mocat_gb300 as mg
+    import oracle
+    from scipy.special import ndtri
+    true_u = ndtri(np.array([3.0, 1.0, 2.0, 0.5]) / 10.0).astype(np.float32)
+    sc = mg.abc.GKThinOrder()
+    sc.data = sc.likelihood_sample(true_u, mg.random.PRNGKey(0)).cpu().numpy()
+    smp = mg.abc.MetropolisedABCSMCSampler(ess_threshold_retain=0.8, termination_alpha=0.1, max_iter=25)
+    B, n = 16, 4096
+    keys = np.stack([np.array([0, 5000 + 64 * rank + b], np.uint32) for b in range(B)])
+    mg.abc.run_batched(sc, smp, 256, keys[:2])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out = mg.abc.run_batched(sc, smp, n, keys)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+
+    def count(ess, res, it, N):
+        return N + sum(N if res[k] else round(float(ess[k - 1])) for k in range(1, int(it) + 1))
+    ess, res, it = out.ess.cpu().numpy(), out.resampled.cpu().numpy(), out.iterations.cpu().numpy()
+    sims = float(sum(count(ess[b], res[b], it[b], n) for b in range(B)))
+    r = {"workload": "ABC-SMC, g-and-k (GKThinOrder of the reference's tests: 4 parameters, 1000 draws -> 100 "
+                     "thinned order statistics), MetropolisedABCSMCSampler (RandomWalkABC, retain 0.8, "
+                     "termination_alpha 0.1, <= 25 iterations), 16 posteriors x 4096 particles, seeded keys",
+         "metric": "simulations/s", "value": sims / dt, "unit": "simulations/s", "s_per_batch": dt,
+         "draws_per_s": sims * 1000.0 / dt, "iterations_mean": float(it.mean())}
+    if rank == 0:
+        nc = 1024
+        t0 = time.perf_counter()
+        ref = oracle.abc_gk_run(4, sc.data, nc, keys[0], retain=0.8, term_alpha=0.1, max_iter=25)
+        dtc = time.perf_counter() - t0
+        simc = count(ref["ess"], ref["resampled"], ref["iterations"], nc)
+        r["cpu_baseline"] = {"value": simc / dtc, "unit": "simulations/s", "cores": oracle.num_threads(),
+                             "kind": "port",
+                             "sample": f"one posterior, N={nc}, {ref['iterations']} iterations ({dtc:.1f} s), "
+                                       "oracle C/OpenMP"}
     return r
 
 
@@ -982,6 +1031,7 @@ def main():
         line["nl1d"] = bench_nl1d(args, flush, rank)
     if not args.no_abc:
         line["abc_smc"] = bench_abc(args, rank)
+        line["abc_gk"] = bench_abc_gk(args, rank)
     if rank == 0:
         v_cpu, cores, dt = cpu_baseline(n, args.cpu_steps)
         line["cpu_baseline"] = {"value": v_cpu, "unit": "particle-steps/s", "cores": cores, "kind": "port",
