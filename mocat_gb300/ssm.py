@@ -793,6 +793,9 @@ def fixed_lag_stitching(ssm_scenario, early_block, t, recent_block, recent_block
 
 def _check_smoother(ssm_scenario, particle_filter):
     _check_lg(ssm_scenario, particle_filter)
+    if isinstance(ssm_scenario, StochasticVolatility):
+        # the stitching kernels take the linear-Gaussian and non-linear benchmark transitions only
+        raise NotImplementedError("StochasticVolatility: no GPU smoothing kernel for this model")
     if not isinstance(particle_filter, BootstrapFilter):
         raise NotImplementedError("the online smoother runs the bootstrap filter")
 

@@ -31,3 +31,13 @@ def test_stochastic_volatility_constants():
     for k in ("phi", "bsig", "r2", "cB", "c0", "m0"):
         assert np.float32(p[k]) == np.float32(q[k]), k
     assert s.phi == np.float32(0.95)
+
+
+def test_sv_smoothing_is_refused():
+    """the online smoother and backward simulation have no stochastic-volatility transition
+    kernel: they refuse the model instead of running another model's arithmetic"""
+    import pytest
+    import mocat_gb300 as mg
+    ssm = mg.ssm.StochasticVolatility(dim=1)
+    with pytest.raises(NotImplementedError):
+        mg.ssm._check_smoother(ssm, mg.ssm.BootstrapFilter())
