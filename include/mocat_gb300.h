@@ -304,6 +304,20 @@ int mgb_transition_potential_pairs_nl1d(const mgb_nl1d_model *model_host, int64_
                                         const float *x1_dev, float t_previous, const float *lw_dev, float *out_dev,
                                         void *stream);
 
+/* Backward simulation and stitching with the stochastic-volatility transition (dim 1,
+ * stochastic_volatility.py:78-85): transition_potential(x0 -> x1) = 0.5 ((x1 - phi x0) pq sqrt(dt))^2,
+ * pq = transition_precision_sqrt (1 / sqrt(transition_covariance)), no normaliser (the reference's
+ * 2-D precision square root carries no det), dt = t_new - t_prev.  Key flows as the
+ * linear-Gaussian entries.  mgb_ffbsi_sv takes the T times on the HOST (t_host), step t using
+ * t_host[t + 1] - t_host[t]; x_hist, lw_hist (T, N) device; workspace mgb_ffbsi_workspace(N, T, 1). */
+int mgb_ffbsi_sv(float phi, float pq, int64_t T, int64_t N, int64_t M, const float *x_hist_dev,
+                 const float *lw_hist_dev, const float *t_host, const uint32_t *key_dev, float *out_dev,
+                 int32_t *idx_dev, void *ws_dev, size_t ws_bytes, void *stream);
+int mgb_stitch_sv(float phi, float pq, int64_t M0, int64_t M1, const float *x0_dev, const float *x1_dev,
+                  const float *lw1_dev, float dt, const uint32_t *key_dev, int32_t *idx_dev, void *stream);
+int mgb_transition_potential_pairs_sv(float phi, float pq, int64_t M, const float *x0_dev, const float *x1_dev,
+                                      float dt, const float *lw_dev, float *out_dev, void *stream);
+
 /* ------------------------------ backward simulation and stitching by rejection
  * maximum_rejections > 0: backward_simulation_rejection (mocat/src/ssm/backward.py:172-214,
  * rejection_resampling :54-169) and rejection_stitching (mocat/src/ssm/online_smoothing.py:59-175,
@@ -345,6 +359,14 @@ int mgb_stitch_rejection_nl1d(const mgb_nl1d_model *model_host, const mgb_reject
                               const float *x0_dev, const float *x1_dev, const float *lw1_dev, float t_previous,
                               const uint32_t *key_dev, int32_t *idx_dev, int64_t *evals_dev, void *ws_dev,
                               size_t ws_bytes, void *stream);
+int mgb_ffbsi_rejection_sv(float phi, float pq, const mgb_rejection_config *cfg_host, int64_t T, int64_t N,
+                           int64_t M, const float *x_hist_dev, const float *lw_hist_dev, const float *t_host,
+                           const uint32_t *key_dev, float *out_dev, int32_t *idx_dev, int64_t *evals_dev,
+                           void *ws_dev, size_t ws_bytes, void *stream);
+int mgb_stitch_rejection_sv(float phi, float pq, const mgb_rejection_config *cfg_host, int64_t M,
+                            const float *x0_dev, const float *x1_dev, const float *lw1_dev, float dt,
+                            const uint32_t *key_dev, int32_t *idx_dev, int64_t *evals_dev, void *ws_dev,
+                            size_t ws_bytes, void *stream);
 
 /* ------------------------------- many stochastic-volatility filters at once
  * B independent run_particle_filter_for_marginals calls (mocat/src/ssm/filtering.py:255-324)

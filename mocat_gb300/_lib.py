@@ -164,6 +164,13 @@ _SIGNATURES = {
                          ctypes.POINTER(PFOutputs), _P], _I32),
     "mgb_ffbsi_nl1d": ([ctypes.POINTER(NL1DModel), _I64, _I64, _I64, _P, _P, _P, _P, _P, _P, _P, _SZ, _P], _I32),
     "mgb_stitch_nl1d": ([ctypes.POINTER(NL1DModel), _I64, _I64, _P, _P, _P, _F, _P, _P, _P], _I32),
+    "mgb_ffbsi_sv": ([_F, _F, _I64, _I64, _I64, _P, _P, _P, _P, _P, _P, _P, _SZ, _P], _I32),
+    "mgb_stitch_sv": ([_F, _F, _I64, _I64, _P, _P, _P, _F, _P, _P, _P], _I32),
+    "mgb_transition_potential_pairs_sv": ([_F, _F, _I64, _P, _P, _F, _P, _P, _P], _I32),
+    "mgb_ffbsi_rejection_sv": ([_F, _F, ctypes.POINTER(RejectionConfig), _I64, _I64, _I64, _P, _P, _P, _P, _P, _P,
+                                _P, _P, _SZ, _P], _I32),
+    "mgb_stitch_rejection_sv": ([_F, _F, ctypes.POINTER(RejectionConfig), _I64, _P, _P, _P, _F, _P, _P, _P, _P, _SZ,
+                                 _P], _I32),
     "mgb_ffbsi_rejection_workspace": ([_I64, _I64, _I64, ctypes.c_int32], _SZ),
     "mgb_stitch_rejection_workspace": ([_I64, ctypes.c_int32], _SZ),
     "mgb_ffbsi_rejection_lg": ([ctypes.POINTER(LGTransition), ctypes.POINTER(RejectionConfig), _I64, _I64, _I64, _P,

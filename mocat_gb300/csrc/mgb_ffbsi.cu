@@ -1,6 +1,6 @@
 // Backward simulation (forward filtering, backward simulation) and particle
-// stitching: the full O(N M) versions, for a linear-Gaussian transition and for
-// the one-dimensional non-linear benchmark transition.
+// stitching: the full O(N M) versions, for a linear-Gaussian transition, the
+// one-dimensional non-linear benchmark transition and the stochastic-volatility one.
 //
 // Reference: backward_simulation_full (mocat/src/ssm/backward.py:217-245),
 // full_resampling / full_resample_single (:20-40):
@@ -22,6 +22,9 @@
 // i and i + ceil(N/2) come from the two halves of one cipher call.  The
 // argmax is reduced in the fixed order (value, then smaller index), so the
 // result does not depend on scheduling.
+#include <type_traits>
+#include <vector>
+
 #include "mgb_transition.cuh"
 
 namespace mgb {
@@ -164,7 +167,7 @@ static int pair_potential(const mgb_lg_transition *tr, int64_t M, const float *x
 template <class TP>
 static int ffbsi_run(TP p, const float *t_all, int64_t T, int64_t N, int64_t M, const float *x_hist,
                      const float *lw_hist, const uint32_t *key, float *out, int32_t *idx, void *ws, size_t ws_bytes,
-                     cudaStream_t s) {
+                     cudaStream_t s, const float *pqs_host = nullptr) {
   constexpr int D = TP::DIM;
   Carver c(ws);
   float *fx = c.take<float>((size_t)D * N);
@@ -181,6 +184,7 @@ static int ffbsi_run(TP p, const float *t_all, int64_t T, int64_t N, int64_t M, 
   if ((st = launch_status())) return st;
   for (int64_t t = T - 2; t >= 0; --t) {
     if constexpr (TP::kDrift) p.tp = t_all + t;
+    if constexpr (std::is_same<TP, SVT>::value) p.pqs = pqs_host[t];
     k_ffbsi_fx<TP><<<(unsigned)((N + FB_TPB - 1) / FB_TPB), FB_TPB, 0, s>>>(p, N, x_hist + (size_t)t * xs, fx);
     if ((st = launch_status())) return st;
     k_ffbsi_step<TP><<<(unsigned)M, FB_TPB, 0, s>>>(p, N, M, fx, lw_hist + (size_t)t * N,
@@ -283,6 +287,31 @@ int mgb_transition_potential_pairs_nl1d(const mgb_nl1d_model *m, int64_t M, cons
                                         float t_previous, const float *lw, float *out, void *stream) {
   if (!m || M < 1 || !x0 || !x1 || !out) return ERR_BAD_ARG;
   return pairs_run(pack_nlt(m, nullptr, t_previous), M, x0, x1, lw, out, (cudaStream_t)stream);
+}
+
+// stochastic volatility (dim 1): t_host the T times on the host; step t's potential scales
+// by sqrt(t_host[t + 1] - t_host[t])
+int mgb_ffbsi_sv(float phi, float pq, int64_t T, int64_t N, int64_t M, const float *x_hist, const float *lw_hist,
+                 const float *t_host, const uint32_t *key, float *out, int32_t *idx, void *ws, size_t ws_bytes,
+                 void *stream) {
+  if (!ffbsi_sizes_ok(T, N, M) || !x_hist || !lw_hist || !t_host || !key || !out || !idx || !ws) return ERR_BAD_ARG;
+  std::vector<float> pqs((size_t)T, pq);
+  for (int64_t t = 0; t + 1 < T; ++t) pqs[t] = pq * std::sqrt(t_host[t + 1] - t_host[t]);
+  return ffbsi_run(pack_svt(phi, pq, 1.0f), nullptr, T, N, M, x_hist, lw_hist, key, out, idx, ws, ws_bytes,
+                   (cudaStream_t)stream, pqs.data());
+}
+
+int mgb_stitch_sv(float phi, float pq, int64_t M0, int64_t M1, const float *x0, const float *x1, const float *lw1,
+                  float dt, const uint32_t *key, int32_t *idx, void *stream) {
+  if (M0 < 1 || M1 < 1 || M0 > 0x7FFFFFFFll || M1 > 0x7FFFFFFFll || !x0 || !x1 || !lw1 || !key || !idx)
+    return ERR_BAD_ARG;
+  return stitch_run(pack_svt(phi, pq, dt), M0, M1, x0, x1, lw1, key, idx, (cudaStream_t)stream);
+}
+
+int mgb_transition_potential_pairs_sv(float phi, float pq, int64_t M, const float *x0, const float *x1, float dt,
+                                      const float *lw, float *out, void *stream) {
+  if (M < 1 || !x0 || !x1 || !out) return ERR_BAD_ARG;
+  return pairs_run(pack_svt(phi, pq, dt), M, x0, x1, lw, out, (cudaStream_t)stream);
 }
 
 }  // extern "C"

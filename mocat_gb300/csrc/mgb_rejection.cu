@@ -1,6 +1,6 @@
 // Backward simulation and particle stitching by rejection sampling
-// (maximum_rejections > 0), for the linear-Gaussian and the non-linear 1-D
-// benchmark transitions.
+// (maximum_rejections > 0), for the linear-Gaussian, the non-linear 1-D
+// benchmark and the stochastic-volatility transitions.
 //
 // Reference: rejection_resampling (mocat/src/ssm/backward.py:54-169) driven by
 // backward_simulation_rejection (:172-214), and rejection_stitching
@@ -31,6 +31,9 @@
 // later launches return at once.  The host launches iterations in groups and
 // reads the flag between groups, so these entry points synchronise their
 // stream.
+#include <type_traits>
+#include <vector>
+
 #include "mgb_transition.cuh"
 
 namespace mgb {
@@ -307,7 +310,8 @@ static int rej_run(const TP &p, const RejCfg &cfg, int64_t n, int64_t Np, const 
 template <class TP>
 static int ffbsi_rej_run(TP p, const RejCfg &cfg, const float *t_all, int64_t T, int64_t N, int64_t M,
                          const float *x_hist, const float *lw_hist, const uint32_t *key, float *out, int32_t *idx,
-                         long long *evals, void *ws, size_t ws_bytes, cudaStream_t s) {
+                         long long *evals, void *ws, size_t ws_bytes, cudaStream_t s,
+                         const float *pqs_host = nullptr) {
   constexpr int D = TP::DIM;
   Carver c(ws);
   float *fx = c.take<float>((size_t)D * N);
@@ -326,6 +330,7 @@ static int ffbsi_rej_run(TP p, const RejCfg &cfg, const float *t_all, int64_t T,
   if ((st = launch_status())) return st;
   for (int64_t t = T - 2; t >= 0; --t) {
     if constexpr (TP::kDrift) p.tp = t_all + t;
+    if constexpr (std::is_same<TP, SVT>::value) p.pqs = pqs_host[t];
     k_ffbsi_fx<TP><<<(unsigned)((N + FB_TPB - 1) / FB_TPB), FB_TPB, 0, s>>>(p, N, x_hist + (size_t)t * xs, fx);
     if ((st = launch_status())) return st;
     st = rej_run<TP, true>(p, cfg, M, N, out + (size_t)(t + 1) * D * M, fx, lw_hist + (size_t)t * N, tkeys + 2 * t,
@@ -467,6 +472,29 @@ int mgb_stitch_rejection_nl1d(const mgb_nl1d_model *m, const mgb_rejection_confi
     return ERR_BAD_ARG;
   return stitch_rej_run(pack_nlt(m, nullptr, t_previous), rc, M, x0, x1, lw1, key, idx, (long long *)evals, ws,
                         ws_bytes, (cudaStream_t)stream);
+}
+
+int mgb_ffbsi_rejection_sv(float phi, float pq, const mgb_rejection_config *cfg, int64_t T, int64_t N, int64_t M,
+                           const float *x_hist, const float *lw_hist, const float *t_host, const uint32_t *key,
+                           float *out, int32_t *idx, int64_t *evals, void *ws, size_t ws_bytes, void *stream) {
+  RejCfg rc;
+  if (!rej_cfg_ok(cfg, rc) || !rej_sizes_ok(T, N, M) || !x_hist || !lw_hist || !t_host || !key || !out || !idx ||
+      !evals || !ws)
+    return ERR_BAD_ARG;
+  std::vector<float> pqs((size_t)T, pq);
+  for (int64_t t = 0; t + 1 < T; ++t) pqs[t] = pq * std::sqrt(t_host[t + 1] - t_host[t]);
+  return ffbsi_rej_run(pack_svt(phi, pq, 1.0f), rc, nullptr, T, N, M, x_hist, lw_hist, key, out, idx,
+                       (long long *)evals, ws, ws_bytes, (cudaStream_t)stream, pqs.data());
+}
+
+int mgb_stitch_rejection_sv(float phi, float pq, const mgb_rejection_config *cfg, int64_t M, const float *x0,
+                            const float *x1, const float *lw1, float dt, const uint32_t *key, int32_t *idx,
+                            int64_t *evals, void *ws, size_t ws_bytes, void *stream) {
+  RejCfg rc;
+  if (!rej_cfg_ok(cfg, rc) || !rej_sizes_ok(1, M, M) || !x0 || !x1 || !lw1 || !key || !idx || !evals || !ws)
+    return ERR_BAD_ARG;
+  return stitch_rej_run(pack_svt(phi, pq, dt), rc, M, x0, x1, lw1, key, idx, (long long *)evals, ws, ws_bytes,
+                        (cudaStream_t)stream);
 }
 
 }  // extern "C"

@@ -8,6 +8,8 @@
 // and the block-wide argmax (first maximum wins, NaN entries skipped) that turns
 // Gumbel draws plus log-weights into a categorical draw.
 #pragma once
+#include <cmath>
+
 #include "mgb_internal.cuh"
 #include "mgb_nl1d.cuh"
 
@@ -58,6 +60,33 @@ struct NLT {
   }
   __device__ __forceinline__ float potential(const float (&diff)[1]) const { return nl_gauss(diff[0], tsd, c); }
 };
+
+// stochastic-volatility transition, dim 1 (stochastic_volatility.py:78-85): mean = phi x0,
+// potential(diff) = 0.5 (diff pqs)^2 with pqs = transition_precision_sqrt sqrt(t_new - t_prev)
+// (the reference multiplies the precision square root by sqrt(dt)); a 2-D precision square
+// root gives no normaliser (gaussian_potential without det_prec, utils.py:67-79).  pqs is set
+// per launch by the host.
+struct SVT {
+  static constexpr int DIM = 1;
+  static constexpr bool kDrift = false;
+  float phi, pqs;
+  uint32_t one;
+  __device__ __forceinline__ void mean(const float (&x)[1], float (&m)[1], float) const {
+    m[0] = __fmul_rn(x[0], phi);
+  }
+  __device__ __forceinline__ float potential(const float (&diff)[1]) const {
+    const float v = __fmul_rn(diff[0], pqs);
+    return __fmul_rn(0.5f, __fmul_rn(v, v));
+  }
+};
+
+inline SVT pack_svt(float phi, float pq, float dt) {
+  SVT p;
+  p.phi = phi;
+  p.pqs = pq * std::sqrt(dt);
+  p.one = 1u;
+  return p;
+}
 
 // the policy's per-launch constant (8 cos(1.2 t_prev)), computed once per block
 // by thread 0; every thread of the block calls this

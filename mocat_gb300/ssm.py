@@ -186,6 +186,12 @@ class StochasticVolatility(StateSpaceModel):
             self.__dict__["_derived"] = (p, s)
         return self.__dict__["_derived"]
 
+    def transition_constants(self):
+        """(phi, pq) of the transition potential, float32: transition_matrix and
+        transition_precision_sqrt = inv(chol(transition_covariance)) (utils.py:247-262)"""
+        f = np.float32
+        return f(self.transition_matrix[0, 0]), f(f(1.0) / f(np.sqrt(f(self.transition_covariance[0, 0]))))
+
     def simulate(self, t_all, random_key):
         """StateSpaceModel.simulate (ssm.py:138-163) with this model's samplers
         (stochastic_volatility.py:71-108): x_0 = e c0 + m0, x_t = phi x_{t-1} + (e sqrt(Q))
@@ -651,9 +657,12 @@ def backward_simulation(ssm_scenario, marginal_particles, random_key, n_samps=No
     rejection sampling (backward_simulation_rejection :172-214).  Returns cdict(value
     (T, n_samps, d), t, num_transition_evals (T,), indices)."""
     nl = isinstance(ssm_scenario, NonLinear1DBenchmark)
-    if not nl and not isinstance(ssm_scenario, TimeHomogenousLinearGaussian):
+    sv = isinstance(ssm_scenario, StochasticVolatility)
+    if not nl and not sv and not isinstance(ssm_scenario, TimeHomogenousLinearGaussian):
         raise NotImplementedError(f"{ssm_scenario.__class__.__name__}: no backward-simulation kernel for this model")
-    if not ssm_scenario.gpu_supported():
+    if sv and ssm_scenario.dim != 1:
+        raise NotImplementedError("StochasticVolatility: the GPU kernels take dim = 1")
+    if not sv and not ssm_scenario.gpu_supported():
         raise NotImplementedError(f"d = {ssm_scenario.dim} not compiled")
     value = marginal_particles.value
     T, n, d = value.shape
@@ -665,16 +674,23 @@ def backward_simulation(ssm_scenario, marginal_particles, random_key, n_samps=No
     out = torch.empty((T, d, M), dtype=torch.float32, device=dev)
     idx = torch.empty((T, M), dtype=torch.int32, device=dev)
     tt = None
-    if nl:
+    if nl or sv:
         tt = _dev.as_f32(marginal_particles.t).reshape(-1).contiguous()
         if tt.numel() != T:
             raise ValueError(f"marginal_particles.t has {tt.numel()} entries for {T} steps")
+    if sv:
+        th = np.ascontiguousarray(tt.cpu().numpy(), np.float32)
+        phi, pq = ssm_scenario.transition_constants()
     if maximum_rejections > 0:
         cfg = _lib.RejectionConfig(int(maximum_rejections), float(transition_dens_bound_parameter),
                                    float(bound_inflation))
         ws = _dev.workspace(_lib.lib().mgb_ffbsi_rejection_workspace(n, M, T, d), dev)
         evals = torch.empty(T, dtype=torch.int64, device=dev)
-        if nl:
+        if sv:
+            call("mgb_ffbsi_rejection_sv", float(phi), float(pq), ctypes.byref(cfg), T, n, M, _dev.ptr(x),
+                 _dev.ptr(lw), th.ctypes.data, _dev.ptr(key), _dev.ptr(out), _dev.ptr(idx), _dev.ptr(evals),
+                 _dev.ptr(ws), ws.numel(), _dev.stream_ptr())
+        elif nl:
             call("mgb_ffbsi_rejection_nl1d", ctypes.byref(ssm_scenario.derived()[1]), ctypes.byref(cfg), T, n, M,
                  _dev.ptr(x), _dev.ptr(lw), _dev.ptr(tt), _dev.ptr(key), _dev.ptr(out), _dev.ptr(idx), _dev.ptr(evals),
                  _dev.ptr(ws), ws.numel(), _dev.stream_ptr())
@@ -685,7 +701,10 @@ def backward_simulation(ssm_scenario, marginal_particles, random_key, n_samps=No
                  _dev.stream_ptr())
         return cdict(value=out.permute(0, 2, 1), t=marginal_particles.t, num_transition_evals=evals, indices=idx)
     ws = _dev.workspace(_lib.lib().mgb_ffbsi_workspace(n, T, d), dev)
-    if nl:
+    if sv:
+        call("mgb_ffbsi_sv", float(phi), float(pq), T, n, M, _dev.ptr(x), _dev.ptr(lw), th.ctypes.data,
+             _dev.ptr(key), _dev.ptr(out), _dev.ptr(idx), _dev.ptr(ws), ws.numel(), _dev.stream_ptr())
+    elif nl:
         call("mgb_ffbsi_nl1d", ctypes.byref(ssm_scenario.derived()[1]), T, n, M, _dev.ptr(x), _dev.ptr(lw),
              _dev.ptr(tt), _dev.ptr(key), _dev.ptr(out), _dev.ptr(idx), _dev.ptr(ws), ws.numel(), _dev.stream_ptr())
     else:
@@ -712,13 +731,22 @@ def forward_filtering_backward_simulation(ssm_scenario, particle_filter, y, t, n
     return out
 
 
-def _pair_potential(ssm_scenario, x0, x1, lw=None, t_prev=0.0):
-    """lw_i + transition_potential(x0_i at t_prev -> x1_i) for particle-major (M, d) rows."""
+def _dt(t_prev, t_new):
+    return float(np.float32(float(t_new)) - np.float32(float(t_prev)))
+
+
+def _pair_potential(ssm_scenario, x0, x1, lw=None, t_prev=0.0, t_new=None):
+    """lw_i + transition_potential(x0_i at t_prev -> x1_i at t_new) for particle-major (M, d) rows."""
     x0t = _dev.as_f32(x0).t().contiguous()
     x1t = _dev.as_f32(x1).t().contiguous()
     M = x0t.shape[1]
     out = torch.empty(M, dtype=torch.float32, device=x0t.device)
     lwd = None if lw is None else _dev.as_f32(lw).reshape(-1).contiguous()
+    if isinstance(ssm_scenario, StochasticVolatility):
+        phi, pq = ssm_scenario.transition_constants()
+        call("mgb_transition_potential_pairs_sv", float(phi), float(pq), M, _dev.ptr(x0t), _dev.ptr(x1t),
+             _dt(t_prev, t_new), _dev.ptr(lwd), _dev.ptr(out), _dev.stream_ptr())
+        return out
     if isinstance(ssm_scenario, NonLinear1DBenchmark):
         call("mgb_transition_potential_pairs_nl1d", ctypes.byref(ssm_scenario.derived()[1]), M, _dev.ptr(x0t),
              _dev.ptr(x1t), float(t_prev), _dev.ptr(lwd), _dev.ptr(out), _dev.stream_ptr())
@@ -737,6 +765,11 @@ def full_stitch(ssm_scenario, x0_all, t, x1_all, tplus1, x1_log_weight, random_k
     M0, M1 = x0t.shape[1], x1t.shape[1]
     lw = _dev.as_f32(x1_log_weight).reshape(-1).contiguous()
     idx = torch.empty(M0, dtype=torch.int32, device=x0t.device)
+    if isinstance(ssm_scenario, StochasticVolatility):
+        phi, pq = ssm_scenario.transition_constants()
+        call("mgb_stitch_sv", float(phi), float(pq), M0, M1, _dev.ptr(x0t), _dev.ptr(x1t), _dev.ptr(lw),
+             _dt(t, tplus1), _dev.ptr(_dev.as_key(random_key)), _dev.ptr(idx), _dev.stream_ptr())
+        return idx
     if isinstance(ssm_scenario, NonLinear1DBenchmark):
         call("mgb_stitch_nl1d", ctypes.byref(ssm_scenario.derived()[1]), M0, M1, _dev.ptr(x0t), _dev.ptr(x1t),
              _dev.ptr(lw), float(t), _dev.ptr(_dev.as_key(random_key)), _dev.ptr(idx), _dev.stream_ptr())
@@ -764,7 +797,12 @@ def rejection_stitching(ssm_scenario, x0_all, t, x1_all, tplus1, x1_log_weight, 
     cfg = _lib.RejectionConfig(int(maximum_rejections), float(init_bound_param), float(bound_inflation))
     ws = _dev.workspace(_lib.lib().mgb_stitch_rejection_workspace(M, d), dev)
     key = _dev.as_key(random_key)
-    if isinstance(ssm_scenario, NonLinear1DBenchmark):
+    if isinstance(ssm_scenario, StochasticVolatility):
+        phi, pq = ssm_scenario.transition_constants()
+        call("mgb_stitch_rejection_sv", float(phi), float(pq), ctypes.byref(cfg), M, _dev.ptr(x0t), _dev.ptr(x1t),
+             _dev.ptr(lw), _dt(t, tplus1), _dev.ptr(key), _dev.ptr(idx), _dev.ptr(evals), _dev.ptr(ws), ws.numel(),
+             _dev.stream_ptr())
+    elif isinstance(ssm_scenario, NonLinear1DBenchmark):
         call("mgb_stitch_rejection_nl1d", ctypes.byref(ssm_scenario.derived()[1]), ctypes.byref(cfg), M,
              _dev.ptr(x0t), _dev.ptr(x1t), _dev.ptr(lw), float(t), _dev.ptr(key), _dev.ptr(idx), _dev.ptr(evals),
              _dev.ptr(ws), ws.numel(), _dev.stream_ptr())
@@ -782,7 +820,7 @@ def fixed_lag_stitching(ssm_scenario, early_block, t, recent_block, recent_block
     stitching for maximum_rejections = 0, rejection stitching otherwise."""
     x0_fixed_all = early_block[-1]
     x0_vary_all, x1_vary_all = recent_block[0], recent_block[1]
-    nilw = _pair_potential(ssm_scenario, x0_vary_all, x1_vary_all, recent_block_log_weight, t)
+    nilw = _pair_potential(ssm_scenario, x0_vary_all, x1_vary_all, recent_block_log_weight, t, tplus1)
     if maximum_rejections > 0:
         inds, evals = rejection_stitching(ssm_scenario, x0_fixed_all, t, x1_vary_all, tplus1, nilw, random_key,
                                           maximum_rejections, init_bound_param, bound_inflation)
@@ -793,9 +831,6 @@ def fixed_lag_stitching(ssm_scenario, early_block, t, recent_block, recent_block
 
 def _check_smoother(ssm_scenario, particle_filter):
     _check_lg(ssm_scenario, particle_filter)
-    if isinstance(ssm_scenario, StochasticVolatility):
-        # the stitching kernels take the linear-Gaussian and non-linear benchmark transitions only
-        raise NotImplementedError("StochasticVolatility: no GPU smoothing kernel for this model")
     if not isinstance(particle_filter, BootstrapFilter):
         raise NotImplementedError("the online smoother runs the bootstrap filter")
 

@@ -85,7 +85,8 @@ class _GKModel(ctypes.Structure):
 
 class _FFBSiModel(ctypes.Structure):
     _fields_ = [("d", ctypes.c_int), ("F", ctypes.c_void_p), ("Pq", ctypes.c_void_p), ("cq", ctypes.c_float),
-                ("nl", ctypes.c_int), ("tsd", ctypes.c_float), ("c", ctypes.c_float)]
+                ("nl", ctypes.c_int), ("tsd", ctypes.c_float), ("c", ctypes.c_float), ("phi", ctypes.c_float),
+                ("pq", ctypes.c_float)]
 
 
 def lib():
@@ -163,6 +164,13 @@ def lib():
         L.o_stitch_lg.argtypes = [ctypes.POINTER(_FFBSiModel), i64, i64, f32p, f32p, f32p, u32p, i32p]
         L.o_transition_potential_pairs.argtypes = [ctypes.POINTER(_FFBSiModel), i64, f32p, f32p, f32p]
         fl, i32 = ctypes.c_float, ctypes.c_int32
+        L.o_ffbsi_sv.argtypes = [fl, fl, i64, i64, i64, f32p, f32p, f32p, u32p, f32p, i32p]
+        L.o_stitch_sv.argtypes = [fl, fl, i64, i64, f32p, f32p, f32p, fl, u32p, i32p]
+        L.o_transition_potential_pairs_sv.argtypes = [fl, fl, i64, f32p, f32p, fl, f32p]
+        L.o_ffbsi_rejection_sv.argtypes = [fl, fl, i64, i64, i64, f32p, f32p, f32p, u32p, i32, fl, fl, f32p, i32p,
+                                           i64p]
+        L.o_stitch_rejection_sv.argtypes = [fl, fl, i64, f32p, f32p, f32p, fl, u32p, i32, fl, fl, i32p]
+        L.o_stitch_rejection_sv.restype = i64
         L.o_ffbsi_rejection_lg.argtypes = [ctypes.POINTER(_FFBSiModel), i64, i64, i64, f32p, f32p, u32p, i32, fl, fl,
                                            f32p, i32p, i64p]
         L.o_ffbsi_rejection_nl1d.argtypes = [ctypes.POINTER(_NLModel), i64, i64, i64, f32p, f32p, f32p, u32p, i32, fl,
@@ -727,6 +735,45 @@ def stitch_rejection_nl1d(params, x0, x1, lw1, t_prev, key, maximum_rejections, 
                                        float(np.float32(t_prev)), _u32(key), int(maximum_rejections),
                                        float(np.float32(init_bound_param)), float(np.float32(bound_inflation)), idx)
     return idx, int(ev)
+
+
+def ffbsi_sv(phi, pq, x_hist, lw_hist, t, key, M, maximum_rejections=0, init_bound_param=0.0, bound_inflation=1.01):
+    """backward_simulation on StochasticVolatility (dim 1): x_hist, lw_hist (T, N), t (T,) -> (samples
+    (T, M), indices (T, M)[, evals (T,) for maximum_rejections > 0])."""
+    x_hist, lw_hist, t = _f32(x_hist), _f32(lw_hist), _f32(t).reshape(-1)
+    T, N = lw_hist.shape
+    out = np.empty((T, M), np.float32)
+    idx = np.empty((T, M), np.int32)
+    if maximum_rejections > 0:
+        ev = np.empty(T, np.int64)
+        lib().o_ffbsi_rejection_sv(float(phi), float(pq), T, N, M, x_hist.reshape(-1), lw_hist.reshape(-1), t,
+                                   _u32(key), int(maximum_rejections), float(np.float32(init_bound_param)),
+                                   float(np.float32(bound_inflation)), out.reshape(-1), idx.reshape(-1), ev)
+        return out, idx, ev
+    lib().o_ffbsi_sv(float(phi), float(pq), T, N, M, x_hist.reshape(-1), lw_hist.reshape(-1), t, _u32(key),
+                     out.reshape(-1), idx.reshape(-1))
+    return out, idx
+
+
+def stitch_sv(phi, pq, x0, x1, lw1, dt, key, maximum_rejections=0, init_bound_param=0.0, bound_inflation=1.01):
+    """full_stitch / rejection_stitching on StochasticVolatility: x0 (M0,), x1 (M1,) -> indices
+    [(, evals) for maximum_rejections > 0]"""
+    x0, x1, lw1 = _f32(x0).reshape(-1), _f32(x1).reshape(-1), _f32(lw1).reshape(-1)
+    idx = np.empty(x0.size, np.int32)
+    if maximum_rejections > 0:
+        ev = lib().o_stitch_rejection_sv(float(phi), float(pq), x0.size, x0, x1, lw1, float(np.float32(dt)),
+                                         _u32(key), int(maximum_rejections), float(np.float32(init_bound_param)),
+                                         float(np.float32(bound_inflation)), idx)
+        return idx, int(ev)
+    lib().o_stitch_sv(float(phi), float(pq), x0.size, x1.size, x0, x1, lw1, float(np.float32(dt)), _u32(key), idx)
+    return idx
+
+
+def transition_potential_pairs_sv(phi, pq, x0, x1, dt):
+    x0, x1 = _f32(x0).reshape(-1), _f32(x1).reshape(-1)
+    out = np.empty(x0.size, np.float32)
+    lib().o_transition_potential_pairs_sv(float(phi), float(pq), x0.size, x0, x1, float(np.float32(dt)), out)
+    return out
 
 
 def num_threads():

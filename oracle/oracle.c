@@ -788,8 +788,9 @@ typedef struct {
     const float *F;    /* d x d transition_matrix */
     const float *Pq;   /* d x d transition_precision_sqrt */
     float cq;          /* (d log 2pi - log transition_precision_det) / 2 */
-    int nl;            /* 1: the non-linear benchmark transition (d = 1, F and Pq unused) */
-    float tsd, c;      /* its transition_sd and log(2 pi) / 2 */
+    int nl;            /* 1: the non-linear benchmark transition, 2: stochastic volatility (d = 1, F and Pq unused) */
+    float tsd, c;      /* the non-linear model's transition_sd and log(2 pi) / 2 */
+    float phi, pq;     /* stochastic volatility: transition_matrix, transition_precision_sqrt */
 } o_ffbsi_model;
 
 /* transition_potential(x0 -> x1):
@@ -799,6 +800,12 @@ typedef struct {
  *                    (nonlinear1d.py:48-54). */
 static inline float o_transition_potential(const o_ffbsi_model *md, const float *x0, const float *x1, float drift)
 {
+    if (md->nl == 2) {
+        /* stochastic volatility (stochastic_volatility.py:78-85): drift carries pq sqrt(dt);
+         * 0.5 ((x1 - x0 phi) pq sqrt(dt))^2, no normaliser */
+        const float v = (x1[0] - x0[0] * md->phi) * drift;
+        return 0.5f * (v * v);
+    }
     if (md->nl) {
         float z = (x1[0] - o_nl_mean(x0[0], drift)) / md->tsd;
         return 0.5f * (z * z) + md->c;
@@ -837,7 +844,8 @@ static void o_ffbsi(const o_ffbsi_model *md, int64_t T, int64_t N, int64_t M, co
     uint32_t *skeys = (uint32_t *)malloc(sizeof(uint32_t) * 2 * (size_t)M);
     for (int64_t t = T - 2; t >= 0; --t) {
         o_split(tkeys + 2 * t, M, skeys);
-        const float drift = md->nl ? o_nl_drift(t_all[t]) : 0.0f;
+        const float drift = md->nl == 1 ? o_nl_drift(t_all[t])
+                            : md->nl == 2 ? md->pq * sqrtf(t_all[t + 1] - t_all[t]) : 0.0f;
         const float *xt = x_hist + t * N * d;
         const float *lw = lw_hist + t * N;
 #pragma omp parallel for schedule(static)
@@ -916,6 +924,36 @@ void o_stitch_nl1d(const o_nl_model *nm, int64_t M0, int64_t M1, const float *x0
 {
     o_ffbsi_model md = o_nl_transition(nm);
     o_stitch(&md, M0, M1, x0, x1, lw1, o_nl_drift(t_prev), key, idx);
+}
+
+/* the stochastic-volatility transition (d = 1): t_all the T times; stitching and pair
+ * potentials take dt = t_new - t_prev */
+static o_ffbsi_model o_sv_transition(float phi, float pq)
+{
+    o_ffbsi_model md = {1, NULL, NULL, 0.0f, 2, 0.0f, 0.0f, phi, pq};
+    return md;
+}
+
+void o_ffbsi_sv(float phi, float pq, int64_t T, int64_t N, int64_t M, const float *x_hist, const float *lw_hist,
+                const float *t_all, const uint32_t *key, float *out, int32_t *idx)
+{
+    o_ffbsi_model md = o_sv_transition(phi, pq);
+    o_ffbsi(&md, T, N, M, x_hist, lw_hist, t_all, key, out, idx);
+}
+
+void o_stitch_sv(float phi, float pq, int64_t M0, int64_t M1, const float *x0, const float *x1, const float *lw1,
+                 float dt, const uint32_t *key, int32_t *idx)
+{
+    o_ffbsi_model md = o_sv_transition(phi, pq);
+    o_stitch(&md, M0, M1, x0, x1, lw1, pq * sqrtf(dt), key, idx);
+}
+
+void o_transition_potential_pairs_sv(float phi, float pq, int64_t M, const float *x0, const float *x1, float dt,
+                                     float *out)
+{
+    o_ffbsi_model md = o_sv_transition(phi, pq);
+    const float pqs = pq * sqrtf(dt);
+    for (int64_t i = 0; i < M; ++i) out[i] = o_transition_potential(&md, x0 + i, x1 + i, pqs);
 }
 
 /* transition_potential(x0_i -> x1_i) for each i (vmap over pairs) */
@@ -1059,7 +1097,8 @@ static void o_ffbsi_rejection(const o_ffbsi_model *md, int64_t T, int64_t N, int
         memcpy(out + ((T - 1) * M + j) * d, x_hist + ((T - 1) * N + idx[(T - 1) * M + j]) * d, sizeof(float) * d);
     evals[0] = 0;
     for (int64_t t = T - 2; t >= 0; --t) {
-        const float drift = md->nl ? o_nl_drift(t_all[t]) : 0.0f;
+        const float drift = md->nl == 1 ? o_nl_drift(t_all[t])
+                            : md->nl == 2 ? md->pq * sqrtf(t_all[t + 1] - t_all[t]) : 0.0f;
         evals[t + 1] = o_rejection(md, 1, M, N, out + (t + 1) * M * d, x_hist + t * N * d, lw_hist + t * N, drift,
                                    tkeys + 2 * t, max_rej, ibp, infl, idx + t * M);
         for (int64_t j = 0; j < M; ++j)
@@ -1088,6 +1127,21 @@ int64_t o_stitch_rejection_lg(const o_ffbsi_model *md, int64_t M, const float *x
                               const uint32_t *key, int32_t max_rej, float ibp, float infl, int32_t *idx)
 {
     return o_rejection(md, 0, M, M, x0, x1, lw1, 0.0f, key, max_rej, ibp, infl, idx);
+}
+
+void o_ffbsi_rejection_sv(float phi, float pq, int64_t T, int64_t N, int64_t M, const float *x_hist,
+                          const float *lw_hist, const float *t_all, const uint32_t *key, int32_t max_rej, float ibp,
+                          float infl, float *out, int32_t *idx, int64_t *evals)
+{
+    o_ffbsi_model md = o_sv_transition(phi, pq);
+    o_ffbsi_rejection(&md, T, N, M, x_hist, lw_hist, t_all, key, max_rej, ibp, infl, out, idx, evals);
+}
+
+int64_t o_stitch_rejection_sv(float phi, float pq, int64_t M, const float *x0, const float *x1, const float *lw1,
+                              float dt, const uint32_t *key, int32_t max_rej, float ibp, float infl, int32_t *idx)
+{
+    o_ffbsi_model md = o_sv_transition(phi, pq);
+    return o_rejection(&md, 0, M, M, x0, x1, lw1, pq * sqrtf(dt), key, max_rej, ibp, infl, idx);
 }
 
 int64_t o_stitch_rejection_nl1d(const o_nl_model *nm, int64_t M, const float *x0, const float *x1, const float *lw1,

@@ -33,11 +33,14 @@ def test_stochastic_volatility_constants():
     assert s.phi == np.float32(0.95)
 
 
-def test_sv_smoothing_is_refused():
-    """the online smoother and backward simulation have no stochastic-volatility transition
-    kernel: they refuse the model instead of running another model's arithmetic"""
+def test_sv_smoothing_checks():
+    """the online smoother takes the stochastic-volatility model with the bootstrap filter
+    and refuses other filters"""
     import pytest
     import mocat_gb300 as mg
     ssm = mg.ssm.StochasticVolatility(dim=1)
+    mg.ssm._check_smoother(ssm, mg.ssm.BootstrapFilter())
     with pytest.raises(NotImplementedError):
-        mg.ssm._check_smoother(ssm, mg.ssm.BootstrapFilter())
+        mg.ssm._check_smoother(ssm, mg.ssm.OptimalNonLinearGaussianParticleFilter())
+    phi, pq = ssm.transition_constants()
+    assert phi == 1.0 and pq == 1.0
