@@ -9,8 +9,8 @@
 Differences from the reference, by design:
   * resampling (ess < ess_threshold_resample n) is systematic, O(n), instead of
     random.categorical;
-  * the output keeps the final particles and per-iteration scalars (threshold,
-    ess, alpha, resampled) rather than the stacked (iterations, n, d) chain;
+  * run() returns the reference's stacked chain for value, log_weight and distance;
+    run_batched keeps the final particles of every posterior (chain=True adds the chain);
   * the stepsize variance and the mean acceptance are float64 sums in a fixed
     order.
 """
@@ -298,11 +298,30 @@ class BatchedABCSMC:
     def done(self):
         return not bool(self._tensor("active", (self.B,), torch.int32).any())
 
-    def run(self):
+    def run(self, chain=False):
+        """to termination; chain=True also records value, log_weight, distance after the startup and
+        every iteration (the reference's stacked chain), as result().chain_*"""
+        self._chain = {k: [] for k in ('value', 'log_weight', 'distance')} if chain else None
         self.init()
+        if chain:
+            self._snap()
         while not self.done() and self.iterations < self.cfg.max_iter:
             self.step()
-        return self.result()
+            if chain:
+                self._snap()
+        out = self.result()
+        if chain:
+            for k, v in self._chain.items():
+                out.__dict__["chain_" + k] = torch.stack(v)
+        return out
+
+    def _d(self):
+        return self.scenario.dim
+
+    def _snap(self):
+        self._chain["value"].append(self._tensor("value", (self.B, self.n, self._d()), torch.float32).clone())
+        self._chain["log_weight"].append(self._tensor("log_weight", (self.B, self.n), torch.float32).clone())
+        self._chain["distance"].append(self._tensor("distance", (self.B, self.n), torch.float32).clone())
 
     def result(self):
         B, n, d, H = self.B, self.n, self.scenario.dim, self.views.hist_len
@@ -320,19 +339,22 @@ class BatchedABCSMC:
                      iterations=it)
 
 
-def run_batched(scenario, sampler, n, random_keys):
+def run_batched(scenario, sampler, n, random_keys, chain=False):
     """mocat.run(scenario, sampler, n, key) for each of B keys, in one batch.  Per-iteration
-    arrays are padded past each posterior's last iteration."""
-    return BatchedABCSMC(scenario, sampler, n, random_keys).run()
+    arrays are padded past each posterior's last iteration; chain=True adds chain_value
+    (L, B, n, d), chain_log_weight and chain_distance (L, B, n)."""
+    return BatchedABCSMC(scenario, sampler, n, random_keys).run(chain)
 
 
 def run(scenario, sampler, n, random_key):
-    """mocat.run (sample.py:110-148) for MetropolisedABCSMCSampler or VanillaABC on an ABC scenario."""
+    """mocat.run (sample.py:110-148) for MetropolisedABCSMCSampler or VanillaABC on an ABC scenario.
+    ABC-SMC returns the reference's stacked layout: value (L, n, d), log_weight and distance
+    (L, n) after the startup and every iteration, threshold, ess, alpha, resampled (L,)."""
     if isinstance(sampler, VanillaABC):
         return _run_vanilla(scenario, sampler, n, random_key)
-    out = run_batched(scenario, sampler, n, _dev.as_key(random_key).reshape(1, 2))
+    out = run_batched(scenario, sampler, n, _dev.as_key(random_key).reshape(1, 2), chain=True)
     L = int(out.iterations[0]) + 1
-    return cdict(value=out.value[0], log_weight=out.log_weight[0], distance=out.distance[0],
-                 prior_potential=out.prior_potential[0], stepsize=out.stepsize[0], threshold=out.threshold[0, :L],
-                 ess=out.ess[0, :L], alpha=out.alpha[0, :L], resampled=out.resampled[0, :L],
-                 iterations=int(out.iterations[0]))
+    return cdict(value=out.chain_value[:L, 0], log_weight=out.chain_log_weight[:L, 0],
+                 distance=out.chain_distance[:L, 0], prior_potential=out.prior_potential[0],
+                 stepsize=out.stepsize[0], threshold=out.threshold[0, :L], ess=out.ess[0, :L], alpha=out.alpha[0, :L],
+                 resampled=out.resampled[0, :L], iterations=int(out.iterations[0]))

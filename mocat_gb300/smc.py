@@ -14,9 +14,8 @@ at once, on Bayesian logistic regression or the Gaussian toy scenario.
 Differences from the reference, by design:
   * resampling (ess <= ess_threshold_resample n) is systematic, O(n), instead of
     random.categorical;
-  * the output keeps the final particles and per-iteration scalars
-    (temperature, log_norm_constant, ess, alpha, resampled) rather than the
-    stacked (iterations, n, d) chain;
+  * run() returns the reference's stacked chain for value and log_weight; run_batched
+    keeps the final particles of every posterior (chain=True adds the stacked chain);
   * ``precision="bf16"`` evaluates the likelihood potential and its gradient on
     the tensor cores (bf16 operands, float32 accumulation); "fp32" on the CUDA cores.
 """
@@ -257,11 +256,29 @@ class BatchedSMC:
     def done(self):
         return not bool(self._tensor("active", (self.B,), torch.int32).any())
 
-    def run(self):
+    def run(self, chain=False):
+        """to termination; chain=True also records value, log_weight after the startup and
+        every iteration (the reference's stacked chain), as result().chain_*"""
+        self._chain = {k: [] for k in ('value', 'log_weight')} if chain else None
         self.init()
+        if chain:
+            self._snap()
         while not self.done() and self.iterations < self.cfg.max_iter:
             self.step()
-        return self.result()
+            if chain:
+                self._snap()
+        out = self.result()
+        if chain:
+            for k, v in self._chain.items():
+                out.__dict__["chain_" + k] = torch.stack(v)
+        return out
+
+    def _d(self):
+        return self.cfg.d
+
+    def _snap(self):
+        self._chain["value"].append(self._tensor("value", (self.B, self.n, self._d()), torch.float32).clone())
+        self._chain["log_weight"].append(self._tensor("log_weight", (self.B, self.n), torch.float32).clone())
 
     def prior_scale_grad(self):
         """(B,) d log Z / d prior_scale at the current particles (Fisher identity)."""
@@ -285,21 +302,24 @@ class BatchedSMC:
                      iterations=it, grad_log_norm_constant_prior_scale=self.prior_scale_grad())
 
 
-def run_batched(scenario, sampler, n, random_keys, precision="fp32", temperature_schedule=None):
+def run_batched(scenario, sampler, n, random_keys, precision="fp32", temperature_schedule=None, chain=False):
     """mocat.run(scenario, sampler, n, key) for each of B keys, in one batch.  Fields carry a
     leading B axis; per-iteration arrays are padded past each posterior's last iteration.
-    temperature_schedule (a run() keyword in the reference) sets the sampler's schedule."""
+    temperature_schedule (a run() keyword in the reference) sets the sampler's schedule;
+    chain=True adds chain_value (L, B, n, d) and chain_log_weight (L, B, n)."""
     if temperature_schedule is not None:
         sampler.set_schedule(temperature_schedule)
-    return BatchedSMC(scenario, sampler, n, random_keys, precision).run()
+    return BatchedSMC(scenario, sampler, n, random_keys, precision).run(chain)
 
 
 def run(scenario, sampler, n, random_key, precision="fp32", temperature_schedule=None):
     """mocat.run (sample.py:110-148) for MetropolisedSMCSampler on a LogisticRegression or
-    Gaussian scenario.  temperature: the per-iteration temperatures (entry 0 after startup)."""
-    out = run_batched(scenario, sampler, n, _dev.as_key(random_key).reshape(1, 2), precision, temperature_schedule)
+    Gaussian scenario, with the reference's stacked layout: value (L, n, d) and log_weight (L, n)
+    after the startup and every iteration, temperature, log_norm_constant, ess, alpha (L,)."""
+    out = run_batched(scenario, sampler, n, _dev.as_key(random_key).reshape(1, 2), precision, temperature_schedule,
+                      chain=True)
     L = int(out.iterations[0]) + 1
-    return cdict(value=out.value[0], log_weight=out.log_weight[0],
+    return cdict(value=out.chain_value[:L, 0], log_weight=out.chain_log_weight[:L, 0],
                  likelihood_potential=out.likelihood_potential[0], temperature=out.temperature[0, :L],
                  log_norm_constant=out.log_norm_constant[0, :L], ess=out.ess[0, :L], alpha=out.alpha[0, :L],
                  resampled=out.resampled[0, :L])

@@ -75,7 +75,8 @@ def test_reference_statistical_check(cuda, mode):
         smp = mg.abc.MetropolisedABCSMCSampler(threshold_schedule=np.linspace(10, 0.1, 10))
     out = mg.abc.run(sc, smp, 1000, mg.random.PRNGKey(0))
     pm, pc = posterior()
-    x = out.value.double().cpu().numpy()
+    assert out.value.shape == (out.iterations + 1, 1000, 3)
+    x = out.value[-1].double().cpu().numpy()
     assert np.abs(pm - x.mean(0)).sum() < 3.0
     assert np.abs(pc - np.cov(x.T)).sum() < 3.0
     assert out.threshold.shape[0] == out.iterations + 1

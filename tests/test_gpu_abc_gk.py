@@ -74,4 +74,4 @@ def test_reference_check(cuda, onlyA, mode):
     else:
         smp = mg.abc.MetropolisedABCSMCSampler(ess_threshold_retain=0.8, termination_alpha=0.1)
     out = mg.abc.run(sc, smp, 1000, mg.random.PRNGKey(0))
-    assert np.abs(true_u - out.value.double().cpu().numpy().mean(0)).sum() < 3.0
+    assert np.abs(true_u - out.value[-1].double().cpu().numpy().mean(0)).sum() < 3.0

@@ -81,7 +81,8 @@ def test_single_posterior_run(cuda):
     sampler = mg.smc.MetropolisedSMCSampler(mg.smc.Underdamped(stepsize=0.05), mcmc_steps=2)
     out = mg.smc.run(sc, sampler, 512, O.PRNGKey(7))
     assert float(out.temperature[-1]) == 1.0
-    assert out.value.shape == (512, 5)
+    L = out.temperature.shape[0]
+    assert out.value.shape == (L, 512, 5) and out.log_weight.shape == (L, 512)
     assert np.isfinite(out.log_norm_constant.cpu().numpy()).all()
 
 
@@ -209,9 +210,9 @@ def test_reference_transport_checks(cuda, move, schedule):
     n = 10000
     out = mg.smc.run(sc, mg.smc.MetropolisedSMCSampler(mv), n, mg.random.PRNGKey(0),
                      temperature_schedule=pre if schedule else None)
-    lw = out.log_weight.cpu().numpy()
+    lw = out.log_weight[-1].cpu().numpy()
     idx = O.resample_gumbel(lw, O.PRNGKey(1), n)
-    x = out.value.cpu().numpy()[idx].astype(np.float64)
+    x = out.value[-1].cpu().numpy()[idx].astype(np.float64)
     post = np.linalg.inv(np.linalg.inv(COV) + np.eye(2) / 49.0)
     np.testing.assert_array_almost_equal(x.mean(0), np.zeros(2), decimal=0)
     np.testing.assert_array_almost_equal(np.cov(x.T), post, decimal=1)
