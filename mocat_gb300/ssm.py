@@ -650,6 +650,17 @@ def _transition_struct(ssm_scenario):
     return ssm_scenario.__dict__["_transition"]
 
 
+def _bsim_output(marginal_particles, out, evals, idx):
+    """backward.py:207-214 / :240-245: a copy of the filter output with the value replaced by the
+    backward trajectories, num_transition_evals added and log_weight removed (the sampled
+    indices are kept as well)"""
+    res = cdict(**{k: v for k, v in marginal_particles.__dict__.items() if k != "log_weight"})
+    res.value = out.permute(0, 2, 1)
+    res.num_transition_evals = evals
+    res.indices = idx
+    return res
+
+
 def backward_simulation(ssm_scenario, marginal_particles, random_key, n_samps=None, maximum_rejections=0,
                         transition_dens_bound_parameter=0.0, bound_inflation=1.01):
     """backward.py:248-270: n_samps trajectories drawn backwards through the filter's particles,
@@ -699,7 +710,7 @@ def backward_simulation(ssm_scenario, marginal_particles, random_key, n_samps=No
             call("mgb_ffbsi_rejection_lg", ctypes.byref(s), ctypes.byref(cfg), T, n, M, _dev.ptr(x), _dev.ptr(lw),
                  _dev.ptr(key), _dev.ptr(out), _dev.ptr(idx), _dev.ptr(evals), _dev.ptr(ws), ws.numel(),
                  _dev.stream_ptr())
-        return cdict(value=out.permute(0, 2, 1), t=marginal_particles.t, num_transition_evals=evals, indices=idx)
+        return _bsim_output(marginal_particles, out, evals, idx)
     ws = _dev.workspace(_lib.lib().mgb_ffbsi_workspace(n, T, d), dev)
     if sv:
         call("mgb_ffbsi_sv", float(phi), float(pq), T, n, M, _dev.ptr(x), _dev.ptr(lw), th.ctypes.data,
@@ -713,7 +724,7 @@ def backward_simulation(ssm_scenario, marginal_particles, random_key, n_samps=No
              _dev.ptr(idx), _dev.ptr(ws), ws.numel(), _dev.stream_ptr())
     evals = torch.full((T,), float(n * M), device=dev)
     evals[0] = 0.0
-    return cdict(value=out.permute(0, 2, 1), t=marginal_particles.t, num_transition_evals=evals, indices=idx)
+    return _bsim_output(marginal_particles, out, evals, idx)
 
 
 def forward_filtering_backward_simulation(ssm_scenario, particle_filter, y, t, n_samps, random_key, n_pf=None,
