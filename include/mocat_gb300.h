@@ -661,6 +661,14 @@ int mgb_abc_gk_simulate(const mgb_abc_gk_model *model_host, int64_t P, const flo
  * threshold else -inf.  acceptance_rate >= 0 replaces the threshold by
  * jnp.quantile(distance, acceptance_rate) (clean_chain_ar); threshold_out (device, 1 float)
  * receives the threshold used.  x (n, d), pp, dist, lw (n) device outputs. */
+/* RandomWalkABC run as an MCMC sampler (abc/mcmc.py:16-100 with the Metropolis correction,
+ * mocat.run): B independent chains (keys_dev (B, 2)) of n states each with a fixed stepsize and
+ * threshold: x' = x + sqrt(stepsize) normal, accepted with probability
+ * min(1, exp(pp - pp') [dist' < threshold]).  x (B, n, d), dist, pp, alpha (B, n) device
+ * outputs; one thread per chain (the chain is serial). */
+int mgb_abc_mcmc_lg(const mgb_abc_lg_model *model_host, int64_t B, int64_t n, const uint32_t *keys_dev, float stepsize,
+                    float threshold, float *x_dev, float *distance_dev, float *prior_potential_dev, float *alpha_dev,
+                    void *stream);
 size_t mgb_abc_vanilla_workspace(int64_t n);
 int mgb_abc_vanilla_lg(const mgb_abc_lg_model *model_host, int64_t n, const uint32_t *key_dev, float threshold,
                        float acceptance_rate, void *ws_dev, size_t ws_bytes, float *x_dev, float *prior_potential_dev,

@@ -346,12 +346,36 @@ def run_batched(scenario, sampler, n, random_keys, chain=False):
     return BatchedABCSMC(scenario, sampler, n, random_keys).run(chain)
 
 
+def run_chains(scenario, sampler, n, random_keys):
+    """RandomWalkABC(stepsize, threshold) run as an MCMC sampler (abc/mcmc.py:16-100, mocat.run) for
+    B independent chains, one per key: value (B, n, d), distance, prior_potential, alpha (B, n).
+    Fixed stepsize and threshold (the Metropolis correction)."""
+    if not isinstance(scenario, LinearGaussian):
+        raise NotImplementedError(f"{scenario.__class__.__name__}: no GPU ABC-MCMC kernel for this scenario")
+    if (scenario.dim, scenario.dim_obs) not in SUPPORTED:
+        raise NotImplementedError(f"(d, dy) = ({scenario.dim}, {scenario.dim_obs}) not compiled")
+    if sampler.stepsize is None or sampler.threshold is None:
+        raise NotImplementedError("RandomWalkABC chains need a fixed stepsize and threshold")
+    keys = _dev.as_key(random_keys).reshape(-1, 2).contiguous()
+    B, d, dev = keys.shape[0], scenario.dim, keys.device
+    x = torch.empty((B, n, d), dtype=torch.float32, device=dev)
+    dist, pp, al = (torch.empty((B, n), dtype=torch.float32, device=dev) for _ in range(3))
+    _keep, model = scenario.derived()
+    call("mgb_abc_mcmc_lg", ctypes.byref(model), B, n, _dev.ptr(keys), float(sampler.stepsize),
+         float(sampler.threshold), _dev.ptr(x), _dev.ptr(dist), _dev.ptr(pp), _dev.ptr(al), _dev.stream_ptr())
+    return cdict(value=x, distance=dist, prior_potential=pp, alpha=al)
+
+
 def run(scenario, sampler, n, random_key):
-    """mocat.run (sample.py:110-148) for MetropolisedABCSMCSampler or VanillaABC on an ABC scenario.
+    """mocat.run (sample.py:110-148) for MetropolisedABCSMCSampler, VanillaABC or RandomWalkABC (an MCMC
+    chain) on an ABC scenario.
     ABC-SMC returns the reference's stacked layout: value (L, n, d), log_weight and distance
     (L, n) after the startup and every iteration, threshold, ess, alpha, resampled (L,)."""
     if isinstance(sampler, VanillaABC):
         return _run_vanilla(scenario, sampler, n, random_key)
+    if isinstance(sampler, RandomWalkABC):
+        out = run_chains(scenario, sampler, n, _dev.as_key(random_key).reshape(1, 2))
+        return cdict(**{k: v[0] for k, v in out.__dict__.items()})
     out = run_batched(scenario, sampler, n, _dev.as_key(random_key).reshape(1, 2), chain=True)
     L = int(out.iterations[0]) + 1
     return cdict(value=out.chain_value[:L, 0], log_weight=out.chain_log_weight[:L, 0],

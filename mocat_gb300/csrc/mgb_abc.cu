@@ -1024,6 +1024,96 @@ static int vabc_gk(const mgb_abc_gk_model *m, int64_t n, const uint32_t *key, fl
   return launch_status();
 }
 
+// --------------------------------------------------------- RandomWalkABC chains
+// mocat.run(scenario, RandomWalkABC(stepsize, threshold), n, key) (abc/mcmc.py:16-100,
+// mcmc/sampler.py:32-110, metropolis.py:48-70) with a fixed stepsize and threshold, one chain
+// per key:
+//   startup   (K, s) = split(K): x_0 = prior_sample(s); (K, _) = split(K) (prior potential);
+//             (K, k) = split(K): simulation of x_0 with k; alpha_0 = 1
+//   step      (K, _) = split(K) (always); (K, k1, k2, k3) = split(K, 4);
+//             x' = x + sqrt(stepsize) normal(k1, (d,)), simulation with k3;
+//             alpha = min(1, exp(pp - pp') [dist' < threshold]) (NaN -> 0);
+//             (K, ku) = split(K); accept if uniform(ku) < alpha
+// The chain is serial: one thread per chain writes its n states.
+template <int D, int DY>
+__global__ void __launch_bounds__(128) k_abc_mcmc_lg(const __grid_constant__ ABCP<D, DY> p, int64_t B, int64_t n,
+                                                      const uint32_t *keys, float stepsize, float thr,
+                                                      float *__restrict__ x_out, float *__restrict__ dist_out,
+                                                      float *__restrict__ pp_out, float *__restrict__ alpha_out) {
+  const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  uint32_t K0 = keys[2 * b], K1 = keys[2 * b + 1], a0, a1, t0, t1;
+  split_at(K0, K1, 2, 1, a0, a1);
+  split_at(K0, K1, 2, 0, t0, t1);
+  split_at(t0, t1, 2, 0, K0, K1);  // prior potential
+  uint32_t bits[D];
+  bits_vec<D>(a0, a1, bits, p.one);
+  float e[D], x[D];
+#pragma unroll
+  for (int j = 0; j < D; ++j) e[j] = bits_to_normal(bits[j]);
+#pragma unroll
+  for (int r = 0; r < D; ++r) {
+    float v = __fmul_rn(p.C0[r * D], e[0]);
+#pragma unroll
+    for (int k = 1; k < D; ++k) v = __fmaf_rn(p.C0[r * D + k], e[k], v);
+    x[r] = __fadd_rn(p.m0[r], v);
+  }
+  float pp = abc_prior_potential<D, DY>(p, x);
+  split_at(K0, K1, 2, 1, a0, a1);
+  float dist = abc_sim_distance<D, DY>(p, x, a0, a1);
+  split_at(K0, K1, 2, 0, t0, t1);
+  K0 = t0;
+  K1 = t1;
+  const float sq = __fsqrt_rn(stepsize);
+  const int64_t base = b * n;
+#pragma unroll
+  for (int j = 0; j < D; ++j) x_out[base * D + j] = x[j];
+  dist_out[base] = dist;
+  pp_out[base] = pp;
+  alpha_out[base] = 1.0f;
+#pragma unroll 1
+  for (int64_t i = 1; i < n; ++i) {
+    split_at(K0, K1, 2, 0, t0, t1);  // always
+    uint32_t n0, n1, c0, c1;
+    split_at(t0, t1, 4, 0, n0, n1);
+    split_at(t0, t1, 4, 1, a0, a1);
+    split_at(t0, t1, 4, 3, c0, c1);
+    bits_vec<D>(a0, a1, bits, p.one);
+    float xp[D];
+#pragma unroll
+    for (int j = 0; j < D; ++j) xp[j] = __fadd_rn(x[j], __fmul_rn(sq, bits_to_normal(bits[j])));
+    const float ppn = abc_prior_potential<D, DY>(p, xp);
+    const float dn = abc_sim_distance<D, DY>(p, xp, c0, c1);
+    float a = __fmul_rn(expf_(__fsub_rn(pp, ppn)), dn < thr ? 1.0f : 0.0f);
+    a = a != a ? 0.0f : fminf(1.0f, a);
+    uint32_t u0, u1, v0, v1;
+    split_at(n0, n1, 2, 0, u0, u1);
+    split_at(n0, n1, 2, 1, v0, v1);
+    const float u = bits_to_unit(bits_at(v0, v1, 1, 0));
+    if (u < a) {
+#pragma unroll
+      for (int j = 0; j < D; ++j) x[j] = xp[j];
+      pp = ppn;
+      dist = dn;
+    }
+    K0 = u0;
+    K1 = u1;
+#pragma unroll
+    for (int j = 0; j < D; ++j) x_out[(base + i) * D + j] = x[j];
+    dist_out[base + i] = dist;
+    pp_out[base + i] = pp;
+    alpha_out[base + i] = a;
+  }
+}
+
+template <int D, int DY>
+static int abc_mcmc_lg(const mgb_abc_lg_model *m, int64_t B, int64_t n, const uint32_t *keys, float stepsize,
+                       float thr, float *x, float *dist, float *pp, float *alpha, cudaStream_t s) {
+  k_abc_mcmc_lg<D, DY><<<(unsigned)((B + 127) / 128), 128, 0, s>>>(pack_abc<D, DY>(m), B, n, keys, stepsize, thr, x,
+                                                                   dist, pp, alpha);
+  return launch_status();
+}
+
 #define MGB_ABC_DISPATCH(FN, ...)                                     \
   do {                                                                \
     const int d_ = m->d, dy_ = m->dy;                                 \
@@ -1150,6 +1240,14 @@ int mgb_abc_vanilla_gk(const mgb_abc_gk_model *m, int64_t n, const uint32_t *key
   if (m->d == 4)
     return vabc_gk<4>(m, n, key, threshold, acceptance_rate, ws, x, pp, dist, lw, threshold_out, (cudaStream_t)stream);
   return vabc_gk<1>(m, n, key, threshold, acceptance_rate, ws, x, pp, dist, lw, threshold_out, (cudaStream_t)stream);
+}
+
+int mgb_abc_mcmc_lg(const mgb_abc_lg_model *m, int64_t B, int64_t n, const uint32_t *keys, float stepsize,
+                    float threshold, float *x, float *dist, float *pp, float *alpha, void *stream) {
+  if (!m || !m->m0 || !m->C0 || !m->P0 || !m->H || !m->L || !m->data || B < 1 || B > 0x7FFFFFFFll || n < 1 ||
+      !keys || !x || !dist || !pp || !alpha || !(stepsize >= 0.0f))
+    return ERR_BAD_ARG;
+  MGB_ABC_DISPATCH(abc_mcmc_lg, m, B, n, keys, stepsize, threshold, x, dist, pp, alpha, (cudaStream_t)stream);
 }
 
 int mgb_abc_gk_simulate(const mgb_abc_gk_model *m, int64_t P, const float *x, const uint32_t *keys, float *summary,

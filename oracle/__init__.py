@@ -152,6 +152,8 @@ def lib():
                                    f32p, f32p, f32p, f32p, i32p]
         L.o_abc_gk_run.restype = ctypes.c_int
         L.o_gk_simulate.argtypes = [ctypes.POINTER(_GKModel), i64, f32p, u32p, vp, vp]
+        L.o_abc_mcmc_lg.argtypes = [ctypes.POINTER(_ABCModel), ctypes.c_int, u32p, ctypes.c_float, ctypes.c_float,
+                                    f32p, f32p, f32p, f32p]
         for nm, mt in (("o_abc_vanilla_lg", _ABCModel), ("o_abc_vanilla_gk", _GKModel)):
             getattr(L, nm).argtypes = [ctypes.POINTER(mt), ctypes.c_int, u32p, ctypes.c_float, ctypes.c_float, f32p,
                                        f32p, f32p, f32p]
@@ -625,6 +627,16 @@ def abc_vanilla(n, key, threshold=np.inf, acceptance_rate=None, lg_params=None, 
     thr = fn(ctypes.byref(s), n, _u32(key), float(threshold), -1.0 if acceptance_rate is None else float(acceptance_rate),
              x.reshape(-1), pp, dist, lw)
     return dict(value=x, prior_potential=pp, distance=dist, log_weight=lw, threshold=np.float32(thr))
+
+
+def abc_mcmc_lg(params, n, key, stepsize, threshold):
+    """mocat.run(LinearGaussian ABC scenario, RandomWalkABC(stepsize, threshold), n, key): one chain;
+    returns dict(value (n, d), distance, prior_potential, alpha (n))."""
+    md, keep = _abc_lg_struct(params)
+    x = np.empty((n, md.d), np.float32)
+    dist, pp, al = (np.empty(n, np.float32) for _ in range(3))
+    lib().o_abc_mcmc_lg(ctypes.byref(md), n, _u32(key), float(stepsize), float(threshold), x.reshape(-1), dist, pp, al)
+    return dict(value=x, distance=dist, prior_potential=pp, alpha=al)
 
 
 def abc_gk_run(d, data, N, key, n_raw=1000, n_sum=100, mcmc_steps=1, max_iter=10000, retain=0.9, resample_thr=0.5,

@@ -1603,6 +1603,61 @@ float o_abc_vanilla_gk(const o_gk_model *gk, int n, const uint32_t *key, float t
     return o_abc_vanilla(NULL, gk, n, key, thr, rate, x, pp, dist, lw);
 }
 
+/* RandomWalkABC as an MCMC sampler (abc/mcmc.py:16-100, metropolis.py:48-70, mocat.run) on the
+ * ABC linear-Gaussian scenario, fixed stepsize and threshold, one chain of n states:
+ * (K, s) = split(K) [x_0]; (K, _) = split(K) [prior potential]; (K, k) = split(K) [simulation];
+ * per step (K, _) = split(K); (K, k1, k2, k3) = split(K, 4); x' = x + sqrt(stepsize) normal(k1);
+ * alpha = min(1, exp(pp - pp') [dist' < threshold]) (NaN -> 0); (K, ku) = split(K); accept if
+ * uniform(ku) < alpha.  x (n, d), dist, pp, alpha (n). */
+void o_abc_mcmc_lg(const o_abc_model *md, int n, const uint32_t *key, float stepsize, float thr, float *x, float *dist,
+                   float *pp, float *alpha)
+{
+    const int d = md->d;
+    uint32_t K0, K1, a0, a1, t0, t1;
+    o_split_at(key[0], key[1], 2, 1, &a0, &a1);
+    o_split_at(key[0], key[1], 2, 0, &t0, &t1);
+    o_split_at(t0, t1, 2, 0, &K0, &K1);
+    float e[16], xc[16], xp[16] = {0.0f};
+    o_normal_vec(a0, a1, d, e);
+    for (int r = 0; r < d; ++r) {
+        float v = md->C0[r * d] * e[0];
+        for (int k = 1; k < d; ++k) v = fmaf(md->C0[r * d + k], e[k], v);
+        xc[r] = md->m0[r] + v;
+    }
+    float p = o_abc_prior_pot(md, xc);
+    o_split_at(K0, K1, 2, 1, &a0, &a1);
+    float ds = o_abc_sim_dist(md, xc, a0, a1);
+    o_split_at(K0, K1, 2, 0, &t0, &t1);
+    K0 = t0; K1 = t1;
+    const float sq = sqrtf(stepsize);
+    memcpy(x, xc, sizeof(float) * d);
+    dist[0] = ds; pp[0] = p; alpha[0] = 1.0f;
+    for (int i = 1; i < n; ++i) {
+        uint32_t n0, n1, c0, c1, u0, u1, v0, v1;
+        o_split_at(K0, K1, 2, 0, &t0, &t1);
+        o_split_at(t0, t1, 4, 0, &n0, &n1);
+        o_split_at(t0, t1, 4, 1, &a0, &a1);
+        o_split_at(t0, t1, 4, 3, &c0, &c1);
+        o_normal_vec(a0, a1, d, e);
+        for (int j = 0; j < d; ++j) xp[j] = xc[j] + sq * e[j];
+        const float ppn = o_abc_prior_pot(md, xp);
+        const float dn = o_abc_sim_dist(md, xp, c0, c1);
+        float a = o_expf(p - ppn) * (dn < thr ? 1.0f : 0.0f);
+        a = a != a ? 0.0f : fminf(1.0f, a);
+        o_split_at(n0, n1, 2, 0, &u0, &u1);
+        o_split_at(n0, n1, 2, 1, &v0, &v1);
+        const float u = o_bits_to_unit(o_bits_at(v0, v1, 1, 0));
+        if (u < a) {
+            memcpy(xc, xp, sizeof(float) * d);
+            p = ppn;
+            ds = dn;
+        }
+        K0 = u0; K1 = u1;
+        memcpy(x + (size_t)i * d, xc, sizeof(float) * d);
+        dist[i] = ds; pp[i] = p; alpha[i] = a;
+    }
+}
+
 /* the same sampler on a g-and-k scenario */
 int o_abc_gk_run(const o_gk_model *gk, const o_abc_config *cf, const uint32_t *key, float *x, float *lw,
                  float *dist, float *stepsize, float *hist_thr, float *hist_ess, float *hist_alpha, int32_t *hist_res)
