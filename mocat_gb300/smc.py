@@ -133,17 +133,24 @@ class Gaussian(Scenario):
         self.precision_sqrt = np.linalg.inv(np.linalg.cholesky(cov))
         self.prior_scale = float(prior_scale)
         self.prior_sample_scale = self.prior_scale if prior_sample_scale is None else float(prior_sample_scale)
-        dev = _dev.device()
-        self._m = torch.as_tensor(self.mean.astype(np.float32), device=dev).contiguous()
-        self._ps = torch.as_tensor(self.precision_sqrt.astype(np.float32), device=dev).contiguous()
+        self._dc = None
         super().__init__(name=name)
+
+    def device_constants(self):
+        """(mean, precision_sqrt) as float32 device tensors, uploaded on first use"""
+        if self._dc is None:
+            dev = _dev.device()
+            self._dc = (torch.as_tensor(self.mean.astype(np.float32), device=dev).contiguous(),
+                        torch.as_tensor(self.precision_sqrt.astype(np.float32), device=dev).contiguous())
+        return self._dc
 
     def prior_potential(self, x, random_key=None):
         x = _dev.as_f32(x)
         return 0.5 * (x * x).sum(-1) / self.prior_scale ** 2
 
     def likelihood_potential(self, x, random_key=None):
-        z = (_dev.as_f32(x) - self._m) @ self._ps.T
+        m, ps = self.device_constants()
+        z = (_dev.as_f32(x) - m) @ ps.T
         return 0.5 * (z * z).sum(-1)
 
 
@@ -219,7 +226,8 @@ class BatchedSMC:
                                   1 if rw else mv.leapfrog_steps, fr,
                                   getattr(scenario, "prior_sample_scale", scenario.prior_scale),
                                   0 if sch is None else len(sch), _dev.ptr(self._sched), 1 if gauss else 0,
-                                  _dev.ptr(scenario._m) if gauss else None, _dev.ptr(scenario._ps) if gauss else None)
+                                  _dev.ptr(scenario.device_constants()[0]) if gauss else None,
+                                  _dev.ptr(scenario.device_constants()[1]) if gauss else None)
         self.keys = keys
         self.Xb = scenario.Xbf16() if precision == "bf16" and not gauss else None
         self.ws = _dev.workspace(_lib.lib().mgb_smc_logreg_workspace(ctypes.byref(self.cfg), self._n_data()))
