@@ -62,3 +62,46 @@ def test_unsupported_dimension_rejected_on_host(L):
     p = ctypes.c_void_p(256)
     need = L.mgb_pf_lg_workspace(1000, 10, d, 0)
     assert L.mgb_pf_lg_run(ctypes.byref(m), 1000, 10, p, p, 0.5, 0, p, need, None, None) == 2
+
+
+def test_new_entry_points_reject_bad_arguments_on_host(L):
+    """Kalman, rejection samplers, stochastic-volatility filter and smoothing, SMC moves, ABC
+    (g-and-k, VanillaABC, RandomWalkABC chains): argument checks run before any device call"""
+    import numpy as np
+    null = None
+    p = ctypes.c_void_p(256)
+    # Kalman: null model, then an unsupported (d, dy)
+    assert L.mgb_kalman_filter(null, 1, 4, p, p, p, null, null) == 1
+    e = np.eye(7, dtype=np.float32)
+    km = _lib.KalmanModel(7, 7, *([e.ctypes.data] * 5), np.zeros(7, np.float32).ctypes.data)
+    assert L.mgb_kalman_filter(ctypes.byref(km), 1, 4, p, p, p, null, null) == 2
+    # rejection samplers: maximum_rejections must be >= 1
+    F = np.eye(2, dtype=np.float32)
+    tr = _lib.LGTransition(2, F.ctypes.data, F.ctypes.data, 0.0)
+    cfg = _lib.RejectionConfig(0, 0.0, 1.01)
+    assert L.mgb_stitch_rejection_lg(ctypes.byref(tr), ctypes.byref(cfg), 16, p, p, p, p, p, p, p, 1 << 20,
+                                     null) == 1
+    cfg.maximum_rejections = 5
+    assert L.mgb_ffbsi_rejection_lg(ctypes.byref(tr), ctypes.byref(cfg), 0, 16, 16, p, p, p, p, p, p, p, 1 << 20,
+                                    null) == 1
+    assert L.mgb_ffbsi_sv(1.0, 1.0, 0, 16, 16, p, p, p, p, p, p, p, 1 << 20, null) == 1
+    # stochastic-volatility filter: an unknown resampling scheme
+    sv = _lib.SVModel(0.95, 0.3, 1.0, 0.9, 1.0, 0.0)
+    assert L.mgb_pf_sv_run(ctypes.byref(sv), 64, 8, p, p, p, 0.5, 7, p, 1 << 30, null, null) == 2
+    # SMC: an unknown move
+    sc = _lib.SMCConfig(1, 64, 2, 1, 0.1, 1.0, 0.5, 0.5, 1e-5, 100, 1.0, 10, 0, 9)
+    assert L.mgb_smc_logreg_init(ctypes.byref(sc), p, p, null, 10, p, p, 1 << 30, null) == 1
+    # g-and-k ABC: d must be 1 or 4
+    acfg = _lib.ABCConfig(1, 64, 1, 10, 0.8, 0.5, 0.01, 1, 0.0, 0, None)
+    gk = _lib.GKModel(3, 1000, 100, 0.8, 0.0, 10.0, 1e-5, 256)
+    assert L.mgb_abc_gk_smc_init(ctypes.byref(acfg), ctypes.byref(gk), p, p, 1 << 30, null) == 1
+    assert L.mgb_abc_gk_simulate(ctypes.byref(gk), 4, p, p, p, null, null) == 1
+    # VanillaABC: too small a workspace; RandomWalkABC chains: a negative stepsize
+    d3 = np.eye(3, dtype=np.float32)
+    v3 = np.zeros(3, np.float32)
+    am = _lib.ABCModel(3, 2, v3.ctypes.data, d3.ctypes.data, d3.ctypes.data, 0.0, d3.ctypes.data, d3.ctypes.data,
+                       v3.ctypes.data)
+    need = L.mgb_abc_vanilla_workspace(1000)
+    assert need > 0
+    assert L.mgb_abc_vanilla_lg(ctypes.byref(am), 1000, p, 1.0, -1.0, p, need - 1, p, p, p, p, p, null) == 4
+    assert L.mgb_abc_mcmc_lg(ctypes.byref(am), 1, 100, p, -0.1, 1.0, p, p, p, p, null) == 1
