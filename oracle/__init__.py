@@ -152,6 +152,8 @@ def lib():
                                    f32p, f32p, f32p, f32p, i32p]
         L.o_abc_gk_run.restype = ctypes.c_int
         L.o_gk_simulate.argtypes = [ctypes.POINTER(_GKModel), i64, f32p, u32p, vp, vp]
+        L.o_abc_mcmc_rm_lg.argtypes = [ctypes.POINTER(_ABCModel), ctypes.c_int, u32p, ctypes.c_float, ctypes.c_float,
+                                       ctypes.c_float, f32p, f32p, f32p, f32p]
         L.o_abc_mcmc_lg.argtypes = [ctypes.POINTER(_ABCModel), ctypes.c_int, u32p, ctypes.c_float, ctypes.c_float,
                                     f32p, f32p, f32p, f32p]
         for nm, mt in (("o_abc_vanilla_lg", _ABCModel), ("o_abc_vanilla_gk", _GKModel)):
@@ -637,6 +639,18 @@ def abc_mcmc_lg(params, n, key, stepsize, threshold):
     dist, pp, al = (np.empty(n, np.float32) for _ in range(3))
     lib().o_abc_mcmc_lg(ctypes.byref(md), n, _u32(key), float(stepsize), float(threshold), x.reshape(-1), dist, pp, al)
     return dict(value=x, distance=dist, prior_potential=pp, alpha=al)
+
+
+def abc_mcmc_rm_lg(params, n, key, target=0.1, scale=1.0, neg_exp=2.0 / 3.0):
+    """RandomWalkABC() with RMMetropolisDiagStepsize(rm_stepsize_scale=scale) on the ABC linear-Gaussian
+    scenario, one chain: dict(value (n, d), alpha (n), threshold (n), stepsize (n, d))."""
+    md, keep = _abc_lg_struct(params)
+    d = md.d
+    x, st = np.empty((n, d), np.float32), np.empty((n, d), np.float32)
+    al, th = np.empty(n, np.float32), np.empty(n, np.float32)
+    lib().o_abc_mcmc_rm_lg(ctypes.byref(md), n, _u32(key), float(target), float(scale), float(np.float32(neg_exp)),
+                           x.reshape(-1), al, th, st.reshape(-1))
+    return dict(value=x, alpha=al, threshold=th, stepsize=st)
 
 
 def abc_gk_run(d, data, N, key, n_raw=1000, n_sum=100, mcmc_steps=1, max_iter=10000, retain=0.9, resample_thr=0.5,

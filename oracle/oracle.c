@@ -1658,6 +1658,81 @@ void o_abc_mcmc_lg(const o_abc_model *md, int n, const uint32_t *key, float step
     }
 }
 
+/* RandomWalkABC with the RMMetropolisDiagStepsize correction (abc/mcmc.py:105-140,
+ * metropolis.py:73-160), the sampler's defaults: threshold and stepsize unset, so the chain starts
+ * at threshold 50 and stepsize 1 per dimension, post_mean x_0, diag_post_cov = stepsize d / 2.38^2.
+ * Each step as o_abc_mcmc_lg with the current threshold and per-dimension stepsize, then, with
+ * rm = scale iter^-neg_exp (iter = step index, exp and log by the library's own functions):
+ *   threshold <- exp(log threshold - rm (alpha - target))                (log Robbins-Monro)
+ *   r = min(rm, 1 - 1e-3); diag <- (1 - r) diag + r (x - post_mean)^2; post_mean <- (1 - r) post_mean + r x;
+ *   stepsize <- diag / d * 2.38^2
+ * Outputs per state: x (n, d), alpha (n), threshold (n), stepsize (n, d). */
+void o_abc_mcmc_rm_lg(const o_abc_model *md, int n, const uint32_t *key, float target, float scale, float neg_exp,
+                      float *x, float *alpha, float *thr_out, float *step_out)
+{
+    const int d = md->d;
+    uint32_t K0, K1, a0, a1, t0, t1;
+    o_split_at(key[0], key[1], 2, 1, &a0, &a1);
+    o_split_at(key[0], key[1], 2, 0, &t0, &t1);
+    o_split_at(t0, t1, 2, 0, &K0, &K1);
+    float e[16], xc[16], xp[16] = {0.0f}, st[16], pm[16], dg[16];
+    o_normal_vec(a0, a1, d, e);
+    for (int r = 0; r < d; ++r) {
+        float v = md->C0[r * d] * e[0];
+        for (int k = 1; k < d; ++k) v = fmaf(md->C0[r * d + k], e[k], v);
+        xc[r] = md->m0[r] + v;
+    }
+    float p = o_abc_prior_pot(md, xc);
+    o_split_at(K0, K1, 2, 1, &a0, &a1);
+    float ds = o_abc_sim_dist(md, xc, a0, a1);
+    o_split_at(K0, K1, 2, 0, &t0, &t1);
+    K0 = t0; K1 = t1;
+    float thr = 50.0f;
+    for (int j = 0; j < d; ++j) {
+        st[j] = 1.0f;
+        pm[j] = xc[j];
+        dg[j] = (st[j] * (float)d) / 5.6644f;
+    }
+    memcpy(x, xc, sizeof(float) * d);
+    memcpy(step_out, st, sizeof(float) * d);
+    alpha[0] = 1.0f; thr_out[0] = thr;
+    (void)ds;
+    for (int i = 1; i < n; ++i) {
+        uint32_t n0, n1, c0, c1, u0, u1, v0, v1;
+        o_split_at(K0, K1, 2, 0, &t0, &t1);
+        o_split_at(t0, t1, 4, 0, &n0, &n1);
+        o_split_at(t0, t1, 4, 1, &a0, &a1);
+        o_split_at(t0, t1, 4, 3, &c0, &c1);
+        o_normal_vec(a0, a1, d, e);
+        for (int j = 0; j < d; ++j) xp[j] = xc[j] + sqrtf(st[j]) * e[j];
+        const float ppn = o_abc_prior_pot(md, xp);
+        const float dn = o_abc_sim_dist(md, xp, c0, c1);
+        float a = o_expf(p - ppn) * (dn < thr ? 1.0f : 0.0f);
+        a = a != a ? 0.0f : fminf(1.0f, a);
+        o_split_at(n0, n1, 2, 0, &u0, &u1);
+        o_split_at(n0, n1, 2, 1, &v0, &v1);
+        const float u = o_bits_to_unit(o_bits_at(v0, v1, 1, 0));
+        if (u < a) {
+            memcpy(xc, xp, sizeof(float) * d);
+            p = ppn;
+            ds = dn;
+        }
+        K0 = u0; K1 = u1;
+        const float rm = scale * o_expf(-neg_exp * o_logf((float)i));
+        thr = o_expf(o_logf(thr) - rm * (a - target));
+        const float r2 = fminf(rm, 0.999f);
+        for (int j = 0; j < d; ++j) {
+            const float dv = xc[j] - pm[j];
+            dg[j] = (1.0f - r2) * dg[j] + r2 * (dv * dv);
+            pm[j] = (1.0f - r2) * pm[j] + r2 * xc[j];
+            st[j] = (dg[j] / (float)d) * 5.6644f;
+        }
+        memcpy(x + (size_t)i * d, xc, sizeof(float) * d);
+        memcpy(step_out + (size_t)i * d, st, sizeof(float) * d);
+        alpha[i] = a; thr_out[i] = thr;
+    }
+}
+
 /* the same sampler on a g-and-k scenario */
 int o_abc_gk_run(const o_gk_model *gk, const o_abc_config *cf, const uint32_t *key, float *x, float *lw,
                  float *dist, float *stepsize, float *hist_thr, float *hist_ess, float *hist_alpha, int32_t *hist_res)

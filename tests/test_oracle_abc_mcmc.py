@@ -66,3 +66,76 @@ def test_reference_fixed_stepsize_check():
     assert out["alpha"][1:].mean() > 0.1
     assert np.abs(pm - x.mean(0)).sum() < 3.0
     assert np.abs(pc - np.cov(x.T)).sum() < 3.0
+
+
+def _python_rm_chain(p, n, key, target=0.1, scale=1.0, neg_exp=F(2.0 / 3.0)):
+    d = p["m0"].size
+    K, s = O.split(key, 2)
+    K = O.split(K, 2)[0]
+    K, _k = O.split(K, 2)
+    e = _normals(s, d)
+    x = np.zeros(d, np.float32)
+    for r in range(d):
+        v = F(p["C0"][r, 0] * e[0])
+        for c in range(1, d):
+            v = _fma(p["C0"][r, c], e[c], v)
+        x[r] = F(p["m0"][r] + v)
+    pp = _prior_pot_exact(p, x)
+    thr = F(50)
+    st = np.ones(d, np.float32)
+    pm = x.copy()
+    dg = np.array([F(F(st[j] * F(d)) / F(5.6644)) for j in range(d)], np.float32)
+    xs, al, th = [x.copy()], [F(1)], [thr]
+    ex = lambda v: F(np.asarray(O.expf(F(v))).reshape(()))
+    lg = lambda v: F(np.asarray(O.logf(F(v))).reshape(()))
+    for i in range(1, n):
+        K = O.split(K, 2)[0]
+        K, k1, _k2, k3 = O.split(K, 4)
+        e = _normals(k1, d)
+        xp = np.array([F(x[j] + F(F(np.sqrt(st[j])) * e[j])) for j in range(d)], np.float32)
+        ppn, dn = _prior_pot_exact(p, xp), _sim_dist(p, xp, k3)
+        with np.errstate(over="ignore", invalid="ignore"):
+            a = F(ex(F(pp - ppn)) * (F(1) if dn < thr else F(0)))
+        a = F(0) if a != a else min(F(1), a)
+        K, ku = O.split(K, 2)
+        if F(np.asarray(O.uniform(ku, ())).reshape(())) < a:
+            x, pp = xp, ppn
+        rm = F(F(scale) * ex(F(-neg_exp * lg(F(i)))))
+        thr = ex(F(lg(thr) - F(rm * F(a - F(target)))))
+        r2 = min(rm, F(0.999))
+        for j in range(d):
+            dv = F(x[j] - pm[j])
+            dg[j] = F(F(F(1) - r2) * dg[j]) + F(r2 * F(dv * dv))
+            pm[j] = F(F(F(1) - r2) * pm[j]) + F(r2 * x[j])
+            st[j] = F(F(dg[j] / F(d)) * F(5.6644))
+        xs.append(x.copy())
+        al.append(a)
+        th.append(thr)
+    return np.stack(xs), np.array(al, np.float32), np.array(th, np.float32), st
+
+
+def test_rm_oracle_matches_python_restatement():
+    """RMMetropolisDiagStepsize (abc/mcmc.py:105-140, metropolis.py:73-160): the adaptive
+    threshold and per-dimension stepsize of the ABC chain"""
+    p = params()
+    key = O.PRNGKey(2)
+    x, al, th, st = _python_rm_chain(p, 80, key)
+    out = O.abc_mcmc_rm_lg(p, 80, key)
+    assert np.array_equal(out["value"], x)
+    assert np.array_equal(out["alpha"], al)
+    assert np.array_equal(out["threshold"], th)
+    assert np.array_equal(out["stepsize"][-1], st)
+
+
+def test_rm_reference_check():
+    """TestMCMCLinearGaussianABC.test_adaptive_diag_stepsize: n = 1e5, target acceptance 0.1: the
+    chain's mean and covariance within 3 of the posterior's, the mean acceptance 0.1 to one
+    decimal, and the final stepsize the chain's per-dimension variance / d * 2.38^2 to one decimal"""
+    pm, pc = posterior()
+    out = O.abc_mcmc_rm_lg(params(), 100000, O.PRNGKey(0))
+    x = out["value"].astype(np.float64)
+    assert np.abs(pm - x.mean(0)).sum() < 3.0
+    assert np.abs(pc - np.cov(x.T)).sum() < 3.0
+    np.testing.assert_almost_equal(out["alpha"].mean(), 0.1, decimal=1)
+    np.testing.assert_array_almost_equal(out["stepsize"][-1], np.diag(np.cov(x, rowvar=False)) / 3 * 2.38 ** 2,
+                                         decimal=1)
