@@ -1,27 +1,28 @@
 """Pins of the oracle's jax.random restatement (CPU).
 
 * threefry2x32-20 against the Random123 known-answer vectors (the three
-  vectors jax's own random tests use);
+  vectors jax's own random tests use), kept in tests/golden/known_answers.json;
 * jax's counter layout against jax's documented outputs: split(PRNGKey(0)),
   random_bits(PRNGKey(1701), (3,)) (odd length: the zero-pad path),
   normal(PRNGKey(0)) and uniform(PRNGKey(0));
 * the float maths against float64 references (accuracy bounds).
 """
+import json
+import os
+
 import numpy as np
 import pytest
 import scipy.special as sp
 
 import oracle as O
 
+GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "known_answers.json")))
 
-@pytest.mark.parametrize("key,ctr,expect", [
-    ((0x00000000, 0x00000000), (0x00000000, 0x00000000), (0x6B200159, 0x99BA4EFE)),
-    ((0xFFFFFFFF, 0xFFFFFFFF), (0xFFFFFFFF, 0xFFFFFFFF), (0x1CB996FC, 0xBB002BE7)),
-    ((0x13198A2E, 0x03707344), (0x243F6A88, 0x85A308D3), (0xC4923A9C, 0x483DF7A0)),
-])
-def test_threefry_known_answers(key, ctr, expect):
-    r0, r1 = O.threefry2x32(key, ctr[0], ctr[1])
-    assert (int(r0[0]), int(r1[0])) == expect
+
+@pytest.mark.parametrize("case", GOLDEN["threefry2x32_20"]["cases"])
+def test_threefry_known_answers(case):
+    r0, r1 = O.threefry2x32(tuple(case["key"]), case["counter"][0], case["counter"][1])
+    assert [int(r0[0]), int(r1[0])] == case["expect"]
 
 
 def test_prngkey_layout():
@@ -30,17 +31,17 @@ def test_prngkey_layout():
 
 
 def test_split_matches_jax_docs():
-    k = O.split(O.PRNGKey(0))
-    assert k.tolist() == [[4146024105, 967050713], [2718843009, 1272950319]]
+    assert O.split(O.PRNGKey(0)).tolist() == GOLDEN["jax_random_documented"]["split_PRNGKey0"]
 
 
 def test_random_bits_odd_length():
-    assert O.random_bits(O.PRNGKey(1701), 3).tolist() == [56197195, 4200222568, 961309823]
+    assert O.random_bits(O.PRNGKey(1701), 3).tolist() == GOLDEN["jax_random_documented"]["random_bits_PRNGKey1701_3"]
 
 
 def test_normal_uniform_scalar_values():
-    assert np.float32(O.normal(O.PRNGKey(0))) == np.float32(-0.20584226)
-    assert np.float32(O.uniform(O.PRNGKey(0))) == np.float32(0.41845703)
+    g = GOLDEN["jax_random_documented"]
+    assert np.float32(O.normal(O.PRNGKey(0))) == np.float32(g["normal_PRNGKey0"])
+    assert np.float32(O.uniform(O.PRNGKey(0))) == np.float32(g["uniform_PRNGKey0"])
 
 
 def test_split_num_consistent_with_bits():
