@@ -431,6 +431,10 @@ ResampleWs carve_resample(Carver &c, int64_t n, int scheme) {
 }
 
 // Zero the control block / tile status words (async; graph-capturable).
+// status and the first ntiles words of status2 hold decoupled-lookback flags
+// (the tile scan of either scheme, and the multinomial scan of the n + 1
+// spacings, which has exactly ntiles tiles), so they must start at zero; the
+// rest of status2 (the systematic fill units) is written before it is read.
 int reset_resample(const ResampleWs &w, cudaStream_t s) {
   if (cudaMemsetAsync(w.ctl, 0, sizeof(ResampleCtl), s) != cudaSuccess) return ERR_CUDA;
   if (cudaMemsetAsync(w.status, 0, sizeof(uint64_t) * w.ntiles, s) != cudaSuccess) return ERR_CUDA;

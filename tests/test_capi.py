@@ -54,6 +54,13 @@ def test_workspace_too_small_rejected_on_host(L):
     assert L.mgb_resample_workspace(1000, 1) > L.mgb_resample_workspace(1000, 0)
 
 
+def test_noalloc_array_holds_the_largest_allowed_size(L):
+    """the fixed 256 KiB array of mgb_resample_systematic_u_noalloc holds the
+    scratch of n = MGB_NOALLOC_MAX_N (a host-only size query)"""
+    max_n = 1 << 24  # MGB_NOALLOC_MAX_N
+    assert L.mgb_resample_workspace(max_n, 0) <= 256 * 1024
+
+
 def test_unsupported_dimension_rejected_on_host(L):
     import numpy as np
     d = 7

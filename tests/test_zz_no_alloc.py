@@ -62,6 +62,22 @@ def test_noalloc_matches_workspace_path_two_calls(cuda):
         assert int(gerr.item()) == int(rerr.item()) == 0
 
 
+def test_noalloc_at_the_largest_allowed_size(cuda):
+    """n = MGB_NOALLOC_MAX_N fills the fixed array the most; then a small call
+    starts from its leftover scratch"""
+    from mocat_gb300 import _lib
+    L = _lib.lib()
+    rng = np.random.default_rng(7)
+    cases = [(MAX_N, 123_457, 3.0), (1000, 5, 1.0)]
+    for n, m23, scale in cases:
+        lw = torch.from_numpy((rng.standard_normal(n) * scale).astype(np.float32)).to(cuda)
+        got, gerr = _noalloc(L, lw, m23)
+        ref, rerr = _with_workspace(L, lw, m23)
+        torch.cuda.synchronize()
+        assert torch.equal(got, ref), n
+        assert int(gerr.item()) == int(rerr.item()) == 0
+
+
 def test_noalloc_rejects_oversize_on_host(cuda):
     from mocat_gb300 import _lib
     L = _lib.lib()
