@@ -102,12 +102,32 @@ int mgb_resample_systematic_u(const float *lw_dev, int64_t n, uint32_t m23, int3
  * as mgb_resample_systematic_u; the scratch lives in a fixed device array
  * inside the library (256 KiB, resident on each device that loads it until
  * exit), so n must not exceed MGB_NOALLOC_MAX_N (else MGB_ERR_UNSUPPORTED).
- * The first call on a device looks up that array's address: make it before
- * any stream capture.  Calls share the array; calls that overlap on the GPU
- * race on it. */
+ * The first call in each CUDA context looks up that array's address (cached
+ * per context ID, so a context made after cudaDeviceReset looks it up again):
+ * make it before any stream capture.  Calls share the array; calls that
+ * overlap on the GPU race on it. */
 #define MGB_NOALLOC_MAX_N (1 << 24)
 int mgb_resample_systematic_u_noalloc(const float *lw_dev, int64_t n, uint32_t m23, int32_t *ancestors_dev,
                                       int32_t *err_dev, void *stream);
+
+/* ------------------------------------------------ bounded device waits
+ * Every spin wait in the library's kernels (the persistent filter's grid
+ * barrier, the decoupled-lookback tile scan) gives up after a fixed number of
+ * polls, raises bit 1 of the error word and lets the kernel finish, so a
+ * wait that cannot end costs a bounded delay and an error status instead of a
+ * hung GPU.  mgb_wait_selftest makes one such wait run out on purpose, with
+ * the library's own wait code and a given poll limit (1 .. 2^22), on a wait
+ * that nothing will satisfy: a grid barrier one block short
+ * (MGB_WAIT_GRID_BARRIER) or a lookback whose predecessor tile never
+ * publishes (MGB_WAIT_LOOKBACK).  It returns MGB_ERR_DEVICE_TIMEOUT when the
+ * wait ran out and reported it (the expected result), synchronising `stream`.
+ * No counterpart in the reference, whose JAX code has no device waits
+ * (its only run-time guard is mocat/src/transport/smc.py:174-175).
+ * ws_dev: mgb_wait_selftest_workspace() bytes. */
+#define MGB_WAIT_GRID_BARRIER 0
+#define MGB_WAIT_LOOKBACK 1
+size_t mgb_wait_selftest_workspace(void);
+int mgb_wait_selftest(int which, int32_t polls, void *ws_dev, size_t ws_bytes, void *stream);
 
 /* ---------------------------------------------------------------- gather
  * Replaces the fancy-index gathers x[..., idx, :] (mocat/src/ssm/filtering.py:199)
@@ -194,6 +214,30 @@ size_t mgb_pf_lg_grad_workspace(int64_t n, int64_t T, int32_t d, int32_t ckpt_ev
 int mgb_pf_lg_grad(const mgb_lg_model *model_host, int64_t n, int64_t T, const uint32_t *key_dev, const float *y_dev,
                    float ess_threshold, int scheme, int32_t ckpt_every, void *ws_dev, size_t ws_bytes,
                    double *log_z_dev, float *grad_dev, int32_t *resampled_dev, void *stream);
+
+/* ------------------------------ score by Fisher's identity (smoothed, PaRIS)
+ * Consistent estimate of d log p(y) / d theta for the model of mgb_pf_lg_grad
+ * (H = I, diagonal Lq and P; theta = (A = F, log q, log r)), made along the
+ * same bootstrap filter (run_particle_filter_for_marginals,
+ * mocat/src/ssm/filtering.py:255-324, as mgb_pf_lg_run on `key`): by Fisher's
+ * identity the score is the smoothed expectation of the complete-data score,
+ * and each particle carries that additive functional forward, PaRIS-style,
+ * averaged over `backward_draws` (K, 1..4) backward draws per step: the
+ * particle's own ancestor, then draws of an independent-Metropolis chain with
+ * `mcmc_steps` (L) uniform proposals each, (K - 1) L <= 4096.  K = 1 traces
+ * the statistic along the genealogy only.  Unlike mgb_pf_lg_grad (the
+ * gradient of the log Z estimate with the resampling held fixed, which does
+ * not converge to the score), the error of this estimate falls as n grows.
+ * smoothing_key_dev (2 words) seeds the backward draws; T <= 2^20.
+ * grad_dev: d*d + 2d floats in mgb_pf_lg_grad's layout (summed in float64).
+ * log_z_dev, resampled_dev (T) and draws_dev ((T, n, K) int32: the source
+ * particle index of every backward draw, row t >= 1) may be NULL.
+ * One launch per phase and step on `stream`; no host synchronisation. */
+size_t mgb_pf_lg_score_workspace(int64_t n, int64_t T, int32_t d);
+int mgb_pf_lg_score(const mgb_lg_model *model_host, int64_t n, int64_t T, const uint32_t *key_dev,
+                    const uint32_t *smoothing_key_dev, const float *y_dev, float ess_threshold, int scheme,
+                    int32_t backward_draws, int32_t mcmc_steps, void *ws_dev, size_t ws_bytes, double *log_z_dev,
+                    float *grad_dev, int32_t *resampled_dev, int32_t *draws_dev, void *stream);
 
 /* --------------------------------------------- backward simulation (FFBSi)
  * backward_simulation with maximum_rejections = 0, i.e. backward_simulation_full

@@ -1,4 +1,5 @@
-"""d log Z / d theta of the bootstrap particle filter by a hand-written adjoint.
+"""Parameter gradients of the bootstrap particle filter: a hand-written adjoint of the
+log Z estimate, and a consistent score estimate by Fisher's identity.
 
 mocat obtains parameter gradients by jax.grad through
 run_particle_filter_for_marginals (mocat/src/ssm/filtering.py:255-324); here the
@@ -13,6 +14,9 @@ log diag R).
 
 * ``log_z_and_grad(ssm_scenario, y, random_key, n, ...)``: log Z and the three
   gradient blocks for a scenario object.
+* ``log_z_and_score(...)``: the score d log p(y) / d theta by Fisher's identity,
+  smoothed along the same filter by PaRIS (mgb_pf_lg_score); its error falls as n
+  grows, which the fixed-ancestor gradient's does not.
 * ``ParticleFilterLogZ``: a torch.autograd.Function whose forward is the
   filter's log Z and whose backward is the adjoint, so that
   ``particle_filter_log_z(A, log_q, log_r, ...)`` composes with torch code.
@@ -66,15 +70,28 @@ def _grad_call(s, d, y, key, n, ess_threshold, resampling, ckpt_every, persisten
 
 
 def log_z_and_grad(ssm_scenario, y, random_key, n, ess_threshold=0.5, resampling="systematic", ckpt_every=32,
-                   persistent=True):
+                   persistent=True, estimator="pathwise", backward_draws=2, mcmc_steps=8, smoothing_key=None):
     """log Z of run_particle_filter_for_marginals(ssm_scenario, BootstrapFilter(), y, ..., n=n)
-    and its gradient with respect to (transition_matrix, log diag transition_covariance,
-    log diag likelihood_covariance), ancestors held fixed.  persistent=False runs the taped
-    forward pass one launch per phase instead of one persistent launch (same gradient;
-    log Z within 1e-6, its float partial sums grouped differently).
+    and a gradient with respect to (transition_matrix, log diag transition_covariance,
+    log diag likelihood_covariance).
+
+    estimator="pathwise": the gradient of the log Z estimate with the ancestors and
+    resampling decisions held fixed (what jax.grad through the reference's filter
+    computes); it does not converge to the score d log p(y) / d theta as n grows,
+    because it drops the resampling's dependence on theta.  persistent=False runs the
+    taped forward pass one launch per phase instead of one persistent launch (same
+    gradient; log Z within 1e-6, its float partial sums grouped differently).
+
+    estimator="fisher": log_z_and_score (the consistent Fisher-identity estimate,
+    smoothed by PaRIS), with backward_draws, mcmc_steps and smoothing_key as there.
 
     Returns cdict(log_z, grad_transition_matrix (d, d), grad_log_transition_covariance_diag (d,),
     grad_log_likelihood_covariance_diag (d,), resampled (T,))."""
+    if estimator == "fisher":
+        return log_z_and_score(ssm_scenario, y, random_key, n, backward_draws=backward_draws, mcmc_steps=mcmc_steps,
+                               smoothing_key=smoothing_key, ess_threshold=ess_threshold, resampling=resampling)
+    if estimator != "pathwise":
+        raise ValueError(f"estimator must be 'pathwise' or 'fisher', not {estimator!r}")
     if not isinstance(ssm_scenario, TimeHomogenousLinearGaussian):
         raise NotImplementedError(f"{ssm_scenario.__class__.__name__}: no adjoint kernel for this model")
     _, s = ssm_scenario.derived()
@@ -83,6 +100,56 @@ def log_z_and_grad(ssm_scenario, y, random_key, n, ess_threshold=0.5, resampling
     return cdict(log_z=lz, grad_transition_matrix=g[:d * d].reshape(d, d),
                  grad_log_transition_covariance_diag=g[d * d:d * d + d],
                  grad_log_likelihood_covariance_diag=g[d * d + d:], resampled=res.bool())
+
+
+def default_smoothing_key(random_key):
+    """split(random_key, 3)[2]: the smoothing draws' key when none is given (the
+    filter itself uses split(random_key, 2), so the streams do not overlap)."""
+    from .random import split
+    return split(_dev.as_key(random_key), 3)[2].contiguous()
+
+
+def log_z_and_score(ssm_scenario, y, random_key, n, backward_draws=2, mcmc_steps=8, smoothing_key=None,
+                    ess_threshold=0.5, resampling="systematic", return_draws=False):
+    """The score d log p(y) / d theta, theta = (transition_matrix, log diag
+    transition_covariance, log diag likelihood_covariance), by Fisher's identity along
+    the bootstrap filter run_particle_filter_for_marginals(ssm_scenario, BootstrapFilter(),
+    y, ..., random_key, n=n) (same particles and log Z), smoothed by PaRIS: every particle
+    carries the smoothed complete-data score forward, averaged over `backward_draws` draws
+    per step (its own ancestor, then an independent-Metropolis chain over the step's
+    particles with `mcmc_steps` uniform proposals per draw).  The estimate is consistent:
+    its error falls as n grows (about n^-1/2 once n is large), unlike the fixed-ancestor
+    pathwise gradient.  One library call (mgb_pf_lg_score), no host synchronisation.
+
+    smoothing_key seeds the backward draws (default: default_smoothing_key(random_key)).
+    Returns cdict(log_z, grad_transition_matrix (d, d), grad_log_transition_covariance_diag (d,),
+    grad_log_likelihood_covariance_diag (d,), resampled (T,), grad (d*d + 2d,)) and, with
+    return_draws, draws (T, n, backward_draws): the source particle of every backward draw."""
+    if not isinstance(ssm_scenario, TimeHomogenousLinearGaussian):
+        raise NotImplementedError(f"{ssm_scenario.__class__.__name__}: no score kernel for this model")
+    _, s = ssm_scenario.derived()
+    d = ssm_scenario.dim
+    if d not in SUPPORTED_D:
+        raise NotImplementedError(f"score for d = {d} not compiled (supported {SUPPORTED_D})")
+    dev = _dev.device()
+    y2 = _dev.as_f32(y).reshape(-1, d).contiguous()
+    T = y2.shape[0]
+    key = _dev.as_key(random_key)
+    skey = default_smoothing_key(key) if smoothing_key is None else _dev.as_key(smoothing_key)
+    ws = _dev.workspace(_lib.lib().mgb_pf_lg_score_workspace(n, T, d), dev)
+    logz = torch.empty(1, dtype=torch.float64, device=dev)
+    grad = torch.empty(d * d + 2 * d, dtype=torch.float32, device=dev)
+    res = torch.empty(T, dtype=torch.int32, device=dev)
+    draws = torch.full((T, n, int(backward_draws)), -1, dtype=torch.int32, device=dev) if return_draws else None
+    call("mgb_pf_lg_score", ctypes.byref(s), n, T, _dev.ptr(key), _dev.ptr(skey), _dev.ptr(y2), float(ess_threshold),
+         SCHEMES[resampling], int(backward_draws), int(mcmc_steps), _dev.ptr(ws), ws.numel(), _dev.ptr(logz),
+         _dev.ptr(grad), _dev.ptr(res), _dev.ptr(draws), _dev.stream_ptr())
+    out = cdict(log_z=logz[0], grad_transition_matrix=grad[:d * d].reshape(d, d),
+                grad_log_transition_covariance_diag=grad[d * d:d * d + d],
+                grad_log_likelihood_covariance_diag=grad[d * d + d:], resampled=res.bool(), grad=grad)
+    if return_draws:
+        out.draws = draws
+    return out
 
 
 def log_z_and_grad_many(ssm_scenario, y, random_keys, n, ess_threshold=0.5, resampling="systematic",
@@ -126,6 +193,62 @@ def log_z_and_grad_many(ssm_scenario, y, random_keys, n, ess_threshold=0.5, resa
                          _dev.ptr(ws[j]), ws[j].numel(),
                          _dev.ptr(logz[b:b + 1]), _dev.ptr(grad[b]), None,
                          ctypes.c_void_p(streams[j].cuda_stream))
+        except Exception as e:  # re-raised on the calling thread
+            errors.append(e)
+
+    threads = [threading.Thread(target=lane, args=(j,)) for j in range(lanes)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    if errors:
+        raise errors[0]
+    for st in streams:
+        cur.wait_stream(st)
+    return cdict(log_z=logz, grad=grad)
+
+
+def log_z_and_score_many(ssm_scenario, y, random_keys, n, backward_draws=2, mcmc_steps=8, smoothing_keys=None,
+                         ess_threshold=0.5, resampling="systematic", max_concurrent=8):
+    """log_z_and_score for B filter keys at once: each evaluation runs on its own CUDA
+    stream, enqueued from its own host thread (the C library releases the interpreter
+    lock), so the launches of different evaluations overlap on the GPU.  The same values
+    as B calls of log_z_and_score (smoothing_keys default to default_smoothing_key of
+    each filter key).
+
+    Returns cdict(log_z (B,), grad (B, d*d + 2d)) in the layout of mgb_pf_lg_score."""
+    import threading
+    if not isinstance(ssm_scenario, TimeHomogenousLinearGaussian):
+        raise NotImplementedError(f"{ssm_scenario.__class__.__name__}: no score kernel for this model")
+    d = ssm_scenario.dim
+    if d not in SUPPORTED_D:
+        raise NotImplementedError(f"score for d = {d} not compiled (supported {SUPPORTED_D})")
+    _, s = ssm_scenario.derived()
+    dev = _dev.device()
+    keys = _dev.as_key(random_keys).reshape(-1, 2).contiguous()
+    B = keys.shape[0]
+    skeys = (torch.stack([default_smoothing_key(keys[b]) for b in range(B)]) if smoothing_keys is None
+             else _dev.as_key(smoothing_keys).reshape(-1, 2).contiguous())
+    y2 = _dev.as_f32(y).reshape(-1, d).contiguous()
+    T = y2.shape[0]
+    nws = _lib.lib().mgb_pf_lg_score_workspace(n, T, d)
+    logz = torch.empty(B, dtype=torch.float64, device=dev)
+    grad = torch.empty((B, d * d + 2 * d), dtype=torch.float32, device=dev)
+    lanes = min(B, max_concurrent)
+    ws = [_dev.workspace(nws, dev) for _ in range(lanes)]
+    streams = [torch.cuda.Stream(dev) for _ in range(lanes)]
+    cur = torch.cuda.current_stream(dev)
+    for st in streams:
+        st.wait_stream(cur)
+    errors = []
+
+    def lane(j):
+        try:
+            for b in range(j, B, lanes):
+                call("mgb_pf_lg_score", ctypes.byref(s), n, T, _dev.ptr(keys[b]), _dev.ptr(skeys[b]), _dev.ptr(y2),
+                     float(ess_threshold), SCHEMES[resampling], int(backward_draws), int(mcmc_steps),
+                     _dev.ptr(ws[j]), ws[j].numel(), _dev.ptr(logz[b:b + 1]), _dev.ptr(grad[b]), None, None,
+                     ctypes.c_void_p(streams[j].cuda_stream))
         except Exception as e:  # re-raised on the calling thread
             errors.append(e)
 

@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libmocatgb.so")
 
-SOURCES = ["mgb_rng.cu", "mgb_resample.cu", "mgb_pf_lg.cu", "mgb_pf_persist.cu", "mgb_noalloc.cu", "mgb_pf_sv_batch.cu", "mgb_pf_opt.cu", "mgb_pf_adjoint.cu", "mgb_smc.cu", "mgb_logreg_tc.cu", "mgb_ffbsi.cu", "mgb_rejection.cu", "mgb_pf_nl1d.cu", "mgb_pf_sv.cu", "mgb_abc.cu", "mgb_kalman.cu"]
+SOURCES = ["mgb_rng.cu", "mgb_resample.cu", "mgb_pf_lg.cu", "mgb_pf_persist.cu", "mgb_noalloc.cu", "mgb_pf_sv_batch.cu", "mgb_pf_opt.cu", "mgb_pf_adjoint.cu", "mgb_pf_score.cu", "mgb_smc.cu", "mgb_logreg_tc.cu", "mgb_ffbsi.cu", "mgb_rejection.cu", "mgb_pf_nl1d.cu", "mgb_pf_sv.cu", "mgb_abc.cu", "mgb_kalman.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fno-strict-aliasing",
                      "-Xptxas", "-warn-spills"]

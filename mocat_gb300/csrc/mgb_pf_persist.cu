@@ -35,12 +35,18 @@
 #include "mgb_nl1d.cuh"
 #include "mgb_sv.cuh"
 
+// co-resident CTAs per SM the persistent kernel is compiled for (a register budget
+// of 65536 / (256 x this) per thread)
+#ifndef MGB_PERSIST_MIN_BLOCKS
+#define MGB_PERSIST_MIN_BLOCKS 2
+#endif
+
 namespace mgb {
 
 // err is the kernel's own (never null) error word: once a wait has run out,
 // later barriers stop waiting and the step loop exits, so a fault can cost at
 // most one bounded wait.
-__device__ __forceinline__ void grid_sync(GridBar *bar, unsigned nblocks, int *err) {
+__device__ __forceinline__ void grid_sync(GridBar *bar, unsigned nblocks, int *err, int limit = BAR_SPIN_LIMIT) {
   __syncthreads();
   if (threadIdx.x == 0) {
     volatile unsigned int *vgen = &bar->gen;
@@ -53,7 +59,7 @@ __device__ __forceinline__ void grid_sync(GridBar *bar, unsigned nblocks, int *e
     } else {
       int polls = 0;
       while (*vgen == g && !(*(volatile int *)err & EB_TIMEOUT)) {
-        if (++polls > BAR_SPIN_LIMIT) {
+        if (++polls > limit) {
           atomicOr(err, EB_TIMEOUT);
           break;
         }
@@ -206,7 +212,7 @@ struct LGModelP {
 };
 
 template <class MP>
-__global__ void __launch_bounds__(PP_TPB, 2) k_pf_persist(const __grid_constant__ MP p,
+__global__ void __launch_bounds__(PP_TPB, MGB_PERSIST_MIN_BLOCKS) k_pf_persist(const __grid_constant__ MP p,
                                                            const __grid_constant__ PersistArgs a) {
   constexpr int D = MP::kD, DY = MP::kDY;
   __shared__ float smf[PP_TPB / 32];
@@ -299,6 +305,7 @@ __global__ void __launch_bounds__(PP_TPB, 2) k_pf_persist(const __grid_constant_
     if (a.trace && t == 1 && threadIdx.x == 0) a.trace[a.T * 10 + blockIdx.x] = globaltimer_ns() - t0;
     stamp(a, t, 1);
     grid_sync(a.bar, G, a.err);
+    if (timed_out(a.err)) break;  // no phase runs on data a timed-out barrier did not order
     stamp(a, t, 2);
 
     // ---- P2: combine (identical in every block)
@@ -363,6 +370,7 @@ __global__ void __launch_bounds__(PP_TPB, 2) k_pf_persist(const __grid_constant_
       }
       stamp(a, t, 4);
       grid_sync(a.bar, G, a.err);
+      if (timed_out(a.err)) break;
       stamp(a, t, 5);
 
       // ---- P4: scan tile sums, place outputs, fill units
@@ -439,10 +447,26 @@ __global__ void __launch_bounds__(PP_TPB, 2) k_pf_persist(const __grid_constant_
       }
       stamp(a, t, 7);
       grid_sync(a.bar, G, a.err);
+      if (timed_out(a.err)) break;
       stamp(a, t, 8);
     }
     res_cur = res_next;
   }
+}
+
+// Bounded-wait self-tests: each makes one of the library's device waits run
+// out on purpose, with no data behind it.  The barrier counts one more arrival
+// than there are blocks (the missing block never comes); the lookback scans
+// tile 1 while tile 0 never publishes its prefix.
+__global__ void k_wait_selftest_barrier(GridBar *bar, int *err, int limit) {
+  grid_sync(bar, gridDim.x + 1, err, limit);
+}
+__global__ void __launch_bounds__(SCAN_TPB) k_wait_selftest_lookback(uint64_t *status, int *err, int limit) {
+  uint64_t v[SCAN_IPT];
+#pragma unroll
+  for (int j = 0; j < SCAN_IPT; ++j) v[j] = 1ull;
+  uint64_t excl, total;
+  tile_scan(v, 1u, status, err, excl, total, limit);
 }
 
 __global__ void k_or_err(const int *src, int *dst) {
@@ -502,3 +526,29 @@ int run_sv_persistent(const mgb_sv_model *m, const PersistArgs &a, cudaStream_t 
 }
 
 }  // namespace mgb
+
+using namespace mgb;
+
+extern "C" size_t mgb_wait_selftest_workspace(void) { return 256; }
+
+extern "C" int mgb_wait_selftest(int which, int32_t polls, void *ws, size_t ws_bytes, void *stream) {
+  if ((which != MGB_WAIT_GRID_BARRIER && which != MGB_WAIT_LOOKBACK) || polls < 1 || polls > BAR_SPIN_LIMIT || !ws ||
+      ws_bytes < mgb_wait_selftest_workspace())
+    return ERR_BAD_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  char *base = (char *)ws;
+  int *err = (int *)base;                       // [0, 4)
+  GridBar *bar = (GridBar *)(base + 16);        // [16, 24)
+  uint64_t *status = (uint64_t *)(base + 32);   // [32, 48): tiles 0 and 1
+  if (cudaMemsetAsync(ws, 0, 64, s) != cudaSuccess) return ERR_CUDA;
+  if (which == MGB_WAIT_GRID_BARRIER)
+    k_wait_selftest_barrier<<<4, 32, 0, s>>>(bar, err, polls);
+  else
+    k_wait_selftest_lookback<<<1, SCAN_TPB, 0, s>>>(status, err, polls);
+  if (launch_status()) return ERR_LAUNCH;
+  int h = 0;
+  if (cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return ERR_CUDA;
+  return (h & EB_TIMEOUT) ? ERR_DEVICE_TIMEOUT : OK;
+}

@@ -234,7 +234,7 @@ __device__ __forceinline__ void st_status(uint64_t *p, uint64_t v) { *(volatile 
 // layout).  On return v[] hold global inclusive prefixes; returns the tile's
 // exclusive prefix and total (via refs).
 __device__ __forceinline__ void tile_scan(uint64_t (&v)[SCAN_IPT], uint32_t tile, uint64_t *status, int *err,
-                                          uint64_t &tile_excl, uint64_t &tile_total) {
+                                          uint64_t &tile_excl, uint64_t &tile_total, int limit = SPIN_LIMIT) {
   __shared__ uint64_t wsum[SCAN_TPB / 32];
   __shared__ uint64_t excl_s;
 #pragma unroll
@@ -271,7 +271,7 @@ __device__ __forceinline__ void tile_scan(uint64_t (&v)[SCAN_IPT], uint32_t tile
           s = ld_status(&status[idx]);
           int polls = 0;
           while ((s >> 62) == 0) {
-            if (++polls > SPIN_LIMIT) {
+            if (++polls > limit) {
               raise_err(err, EB_TIMEOUT);
               s = SFLAG_PFX;
               break;

@@ -122,6 +122,9 @@ def lib():
         L.o_lg_run_tape.argtypes = [ctypes.POINTER(_LGModel), i64, i64, u32p, f32p, ctypes.c_float, ctypes.c_int,
                                     f32p, i32p, i32p]
         L.o_lg_run_tape.restype = ctypes.c_double
+        L.o_lg_score.argtypes = [ctypes.POINTER(_LGModel), i64, i64, u32p, u32p, f32p, ctypes.c_float, ctypes.c_int,
+                                 ctypes.c_int, ctypes.c_int, f64p, f32p, i32p, vp]
+        L.o_lg_score.restype = ctypes.c_double
         L.o_lg_step_keys.argtypes = [u32p, i64, u32p]
         L.o_lg_normals.argtypes = [u32p, i64, ctypes.c_int, f32p]
         L.o_opt_init.argtypes = [ctypes.POINTER(_OptModel), i64, u32p, f32p, f32p, f32p]
@@ -383,6 +386,25 @@ def lg_run_tape(params, n, key, y, ess_threshold=0.5, scheme="systematic"):
     logZ = lib().o_lg_run_tape(ctypes.byref(s), n, T, _u32(key), y.reshape(-1), float(ess_threshold),
                                SCHEMES[scheme], ess, res, anc.reshape(-1))
     return dict(log_z=logZ, ess=ess, resampled=res.astype(bool), ancestors=anc)
+
+
+def lg_score(params, n, key, smoothing_key, y, ess_threshold=0.5, scheme="systematic", backward_draws=2,
+             mcmc_steps=8, draws=False):
+    """Fisher-identity score of the bootstrap filter of lg_run(params, n, key, y, ...),
+    smoothed by PaRIS with independent-Metropolis backward draws (o_lg_score).
+    params: H = I, diagonal Lq and P.  Returns dict(log_z, grad (d*d + 2d, float64:
+    dF row-major, d/dlog q, d/dlog r), ess, resampled, draws (T, n, K) or None)."""
+    s, keep = _lg_struct(params)
+    y = _f32(y).reshape(len(y), -1)
+    T = y.shape[0]
+    d = params["d"]
+    grad = np.empty(d * d + 2 * d, np.float64)
+    ess = np.empty(T, np.float32)
+    res = np.empty(T, np.int32)
+    dr = np.full((T, n, backward_draws), -1, np.int32) if draws else None
+    logZ = lib().o_lg_score(ctypes.byref(s), n, T, _u32(key), _u32(smoothing_key), y.reshape(-1), float(ess_threshold),
+                            SCHEMES[scheme], int(backward_draws), int(mcmc_steps), grad, ess, res, _ptr(dr))
+    return dict(log_z=logZ, grad=grad, ess=ess, resampled=res.astype(bool), draws=dr)
 
 
 def lg_step_keys(key, T):

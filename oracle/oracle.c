@@ -324,15 +324,16 @@ void o_lg_propagate(const o_lg_model *md, int64_t n, const uint32_t *kt, const f
  * Outputs: logZ (log-marginal-likelihood built from the log-weights),
  * ess[T], resampled[T] (resampled[t] = 1 when step t started with a resample),
  * optional histories x_hist (T, n, d) and lw_hist (T, n) (NULL to skip). */
+typedef struct o_score_ctx o_score_ctx;
 static double o_lg_run_impl(const o_lg_model *md, int64_t n, int64_t T, const uint32_t *key, const float *y,
                             float ess_threshold, int scheme, float *ess_out, int32_t *resampled_out,
-                            float *x_hist, float *lw_hist, int32_t *anc_hist);
+                            float *x_hist, float *lw_hist, int32_t *anc_hist, o_score_ctx *sc);
 
 double o_lg_run(const o_lg_model *md, int64_t n, int64_t T, const uint32_t *key, const float *y,
                 float ess_threshold, int scheme, float *ess_out, int32_t *resampled_out,
                 float *x_hist, float *lw_hist)
 {
-    return o_lg_run_impl(md, n, T, key, y, ess_threshold, scheme, ess_out, resampled_out, x_hist, lw_hist, NULL);
+    return o_lg_run_impl(md, n, T, key, y, ess_threshold, scheme, ess_out, resampled_out, x_hist, lw_hist, NULL, NULL);
 }
 
 /* o_lg_run that also records the ancestors: anc_hist (T, n), row t written
@@ -340,7 +341,7 @@ double o_lg_run(const o_lg_model *md, int64_t n, int64_t T, const uint32_t *key,
 double o_lg_run_tape(const o_lg_model *md, int64_t n, int64_t T, const uint32_t *key, const float *y,
                      float ess_threshold, int scheme, float *ess_out, int32_t *resampled_out, int32_t *anc_hist)
 {
-    return o_lg_run_impl(md, n, T, key, y, ess_threshold, scheme, ess_out, resampled_out, NULL, NULL, anc_hist);
+    return o_lg_run_impl(md, n, T, key, y, ess_threshold, scheme, ess_out, resampled_out, NULL, NULL, anc_hist, NULL);
 }
 
 /* Key schedule of run_particle_filter_for_marginals (filtering.py:267-278):
@@ -365,9 +366,175 @@ void o_lg_normals(const uint32_t *kt, int64_t n, int d, float *e)
     }
 }
 
+/* ------------------------------------- score by Fisher's identity (PaRIS)
+ * d log p(y_{0:T-1}) / d theta for theta = (F, log q, log r) of a model with
+ * H = I, Lq = diag(sqrt q), P = diag(1 / sqrt r), by Fisher's identity
+ *   score = E[ sum_t h_t(x_{t-1}, x_t) + sum_t g_t(x_t) | y ],
+ *   h_t: dF_kl = e_k x_{t-1,l} / q_k,  dlog q_k = e_k^2 / (2 q_k) - 1/2  (e = x_t - F x_{t-1}),
+ *   g_t: dlog r_k = (y_k - x_k)^2 / (2 r_k) - 1/2,
+ * estimated along the bootstrap filter of o_lg_run by PaRIS (Olsson and
+ * Westerborn, Bernoulli 23(3), 2017): every particle carries the statistic
+ *   tau_t^i = (1/K) sum_k [tau_{t-1}^{J_k} + h_t(x_{t-1}^{J_k}, x_t^i)] + g_t(x_t^i),
+ * and the estimate is sum_i W_{T-1}^i tau_{T-1}^i.  The K backward draws J_k
+ * follow Dau and Chopin ("On backward smoothing algorithms", Ann. Statist.
+ * 51(5), 2023): J_1 is the particle's own ancestor, and each further draw
+ * continues an independent-Metropolis chain over the step's source
+ * population m = 0..n-1 (the resampled particles x_{t-1}^{a_m}, or all
+ * x_{t-1}^m with their weights when step t did not resample), target
+ * exp(lb_m) f(x_t^i | x_{t-1}^{src(m)}) with lb = 0 (resampled) or lw_{t-1},
+ * proposal uniform over m, L proposals per draw.  The random numbers of
+ * proposal s of particle i at step t: (w0, w1) = threefry2x32(skey, (i, (t << 12) | s)),
+ * m' = (w0 * n) >> 32, E = exponential(w1); accept when (lf' - lf) + E > 0.
+ * Every float operation is written out in the order the GPU kernel uses. */
+struct o_score_ctx {
+    int K, L;
+    uint32_t skey[2];
+    float iq[64], half_iq[64], half_ir[64];
+    int P, TS;
+    float *tau_a, *tau_b;   /* (n, TS) */
+    float *mu;              /* (n, d + 1): F x_src, lb */
+    int32_t *draws;         /* (T, n, K) or NULL */
+    float *lw_last;         /* (n): the filter's final log-weights */
+};
+
+static inline float o_score_lf(const float *xi, const float *mu, const float *iq, int d)
+{
+    float s2 = 0.0f;
+    for (int r = 0; r < d; ++r) {
+        float dr = xi[r] - mu[r];
+        s2 = fmaf(dr * dr, iq[r], s2);
+    }
+    return mu[d] - 0.5f * s2;
+}
+
+static void o_score_init(o_score_ctx *sc, const o_lg_model *md, int64_t n, const float *x, const float *y0)
+{
+    const int d = md->d;
+    for (int64_t i = 0; i < n; ++i) {
+        float *to = sc->tau_a + i * sc->TS;
+        for (int q = 0; q < sc->TS; ++q) to[q] = 0.0f;
+        for (int r = 0; r < d; ++r) {
+            float dr = y0[r] - x[i * d + r];
+            to[d * d + d + r] = dr * dr * sc->half_ir[r] - 0.5f;
+        }
+    }
+}
+
+static void o_score_step(o_score_ctx *sc, const o_lg_model *md, int64_t n, int64_t t, const float *xprev,
+                         const float *xnew, const int32_t *anc, const float *lw_prev, const float *yt)
+{
+    const int d = md->d, K = sc->K, L = sc->L, TS = sc->TS, MS = d + 1;
+    float *mu = sc->mu;
+#pragma omp parallel for schedule(static)
+    for (int64_t m = 0; m < n; ++m) {
+        const float *xs = xprev + (int64_t)(anc ? anc[m] : m) * d;
+        for (int r = 0; r < d; ++r) {
+            const float *f = md->F + r * d;
+            float fx = f[0] * xs[0];
+            for (int k = 1; k < d; ++k) fx = fmaf(f[k], xs[k], fx);
+            mu[m * MS + r] = fx;
+        }
+        mu[m * MS + d] = anc ? 0.0f : lw_prev[m];
+    }
+    const float invK = (float)(1.0 / K);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        const float *xi = xnew + i * d;
+        int64_t mk[4], jk[4];
+        mk[0] = i;
+        int64_t cur = i;
+        float lcur = o_score_lf(xi, mu + i * MS, sc->iq, d);
+        for (int k = 1; k < K; ++k) {
+            for (int l = 0; l < L; ++l) {
+                uint32_t w0, w1;
+                o_threefry2x32(sc->skey[0], sc->skey[1], (uint32_t)i, ((uint32_t)t << 12) | (uint32_t)((k - 1) * L + l),
+                               &w0, &w1);
+                const int64_t prop = (int64_t)(((uint64_t)w0 * (uint64_t)n) >> 32);
+                const float E = o_bits_to_exponential(w1);
+                const float lp = o_score_lf(xi, mu + prop * MS, sc->iq, d);
+                if ((lp - lcur) + E > 0.0f) { cur = prop; lcur = lp; }
+            }
+            mk[k] = cur;
+        }
+        float e[4][64], v[4][64];
+        const float *xp[4], *tp[4];
+        for (int k = 0; k < K; ++k) {
+            jk[k] = anc ? anc[mk[k]] : mk[k];
+            xp[k] = xprev + jk[k] * d;
+            tp[k] = sc->tau_a + jk[k] * TS;
+            for (int r = 0; r < d; ++r) {
+                e[k][r] = xi[r] - mu[mk[k] * MS + r];
+                v[k][r] = e[k][r] * sc->iq[r];
+            }
+            if (sc->draws) sc->draws[(t * n + i) * K + k] = (int32_t)jk[k];
+        }
+        float *to = sc->tau_b + i * TS;
+        for (int q = 0; q < TS; ++q) {
+            float acc = 0.0f, out;
+            if (q < d * d) {
+                const int r = q / d, c = q % d;
+                for (int k = 0; k < K; ++k) { acc = acc + tp[k][q]; acc = acc + v[k][r] * xp[k][c]; }
+                out = acc * invK;
+            } else if (q < d * d + d) {
+                const int r = q - d * d;
+                for (int k = 0; k < K; ++k) { acc = acc + tp[k][q]; acc = acc + (e[k][r] * e[k][r] * sc->half_iq[r] - 0.5f); }
+                out = acc * invK;
+            } else if (q < sc->P) {
+                const int r = q - d * d - d;
+                for (int k = 0; k < K; ++k) acc = acc + tp[k][q];
+                float dr = yt[r] - xi[r];
+                out = acc * invK + (dr * dr * sc->half_ir[r] - 0.5f);
+            } else {
+                out = 0.0f;
+            }
+            to[q] = out;
+        }
+    }
+    float *tmp = sc->tau_a; sc->tau_a = sc->tau_b; sc->tau_b = tmp;
+}
+
+/* The score estimate of the filter run o_lg_run(md, n, T, key, y, ...) would
+ * make: grad (d*d + 2d doubles) = sum_i W^i tau^i (float64 sum in particle
+ * order) with W = exp(lw_{T-1} - LSE), plus log Z, ess, resampled as o_lg_run;
+ * draws (T, n, K) (row 0 untouched) may be NULL.  K in 1..4, (K-1) L < 4096. */
+double o_lg_score(const o_lg_model *md, int64_t n, int64_t T, const uint32_t *key, const uint32_t *skey,
+                  const float *y, float ess_threshold, int scheme, int K, int L, double *grad, float *ess_out,
+                  int32_t *resampled_out, int32_t *draws)
+{
+    const int d = md->d;
+    o_score_ctx sc;
+    sc.K = K; sc.L = L;
+    sc.skey[0] = skey[0]; sc.skey[1] = skey[1];
+    for (int r = 0; r < d; ++r) {
+        const double q = (double)md->Lq[r * d + r] * (double)md->Lq[r * d + r];
+        const double pr = (double)md->P[r * d + r];
+        sc.iq[r] = (float)(1.0 / q);
+        sc.half_iq[r] = (float)(0.5 / q);
+        sc.half_ir[r] = (float)(0.5 * pr * pr);
+    }
+    sc.P = d * d + 2 * d;
+    sc.TS = (sc.P + 3) / 4 * 4;
+    sc.tau_a = (float *)malloc(sizeof(float) * (size_t)n * sc.TS);
+    sc.tau_b = (float *)malloc(sizeof(float) * (size_t)n * sc.TS);
+    sc.mu = (float *)malloc(sizeof(float) * (size_t)n * (d + 1));
+    sc.draws = draws;
+    float *lw_last = (float *)malloc(sizeof(float) * (size_t)n);
+    sc.lw_last = lw_last;
+    double logZ = o_lg_run_impl(md, n, T, key, y, ess_threshold, scheme, ess_out, resampled_out, NULL, NULL, NULL, &sc);
+    double st[4];
+    o_lse_ess(lw_last, n, st);
+    for (int q = 0; q < sc.P; ++q) grad[q] = 0.0;
+    for (int64_t i = 0; i < n; ++i) {
+        const double w = exp((double)lw_last[i] - st[1]);
+        for (int q = 0; q < sc.P; ++q) grad[q] += w * (double)sc.tau_a[i * sc.TS + q];
+    }
+    free(sc.tau_a); free(sc.tau_b); free(sc.mu); free(lw_last);
+    return logZ;
+}
+
 static double o_lg_run_impl(const o_lg_model *md, int64_t n, int64_t T, const uint32_t *key, const float *y,
                             float ess_threshold, int scheme, float *ess_out, int32_t *resampled_out,
-                            float *x_hist, float *lw_hist, int32_t *anc_hist)
+                            float *x_hist, float *lw_hist, int32_t *anc_hist, o_score_ctx *sc)
 {
     const int d = md->d, dy = md->dy;
     float *xa = (float *)malloc(sizeof(float) * (size_t)(n * d));
@@ -381,6 +548,7 @@ static double o_lg_run_impl(const o_lg_model *md, int64_t n, int64_t T, const ui
     sk[0] = keys2[2]; sk[1] = keys2[3];
 
     o_lg_init(md, n, sk, y, xa, la);
+    if (sc) o_score_init(sc, md, n, xa, y);
     double st[4];
     o_lse_ess(la, n, st);
     double logn = log((double)n);
@@ -409,6 +577,7 @@ static double o_lg_run_impl(const o_lg_model *md, int64_t n, int64_t T, const ui
         }
         if (res && anc_hist) memcpy(anc_hist + t * n, anc, sizeof(int32_t) * (size_t)n);
         o_lg_propagate(md, n, kt, y + t * dy, xa, res ? anc : NULL, res ? NULL : la, xb, lb);
+        if (sc) o_score_step(sc, md, n, t, xa, xb, res ? anc : NULL, la, y + t * dy);
         o_lse_ess(lb, n, st);
         logZ += st[1] - (res ? logn : lse_prev);
         lse_prev = st[1];
@@ -420,6 +589,7 @@ static double o_lg_run_impl(const o_lg_model *md, int64_t n, int64_t T, const ui
         float *tp = xa; xa = xb; xb = tp;
         tp = la; la = lb; lb = tp;
     }
+    if (sc) memcpy(sc->lw_last, la, sizeof(float) * (size_t)n);
     free(tkeys);
     free(xa); free(xb); free(la); free(lb); free(anc);
     return logZ;
