@@ -28,9 +28,15 @@ JAX and is not installable here) on the same workload, all host threads.
 Multi-GPU (torchrun): independent replicas, one filter per rank, no
 collective on the data path; value = all ranks' particle-steps / max time.
 
-adjoint -- gradient evaluations per second of log Z with respect to
-(A, log diag Q, log diag R) at N = 65536, T = 1000 (checkpoint every 32
-steps), next to finite differences of the plain filter.
+adjoint -- gradient evaluations per second with respect to (A, log diag Q,
+log diag R) at N = 65536, T = 1000, each with its error against the exact
+Kalman score: the consistent Fisher-identity score smoothed by PaRIS (also at
+N = 2^20 and 8 at a time on 8 streams), the fixed-ancestor adjoint of log Z
+(checkpoint every 32 steps), and finite differences of the plain filter.
+
+Output: the contract's keys, then "legs": every sub-workload in short form
+(value, unit, e2e, roofline fraction, CPU baseline); the full object with all
+details is printed to stderr.
 
 smc_logreg -- the tempered SMC sampler on Bayesian logistic regression
 (1e5 x 50 data, 16384 particles per posterior, 256 posteriors): particle
@@ -246,10 +252,18 @@ def bench_sv_batch(args, flush, rank):
 
 
 def bench_adjoint(args, flush, rank):
-    """d log Z / d theta (theta = A, log diag Q, log diag R: 120 parameters) of the d = 10
-    filter at N = 65536, T = 1000, checkpoint every 32 steps: gradient evaluations per
-    second through the public call, against finite differences of the plain filter
-    (2 x 120 forward runs per gradient)."""
+    """Gradients of the d = 10 filter at N = 65536, T = 1000 with respect to theta =
+    (A, log diag Q, log diag R) (120 parameters): gradient evaluations per second through
+    the public calls, each with its error against the exact Kalman score (relative 2-norm):
+      score     -- Fisher identity smoothed by PaRIS (log_z_and_score, 2 backward draws,
+                   8 independent-Metropolis proposals each), consistent in N; also at N = 2^20;
+      pathwise  -- the adjoint of log Z with the ancestors held fixed (log_z_and_grad,
+                   checkpoint every 32 steps), which does not converge to the score;
+      plain_fd  -- the plain form: central finite differences of the plain filter's log Z
+                   with common random numbers, 2 x 120 sequential forward runs per gradient;
+      batched   -- 8 score evaluations on 8 streams (log_z_and_score_many).
+    cpu_baseline: the exact score by the float64 Kalman recursion on the host (the
+    oracle's), which is also the reference for every error figure."""
     import torch
     import mocat_gb300 as mg
     n, T = args.adj_n, args.adj_T
@@ -257,48 +271,95 @@ def bench_adjoint(args, flush, rank):
     ssm = mg.ssm.TimeHomogenousLinearGaussian(**a)
     y = ssm.simulate(np.arange(T), mg.random.PRNGKey(0)).y.contiguous()
     key = mg.random.PRNGKey(1 + rank)
-    o = mg.adjoint.log_z_and_grad(ssm, y, key, n, ckpt_every=32)
-    torch.cuda.synchronize()
-    ts = []
-    for _ in range(max(3, args.steps)):
-        flush.zero_()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        o = mg.adjoint.log_z_and_grad(ssm, y, key, n, ckpt_every=32)
-        torch.cat([o.grad_transition_matrix.reshape(-1), o.grad_log_transition_covariance_diag,
-                   o.grad_log_likelihood_covariance_diag]).cpu()
-        ts.append(time.perf_counter() - t0)
-    t_grad = statistics.median(ts)
-    # batched: 8 evaluations (different keys) on 8 streams, enqueued from 8 host threads
-    kb = np.stack([np.array([0, 100 + 8 * rank + b], np.uint32) for b in range(8)])
-    mg.adjoint.log_z_and_grad_many(ssm, y, kb, n, ckpt_every=32, max_concurrent=8).grad.cpu()
-    tb = []
-    for _ in range(3):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        mg.adjoint.log_z_and_grad_many(ssm, y, kb, n, ckpt_every=32, max_concurrent=8).grad.cpu()
-        tb.append(time.perf_counter() - t0)
-    t_batch = statistics.median(tb)
-    # plain form: one forward filter run (persistent kernel) per finite-difference point
-    fw = []
-    for _ in range(3):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        f = mg.ssm.run_particle_filter_for_marginals(ssm, mg.ssm.BootstrapFilter(), y, np.arange(T), key, n=n,
-                                                     history=False)
-        float(f.log_z)
-        fw.append(time.perf_counter() - t0)
-    t_fwd = statistics.median(fw)
     npar = D * D + 2 * D
+    K, L = 2, 8
+
+    def flat(o):
+        return torch.cat([o.grad_transition_matrix.reshape(-1), o.grad_log_transition_covariance_diag,
+                          o.grad_log_likelihood_covariance_diag])
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        ts, outs = [], []
+        for _ in range(reps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            g = fn().cpu()
+            ts.append(time.perf_counter() - t0)
+            outs.append(g.double().numpy())
+        return statistics.median(ts), outs
+
+    t_path, g_path = timed(lambda: flat(mg.adjoint.log_z_and_grad(ssm, y, key, n, ckpt_every=32)), max(3, args.steps))
+    t_score, _ = timed(lambda: mg.adjoint.log_z_and_score(ssm, y, key, n, K, L).grad, max(3, args.steps))
+    score_keys = [mg.random.PRNGKey(500 + 10 * rank + s) for s in range(3)]
+    g_score = [mg.adjoint.log_z_and_score(ssm, y, k, n, K, L).grad.double().cpu().numpy() for k in score_keys]
+    nb = 1 << 20
+    t_big, _ = timed(lambda: mg.adjoint.log_z_and_score(ssm, y, key, nb, K, L).grad, 2)
+    g_big = [mg.adjoint.log_z_and_score(ssm, y, k, nb, K, L).grad.double().cpu().numpy() for k in score_keys[:2]]
+    # batched: 8 score evaluations (different keys) on 8 streams, enqueued from 8 host threads
+    kb = np.stack([np.array([0, 100 + 8 * rank + b], np.uint32) for b in range(8)])
+    t_batch, _ = timed(lambda: mg.adjoint.log_z_and_score_many(ssm, y, kb, n, K, L, max_concurrent=8).grad, 3)
+    # plain form: one forward filter run (persistent kernel) per finite-difference point
+    t_fwd, _ = timed(lambda: mg.ssm.run_particle_filter_for_marginals(ssm, mg.ssm.BootstrapFilter(), y, np.arange(T),
+                                                                      key, n=n, history=False).log_z.reshape(1), 3)
+    g_fd = None
+    if rank == 0:
+        # one full finite-difference gradient (same key: common random numbers), for its error
+        h = 1e-3
+        A0 = np.asarray(a["transition_matrix"], np.float64)
+        lq0 = np.log(np.diag(np.asarray(a["transition_covariance"], np.float64)))
+        lr0 = np.log(np.diag(np.asarray(a["likelihood_covariance"], np.float64)))
+        th0 = np.concatenate([A0.reshape(-1), lq0, lr0])
+
+        def lz(th):
+            m = mg.ssm.TimeHomogenousLinearGaussian(a["initial_mean"], a["initial_covariance"],
+                                                    th[:D * D].reshape(D, D), np.diag(np.exp(th[D * D:D * D + D])),
+                                                    a["likelihood_matrix"], np.diag(np.exp(th[D * D + D:])))
+            return float(mg.ssm.run_particle_filter_for_marginals(m, mg.ssm.BootstrapFilter(), y, np.arange(T), key,
+                                                                  n=n, history=False).log_z)
+        g_fd = np.empty(npar)
+        for j in range(npar):
+            e = np.zeros(npar)
+            e[j] = h
+            g_fd[j] = (lz(th0 + e) - lz(th0 - e)) / (2 * h)
     res = {"workload": f"d={D} linear-Gaussian (bench model), N={n}, T={T}, theta=(A, log diag Q, log diag R) "
-                       f"= {npar} parameters, ancestors held fixed, checkpoint every 32 steps",
-           "metric": "grad-evals/s", "value": 1.0 / t_grad, "unit": "grad-evals/s", "s_per_grad": t_grad,
-           "particle_steps_per_s_forward_plus_backward": n * T / t_grad,
-           "plain_fd": {"forward_s": t_fwd, "runs_per_grad": 2 * npar, "value": 1.0 / (2 * npar * t_fwd),
-                        "unit": "grad-evals/s"},
-           "speedup_vs_plain_fd": 2 * npar * t_fwd / t_grad,
-           "batched": {"evaluations": 8, "streams": 8, "value": 8.0 / t_batch, "unit": "grad-evals/s",
-                       "speedup_vs_plain_fd": 8.0 / t_batch * 2 * npar * t_fwd}}
+                       f"= {npar} parameters",
+           "metric": "grad-evals/s", "unit": "grad-evals/s",
+           "score": {"value": 1.0 / t_score, "n": n, "backward_draws": K, "mcmc_steps": L, "s_per_grad": t_score},
+           "score_n1M": {"value": 1.0 / t_big, "n": nb, "s_per_grad": t_big},
+           "pathwise": {"value": 1.0 / t_path, "s_per_grad": t_path, "checkpoint_every": 32},
+           "plain_fd": {"value": 1.0 / (2 * npar * t_fwd), "forward_s": t_fwd, "runs_per_grad": 2 * npar,
+                        "step": 1e-3},
+           "batched": {"evaluations": 8, "streams": 8, "value": 8.0 / t_batch, "estimator": "score"}}
+    res["value"] = res["score"]["value"]
+    if rank == 0:
+        from oracle import kalman
+        th = (np.asarray(a["transition_matrix"], np.float64),
+              np.log(np.diag(np.asarray(a["transition_covariance"], np.float64))), np.eye(D),
+              np.log(np.diag(np.asarray(a["likelihood_covariance"], np.float64))), np.zeros(D), np.eye(D),
+              y.double().cpu().numpy())
+        t0 = time.perf_counter()
+        _, g_ex = kalman.loglik_and_grad(*th)
+        dtk = time.perf_counter() - t0
+
+        def err(g):
+            return float(np.linalg.norm(g - g_ex) / np.linalg.norm(g_ex))
+        res["score"]["err_vs_kalman"] = float(np.mean([err(g) for g in g_score]))
+        res["score_n1M"]["err_vs_kalman"] = float(np.mean([err(g) for g in g_big]))
+        res["pathwise"]["err_vs_kalman"] = err(g_path[0])
+        res["plain_fd"]["err_vs_kalman"] = err(g_fd)
+        res["err_unit"] = "relative 2-norm distance to the exact Kalman score"
+        # the score at N reaches an error at or below the plain form's: its speed-up there
+        if res["score"]["err_vs_kalman"] <= res["plain_fd"]["err_vs_kalman"]:
+            res["speedup_vs_plain_fd_at_no_worse_error"] = res["score"]["value"] / res["plain_fd"]["value"]
+            res["batched_speedup_vs_plain_fd_at_no_worse_error"] = res["batched"]["value"] / res["plain_fd"]["value"]
+        e2 = res["score_n1M"]["err_vs_kalman"]
+        res["score_n_for_1e-3_extrapolated"] = float(nb * (e2 / 1e-3) ** 2)
+        res["cpu_baseline"] = {"value": 1.0 / dtk, "unit": "grad-evals/s", "cores": 1, "kind": "port",
+                               "sample": f"exact score by the float64 Kalman recursion with {npar} tangent "
+                                         f"directions, T={T} ({dtk:.1f} s; oracle numpy)"}
     return res
 
 
@@ -503,9 +564,10 @@ def bench_abc(args, rank):
         dtc = time.perf_counter() - t0
         simc = sum(n if ref["resampled"][k] else round(float(ref["ess"][k - 1]))
                    for k in range(1, ref["iterations"] + 1))
-        r["cpu_baseline"] = {"value": simc / dtc, "unit": "simulations/s", "cores": 1, "kind": "port",
+        r["cpu_baseline"] = {"value": simc / dtc, "unit": "simulations/s", "cores": oracle.num_threads(),
+                             "kind": "port",
                              "sample": f"one posterior, N={n}, {ref['iterations']} iterations ({dtc:.1f} s), "
-                                       "oracle C (one thread)"}
+                                       "oracle C/OpenMP (particle loops on all host threads)"}
     return r
 
 
@@ -801,12 +863,44 @@ def run_reference(args, rank):
     line = {"metric": METRIC, "value": v, "unit": "particle-steps/s", "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": args.n * steps_per_sample / v * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "sample": f"N=2^20, {steps_per_sample} filter steps per bench step"},
+            "config": {"workload": WORKLOAD, "sample": f"N=2^20, {steps_per_sample} of the T=1000 filter steps per "
+                                                       "bench step (throughput per particle-step is independent of "
+                                                       "T)", "same_config": False},
             "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": cores, "kind": "port",
                              "sample": f"N={args.n}, {steps_per_sample} steps of the same filter (oracle C/OpenMP "
                                        "restatement; the reference is JAX, not installable here)"},
             "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
+
+
+def _r(v):
+    return float(f"{v:.4g}") if isinstance(v, float) else v
+
+
+def _compact_leg(name, d):
+    """value, unit, e2e, roofline fraction and CPU baseline of one sub-workload (the
+    full object goes to stderr)."""
+    c = {"value": _r(d.get("value")), "unit": d.get("unit")}
+    if isinstance(d.get("e2e"), dict):
+        c["e2e"] = _r(d["e2e"].get("value"))
+    if isinstance(d.get("roofline"), dict):
+        c["frac"] = _r(d["roofline"].get("frac"))
+        c["bound"] = d["roofline"].get("bound")
+    if name == "config1":
+        c = {"us_per_step": _r(d.get("us_per_step_device")), "e2e_us_per_step": _r(d.get("us_per_step_e2e"))}
+    if name == "adjoint":
+        for k in ("score", "score_n1M", "pathwise", "plain_fd"):
+            if k in d:
+                c[k] = {"value": _r(d[k].get("value")), "err": _r(d[k].get("err_vs_kalman"))}
+        c["batched"] = _r(d.get("batched", {}).get("value"))
+        for k in ("speedup_vs_plain_fd_at_no_worse_error", "batched_speedup_vs_plain_fd_at_no_worse_error",
+                  "score_n_for_1e-3_extrapolated"):
+            if k in d:
+                c[k] = _r(d[k])
+    if isinstance(d.get("cpu_baseline"), dict):
+        cb = d["cpu_baseline"]
+        c["cpu"] = {"value": _r(cb.get("value")), "cores": cb.get("cores"), "kind": cb.get("kind")}
+    return c
 
 
 def main():
@@ -1036,6 +1130,16 @@ def main():
         v_cpu, cores, dt = cpu_baseline(n, args.cpu_steps)
         line["cpu_baseline"] = {"value": v_cpu, "unit": "particle-steps/s", "cores": cores, "kind": "port",
                                 "sample": f"N={n}, {args.cpu_steps} filter steps ({dt:.1f} s), oracle C/OpenMP"}
+        # the full object (every sub-workload's details) on stderr; on stdout the contract's
+        # keys first and the sub-workloads last, in short form, so that a kept tail of the
+        # line holds all of them
+        print(json.dumps(line), file=sys.stderr, flush=True)
+        legs = {}
+        for name in ("config1", "batched_sv", "adjoint", "smc_logreg", "nl1d", "abc_smc", "abc_gk"):
+            if name in line:
+                legs[name] = _compact_leg(name, line.pop(name))
+        line["roofline"].pop("issue_bound_note", None)
+        line["legs"] = legs
         print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()

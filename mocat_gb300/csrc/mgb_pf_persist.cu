@@ -35,20 +35,20 @@
 #include "mgb_nl1d.cuh"
 #include "mgb_sv.cuh"
 
-// co-resident CTAs per SM the persistent kernel is compiled for (a register budget
-// of 65536 / (256 x this) per thread)
-#ifndef MGB_PERSIST_MIN_BLOCKS
-#define MGB_PERSIST_MIN_BLOCKS 2
-#endif
-
 namespace mgb {
 
 // err is the kernel's own (never null) error word: once a wait has run out,
 // later barriers stop waiting and the step loop exits, so a fault can cost at
-// most one bounded wait.
-__device__ __forceinline__ void grid_sync(GridBar *bar, unsigned nblocks, int *err, int limit = BAR_SPIN_LIMIT) {
+// most one bounded wait.  Returns true (in every thread of the block) when this
+// block left the barrier without every block having arrived: its wait ran out,
+// or another block's had.  Only thread 0 reads the error word; the result
+// reaches the other threads through shared memory at the closing __syncthreads,
+// so a normal pass adds no global load.
+__device__ __forceinline__ bool grid_sync(GridBar *bar, unsigned nblocks, int *err, int limit = BAR_SPIN_LIMIT) {
+  __shared__ int gs_out;
   __syncthreads();
   if (threadIdx.x == 0) {
+    int out = 0;
     volatile unsigned int *vgen = &bar->gen;
     const unsigned int g = *vgen;
     __threadfence();
@@ -58,16 +58,23 @@ __device__ __forceinline__ void grid_sync(GridBar *bar, unsigned nblocks, int *e
       atomicAdd(&bar->gen, 1u);
     } else {
       int polls = 0;
-      while (*vgen == g && !(*(volatile int *)err & EB_TIMEOUT)) {
+      while (*vgen == g) {
+        if (*(volatile int *)err & EB_TIMEOUT) {
+          out = 1;
+          break;
+        }
         if (++polls > limit) {
           atomicOr(err, EB_TIMEOUT);
+          out = 1;
           break;
         }
       }
     }
     __threadfence();
+    gs_out = out;
   }
   __syncthreads();
+  return gs_out != 0;
 }
 
 __device__ __forceinline__ uint64_t globaltimer_ns() {
@@ -212,7 +219,7 @@ struct LGModelP {
 };
 
 template <class MP>
-__global__ void __launch_bounds__(PP_TPB, MGB_PERSIST_MIN_BLOCKS) k_pf_persist(const __grid_constant__ MP p,
+__global__ void __launch_bounds__(PP_TPB, 2) k_pf_persist(const __grid_constant__ MP p,
                                                            const __grid_constant__ PersistArgs a) {
   constexpr int D = MP::kD, DY = MP::kDY;
   __shared__ float smf[PP_TPB / 32];
@@ -304,8 +311,8 @@ __global__ void __launch_bounds__(PP_TPB, MGB_PERSIST_MIN_BLOCKS) k_pf_persist(c
     }
     if (a.trace && t == 1 && threadIdx.x == 0) a.trace[a.T * 10 + blockIdx.x] = globaltimer_ns() - t0;
     stamp(a, t, 1);
-    grid_sync(a.bar, G, a.err);
-    if (timed_out(a.err)) break;  // no phase runs on data a timed-out barrier did not order
+    // no phase runs on data that a barrier which did not complete failed to order
+    if (grid_sync(a.bar, G, a.err)) break;
     stamp(a, t, 2);
 
     // ---- P2: combine (identical in every block)
@@ -369,8 +376,7 @@ __global__ void __launch_bounds__(PP_TPB, MGB_PERSIST_MIN_BLOCKS) k_pf_persist(c
         for (int j = 0; j < SCAN_IPT; ++j) v[j] = w[j];
       }
       stamp(a, t, 4);
-      grid_sync(a.bar, G, a.err);
-      if (timed_out(a.err)) break;
+      if (grid_sync(a.bar, G, a.err)) break;
       stamp(a, t, 5);
 
       // ---- P4: scan tile sums, place outputs, fill units
@@ -446,8 +452,7 @@ __global__ void __launch_bounds__(PP_TPB, MGB_PERSIST_MIN_BLOCKS) k_pf_persist(c
         }
       }
       stamp(a, t, 7);
-      grid_sync(a.bar, G, a.err);
-      if (timed_out(a.err)) break;
+      if (grid_sync(a.bar, G, a.err)) break;
       stamp(a, t, 8);
     }
     res_cur = res_next;

@@ -47,6 +47,15 @@ def random_bits(key, shape=()):
     return _draw("mgb_random_bits", key, shape, torch.uint32)
 
 
+def normal_keys(keys, d):
+    """normal(keys[i], (d,)) for every key of a (n, 2) key array, as one (n, d) draw:
+    the batched form of the per-particle draws of a vmapped plugin method."""
+    keys = _dev.as_key(keys).reshape(-1, 2).contiguous()
+    out = torch.empty((keys.shape[0], int(d)), dtype=torch.float32, device=keys.device)
+    call("mgb_normal_keys", _dev.ptr(keys), keys.shape[0], int(d), _dev.ptr(out), _dev.stream_ptr())
+    return out
+
+
 def uniform(key, shape=(), minval=0.0, maxval=1.0):
     u = _draw("mgb_uniform", key, shape, torch.float32)
     if minval == 0.0 and maxval == 1.0:

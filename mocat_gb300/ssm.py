@@ -285,6 +285,19 @@ def _normal_keys(keys, d):
 
 
 class ParticleFilter:
+    """Plugin interface of mocat/src/ssm/filtering.py:20-139.
+
+    The built-in models run on fused CUDA kernels.  Any other model or filter runs
+    through the generic driver (run_particle_filter_for_marginals and friends), which
+    calls the two vectorised methods below with the whole particle batch as torch
+    tensors on the GPU and does the rest (keys, logsumexp / ESS, resampling, gather,
+    log Z) with the library's kernels.  Where the reference vmaps a per-particle
+    method, the GPU plugin receives the batch: a model's initial_sample(t, random_keys),
+    transition_sample(x_previous, t_previous, t_new, random_keys) and
+    likelihood_potential(x, y, t) take x of shape (n, d) and random_keys of shape (n, 2)
+    (uint32, jax's key layout; mocat_gb300.random.normal_keys draws from them) and
+    return (n, d) / (n,) float32 CUDA tensors.  A filter may instead override the two
+    vectorised methods."""
     name = "Particle Filter"
 
     def __init__(self, name=None):
@@ -296,6 +309,20 @@ class ParticleFilter:
 
     def startup(self, ssm_scenario):
         pass
+
+    def initial_sample_and_weight_vectorised(self, ssm_scenario, y, t, random_keys):
+        """filtering.py:65-78 with the batch: (x (n, d), log_weight (n,))."""
+        x = ssm_scenario.initial_sample(t, random_keys)
+        if y is None:
+            return x, torch.zeros(x.shape[0], dtype=torch.float32, device=x.device)
+        return x, -ssm_scenario.likelihood_potential(x, y, t)
+
+    def propose_and_intermediate_weight_vectorised(self, ssm_scenario, x_previous, t_previous, y_new, t_new,
+                                                   random_keys):
+        """filtering.py:124-139 for the bootstrap proposal (filtering.py:142-170): the
+        transition's draw, weighted by the likelihood."""
+        x_new = ssm_scenario.transition_sample(x_previous, t_previous, t_new, random_keys)
+        return x_new, -ssm_scenario.likelihood_potential(x_new, y_new, t_new)
 
 
 class BootstrapFilter(ParticleFilter):
@@ -352,6 +379,25 @@ class OptimalNonLinearGaussianParticleFilter(ParticleFilter):
                                      c["C0c"].ctypes.data, c["m0"].ctypes.data)
 
 
+def _overrides(obj, base, names):
+    return any(getattr(type(obj), m, None) is not getattr(base, m, None) for m in names)
+
+
+def _fused(ssm_scenario, particle_filter):
+    """True when a fused kernel runs this model / filter pair: a built-in model (or a
+    subclass that keeps its plugin methods) with a built-in filter (or a subclass that
+    keeps its vectorised methods).  False routes the pair to the generic driver."""
+    pf_base = next((b for b in (OptimalNonLinearGaussianParticleFilter, BootstrapFilter)
+                    if isinstance(particle_filter, b)), None)
+    if pf_base is None or _overrides(particle_filter, pf_base, ("initial_sample_and_weight_vectorised",
+                                                                  "propose_and_intermediate_weight_vectorised")):
+        return False
+    for base in (TimeHomogenousLinearGaussian, StochasticVolatility, NonLinear1DBenchmark):
+        if isinstance(ssm_scenario, base):
+            return not _overrides(ssm_scenario, base, ("initial_sample", "transition_sample", "likelihood_potential"))
+    return False
+
+
 def _check_lg(ssm_scenario, particle_filter):
     if isinstance(ssm_scenario, StochasticVolatility):
         if type(particle_filter) is not BootstrapFilter:
@@ -392,6 +438,8 @@ def _y2(y, dy):
 
 def initiate_particles(ssm_scenario, particle_filter, n, random_key, y=None, t=None):
     """filtering.py:173-193: particles (1, n, d), log-weights (1, n), ess (1,)."""
+    if not _fused(ssm_scenario, particle_filter):
+        return _initiate_generic(ssm_scenario, particle_filter, n, random_key, y, t)
     _check_lg(ssm_scenario, particle_filter)
     particle_filter.startup(ssm_scenario)
     prefix, s = _kernels(ssm_scenario, particle_filter)
@@ -449,6 +497,9 @@ def _step(s, n, key, y_t, x_prev_soa, anc, lw_prev, prefix="mgb_pf_lg", t_prev=N
 def propagate_particle_filter(ssm_scenario, particle_filter, particles, y_new, t_new, random_key,
                               ess_threshold=0.5, resample_full=True, resampling="systematic"):
     """filtering.py:220-252: resample if ess < threshold n, then propagate and append."""
+    if not _fused(ssm_scenario, particle_filter):
+        return _propagate_generic(ssm_scenario, particle_filter, particles, y_new, t_new, random_key, ess_threshold,
+                                  resample_full, resampling)
     _check_lg(ssm_scenario, particle_filter)
     prefix, s = _kernels(ssm_scenario, particle_filter)
     n = particles.value.shape[1]
@@ -477,8 +528,13 @@ def run_particle_filter_for_marginals(ssm_scenario, particle_filter, y, t, rando
     persistent=False forces one kernel launch per phase and step instead of the
     single persistent launch (bootstrap filter on the linear-Gaussian or the
     non-linear benchmark model, systematic resampling, even n <= 2^21); results
-    are the same.
+    are the same.  A model or filter without a fused kernel runs through the
+    generic driver (ParticleFilter's vectorised plugin methods, the library's
+    logsumexp / resampling / gather kernels); persistent is then ignored.
     """
+    if not _fused(ssm_scenario, particle_filter):
+        return _run_generic(ssm_scenario, particle_filter, y, t, random_key, n, initial_sample, ess_threshold,
+                            resampling, history)
     _check_lg(ssm_scenario, particle_filter)
     particle_filter.startup(ssm_scenario)
     prefix, s = _kernels(ssm_scenario, particle_filter)
@@ -521,6 +577,131 @@ def run_particle_filter_for_marginals(ssm_scenario, particle_filter, y, t, rando
     tt = torch.as_tensor(np.asarray(t if not isinstance(t, torch.Tensor) else t.cpu()), device=dev)
     return cdict(value=xh.permute(0, 2, 1), log_weight=lh, ess=ess, t=tt, y=y2, log_z=logz[0],
                  resampled=res.bool(), degenerate=bool(e & 2))
+
+
+# ---------------------------------------------------------------- generic driver
+def _lse_ess(lw):
+    """(LSE, ESS) of log-weights on the device (mgb_lse_ess), as float64 device scalars."""
+    n = lw.numel()
+    ws = _dev.workspace(_lib.lib().mgb_lse_ess_workspace(n), lw.device)
+    out = torch.empty(4, dtype=torch.float64, device=lw.device)
+    call("mgb_lse_ess", _dev.ptr(lw), n, _dev.ptr(out), _dev.ptr(ws), ws.numel(), _dev.stream_ptr())
+    return out[1], out[3]
+
+
+def _plugin_xw(x, lw, n, where):
+    """the plugin's (x, log_weight) as contiguous float32 device tensors (n, d), (n,)."""
+    if not isinstance(x, torch.Tensor) or not x.is_cuda or not isinstance(lw, torch.Tensor) or not lw.is_cuda:
+        raise _lib.MGBError(1, f"{where}: the plugin must return CUDA tensors (no host path)")
+    x = x.to(torch.float32)
+    if x.dim() == 1:
+        x = x[:, None]
+    lw = lw.to(torch.float32).reshape(-1)
+    if x.shape[0] != n or lw.numel() != n:
+        raise ValueError(f"{where}: plugin returned {tuple(x.shape)} / {tuple(lw.shape)} for n = {n}")
+    return x.contiguous(), lw.contiguous()
+
+
+def _gather(x, anc):
+    out = torch.empty_like(x)
+    call("mgb_gather_rows", _dev.ptr(x), x.shape[1], _dev.ptr(anc), x.shape[0], _dev.ptr(out), _dev.stream_ptr())
+    return out
+
+
+def _initiate_generic(ssm_scenario, particle_filter, n, random_key, y=None, t=None):
+    particle_filter.startup(ssm_scenario)
+    dev = _dev.device()
+    sub_keys = mrandom.split(_dev.as_key(random_key), n)
+    yd = None if y is None else _dev.as_f32(y).reshape(-1)
+    x, lw = _plugin_xw(*particle_filter.initial_sample_and_weight_vectorised(ssm_scenario, yd, t, sub_keys), n,
+                       "initial_sample_and_weight_vectorised")
+    _, ess = _lse_ess(lw)
+    return cdict(value=x[None], log_weight=lw[None],
+                 t=torch.atleast_1d(torch.as_tensor(0.0 if t is None else t, device=dev)),
+                 y=None if yd is None else yd[None], ess=ess.float().reshape(1))
+
+
+def _generic_step(ssm_scenario, particle_filter, x, lw, ess, n, key, y_t, t_prev, t_new, ess_threshold, resampling):
+    """One body of the reference's scan (filtering.py:280-311): resample on the
+    previous ESS, propagate with split(k_t, n), add the carried log-weight."""
+    res = bool(np.float32(float(ess)) < np.float32(ess_threshold) * np.float32(n))
+    if res:
+        anc = resample(lw, key, resampling)
+        x_res, lw_res = _gather(x, anc), torch.zeros_like(lw)
+    else:
+        x_res, lw_res = x, lw
+    keys = mrandom.split(key, n)
+    x_new, lw_inc = _plugin_xw(*particle_filter.propose_and_intermediate_weight_vectorised(
+        ssm_scenario, x_res, t_prev, y_t, t_new, keys), n, "propose_and_intermediate_weight_vectorised")
+    return x_new, lw_res + lw_inc, res
+
+
+def _propagate_generic(ssm_scenario, particle_filter, particles, y_new, t_new, random_key, ess_threshold=0.5,
+                       resample_full=True, resampling="systematic"):
+    n = particles.value.shape[1]
+    key = _dev.as_key(random_key)
+    if float(particles.ess[-1]) < ess_threshold * n:
+        particles = resample_particles(particles, key, resample_full, resampling)
+    x_prev = particles.value[-1].contiguous()
+    lw_prev = particles.log_weight[-1].contiguous()
+    y_t = _dev.as_f32(y_new).reshape(-1)
+    keys = mrandom.split(key, n)
+    x_new, lw_inc = _plugin_xw(*particle_filter.propose_and_intermediate_weight_vectorised(
+        ssm_scenario, x_prev, particles.t[-1], y_t, t_new, keys), n, "propose_and_intermediate_weight_vectorised")
+    lw_new = lw_prev + lw_inc
+    out = particles.copy()
+    out.value = torch.cat([particles.value, x_new[None]], 0)
+    out.log_weight = torch.cat([particles.log_weight, lw_new[None]], 0)
+    out.y = torch.cat([particles.y, y_t[None]], 0) if particles.y is not None else y_t[None]
+    out.t = torch.cat([particles.t, torch.atleast_1d(torch.as_tensor(t_new, device=out.t.device)).to(out.t.dtype)])
+    out.ess = torch.cat([particles.ess, ess_log_weight(lw_new).reshape(1).float()])
+    return out
+
+
+def _run_generic(ssm_scenario, particle_filter, y, t, random_key, n=None, initial_sample=None, ess_threshold=0.5,
+                 resampling="systematic", history=True):
+    """run_particle_filter_for_marginals (filtering.py:255-324) for a user model or filter:
+    the key schedule, ESS trigger, key reuse (k_t resamples and seeds split(k_t, n)) and
+    log-weight carry of the reference; the plugin's vectorised methods propagate and weight."""
+    particle_filter.startup(ssm_scenario)
+    dev = _dev.device()
+    y2 = _dev.as_f32(y)
+    if y2.dim() == 1:
+        y2 = y2[:, None]
+    t_np = np.asarray(t.cpu() if isinstance(t, torch.Tensor) else t, np.float32).reshape(-1)
+    key = _dev.as_key(random_key)
+    if initial_sample is None:
+        k2 = mrandom.split(key)
+        key, sub = k2[0].contiguous(), k2[1].contiguous()
+        initial_sample = _initiate_generic(ssm_scenario, particle_filter, n, sub, y2[0], float(t_np[0]))
+        y2, t_np = y2[1:], t_np[1:]
+    x = initial_sample.value[-1].contiguous()
+    lw = initial_sample.log_weight[-1].contiguous()
+    n = lw.numel()
+    lse_prev, ess = _lse_ess(lw)
+    logz = lse_prev - math.log(n)
+    t_prev = float(initial_sample.t[-1])
+    Tp = y2.shape[0]
+    keys = mrandom.split(key, Tp) if Tp else None
+    xs, lws, esss, resd = [x], [lw], [ess.float()], [False]
+    for i in range(Tp):
+        x, lw, res = _generic_step(ssm_scenario, particle_filter, x, lw, ess, n, keys[i].contiguous(),
+                                   y2[i].contiguous(), t_prev, float(t_np[i]), ess_threshold, resampling)
+        lse, ess = _lse_ess(lw)
+        logz = logz + lse - (math.log(n) if res else lse_prev)
+        lse_prev = lse
+        t_prev = float(t_np[i])
+        if history:
+            xs.append(x)
+            lws.append(lw)
+        esss.append(ess.float())
+        resd.append(res)
+    value = torch.stack(xs) if history else x[None]
+    log_weight = torch.stack(lws) if history else lw[None]
+    tt = torch.cat([initial_sample.t.to(torch.float32), torch.as_tensor(t_np, device=dev)])
+    yy = torch.cat([initial_sample.y, y2]) if initial_sample.y is not None else y2
+    return cdict(value=value, log_weight=log_weight, ess=torch.stack(esss), t=tt, y=yy, log_z=logz.reshape(()),
+                 resampled=torch.tensor(resd, device=dev))
 
 
 def _run_from(ssm_scenario, s, initial_sample, y2, t, key, ess_threshold, resampling, prefix="mgb_pf_lg"):

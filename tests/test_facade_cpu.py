@@ -44,3 +44,26 @@ def test_sv_smoothing_checks():
         mg.ssm._check_smoother(ssm, mg.ssm.OptimalNonLinearGaussianParticleFilter())
     phi, pq = ssm.transition_constants()
     assert phi == 1.0 and pq == 1.0
+
+
+def test_fused_routing():
+    """built-in models with built-in filters stay on the fused kernels; subclasses that keep
+    the plugin methods too; overriding a plugin method, or a model of the user's own,
+    routes to the generic driver"""
+    import mocat_gb300 as mg
+    lg = mg.ssm.TimeHomogenousLinearGaussian(np.zeros(2), np.eye(2), 0.5 * np.eye(2), np.eye(2), np.eye(2), np.eye(2))
+    assert mg.ssm._fused(lg, mg.ssm.BootstrapFilter())
+
+    class Named(mg.ssm.TimeHomogenousLinearGaussian):
+        name = "mine"
+    assert mg.ssm._fused(Named(np.zeros(2), np.eye(2), 0.5 * np.eye(2), np.eye(2), np.eye(2), np.eye(2)),
+                         mg.ssm.BootstrapFilter())
+
+    class MyBoot(mg.ssm.BootstrapFilter):
+        def propose_and_intermediate_weight_vectorised(self, *a):
+            return super().propose_and_intermediate_weight_vectorised(*a)
+    assert not mg.ssm._fused(lg, MyBoot())
+
+    class Mine(mg.ssm.StateSpaceModel):
+        dim = dim_obs = 1
+    assert not mg.ssm._fused(Mine(), mg.ssm.BootstrapFilter())
