@@ -89,12 +89,24 @@ __device__ __forceinline__ void stamp(const PersistArgs &a, int64_t t, int k) {
 
 __device__ __forceinline__ bool timed_out(const int *err) { return (*(volatile const int *)err & EB_TIMEOUT) != 0; }
 
+// warp partial of per-lane online accumulators: lane 0's value of a fixed
+// shuffle tree (each lane's order is fixed, so lane 0's result does not depend
+// on timing)
+__device__ __forceinline__ LsePartial warp_online_partial(float m, float s1, float s2, int nanf) {
+  const float Mw = warp_max(m);
+  const float f = (m > -INFINITY && Mw < INFINITY) ? expf(m - Mw) : 0.0f;
+  const float b1 = warp_sum<float>(s1 * f);
+  const float b2 = warp_sum<float>(s2 * (f * f));
+  const int bn = __any_sync(0xffffffffu, nanf);
+  return LsePartial{Mw, b1, b2, bn};
+}
+
 // Fixed-order combine of the chunk partials (identical in every block): float
 // shuffle trees only -- FP64 throughput is low on this part and this runs in
 // every block every step.  Logarithms in float; log Z accumulates in float64.
 template <int TPB>
 __device__ __forceinline__ LseOut combine_chunks(const LsePartial *parts, int np, float *smf, LseOut *res_s) {
-  // up to 8 partials per thread stay in registers between the max and the sums
+  // up to 10 partials per thread stay in registers between the max and the sums
   // (one L2 round trip); more chunks than that are read twice
   constexpr int PER = 8;
   const bool one_pass = np <= PER * TPB;
@@ -228,13 +240,14 @@ __global__ void __launch_bounds__(PP_TPB, 2) k_pf_persist(const __grid_constant_
   __shared__ int32_t sK[PP_MAX_TILES + 1];
   __shared__ int32_t sU[PP_MAX_TILES + 1];
   __shared__ LseOut res_s;
-  __shared__ int chunk_s;
   __shared__ float y_s[DY];
   __shared__ uint64_t sC[SCAN_TILE];
   __shared__ ResampleCtl sc;
   const unsigned G = gridDim.x;
   const int64_t n = a.n, h = n >> 1;
-  const int nchunks = (int)((h + PP_TPB - 1) / PP_TPB);
+  const int lane = threadIdx.x & 31;
+  const int64_t wid = (int64_t)blockIdx.x * (PP_TPB / 32) + (threadIdx.x >> 5);
+  const int nwarps = (int)G * (PP_TPB / 32);  // one LSE partial per warp (<= PP_MAX_CHUNKS)
   const int ntiles = (int)((n + SCAN_TILE - 1) / SCAN_TILE);
   const float scale = __int_as_float((weight_shift(n) + 127) << 23);
   int res_cur = 0;
@@ -256,58 +269,60 @@ __global__ void __launch_bounds__(PP_TPB, 2) k_pf_persist(const __grid_constant_
     const float *y = y_s;
     LsePartial *parts = a.parts + (t & 1) * PP_MAX_CHUNKS;
 
-    // ---- P1: propagate + weight, 256-pair chunks taken from a per-step
-    // counter (SMs that run ahead take more chunks); one partial per chunk, so
-    // the combine does not depend on which block ran which chunk
+    // ---- P1: propagate + weight.  Warp w of the W warps of the grid takes the
+    // 32-pair rounds w, w + W, w + 2W, ... (a static assignment: each warp's
+    // partial covers a fixed set of particles in a fixed order, so the combine
+    // does not depend on timing), each lane keeps an online (max, sum e, sum e^2)
+    // across its rounds, and the warp writes one partial.  No block-wide barrier
+    // inside the phase: a warp never waits for the block's slowest warp.
+    __syncthreads();  // y_s
     const uint64_t t0 = (a.trace && t == 1 && threadIdx.x == 0) ? globaltimer_ns() : 0;
-    for (;;) {
-      if (threadIdx.x == 0) chunk_s = atomicAdd(&a.chunk_ctr[t], 1);
-      __syncthreads();
-      const int c = chunk_s;
-      if (c >= nchunks) break;
-      const int64_t i = (int64_t)c * PP_TPB + threadIdx.x;
+    {
       float m = -INFINITY, s1 = 0.0f, s2 = 0.0f;
       int nanf = 0;
-      if (i < h && t == 0) {
-        uint32_t r0, r1, q0, q1;
-        threefry2x32_m(k0, k1, (uint32_t)(2 * i), (uint32_t)(2 * i + n), p.one(), r0, r1);
-        threefry2x32_m(k0, k1, (uint32_t)(2 * i + 1), (uint32_t)(2 * i + 1 + n), p.one(), q0, q1);
+      for (int64_t base = wid * 32; base < h; base += nwarps * 32) {
+        const int64_t i = base + lane;
+        if (i < h && t == 0) {
+          uint32_t r0, r1, q0, q1;
+          threefry2x32_m(k0, k1, (uint32_t)(2 * i), (uint32_t)(2 * i + n), p.one(), r0, r1);
+          threefry2x32_m(k0, k1, (uint32_t)(2 * i + 1), (uint32_t)(2 * i + 1 + n), p.one(), q0, q1);
 #pragma unroll 1
-        for (int s = 0; s < 2; ++s) {
-          const float l = p.init(n, s ? r1 : r0, s ? q1 : q0, s ? i + h : i, y, xo, lo);
-          online_acc(l, m, s1, s2, nanf);
-        }
-      } else if (i < h) {
-        // both particles' ancestors and source states are requested before the
-        // key-split ciphers run, so the cipher arithmetic hides the gather latency
-        // ancestors of this step (from the tape when one is recorded)
-        const int32_t *anc_t = a.anc_hist ? a.anc_hist + (size_t)t * n : a.anc;
-        const int64_t sa = res_cur ? (int64_t)__ldcg(&anc_t[i]) : i;
-        const int64_t sb = res_cur ? (int64_t)__ldcg(&anc_t[i + h]) : i + h;
-        float xa_[D], xb_[D];
+          for (int s = 0; s < 2; ++s) {
+            const float l = p.init(n, s ? r1 : r0, s ? q1 : q0, s ? i + h : i, y, xo, lo);
+            online_acc(l, m, s1, s2, nanf);
+          }
+        } else if (i < h) {
+          // both particles' ancestors and source states are requested before the
+          // key-split ciphers run, so the cipher arithmetic hides the gather latency
+          // ancestors of this step (from the tape when one is recorded)
+          const int32_t *anc_t = a.anc_hist ? a.anc_hist + (size_t)t * n : a.anc;
+          const int64_t sa = res_cur ? (int64_t)__ldcg(&anc_t[i]) : i;
+          const int64_t sb = res_cur ? (int64_t)__ldcg(&anc_t[i + h]) : i + h;
+          float xa_[D], xb_[D];
 #pragma unroll
-        for (int j = 0; j < D; ++j) {
-          xa_[j] = __ldcg(&xi[j * n + sa]);
-          xb_[j] = __ldcg(&xi[j * n + sb]);
-        }
-        const float la_ = res_cur ? 0.0f : __ldcg(&li[i]);
-        const float lb_ = res_cur ? 0.0f : __ldcg(&li[i + h]);
-        uint32_t r0, r1, q0, q1;
-        threefry2x32_m(k0, k1, (uint32_t)(2 * i), (uint32_t)(2 * i + n), p.one(), r0, r1);
-        threefry2x32_m(k0, k1, (uint32_t)(2 * i + 1), (uint32_t)(2 * i + 1 + n), p.one(), q0, q1);
-        // the pair runs as a two-trip loop (not unrolled): one copy of the
-        // particle code keeps the hot loop inside the instruction cache
+          for (int j = 0; j < D; ++j) {
+            xa_[j] = __ldcg(&xi[j * n + sa]);
+            xb_[j] = __ldcg(&xi[j * n + sb]);
+          }
+          const float la_ = res_cur ? 0.0f : __ldcg(&li[i]);
+          const float lb_ = res_cur ? 0.0f : __ldcg(&li[i + h]);
+          uint32_t r0, r1, q0, q1;
+          threefry2x32_m(k0, k1, (uint32_t)(2 * i), (uint32_t)(2 * i + n), p.one(), r0, r1);
+          threefry2x32_m(k0, k1, (uint32_t)(2 * i + 1), (uint32_t)(2 * i + 1 + n), p.one(), q0, q1);
+          // the pair runs as a two-trip loop (not unrolled): one copy of the
+          // particle code keeps the hot loop inside the instruction cache
 #pragma unroll 1
-        for (int s = 0; s < 2; ++s) {
-          float xs[D];
+          for (int s = 0; s < 2; ++s) {
+            float xs[D];
 #pragma unroll
-          for (int j = 0; j < D; ++j) xs[j] = s ? xb_[j] : xa_[j];
-          const float l = p.step(n, s ? r1 : r0, s ? q1 : q0, s ? i + h : i, xs, s ? lb_ : la_, y, aux, xo, lo);
-          online_acc(l, m, s1, s2, nanf);
+            for (int j = 0; j < D; ++j) xs[j] = s ? xb_[j] : xa_[j];
+            const float l = p.step(n, s ? r1 : r0, s ? q1 : q0, s ? i + h : i, xs, s ? lb_ : la_, y, aux, xo, lo);
+            online_acc(l, m, s1, s2, nanf);
+          }
         }
       }
-      const LsePartial part = block_online_partial<PP_TPB>(m, s1, s2, nanf, smf);
-      if (threadIdx.x == 0) parts[c] = part;
+      const LsePartial part = warp_online_partial(m, s1, s2, nanf);
+      if (lane == 0) parts[wid] = part;
     }
     if (a.trace && t == 1 && threadIdx.x == 0) a.trace[a.T * 10 + blockIdx.x] = globaltimer_ns() - t0;
     stamp(a, t, 1);
@@ -316,7 +331,7 @@ __global__ void __launch_bounds__(PP_TPB, 2) k_pf_persist(const __grid_constant_
     stamp(a, t, 2);
 
     // ---- P2: combine (identical in every block)
-    const LseOut o = combine_chunks<PP_TPB>(parts, nchunks, smf, &res_s);
+    const LseOut o = combine_chunks<PP_TPB>(parts, nwarps, smf, &res_s);
     logz = t == 0 ? o.lse - a.logn : logz + o.lse - (res_cur ? a.logn : lse_prev);
     lse_prev = o.lse;
     const int res_next = ((float)o.ess < a.thr_n) ? 1 : 0;
@@ -494,7 +509,8 @@ static int launch_persist(const MP &p, const PersistArgs &args, cudaStream_t s) 
   // no more blocks than there are 256-pair propagate chunks: a small filter's grid
   // barriers then span a few blocks instead of every co-resident one
   const int64_t chunks = (args.n / 2 + PP_TPB - 1) / PP_TPB;
-  const int64_t cap = (int64_t)sms * per_sm;
+  int64_t cap = (int64_t)sms * per_sm;
+  if (cap * (PP_TPB / 32) > PP_MAX_CHUNKS) cap = PP_MAX_CHUNKS / (PP_TPB / 32);  // one LSE partial per warp
   const dim3 grid((unsigned)(chunks < cap ? (chunks > 0 ? chunks : 1) : cap)), block(PP_TPB);
   if (cudaLaunchCooperativeKernel((void *)k_pf_persist<MP>, grid, block, kargs, 0, s) != cudaSuccess)
     return ERR_LAUNCH;

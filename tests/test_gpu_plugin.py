@@ -25,7 +25,8 @@ pytestmark = pytest.mark.gpu
 def _user_lg1d(F, Q, H, R, m0, S0):
     """the user's model: the reference's TimeHomogenousLinearGaussian for d = 1, in torch"""
     import mocat_gb300 as mg
-    p = models.lg_params(m0, S0, F, Q, H, R)
+    one = np.eye(1)
+    p = models.lg_params(np.full(1, m0), S0 * one, F * one, Q * one, H * one, R * one)
     f32 = np.float32
 
     class UserLG1D(mg.ssm.StateSpaceModel):
