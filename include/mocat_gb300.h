@@ -239,6 +239,19 @@ int mgb_pf_lg_score(const mgb_lg_model *model_host, int64_t n, int64_t T, const 
                     int32_t backward_draws, int32_t mcmc_steps, void *ws_dev, size_t ws_bytes, double *log_z_dev,
                     float *grad_dev, int32_t *resampled_dev, int32_t *draws_dev, void *stream);
 
+/* mgb_pf_lg_score for B filters at once (keys_dev and smoothing_keys_dev: (B, 2)),
+ * one launch per phase and step for all B: every per-step kernel runs one
+ * filter per grid row on that filter's workspace slab, so B latency-bound
+ * filters share each launch.  Systematic resampling, even n.  Each filter's
+ * log Z and score equal those of mgb_pf_lg_score with its keys, bit for bit.
+ * log_z_dev: B doubles (may be NULL); grad_dev: (B, d*d + 2d) floats.
+ * No counterpart in the reference beyond mgb_pf_lg_score's (one filter per call there). */
+size_t mgb_pf_lg_score_batch_workspace(int64_t n, int64_t T, int32_t d, int64_t B);
+int mgb_pf_lg_score_batch(const mgb_lg_model *model_host, int64_t n, int64_t T, int64_t B, const uint32_t *keys_dev,
+                          const uint32_t *smoothing_keys_dev, const float *y_dev, float ess_threshold,
+                          int32_t backward_draws, int32_t mcmc_steps, void *ws_dev, size_t ws_bytes, double *log_z_dev,
+                          float *grad_dev, void *stream);
+
 /* --------------------------------------------- backward simulation (FFBSi)
  * backward_simulation with maximum_rejections = 0, i.e. backward_simulation_full
  * (mocat/src/ssm/backward.py:217-245, full_resampling :20-40), for a linear-Gaussian

@@ -145,6 +145,9 @@ _SIGNATURES = {
                        _I32),
     "mgb_wait_selftest_workspace": ([], _SZ),
     "mgb_wait_selftest": ([ctypes.c_int, ctypes.c_int32, _P, _SZ, _P], _I32),
+    "mgb_pf_lg_score_batch_workspace": ([_I64, _I64, ctypes.c_int32, _I64], _SZ),
+    "mgb_pf_lg_score_batch": ([ctypes.POINTER(LGModel), _I64, _I64, _I64, _P, _P, _P, _F, ctypes.c_int32,
+                               ctypes.c_int32, _P, _SZ, _P, _P, _P], _I32),
     "mgb_pf_lg_score_workspace": ([_I64, _I64, ctypes.c_int32], _SZ),
     "mgb_pf_lg_score": ([ctypes.POINTER(LGModel), _I64, _I64, _P, _P, _P, _F, _I32, ctypes.c_int32, ctypes.c_int32, _P,
                          _SZ, _P, _P, _P, _P, _P], _I32),

@@ -208,6 +208,36 @@ def log_z_and_grad_many(ssm_scenario, y, random_keys, n, ess_threshold=0.5, resa
     return cdict(log_z=logz, grad=grad)
 
 
+def log_z_and_score_batched(ssm_scenario, y, random_keys, n, backward_draws=2, mcmc_steps=8, smoothing_keys=None,
+                            ess_threshold=0.5):
+    """log_z_and_score for B filter keys in one library call (mgb_pf_lg_score_batch): every
+    per-step kernel runs all B filters, one per grid row, so filters too small to fill the
+    GPU share each launch.  Systematic resampling, even n; the same values as B calls of
+    log_z_and_score (smoothing_keys default to default_smoothing_key of each filter key).
+
+    Returns cdict(log_z (B,), grad (B, d*d + 2d)) in the layout of mgb_pf_lg_score."""
+    if not isinstance(ssm_scenario, TimeHomogenousLinearGaussian):
+        raise NotImplementedError(f"{ssm_scenario.__class__.__name__}: no score kernel for this model")
+    d = ssm_scenario.dim
+    if d not in SUPPORTED_D:
+        raise NotImplementedError(f"score for d = {d} not compiled (supported {SUPPORTED_D})")
+    _, s = ssm_scenario.derived()
+    dev = _dev.device()
+    keys = _dev.as_key(random_keys).reshape(-1, 2).contiguous()
+    B = keys.shape[0]
+    skeys = (torch.stack([default_smoothing_key(keys[b]) for b in range(B)]).contiguous() if smoothing_keys is None
+             else _dev.as_key(smoothing_keys).reshape(-1, 2).contiguous())
+    y2 = _dev.as_f32(y).reshape(-1, d).contiguous()
+    T = y2.shape[0]
+    ws = _dev.workspace(_lib.lib().mgb_pf_lg_score_batch_workspace(n, T, d, B), dev)
+    logz = torch.empty(B, dtype=torch.float64, device=dev)
+    grad = torch.empty((B, d * d + 2 * d), dtype=torch.float32, device=dev)
+    call("mgb_pf_lg_score_batch", ctypes.byref(s), n, T, B, _dev.ptr(keys), _dev.ptr(skeys), _dev.ptr(y2),
+         float(ess_threshold), int(backward_draws), int(mcmc_steps), _dev.ptr(ws), ws.numel(), _dev.ptr(logz),
+         _dev.ptr(grad), _dev.stream_ptr())
+    return cdict(log_z=logz, grad=grad)
+
+
 def log_z_and_score_many(ssm_scenario, y, random_keys, n, backward_draws=2, mcmc_steps=8, smoothing_keys=None,
                          ess_threshold=0.5, resampling="systematic", max_concurrent=8):
     """log_z_and_score for B filter keys at once: each evaluation runs on its own CUDA

@@ -76,12 +76,11 @@ __global__ void __launch_bounds__(PF_TPB) k_lg_step(const __grid_constant__ LGP<
 // particle i + n/2 is the .x1 halves of the same two cipher calls, so the
 // pair costs two key-split evaluations instead of four.
 template <int D, int DY, bool FUSED>
-__global__ void __launch_bounds__(PF_TPB, 2) k_lg_step2(const __grid_constant__ LGP<D, DY> p, int64_t n,
-                                                         const uint32_t *key, const float *y_t,
-                                                         const float *__restrict__ x_prev, const int32_t *anc,
-                                                         const float *lw_prev, const int32_t *res_flag,
-                                                         float *__restrict__ x_new, float *__restrict__ lw_new,
-                                                         PFCtl ctl, int64_t t) {
+__device__ __forceinline__ void lg_step2_body(const LGP<D, DY> &p, int64_t n, const uint32_t *key, const float *y_t,
+                                              const float *__restrict__ x_prev, const int32_t *anc,
+                                              const float *lw_prev, const int32_t *res_flag,
+                                              float *__restrict__ x_new, float *__restrict__ lw_new,
+                                              const PFCtl &ctl, int64_t t) {
   const int64_t h = n >> 1;
   const int64_t i = blockIdx.x * (int64_t)PF_TPB + threadIdx.x;
   const bool res = res_flag ? (*res_flag != 0) : (anc != nullptr);
@@ -105,6 +104,15 @@ __global__ void __launch_bounds__(PF_TPB, 2) k_lg_step2(const __grid_constant__ 
     }
   }
   if (FUSED) pf_reduce_online<PF_TPB>(m, a1, a2, nanf, ctl, t);
+}
+template <int D, int DY, bool FUSED>
+__global__ void __launch_bounds__(PF_TPB, 2) k_lg_step2(const __grid_constant__ LGP<D, DY> p, int64_t n,
+                                                         const uint32_t *key, const float *y_t,
+                                                         const float *__restrict__ x_prev, const int32_t *anc,
+                                                         const float *lw_prev, const int32_t *res_flag,
+                                                         float *__restrict__ x_new, float *__restrict__ lw_new,
+                                                         PFCtl ctl, int64_t t) {
+  lg_step2_body<D, DY, FUSED>(p, n, key, y_t, x_prev, anc, lw_prev, res_flag, x_new, lw_new, ctl, t);
 }
 
 }  // namespace mgb

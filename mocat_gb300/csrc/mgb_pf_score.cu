@@ -36,6 +36,7 @@
 // (mu_m, lb_m) and the statistics tau are particle-major so that a randomly
 // indexed row is a few contiguous 32-byte sectors.
 #include <cmath>
+#include <type_traits>
 
 #include "mgb_internal.cuh"
 #include "mgb_resample.cuh"
@@ -43,6 +44,7 @@
 #include "mgb_lg.cuh"
 #include "mgb_pf_common.cuh"
 #include "mgb_lg_kernels.cuh"
+#include "mgb_systematic.cuh"
 
 namespace mgb {
 
@@ -122,10 +124,9 @@ __global__ void __launch_bounds__(SC_TPB) k_score_init(const __grid_constant__ S
 
 // proposal rows of step t: mu_m = A x_{t-1}^{src(m)} (the transition's fma chain), lb_m
 template <int D>
-__global__ void __launch_bounds__(SC_TPB) k_score_mu(const __grid_constant__ ScoreP<D> c, int64_t n,
-                                                      const float *__restrict__ xprev, const int32_t *anc,
-                                                      const int32_t *res_flag, const float *lw_prev,
-                                                      float *__restrict__ mu) {
+__device__ __forceinline__ void score_mu_body(const ScoreP<D> &c, int64_t n, const float *__restrict__ xprev,
+                                              const int32_t *anc, const int32_t *res_flag, const float *lw_prev,
+                                              float *__restrict__ mu) {
   using S = ScoreDims<D>;
   const int64_t m = blockIdx.x * (int64_t)SC_TPB + threadIdx.x;
   if (m >= n) return;
@@ -150,10 +151,17 @@ __global__ void __launch_bounds__(SC_TPB) k_score_mu(const __grid_constant__ Sco
   for (int j = 0; j < S::MS / 4; ++j) o[j] = make_float4(row[4 * j], row[4 * j + 1], row[4 * j + 2], row[4 * j + 3]);
 }
 
+template <int D>
+__global__ void __launch_bounds__(SC_TPB) k_score_mu(const __grid_constant__ ScoreP<D> c, int64_t n,
+                                                      const float *__restrict__ xprev, const int32_t *anc,
+                                                      const int32_t *res_flag, const float *lw_prev,
+                                                      float *__restrict__ mu) {
+  score_mu_body<D>(c, n, xprev, anc, res_flag, lw_prev, mu);
+}
+
 // one PaRIS step: backward draws, then tau_t^i
 template <int D>
-__global__ void __launch_bounds__(SC_TPB) k_score_step(const __grid_constant__ ScoreP<D> c, int64_t n,
-                                                        const ScoreStep a) {
+__device__ __forceinline__ void score_step_body(const ScoreP<D> &c, int64_t n, const ScoreStep &a) {
   using S = ScoreDims<D>;
   constexpr int B = 4;  // independent proposals evaluated together (their loads overlap)
   const int64_t i = blockIdx.x * (int64_t)SC_TPB + threadIdx.x;
@@ -272,6 +280,12 @@ __global__ void __launch_bounds__(SC_TPB) k_score_step(const __grid_constant__ S
   }
 }
 
+template <int D>
+__global__ void __launch_bounds__(SC_TPB) k_score_step(const __grid_constant__ ScoreP<D> c, int64_t n,
+                                                        const ScoreStep a) {
+  score_step_body<D>(c, n, a);
+}
+
 // partial[b][q] = sum over block b's particles of W_i tau_i[q] (float64, fixed order)
 constexpr int SC_SUM_TPB = 128;
 constexpr int SC_SUM_CHUNK = 256;
@@ -314,6 +328,20 @@ __global__ void k_score_sum(const double *partial, int nb, int P, float *grad) {
 
 constexpr int SC_SUM_BLOCKS = 2 * kNumSMs;
 
+template <int D>
+static ScoreP<D> make_score_params(const LGP<D, D> &p) {
+  ScoreP<D> c;
+  for (int i = 0; i < D * D; ++i) c.F[i] = p.F[i];
+  for (int r = 0; r < D; ++r) {
+    const double q = (double)p.Lq[r * D + r] * (double)p.Lq[r * D + r];
+    const double pr = (double)p.P[r * D + r];
+    c.iq[r] = (float)(1.0 / q);
+    c.half_iq[r] = (float)(0.5 / q);
+    c.half_ir[r] = (float)(0.5 * pr * pr);
+  }
+  return c;
+}
+
 struct ScoreWs {
   RunWs run;
   float *tau_a, *tau_b;
@@ -345,15 +373,7 @@ static int score_lg(const mgb_lg_model *m, int64_t n, int64_t T, const uint32_t 
   using S = ScoreDims<D>;
   const LGP<D, D> p = pack_lg<D, D>(m);
   if (!p.lq_diag || !p.p_diag || !p.h_eye) return ERR_UNSUPPORTED;
-  ScoreP<D> c;
-  for (int i = 0; i < D * D; ++i) c.F[i] = p.F[i];
-  for (int r = 0; r < D; ++r) {
-    const double q = (double)p.Lq[r * D + r] * (double)p.Lq[r * D + r];
-    const double pr = (double)p.P[r * D + r];
-    c.iq[r] = (float)(1.0 / q);
-    c.half_iq[r] = (float)(0.5 / q);
-    c.half_ir[r] = (float)(0.5 * pr * pr);
-  }
+  const ScoreP<D> c = make_score_params<D>(p);
   Carver cv(ws);
   ScoreWs w = carve_score(cv, n, T, D, scheme);
   if (cv.bytes() > ws_bytes) return ERR_WORKSPACE;
@@ -426,11 +446,230 @@ static int score_lg(const mgb_lg_model *m, int64_t n, int64_t T, const uint32_t 
   return launch_status();
 }
 
+
+// ------------------------------------------------------------ many filters
+// mgb_pf_lg_score_batch runs B filters, each with its own workspace slab of
+// `ws` bytes laid out exactly as filter 0's, so every per-filter pointer is
+// filter 0's plus b * ws bytes.  The per-step kernels take filter 0's pointers
+// and run one filter per grid row (blockIdx.y = b) with the same code as the
+// single-filter kernels; the observations and the model are shared.
+template <class T>
+__device__ __forceinline__ T *slab(T *p, int64_t off) {
+  return p ? reinterpret_cast<T *>(reinterpret_cast<char *>(const_cast<typename std::remove_const<T>::type *>(p)) +
+                                   off)
+           : nullptr;
+}
+__device__ __forceinline__ PFCtl slab_ctl(const PFCtl &c, int64_t o) {
+  PFCtl r = c;
+  r.parts = slab(c.parts, o);
+  r.counter = slab(c.counter, o);
+  r.st = slab(c.st, o);
+  r.ess_hist = slab(c.ess_hist, o);
+  r.res_hist = slab(c.res_hist, o);
+  r.rctl = slab(c.rctl, o);
+  r.rstatus = slab(c.rstatus, o);
+  r.rstatus2 = slab(c.rstatus2, o);
+  r.logz_out = nullptr;
+  return r;
+}
+
+__global__ void __launch_bounds__(SCAN_TPB) k_tile_sums_b(const float *lw, int64_t n, const float *Mptr,
+                                                           const uint32_t *key, const int32_t *flag, ResampleCtl *ctl,
+                                                           uint64_t *tile_pfx, uint64_t *units, int64_t ws) {
+  const int64_t o = (int64_t)blockIdx.y * ws;
+  tile_sums_body(slab(lw, o), n, slab(Mptr, o), slab(key, o), 0, 0u, slab(flag, o), slab(ctl, o), slab(tile_pfx, o),
+                 slab(units, o));
+}
+__global__ void __launch_bounds__(SCAN_TPB) k_systematic_b(const float *lw, int64_t n, const float *Mptr,
+                                                            const int32_t *flag, const ResampleCtl *ctl,
+                                                            const uint64_t *tile_pfx, const uint64_t *units,
+                                                            int32_t *anc, int64_t ws) {
+  const int64_t o = (int64_t)blockIdx.y * ws;
+  systematic_body(slab(lw, o), n, slab(Mptr, o), slab(flag, o), slab(ctl, o), slab(tile_pfx, o), slab(units, o),
+                  slab(anc, o), nullptr);
+}
+template <int D>
+__global__ void __launch_bounds__(PF_TPB, 2) k_lg_step2_b(const __grid_constant__ LGP<D, D> p, int64_t n,
+                                                           const uint32_t *key, const float *y_t, const float *x_prev,
+                                                           const int32_t *anc, const float *lw_prev,
+                                                           const int32_t *res_flag, float *x_new, float *lw_new,
+                                                           PFCtl ctl, int64_t t, int64_t ws) {
+  const int64_t o = (int64_t)blockIdx.y * ws;
+  lg_step2_body<D, D, true>(p, n, slab(key, o), y_t, slab(x_prev, o), slab(anc, o), slab(lw_prev, o),
+                            slab(res_flag, o), slab(x_new, o), slab(lw_new, o), slab_ctl(ctl, o), t);
+}
+template <int D>
+__global__ void __launch_bounds__(SC_TPB) k_score_mu_b(const __grid_constant__ ScoreP<D> c, int64_t n,
+                                                        const float *xprev, const int32_t *anc, const int32_t *res_flag,
+                                                        const float *lw_prev, float *mu, int64_t ws) {
+  const int64_t o = (int64_t)blockIdx.y * ws;
+  score_mu_body<D>(c, n, slab(xprev, o), slab(anc, o), slab(res_flag, o), slab(lw_prev, o), slab(mu, o));
+}
+template <int D>
+__global__ void __launch_bounds__(SC_TPB) k_score_step_b(const __grid_constant__ ScoreP<D> c, int64_t n,
+                                                          const ScoreStep a0, int64_t ws) {
+  const int64_t o = (int64_t)blockIdx.y * ws;
+  ScoreStep a = a0;
+  a.x = slab(a0.x, o);
+  a.xprev = slab(a0.xprev, o);
+  a.mu = slab(a0.mu, o);
+  a.anc = slab(a0.anc, o);
+  a.res = slab(a0.res, o);
+  a.tau_prev = slab(a0.tau_prev, o);
+  a.tau = slab(a0.tau, o);
+  a.skey = slab(a0.skey, o);
+  a.draws = nullptr;
+  score_step_body<D>(c, n, a);
+}
+
+// a filter's slab: the single-filter workspace plus its smoothing key
+static size_t score_slab_bytes(int64_t n, int64_t T, int d) {
+  Carver c(nullptr);
+  carve_score(c, n, T, d, MGB_RESAMPLE_SYSTEMATIC);
+  c.take<uint32_t>(2);
+  return c.bytes();
+}
+
+template <int D>
+static int score_lg_batch(const mgb_lg_model *m, int64_t n, int64_t T, int64_t B, const uint32_t *keys,
+                          const uint32_t *skeys, const float *y, float thr, int K, int L, void *ws, size_t ws_bytes,
+                          double *logz_out, float *grad_out, cudaStream_t s) {
+  using S = ScoreDims<D>;
+  const LGP<D, D> p = pack_lg<D, D>(m);
+  if (!p.lq_diag || !p.p_diag || !p.h_eye) return ERR_UNSUPPORTED;
+  const ScoreP<D> c = make_score_params<D>(p);
+  const int64_t W = (int64_t)score_slab_bytes(n, T, D);
+  if ((size_t)(W * B) > ws_bytes) return ERR_WORKSPACE;
+  char *base = (char *)ws;
+  Carver c0(base);
+  ScoreWs w0 = carve_score(c0, n, T, D, MGB_RESAMPLE_SYSTEMATIC);
+  uint32_t *sk0 = c0.take<uint32_t>(2);
+  RunWs &r0 = w0.run;
+  int st;
+  auto ctl_of = [&](const RunWs &r) {
+    PFCtl ctl;
+    ctl.parts = r.parts;
+    ctl.counter = r.counter;
+    ctl.st = r.st;
+    ctl.ess_hist = r.ess_hist;
+    ctl.res_hist = r.res_hist;
+    ctl.rctl = r.rws.ctl;
+    ctl.rstatus = r.rws.status;
+    ctl.rstatus2 = r.rws.status2;
+    ctl.ntiles = (int)r.rws.ntiles;
+    ctl.thr_n = thr * (float)n;
+    ctl.logn = log((double)n);
+    ctl.logz_out = nullptr;
+    return ctl;
+  };
+  const unsigned grid = (unsigned)((n + PF_TPB - 1) / PF_TPB);
+  const unsigned grid2 = (unsigned)((n / 2 + PF_TPB - 1) / PF_TPB);
+  const unsigned gs = (unsigned)((n + SC_TPB - 1) / SC_TPB);
+  const unsigned tiles = (unsigned)((n + SCAN_TILE - 1) / SCAN_TILE);
+  // per-filter set-up: state, keys, initial particles and statistics
+  for (int64_t b = 0; b < B; ++b) {
+    Carver cb(base + b * W);
+    ScoreWs w = carve_score(cb, n, T, D, MGB_RESAMPLE_SYSTEMATIC);
+    uint32_t *skb = cb.take<uint32_t>(2);
+    RunWs &r = w.run;
+    if (cudaMemsetAsync(r.st, 0, sizeof(PFState), s) != cudaSuccess) return ERR_CUDA;
+    if (cudaMemsetAsync(r.counter, 0, sizeof(unsigned int), s) != cudaSuccess) return ERR_CUDA;
+    if (cudaMemsetAsync(r.res_hist, 0, sizeof(int32_t) * (T + 1), s) != cudaSuccess) return ERR_CUDA;
+    if ((st = reset_resample(r.rws, s))) return st;
+    if (cudaMemcpyAsync(skb, skeys + 2 * b, 2 * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+      return ERR_CUDA;
+    if ((st = launch_setup_keys(keys + 2 * b, T, r.keys, s))) return st;
+    k_lg_init<D, D, true><<<grid, PF_TPB, 0, s>>>(p, n, r.keys, y, r.xa, r.la, ctl_of(r));
+    k_score_init<D><<<gs, SC_TPB, 0, s>>>(c, n, r.xa, y, w.tau_a);
+    if ((st = launch_status())) return st;
+  }
+  const PFCtl ctl0 = ctl_of(r0);
+  float *xa = r0.xa, *xb = r0.xb, *la = r0.la, *lb = r0.lb;
+  float *ta = w0.tau_a, *tb = w0.tau_b;
+  ScoreStep a;
+  a.skey = sk0;
+  a.K = K;
+  a.L = L;
+  a.invK = (float)(1.0 / K);
+  a.draws = nullptr;
+  const dim3 gB(1, (unsigned)B);
+  for (int64_t t = 1; t < T; ++t) {
+    k_tile_sums_b<<<dim3(tiles, (unsigned)B), SCAN_TPB, 0, s>>>(la, n, &r0.st->M, r0.keys + 2 * t, r0.res_hist + t,
+                                                                r0.rws.ctl, r0.rws.status, r0.rws.status2, W);
+    k_systematic_b<<<dim3(2 * tiles, (unsigned)B), SCAN_TPB, 0, s>>>(la, n, &r0.st->M, r0.res_hist + t, r0.rws.ctl,
+                                                                     r0.rws.status, r0.rws.status2, r0.anc, W);
+    k_lg_step2_b<D><<<dim3(grid2, (unsigned)B), PF_TPB, 0, s>>>(p, n, r0.keys + 2 * t, y + (size_t)t * D, xa, r0.anc,
+                                                                la, r0.res_hist + t, xb, lb, ctl0, t, W);
+    k_score_mu_b<D><<<dim3(gs, (unsigned)B), SC_TPB, 0, s>>>(c, n, xa, r0.anc, r0.res_hist + t, la, w0.mu, W);
+    a.x = xb;
+    a.xprev = xa;
+    a.mu = w0.mu;
+    a.anc = r0.anc;
+    a.res = r0.res_hist + t;
+    a.tau_prev = ta;
+    a.tau = tb;
+    a.y = y + (size_t)t * D;
+    a.t = (uint32_t)t;
+    k_score_step_b<D><<<dim3(gs, (unsigned)B), SC_TPB, 0, s>>>(c, n, a, W);
+    if ((st = launch_status())) return st;
+    float *tp = xa; xa = xb; xb = tp;
+    tp = la; la = lb; lb = tp;
+    tp = ta; ta = tb; tb = tp;
+  }
+  (void)gB;
+  // per-filter results: log Z, then the weighted sum of the statistics
+  const int64_t off_la = (char *)la - base, off_ta = (char *)ta - base;
+  for (int64_t b = 0; b < B; ++b) {
+    Carver cb(base + b * W);
+    ScoreWs w = carve_score(cb, n, T, D, MGB_RESAMPLE_SYSTEMATIC);
+    const float *lab = (const float *)(base + b * W + off_la);
+    const float *tab = (const float *)(base + b * W + off_ta);
+    if ((st = launch_finish(w.run.st, w.run.res_hist, T, logz_out ? logz_out + b : nullptr, nullptr, s))) return st;
+    if ((st = mgb_lse_ess(lab, n, w.lse4, w.lse_ws, w.lse_bytes, s))) return st;
+    const int64_t nchunks = (n + SC_SUM_CHUNK - 1) / SC_SUM_CHUNK;
+    const unsigned nb = (unsigned)(nchunks < SC_SUM_BLOCKS ? nchunks : SC_SUM_BLOCKS);
+    k_score_wsum<D><<<nb, SC_SUM_TPB, 0, s>>>(n, lab, w.lse4 + 1, tab, w.partial);
+    k_score_sum<<<1, 128, 0, s>>>(w.partial, (int)nb, S::P, grad_out + b * S::P);
+    if ((st = launch_status())) return st;
+  }
+  return OK;
+}
 }  // namespace mgb
 
 using namespace mgb;
 
 extern "C" {
+
+size_t mgb_pf_lg_score_batch_workspace(int64_t n, int64_t T, int32_t d, int64_t B) {
+  if (n < 1 || T < 1 || d < 1 || B < 1) return 0;
+  return score_slab_bytes(n, T, d) * (size_t)B;
+}
+
+int mgb_pf_lg_score_batch(const mgb_lg_model *m, int64_t n, int64_t T, int64_t B, const uint32_t *keys,
+                          const uint32_t *smoothing_keys, const float *y, float ess_threshold, int32_t backward_draws,
+                          int32_t mcmc_steps, void *ws, size_t ws_bytes, double *log_z, float *grad, void *stream) {
+  if (!m || !m->F || !m->Lq || !m->H || !m->P || !m->C0 || !m->m0 || n < 2 || n > 0x7FFFFFFFll || T < 1 ||
+      T > (1 << 20) || B < 1 || B > 65535 || !keys || !smoothing_keys || !y || !ws || !grad || backward_draws < 1 ||
+      backward_draws > SC_KMAX || mcmc_steps < 0 || (int64_t)(backward_draws - 1) * mcmc_steps > 4096)
+    return ERR_BAD_ARG;
+  if (m->dy != m->d || n % 2 != 0) return ERR_UNSUPPORTED;
+  cudaStream_t s = (cudaStream_t)stream;
+#define MGB_SCORE_BATCH_CASE(DD)                                                                               \
+  case DD:                                                                                                     \
+    return score_lg_batch<DD>(m, n, T, B, keys, smoothing_keys, y, ess_threshold, backward_draws, mcmc_steps, ws, \
+                              ws_bytes, log_z, grad, s);
+  switch (m->d) {
+    MGB_SCORE_BATCH_CASE(1)
+    MGB_SCORE_BATCH_CASE(2)
+    MGB_SCORE_BATCH_CASE(3)
+    MGB_SCORE_BATCH_CASE(4)
+    MGB_SCORE_BATCH_CASE(5)
+    MGB_SCORE_BATCH_CASE(8)
+    MGB_SCORE_BATCH_CASE(10)
+    default: return ERR_UNSUPPORTED;
+  }
+#undef MGB_SCORE_BATCH_CASE
+}
 
 size_t mgb_pf_lg_score_workspace(int64_t n, int64_t T, int32_t d) {
   if (n < 1 || T < 1 || d < 1) return 0;

@@ -103,3 +103,18 @@ def test_many_concurrent_scores_equal_single_calls(cuda):
         o = mg.adjoint.log_z_and_score(ssm, y, keys[b], 4096, backward_draws=3, mcmc_steps=4)
         assert float(o.log_z) == float(many.log_z[b])
         assert torch.equal(o.grad, many.grad[b])
+
+
+@pytest.mark.parametrize("d,n,T,B,K,L,thr", [(10, 4096, 40, 5, 2, 8, 0.5), (3, 2048, 30, 3, 4, 3, 0.8),
+                                             (1, 1000, 25, 2, 1, 0, 1.1)])
+def test_batched_scores_equal_single_calls(cuda, d, n, T, B, K, L, thr):
+    """one call for B filters (one launch per phase and step for all of them) gives each
+    filter's log Z and score bit for bit"""
+    import mocat_gb300 as mg
+    A, q, r, p, y, ssm = _setup(d, T, 4)
+    keys = np.stack([O.PRNGKey(20 + s) for s in range(B)])
+    bat = mg.adjoint.log_z_and_score_batched(ssm, y, keys, n, backward_draws=K, mcmc_steps=L, ess_threshold=thr)
+    for b in range(B):
+        o = mg.adjoint.log_z_and_score(ssm, y, keys[b], n, backward_draws=K, mcmc_steps=L, ess_threshold=thr)
+        assert float(o.log_z) == float(bat.log_z[b])
+        assert torch.equal(o.grad, bat.grad[b])
