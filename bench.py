@@ -735,7 +735,7 @@ def profile_main(args):
     from mocat_gb300 import _dev, _lib
     torch.cuda.set_device(0)
     dev = torch.device("cuda", 0)
-    if args.profile_model in ("adjoint", "lgstep", "logreg", "svbatch"):
+    if args.profile_model in ("adjoint", "lgstep", "score", "logreg", "svbatch"):
         return profile_other(args)
     ssm, d, prefix = _profile_model(args.profile_model)
     n, T = args.n, args.T
@@ -794,6 +794,8 @@ def profile_other(args):
       adjoint  mocat_gb300.adjoint.log_z_and_grad on the headline model, n = --n, T = --T
                (--launch-per-step: the forward pass one launch per phase);
       lgstep   the headline filter on the launch-per-step path (k_lg_step2 per step), n = --n, T = --T;
+      score    mocat_gb300.adjoint.log_z_and_score (2 backward draws, 8 proposals) on the headline
+               model, n = --n, T = --T;
       logreg   LogisticRegression.likelihood_potential_and_grad, 1e5 x 50 seeded data, P = --n
                parameter rows, --profile-precision bf16 | fp32 (three timed calls);
       svbatch  BatchedFilters over synthetic_sv_batch(--n series, seed 0, T in [50, --T]), launch
@@ -802,10 +804,12 @@ def profile_other(args):
     import mocat_gb300 as mg
     m, n, T = args.profile_model, args.n, args.T
     out = {"model": m, "n": n, "T": T}
-    if m in ("adjoint", "lgstep"):
+    if m in ("adjoint", "lgstep", "score"):
         ssm = mg.ssm.TimeHomogenousLinearGaussian(**model_arrays())
         y = ssm.simulate(np.arange(T), mg.random.PRNGKey(0)).y.contiguous()
-        if m == "adjoint":
+        if m == "score":
+            o = mg.adjoint.log_z_and_score(ssm, y, mg.random.PRNGKey(1), n, backward_draws=2, mcmc_steps=8)
+        elif m == "adjoint":
             o = mg.adjoint.log_z_and_grad(ssm, y, mg.random.PRNGKey(1), n, ckpt_every=32,
                                           persistent=not args.launch_per_step)
         else:
@@ -923,7 +927,7 @@ def main():
     ap.add_argument("--profile-run", action="store_true")
     ap.add_argument("--phase-trace", action="store_true")
     ap.add_argument("--profile-model", default="lg",
-                    choices=["lg", "nl1d", "adjoint", "lgstep", "logreg", "svbatch"])
+                    choices=["lg", "nl1d", "adjoint", "lgstep", "score", "logreg", "svbatch"])
     ap.add_argument("--profile-precision", default="bf16", choices=["bf16", "fp32"])
     ap.add_argument("--launch-per-step", action="store_true")
     ap.add_argument("--smc-B", type=int, default=256)
