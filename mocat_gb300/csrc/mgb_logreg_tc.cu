@@ -151,17 +151,18 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
 // softplus(w) = max(w, 0) + log(1 + e^-|z|) with w = (1 - 2y) z, and sum_j max(w_j, 0) =
 // (sum_j w_j + sum_j |z_j|) / 2 where sum_j w_j = beta . u, u = X^T (1 - 2y) (added once per
 // row): per element only |z| is accumulated (a0, a1: |z| of valid columns, 0 past n_data)
-__device__ __forceinline__ void epi_pair(float z0, float z1, float a0, float a1, uint32_t y0, uint32_t y1,
-                                         float &s_abs, float &prod, uint32_t &packed) {
+// c = (0.5 - y0, 0.5 - y1) as bf16x2 comes precomputed per column pair (k_logreg_cw); the
+// even and odd columns keep separate products (two independent multiply chains)
+__device__ __forceinline__ void epi_pair(float z0, float z1, float a0, float a1, uint32_t c, float &s_abs,
+                                         float &prod0, float &prod1, uint32_t &packed) {
   s_abs += a0 + a1;
   const float e0 = exp2f_approx(-1.4426950408889634f * fabsf(z0));
   const float e1 = exp2f_approx(-1.4426950408889634f * fabsf(z1));
-  prod = fmaf(prod, e0, prod);
-  prod = fmaf(prod, e1, prod);
+  prod0 = fmaf(prod0, e0, prod0);
+  prod1 = fmaf(prod1, e1, prod1);
   uint32_t zh = pack_bf16(z0, z1), h;
   asm("mul.rn.bf16x2 %0, %1, %2;" : "=r"(zh) : "r"(zh), "r"(0x3F003F00u));  // z / 2 (exact)
   asm("tanh.approx.bf16x2 %0, %1;" : "=r"(h) : "r"(zh));
-  const uint32_t c = 0x3F003F00u | (y0 << 15) | (y1 << 31);  // (0.5 - y0, 0.5 - y1)
   asm("fma.rn.bf16x2 %0, %1, %2, %3;" : "=r"(packed) : "r"(h), "r"(0x3F003F00u), "r"(c));
 }
 
@@ -169,6 +170,7 @@ struct TCArgs {
   const float *beta;
   const float *y;
   const float *u;  // (TC_K) X^T (1 - 2y) from the bf16 rows
+  const uint4 *cw;  // (tiles x 16) bf16x2 words (0.5 - y_2p, 0.5 - y_2p+1), 4 per 8 columns
   const int32_t *active;
   float *lik, *grad;
   int *err;
@@ -305,18 +307,20 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_logreg_tc(const __grid_consta
     const int row = q * 32 + lane;      // parameter row within the tile
     const uint32_t lane_off = (uint32_t)(q * 32) << 16;
     double pot = 0.0;
+    float pot_f = 0.0f;  // 16 tiles at a time in float, then into the double
     bool ok = true;
-    float ynext = 0.0f;
-    {
-      const int64_t i = (int64_t)cg * 32 + lane;
-      if (i < a.n_data) ynext = __ldg(&a.y[i]);
-    }
+    // this warp's 16 label words of tile t: cw[t * 16 + cg * 4 .. + 4] (uniform across lanes)
+    uint4 cnext[4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) cnext[m] = __ldg(&a.cw[cg * 4 + m]);
     for (int t = 0; t < nt && ok; ++t) {
       const int zb = t & 1, rb = t & 1;
-      const float ycur = ynext;  // y of column cg*32 + lane of this tile (gathered into a bit mask below)
-      {
-        const int64_t i = (int64_t)(t + 1) * TC_DT + cg * 32 + lane;
-        ynext = (i < a.n_data) ? __ldg(&a.y[i]) : 0.0f;
+      uint4 ccur[4];
+#pragma unroll
+      for (int m = 0; m < 4; ++m) ccur[m] = cnext[m];
+      if (t + 1 < nt) {
+#pragma unroll
+        for (int m = 0; m < 4; ++m) cnext[m] = __ldg(&a.cw[(int64_t)(t + 1) * 16 + cg * 4 + m]);
       }
       ok = mbar_wait(&bar_zfull[zb], (t >> 1) & 1, &abort_flag) &&
            mbar_wait(&bar_rempty[rb], ((t >> 1) & 1) ^ 1, &abort_flag);
@@ -329,28 +333,28 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_logreg_tc(const __grid_consta
       mbar_arrive(&bar_zempty[zb]);
       const int64_t i0 = (int64_t)t * TC_DT + cg * 32;
       const int nvalid = (int)min((int64_t)32, a.n_data - i0);
-      // labels of this warp's 32 columns as a bit mask; columns past n_data count as y = 0 with z = 0
-      const uint32_t ymask = __ballot_sync(0xffffffffu, ycur != 0.0f);
-      float s_abs = 0.0f, prod = 1.0f;
+      const uint32_t cwd[16] = {ccur[0].x, ccur[0].y, ccur[0].z, ccur[0].w, ccur[1].x, ccur[1].y, ccur[1].z, ccur[1].w,
+                                ccur[2].x, ccur[2].y, ccur[2].z, ccur[2].w, ccur[3].x, ccur[3].y, ccur[3].z, ccur[3].w};
+      float s_abs = 0.0f, prod0 = 1.0f, prod1 = 1.0f;
       uint32_t packed[16];
       if (nvalid == 32) {
 #pragma unroll
         for (int j = 0; j < 32; j += 2) {
           const float z0 = __uint_as_float(v[j]), z1 = __uint_as_float(v[j + 1]);
-          epi_pair(z0, z1, fabsf(z0), fabsf(z1), (ymask >> j) & 1u, (ymask >> (j + 1)) & 1u, s_abs, prod,
-                   packed[j >> 1]);
+          epi_pair(z0, z1, fabsf(z0), fabsf(z1), cwd[j >> 1], s_abs, prod0, prod1, packed[j >> 1]);
         }
       } else {
+        // columns past n_data: z = -inf (adds 0 to both sums), label word 0.5 (y = 0)
 #pragma unroll
         for (int j = 0; j < 32; j += 2) {
           const bool ok0 = j < nvalid, ok1 = j + 1 < nvalid;
           const float z0 = __uint_as_float(v[j]), z1 = __uint_as_float(v[j + 1]);
           epi_pair(ok0 ? z0 : -INFINITY, ok1 ? z1 : -INFINITY, ok0 ? fabsf(z0) : 0.0f, ok1 ? fabsf(z1) : 0.0f,
-                   ok0 ? (ymask >> j) & 1u : 0u, ok1 ? (ymask >> (j + 1)) & 1u : 0u, s_abs, prod, packed[j >> 1]);
+                   cwd[j >> 1], s_abs, prod0, prod1, packed[j >> 1]);
           if (!ok1) packed[j >> 1] &= ok0 ? 0x0000FFFFu : 0u;
         }
       }
-      const float s_l2 = log2f_approx(prod);
+      const float s_l2 = log2f_approx(prod0 * prod1);
       const float tsum = fmaf(0.69314718055994531f, s_l2, 0.5f * s_abs);
       unsigned char *sub = sR + rb * 2 * TILE_BYTES + (cg >> 1) * TILE_BYTES;
 #pragma unroll
@@ -361,8 +365,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_logreg_tc(const __grid_consta
       }
       fence_async_smem();
       mbar_arrive(&bar_rfull[rb]);
-      pot += (double)tsum;
+      pot_f += tsum;
+      if ((t & 15) == 15) {
+        pot += (double)pot_f;
+        pot_f = 0.0f;
+      }
     }
+    pot += (double)pot_f;
     pot_s[cg][row] = pot;
     if (cg == 0 && ok && mbar_wait(&bar_gdone, 0, &abort_flag)) {
       tc_fence_after();
@@ -447,8 +456,23 @@ __global__ void k_logreg_u_sum(const float *partial, float *u) {
   u[threadIdx.x] = s;
 }
 
-// err word, block partials of u, u
-size_t logreg_tc_workspace(int64_t, int64_t, int) { return 256 + sizeof(float) * (TC_UBLOCKS + 1) * TC_K; }
+// label words: cw[t * 64 + p] = bf16x2 (0.5 - y_{2p}, 0.5 - y_{2p+1}) of tile t's columns 2p, 2p+1
+// (y = 0 past n_data), the constant of the epilogue's r = tanh(z/2)/2 + (0.5 - y)
+__global__ void k_logreg_cw(const float *y, int64_t n_data, int64_t nwords, uint32_t *cw) {
+  for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < nwords; w += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = 2 * w;
+    const uint32_t y0 = (j < n_data && y[j] != 0.0f) ? 1u : 0u;
+    const uint32_t y1 = (j + 1 < n_data && y[j + 1] != 0.0f) ? 1u : 0u;
+    cw[w] = 0x3F003F00u | (y0 << 15) | (y1 << 31);
+  }
+}
+
+// err word, block partials of u, u, label words (one 16-byte aligned slab)
+static size_t cw_offset() { return ((256 + sizeof(float) * (TC_UBLOCKS + 1) * TC_K) + 255) & ~(size_t)255; }
+size_t logreg_tc_workspace(int64_t, int64_t n_data, int) {
+  const int64_t nt = (n_data + TC_DT - 1) / TC_DT;
+  return cw_offset() + sizeof(uint32_t) * (size_t)nt * (TC_DT / 2);
+}
 
 int logreg_tc(const SMCData &dat, const float *beta, int64_t P, const int32_t *active, int N, float *lik, float *grad,
               void *ws, size_t ws_bytes, cudaStream_t s) {
@@ -468,8 +492,11 @@ int logreg_tc(const SMCData &dat, const float *beta, int64_t P, const int32_t *a
   if (cudaMemsetAsync(err, 0, sizeof(int), s) != cudaSuccess) return ERR_CUDA;
   k_logreg_u_part<<<TC_UBLOCKS, 256, 0, s>>>(dat.Xb, dat.y, dat.n_data, partial);
   k_logreg_u_sum<<<1, TC_K, 0, s>>>(partial, u);
+  const int64_t nwords = ((dat.n_data + TC_DT - 1) / TC_DT) * (TC_DT / 2);
+  uint32_t *cw = (uint32_t *)((char *)ws + cw_offset());
+  k_logreg_cw<<<grid_for(nwords, 256), 256, 0, s>>>(dat.y, dat.n_data, nwords, cw);
   if ((st = launch_status())) return st;
-  TCArgs a{beta, dat.y, u, active, lik, grad, err, P, dat.n_data, dat.d, N > 0 ? N : (int)P};
+  TCArgs a{beta, dat.y, u, (const uint4 *)cw, active, lik, grad, err, P, dat.n_data, dat.d, N > 0 ? N : (int)P};
   const unsigned grid = (unsigned)((P + TC_ROWS - 1) / TC_ROWS);
   k_logreg_tc<<<grid, TC_THREADS, TC_SMEM, s>>>(map, a);
   return launch_status();
