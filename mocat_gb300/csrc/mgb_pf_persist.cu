@@ -46,6 +46,10 @@ namespace mgb {
 // so a normal pass adds no global load.
 __device__ __forceinline__ bool grid_sync(GridBar *bar, unsigned nblocks, int *err, int limit = BAR_SPIN_LIMIT) {
   __shared__ int gs_out;
+  if (nblocks == 1) {  // one block: a block barrier orders its own global writes
+    __syncthreads();
+    return false;
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
     int out = 0;
@@ -511,7 +515,11 @@ static int launch_persist(const MP &p, const PersistArgs &args, cudaStream_t s) 
   const int64_t chunks = (args.n / 2 + PP_TPB - 1) / PP_TPB;
   int64_t cap = (int64_t)sms * per_sm;
   if (cap * (PP_TPB / 32) > PP_MAX_CHUNKS) cap = PP_MAX_CHUNKS / (PP_TPB / 32);  // one LSE partial per warp
-  const dim3 grid((unsigned)(chunks < cap ? (chunks > 0 ? chunks : 1) : cap)), block(PP_TPB);
+  int64_t g = chunks < cap ? (chunks > 0 ? chunks : 1) : cap;
+  // a small filter (a few 256-pair chunks of a low-dimensional model) runs in one block:
+  // its steps are short enough that grid barriers between blocks would dominate them
+  if (chunks * MP::kD <= 4) g = 1;
+  const dim3 grid((unsigned)g), block(PP_TPB);
   if (cudaLaunchCooperativeKernel((void *)k_pf_persist<MP>, grid, block, kargs, 0, s) != cudaSuccess)
     return ERR_LAUNCH;
   k_or_err<<<1, 1, 0, s>>>(args.err, args.user_err);
