@@ -105,6 +105,17 @@ __device__ __forceinline__ LsePartial warp_online_partial(float m, float s1, flo
   return LsePartial{Mw, b1, b2, bn};
 }
 
+// combine of up to 32 partials, one per lane (inactive lanes pass m = -inf):
+// lane 0's value of a fixed shuffle tree
+__device__ __forceinline__ LsePartial warp_partial_combine(const LsePartial &q) {
+  const float Mw = warp_max(q.m);
+  const float f = (q.m > -INFINITY && Mw < INFINITY) ? expf(q.m - Mw) : 0.0f;
+  const float b1 = warp_sum<float>(q.s1 * f);
+  const float b2 = warp_sum<float>(q.s2 * (f * f));
+  const int bn = __any_sync(0xffffffffu, q.nan);
+  return LsePartial{Mw, b1, b2, bn};
+}
+
 // Fixed-order combine of the chunk partials (identical in every block): float
 // shuffle trees only -- FP64 throughput is low on this part and this runs in
 // every block every step.  Logarithms in float; log Z accumulates in float64.
@@ -244,6 +255,7 @@ __global__ void __launch_bounds__(PP_TPB, 2) k_pf_persist(const __grid_constant_
   __shared__ int32_t sK[PP_MAX_TILES + 1];
   __shared__ int32_t sU[PP_MAX_TILES + 1];
   __shared__ LseOut res_s;
+  __shared__ LsePartial wp_s[PP_TPB / 32];
   __shared__ float y_s[DY];
   __shared__ uint64_t sC[SCAN_TILE];
   __shared__ ResampleCtl sc;
@@ -251,7 +263,7 @@ __global__ void __launch_bounds__(PP_TPB, 2) k_pf_persist(const __grid_constant_
   const int64_t n = a.n, h = n >> 1;
   const int lane = threadIdx.x & 31;
   const int64_t wid = (int64_t)blockIdx.x * (PP_TPB / 32) + (threadIdx.x >> 5);
-  const int nwarps = (int)G * (PP_TPB / 32);  // one LSE partial per warp (<= PP_MAX_CHUNKS)
+  const int nwarps = (int)G * (PP_TPB / 32);
   const int ntiles = (int)((n + SCAN_TILE - 1) / SCAN_TILE);
   const float scale = __int_as_float((weight_shift(n) + 127) << 23);
   int res_cur = 0;
@@ -274,11 +286,12 @@ __global__ void __launch_bounds__(PP_TPB, 2) k_pf_persist(const __grid_constant_
     LsePartial *parts = a.parts + (t & 1) * PP_MAX_CHUNKS;
 
     // ---- P1: propagate + weight.  Warp w of the W warps of the grid takes the
-    // 32-pair rounds w, w + W, w + 2W, ... (a static assignment: each warp's
-    // partial covers a fixed set of particles in a fixed order, so the combine
-    // does not depend on timing), each lane keeps an online (max, sum e, sum e^2)
-    // across its rounds, and the warp writes one partial.  No block-wide barrier
-    // inside the phase: a warp never waits for the block's slowest warp.
+    // 32-pair rounds w, w + W, w + 2W, ... (a static assignment: each partial
+    // covers a fixed set of particles in a fixed order, so the combine does not
+    // depend on timing), each lane keeps an online (max, sum e, sum e^2) across
+    // its rounds, and at the end of the phase the block combines its warps'
+    // partials in warp order into one.  No block-wide barrier inside the rounds:
+    // a warp never waits for the block's slowest warp.
     __syncthreads();  // y_s
     const uint64_t t0 = (a.trace && t == 1 && threadIdx.x == 0) ? globaltimer_ns() : 0;
     {
@@ -325,8 +338,15 @@ __global__ void __launch_bounds__(PP_TPB, 2) k_pf_persist(const __grid_constant_
           }
         }
       }
-      const LsePartial part = warp_online_partial(m, s1, s2, nanf);
-      if (lane == 0) parts[wid] = part;
+      // the block's 8 warp partials, combined in warp order: one partial per block
+      const LsePartial wpart = warp_online_partial(m, s1, s2, nanf);
+      if (lane == 0) wp_s[threadIdx.x >> 5] = wpart;
+      __syncthreads();
+      if (threadIdx.x < 32) {
+        const LsePartial q = lane < PP_TPB / 32 ? wp_s[lane] : LsePartial{-INFINITY, 0.0f, 0.0f, 0};
+        const LsePartial part = warp_partial_combine(q);
+        if (lane == 0) parts[blockIdx.x] = part;
+      }
     }
     if (a.trace && t == 1 && threadIdx.x == 0) a.trace[a.T * 10 + blockIdx.x] = globaltimer_ns() - t0;
     stamp(a, t, 1);
@@ -335,7 +355,7 @@ __global__ void __launch_bounds__(PP_TPB, 2) k_pf_persist(const __grid_constant_
     stamp(a, t, 2);
 
     // ---- P2: combine (identical in every block)
-    const LseOut o = combine_chunks<PP_TPB>(parts, nwarps, smf, &res_s);
+    const LseOut o = combine_chunks<PP_TPB>(parts, (int)G, smf, &res_s);
     logz = t == 0 ? o.lse - a.logn : logz + o.lse - (res_cur ? a.logn : lse_prev);
     lse_prev = o.lse;
     const int res_next = ((float)o.ess < a.thr_n) ? 1 : 0;
@@ -514,7 +534,7 @@ static int launch_persist(const MP &p, const PersistArgs &args, cudaStream_t s) 
   // barriers then span a few blocks instead of every co-resident one
   const int64_t chunks = (args.n / 2 + PP_TPB - 1) / PP_TPB;
   int64_t cap = (int64_t)sms * per_sm;
-  if (cap * (PP_TPB / 32) > PP_MAX_CHUNKS) cap = PP_MAX_CHUNKS / (PP_TPB / 32);  // one LSE partial per warp
+  if (cap > PP_MAX_CHUNKS) cap = PP_MAX_CHUNKS;  // one LSE partial per block
   int64_t g = chunks < cap ? (chunks > 0 ? chunks : 1) : cap;
   // a small filter (a few 256-pair chunks of a low-dimensional model) runs in one block:
   // its steps are short enough that grid barriers between blocks would dominate them

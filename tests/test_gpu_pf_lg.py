@@ -162,3 +162,23 @@ def test_online_propagate_matches_run(cuda):
     assert np.array_equal(parts.value[-1].cpu().numpy(), full.value[-1].cpu().numpy())
     assert np.array_equal(parts.log_weight[-1].cpu().numpy(), full.log_weight[-1].cpu().numpy())
     assert np.allclose(parts.ess.cpu().numpy(), full.ess.cpu().numpy(), rtol=1e-5)
+
+
+@pytest.mark.parametrize("d,dy", [(1, 1), (3, 1), (4, 4), (10, 10)])
+def test_simulate_equals_oracle(cuda, d, dy):
+    """StateSpaceModel.simulate (ssm.py:138-163) of the linear-Gaussian model: the key layout
+    split(key, 2T) (first T keys for the latent chain, last T for the observations) and the
+    states and observations, bit for bit against the oracle's restatement"""
+    import mocat_gb300 as mg
+    rng = np.random.default_rng(d + dy)
+    A = models.random_stable_matrix(d, d)
+    Q = np.diag(rng.uniform(0.1, 0.5, d))
+    H = rng.standard_normal((dy, d))
+    R = np.diag(rng.uniform(0.2, 1.0, dy))
+    m0, S0 = rng.standard_normal(d), np.eye(d) * 2.0
+    T = 37
+    ssm = mg.ssm.TimeHomogenousLinearGaussian(m0, S0, A, Q, H, R)
+    sim = ssm.simulate(np.arange(T), O.PRNGKey(5))
+    x, y = models.simulate_lg(models.lg_params(m0, S0, A, Q, H, R), T, O.PRNGKey(5))
+    assert np.array_equal(sim.x.cpu().numpy(), x)
+    assert np.array_equal(sim.y.cpu().numpy(), y)
