@@ -160,7 +160,9 @@ __global__ void __launch_bounds__(SC_TPB) k_score_mu(const __grid_constant__ Sco
 }
 
 // one PaRIS step: backward draws, then tau_t^i
-template <int D>
+// KK = the number of backward draws, a compile-time constant so that only KK draws'
+// residuals and sources occupy registers
+template <int D, int KK>
 __device__ __forceinline__ void score_step_body(const ScoreP<D> &c, int64_t n, const ScoreStep &a) {
   using S = ScoreDims<D>;
   constexpr int B = 4;  // independent proposals evaluated together (their loads overlap)
@@ -171,7 +173,7 @@ __device__ __forceinline__ void score_step_body(const ScoreP<D> &c, int64_t n, c
   float xi[D];
 #pragma unroll
   for (int r = 0; r < D; ++r) xi[r] = a.x[r * n + i];
-  int64_t mk[SC_KMAX];
+  int64_t mk[KK];
   {
     float row[S::MS];
     load_row<D>(a.mu + i * S::MS, row);
@@ -179,8 +181,8 @@ __device__ __forceinline__ void score_step_body(const ScoreP<D> &c, int64_t n, c
     int64_t cur = i;
     mk[0] = i;
 #pragma unroll
-    for (int k = 1; k < SC_KMAX; ++k) {
-      if (k < a.K) {
+    for (int k = 1; k < KK; ++k) {
+      if (k < KK) {
         for (int l0 = 0; l0 < a.L; l0 += B) {
           float lp[B], E[B];
           int64_t prop[B];
@@ -209,13 +211,13 @@ __device__ __forceinline__ void score_step_body(const ScoreP<D> &c, int64_t n, c
     }
   }
   // the draws' source particles, their states and residuals
-  float e[SC_KMAX][D], v[SC_KMAX][D], xp[SC_KMAX][D];
-  const float4 *tp[SC_KMAX];
+  float e[KK][D], v[KK][D], xp[KK][D];
+  const float4 *tp[KK];
 #pragma unroll
-  for (int k = 0; k < SC_KMAX; ++k) {
-    const int kk = k < a.K ? k : 0;
+  for (int k = 0; k < KK; ++k) {
+    const int kk = k < KK ? k : 0;
     const int64_t j = res ? (int64_t)__ldg(&a.anc[mk[kk]]) : mk[kk];
-    if (a.draws && k < a.K) a.draws[i * a.K + k] = (int32_t)j;
+    if (a.draws && k < KK) a.draws[i * KK + k] = (int32_t)j;
     float row[S::MS];
     load_row<D>(a.mu + mk[kk] * S::MS, row);
 #pragma unroll
@@ -235,9 +237,9 @@ __device__ __forceinline__ void score_step_body(const ScoreP<D> &c, int64_t n, c
   float4 *to = reinterpret_cast<float4 *>(a.tau + i * S::TS);
 #pragma unroll
   for (int q4 = 0; q4 < S::TS / 4; ++q4) {
-    float4 pv[SC_KMAX];
+    float4 pv[KK];
 #pragma unroll
-    for (int k = 0; k < SC_KMAX; ++k) pv[k] = k < a.K ? __ldg(tp[k] + q4) : make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int k = 0; k < KK; ++k) pv[k] = k < KK ? __ldg(tp[k] + q4) : make_float4(0.f, 0.f, 0.f, 0.f);
     float out[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
@@ -246,8 +248,8 @@ __device__ __forceinline__ void score_step_body(const ScoreP<D> &c, int64_t n, c
       if (q < D * D) {
         const int r = q / D, col = q % D;
 #pragma unroll
-        for (int k = 0; k < SC_KMAX; ++k)
-          if (k < a.K) {
+        for (int k = 0; k < KK; ++k)
+          if (k < KK) {
             const float tv = u == 0 ? pv[k].x : u == 1 ? pv[k].y : u == 2 ? pv[k].z : pv[k].w;
             acc = __fadd_rn(acc, tv);
             acc = __fadd_rn(acc, __fmul_rn(v[k][r], xp[k][col]));
@@ -256,8 +258,8 @@ __device__ __forceinline__ void score_step_body(const ScoreP<D> &c, int64_t n, c
       } else if (q < D * D + D) {
         const int r = q - D * D;
 #pragma unroll
-        for (int k = 0; k < SC_KMAX; ++k)
-          if (k < a.K) {
+        for (int k = 0; k < KK; ++k)
+          if (k < KK) {
             const float tv = u == 0 ? pv[k].x : u == 1 ? pv[k].y : u == 2 ? pv[k].z : pv[k].w;
             acc = __fadd_rn(acc, tv);
             acc = __fadd_rn(acc, __fsub_rn(__fmul_rn(__fmul_rn(e[k][r], e[k][r]), c.half_iq[r]), 0.5f));
@@ -266,8 +268,8 @@ __device__ __forceinline__ void score_step_body(const ScoreP<D> &c, int64_t n, c
       } else if (q < S::P) {
         const int r = q - D * D - D;
 #pragma unroll
-        for (int k = 0; k < SC_KMAX; ++k)
-          if (k < a.K) {
+        for (int k = 0; k < KK; ++k)
+          if (k < KK) {
             const float tv = u == 0 ? pv[k].x : u == 1 ? pv[k].y : u == 2 ? pv[k].z : pv[k].w;
             acc = __fadd_rn(acc, tv);
           }
@@ -280,10 +282,10 @@ __device__ __forceinline__ void score_step_body(const ScoreP<D> &c, int64_t n, c
   }
 }
 
-template <int D>
+template <int D, int KK>
 __global__ void __launch_bounds__(SC_TPB) k_score_step(const __grid_constant__ ScoreP<D> c, int64_t n,
                                                         const ScoreStep a) {
-  score_step_body<D>(c, n, a);
+  score_step_body<D, KK>(c, n, a);
 }
 
 // partial[b][q] = sum over block b's particles of W_i tau_i[q] (float64, fixed order)
@@ -431,7 +433,12 @@ static int score_lg(const mgb_lg_model *m, int64_t n, int64_t T, const uint32_t 
     a.y = y + (size_t)t * D;
     a.draws = draws_out ? draws_out + (size_t)t * n * K : nullptr;
     a.t = (uint32_t)t;
-    k_score_step<D><<<gs, SC_TPB, 0, s>>>(c, n, a);
+    switch (K) {
+      case 1: k_score_step<D, 1><<<gs, SC_TPB, 0, s>>>(c, n, a); break;
+      case 2: k_score_step<D, 2><<<gs, SC_TPB, 0, s>>>(c, n, a); break;
+      case 3: k_score_step<D, 3><<<gs, SC_TPB, 0, s>>>(c, n, a); break;
+      default: k_score_step<D, 4><<<gs, SC_TPB, 0, s>>>(c, n, a); break;
+    }
     if ((st = launch_status())) return st;
     float *tp = xa; xa = xb; xb = tp;
     tp = la; la = lb; lb = tp;
@@ -505,7 +512,7 @@ __global__ void __launch_bounds__(SC_TPB) k_score_mu_b(const __grid_constant__ S
   const int64_t o = (int64_t)blockIdx.y * ws;
   score_mu_body<D>(c, n, slab(xprev, o), slab(anc, o), slab(res_flag, o), slab(lw_prev, o), slab(mu, o));
 }
-template <int D>
+template <int D, int KK>
 __global__ void __launch_bounds__(SC_TPB) k_score_step_b(const __grid_constant__ ScoreP<D> c, int64_t n,
                                                           const ScoreStep a0, int64_t ws) {
   const int64_t o = (int64_t)blockIdx.y * ws;
@@ -519,7 +526,7 @@ __global__ void __launch_bounds__(SC_TPB) k_score_step_b(const __grid_constant__
   a.tau = slab(a0.tau, o);
   a.skey = slab(a0.skey, o);
   a.draws = nullptr;
-  score_step_body<D>(c, n, a);
+  score_step_body<D, KK>(c, n, a);
 }
 
 // a filter's slab: the single-filter workspace plus its smoothing key
@@ -610,7 +617,12 @@ static int score_lg_batch(const mgb_lg_model *m, int64_t n, int64_t T, int64_t B
     a.tau = tb;
     a.y = y + (size_t)t * D;
     a.t = (uint32_t)t;
-    k_score_step_b<D><<<dim3(gs, (unsigned)B), SC_TPB, 0, s>>>(c, n, a, W);
+    switch (K) {
+      case 1: k_score_step_b<D, 1><<<dim3(gs, (unsigned)B), SC_TPB, 0, s>>>(c, n, a, W); break;
+      case 2: k_score_step_b<D, 2><<<dim3(gs, (unsigned)B), SC_TPB, 0, s>>>(c, n, a, W); break;
+      case 3: k_score_step_b<D, 3><<<dim3(gs, (unsigned)B), SC_TPB, 0, s>>>(c, n, a, W); break;
+      default: k_score_step_b<D, 4><<<dim3(gs, (unsigned)B), SC_TPB, 0, s>>>(c, n, a, W); break;
+    }
     if ((st = launch_status())) return st;
     float *tp = xa; xa = xb; xb = tp;
     tp = la; la = lb; lb = tp;
