@@ -112,3 +112,37 @@ def test_new_entry_points_reject_bad_arguments_on_host(L):
     assert need > 0
     assert L.mgb_abc_vanilla_lg(ctypes.byref(am), 1000, p, 1.0, -1.0, p, need - 1, p, p, p, p, p, null) == 4
     assert L.mgb_abc_mcmc_lg(ctypes.byref(am), 1, 100, p, -0.1, 1.0, p, p, p, p, null) == 1
+
+
+def test_score_entry_points_reject_bad_arguments_on_host(L):
+    """mgb_pf_lg_score / mgb_pf_lg_score_batch / mgb_wait_selftest: every argument check runs
+    before any device call (1 = bad argument, 2 = unsupported configuration)"""
+    import numpy as np
+    d = 3
+    eye = np.eye(d, dtype=np.float32)
+    arrs = [eye, eye, eye, eye, eye, np.zeros(d, np.float32)]
+    m = _lib.LGModel(d, d, *[a.ctypes.data for a in arrs], 1.0)
+    p = ctypes.c_void_p(256)
+    big = 1 << 30
+    args = lambda K, L_, T=20, n=1024: (ctypes.byref(m), n, T, p, p, p, 0.5, 0, K, L_, p, big, None, p, None, None,
+                                        None)
+    assert L.mgb_pf_lg_score(*args(0, 8)) == 1             # no backward draw
+    assert L.mgb_pf_lg_score(*args(5, 8)) == 1             # more than 4 draws
+    assert L.mgb_pf_lg_score(*args(3, 2049)) == 1          # (K - 1) L > 4096
+    assert L.mgb_pf_lg_score(*args(2, 8, T=(1 << 20) + 1)) == 1
+    assert L.mgb_pf_lg_score(*args(2, 8, n=1)) == 1
+    full = np.full((d, d), 0.1, np.float32)                # a non-diagonal transition covariance
+    m2 = _lib.LGModel(d, d, eye.ctypes.data, full.ctypes.data, eye.ctypes.data, eye.ctypes.data, eye.ctypes.data,
+                      arrs[5].ctypes.data, 1.0)
+    assert L.mgb_pf_lg_score(ctypes.byref(m2), 1024, 20, p, p, p, 0.5, 0, 2, 8, p, big, None, p, None, None,
+                             None) == 2
+    m3 = _lib.LGModel(d, 1, *[a.ctypes.data for a in arrs], 1.0)  # dy != d
+    assert L.mgb_pf_lg_score(ctypes.byref(m3), 1024, 20, p, p, p, 0.5, 0, 2, 8, p, big, None, p, None, None,
+                             None) == 2
+    bargs = lambda B, n=1024, K=2: (ctypes.byref(m), n, 20, B, p, p, p, 0.5, K, 8, p, big, None, p, None)
+    assert L.mgb_pf_lg_score_batch(*bargs(0)) == 1
+    assert L.mgb_pf_lg_score_batch(*bargs(4, K=0)) == 1
+    assert L.mgb_pf_lg_score_batch(*bargs(4, n=1023)) == 2  # even n only
+    assert L.mgb_pf_lg_score_batch_workspace(1024, 20, d, 4) == 4 * L.mgb_pf_lg_score_batch_workspace(1024, 20, d, 1)
+    assert L.mgb_wait_selftest(2, 64, p, 256, None) == 1
+    assert L.mgb_wait_selftest(0, 0, p, 256, None) == 1
