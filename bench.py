@@ -775,14 +775,11 @@ def profile_main(args):
         res = {"model": args.profile_model, "n": n, "T": T, "ess_threshold": thr, "us_propagate": med(0, 1),
                "us_barrier1": med(1, 2), "us_combine": med(2, 3)}
         if thr > 0:
-            res.update({"us_tile_sums": med(3, 4), "us_barrier2": med(4, 5), "us_fill_setup": med(5, 6),
-                        "us_fill_units": med(6, 7), "us_barrier3": med(7, 8)})
+            res.update({"us_tile_sums": med(3, 4), "us_barrier2": med(4, 5), "us_tile_scan": med(5, 6),
+                        "us_fill": med(6, 7), "us_barrier3": med(7, 8)})
         res["us_step"] = float(np.median(np.diff(st[:, 0])) / 1e3)
         if thr > 0:
             full = tr.cpu().numpy().astype(np.float64)
-            res["fill_units_median"] = float(np.median(st[:, 9]))
-            blk0 = full[T * 10 + 1024:T * 10 + 2048]
-            res["step1_block0_unit_done_us"] = [round(v / 1e3, 2) for v in blk0[blk0 > 0][:16]]
             p1 = full[T * 10:T * 10 + 1024]
             p1 = p1[p1 > 0] / 1e3
             res["step1_propagate_us_blocks"] = [float(p1.min()), float(np.median(p1)), float(p1.max())]

@@ -175,13 +175,11 @@ typedef struct {
   float *x_final;     /* (d, n) final particles */
   float *lw_final;    /* (n,) final log-weights */
   int32_t *err;       /* device error word */
-  uint64_t *trace;    /* (T * 10 + 2048) diagnostics of the persistent kernel (NULL = off):
+  uint64_t *trace;    /* (T * 10 + 1024) diagnostics of the persistent kernel (NULL = off):
                          [t * 10 + k] device-clock ns at the phase boundaries of step t seen by
                          block 0 (start, propagate done, barrier, combine done, tile sums done,
-                         barrier, fill set-up done, fill done, barrier), [t * 10 + 9] the
-                         number of fill units of step t; [T * 10 + b] (b < 1024) ns block b
-                         spent propagating step 1; [T * 10 + 1024 + j] ns after step 1's fill
-                         set-up at which block 0 finished its j-th fill unit */
+                         barrier, tile-sum scan done, offspring runs written, barrier);
+                         [T * 10 + b] (b < 1024) ns block b spent propagating step 1 */
 } mgb_pf_outputs;
 
 /* run_particle_filter_for_marginals (mocat/src/ssm/filtering.py:255-324) with

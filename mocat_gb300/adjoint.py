@@ -294,62 +294,6 @@ def log_z_and_score_many(ssm_scenario, y, random_keys, n, backward_draws=2, mcmc
     return cdict(log_z=logz, grad=grad)
 
 
-def log_z_and_score_many(ssm_scenario, y, random_keys, n, backward_draws=2, mcmc_steps=8, smoothing_keys=None,
-                         ess_threshold=0.5, resampling="systematic", max_concurrent=8):
-    """log_z_and_score for B filter keys at once: each evaluation runs on its own CUDA
-    stream, enqueued from its own host thread (the C library releases the interpreter
-    lock), so the launches of different evaluations overlap on the GPU.  The same values
-    as B calls of log_z_and_score (smoothing_keys default to default_smoothing_key of
-    each filter key).
-
-    Returns cdict(log_z (B,), grad (B, d*d + 2d)) in the layout of mgb_pf_lg_score."""
-    import threading
-    if not isinstance(ssm_scenario, TimeHomogenousLinearGaussian):
-        raise NotImplementedError(f"{ssm_scenario.__class__.__name__}: no score kernel for this model")
-    d = ssm_scenario.dim
-    if d not in SUPPORTED_D:
-        raise NotImplementedError(f"score for d = {d} not compiled (supported {SUPPORTED_D})")
-    _, s = ssm_scenario.derived()
-    dev = _dev.device()
-    keys = _dev.as_key(random_keys).reshape(-1, 2).contiguous()
-    B = keys.shape[0]
-    skeys = (torch.stack([default_smoothing_key(keys[b]) for b in range(B)]) if smoothing_keys is None
-             else _dev.as_key(smoothing_keys).reshape(-1, 2).contiguous())
-    y2 = _dev.as_f32(y).reshape(-1, d).contiguous()
-    T = y2.shape[0]
-    nws = _lib.lib().mgb_pf_lg_score_workspace(n, T, d)
-    logz = torch.empty(B, dtype=torch.float64, device=dev)
-    grad = torch.empty((B, d * d + 2 * d), dtype=torch.float32, device=dev)
-    lanes = min(B, max_concurrent)
-    ws = [_dev.workspace(nws, dev) for _ in range(lanes)]
-    streams = [torch.cuda.Stream(dev) for _ in range(lanes)]
-    cur = torch.cuda.current_stream(dev)
-    for st in streams:
-        st.wait_stream(cur)
-    errors = []
-
-    def lane(j):
-        try:
-            for b in range(j, B, lanes):
-                call("mgb_pf_lg_score", ctypes.byref(s), n, T, _dev.ptr(keys[b]), _dev.ptr(skeys[b]), _dev.ptr(y2),
-                     float(ess_threshold), SCHEMES[resampling], int(backward_draws), int(mcmc_steps),
-                     _dev.ptr(ws[j]), ws[j].numel(), _dev.ptr(logz[b:b + 1]), _dev.ptr(grad[b]), None, None,
-                     ctypes.c_void_p(streams[j].cuda_stream))
-        except Exception as e:  # re-raised on the calling thread
-            errors.append(e)
-
-    threads = [threading.Thread(target=lane, args=(j,)) for j in range(lanes)]
-    for t in threads:
-        t.start()
-    for t in threads:
-        t.join()
-    if errors:
-        raise errors[0]
-    for st in streams:
-        cur.wait_stream(st)
-    return cdict(log_z=logz, grad=grad)
-
-
 class ParticleFilterLogZ(torch.autograd.Function):
     """forward: log Z of the bootstrap filter for theta = (A, log q, log r);
     backward: the adjoint (ancestors held fixed), computed in the same library call."""

@@ -60,7 +60,9 @@ __host__ __device__ inline float *persist_lbuf(const PersistArgs &a, int64_t s) 
   return (s & 1) ? a.lb : a.la;
 }
 
-// Persistent path: systematic resampling, even n, n <= 2^21 (tile prefixes in smem).
+// Persistent path: systematic resampling, even n, n <= 2^21 (tile prefixes in
+// smem; the branch-free offspring count is exact up to that size).
+static_assert((int64_t)PP_MAX_TILES * SCAN_TILE <= SYS_COUNT_SMALL_MAX_N, "sys_count_small bound");
 inline bool persistent_ok(int64_t n, int scheme) {
   return scheme == MGB_RESAMPLE_SYSTEMATIC && n % 2 == 0 && (n + SCAN_TILE - 1) / SCAN_TILE <= PP_MAX_TILES;
 }

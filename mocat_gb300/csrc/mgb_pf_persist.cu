@@ -15,10 +15,11 @@
 //       so every block reaches the same logsumexp / ESS / resample decision);
 //       block 0 records ESS, the resample flag and log Z
 //   and, when the next step resamples,
-//   P3  exact fixed-point tile sums of the new log-weights           -> barrier
-//   P4  every block scans the tile sums in shared memory, places each tile's
-//       output range, cuts it into units of <= 2048 outputs and fills the
-//       units assigned to it (grid-stride)                           -> barrier
+//   P3  exact fixed-point tile sums of the new log-weights, and each tile's
+//       within-tile prefixes                                          -> barrier
+//   P4  every block scans the tile sums in shared memory; for the particles
+//       of its own tiles it computes the exact systematic offspring counts and
+//       writes each particle's run of ancestor indices               -> barrier
 // A non-resampling step costs one grid barrier, a resampling step three; no
 // kernel launches, no host round trips.  Data written inside the kernel is
 // read back through L2 (__ldcg): L1 is not coherent across SMs.  The grid
@@ -207,24 +208,15 @@ __device__ __forceinline__ void load_tile_lw(const float *lw, int64_t i0, int64_
   }
 }
 
-// tile of the u-th unit of a numbering whose per-tile prefix is sU (the largest
-// tile b with sU[b] <= u), its particle count and its within-tile prefixes
-// (thread's elements threadIdx.x + j PP_TPB) into v
-__device__ __forceinline__ void unit_load(int u, int ntiles, int64_t n, const int32_t *sU, const uint64_t *cloc,
-                                          int &tile, int &cnt_valid, uint64_t (&v)[SCAN_IPT]) {
-  int lo_b = 0, hi_b = ntiles;
-  while (hi_b - lo_b > 1) {
-    const int mid = (lo_b + hi_b) >> 1;
-    if (sU[mid] <= u) lo_b = mid;
-    else hi_b = mid;
-  }
-  tile = lo_b;
-  const int64_t base = (int64_t)tile * SCAN_TILE;
-  cnt_valid = (int)(n - base < SCAN_TILE ? n - base : SCAN_TILE);
+// within-tile inclusive prefixes of particles base + threadIdx.x + PP_TPB r
+// (r < SCAN_IPT; warp-contiguous), written by other blocks this step and so
+// read through L2; past n they are never used
+__device__ __forceinline__ void load_tile_cloc(const uint64_t *cloc, int64_t base, int64_t n,
+                                               uint64_t (&X)[SCAN_IPT]) {
 #pragma unroll
-  for (int j = 0; j < SCAN_IPT; ++j) {
-    const int jj = threadIdx.x + j * PP_TPB;
-    v[j] = jj < cnt_valid ? __ldcg(&cloc[base + jj]) : 0ull;
+  for (int r = 0; r < SCAN_IPT; ++r) {
+    const int64_t i = base + threadIdx.x + PP_TPB * r;
+    X[r] = i < n ? __ldcg(&cloc[i]) : 0ull;
   }
 }
 
@@ -245,20 +237,99 @@ struct LGModelP {
   }
 };
 
+// P4 of a resampling step: every block scans the tile sums (identical result
+// in every block), then writes the ancestors of the outputs of its own tiles.
+// Particle j, with global inclusive prefix X_j, takes the outputs
+// [K(X_{j-1}), K(X_j)), K the exact systematic threshold count
+// (sys_count_small, branch-free); a tile's outputs are written RUN_WINDOW at
+// a time through a shared window (runs marked, max-scanned, stored
+// coalesced).  All global accesses are warp-contiguous.  Out of line: its
+// registers then do not shape the allocation of the propagate loop, and the
+// call costs a few register saves once per resampling step.
+__device__ __noinline__ void resample_fill(const PersistArgs &a, int64_t t, int64_t n, int ntiles,
+                                           int32_t *__restrict__ anc_n) {
+  __shared__ uint64_t sP[PP_MAX_TILES];
+  __shared__ unsigned long long smu[PP_TPB / 32];
+  __shared__ int32_t sKt[SCAN_TILE];
+  __shared__ __align__(16) int32_t stage[RUN_WINDOW];  // int4 accesses
+  __shared__ int32_t wmax_s[PP_TPB / 32];
+  __shared__ int32_t k0_s;
+  const int G = (int)gridDim.x;
+  const int per = (ntiles + PP_TPB - 1) / PP_TPB;
+  const int b0 = threadIdx.x * per, b1 = min(b0 + per, ntiles);
+  unsigned long long ts[4];
+  unsigned long long run = 0;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    ts[j] = (j < per && b0 + j < b1) ? __ldcg(&a.tile_sum[b0 + j]) : 0ull;
+    run += ts[j];
+  }
+  unsigned long long Q;
+  unsigned long long pre = block_excl_scan_u64(run, smu, Q);
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+    if (j < per && b0 + j < b1) {
+      sP[b0 + j] = pre;
+      pre += ts[j];
+    }
+  const int degenerate = __ldcg(&a.degen[t]) || Q == 0;
+  if (degenerate) {
+    for (int64_t i = blockIdx.x * (int64_t)PP_TPB + threadIdx.x; i < n; i += (int64_t)G * PP_TPB) anc_n[i] = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(a.err, EB_DEGENERATE);
+  } else {
+    const uint32_t m23 = bits_at(__ldg(&a.keys[2 * (t + 1)]), __ldg(&a.keys[2 * (t + 1) + 1]), 1, 0) >> 9;
+    const float n_over_q = __fdiv_rn((float)n, (float)Q);
+    __syncthreads();                 // sP
+    stamp(a, t, 6);
+    for (int tile = blockIdx.x; tile < ntiles; tile += G) {
+      const int64_t base = (int64_t)tile * SCAN_TILE;
+      const uint64_t P = sP[tile];
+      uint64_t X[SCAN_IPT];
+      load_tile_cloc(a.cloc, base, n, X);
+      // K of the tile's particles (particle base + threadIdx.x + PP_TPB r);
+      // past n, K = n (empty runs after the last particle, whose K is n)
+#pragma unroll
+      for (int r = 0; r < SCAN_IPT; ++r) {
+        const int jj = threadIdx.x + PP_TPB * r;
+        sKt[jj] = base + jj < n ? sys_count_small(P + X[r], (int32_t)n, m23, Q, n_over_q) : (int32_t)n;
+      }
+      if (threadIdx.x == 0) k0_s = sys_count_small(P, (int32_t)n, m23, Q, n_over_q);
+      __syncthreads();
+      const int32_t k0 = k0_s, k1 = sKt[SCAN_TILE - 1];
+      for (int32_t w0 = k0; w0 < k1; w0 += RUN_WINDOW) {
+        int4 *s4 = (int4 *)stage;
+#pragma unroll
+        for (int j = 0; j < RUN_WINDOW / 4 / PP_TPB; ++j) s4[threadIdx.x + PP_TPB * j] = make_int4(-1, -1, -1, -1);
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < SCAN_IPT; ++r) {
+          const int jj = threadIdx.x + PP_TPB * r;
+          const int32_t lo = jj ? sKt[jj - 1] : k0, hi = sKt[jj];
+          const int32_t st = lo > w0 ? lo : w0;
+          if (hi > st && st < w0 + RUN_WINDOW) stage[st - w0] = jj;
+        }
+        __syncthreads();
+        window_max_scan(stage, wmax_s);
+        __syncthreads();
+        const int cnt = k1 - w0 < RUN_WINDOW ? k1 - w0 : RUN_WINDOW;
+        // every slot is covered (slot 0 by the run through w0); the clamp only keeps a
+        // wrong count from producing an out-of-range ancestor
+        for (int q = threadIdx.x; q < cnt; q += PP_TPB) anc_n[w0 + q] = (int32_t)(base + max(stage[q], 0));
+        __syncthreads();  // the window is cleared again, or sKt rewritten by the next tile
+      }
+    }
+  }
+}
+
 template <class MP>
 __global__ void __launch_bounds__(PP_TPB, 2) k_pf_persist(const __grid_constant__ MP p,
                                                            const __grid_constant__ PersistArgs a) {
   constexpr int D = MP::kD, DY = MP::kDY;
   __shared__ float smf[PP_TPB / 32];
   __shared__ unsigned long long smu[PP_TPB / 32];
-  __shared__ uint64_t sP[PP_MAX_TILES + 1];
-  __shared__ int32_t sK[PP_MAX_TILES + 1];
-  __shared__ int32_t sU[PP_MAX_TILES + 1];
   __shared__ LseOut res_s;
   __shared__ LsePartial wp_s[PP_TPB / 32];
   __shared__ float y_s[DY];
-  __shared__ uint64_t sC[SCAN_TILE];
-  __shared__ ResampleCtl sc;
   const unsigned G = gridDim.x;
   const int64_t n = a.n, h = n >> 1;
   const int lane = threadIdx.x & 31;
@@ -418,78 +489,8 @@ __global__ void __launch_bounds__(PP_TPB, 2) k_pf_persist(const __grid_constant_
       if (grid_sync(a.bar, G, a.err)) break;
       stamp(a, t, 5);
 
-      // ---- P4: scan tile sums, place outputs, fill units
-      const int per = (ntiles + PP_TPB - 1) / PP_TPB;
-      const int b0 = threadIdx.x * per, b1 = min(b0 + per, ntiles);
-      unsigned long long ts[4];
-      unsigned long long run = 0;
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        ts[j] = (j < per && b0 + j < b1) ? __ldcg(&a.tile_sum[b0 + j]) : 0ull;
-        run += ts[j];
-      }
-      unsigned long long Q;
-      unsigned long long pre = block_excl_scan_u64(run, smu, Q);
-#pragma unroll
-      for (int j = 0; j < 4; ++j)
-        if (j < per && b0 + j < b1) {
-          sP[b0 + j] = pre;
-          pre += ts[j];
-        }
-      if (threadIdx.x == 0) sP[ntiles] = Q;
-      const int degenerate = __ldcg(&a.degen[t]) || Q == 0;
-      if (degenerate) {
-        for (int64_t i = blockIdx.x * (int64_t)PP_TPB + threadIdx.x; i < n; i += (int64_t)G * PP_TPB) anc_n[i] = 0;
-        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(a.err, EB_DEGENERATE);
-      } else {
-        const uint32_t m23 = bits_at(__ldg(&a.keys[2 * (t + 1)]), __ldg(&a.keys[2 * (t + 1) + 1]), 1, 0) >> 9;
-        if (threadIdx.x == 0) sys_constants(Q, (uint64_t)n, m23, sc, a.magic);
-        const float n_over_q = __fdiv_rn((float)n, (float)Q);
-        for (int b = threadIdx.x; b <= ntiles; b += PP_TPB) sK[b] = (int32_t)sys_count(sP[b], n, m23, Q, n_over_q);
-        __syncthreads();
-        unsigned long long nu = 0;
-        for (int b = b0; b < b1; ++b) nu += (unsigned long long)((sK[b + 1] - sK[b] + SCAN_TILE - 1) / SCAN_TILE);
-        unsigned long long utot;
-        unsigned long long uo = block_excl_scan_u64(nu, smu, utot);
-        for (int b = b0; b < b1; ++b) {
-          sU[b] = (int32_t)uo;
-          uo += (unsigned long long)((sK[b + 1] - sK[b] + SCAN_TILE - 1) / SCAN_TILE);
-        }
-        if (threadIdx.x == 0) sU[ntiles] = (int32_t)utot;
-        __syncthreads();
-        stamp(a, t, 6);
-        if (a.trace && blockIdx.x == 0 && threadIdx.x == 0) a.trace[t * 10 + 9] = utot;
-        const ResampleCtl c = sc;
-        // units run round robin, one after another per block; the next unit's
-        // prefixes are requested into registers while the current one merges
-        // from shared memory
-        int u = blockIdx.x;
-        int tile = 0, cnt_valid = 0;
-        uint64_t cv[SCAN_IPT];
-        if (u < (int)utot) unit_load(u, ntiles, n, sU, a.cloc, tile, cnt_valid, cv);
-        int done = 0;
-        while (u < (int)utot) {
-          const int64_t kb = sK[tile] + (int64_t)(u - sU[tile]) * SCAN_TILE;
-          const int64_t ke = kb + SCAN_TILE < (int64_t)sK[tile + 1] ? kb + SCAN_TILE : (int64_t)sK[tile + 1];
-          const int64_t base = (int64_t)tile * SCAN_TILE;
-          const uint64_t P = sP[tile];
-#pragma unroll
-          for (int j = 0; j < SCAN_IPT; ++j) {
-            const int jj = threadIdx.x + j * PP_TPB;
-            if (jj < cnt_valid) sC[jj] = P + cv[j];
-          }
-          __syncthreads();
-          const int cnt = cnt_valid;
-          const int un = u + (int)G;
-          if (un < (int)utot) unit_load(un, ntiles, n, sU, a.cloc, tile, cnt_valid, cv);
-          merge_fill(sC, cnt, c, kb, (int)(ke - kb), base, n, anc_n);
-          __syncthreads();
-          if (a.trace && t == 1 && blockIdx.x == 0 && threadIdx.x == 0 && done < 1024)
-            a.trace[a.T * 10 + 1024 + done] = globaltimer_ns() - a.trace[t * 10 + 6];
-          ++done;
-          u = un;
-        }
-      }
+      // ---- P4: offspring runs of the next step (out of line, see resample_fill)
+      resample_fill(a, t, n, ntiles, anc_n);
       stamp(a, t, 7);
       if (grid_sync(a.bar, G, a.err)) break;
       stamp(a, t, 8);

@@ -353,26 +353,53 @@ __device__ __forceinline__ void merge_fill(const uint64_t *sC, int cnt, const Re
   }
 }
 
-// Writes a particle's offspring run anc[lo, hi) = idx: short runs directly,
-// runs longer than RUN_DIRECT_MAX are queued in shared memory and filled by
-// whole warps afterwards (fill_queued_runs), so one heavy particle does not
-// serialise its warp.
-constexpr int RUN_DIRECT_MAX = 16;
-constexpr int RUN_QUEUE = 256;  // >= 2048 outputs / RUN_DIRECT_MAX
-__device__ __forceinline__ void write_run(int32_t *anc, int64_t lo, int64_t hi, int32_t idx, int4 *q, int *nq) {
-  if (hi - lo > RUN_DIRECT_MAX) {
-    const int slot = atomicAdd(nq, 1);
-    q[slot] = make_int4((int)lo, (int)hi, idx, 0);
-  } else {
-    for (int64_t k = lo; k < hi; ++k) anc[k] = idx;
-  }
-}
-template <int TPB>
-__device__ __forceinline__ void fill_queued_runs(int32_t *anc, const int4 *q, const int *nq) {
+// Offspring-run window of the persistent filter: RUN_WINDOW consecutive
+// outputs in shared memory.  Every particle whose run [lo, hi) meets the window
+// marks the window slot of its first output there with its tile-local number;
+// an inclusive max-scan then gives every slot the particle that covers it (runs
+// are disjoint and ordered by particle, so the covering particle is the largest
+// mark at or before the slot).  256 threads, 16 consecutive slots each.
+constexpr int RUN_WINDOW = 4096;
+__device__ __forceinline__ void window_max_scan(int32_t *stage, int32_t *wmax /* >= 8 */) {
+  static_assert(RUN_WINDOW == 256 * 16, "16 slots per thread");
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int r = warp; r < *nq; r += TPB / 32) {
-    const int4 v = q[r];
-    for (int k = v.x + lane; k < v.y; k += 32) anc[k] = v.z;
+  int4 *s4 = (int4 *)stage + threadIdx.x * 4;
+  int4 v[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) v[j] = s4[j];
+  int run = -1;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    run = max(run, v[j].x);
+    v[j].x = run;
+    run = max(run, v[j].y);
+    v[j].y = run;
+    run = max(run, v[j].z);
+    v[j].z = run;
+    run = max(run, v[j].w);
+    v[j].w = run;
+  }
+  int x = run;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x = max(x, y);
+  }
+  if (lane == 31) wmax[warp] = x;
+  __syncthreads();
+  int carry = -1;
+#pragma unroll
+  for (int w = 0; w < 8; ++w)
+    if (w < warp) carry = max(carry, wmax[w]);
+  const int ex = __shfl_up_sync(0xffffffffu, x, 1);
+  if (lane > 0) carry = max(carry, ex);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    v[j].x = max(v[j].x, carry);
+    v[j].y = max(v[j].y, carry);
+    v[j].z = max(v[j].z, carry);
+    v[j].w = max(v[j].w, carry);
+    s4[j] = v[j];
   }
 }
 
@@ -418,6 +445,26 @@ __device__ __forceinline__ int64_t sys_count(uint64_t X, int64_t n, uint64_t m, 
   while (kk > 0 && mul_le(X, den, (((uint64_t)(kk - 1)) << 23) + m, Q)) --kk;
   while (kk < n && !mul_le(X, den, (((uint64_t)kk) << 23) + m, Q)) ++kk;
   return kk;
+}
+
+// sys_count for n <= 2^21, without branches.  The float estimate est of
+// Y - u (Y = X n / Q, u = m / 2^23) is within 0.8 of it: X, Q and n / Q each
+// carry a relative error below 2^-23 and the product one below 2^-24, so Y
+// is off by less than 2^-21.6 Y <= 0.66 for Y <= n <= 2^21, and the final
+// subtraction rounds by at most 1/8.  K lies in [Y - u, Y - u + 1), so K is
+// ceil(est) - 1, ceil(est) or ceil(est) + 1, and the two exact tests f(kk - 1)
+// and f(kk) pick it.
+constexpr int64_t SYS_COUNT_SMALL_MAX_N = 1 << 21;
+__device__ __forceinline__ int32_t sys_count_small(uint64_t X, int32_t n, uint64_t m, uint64_t Q, float n_over_q) {
+  const uint64_t den = (uint64_t)n << 23;
+  const float xf = __fmaf_rn(__uint2float_rn((uint32_t)(X >> 32)), 0x1p32f, __uint2float_rn((uint32_t)X));
+  const float est = fminf(fmaxf(__fmul_rn(xf, n_over_q) - (float)m * 0x1p-23f, -1.0f), (float)n);
+  int32_t kk = (int32_t)ceilf(est);
+  kk = kk < 0 ? 0 : (kk > n ? n : kk);
+  // f(k) := (k 2^23 + m) Q < X den, true for k < K, false from K on
+  const bool f_lo = kk == 0 || !mul_le(X, den, (((uint64_t)(uint32_t)(kk - 1)) << 23) + m, Q);
+  const bool f_hi = kk < n && !mul_le(X, den, (((uint64_t)(uint32_t)kk) << 23) + m, Q);
+  return kk - (f_lo ? 0 : 1) + (f_hi ? 1 : 0);
 }
 
 }  // namespace mgb

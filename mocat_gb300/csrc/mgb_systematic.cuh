@@ -134,9 +134,9 @@ __device__ __forceinline__ void tile_sums_body(const float *__restrict__ lw, int
 }
 
 // Pass 2: one block per unit.  The block rescans its tile into exact
-// inclusive prefixes C_j and each thread's 8 consecutive particles write their
-// offspring ranges [K(C_{j-1}), K(C_j)) clipped to the unit's outputs (no
-// per-output search; a heavy particle just issues more stores).
+// inclusive prefixes C_j in shared memory and merges them with the sorted
+// thresholds of the unit's outputs (merge_fill): output k goes to the first
+// particle with C_j > T_k.
 __device__ __forceinline__ void systematic_body(const float *__restrict__ lw, int64_t n, const float *Mptr,
                                                           const int32_t *flag, const ResampleCtl *ctl,
                                                           const uint64_t *__restrict__ tile_pfx,
