@@ -69,40 +69,6 @@ __device__ __forceinline__ void sys_constants(uint64_t Q, uint64_t n, uint32_t m
   c.magic = magic;
 }
 
-// #{j < cnt : c[j] <= T} for sorted c, given the answer is >= from:
-// galloping steps 1, 2, 4, ... from `from`, then a binary search, so the cost is
-// O(log gap) even across long runs of zero-weight particles.
-__device__ __forceinline__ int count_le_from(const uint64_t *c, int cnt, uint64_t T, int from) {
-  if (from >= cnt || c[from] > T) return from;
-  int lo = from + 1, step = 1;  // c[lo - 1] <= T
-  int hi = lo;
-  while (true) {
-    hi = lo + step;
-    if (hi >= cnt) {
-      hi = cnt;
-      break;
-    }
-    if (c[hi - 1] > T) break;
-    lo = hi;
-    step <<= 1;
-  }
-  // answer in [lo, hi]: c[lo - 1] <= T, c[hi - 1] > T or hi == cnt
-  while (lo < hi) {
-    const int mid = (lo + hi) >> 1;
-    if (c[mid] <= T) lo = mid + 1;
-    else hi = mid;
-  }
-  return lo;
-}
-
-// T_k from the constants above (exact; one 64-bit high multiply + one fix-up)
-__device__ __forceinline__ uint64_t sys_threshold(const ResampleCtl &c, uint64_t k, uint64_t n) {
-  const uint64_t num = k * c.rn + c.bh;
-  uint64_t q = __umul64hi(num, c.magic);
-  if (num - q * n >= n) ++q;
-  return k * c.qn + c.a + q;
-}
-
 struct LsePartial {
   float m, s1, s2;
   int nan;
@@ -320,37 +286,6 @@ __device__ __forceinline__ void thr_next(ThrCursor &t, const ResampleCtl &c, uin
   const uint64_t carry = t.rem >= n ? 1ull : 0ull;
   t.rem -= carry * n;
   t.T += c.qn + carry;
-}
-
-// Merge-path fill of one unit: sC[0..cnt) are the tile's sorted inclusive
-// prefixes, outputs k in [kb, kb + nout) have sorted thresholds T_k; output k
-// goes to particle base + #{j : sC[j] <= T_k}.  Thread t merges diagonal
-// [16 t, 16 t + 16) after one partition search, O(1) work per element.
-constexpr int MERGE_PER = 16;
-__device__ __forceinline__ void merge_fill(const uint64_t *sC, int cnt, const ResampleCtl &c, int64_t kb, int nout,
-                                           int64_t base, int64_t n, int32_t *anc) {
-  const int total = cnt + nout;
-  const int d0 = threadIdx.x * MERGE_PER;
-  if (d0 >= total) return;
-  int lo = d0 > nout ? d0 - nout : 0, hi = d0 < cnt ? d0 : cnt;
-  while (lo < hi) {  // split: A[mid] before B[d0 - 1 - mid] iff sC[mid] <= T
-    const int mid = (lo + hi) >> 1;
-    const uint64_t T = thr_at(c, (uint64_t)(kb + d0 - 1 - mid), (uint64_t)n).T;
-    if (sC[mid] <= T) lo = mid + 1;
-    else hi = mid;
-  }
-  int i = lo, kk = d0 - lo;
-  ThrCursor cur = thr_at(c, (uint64_t)(kb + (kk < nout ? kk : 0)), (uint64_t)n);
-  const int d1 = d0 + MERGE_PER < total ? d0 + MERGE_PER : total;
-  for (int d = d0; d < d1; ++d) {
-    if (i < cnt && (kk >= nout || sC[i] <= cur.T)) {
-      ++i;
-    } else {
-      anc[kb + kk] = (int32_t)(base + (i < cnt ? i : cnt - 1));
-      ++kk;
-      thr_next(cur, c, (uint64_t)n);
-    }
-  }
 }
 
 // Offspring-run window of the persistent filter: RUN_WINDOW consecutive

@@ -35,7 +35,7 @@ __device__ __forceinline__ void load_tile_q(const float *__restrict__ lw, int64_
 constexpr int SYS_UNIT = SCAN_TILE;  // outputs per fill block
 
 // Pass 1: per-tile sums of q; the last block scans them in place into
-// exclusive tile prefixes P_t, sets Q and the threshold constants, and cuts
+// exclusive tile prefixes P_t, sets Q and the uniform's mantissa, and cuts
 // every tile's output range [K(P_t), K(P_{t+1})) into units of at most
 // SYS_UNIT outputs: units[u] = (t << 32) | first output of the unit.
 __device__ __forceinline__ void tile_sums_body(const float *__restrict__ lw, int64_t n, const float *Mptr,
@@ -123,28 +123,29 @@ __device__ __forceinline__ void tile_sums_body(const float *__restrict__ lw, int
     ctl->units = (unsigned int)utot;
     ctl->m23 = m;
     ctl->tile_counter = 0u;
-    ResampleCtl cc;
-    sys_constants(Q, (uint64_t)n, m, cc, ~0ull / (unsigned long long)n);
-    ctl->qn = cc.qn;
-    ctl->rn = cc.rn;
-    ctl->a = cc.a;
-    ctl->bh = cc.bh;
-    ctl->magic = cc.magic;
   }
 }
 
 // Pass 2: one block per unit.  The block rescans its tile into exact
-// inclusive prefixes C_j in shared memory and merges them with the sorted
-// thresholds of the unit's outputs (merge_fill): output k goes to the first
-// particle with C_j > T_k.
+// inclusive prefixes C_j (shared memory), computes every particle's offspring
+// count K(C_j) (sys_count_small, branch-free, for n <= 2^21; sys_count above)
+// and writes the unit's outputs [kb, ke) through a shared window: particle j's
+// run [K(C_{j-1}), K(C_j)) marks its first slot in the unit, an inclusive
+// max-scan gives every slot its particle, and the slots are stored coalesced.
+// Output k goes to the first particle with C_j > T_k, as in a merge of the
+// prefixes with the thresholds.
 __device__ __forceinline__ void systematic_body(const float *__restrict__ lw, int64_t n, const float *Mptr,
                                                           const int32_t *flag, const ResampleCtl *ctl,
                                                           const uint64_t *__restrict__ tile_pfx,
                                                           const uint64_t *__restrict__ units,
                                                           int32_t *__restrict__ anc, int *err) {
   if (flag && *flag == 0) return;
+  static_assert(SYS_UNIT <= RUN_WINDOW && SCAN_TPB == 256, "one window per unit");
   __shared__ unsigned long long wsum[SCAN_TPB / 32];
-  __shared__ uint64_t cs[SCAN_TILE];
+  __shared__ __align__(16) uint64_t cs[SCAN_TILE];  // prefixes, then the output window
+  __shared__ int32_t sK[SCAN_TILE];
+  __shared__ int32_t wmax[SCAN_TPB / 32];
+  __shared__ int32_t k0_s;
   const int64_t ntiles_real = (n + SCAN_TILE - 1) / SCAN_TILE;
   const uint64_t Q = *(volatile const unsigned long long *)&ctl->total;
   const int degenerate = *(volatile const int *)&ctl->degenerate || Q == 0;
@@ -183,9 +184,39 @@ __device__ __forceinline__ void systematic_body(const float *__restrict__ lw, in
     cs[threadIdx.x * SCAN_IPT + j] = cc;
   }
   __syncthreads();
-  const ResampleCtl c = *ctl;
   const int cnt_valid = (int)(n - base < SCAN_TILE ? n - base : SCAN_TILE);
-  merge_fill(cs, cnt_valid, c, kb, (int)(ke - kb), base, n, anc);
+  const bool small = n <= SYS_COUNT_SMALL_MAX_N;
+  // K of the tile's particles (past n: K = n, empty runs after the last particle)
+#pragma unroll
+  for (int r = 0; r < SCAN_IPT; ++r) {
+    const int jj = threadIdx.x + SCAN_TPB * r;
+    int32_t k = (int32_t)n;
+    if (jj < cnt_valid)
+      k = small ? sys_count_small(cs[jj], (int32_t)n, m, Q, n_over_q) : (int32_t)sys_count(cs[jj], n, m, Q, n_over_q);
+    sK[jj] = k;
+  }
+  if (threadIdx.x == 0)
+    k0_s = small ? sys_count_small(P, (int32_t)n, m, Q, n_over_q) : (int32_t)sys_count(P, n, m, Q, n_over_q);
+  __syncthreads();
+  int32_t *stage = (int32_t *)cs;
+  int4 *s4 = (int4 *)stage;
+#pragma unroll
+  for (int j = 0; j < RUN_WINDOW / 4 / SCAN_TPB; ++j) s4[threadIdx.x + SCAN_TPB * j] = make_int4(-1, -1, -1, -1);
+  __syncthreads();
+  const int32_t k0 = k0_s, w0 = (int32_t)kb, w1 = (int32_t)ke;
+#pragma unroll
+  for (int r = 0; r < SCAN_IPT; ++r) {
+    const int jj = threadIdx.x + SCAN_TPB * r;
+    const int32_t lo = jj ? sK[jj - 1] : k0, hi = sK[jj];
+    const int32_t st = lo > w0 ? lo : w0;
+    if (hi > st && st < w1) stage[st - w0] = jj;
+  }
+  __syncthreads();
+  window_max_scan(stage, wmax);
+  __syncthreads();
+  // every slot is covered (slot 0 by the run through kb); the clamp only keeps a
+  // wrong count from producing an out-of-range ancestor
+  for (int q = threadIdx.x; q < w1 - w0; q += SCAN_TPB) anc[w0 + q] = (int32_t)(base + max(stage[q], 0));
 }
 
 }  // namespace mgb
