@@ -27,7 +27,6 @@ struct PersistArgs {
   float *x_hist, *lw_hist;        // (T, d, n), (T, n) or null
   int32_t *anc;
   LsePartial *parts;              // 2 * PP_MAX_CHUNKS (one per chunk, double-buffered by step parity)
-  int *chunk_ctr;                 // (T,) chunk counters (zeroed)
   uint64_t *cloc;                 // (n,) within-tile inclusive fixed-point prefixes
   uint64_t *tile_sum;             // tiles
   int *degen;                     // (T,) degenerate-weights flag per step
@@ -69,7 +68,6 @@ inline bool persistent_ok(int64_t n, int scheme) {
 
 struct PersistWs {
   LsePartial *parts;
-  int *chunk_ctr;
   uint64_t *cloc;
   uint64_t *tile_sum;
   int *degen;
@@ -81,7 +79,6 @@ struct PersistWs {
 inline PersistWs carve_persist(Carver &c, int64_t n, int64_t T) {
   PersistWs w;
   w.parts = c.take<LsePartial>(2 * PP_MAX_CHUNKS);
-  w.chunk_ctr = c.take<int>((size_t)T);
   w.cloc = c.take<uint64_t>((size_t)n);
   w.tile_sum = c.take<uint64_t>((size_t)((n + SCAN_TILE - 1) / SCAN_TILE));
   w.degen = c.take<int>((size_t)T);
@@ -98,7 +95,6 @@ inline int persist_setup(const RunWs &w, const PersistWs &pw, int64_t n, int64_t
   if (cudaMemsetAsync(pw.degen, 0, sizeof(int) * T, s) != cudaSuccess) return ERR_CUDA;
   if (cudaMemsetAsync(pw.bar, 0, sizeof(GridBar), s) != cudaSuccess) return ERR_CUDA;
   if (cudaMemsetAsync(pw.err, 0, sizeof(int), s) != cudaSuccess) return ERR_CUDA;
-  if (cudaMemsetAsync(pw.chunk_ctr, 0, sizeof(int) * T, s) != cudaSuccess) return ERR_CUDA;
   const bool hx = out && out->x_hist, hl = out && out->lw_hist;
   a.n = n;
   a.T = T;
@@ -114,7 +110,6 @@ inline int persist_setup(const RunWs &w, const PersistWs &pw, int64_t n, int64_t
   a.lw_hist = hl ? out->lw_hist : nullptr;
   a.anc = w.anc;
   a.parts = pw.parts;
-  a.chunk_ctr = pw.chunk_ctr;
   a.cloc = pw.cloc;
   a.tile_sum = pw.tile_sum;
   a.degen = pw.degen;
