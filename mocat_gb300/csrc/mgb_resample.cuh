@@ -288,23 +288,25 @@ __device__ __forceinline__ void thr_next(ThrCursor &t, const ResampleCtl &c, uin
   t.T += c.qn + carry;
 }
 
-// Offspring-run window of the persistent filter: RUN_WINDOW consecutive
-// outputs in shared memory.  Every particle whose run [lo, hi) meets the window
-// marks the window slot of its first output there with its tile-local number;
-// an inclusive max-scan then gives every slot the particle that covers it (runs
-// are disjoint and ordered by particle, so the covering particle is the largest
-// mark at or before the slot).  256 threads, 16 consecutive slots each.
+// Offspring-run window: RUN_WINDOW consecutive outputs in shared memory.
+// Every particle whose run [lo, hi) meets the window marks the window slot of
+// its first output there with its tile-local number; an inclusive max-scan
+// then gives every slot the particle that covers it (runs are disjoint and
+// ordered by particle, so the covering particle is the largest mark at or
+// before the slot).  TPB threads, RUN_WINDOW / TPB consecutive slots each.
 constexpr int RUN_WINDOW = 4096;
-__device__ __forceinline__ void window_max_scan(int32_t *stage, int32_t *wmax /* >= 8 */) {
-  static_assert(RUN_WINDOW == 256 * 16, "16 slots per thread");
+template <int TPB = 256>
+__device__ __forceinline__ void window_max_scan(int32_t *stage, int32_t *wmax /* >= TPB / 32 */) {
+  constexpr int V = RUN_WINDOW / TPB / 4;  // int4 per thread
+  static_assert(V * 4 * TPB == RUN_WINDOW && TPB % 32 == 0, "whole int4 slots per thread");
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int4 *s4 = (int4 *)stage + threadIdx.x * 4;
-  int4 v[4];
+  int4 *s4 = (int4 *)stage + threadIdx.x * V;
+  int4 v[V];
 #pragma unroll
-  for (int j = 0; j < 4; ++j) v[j] = s4[j];
+  for (int j = 0; j < V; ++j) v[j] = s4[j];
   int run = -1;
 #pragma unroll
-  for (int j = 0; j < 4; ++j) {
+  for (int j = 0; j < V; ++j) {
     run = max(run, v[j].x);
     v[j].x = run;
     run = max(run, v[j].y);
@@ -324,12 +326,12 @@ __device__ __forceinline__ void window_max_scan(int32_t *stage, int32_t *wmax /*
   __syncthreads();
   int carry = -1;
 #pragma unroll
-  for (int w = 0; w < 8; ++w)
+  for (int w = 0; w < TPB / 32; ++w)
     if (w < warp) carry = max(carry, wmax[w]);
   const int ex = __shfl_up_sync(0xffffffffu, x, 1);
   if (lane > 0) carry = max(carry, ex);
 #pragma unroll
-  for (int j = 0; j < 4; ++j) {
+  for (int j = 0; j < V; ++j) {
     v[j].x = max(v[j].x, carry);
     v[j].y = max(v[j].y, carry);
     v[j].z = max(v[j].z, carry);
@@ -338,7 +340,9 @@ __device__ __forceinline__ void window_max_scan(int32_t *stage, int32_t *wmax /*
   }
 }
 
-// block-wide exclusive scan of one u64 per thread (returns the block total too)
+// block-wide exclusive scan of one u64 per thread over TPB threads (returns the
+// block total too); sm holds TPB / 32 words
+template <int TPB = SCAN_TPB>
 __device__ __forceinline__ unsigned long long block_excl_scan_u64(unsigned long long v, unsigned long long *sm,
                                                                   unsigned long long &total) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -353,7 +357,7 @@ __device__ __forceinline__ unsigned long long block_excl_scan_u64(unsigned long 
   __syncthreads();
   unsigned long long wpre = 0, tot = 0;
 #pragma unroll
-  for (int w = 0; w < SCAN_TPB / 32; ++w) {
+  for (int w = 0; w < TPB / 32; ++w) {
     if (w < warp) wpre += sm[w];
     tot += sm[w];
   }
