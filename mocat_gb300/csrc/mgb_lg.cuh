@@ -51,24 +51,27 @@ __device__ __forceinline__ float lg_potential(const LGP<D, DY> &p, const float (
 }
 
 // x_new = F x + Lq eps (fma chains in ascending column order)
+// row r of the transition mean F x and of the noise Lq e
+template <int D, int DY>
+__device__ __forceinline__ float lg_mean_row(const LGP<D, DY> &p, const float (&xs)[D], int r) {
+  float fx = __fmul_rn(p.F[r * D], xs[0]);
+#pragma unroll
+  for (int k = 1; k < D; ++k) fx = __fmaf_rn(p.F[r * D + k], xs[k], fx);
+  return fx;
+}
+template <int D, int DY>
+__device__ __forceinline__ float lg_noise_row(const LGP<D, DY> &p, const float (&e)[D], int r) {
+  if (p.lq_diag) return __fmul_rn(p.Lq[r * D + r], e[r]);
+  float le = __fmul_rn(p.Lq[r * D], e[0]);
+#pragma unroll
+  for (int k = 1; k < D; ++k) le = __fmaf_rn(p.Lq[r * D + k], e[k], le);
+  return le;
+}
 template <int D, int DY>
 __device__ __forceinline__ void lg_transition(const LGP<D, DY> &p, const float (&xs)[D], const float (&e)[D],
                                               float (&xn)[D]) {
 #pragma unroll
-  for (int r = 0; r < D; ++r) {
-    float fx = __fmul_rn(p.F[r * D], xs[0]);
-#pragma unroll
-    for (int k = 1; k < D; ++k) fx = __fmaf_rn(p.F[r * D + k], xs[k], fx);
-    float le;
-    if (p.lq_diag) {
-      le = __fmul_rn(p.Lq[r * D + r], e[r]);
-    } else {
-      le = __fmul_rn(p.Lq[r * D], e[0]);
-#pragma unroll
-      for (int k = 1; k < D; ++k) le = __fmaf_rn(p.Lq[r * D + k], e[k], le);
-    }
-    xn[r] = __fadd_rn(fx, le);
-  }
+  for (int r = 0; r < D; ++r) xn[r] = __fadd_rn(lg_mean_row<D, DY>(p, xs, r), lg_noise_row<D, DY>(p, e, r));
 }
 
 template <int D>
@@ -108,26 +111,52 @@ __device__ __forceinline__ float lg_particle_regs(const LGP<D, DY> &p, int64_t n
   return l;
 }
 
-template <int D, int DY, bool CG = false>
-__device__ __forceinline__ float lg_particle(const LGP<D, DY> &p, int64_t n, uint32_t ka, uint32_t kb, int64_t i,
-                                             bool res, const float *__restrict__ x_prev, const int32_t *anc,
-                                             const float *lws, const float *y, float *__restrict__ x_new,
-                                             float *__restrict__ lw_new) {
-  uint32_t b[D];
-  bits_vec<D>(ka, kb, b, p.one);
-  float e[D], xs[D], xn[D];
-#pragma unroll
-  for (int j = 0; j < D; ++j) e[j] = bits_to_normal(b[j]);
+// MUS > 0: also writes the particle's proposal row for the score's backward
+// kernel, mu[i * MUS ..] = (F x_src (the transition mean, the same float
+// operations as the propagate), the carried log-weight, zero padding)
+template <int D, int DY, bool CG = false, int MUS = 0>
+__device__ __forceinline__ float lg_particle_e(const LGP<D, DY> &p, int64_t n, const float (&e)[D], int64_t i,
+                                               bool res, const float *__restrict__ x_prev, const int32_t *anc,
+                                               const float *lws, const float *y, float *__restrict__ x_new,
+                                               float *__restrict__ lw_new, float *__restrict__ mu = nullptr) {
+  float xs[D], xn[D];
   const int64_t src = res ? (int64_t)ld<CG>(&anc[i]) : i;
 #pragma unroll
   for (int j = 0; j < D; ++j) xs[j] = ld<CG>(&x_prev[j * n + src]);
-  lg_transition<D, DY>(p, xs, e, xn);
+  const float lres = lws ? ld<CG>(&lws[i]) : 0.0f;
+  if (MUS > 0) {
+    static_assert(MUS == 0 || (MUS % 4 == 0 && MUS > D), "16-byte rows holding D means and the log-weight");
+    float row[MUS > 0 ? MUS : 4];
+#pragma unroll
+    for (int r = 0; r < D; ++r) row[r] = lg_mean_row<D, DY>(p, xs, r);
+    row[D] = lres;
+#pragma unroll
+    for (int r = D + 1; r < MUS; ++r) row[r] = 0.0f;
+    float4 *o = reinterpret_cast<float4 *>(mu + i * MUS);
+#pragma unroll
+    for (int j = 0; j < MUS / 4; ++j) o[j] = make_float4(row[4 * j], row[4 * j + 1], row[4 * j + 2], row[4 * j + 3]);
+#pragma unroll
+    for (int r = 0; r < D; ++r) xn[r] = __fadd_rn(row[r], lg_noise_row<D, DY>(p, e, r));
+  } else {
+    lg_transition<D, DY>(p, xs, e, xn);
+  }
 #pragma unroll
   for (int r = 0; r < D; ++r) x_new[r * n + i] = xn[r];
-  const float lres = lws ? ld<CG>(&lws[i]) : 0.0f;
   const float l = __fsub_rn(lres, lg_potential<D, DY>(p, xn, y));
   lw_new[i] = l;
   return l;
+}
+template <int D, int DY, bool CG = false, int MUS = 0>
+__device__ __forceinline__ float lg_particle(const LGP<D, DY> &p, int64_t n, uint32_t ka, uint32_t kb, int64_t i,
+                                             bool res, const float *__restrict__ x_prev, const int32_t *anc,
+                                             const float *lws, const float *y, float *__restrict__ x_new,
+                                             float *__restrict__ lw_new, float *__restrict__ mu = nullptr) {
+  uint32_t b[D];
+  bits_vec<D>(ka, kb, b, p.one);
+  float e[D];
+#pragma unroll
+  for (int j = 0; j < D; ++j) e[j] = bits_to_normal(b[j]);
+  return lg_particle_e<D, DY, CG, MUS>(p, n, e, i, res, x_prev, anc, lws, y, x_new, lw_new, mu);
 }
 
 // initial draw of one particle: x = C0 eps + m0, lw = -potential(x, y0)

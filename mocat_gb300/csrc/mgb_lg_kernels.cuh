@@ -36,14 +36,15 @@ __global__ void __launch_bounds__(PF_TPB) k_lg_init(const __grid_constant__ LGP<
   if (FUSED) pf_reduce<PF_TPB>(l, active, ctl, 0);
 }
 
-// one bootstrap step; res_flag (nullable) decides resampled vs identity at run time
-template <int D, int DY, bool FUSED>
+// one bootstrap step; res_flag (nullable) decides resampled vs identity at run time.
+// MUS > 0: also the score's proposal rows mu (lg_particle)
+template <int D, int DY, bool FUSED, int MUS = 0>
 __global__ void __launch_bounds__(PF_TPB) k_lg_step(const __grid_constant__ LGP<D, DY> p, int64_t n,
                                                      const uint32_t *key, const float *y_t,
                                                      const float *__restrict__ x_prev, const int32_t *anc,
                                                      const float *lw_prev, const int32_t *res_flag,
                                                      float *__restrict__ x_new, float *__restrict__ lw_new,
-                                                     PFCtl ctl, int64_t t) {
+                                                     PFCtl ctl, int64_t t, float *__restrict__ mu = nullptr) {
   const int64_t i = blockIdx.x * (int64_t)PF_TPB + threadIdx.x;
   const bool res = res_flag ? (*res_flag != 0) : (anc != nullptr);
   const uint32_t k0 = key[0], k1 = key[1];
@@ -53,20 +54,12 @@ __global__ void __launch_bounds__(PF_TPB) k_lg_step(const __grid_constant__ LGP<
   float l = -INFINITY;
   const bool active = i < n;
   if (active) {
-    float e[D], xs[D], xn[D];
+    float e[D];
     particle_normals<D>(k0, k1, n, i, e);
-    const int64_t src = res ? (int64_t)anc[i] : i;
-#pragma unroll
-    for (int j = 0; j < D; ++j) xs[j] = __ldg(&x_prev[j * n + src]);
-    lg_transition<D, DY>(p, xs, e, xn);
-#pragma unroll
-    for (int r = 0; r < D; ++r) x_new[r * n + i] = xn[r];
     // run mode (res_flag set): lw_res = 0 after a resample (filtering.py:292);
     // standalone mode: lw_prev as given (NULL = 0)
     const float *lws = res_flag ? (res ? nullptr : lw_prev) : lw_prev;
-    const float lres = lws ? lws[i] : 0.0f;
-    l = __fsub_rn(lres, lg_potential<D, DY>(p, xn, y));
-    lw_new[i] = l;
+    l = lg_particle_e<D, DY, false, MUS>(p, n, e, i, res, x_prev, anc, lws, y, x_new, lw_new, mu);
   }
   if (FUSED) pf_reduce<PF_TPB>(l, active, ctl, t);
 }
@@ -75,12 +68,12 @@ __global__ void __launch_bounds__(PF_TPB) k_lg_step(const __grid_constant__ LGP<
 // key of particle i is (T(2i, 2i+n).x0, T(2i+1, 2i+1+n).x0) and the key of
 // particle i + n/2 is the .x1 halves of the same two cipher calls, so the
 // pair costs two key-split evaluations instead of four.
-template <int D, int DY, bool FUSED>
+template <int D, int DY, bool FUSED, int MUS = 0>
 __device__ __forceinline__ void lg_step2_body(const LGP<D, DY> &p, int64_t n, const uint32_t *key, const float *y_t,
                                               const float *__restrict__ x_prev, const int32_t *anc,
                                               const float *lw_prev, const int32_t *res_flag,
                                               float *__restrict__ x_new, float *__restrict__ lw_new,
-                                              const PFCtl &ctl, int64_t t) {
+                                              const PFCtl &ctl, int64_t t, float *__restrict__ mu = nullptr) {
   const int64_t h = n >> 1;
   const int64_t i = blockIdx.x * (int64_t)PF_TPB + threadIdx.x;
   const bool res = res_flag ? (*res_flag != 0) : (anc != nullptr);
@@ -98,21 +91,21 @@ __device__ __forceinline__ void lg_step2_body(const LGP<D, DY> &p, int64_t n, co
     // two-trip loop, not unrolled: one copy of the particle code (instruction cache)
 #pragma unroll 1
     for (int s = 0; s < 2; ++s) {
-      const float l = lg_particle<D, DY>(p, n, s ? r1 : r0, s ? s1 : s0, s ? i + h : i, res, x_prev, anc, lws, y,
-                                         x_new, lw_new);
+      const float l = lg_particle<D, DY, false, MUS>(p, n, s ? r1 : r0, s ? s1 : s0, s ? i + h : i, res, x_prev,
+                                                     anc, lws, y, x_new, lw_new, mu);
       online_acc(l, m, a1, a2, nanf);
     }
   }
   if (FUSED) pf_reduce_online<PF_TPB>(m, a1, a2, nanf, ctl, t);
 }
-template <int D, int DY, bool FUSED>
+template <int D, int DY, bool FUSED, int MUS = 0>
 __global__ void __launch_bounds__(PF_TPB, 2) k_lg_step2(const __grid_constant__ LGP<D, DY> p, int64_t n,
                                                          const uint32_t *key, const float *y_t,
                                                          const float *__restrict__ x_prev, const int32_t *anc,
                                                          const float *lw_prev, const int32_t *res_flag,
                                                          float *__restrict__ x_new, float *__restrict__ lw_new,
-                                                         PFCtl ctl, int64_t t) {
-  lg_step2_body<D, DY, FUSED>(p, n, key, y_t, x_prev, anc, lw_prev, res_flag, x_new, lw_new, ctl, t);
+                                                         PFCtl ctl, int64_t t, float *__restrict__ mu = nullptr) {
+  lg_step2_body<D, DY, FUSED, MUS>(p, n, key, y_t, x_prev, anc, lw_prev, res_flag, x_new, lw_new, ctl, t, mu);
 }
 
 }  // namespace mgb

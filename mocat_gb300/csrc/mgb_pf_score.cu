@@ -122,43 +122,6 @@ __global__ void __launch_bounds__(SC_TPB) k_score_init(const __grid_constant__ S
   }
 }
 
-// proposal rows of step t: mu_m = A x_{t-1}^{src(m)} (the transition's fma chain), lb_m
-template <int D>
-__device__ __forceinline__ void score_mu_body(const ScoreP<D> &c, int64_t n, const float *__restrict__ xprev,
-                                              const int32_t *anc, const int32_t *res_flag, const float *lw_prev,
-                                              float *__restrict__ mu) {
-  using S = ScoreDims<D>;
-  const int64_t m = blockIdx.x * (int64_t)SC_TPB + threadIdx.x;
-  if (m >= n) return;
-  const int res = *res_flag;
-  const int64_t src = res ? (int64_t)anc[m] : m;
-  float xs[D];
-#pragma unroll
-  for (int k = 0; k < D; ++k) xs[k] = __ldg(&xprev[k * n + src]);
-  float row[S::MS];
-#pragma unroll
-  for (int r = 0; r < D; ++r) {
-    float fx = __fmul_rn(c.F[r * D], xs[0]);
-#pragma unroll
-    for (int k = 1; k < D; ++k) fx = __fmaf_rn(c.F[r * D + k], xs[k], fx);
-    row[r] = fx;
-  }
-  row[D] = res ? 0.0f : lw_prev[m];
-#pragma unroll
-  for (int r = D + 1; r < S::MS; ++r) row[r] = 0.0f;
-  float4 *o = reinterpret_cast<float4 *>(mu + m * S::MS);
-#pragma unroll
-  for (int j = 0; j < S::MS / 4; ++j) o[j] = make_float4(row[4 * j], row[4 * j + 1], row[4 * j + 2], row[4 * j + 3]);
-}
-
-template <int D>
-__global__ void __launch_bounds__(SC_TPB) k_score_mu(const __grid_constant__ ScoreP<D> c, int64_t n,
-                                                      const float *__restrict__ xprev, const int32_t *anc,
-                                                      const int32_t *res_flag, const float *lw_prev,
-                                                      float *__restrict__ mu) {
-  score_mu_body<D>(c, n, xprev, anc, res_flag, lw_prev, mu);
-}
-
 // one PaRIS step: backward draws, then tau_t^i
 // KK = the number of backward draws, a compile-time constant so that only KK draws'
 // residuals and sources occupy registers
@@ -416,13 +379,14 @@ static int score_lg(const mgb_lg_model *m, int64_t n, int64_t T, const uint32_t 
     if ((st = launch_resample(la, n, scheme, &r.st->M, r.keys + 2 * t, 0, 0u, r.res_hist + t, r.rws, r.anc, nullptr,
                               s)))
       return st;
+    // the propagate also writes the proposal rows mu (F x of each particle's source and its
+    // carried log-weight) that the backward draws of this step read
     if (n % 2 == 0)
-      k_lg_step2<D, D, true><<<grid2, PF_TPB, 0, s>>>(p, n, r.keys + 2 * t, y + (size_t)t * D, xa, r.anc, la,
-                                                      r.res_hist + t, xb, lb, ctl, t);
+      k_lg_step2<D, D, true, S::MS><<<grid2, PF_TPB, 0, s>>>(p, n, r.keys + 2 * t, y + (size_t)t * D, xa, r.anc, la,
+                                                             r.res_hist + t, xb, lb, ctl, t, w.mu);
     else
-      k_lg_step<D, D, true><<<grid, PF_TPB, 0, s>>>(p, n, r.keys + 2 * t, y + (size_t)t * D, xa, r.anc, la,
-                                                    r.res_hist + t, xb, lb, ctl, t);
-    k_score_mu<D><<<gs, SC_TPB, 0, s>>>(c, n, xa, r.anc, r.res_hist + t, la, w.mu);
+      k_lg_step<D, D, true, S::MS><<<grid, PF_TPB, 0, s>>>(p, n, r.keys + 2 * t, y + (size_t)t * D, xa, r.anc, la,
+                                                           r.res_hist + t, xb, lb, ctl, t, w.mu);
     a.x = xb;
     a.xprev = xa;
     a.mu = w.mu;
@@ -500,17 +464,11 @@ __global__ void __launch_bounds__(PF_TPB, 2) k_lg_step2_b(const __grid_constant_
                                                            const uint32_t *key, const float *y_t, const float *x_prev,
                                                            const int32_t *anc, const float *lw_prev,
                                                            const int32_t *res_flag, float *x_new, float *lw_new,
-                                                           PFCtl ctl, int64_t t, int64_t ws) {
+                                                           PFCtl ctl, int64_t t, float *mu, int64_t ws) {
   const int64_t o = (int64_t)blockIdx.y * ws;
-  lg_step2_body<D, D, true>(p, n, slab(key, o), y_t, slab(x_prev, o), slab(anc, o), slab(lw_prev, o),
-                            slab(res_flag, o), slab(x_new, o), slab(lw_new, o), slab_ctl(ctl, o), t);
-}
-template <int D>
-__global__ void __launch_bounds__(SC_TPB) k_score_mu_b(const __grid_constant__ ScoreP<D> c, int64_t n,
-                                                        const float *xprev, const int32_t *anc, const int32_t *res_flag,
-                                                        const float *lw_prev, float *mu, int64_t ws) {
-  const int64_t o = (int64_t)blockIdx.y * ws;
-  score_mu_body<D>(c, n, slab(xprev, o), slab(anc, o), slab(res_flag, o), slab(lw_prev, o), slab(mu, o));
+  lg_step2_body<D, D, true, ScoreDims<D>::MS>(p, n, slab(key, o), y_t, slab(x_prev, o), slab(anc, o),
+                                              slab(lw_prev, o), slab(res_flag, o), slab(x_new, o), slab(lw_new, o),
+                                              slab_ctl(ctl, o), t, slab(mu, o));
 }
 template <int D, int KK>
 __global__ void __launch_bounds__(SC_TPB) k_score_step_b(const __grid_constant__ ScoreP<D> c, int64_t n,
@@ -606,8 +564,7 @@ static int score_lg_batch(const mgb_lg_model *m, int64_t n, int64_t T, int64_t B
     k_systematic_b<<<dim3(2 * tiles, (unsigned)B), SCAN_TPB, 0, s>>>(la, n, &r0.st->M, r0.res_hist + t, r0.rws.ctl,
                                                                      r0.rws.status, r0.rws.status2, r0.anc, W);
     k_lg_step2_b<D><<<dim3(grid2, (unsigned)B), PF_TPB, 0, s>>>(p, n, r0.keys + 2 * t, y + (size_t)t * D, xa, r0.anc,
-                                                                la, r0.res_hist + t, xb, lb, ctl0, t, W);
-    k_score_mu_b<D><<<dim3(gs, (unsigned)B), SC_TPB, 0, s>>>(c, n, xa, r0.anc, r0.res_hist + t, la, w0.mu, W);
+                                                                la, r0.res_hist + t, xb, lb, ctl0, t, w0.mu, W);
     a.x = xb;
     a.xprev = xa;
     a.mu = w0.mu;
