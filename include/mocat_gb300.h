@@ -147,7 +147,10 @@ int mgb_gather_rows(const float *x_dev, int64_t width, const int32_t *ancestors_
  *   F, Lq, C0: d x d (transition_matrix, transition_covariance_sqrt,
  *   initial_covariance_sqrt); H: dy x d (likelihood_matrix); P: dy x dy
  *   (likelihood_precision_sqrt); m0: d; c = (dy log 2 pi - log det_prec) / 2.
- * Supported (d, dy): (d, 1) for d in {1,2,3,4,5,8,10}; (d, d) for d in {2,3,4,5,8,10}.
+ * Compiled (d, dy): (d, 1) for d in {1,2,3,4,5,8,10}; (d, d) for d in {2,3,4,5,8,10}.
+ * mgb_pf_lg_init / mgb_pf_lg_propagate / mgb_pf_lg_run also take any other d, dy <= 32
+ * (run-time-dimension kernels, the same values, one launch per phase and step); the
+ * other entry points that take this model need a compiled pair.
  */
 typedef struct {
   int32_t d, dy;

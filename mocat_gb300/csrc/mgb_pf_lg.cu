@@ -166,6 +166,235 @@ static int step_lg(const mgb_lg_model *m, int64_t n, const uint32_t *key, const 
   return launch_status();
 }
 
+// ---------------------------------------------------------------------------
+// Run-time dimensions: the bootstrap filter for (d, dy) pairs without a compiled
+// instance (d, dy <= LGD_MAX).  One particle per thread, the model's matrices in
+// the kernel's parameter block (read through the constant cache, every thread
+// at the same address), the per-particle vectors in local arrays.  Every value
+// is the same float operation sequence as the templated kernels' (the fma
+// chains of lg_transition / lg_potential / k_lg_init, the same draws), so the
+// results are the oracle's bit for bit; only the speed differs.
+constexpr int LGD_MAX = 32;
+struct LGDyn {
+  float F[LGD_MAX * LGD_MAX], Lq[LGD_MAX * LGD_MAX], H[LGD_MAX * LGD_MAX], P[LGD_MAX * LGD_MAX],
+      C0[LGD_MAX * LGD_MAX], m0[LGD_MAX];
+  float c;
+  int d, dy, lq_diag, h_eye, p_diag;
+};
+
+static bool lgd_ok(const mgb_lg_model *m) { return m->d <= LGD_MAX && m->dy <= LGD_MAX; }
+
+static LGDyn pack_lgd(const mgb_lg_model *m) {
+  LGDyn p;
+  const int d = m->d, dy = m->dy;
+  p.d = d;
+  p.dy = dy;
+  for (int i = 0; i < d * d; ++i) {
+    p.F[i] = m->F[i];
+    p.Lq[i] = m->Lq[i];
+    p.C0[i] = m->C0[i];
+  }
+  for (int i = 0; i < dy * d; ++i) p.H[i] = m->H[i];
+  for (int i = 0; i < dy * dy; ++i) p.P[i] = m->P[i];
+  for (int i = 0; i < d; ++i) p.m0[i] = m->m0[i];
+  p.c = m->c;
+  auto diag = [](const float *a, int k) {
+    for (int r = 0; r < k; ++r)
+      for (int c = 0; c < k; ++c)
+        if (r != c && a[r * k + c] != 0.0f) return 0;
+    return 1;
+  };
+  p.lq_diag = diag(p.Lq, d);
+  p.p_diag = diag(p.P, dy);
+  p.h_eye = 0;
+  if (dy == d) {
+    int eye = 1;
+    for (int r = 0; r < d; ++r)
+      for (int c = 0; c < d; ++c) eye &= p.H[r * d + c] == (r == c ? 1.0f : 0.0f);
+    p.h_eye = eye;
+  }
+  return p;
+}
+
+// normal(split(k, n)[i], (d,)): ceil(d / 2) cipher calls, counters (j, j + H)
+__device__ __forceinline__ void lgd_normals(uint32_t k0, uint32_t k1, int64_t n, int64_t i, int d, float *e) {
+  uint32_t a0, a1;
+  split_at(k0, k1, (uint64_t)n, (uint64_t)i, a0, a1);
+  const int H = (d + 1) / 2;
+  for (int j = 0; j < H; ++j) {
+    uint32_t r0, r1;
+    threefry2x32(a0, a1, (uint32_t)j, (j + H < d) ? (uint32_t)(j + H) : 0u, r0, r1);
+    e[j] = bits_to_normal(r0);
+    if (j + H < d) e[j + H] = bits_to_normal(r1);
+  }
+}
+
+__device__ __forceinline__ float lgd_potential(const LGDyn &p, const float *x, const float *y) {
+  const int d = p.d, dy = p.dy;
+  float diff[LGD_MAX];
+  if (dy == d && p.h_eye) {
+    for (int j = 0; j < dy; ++j) diff[j] = __fsub_rn(y[j], x[j]);
+  } else {
+    for (int j = 0; j < dy; ++j) {
+      float hx = __fmul_rn(p.H[j * d], x[0]);
+      for (int k = 1; k < d; ++k) hx = __fmaf_rn(p.H[j * d + k], x[k], hx);
+      diff[j] = __fsub_rn(y[j], hx);
+    }
+  }
+  float quad = 0.0f;
+  for (int k = 0; k < dy; ++k) {
+    float v;
+    if (p.p_diag) {
+      v = __fmul_rn(diff[k], p.P[k * dy + k]);
+    } else {
+      v = __fmul_rn(diff[0], p.P[k]);
+      for (int j = 1; j < dy; ++j) v = __fmaf_rn(diff[j], p.P[j * dy + k], v);
+    }
+    quad = k == 0 ? __fmul_rn(v, v) : __fmaf_rn(v, v, quad);
+  }
+  return __fadd_rn(__fmul_rn(0.5f, quad), p.c);
+}
+
+template <bool FUSED>
+__global__ void __launch_bounds__(PF_TPB) k_lgd_init(const __grid_constant__ LGDyn p, int64_t n, const uint32_t *key,
+                                                      const float *y0, float *__restrict__ x,
+                                                      float *__restrict__ lw, PFCtl ctl) {
+  const int64_t i = blockIdx.x * (int64_t)PF_TPB + threadIdx.x;
+  const uint32_t k0 = key[0], k1 = key[1];
+  __shared__ float y[LGD_MAX];
+  if (threadIdx.x < p.dy) y[threadIdx.x] = y0 ? y0[threadIdx.x] : 0.0f;
+  __syncthreads();
+  float l = -INFINITY;
+  const bool active = i < n;
+  if (active) {
+    const int d = p.d;
+    float e[LGD_MAX], xv[LGD_MAX];
+    lgd_normals(k0, k1, n, i, d, e);
+    for (int r = 0; r < d; ++r) {
+      float v = __fmul_rn(p.C0[r * d], e[0]);
+      for (int k = 1; k < d; ++k) v = __fmaf_rn(p.C0[r * d + k], e[k], v);
+      xv[r] = __fadd_rn(v, p.m0[r]);
+      x[r * n + i] = xv[r];
+    }
+    l = y0 ? -lgd_potential(p, xv, y) : 0.0f;
+    lw[i] = l;
+  }
+  if (FUSED) pf_reduce<PF_TPB>(l, active, ctl, 0);
+}
+
+// one step; res_flag (nullable) decides resampled vs identity at run time, as k_lg_step
+template <bool FUSED>
+__global__ void __launch_bounds__(PF_TPB) k_lgd_step(const __grid_constant__ LGDyn p, int64_t n, const uint32_t *key,
+                                                      const float *y_t, const float *__restrict__ x_prev,
+                                                      const int32_t *anc, const float *lw_prev,
+                                                      const int32_t *res_flag, float *__restrict__ x_new,
+                                                      float *__restrict__ lw_new, PFCtl ctl, int64_t t) {
+  const int64_t i = blockIdx.x * (int64_t)PF_TPB + threadIdx.x;
+  const bool res = res_flag ? (*res_flag != 0) : (anc != nullptr);
+  const uint32_t k0 = key[0], k1 = key[1];
+  __shared__ float y[LGD_MAX];
+  if (threadIdx.x < p.dy) y[threadIdx.x] = y_t[threadIdx.x];
+  __syncthreads();
+  float l = -INFINITY;
+  const bool active = i < n;
+  if (active) {
+    const int d = p.d;
+    float e[LGD_MAX], xs[LGD_MAX], xn[LGD_MAX];
+    lgd_normals(k0, k1, n, i, d, e);
+    const int64_t src = res ? (int64_t)anc[i] : i;
+    for (int j = 0; j < d; ++j) xs[j] = __ldg(&x_prev[j * n + src]);
+    for (int r = 0; r < d; ++r) {
+      float fx = __fmul_rn(p.F[r * d], xs[0]);
+      for (int k = 1; k < d; ++k) fx = __fmaf_rn(p.F[r * d + k], xs[k], fx);
+      float le;
+      if (p.lq_diag) {
+        le = __fmul_rn(p.Lq[r * d + r], e[r]);
+      } else {
+        le = __fmul_rn(p.Lq[r * d], e[0]);
+        for (int k = 1; k < d; ++k) le = __fmaf_rn(p.Lq[r * d + k], e[k], le);
+      }
+      xn[r] = __fadd_rn(fx, le);
+      x_new[r * n + i] = xn[r];
+    }
+    const float *lws = res_flag ? (res ? nullptr : lw_prev) : lw_prev;
+    const float lres = lws ? __ldg(&lws[i]) : 0.0f;
+    l = __fsub_rn(lres, lgd_potential(p, xn, y));
+    lw_new[i] = l;
+  }
+  if (FUSED) pf_reduce<PF_TPB>(l, active, ctl, t);
+}
+
+static int run_lgd(const mgb_lg_model *m, int64_t n, int64_t T, const uint32_t *key, const float *y, float thr,
+                   int scheme, bool, void *ws, size_t ws_bytes, const mgb_pf_outputs *out, cudaStream_t s) {
+  const LGDyn p = pack_lgd(m);
+  const int D = p.d, DY = p.dy;
+  const bool hx = out && out->x_hist, hl = out && out->lw_hist;
+  Carver c(ws);
+  RunWs w = carve_run(c, n, T, D, scheme, !hx, !hl, !(out && out->ess));
+  carve_persist(c, n, T);  // the layout mgb_pf_lg_workspace sizes
+  if (c.bytes() > ws_bytes) return ERR_WORKSPACE;
+  float *ess = (out && out->ess) ? out->ess : w.ess_hist;
+  int *err = out ? out->err : nullptr;
+  if (cudaMemsetAsync(w.st, 0, sizeof(PFState), s) != cudaSuccess) return ERR_CUDA;
+  if (cudaMemsetAsync(w.counter, 0, sizeof(unsigned int), s) != cudaSuccess) return ERR_CUDA;
+  if (cudaMemsetAsync(w.res_hist, 0, sizeof(int32_t) * (T + 1), s) != cudaSuccess) return ERR_CUDA;
+  int st = reset_resample(w.rws, s);
+  if (st) return st;
+  k_setup_keys<<<grid_for(T, 256), 256, 0, s>>>(key, T, w.keys);
+  PFCtl ctl;
+  ctl.parts = w.parts;
+  ctl.counter = w.counter;
+  ctl.st = w.st;
+  ctl.ess_hist = ess;
+  ctl.res_hist = w.res_hist;
+  ctl.rctl = w.rws.ctl;
+  ctl.rstatus = w.rws.status;
+  ctl.rstatus2 = w.rws.status2;
+  ctl.ntiles = (int)w.rws.ntiles;
+  ctl.thr_n = thr * (float)n;
+  ctl.logn = log((double)n);
+  ctl.logz_out = nullptr;
+  const unsigned grid = (unsigned)((n + PF_TPB - 1) / PF_TPB);
+  auto xbuf = [&](int64_t t) -> float * { return hx ? out->x_hist + (size_t)t * D * n : (t & 1 ? w.xb : w.xa); };
+  auto lbuf = [&](int64_t t) -> float * { return hl ? out->lw_hist + (size_t)t * n : (t & 1 ? w.lb : w.la); };
+  k_lgd_init<true><<<grid, PF_TPB, 0, s>>>(p, n, w.keys, y, xbuf(0), lbuf(0), ctl);
+  if ((st = launch_status())) return st;
+  for (int64_t t = 1; t < T; ++t) {
+    st = launch_resample(lbuf(t - 1), n, scheme, &w.st->M, w.keys + 2 * t, 0, 0u, w.res_hist + t, w.rws, w.anc,
+                         err, s);
+    if (st) return st;
+    k_lgd_step<true><<<grid, PF_TPB, 0, s>>>(p, n, w.keys + 2 * t, y + (size_t)t * DY, xbuf(t - 1), w.anc,
+                                             lbuf(t - 1), w.res_hist + t, xbuf(t), lbuf(t), ctl, t);
+    if ((st = launch_status())) return st;
+  }
+  k_finish<<<grid_for(T, 256), 256, 0, s>>>(w.st, w.res_hist, T, out ? out->log_z : nullptr,
+                                            out ? out->resampled : nullptr);
+  if (out && out->x_final && cudaMemcpyAsync(out->x_final, xbuf(T - 1), sizeof(float) * D * n,
+                                             cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+    return ERR_CUDA;
+  if (out && out->lw_final && cudaMemcpyAsync(out->lw_final, lbuf(T - 1), sizeof(float) * n,
+                                              cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+    return ERR_CUDA;
+  return launch_status();
+}
+
+static int init_lgd(const mgb_lg_model *m, int64_t n, const uint32_t *key, const float *y0, float *x, float *lw,
+                    cudaStream_t s) {
+  const LGDyn p = pack_lgd(m);
+  PFCtl ctl{};
+  k_lgd_init<false><<<(unsigned)((n + PF_TPB - 1) / PF_TPB), PF_TPB, 0, s>>>(p, n, key, y0, x, lw, ctl);
+  return launch_status();
+}
+
+static int step_lgd(const mgb_lg_model *m, int64_t n, const uint32_t *key, const float *y, const float *xp,
+                    const int32_t *anc, const float *lwp, float *xn, float *lwn, cudaStream_t s) {
+  const LGDyn p = pack_lgd(m);
+  PFCtl ctl{};
+  k_lgd_step<false><<<(unsigned)((n + PF_TPB - 1) / PF_TPB), PF_TPB, 0, s>>>(p, n, key, y, xp, anc, lwp, nullptr,
+                                                                              xn, lwn, ctl, 0);
+  return launch_status();
+}
+
 // (d, dy) dispatch over the compiled instantiations
 #define MGB_LG_DISPATCH(FN, ...)                                   \
   do {                                                             \
@@ -179,7 +408,7 @@ static int step_lg(const mgb_lg_model *m, int64_t n, const uint32_t *key, const 
         case 5: return FN<5, 1>(__VA_ARGS__);                      \
         case 8: return FN<8, 1>(__VA_ARGS__);                      \
         case 10: return FN<10, 1>(__VA_ARGS__);                    \
-        default: return ERR_UNSUPPORTED;                           \
+        default: break;                                            \
       }                                                            \
     } else if (dy_ == d_) {                                        \
       switch (d_) {                                                \
@@ -189,9 +418,11 @@ static int step_lg(const mgb_lg_model *m, int64_t n, const uint32_t *key, const 
         case 5: return FN<5, 5>(__VA_ARGS__);                      \
         case 8: return FN<8, 8>(__VA_ARGS__);                      \
         case 10: return FN<10, 10>(__VA_ARGS__);                   \
-        default: return ERR_UNSUPPORTED;                           \
+        default: break;                                            \
       }                                                            \
     }                                                              \
+    /* no compiled instance: the run-time-dimension kernels */     \
+    if (lgd_ok(m)) return FN##d(__VA_ARGS__);                      \
     return ERR_UNSUPPORTED;                                        \
   } while (0)
 

@@ -28,6 +28,7 @@ LOG2PI = math.log(2.0 * math.pi)
 RUN_LAUNCH_PER_STEP = 0x100  # MGB_RUN_LAUNCH_PER_STEP
 LG_SUPPORTED = {(1, 1), (2, 1), (3, 1), (4, 1), (5, 1), (8, 1), (10, 1),
                 (2, 2), (3, 3), (4, 4), (5, 5), (8, 8), (10, 10)}
+LG_RUNTIME_MAX = 32  # bootstrap filter at other (d, dy): run-time-dimension kernels, d, dy <= 32
 
 
 def _np(a):
@@ -120,7 +121,13 @@ class TimeHomogenousLinearGaussian(StateSpaceModel):
         return self.__dict__["_derived"]
 
     def gpu_supported(self):
+        """(d, dy) has compiled kernels for every path (filters, Kalman, smoothers, gradients)"""
         return (self.dim, self.dim_obs) in LG_SUPPORTED
+
+    def gpu_bootstrap_supported(self):
+        """the bootstrap filter runs on the GPU: compiled kernels, or the run-time-dimension
+        kernels (bit-identical, one launch per phase) for d, dy <= 32"""
+        return self.gpu_supported() or (self.dim <= LG_RUNTIME_MAX and self.dim_obs <= LG_RUNTIME_MAX)
 
     def simulate(self, t_all, random_key):
         """StateSpaceModel.simulate (ssm.py:138-163): split(key, 2T), first T keys drive
@@ -413,7 +420,8 @@ def _check_lg(ssm_scenario, particle_filter):
         raise NotImplementedError(f"{ssm_scenario.__class__.__name__}: no fused GPU kernel for this model")
     if not isinstance(particle_filter, (BootstrapFilter, OptimalNonLinearGaussianParticleFilter)):
         raise NotImplementedError(f"{particle_filter.__class__.__name__}: no fused GPU kernel for this filter")
-    if not ssm_scenario.gpu_supported():
+    boot = not isinstance(particle_filter, OptimalNonLinearGaussianParticleFilter)
+    if not (ssm_scenario.gpu_bootstrap_supported() if boot else ssm_scenario.gpu_supported()):
         raise NotImplementedError(f"(d, dy) = ({ssm_scenario.dim}, {ssm_scenario.dim_obs}) not compiled")
 
 
@@ -531,6 +539,12 @@ def run_particle_filter_for_marginals(ssm_scenario, particle_filter, y, t, rando
     are the same.  A model or filter without a fused kernel runs through the
     generic driver (ParticleFilter's vectorised plugin methods, the library's
     logsumexp / resampling / gather kernels); persistent is then ignored.
+
+    resampling defaults to "systematic", a deliberate deviation: the reference
+    draws ancestors with random.categorical (filtering.py:199), which is
+    resampling="categorical" here (the same Gumbel-max draws, O(n^2) per step,
+    small n only).  Systematic resampling has lower variance and is O(n), but
+    gives different ancestors from the reference's on the same key.
     """
     if not _fused(ssm_scenario, particle_filter):
         return _run_generic(ssm_scenario, particle_filter, y, t, random_key, n, initial_sample, ess_threshold,
@@ -1023,6 +1037,8 @@ def fixed_lag_stitching(ssm_scenario, early_block, t, recent_block, recent_block
 
 def _check_smoother(ssm_scenario, particle_filter):
     _check_lg(ssm_scenario, particle_filter)
+    if isinstance(ssm_scenario, TimeHomogenousLinearGaussian) and not ssm_scenario.gpu_supported():
+        raise NotImplementedError(f"(d, dy) = ({ssm_scenario.dim}, {ssm_scenario.dim_obs}) not compiled")
     if not isinstance(particle_filter, BootstrapFilter):
         raise NotImplementedError("the online smoother runs the bootstrap filter")
 

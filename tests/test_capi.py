@@ -62,13 +62,19 @@ def test_noalloc_array_holds_the_largest_allowed_size(L):
 
 
 def test_unsupported_dimension_rejected_on_host(L):
+    """dimensions above the run-time-dimension kernels' limit (32) are refused before any
+    device call, for the whole filter and the online init / propagate entry points"""
     import numpy as np
-    d = 7
+    d = 33
     arrs = [np.eye(d, dtype=np.float32) for _ in range(5)] + [np.zeros(d, np.float32)]
     m = _lib.LGModel(d, d, *[a.ctypes.data for a in arrs], 1.0)
     p = ctypes.c_void_p(256)
     need = L.mgb_pf_lg_workspace(1000, 10, d, 0)
     assert L.mgb_pf_lg_run(ctypes.byref(m), 1000, 10, p, p, 0.5, 0, p, need, None, None) == 2
+    assert L.mgb_pf_lg_init(ctypes.byref(m), 1000, p, p, p, p, None) == 2
+    assert L.mgb_pf_lg_propagate(ctypes.byref(m), 1000, p, p, p, None, None, p, p, None) == 2
+    m1 = _lib.LGModel(5, 33, *[a.ctypes.data for a in arrs], 1.0)  # dy above the limit
+    assert L.mgb_pf_lg_init(ctypes.byref(m1), 1000, p, p, p, p, None) == 2
 
 
 def test_new_entry_points_reject_bad_arguments_on_host(L):

@@ -76,6 +76,56 @@ def test_run_matches_oracle(cuda, scheme, d, odd, persistent):
     assert abs(float(out.log_z) - ref["log_z"]) <= 1e-5 * abs(ref["log_z"])
 
 
+@pytest.mark.parametrize("d,dy,diag_r", [(6, 6, True), (7, 3, False), (4, 2, True), (12, 12, False), (9, 1, True),
+                                         (32, 5, False)])
+def test_runtime_dimensions_bit_exact(cuda, d, dy, diag_r):
+    """(d, dy) pairs without a compiled kernel run on the run-time-dimension kernels: the
+    online init / propagate and the whole filter (both resampling schemes, n even and odd)
+    equal the oracle bit for bit, as the compiled pairs do"""
+    import mocat_gb300 as mg
+    from mocat_gb300.ssm import _step
+    p, ssm = _models(d, dy, seed=40 + d, diag_r=diag_r)
+    assert not ssm.gpu_supported() and ssm.gpu_bootstrap_supported()
+    T = 15
+    _, y = models.simulate_lg(p, T, O.PRNGKey(0))
+    for n in (3000, 3001):
+        key = O.PRNGKey(1)
+        x0, lw0 = O.lg_init(p, n, key, y[0])
+        ip = mg.ssm.initiate_particles(ssm, mg.ssm.BootstrapFilter(), n, key, y[0])
+        assert np.array_equal(ip.value[0].cpu().numpy(), x0)
+        assert np.array_equal(ip.log_weight[0].cpu().numpy(), lw0)
+        _, s = ssm.derived()
+        kt = O.split(O.PRNGKey(2), 1)[0]
+        anc = np.sort(np.random.default_rng(0).integers(0, n, n)).astype(np.int32)
+        xr, lr = O.lg_propagate(p, kt, y[1], x0, anc, None)
+        xn, ln = _step(s, n, torch.from_numpy(kt.view(np.int32)).cuda().view(torch.uint32),
+                       torch.from_numpy(y[1]).cuda(), torch.from_numpy(np.ascontiguousarray(x0.T)).cuda(),
+                       torch.from_numpy(anc).cuda(), None)
+        assert np.array_equal(xn.t().cpu().numpy(), xr)
+        assert np.array_equal(ln.cpu().numpy(), lr)
+        for scheme in ("systematic", "multinomial"):
+            ref = O.lg_run(p, n, O.PRNGKey(3), y, ess_threshold=0.8, scheme=scheme, history=True)
+            out = mg.ssm.run_particle_filter_for_marginals(ssm, mg.ssm.BootstrapFilter(), y, np.arange(T),
+                                                           O.PRNGKey(3), n=n, ess_threshold=0.8, resampling=scheme)
+            assert ref["resampled"].sum() >= 2
+            assert np.array_equal(out.resampled.cpu().numpy(), ref["resampled"])
+            assert np.array_equal(out.value.cpu().numpy(), ref["value"])
+            assert np.array_equal(out.log_weight.cpu().numpy(), ref["log_weight"])
+            assert abs(float(out.log_z) - ref["log_z"]) <= 1e-5 * abs(ref["log_z"])
+
+
+def test_runtime_dimension_limits(cuda):
+    """above 32 the bootstrap filter is refused on the host; the other paths need a compiled pair"""
+    import mocat_gb300 as mg
+    p, ssm = _models(33, 33, seed=1)
+    assert not ssm.gpu_bootstrap_supported()
+    with pytest.raises(NotImplementedError):
+        mg.ssm.initiate_particles(ssm, mg.ssm.BootstrapFilter(), 100, O.PRNGKey(0), np.zeros(33, np.float32))
+    _, ssm6 = _models(6, 6, seed=1)
+    with pytest.raises(NotImplementedError):
+        mg.ssm.run_kalman_filter_for_marginals(ssm6, np.zeros((4, 6), np.float32))
+
+
 @pytest.mark.parametrize("d", [3, 10])
 def test_structured_matrices_bit_exact(cuda, d):
     """Diagonal Q and R, H = I take the specialised paths; values equal the dense oracle's."""
