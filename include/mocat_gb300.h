@@ -466,6 +466,35 @@ int mgb_pf_sv_run(const mgb_sv_model *model_host, int64_t n, int64_t T, const ui
                   const float *t_dev, float ess_threshold, int scheme, void *ws_dev, size_t ws_bytes,
                   const mgb_pf_outputs *out, void *stream);
 
+/* The d-dimensional stochastic-volatility model (mocat/src/ssm/scenarios/
+ * stochastic_volatility.py:15-108) with a diagonal likelihood covariance R, on
+ * run-time-dimension kernels (1 <= d <= 32):
+ *   x_0 = C0 normal(key, (d,)) + m0                   (initial_sample :71-76)
+ *   x_t = A x_{t-1} + (Lq normal(key, (d,))) sqrt(dt)  (transition_sample :87-94)
+ *   potential(x, y) = cB + sum_j (0.5 x_j + 0.5 y_j^2 r2_j exp(-x_j))   (:96-102)
+ * with r2 = 1 / R and cB = (d log 2 pi - sum_j log r2_j) / 2.  Host pointers,
+ * row-major float32. */
+typedef struct {
+  int32_t d;
+  const float *A, *Lq, *C0, *m0; /* transition_matrix, transition_covariance_sqrt,
+                                    initial_covariance_sqrt (d x d); initial_mean (d) */
+  const float *r2;                /* (d) 1 / likelihood_covariance_diag */
+  float cB;
+} mgb_svd_model;
+/* initiate_particles / one propagate step (dt = t_new - t_previous) / the whole filter
+ * with the times t_dev (T,) (run_particle_filter_for_marginals, filtering.py:255-324),
+ * arguments and outputs as mgb_pf_sv_*; x is (d, n) dimension-major; one launch per
+ * phase and step */
+int mgb_pf_svd_init(const mgb_svd_model *model_host, int64_t n, const uint32_t *key_dev, const float *y0_dev,
+                    float *x_dev, float *lw_dev, void *stream);
+int mgb_pf_svd_propagate(const mgb_svd_model *model_host, int64_t n, const uint32_t *key_dev, const float *y_dev,
+                         float dt, const float *x_prev_dev, const int32_t *ancestors_dev, const float *lw_prev_dev,
+                         float *x_new_dev, float *lw_new_dev, void *stream);
+size_t mgb_pf_svd_workspace(int64_t n, int64_t T, int32_t d, int scheme);
+int mgb_pf_svd_run(const mgb_svd_model *model_host, int64_t n, int64_t T, const uint32_t *key_dev,
+                   const float *y_dev, const float *t_dev, float ess_threshold, int scheme, void *ws_dev,
+                   size_t ws_bytes, const mgb_pf_outputs *out, void *stream);
+
 /* launch shape of a batched run (from mgb_pf_sv_batch_plan / _autotune) */
 typedef struct {
   int32_t threads;     /* CTA size: 256, 512 or 1024 */

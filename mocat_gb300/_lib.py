@@ -87,6 +87,11 @@ class SVModel(ctypes.Structure):
                 ("c0", ctypes.c_float), ("m0", ctypes.c_float)]
 
 
+class SVDModel(ctypes.Structure):
+    _fields_ = [("d", ctypes.c_int32), ("A", ctypes.c_void_p), ("Lq", ctypes.c_void_p), ("C0", ctypes.c_void_p),
+                ("m0", ctypes.c_void_p), ("r2", ctypes.c_void_p), ("cB", ctypes.c_float)]
+
+
 class SVLaunch(ctypes.Structure):
     _fields_ = [("threads", ctypes.c_int32), ("ppt", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32),
                 ("nbundles", ctypes.c_int32), ("smem_bytes", ctypes.c_int64)]
@@ -160,6 +165,11 @@ _SIGNATURES = {
     "mgb_pf_opt_workspace": ([_I64, _I64, ctypes.c_int32, _I32], _SZ),
     "mgb_pf_opt_run": ([ctypes.POINTER(OptModel), _I64, _I64, _P, _P, _F, _I32, _P, _SZ, ctypes.POINTER(PFOutputs),
                         _P], _I32),
+    "mgb_pf_svd_init": ([ctypes.POINTER(SVDModel), _I64, _P, _P, _P, _P, _P], _I32),
+    "mgb_pf_svd_propagate": ([ctypes.POINTER(SVDModel), _I64, _P, _P, _F, _P, _P, _P, _P, _P, _P], _I32),
+    "mgb_pf_svd_workspace": ([_I64, _I64, ctypes.c_int32, ctypes.c_int], _SZ),
+    "mgb_pf_svd_run": ([ctypes.POINTER(SVDModel), _I64, _I64, _P, _P, _P, _F, ctypes.c_int, _P, _SZ,
+                        ctypes.POINTER(PFOutputs), _P], _I32),
     "mgb_pf_sv_init": ([ctypes.POINTER(SVModel), _I64, _P, _P, _P, _P, _P], _I32),
     "mgb_pf_sv_propagate": ([ctypes.POINTER(SVModel), _I64, _P, _P, _F, _P, _P, _P, _P, _P, _P], _I32),
     "mgb_pf_sv_workspace": ([_I64, _I64, ctypes.c_int], _SZ),

@@ -53,6 +53,8 @@ class BatchedFilters:
                  resampling="multinomial", launch=None, tune=False, probe_steps=128, lengths=None, pin_y=False):
         if not isinstance(ssm_scenario, StochasticVolatility):
             raise NotImplementedError(f"{ssm_scenario.__class__.__name__}: no batched GPU kernel for this model")
+        if ssm_scenario.dim != 1:
+            raise NotImplementedError("batched stochastic-volatility filters take dim = 1")
         if not isinstance(particle_filter, BootstrapFilter):
             raise NotImplementedError(f"{particle_filter.__class__.__name__}: no batched GPU kernel for this filter")
         if resampling not in ("multinomial", "systematic"):

@@ -395,6 +395,179 @@ static int step_lgd(const mgb_lg_model *m, int64_t n, const uint32_t *key, const
   return launch_status();
 }
 
+// ---------------------------------------------------------------------------
+// The d-dimensional stochastic-volatility model (stochastic_volatility.py:15-108,
+// diagonal likelihood covariance) on the same run-time-dimension scheme:
+//   x_0 = C0 e + m0;  x_t = A x_{t-1} + (Lq e) sqrt(t_t - t_{t-1})
+//   potential = cB + sum_j (0.5 x_j + (0.5 y_j^2 r2_j) exp(-x_j)),  r2 = 1 / R,
+// accumulated j = 0, 1, ... from cB (for d = 1 the dim-1 kernels' formula).
+struct SVDyn {
+  float A[LGD_MAX * LGD_MAX], Lq[LGD_MAX * LGD_MAX], C0[LGD_MAX * LGD_MAX], m0[LGD_MAX], r2[LGD_MAX];
+  float cB;
+  int d, lq_diag;
+};
+
+static bool svd_model_ok(const mgb_svd_model *m) {
+  return m && m->d >= 1 && m->d <= LGD_MAX && m->A && m->Lq && m->C0 && m->m0 && m->r2;
+}
+
+static SVDyn pack_svd(const mgb_svd_model *m) {
+  SVDyn p;
+  const int d = m->d;
+  p.d = d;
+  for (int i = 0; i < d * d; ++i) {
+    p.A[i] = m->A[i];
+    p.Lq[i] = m->Lq[i];
+    p.C0[i] = m->C0[i];
+  }
+  for (int i = 0; i < d; ++i) {
+    p.m0[i] = m->m0[i];
+    p.r2[i] = m->r2[i];
+  }
+  p.cB = m->cB;
+  int diag = 1;
+  for (int r = 0; r < d; ++r)
+    for (int c = 0; c < d; ++c)
+      if (r != c && p.Lq[r * d + c] != 0.0f) diag = 0;
+  p.lq_diag = diag;
+  return p;
+}
+
+__device__ __forceinline__ float svd_potential(const SVDyn &p, const float *x, const float *y) {
+  float pot = p.cB;
+  for (int j = 0; j < p.d; ++j) {
+    const float a = __fmul_rn(__fmul_rn(0.5f, __fmul_rn(y[j], y[j])), p.r2[j]);
+    pot = __fmaf_rn(a, expf_(-x[j]), __fmaf_rn(0.5f, x[j], pot));
+  }
+  return pot;
+}
+
+template <bool FUSED>
+__global__ void __launch_bounds__(PF_TPB) k_svd_init(const __grid_constant__ SVDyn p, int64_t n, const uint32_t *key,
+                                                      const float *y0, float *__restrict__ x,
+                                                      float *__restrict__ lw, PFCtl ctl) {
+  const int64_t i = blockIdx.x * (int64_t)PF_TPB + threadIdx.x;
+  const uint32_t k0 = key[0], k1 = key[1];
+  __shared__ float y[LGD_MAX];
+  if (threadIdx.x < p.d) y[threadIdx.x] = y0 ? y0[threadIdx.x] : 0.0f;
+  __syncthreads();
+  float l = -INFINITY;
+  const bool active = i < n;
+  if (active) {
+    const int d = p.d;
+    float e[LGD_MAX], xv[LGD_MAX];
+    lgd_normals(k0, k1, n, i, d, e);
+    for (int r = 0; r < d; ++r) {
+      float v = __fmul_rn(p.C0[r * d], e[0]);
+      for (int k = 1; k < d; ++k) v = __fmaf_rn(p.C0[r * d + k], e[k], v);
+      xv[r] = __fadd_rn(v, p.m0[r]);
+      x[r * n + i] = xv[r];
+    }
+    l = y0 ? -svd_potential(p, xv, y) : 0.0f;
+    lw[i] = l;
+  }
+  if (FUSED) pf_reduce<PF_TPB>(l, active, ctl, 0);
+}
+
+// one step; dt = t_dev[t] - t_dev[t-1] when t_dev is given, else dt_arg
+template <bool FUSED>
+__global__ void __launch_bounds__(PF_TPB) k_svd_step(const __grid_constant__ SVDyn p, int64_t n, const uint32_t *key,
+                                                      const float *y_t, const float *t_dev, float dt_arg,
+                                                      const float *__restrict__ x_prev, const int32_t *anc,
+                                                      const float *lw_prev, const int32_t *res_flag,
+                                                      float *__restrict__ x_new, float *__restrict__ lw_new,
+                                                      PFCtl ctl, int64_t t) {
+  const int64_t i = blockIdx.x * (int64_t)PF_TPB + threadIdx.x;
+  const bool res = res_flag ? (*res_flag != 0) : (anc != nullptr);
+  const uint32_t k0 = key[0], k1 = key[1];
+  __shared__ float y[LGD_MAX];
+  if (threadIdx.x < p.d) y[threadIdx.x] = y_t[threadIdx.x];
+  __syncthreads();
+  float l = -INFINITY;
+  const bool active = i < n;
+  if (active) {
+    const int d = p.d;
+    const float dt = t_dev ? __fsub_rn(__ldg(&t_dev[t]), __ldg(&t_dev[t - 1])) : dt_arg;
+    const float sdt = __fsqrt_rn(dt);
+    float e[LGD_MAX], xs[LGD_MAX], xn[LGD_MAX];
+    lgd_normals(k0, k1, n, i, d, e);
+    const int64_t src = res ? (int64_t)anc[i] : i;
+    for (int j = 0; j < d; ++j) xs[j] = __ldg(&x_prev[j * n + src]);
+    for (int r = 0; r < d; ++r) {
+      float fx = __fmul_rn(p.A[r * d], xs[0]);
+      for (int k = 1; k < d; ++k) fx = __fmaf_rn(p.A[r * d + k], xs[k], fx);
+      float le;
+      if (p.lq_diag) {
+        le = __fmul_rn(p.Lq[r * d + r], e[r]);
+      } else {
+        le = __fmul_rn(p.Lq[r * d], e[0]);
+        for (int k = 1; k < d; ++k) le = __fmaf_rn(p.Lq[r * d + k], e[k], le);
+      }
+      xn[r] = __fadd_rn(fx, __fmul_rn(le, sdt));
+      x_new[r * n + i] = xn[r];
+    }
+    const float *lws = res_flag ? (res ? nullptr : lw_prev) : lw_prev;
+    const float lres = lws ? __ldg(&lws[i]) : 0.0f;
+    l = __fsub_rn(lres, svd_potential(p, xn, y));
+    lw_new[i] = l;
+  }
+  if (FUSED) pf_reduce<PF_TPB>(l, active, ctl, t);
+}
+
+static int run_svd(const mgb_svd_model *m, int64_t n, int64_t T, const uint32_t *key, const float *y,
+                   const float *t_dev, float thr, int scheme, void *ws, size_t ws_bytes, const mgb_pf_outputs *out,
+                   cudaStream_t s) {
+  const SVDyn p = pack_svd(m);
+  const int D = p.d;
+  const bool hx = out && out->x_hist, hl = out && out->lw_hist;
+  Carver c(ws);
+  RunWs w = carve_run(c, n, T, D, scheme, !hx, !hl, !(out && out->ess));
+  if (c.bytes() > ws_bytes) return ERR_WORKSPACE;
+  float *ess = (out && out->ess) ? out->ess : w.ess_hist;
+  int *err = out ? out->err : nullptr;
+  if (cudaMemsetAsync(w.st, 0, sizeof(PFState), s) != cudaSuccess) return ERR_CUDA;
+  if (cudaMemsetAsync(w.counter, 0, sizeof(unsigned int), s) != cudaSuccess) return ERR_CUDA;
+  if (cudaMemsetAsync(w.res_hist, 0, sizeof(int32_t) * (T + 1), s) != cudaSuccess) return ERR_CUDA;
+  int st = reset_resample(w.rws, s);
+  if (st) return st;
+  k_setup_keys<<<grid_for(T, 256), 256, 0, s>>>(key, T, w.keys);
+  PFCtl ctl;
+  ctl.parts = w.parts;
+  ctl.counter = w.counter;
+  ctl.st = w.st;
+  ctl.ess_hist = ess;
+  ctl.res_hist = w.res_hist;
+  ctl.rctl = w.rws.ctl;
+  ctl.rstatus = w.rws.status;
+  ctl.rstatus2 = w.rws.status2;
+  ctl.ntiles = (int)w.rws.ntiles;
+  ctl.thr_n = thr * (float)n;
+  ctl.logn = log((double)n);
+  ctl.logz_out = nullptr;
+  const unsigned grid = (unsigned)((n + PF_TPB - 1) / PF_TPB);
+  auto xbuf = [&](int64_t t) -> float * { return hx ? out->x_hist + (size_t)t * D * n : (t & 1 ? w.xb : w.xa); };
+  auto lbuf = [&](int64_t t) -> float * { return hl ? out->lw_hist + (size_t)t * n : (t & 1 ? w.lb : w.la); };
+  k_svd_init<true><<<grid, PF_TPB, 0, s>>>(p, n, w.keys, y, xbuf(0), lbuf(0), ctl);
+  if ((st = launch_status())) return st;
+  for (int64_t t = 1; t < T; ++t) {
+    st = launch_resample(lbuf(t - 1), n, scheme, &w.st->M, w.keys + 2 * t, 0, 0u, w.res_hist + t, w.rws, w.anc,
+                         err, s);
+    if (st) return st;
+    k_svd_step<true><<<grid, PF_TPB, 0, s>>>(p, n, w.keys + 2 * t, y + (size_t)t * D, t_dev, 1.0f, xbuf(t - 1),
+                                             w.anc, lbuf(t - 1), w.res_hist + t, xbuf(t), lbuf(t), ctl, t);
+    if ((st = launch_status())) return st;
+  }
+  k_finish<<<grid_for(T, 256), 256, 0, s>>>(w.st, w.res_hist, T, out ? out->log_z : nullptr,
+                                            out ? out->resampled : nullptr);
+  if (out && out->x_final && cudaMemcpyAsync(out->x_final, xbuf(T - 1), sizeof(float) * D * n,
+                                             cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+    return ERR_CUDA;
+  if (out && out->lw_final && cudaMemcpyAsync(out->lw_final, lbuf(T - 1), sizeof(float) * n,
+                                              cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+    return ERR_CUDA;
+  return launch_status();
+}
+
 // (d, dy) dispatch over the compiled instantiations
 #define MGB_LG_DISPATCH(FN, ...)                                   \
   do {                                                             \
@@ -464,6 +637,46 @@ int mgb_pf_lg_run(const mgb_lg_model *m, int64_t n, int64_t T, const uint32_t *k
   if (scheme == MGB_RESAMPLE_CATEGORICAL && n > 46340) return ERR_UNSUPPORTED;
   if (ws_bytes < mgb_pf_lg_workspace(n, T, m->d, scheme)) return ERR_WORKSPACE;
   MGB_LG_DISPATCH(run_lg, m, n, T, key, y, thr, scheme, persistent, ws, ws_bytes, out, (cudaStream_t)stream);
+}
+
+size_t mgb_pf_svd_workspace(int64_t n, int64_t T, int32_t d, int scheme) {
+  Carver c(nullptr);
+  carve_run(c, n, T < 1 ? 1 : T, d, scheme & 0xff, true, true, true);
+  return c.bytes();
+}
+
+int mgb_pf_svd_init(const mgb_svd_model *m, int64_t n, const uint32_t *key, const float *y0, float *x, float *lw,
+                    void *stream) {
+  if (!m || n < 1 || n > 0x7FFFFFFFll || !key || !x || !lw) return ERR_BAD_ARG;
+  if (!svd_model_ok(m)) return m->d > LGD_MAX ? ERR_UNSUPPORTED : ERR_BAD_ARG;
+  const SVDyn p = pack_svd(m);
+  PFCtl ctl{};
+  k_svd_init<false><<<(unsigned)((n + PF_TPB - 1) / PF_TPB), PF_TPB, 0, (cudaStream_t)stream>>>(p, n, key, y0, x, lw,
+                                                                                               ctl);
+  return launch_status();
+}
+
+int mgb_pf_svd_propagate(const mgb_svd_model *m, int64_t n, const uint32_t *key, const float *y, float dt,
+                         const float *xp, const int32_t *anc, const float *lwp, float *xn, float *lwn, void *stream) {
+  if (!m || n < 1 || n > 0x7FFFFFFFll || !key || !y || !xp || !xn || !lwn || !(dt >= 0.0f)) return ERR_BAD_ARG;
+  if (!svd_model_ok(m)) return m->d > LGD_MAX ? ERR_UNSUPPORTED : ERR_BAD_ARG;
+  const SVDyn p = pack_svd(m);
+  PFCtl ctl{};
+  k_svd_step<false><<<(unsigned)((n + PF_TPB - 1) / PF_TPB), PF_TPB, 0, (cudaStream_t)stream>>>(
+      p, n, key, y, nullptr, dt, xp, anc, lwp, nullptr, xn, lwn, ctl, 0);
+  return launch_status();
+}
+
+int mgb_pf_svd_run(const mgb_svd_model *m, int64_t n, int64_t T, const uint32_t *key, const float *y,
+                   const float *t, float thr, int scheme, void *ws, size_t ws_bytes, const mgb_pf_outputs *out,
+                   void *stream) {
+  if (!m || n < 1 || n > 0x7FFFFFFFll || T < 1 || !key || !y || !ws) return ERR_BAD_ARG;
+  if (!svd_model_ok(m)) return m->d > LGD_MAX ? ERR_UNSUPPORTED : ERR_BAD_ARG;
+  scheme &= ~MGB_RUN_LAUNCH_PER_STEP;
+  if (scheme < 0 || scheme > 2) return ERR_BAD_ARG;
+  if (scheme == MGB_RESAMPLE_CATEGORICAL && n > 46340) return ERR_UNSUPPORTED;
+  if (ws_bytes < mgb_pf_svd_workspace(n, T, m->d, scheme)) return ERR_WORKSPACE;
+  return run_svd(m, n, T, key, y, t, thr, scheme, ws, ws_bytes, out, (cudaStream_t)stream);
 }
 
 }  // extern "C"

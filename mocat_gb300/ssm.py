@@ -152,8 +152,12 @@ class TimeHomogenousLinearGaussian(StateSpaceModel):
 
 class StochasticVolatility(StateSpaceModel):
     """x_t ~ N(A x_{t-1}, Q dt), y_t ~ N(0, R exp(x_t)) elementwise
-    (mocat/src/ssm/scenarios/stochastic_volatility.py:15-108).  The GPU kernels
-    take dim = 1 (many independent series run as a batch)."""
+    (mocat/src/ssm/scenarios/stochastic_volatility.py:15-108).  dim = 1 runs the
+    scalar kernels (single series, batches of many series, smoothers); dim 2..32 the
+    bootstrap filter on run-time-dimension kernels.  likelihood_covariance_diag is the
+    diagonal of R (a matrix argument is reduced to its diagonal); the reference's
+    default, an identity matrix, drops the potential's normalising constant there,
+    which only shifts log Z."""
     name = "Stochastic Volatility"
     _PARAMS = ("initial_mean", "initial_covariance", "transition_matrix", "transition_covariance",
                "likelihood_covariance_diag")
@@ -179,9 +183,22 @@ class StochasticVolatility(StateSpaceModel):
     def derived(self, dt=1.0):
         """float32 constants of the d = 1 kernels and the C-ABI struct:
         phi = A, bsig = sqrt(Q) sqrt(dt), r2 = 1 / R, cB = (log 2 pi - log r2) / 2,
-        c0 = sqrt(initial_covariance), m0 = initial_mean."""
+        c0 = sqrt(initial_covariance), m0 = initial_mean.  dim > 1: the constants of the
+        run-time-dimension kernels (mgb_svd_model): A, Lq = chol(Q), C0 = chol(initial
+        covariance), m0, r2 = 1 / R, cB = (d log 2 pi - sum log r2) / 2."""
         if self.dim != 1:
-            raise NotImplementedError("StochasticVolatility: the GPU kernels take dim = 1")
+            if "_derived" not in self.__dict__:
+                d = self.dim
+                f32 = lambda a: np.ascontiguousarray(a, np.float32)
+                r2 = f32(1.0 / np.asarray(self.likelihood_covariance_diag, np.float64))
+                p = dict(d=d, A=f32(self.transition_matrix), Lq=f32(np.linalg.cholesky(self.transition_covariance)),
+                         C0=f32(np.linalg.cholesky(self.initial_covariance)), m0=f32(self.initial_mean), r2=r2,
+                         cB=np.float32(0.5 * (d * LOG2PI - np.sum(np.log(r2.astype(np.float64))))),
+                         sqrtR=f32(np.sqrt(self.likelihood_covariance_diag)))
+                s = _lib.SVDModel(d, p["A"].ctypes.data, p["Lq"].ctypes.data, p["C0"].ctypes.data,
+                                  p["m0"].ctypes.data, p["r2"].ctypes.data, float(p["cB"]))
+                self.__dict__["_derived"] = (p, s)
+            return self.__dict__["_derived"]
         if "_derived" not in self.__dict__ or self.__dict__["_derived"][0]["dt"] != dt:
             r2 = np.float32(1.0 / float(self.likelihood_covariance_diag[0]))
             p = dict(dt=dt, phi=np.float32(self.transition_matrix[0, 0]),
@@ -196,13 +213,18 @@ class StochasticVolatility(StateSpaceModel):
     def transition_constants(self):
         """(phi, pq) of the transition potential, float32: transition_matrix and
         transition_precision_sqrt = inv(chol(transition_covariance)) (utils.py:247-262)"""
+        if self.dim != 1:
+            raise NotImplementedError("StochasticVolatility: the smoothing kernels take dim = 1")
         f = np.float32
         return f(self.transition_matrix[0, 0]), f(f(1.0) / f(np.sqrt(f(self.transition_covariance[0, 0]))))
 
     def simulate(self, t_all, random_key):
         """StateSpaceModel.simulate (ssm.py:138-163) with this model's samplers
         (stochastic_volatility.py:71-108): x_0 = e c0 + m0, x_t = phi x_{t-1} + (e sqrt(Q))
-        sqrt(t_t - t_{t-1}), y_t = sqrt(R) exp(x_t / 2) e; normals drawn on the GPU."""
+        sqrt(t_t - t_{t-1}), y_t = sqrt(R) exp(x_t / 2) e; normals drawn on the GPU
+        (dim > 1: x_0 = C0 e + m0, x_t = A x_{t-1} + (Lq e) sqrt(dt))."""
+        if self.dim != 1:
+            return self._simulate_d(t_all, random_key)
         p, _ = self.derived()
         f = np.float32
         t = np.asarray(t_all.cpu() if isinstance(t_all, torch.Tensor) else t_all, np.float32).reshape(-1)
@@ -219,6 +241,25 @@ class StochasticVolatility(StateSpaceModel):
         dev = _dev.device()
         return cdict(x=torch.from_numpy(x[:, None]).to(dev), y=torch.from_numpy(y[:, None]).to(dev),
                      t=torch.as_tensor(t, device=dev), name=f"{self.name} simulation")
+
+    def _simulate_d(self, t_all, random_key):
+        p, _ = self.derived()
+        f = np.float32
+        d = self.dim
+        t = np.asarray(t_all.cpu() if isinstance(t_all, torch.Tensor) else t_all, np.float32).reshape(-1)
+        T = t.size
+        keys = mrandom.split(random_key, 2 * T)
+        ex = _normal_keys(keys[:T], d).cpu().numpy()
+        ey = _normal_keys(keys[T:], d).cpu().numpy()
+        x = np.empty((T, d), np.float32)
+        x[0] = (p["C0"] @ ex[0]).astype(np.float32) + p["m0"]
+        for i in range(1, T):
+            sdt = f(np.sqrt(f(t[i] - t[i - 1])))
+            x[i] = (p["A"] @ x[i - 1]).astype(np.float32) + (p["Lq"] @ ex[i]).astype(np.float32) * sdt
+        y = (p["sqrtR"] * np.exp(f(0.5) * x).astype(np.float32) * ey).astype(np.float32)
+        dev = _dev.device()
+        return cdict(x=torch.from_numpy(x).to(dev), y=torch.from_numpy(y).to(dev), t=torch.as_tensor(t, device=dev),
+                     name=f"{self.name} simulation")
 
 
 class NonLinear1DBenchmark(StateSpaceModel):
@@ -409,8 +450,8 @@ def _check_lg(ssm_scenario, particle_filter):
     if isinstance(ssm_scenario, StochasticVolatility):
         if type(particle_filter) is not BootstrapFilter:
             raise NotImplementedError(f"{particle_filter.__class__.__name__}: no fused GPU kernel for this model")
-        if ssm_scenario.dim != 1:
-            raise NotImplementedError("StochasticVolatility: the GPU kernels take dim = 1")
+        if not 1 <= ssm_scenario.dim <= LG_RUNTIME_MAX:
+            raise NotImplementedError(f"StochasticVolatility: the GPU kernels take dim 1..{LG_RUNTIME_MAX}")
         return
     if isinstance(ssm_scenario, NonLinear1DBenchmark):
         if type(particle_filter) is not BootstrapFilter:
@@ -430,6 +471,8 @@ def _kernels(ssm_scenario, particle_filter):
     if isinstance(ssm_scenario, NonLinear1DBenchmark):
         return "mgb_pf_nl1d", ssm_scenario.derived()[1]
     if isinstance(ssm_scenario, StochasticVolatility):
+        if ssm_scenario.dim != 1:
+            return "mgb_pf_svd", ssm_scenario.derived()[1]
         # bsig of the dt = 1 struct is transition_covariance_sqrt; the kernels scale it by sqrt(dt)
         return "mgb_pf_sv", ssm_scenario.derived(1.0)[1]
     if isinstance(particle_filter, OptimalNonLinearGaussianParticleFilter):
@@ -493,7 +536,7 @@ def _step(s, n, key, y_t, x_prev_soa, anc, lw_prev, prefix="mgb_pf_lg", t_prev=N
     # model's on t_new - t_previous (float32, as the reference's time arrays)
     if prefix == "mgb_pf_nl1d":
         tp = (float(t_prev),)
-    elif prefix == "mgb_pf_sv":
+    elif prefix in ("mgb_pf_sv", "mgb_pf_svd"):
         tp = (float(np.float32(float(t_new)) - np.float32(float(t_prev))),)
     else:
         tp = ()
@@ -560,12 +603,13 @@ def run_particle_filter_for_marginals(ssm_scenario, particle_filter, y, t, rando
     if initial_sample is not None:
         return _run_from(ssm_scenario, s, initial_sample, y2, t, key, ess_threshold, resampling, prefix)
     T = y2.shape[0]
-    nl = prefix in ("mgb_pf_nl1d", "mgb_pf_sv")
+    nl = prefix in ("mgb_pf_nl1d", "mgb_pf_sv", "mgb_pf_svd")
     if nl:
         t32 = _dev.as_f32(t).reshape(-1).contiguous()
         if t32.numel() != T:
             raise ValueError(f"t has {t32.numel()} entries for {T} observations")
-        ws = _dev.workspace(getattr(_lib.lib(), prefix + "_workspace")(n, T, sc), dev)
+        wsa = (n, T, d, sc) if prefix == "mgb_pf_svd" else (n, T, sc)
+        ws = _dev.workspace(getattr(_lib.lib(), prefix + "_workspace")(*wsa), dev)
     else:
         ws = _dev.workspace(getattr(_lib.lib(), prefix + "_workspace")(n, T, d, sc), dev)
     logz = torch.empty(1, dtype=torch.float64, device=dev)
@@ -1037,6 +1081,8 @@ def fixed_lag_stitching(ssm_scenario, early_block, t, recent_block, recent_block
 
 def _check_smoother(ssm_scenario, particle_filter):
     _check_lg(ssm_scenario, particle_filter)
+    if isinstance(ssm_scenario, StochasticVolatility) and ssm_scenario.dim != 1:
+        raise NotImplementedError("StochasticVolatility: the smoothing kernels take dim = 1")
     if isinstance(ssm_scenario, TimeHomogenousLinearGaussian) and not ssm_scenario.gpu_supported():
         raise NotImplementedError(f"(d, dy) = ({ssm_scenario.dim}, {ssm_scenario.dim_obs}) not compiled")
     if not isinstance(particle_filter, BootstrapFilter):

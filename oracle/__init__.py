@@ -62,6 +62,11 @@ class _SVModel(ctypes.Structure):
                 ("cB", ctypes.c_float), ("c0", ctypes.c_float), ("m0", ctypes.c_float)]
 
 
+class _SVDModel(ctypes.Structure):
+    _fields_ = [("d", ctypes.c_int), ("A", vp), ("Lq", vp), ("C0", vp), ("m0", vp), ("r2", vp),
+                ("cB", ctypes.c_float)]
+
+
 class _NLModel(ctypes.Structure):
     _fields_ = [("s0", ctypes.c_float), ("tsd", ctypes.c_float), ("lsd", ctypes.c_float), ("c", ctypes.c_float)]
 
@@ -140,6 +145,12 @@ def lib():
         L.o_sv_run_hist.restype = ctypes.c_double
         L.o_sv_batch.argtypes = [ctypes.POINTER(_SVModel), i64, i64p, i64p, i64p, f32p, u32p, ctypes.c_float,
                                  ctypes.c_int, f64p]
+        L.o_svd_init.argtypes = [ctypes.POINTER(_SVDModel), i64, u32p, vp, f32p, f32p]
+        L.o_svd_propagate.argtypes = [ctypes.POINTER(_SVDModel), i64, u32p, f32p, ctypes.c_float, f32p, vp, vp, f32p,
+                                      f32p]
+        L.o_svd_run_hist.argtypes = [ctypes.POINTER(_SVDModel), i64, i64, u32p, f32p, vp, ctypes.c_float,
+                                     ctypes.c_int, f32p, i32p, vp, vp]
+        L.o_svd_run_hist.restype = ctypes.c_double
         L.o_nl_drift.argtypes = [ctypes.c_float]
         L.o_nl_drift.restype = ctypes.c_float
         L.o_nl_init.argtypes = [ctypes.POINTER(_NLModel), i64, u32p, vp, f32p, f32p]
@@ -492,6 +503,54 @@ def sv_run_hist(params, n, key, y, t=None, ess_threshold=0.5, scheme="systematic
     lh = np.empty((T, n), np.float32)
     logZ = lib().o_sv_run_hist(ctypes.byref(s), n, T, _u32(key), y, _ptr(tt), float(ess_threshold),
                                SCHEMES[scheme], ess, res, _ptr(xh), _ptr(lh))
+    return dict(log_z=logZ, ess=ess, resampled=res.astype(bool), value=xh, log_weight=lh)
+
+
+def _svd_struct(p):
+    keep = [np.ascontiguousarray(p[k], np.float32) for k in ("A", "Lq", "C0", "m0", "r2")]
+    s = _SVDModel(int(p["d"]), *[a.ctypes.data for a in keep], float(p["cB"]))
+    return s, keep
+
+
+def svd_init(params, n, key, y0):
+    """initiate_particles for the d-dimensional stochastic-volatility model: x (n, d), lw (n,)"""
+    s, keep = _svd_struct(params)
+    d = int(params["d"])
+    x = np.empty((n, d), np.float32)
+    lw = np.empty(n, np.float32)
+    y0 = None if y0 is None else _f32(y0).reshape(d)
+    lib().o_svd_init(ctypes.byref(s), n, _u32(key), _ptr(y0), x, lw)
+    return x, lw
+
+
+def svd_propagate(params, kt, y, dt, x_prev, anc=None, lw_prev=None):
+    """one bootstrap step of the d-dimensional stochastic-volatility model (x particle-major)"""
+    s, keep = _svd_struct(params)
+    x_prev = _f32(x_prev)
+    n, d = x_prev.shape
+    anc = None if anc is None else np.ascontiguousarray(anc, np.int32)
+    lw_prev = None if lw_prev is None else _f32(lw_prev)
+    xn = np.empty((n, d), np.float32)
+    ln = np.empty(n, np.float32)
+    lib().o_svd_propagate(ctypes.byref(s), n, _u32(kt), _f32(y).reshape(d), float(dt), x_prev, _ptr(anc),
+                          _ptr(lw_prev), xn, ln)
+    return xn, ln
+
+
+def svd_run_hist(params, n, key, y, t=None, ess_threshold=0.5, scheme="systematic"):
+    """run_particle_filter_for_marginals on the d-dimensional stochastic-volatility model with
+    the history: value (T, n, d), log_weight (T, n), ess, resampled, log_z"""
+    s, keep = _svd_struct(params)
+    d = int(params["d"])
+    y = _f32(y).reshape(-1, d)
+    T = y.shape[0]
+    tt = None if t is None else _f32(t).reshape(-1)
+    ess = np.empty(T, np.float32)
+    res = np.empty(T, np.int32)
+    xh = np.empty((T, n, d), np.float32)
+    lh = np.empty((T, n), np.float32)
+    logZ = lib().o_svd_run_hist(ctypes.byref(s), n, T, _u32(key), y, _ptr(tt), float(ess_threshold),
+                                SCHEMES[scheme], ess, res, _ptr(xh), _ptr(lh))
     return dict(log_z=logZ, ess=ess, resampled=res.astype(bool), value=xh, log_weight=lh)
 
 

@@ -98,6 +98,52 @@ def sv_params(phi=0.95, sigma=0.3, likelihood_variance=1.0, initial_variance=Non
                 sqrtR=np.float32(np.sqrt(likelihood_variance)))
 
 
+def svd_params(initial_mean=None, initial_covariance=None, transition_matrix=None, transition_covariance=None,
+               likelihood_covariance_diag=None, dim=None):
+    """float32 constants of the d-dimensional stochastic-volatility model
+    (stochastic_volatility.py:25-108, diagonal likelihood covariance): A, Lq = chol(Q),
+    C0 = chol(initial_covariance), m0, r2 = 1 / R (R = likelihood_covariance_diag) and
+    cB = (d log 2 pi - sum log r2) / 2."""
+    for a in (initial_mean, initial_covariance, transition_matrix, transition_covariance, likelihood_covariance_diag):
+        if dim is None and a is not None and np.ndim(a) > 0:
+            dim = np.shape(a)[-1]
+    d = int(dim)
+    m0 = np.zeros(d) if initial_mean is None else np.asarray(initial_mean, np.float64).reshape(d)
+    S0 = np.eye(d) if initial_covariance is None else _mat(initial_covariance, d)
+    A = np.eye(d) if transition_matrix is None else _mat(transition_matrix, d)
+    Q = np.eye(d) if transition_covariance is None else _mat(transition_covariance, d)
+    R = np.ones(d) if likelihood_covariance_diag is None else np.asarray(likelihood_covariance_diag, np.float64)
+    R = np.diag(R) if R.ndim == 2 else R.reshape(d)
+    f32 = lambda a: np.ascontiguousarray(a, np.float32)
+    r2 = f32(1.0 / R)
+    return dict(d=d, A=f32(A), Lq=f32(np.linalg.cholesky(Q)), C0=f32(np.linalg.cholesky(S0)), m0=f32(m0), r2=r2,
+                cB=np.float32(0.5 * (d * LOG2PI - np.sum(np.log(r2.astype(np.float64))))), sqrtR=f32(np.sqrt(R)),
+                Q=Q, R=R, S0=S0, A64=A)
+
+
+def simulate_svd(p, t, key):
+    """StateSpaceModel.simulate (ssm.py:138-163) for the d-dimensional stochastic-volatility
+    model, float32 host arithmetic: x_0 = C0 e + m0, x_t = A x_{t-1} + (Lq e) sqrt(dt),
+    y_t = sqrt(R) exp(x_t / 2) e'."""
+    from . import split, normal
+    t = np.asarray(t, np.float32).reshape(-1)
+    T, d = t.size, p["d"]
+    keys = split(key, 2 * T)
+    f = np.float32
+    x = np.empty((T, d), np.float32)
+    y = np.empty((T, d), np.float32)
+    for i in range(T):
+        e = normal(keys[i], d)
+        if i == 0:
+            x[0] = (p["C0"] @ e).astype(np.float32) + p["m0"]
+        else:
+            sdt = f(np.sqrt(f(t[i] - t[i - 1])))
+            x[i] = (p["A"] @ x[i - 1]).astype(np.float32) + ((p["Lq"] @ e).astype(np.float32) * sdt)
+        ey = normal(keys[T + i], d)
+        y[i] = (p["sqrtR"] * np.exp(f(0.5) * x[i]).astype(np.float32) * ey).astype(np.float32)
+    return x, y
+
+
 def simulate_lg(p, T, key):
     """StateSpaceModel.simulate (ssm.py:138-163) for the linear-Gaussian model, float32."""
     keys = split(key, 2 * T)

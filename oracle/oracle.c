@@ -835,6 +835,143 @@ double o_sv_run_hist(const o_sv_model *md, int64_t n, int64_t T, const uint32_t 
     return o_sv_run_impl(md, n, T, key, y, t_all, ess_threshold, scheme, ess_out, resampled_out, x_hist, lw_hist);
 }
 
+/* ------------------------------------- stochastic volatility, dimension d */
+
+/* StochasticVolatility (stochastic_volatility.py:15-108) with a diagonal likelihood
+ * covariance R (likelihood_covariance_diag, a vector):
+ *   initial_sample     x_0 = C0 normal(key, (d,)) + m0                         (:71-76)
+ *   transition_sample  x_t = A x_{t-1} + (Lq normal(key, (d,))) sqrt(t_t - t_{t-1}) (:87-94)
+ *   likelihood_potential with s_j = r_j / exp(x_j / 2), r_j^2 = 1 / R_j:
+ *     sum_j 0.5 y_j^2 s_j^2 + (d log 2pi - sum_j log s_j^2) / 2
+ *     = cB + sum_j (0.5 x_j + (0.5 y_j^2 r2_j) exp(-x_j)),  cB = (d log 2pi - sum log r2_j) / 2
+ * accumulated j = 0, 1, ... as pot = fma(a_j, exp(-x_j), fma(0.5, x_j, pot)) from pot = cB
+ * (for d = 1 the dim-1 model's formula).  Matrix-vector products are fma chains in
+ * ascending column order. */
+typedef struct {
+    int d;
+    const float *A;   /* d x d transition_matrix */
+    const float *Lq;  /* d x d transition_covariance_sqrt */
+    const float *C0;  /* d x d initial_covariance_sqrt */
+    const float *m0;  /* d initial_mean */
+    const float *r2;  /* d: 1 / likelihood_covariance_diag */
+    float cB;
+} o_svd_model;
+
+static inline float o_svd_potential(const o_svd_model *md, const float *x, const float *y)
+{
+    float pot = md->cB;
+    for (int j = 0; j < md->d; ++j) {
+        float a = (0.5f * (y[j] * y[j])) * md->r2[j];
+        pot = fmaf(a, o_expf(-x[j]), fmaf(0.5f, x[j], pot));
+    }
+    return pot;
+}
+
+static inline void o_svd_mv(const float *M, const float *v, int d, int r, float *out)
+{
+    const float *m = M + r * d;
+    float acc = m[0] * v[0];
+    for (int k = 1; k < d; ++k) acc = fmaf(m[k], v[k], acc);
+    *out = acc;
+}
+
+/* x particle-major (n, d) */
+void o_svd_init(const o_svd_model *md, int64_t n, const uint32_t *key, const float *y0, float *x, float *lw)
+{
+    const int d = md->d;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        uint32_t a0, a1;
+        float e[64];
+        o_split_at(key[0], key[1], (uint64_t)n, (uint64_t)i, &a0, &a1);
+        o_normal_vec(a0, a1, d, e);
+        float *xi = x + i * d;
+        for (int r = 0; r < d; ++r) {
+            float v;
+            o_svd_mv(md->C0, e, d, r, &v);
+            xi[r] = v + md->m0[r];
+        }
+        lw[i] = y0 ? -o_svd_potential(md, xi, y0) : 0.0f;
+    }
+}
+
+/* one step: x_new = A x_src + (Lq e) sdt, sdt = sqrt(dt); lw_new = lw_res - potential */
+void o_svd_propagate(const o_svd_model *md, int64_t n, const uint32_t *kt, const float *y, float dt,
+                     const float *x_prev, const int32_t *anc, const float *lw_prev, float *x_new, float *lw_new)
+{
+    const int d = md->d;
+    const float sdt = sqrtf(dt);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        uint32_t a0, a1;
+        float e[64];
+        o_split_at(kt[0], kt[1], (uint64_t)n, (uint64_t)i, &a0, &a1);
+        o_normal_vec(a0, a1, d, e);
+        const float *xs = x_prev + (anc ? (int64_t)anc[i] : i) * d;
+        float *xn = x_new + i * d;
+        for (int r = 0; r < d; ++r) {
+            float fx, le;
+            o_svd_mv(md->A, xs, d, r, &fx);
+            o_svd_mv(md->Lq, e, d, r, &le);
+            xn[r] = fx + le * sdt;
+        }
+        lw_new[i] = (lw_prev ? lw_prev[i] : 0.0f) - o_svd_potential(md, xn, y);
+    }
+}
+
+/* run_particle_filter_for_marginals with the bootstrap filter; t_all (nullable): the T
+ * times (else unit steps); scheme as in o_lg_run; x_hist (T, n, d), lw_hist (T, n)
+ * nullable.  Returns log Z. */
+double o_svd_run_hist(const o_svd_model *md, int64_t n, int64_t T, const uint32_t *key, const float *y,
+                      const float *t_all, float ess_threshold, int scheme, float *ess_out, int32_t *resampled_out,
+                      float *x_hist, float *lw_hist)
+{
+    const int d = md->d;
+    float *xa = (float *)malloc(sizeof(float) * (size_t)n * d), *xb = (float *)malloc(sizeof(float) * (size_t)n * d);
+    float *la = (float *)malloc(sizeof(float) * (size_t)n), *lb = (float *)malloc(sizeof(float) * (size_t)n);
+    int32_t *anc = (int32_t *)malloc(sizeof(int32_t) * (size_t)n);
+    uint32_t keys2[4], rk[2], sk[2];
+    o_split(key, 2, keys2);
+    rk[0] = keys2[0]; rk[1] = keys2[1];
+    sk[0] = keys2[2]; sk[1] = keys2[3];
+    o_svd_init(md, n, sk, y, xa, la);
+    if (x_hist) memcpy(x_hist, xa, sizeof(float) * (size_t)n * d);
+    if (lw_hist) memcpy(lw_hist, la, sizeof(float) * (size_t)n);
+    double st[4];
+    o_lse_ess(la, n, st);
+    double logn = log((double)n);
+    double logZ = st[1] - logn, lse_prev = st[1];
+    float ess_prev = (float)st[3];
+    if (ess_out) ess_out[0] = ess_prev;
+    if (resampled_out) resampled_out[0] = 0;
+    uint32_t *tkeys = (uint32_t *)malloc(sizeof(uint32_t) * 2 * (size_t)(T > 1 ? T - 1 : 1));
+    if (T > 1) o_split(rk, T - 1, tkeys);
+    for (int64_t t = 1; t < T; ++t) {
+        const uint32_t *kt = tkeys + 2 * (t - 1);
+        int res = ess_prev < ess_threshold * (float)n;
+        if (res) {
+            if (scheme == 0) o_resample_systematic(la, n, o_bits_at(kt[0], kt[1], 1, 0) >> 9, anc);
+            else if (scheme == 1) o_resample_multinomial(la, n, kt, anc);
+            else o_resample_gumbel(la, n, n, kt, anc);
+        }
+        const float dt = t_all ? t_all[t] - t_all[t - 1] : 1.0f;
+        o_svd_propagate(md, n, kt, y + t * d, dt, xa, res ? anc : NULL, res ? NULL : la, xb, lb);
+        o_lse_ess(lb, n, st);
+        logZ += st[1] - (res ? logn : lse_prev);
+        lse_prev = st[1];
+        ess_prev = (float)st[3];
+        if (ess_out) ess_out[t] = ess_prev;
+        if (resampled_out) resampled_out[t] = res;
+        if (x_hist) memcpy(x_hist + t * n * d, xb, sizeof(float) * (size_t)n * d);
+        if (lw_hist) memcpy(lw_hist + t * n, lb, sizeof(float) * (size_t)n);
+        float *tp = xa; xa = xb; xb = tp;
+        tp = la; la = lb; lb = tp;
+    }
+    free(tkeys);
+    free(xa); free(xb); free(la); free(lb); free(anc);
+    return logZ;
+}
+
 /* Many independent SV filters (the batched workload), each with its own
  * (n_b, T_b, y_b, key_b); filters run in parallel across host threads. */
 void o_sv_batch(const o_sv_model *md, int64_t B, const int64_t *n, const int64_t *T, const int64_t *y_off,
@@ -1845,7 +1982,7 @@ void o_abc_mcmc_rm_lg(const o_abc_model *md, int n, const uint32_t *key, float t
     o_split_at(key[0], key[1], 2, 1, &a0, &a1);
     o_split_at(key[0], key[1], 2, 0, &t0, &t1);
     o_split_at(t0, t1, 2, 0, &K0, &K1);
-    float e[16], xc[16], xp[16] = {0.0f}, st[16], pm[16], dg[16];
+    float e[16], xc[16] = {0.0f}, xp[16] = {0.0f}, st[16], pm[16], dg[16];
     o_normal_vec(a0, a1, d, e);
     for (int r = 0; r < d; ++r) {
         float v = md->C0[r * d] * e[0];
