@@ -120,6 +120,10 @@ class TimeHomogenousLinearGaussian(StateSpaceModel):
             self.__dict__["_derived"] = (p, s)
         return self.__dict__["_derived"]
 
+    def transition_function(self, x_previous, t_previous, t_new):
+        """F x on the batch (n, d) (the mean of transition_sample, linear_gaussian.py:86-94)"""
+        return x_previous @ torch.as_tensor(np.asarray(self.transition_matrix, np.float32), device=x_previous.device).T
+
     def gpu_supported(self):
         """(d, dy) has compiled kernels for every path (filters, Kalman, smoothers, gradients)"""
         return (self.dim, self.dim_obs) in LG_SUPPORTED
@@ -148,6 +152,81 @@ class TimeHomogenousLinearGaussian(StateSpaceModel):
         dev = _dev.device()
         return cdict(x=torch.from_numpy(x).to(dev), y=torch.from_numpy(y).to(dev),
                      t=torch.as_tensor(np.asarray(t_all), device=dev), name=f"{self.name} simulation")
+
+
+class NonLinearGaussian(StateSpaceModel):
+    """x_t ~ N(f(x_{t-1}, t_previous, t_new), Q), y_t ~ N(H x_t, R), Q, H, R time-homogeneous
+    (mocat/src/ssm/nonlinear_gaussian.py:19-131).  Subclass it and implement
+    transition_function(x_previous, t_previous, t_new) on the whole particle batch: x_previous
+    is an (n, d) float32 CUDA tensor, the result (n, d).  The filters then run through the
+    generic driver (the library's key, normal, logsumexp / ESS, resampling and gather kernels,
+    the model's arithmetic in torch); OptimalNonLinearGaussianParticleFilter uses the
+    transition function and the constants of its startup."""
+    dim = None
+
+    def __init__(self, initial_mean=None, initial_covariance=None, transition_covariance=None,
+                 likelihood_matrix=None, likelihood_covariance=None, name=None):
+        super().__init__(name=name)
+        d = self.dim
+        if d is None:
+            for a in (initial_mean, initial_covariance, transition_covariance, likelihood_matrix,
+                      likelihood_covariance):
+                if a is not None and np.ndim(a) > 0:
+                    d = int(np.shape(a)[-1])
+                    break
+        if d is None:
+            raise AttributeError(f"Could not find dimension for {self.__class__.__name__}")
+        self.dim = d
+        self.initial_mean = np.zeros(d) if initial_mean is None else _np(initial_mean).reshape(d)
+        self.initial_covariance = np.eye(d) if initial_covariance is None else _as_matrix(initial_covariance, d)
+        self.transition_covariance = (np.eye(d) if transition_covariance is None
+                                      else _as_matrix(transition_covariance, d))
+        self.likelihood_matrix = np.eye(d) if likelihood_matrix is None else np.atleast_2d(_np(likelihood_matrix))
+        self.dim_obs = self.likelihood_matrix.shape[0]
+        self.likelihood_covariance = (np.eye(self.dim_obs) if likelihood_covariance is None
+                                      else _as_matrix(likelihood_covariance, self.dim_obs))
+
+    def __setattr__(self, key, value):
+        self.__dict__[key] = value
+        if key in ("initial_mean", "initial_covariance", "transition_covariance", "likelihood_matrix",
+                   "likelihood_covariance"):
+            self.__dict__.pop("_consts", None)
+
+    def constants(self):
+        """float32 CUDA tensors: m0, C0 = chol(initial_covariance), Lq = chol(Q), H,
+        P = inv(chol(R)) (the likelihood precision square root) and c = (dy log 2 pi -
+        log det(R^-1)) / 2, as reset_covariance (utils.py:247-262) derives them"""
+        if "_consts" not in self.__dict__:
+            dev = _dev.device()
+            R = self.likelihood_covariance
+            P = np.linalg.inv(np.linalg.cholesky(R))
+            t = lambda a: torch.as_tensor(np.asarray(a, np.float32), device=dev)
+            self.__dict__["_consts"] = dict(
+                m0=t(self.initial_mean), C0=t(np.linalg.cholesky(self.initial_covariance)),
+                Lq=t(np.linalg.cholesky(self.transition_covariance)), H=t(self.likelihood_matrix), P=t(P),
+                c=float(np.float32((self.dim_obs * LOG2PI + np.log(np.linalg.det(R))) / 2.0)))
+        return self.__dict__["_consts"]
+
+    def transition_function(self, x_previous, t_previous, t_new):
+        raise NotImplementedError(f"{self.__class__.__name__} nonlinear transition_function not implemented")
+
+    def initial_sample(self, t, random_keys):
+        """normal(key_i, (d,)) @ C0^T + m0 (nonlinear_gaussian.py:87-91)"""
+        c = self.constants()
+        return mrandom.normal_keys(random_keys, self.dim) @ c["C0"].T + c["m0"]
+
+    def transition_sample(self, x_previous, t_previous, t_new, random_keys):
+        """f(x) + normal(key_i, (d,)) @ transition_covariance_sqrt (:106-112; the reference
+        multiplies by the Cholesky factor itself, not its transpose)"""
+        c = self.constants()
+        return (self.transition_function(x_previous, t_previous, t_new)
+                + mrandom.normal_keys(random_keys, self.dim) @ c["Lq"])
+
+    def likelihood_potential(self, x, y, t):
+        """gaussian_potential(y, x H^T, sqrt_prec = P) = 0.5 |(y - H x) P|^2 + c (:114-120)"""
+        c = self.constants()
+        v = (_dev.as_f32(y).reshape(1, -1) - x @ c["H"].T) @ c["P"]
+        return 0.5 * (v * v).sum(-1) + c["c"]
 
 
 class StochasticVolatility(StateSpaceModel):
@@ -380,14 +459,44 @@ class BootstrapFilter(ParticleFilter):
 
 class OptimalNonLinearGaussianParticleFilter(ParticleFilter):
     """Optimal proposal for linear-Gaussian observations
-    (mocat/src/ssm/nonlinear_gaussian.py:134-281), on the GPU for a linear
-    transition f(x) = F x (a TimeHomogenousLinearGaussian scenario).  startup
-    computes the reference's constants (:154-184) in float64 and keeps float32
-    copies for the kernels."""
+    (mocat/src/ssm/nonlinear_gaussian.py:134-281): fused kernels for a linear transition
+    f(x) = F x (a TimeHomogenousLinearGaussian scenario); a NonLinearGaussian scenario runs
+    the vectorised methods below through the generic driver.  startup computes the
+    reference's constants (:154-184) in float64 and keeps float32 copies."""
     name = "Optimal Non-linear Gaussian Particle Filter"
 
+    def _t(self, name):
+        return torch.as_tensor(np.asarray(self._consts[name], np.float32), device=_dev.device())
+
+    def initial_sample_and_weight_vectorised(self, ssm_scenario, y, t, random_keys):
+        """(:223-229, initial_sample :205-215): mean m0 + K0 (y - H m0), one (n, d) normal
+        draw from the first particle key, times the conditioned covariance square root
+        (not transposed, as the reference); zero log-weights"""
+        if getattr(self, "_consts", None) is None:
+            self.startup(ssm_scenario)
+        n = random_keys.shape[0]
+        m0, H, K0 = self._t("m064"), self._t("H64"), self._t("K0")
+        mean = m0 + K0 @ (_dev.as_f32(y).reshape(-1) - H @ m0)
+        e = mrandom.normal(random_keys[0], (n, ssm_scenario.dim))
+        return mean + e @ self._t("C0c"), torch.zeros(n, dtype=torch.float32, device=e.device)
+
+    def propose_and_intermediate_weight_vectorised(self, ssm_scenario, x_previous, t_previous, y_new, t_new,
+                                                   random_keys):
+        """(:264-281): mx = f(x), x_new = mx + (y - mx H^T) K^T + normal(keys[0], (n, d)) S^T,
+        log-weight -(0.5 |(y - mx H^T) W|^2 + cw)"""
+        if getattr(self, "_consts", None) is None:
+            self.startup(ssm_scenario)
+        H, K, S, W = self._t("H64"), self._t("K"), self._t("S"), self._t("W")
+        mx = ssm_scenario.transition_function(x_previous, t_previous, t_new)
+        r = _dev.as_f32(y_new).reshape(1, -1) - mx @ H.T
+        e = mrandom.normal(random_keys[0], tuple(x_previous.shape))
+        x_new = mx + r @ K.T + e @ S.T
+        v = r @ W
+        return x_new, -(0.5 * (v * v).sum(-1) + float(self._consts["cw"]))
+
     def startup(self, ssm_scenario):
-        p, _ = ssm_scenario.derived()
+        lg = isinstance(ssm_scenario, TimeHomogenousLinearGaussian)
+        p = ssm_scenario.derived()[0] if lg else None
         S0 = ssm_scenario.initial_covariance
         Q = ssm_scenario.transition_covariance
         H = ssm_scenario.likelihood_matrix
@@ -417,11 +526,16 @@ class OptimalNonLinearGaussianParticleFilter(ParticleFilter):
         self.weight_precision_sqrt = np.linalg.cholesky(weight_precision)
         self.weight_precision_det = np.linalg.det(weight_precision)
         dy = H.shape[0]
-        c = dict(d=p["d"], dy=dy, F=p["F"], H=p["H"], K=_f32(self.proposal_kalman_gain),
+        c = dict(d=ssm_scenario.dim, dy=dy, K=_f32(self.proposal_kalman_gain),
                  S=_f32(self.proposal_covariance_sqrt), W=_f32(self.weight_precision_sqrt),
                  cw=np.float32((dy * LOG2PI - np.log(self.weight_precision_det)) / 2.0),
-                 K0=_f32(self.initial_kalman_gain), C0c=_f32(self.initial_conditioned_covariance_sqrt), m0=p["m0"])
+                 K0=_f32(self.initial_kalman_gain), C0c=_f32(self.initial_conditioned_covariance_sqrt),
+                 H64=_f32(H), m064=_f32(ssm_scenario.initial_mean))
         self._consts = c
+        if not lg:
+            self._struct = None
+            return
+        c.update(F=p["F"], H=p["H"], m0=p["m0"])
         self._struct = _lib.OptModel(c["d"], c["dy"], c["F"].ctypes.data, c["H"].ctypes.data, c["K"].ctypes.data,
                                      c["S"].ctypes.data, c["W"].ctypes.data, float(c["cw"]), c["K0"].ctypes.data,
                                      c["C0c"].ctypes.data, c["m0"].ctypes.data)
