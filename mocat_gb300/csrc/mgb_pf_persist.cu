@@ -53,17 +53,23 @@ __device__ __forceinline__ bool grid_sync(GridBar *bar, unsigned nblocks, int *e
   }
   __syncthreads();
   if (threadIdx.x == 0) {
+    // Release / acquire at GPU scope instead of full fences: the arrival (acq_rel)
+    // publishes this block's writes (ordered before it by the block barrier) and, in
+    // the last block to arrive, acquires every other block's; that block's release
+    // of the generation passes them all on to the waiters' acquiring loads.
     int out = 0;
-    volatile unsigned int *vgen = &bar->gen;
-    const unsigned int g = *vgen;
-    __threadfence();
-    if (atomicAdd(&bar->count, 1u) == nblocks - 1) {
-      bar->count = 0u;
-      __threadfence();
-      atomicAdd(&bar->gen, 1u);
+    unsigned int g, prev;
+    asm volatile("ld.relaxed.gpu.u32 %0, [%1];" : "=r"(g) : "l"(&bar->gen) : "memory");
+    asm volatile("atom.acq_rel.gpu.add.u32 %0, [%1], 1;" : "=r"(prev) : "l"(&bar->count) : "memory");
+    if (prev == nblocks - 1) {
+      asm volatile("st.relaxed.gpu.u32 [%0], 0;" ::"l"(&bar->count) : "memory");
+      asm volatile("red.release.gpu.add.u32 [%0], 1;" ::"l"(&bar->gen) : "memory");
     } else {
       int polls = 0;
-      while (*vgen == g) {
+      while (true) {
+        unsigned int cur;
+        asm volatile("ld.acquire.gpu.u32 %0, [%1];" : "=r"(cur) : "l"(&bar->gen) : "memory");
+        if (cur != g) break;
         if (*(volatile int *)err & EB_TIMEOUT) {
           out = 1;
           break;
@@ -75,7 +81,6 @@ __device__ __forceinline__ bool grid_sync(GridBar *bar, unsigned nblocks, int *e
         }
       }
     }
-    __threadfence();
     gs_out = out;
   }
   __syncthreads();
