@@ -252,6 +252,16 @@ __device__ __forceinline__ bool mul_le(uint64_t a, uint64_t b, uint64_t c, uint6
   return h1 < h2 || (h1 == h2 && l1 <= l2);
 }
 
+// Arrival of a block at a "last block finishes" counter, by thread 0 after the
+// block's results are stored: the GPU-scope acq_rel add publishes them (release) and,
+// in the last block to arrive, makes every other block's visible (acquire; the block
+// barrier that follows passes them on to its other threads).  True in the last block.
+__device__ __forceinline__ bool last_block_arrival(unsigned int *counter) {
+  unsigned int prev;
+  asm volatile("atom.acq_rel.gpu.add.u32 %0, [%1], 1;" : "=r"(prev) : "l"(counter) : "memory");
+  return prev == gridDim.x - 1;
+}
+
 // ---------------------------------------------------------- reductions
 __device__ __forceinline__ float warp_max(float v) {
 #pragma unroll

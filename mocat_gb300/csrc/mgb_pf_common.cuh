@@ -70,12 +70,10 @@ __device__ __forceinline__ void pf_reduce(float lw, bool active, const PFCtl &ct
   const LsePartial part = block_lse_partial<TPB>(active && !nan ? lw : -INFINITY, nan, smf, smd);
   if (threadIdx.x == 0) {
     ctl.parts[blockIdx.x] = part;
-    __threadfence();
-    last = atomicAdd(ctl.counter, 1u) == gridDim.x - 1;
+    last = last_block_arrival(ctl.counter);
   }
   __syncthreads();
   if (!last) return;
-  __threadfence();
   pf_finalize<TPB>(ctl, t, smf, smd);
 }
 
@@ -87,12 +85,10 @@ __device__ __forceinline__ void pf_reduce_online(float m, float s1, float s2, in
   const LsePartial part = block_online_partial<TPB>(m, s1, s2, nanf, smf);
   if (threadIdx.x == 0) {
     ctl.parts[blockIdx.x] = part;
-    __threadfence();
-    last = atomicAdd(ctl.counter, 1u) == gridDim.x - 1;
+    last = last_block_arrival(ctl.counter);
   }
   __syncthreads();
   if (!last) return;
-  __threadfence();
   pf_finalize<TPB>(ctl, t, smf, smd);
 }
 

@@ -41,12 +41,10 @@ __global__ void __launch_bounds__(TPB) k_lse_ess(const float *__restrict__ lw, i
   const int nn = __syncthreads_or(nan);
   if (threadIdx.x == 0) {
     parts[blockIdx.x] = LsePartial{mb, d1, d2, nn};
-    __threadfence();
-    last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    last = last_block_arrival(counter);
   }
   __syncthreads();
   if (!last) return;
-  __threadfence();
   const LseOut o = combine_lse<TPB>(parts, gridDim.x, smf, smd);
   if (threadIdx.x == 0) {
     *out = o;

@@ -60,12 +60,10 @@ __device__ __forceinline__ void tile_sums_body(const float *__restrict__ lw, int
   if (threadIdx.x == 0) {
     tile_pfx[blockIdx.x] = acc;
     if (bad) atomicOr(&ctl->degenerate, 1);
-    __threadfence();
-    last = atomicAdd(&ctl->tile_counter, 1u) == gridDim.x - 1;
+    last = last_block_arrival(&ctl->tile_counter);
   }
   __syncthreads();
   if (!last) return;
-  __threadfence();
   const int nt = (int)gridDim.x;
   const int per = (nt + SCAN_TPB - 1) / SCAN_TPB;
   const int b0 = threadIdx.x * per, b1 = min(b0 + per, nt);
