@@ -587,6 +587,9 @@ typedef struct {
   int32_t likelihood;           /* MGB_LIK_LOGISTIC or MGB_LIK_GAUSSIAN */
   const float *gauss_mean_dev;  /* (d) device, MGB_LIK_GAUSSIAN */
   const float *gauss_prec_sqrt_dev; /* (d, d) row-major device, MGB_LIK_GAUSSIAN */
+  int32_t resampling;           /* MGB_RESAMPLE_SYSTEMATIC (O(N), default) or MGB_RESAMPLE_CATEGORICAL
+                                   (the reference's random.categorical, smc.py:61-71: O(N^2) Gumbel-max
+                                   draws, N <= 46340) */
 } mgb_smc_logreg_config;
 
 /* device pointers into the sampler's workspace */

@@ -106,7 +106,8 @@ class SMCConfig(ctypes.Structure):
                 ("move", ctypes.c_int32), ("leapfrog_steps", ctypes.c_int32), ("friction", ctypes.c_float),
                 ("prior_sample_scale", ctypes.c_float), ("n_schedule", ctypes.c_int32),
                 ("schedule_dev", ctypes.c_void_p), ("likelihood", ctypes.c_int32),
-                ("gauss_mean_dev", ctypes.c_void_p), ("gauss_prec_sqrt_dev", ctypes.c_void_p)]
+                ("gauss_mean_dev", ctypes.c_void_p), ("gauss_prec_sqrt_dev", ctypes.c_void_p),
+                ("resampling", ctypes.c_int32)]
 
 
 class SMCViews(ctypes.Structure):

@@ -276,6 +276,44 @@ __global__ void __launch_bounds__(ADAPT_TPB) k_smc_resample(SMCView v) {
   group_systematic_fill(C, N, Q, r >> 9, ~0ull / (uint64_t)N, anc, tg, ADAPT_TPB);
 }
 
+// the reference's categorical resampling per posterior (random.categorical(key, lw, (N,)),
+// smc.py:61-71): a_k = argmax_i gumbel(bits(key, N N)[k N + i]) + lw_i, first maximum, NaN
+// ignored (as k_categorical); one warp per output, grid (., B)
+__global__ void __launch_bounds__(256) k_smc_categorical(SMCView v) {
+  const int b = blockIdx.y, N = v.N, lane = threadIdx.x & 31;
+  int32_t *anc = v.anc + (int64_t)b * N;
+  const int64_t warp = (blockIdx.x * 256LL + threadIdx.x) >> 5, nwarps = ((int64_t)gridDim.x * 256) >> 5;
+  if (!v.active[b] || !v.resampled[b]) {
+    for (int64_t k = blockIdx.x * 256LL + threadIdx.x; k < N; k += (int64_t)gridDim.x * 256) anc[k] = (int32_t)k;
+    return;
+  }
+  const float *lw = v.lw + (int64_t)b * N;
+  const uint32_t k0 = v.rkey[2 * b], k1 = v.rkey[2 * b + 1];
+  const uint64_t tot = (uint64_t)N * (uint64_t)N;
+  for (int64_t k = warp; k < N; k += nwarps) {
+    float best = -INFINITY;
+    int64_t bi = N;
+    for (int64_t i = lane; i < N; i += 32) {
+      const float g = bits_to_gumbel(bits_at(k0, k1, tot, (uint64_t)k * (uint64_t)N + (uint64_t)i));
+      const float val = __fadd_rn(g, lw[i]);
+      if (val > best) {
+        best = val;
+        bi = i;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+      const int64_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ob > best || (ob == best && oi < bi)) {
+        best = ob;
+        bi = oi;
+      }
+    }
+    if (lane == 0) anc[k] = (int32_t)(bi < N ? bi : 0);
+  }
+}
+
 // rows of every posterior gathered by its ancestors (identity when it did not resample)
 template <int D>
 __global__ void __launch_bounds__(SMC_TPB) k_smc_gather(SMCView v) {
@@ -707,6 +745,7 @@ static bool smc_cfg_ok(const mgb_smc_logreg_config *cfg) {
   if (cfg->move != MGB_MOVE_UNDERDAMPED && cfg->move != MGB_MOVE_RANDOM_WALK) return false;
   if (cfg->leapfrog_steps < 0 || cfg->prior_sample_scale < 0.0f || cfg->n_schedule < 0) return false;
   if (cfg->n_schedule > 0 && !cfg->schedule_dev) return false;
+  if (cfg->resampling != MGB_RESAMPLE_SYSTEMATIC && cfg->resampling != MGB_RESAMPLE_CATEGORICAL) return false;
   if (cfg->likelihood == MGB_LIK_GAUSSIAN) return cfg->gauss_mean_dev && cfg->gauss_prec_sqrt_dev;
   return cfg->likelihood == MGB_LIK_LOGISTIC;
 }
@@ -775,10 +814,16 @@ static int smc_step_t(const mgb_smc_logreg_config *cfg, const SMCData &dat, SMCV
   int st;
   k_smc_keys<<<g, SMC_TPB, 0, s>>>(v, cfg->ess_threshold_resample, smc_msplit(cfg));
   if ((st = launch_status())) return st;
-  const size_t rs_smem = sizeof(uint64_t) * (size_t)cfg->N;
-  if (cudaFuncSetAttribute(k_smc_resample, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rs_smem) != cudaSuccess)
-    return ERR_UNSUPPORTED;
-  k_smc_resample<<<cfg->B, ADAPT_TPB, rs_smem, s>>>(v);
+  if (cfg->resampling == MGB_RESAMPLE_CATEGORICAL) {
+    const unsigned gx = (unsigned)std::min<int64_t>(((int64_t)cfg->N * 32 + 255) / 256, 1024);
+    k_smc_categorical<<<dim3(gx, (unsigned)cfg->B), 256, 0, s>>>(v);
+  } else {
+    const size_t rs_smem = sizeof(uint64_t) * (size_t)cfg->N;
+    if (cudaFuncSetAttribute(k_smc_resample, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rs_smem) !=
+        cudaSuccess)
+      return ERR_UNSUPPORTED;
+    k_smc_resample<<<cfg->B, ADAPT_TPB, rs_smem, s>>>(v);
+  }
   if ((st = launch_status())) return st;
   k_smc_gather<D><<<g, SMC_TPB, 0, s>>>(v);
   if ((st = launch_status())) return st;

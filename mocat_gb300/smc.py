@@ -12,8 +12,9 @@ at once, on Bayesian logistic regression or the Gaussian toy scenario.
         MetropolisedSMCSampler(RandomWalk(stepsize=1.0)), 10000, key, temperature_schedule=sched)
 
 Differences from the reference, by design:
-  * resampling (ess <= ess_threshold_resample n) is systematic, O(n), instead of
-    random.categorical;
+  * resampling (ess <= ess_threshold_resample n) is systematic, O(n), by default;
+    MetropolisedSMCSampler(..., resampling="categorical") draws the reference's
+    random.categorical instead (smc.py:61-71: O(n^2) Gumbel-max draws);
   * run() returns the reference's stacked chain for value and log_weight; run_batched
     keeps the final particles of every posterior (chain=True adds the stacked chain);
   * ``precision="bf16"`` evaluates the likelihood potential and its gradient on
@@ -162,7 +163,7 @@ class MetropolisedSMCSampler:
 
     def __init__(self, mcmc_sampler, mcmc_correction="sampler_default", mcmc_steps=1, max_iter=int(1e4),
                  temperature_schedule=None, max_temperature=1.0, ess_threshold_retain=0.9,
-                 ess_threshold_resample=0.5, bisection_tol=1e-5, max_bisection_iter=1000):
+                 ess_threshold_resample=0.5, bisection_tol=1e-5, max_bisection_iter=1000, resampling="systematic"):
         if isinstance(mcmc_sampler, type):
             mcmc_sampler = mcmc_sampler()
         if mcmc_correction not in ("sampler_default", "Metropolis"):
@@ -179,6 +180,10 @@ class MetropolisedSMCSampler:
         self.ess_threshold_resample = float(ess_threshold_resample)
         self.bisection_tol = float(bisection_tol)
         self.max_bisection_iter = int(max_bisection_iter)
+        if resampling not in ("systematic", "categorical"):
+            raise NotImplementedError(f"resampling {resampling!r}: the GPU sampler resamples 'systematic' or "
+                                      "'categorical'")
+        self.resampling = resampling
         self.temperature_schedule = None
         self.set_schedule(temperature_schedule)
 
@@ -227,7 +232,8 @@ class BatchedSMC:
                                   getattr(scenario, "prior_sample_scale", scenario.prior_scale),
                                   0 if sch is None else len(sch), _dev.ptr(self._sched), 1 if gauss else 0,
                                   _dev.ptr(scenario.device_constants()[0]) if gauss else None,
-                                  _dev.ptr(scenario.device_constants()[1]) if gauss else None)
+                                  _dev.ptr(scenario.device_constants()[1]) if gauss else None,
+                                  2 if getattr(sampler, "resampling", "systematic") == "categorical" else 0)
         self.keys = keys
         self.Xb = scenario.Xbf16() if precision == "bf16" and not gauss else None
         self.ws = _dev.workspace(_lib.lib().mgb_smc_logreg_workspace(ctypes.byref(self.cfg), self._n_data()))

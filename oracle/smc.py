@@ -8,8 +8,9 @@ RandomWalk moves (mocat/src/mcmc/standard_mcmc.py:20-153; utils.leapfrog mocat/s
 Metropolis.correct mocat/src/mcmc/metropolis.py:48-70), regula-falsi
 temperatures (utils.bisect mocat/src/utils.py:205-237) or a temperature schedule and the key schedule of
 mocat.run (mocat/src/sample.py:110-148), with the same two choices as the GPU
-sampler: systematic resampling and no re-evaluation of the (deterministic)
-potentials at the start of each MCMC block.  Draws come from the oracle's
+sampler: systematic resampling (or, with resampling="categorical", the reference's
+random.categorical) and no re-evaluation of the (deterministic) potentials at the
+start of each MCMC block.  Draws come from the oracle's
 jax.random restatement, so kernel and restatement see the same random numbers;
 arithmetic is float64.
 
@@ -77,16 +78,16 @@ def gaussian_potential_grad(mean, prec_sqrt, beta):
 
 
 def run(X, y, prior_scale, N, key, stepsize, mcmc_steps=5, retain=0.5, resample_thr=0.5, tol=1e-5,
-        max_bisect=1000, max_temp=1.0, max_iter=1000):
+        max_bisect=1000, max_temp=1.0, max_iter=1000, resampling="systematic"):
     """Logistic regression with MALA moves; see run_general."""
     return run_general(lambda b: potential_grad(X, y, b), np.asarray(X).shape[1], prior_scale, N, key, stepsize,
                        mcmc_steps=mcmc_steps, retain=retain, resample_thr=resample_thr, tol=tol,
-                       max_bisect=max_bisect, max_temp=max_temp, max_iter=max_iter)
+                       max_bisect=max_bisect, max_temp=max_temp, max_iter=max_iter, resampling=resampling)
 
 
 def run_general(lik_fn, d, prior_scale, N, key, stepsize, mcmc_steps=5, retain=0.5, resample_thr=0.5, tol=1e-5,
                 max_bisect=1000, max_temp=1.0, max_iter=1000, move="underdamped", leapfrog_steps=1,
-                friction=math.inf, sample_scale=None, schedule=None):
+                friction=math.inf, sample_scale=None, schedule=None, resampling="systematic"):
     """lik_fn(beta (P, d)) -> (lik (P,), grad (P, d)).  move "underdamped" (leapfrog_steps, friction;
     standard_mcmc.py:72-153) or "random_walk" (standard_mcmc.py:20-64); schedule: the
     temperature_schedule without its leading 0 (max_temp, max_iter follow it).  Returns
@@ -136,8 +137,11 @@ def run_general(lik_fn, d, prior_scale, N, key, stepsize, mcmc_steps=5, retain=0
         keys_all = _split(e, N + 2)
         pkeys = [_split(keys_all[j], msplit)[0] for j in range(N)]
         if res:
-            m23 = int(O.random_bits(keys_all[N], 1)[0]) >> 9
-            anc = O.resample_systematic(lw.astype(np.float32), m23)
+            if resampling == "categorical":  # random.categorical(key, lw, (N,)) (smc.py:61-71)
+                anc = O.resample_gumbel(lw.astype(np.float32), keys_all[N])
+            else:
+                m23 = int(O.random_bits(keys_all[N], 1)[0]) >> 9
+                anc = O.resample_systematic(lw.astype(np.float32), m23)
             beta, lik, glik, ms = beta[anc], lik[anc], glik[anc], ms[anc]
             lw_res, ess_res = np.zeros(N), float(N)
         else:

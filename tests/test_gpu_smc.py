@@ -59,6 +59,31 @@ def test_sampler_matches_restatement(cuda, d, N, seed):
         np.testing.assert_allclose(out.value[b].cpu().numpy(), ref["value"], atol=1e-3)
 
 
+def test_categorical_resampling_matches_restatement(cuda):
+    """resampling="categorical": the reference's random.categorical ancestors (O(N^2)
+    Gumbel-max draws from the resampling key), against the restatement with the same draws"""
+    import mocat_gb300 as mg
+    d, N = 3, 96
+    X, y = _data(200, d, 5)
+    sc = mg.smc.LogisticRegression(X, y, prior_scale=1.0)
+    sampler = mg.smc.MetropolisedSMCSampler(mg.smc.Underdamped(stepsize=0.15), mcmc_steps=3,
+                                            ess_threshold_retain=0.6, resampling="categorical")
+    keys = np.stack([O.PRNGKey(41), O.PRNGKey(42)])
+    out = mg.smc.run_batched(sc, sampler, N, keys)
+    for b in range(2):
+        ref = osmc.run(X, y, 1.0, N, keys[b], stepsize=0.15, mcmc_steps=3, retain=0.6, resampling="categorical")
+        L = int(out.iterations[b]) + 1
+        assert L == len(ref["temperature"]) and sum(ref["resampled"]) >= 2
+        np.testing.assert_allclose(out.temperature[b, :L].cpu().numpy(), ref["temperature"], rtol=1e-4)
+        assert np.array_equal(out.resampled[b, :L].cpu().numpy(), ref["resampled"])
+        np.testing.assert_allclose(out.log_norm_constant[b, :L].cpu().numpy(), ref["log_norm_constant"], rtol=1e-4)
+        np.testing.assert_allclose(out.value[b].cpu().numpy(), ref["value"], atol=1e-3)
+    # and a different chain from the systematic default on the same keys
+    sys_out = mg.smc.run_batched(sc, mg.smc.MetropolisedSMCSampler(mg.smc.Underdamped(stepsize=0.15), mcmc_steps=3,
+                                                                   ess_threshold_retain=0.6), N, keys)
+    assert not torch.equal(sys_out.value, out.value)
+
+
 def test_batched_log_evidence_matches_quadrature(cuda):
     import mocat_gb300 as mg
     X, y = _data(100, 2)
