@@ -641,7 +641,8 @@ int mgb_smc_logreg_step(const mgb_smc_logreg_config *cfg, const float *X_dev, co
  * lag_ones (B, T-1, d, d; may be NULL) replaces run_kalman_smoother_for_marginals_and_lag_ones
  * (kalman.py:60-94): <mean_t^f, mean_{t+1}^s> + G (cov_{t+1}^s + <mean_{t+1}^s - mean_{t+1}^f,
  * mean_{t+1}^s>), the reference's 1-D `@` products being dot products.
- * (d, dy) as for mgb_lg_model. */
+ * (d, dy): the compiled pairs of mgb_lg_model, or any other d, dy <= 32 (a run-time-dimension
+ * instance of the same kernels). */
 typedef struct {
   int32_t d, dy;
   const float *F, *Q, *H, *R, *m0, *C0;

@@ -22,14 +22,23 @@ namespace mgb {
 
 constexpr int KF_TPB = 128;
 
-template <int D, int DY>
+// The kernels take the dimensions as KFP::d / KFP::dy: for a compiled pair they are the
+// template arguments (compile-time constants, loops fully known), for the run-time
+// instance KFP<KF_DMAX, KF_DMAX, true> the values stored in the parameter block; array
+// extents are the template arguments either way, and every product is the same
+// sequence of operations.
+constexpr int KF_DMAX = 32;
+template <int D, int DY, bool RT = false>
 struct KFP {
   float F[D * D], Q[D * D], H[DY * D], R[DY * DY], m0[D], C0[D * D];
+  int rd, rdy;  // run-time dimensions (RT)
+  __device__ __forceinline__ int d() const { return RT ? rd : D; }
+  __device__ __forceinline__ int dy() const { return RT ? rdy : DY; }
 };
 
 // C[r][c] = sum_k A[r][k] B[k][c] (+ Add[r][c]); A (m x k), B (k x n) with row strides
-template <int M, int K, int N>
-__device__ __forceinline__ void mm(const float *A, const float *B, const float *Add, float *C, bool transB = false) {
+__device__ __forceinline__ void mm(int M, int K, int N, const float *A, const float *B, const float *Add, float *C,
+                                   bool transB = false) {
   for (int idx = threadIdx.x; idx < M * N; idx += KF_TPB) {
     const int r = idx / N, c = idx % N;
     float v = __fmul_rn(A[r * K], transB ? B[c * K] : B[c]);
@@ -40,8 +49,7 @@ __device__ __forceinline__ void mm(const float *A, const float *B, const float *
 
 // inverse of the N x N matrix S into Si by Gauss-Jordan elimination with
 // partial pivoting on the augmented [S | I] in W (N x 2N); log|det S| into *logdet
-template <int N>
-__device__ void gj_inverse(const float *S, float *W, float *Si, float *col, int *piv_row, double *logdet) {
+__device__ void gj_inverse(int N, const float *S, float *W, float *Si, float *col, int *piv_row, double *logdet) {
   for (int idx = threadIdx.x; idx < N * 2 * N; idx += KF_TPB) {
     const int r = idx / (2 * N), c = idx % (2 * N);
     W[idx] = c < N ? S[r * N + c] : (c - N == r ? 1.0f : 0.0f);
@@ -84,13 +92,14 @@ __device__ void gj_inverse(const float *S, float *W, float *Si, float *col, int 
   __syncthreads();
 }
 
-template <int D, int DY>
-__global__ void __launch_bounds__(KF_TPB) k_kalman_filter(const __grid_constant__ KFP<D, DY> p, int64_t T,
+template <int CD, int CDY, bool RT>
+__global__ void __launch_bounds__(KF_TPB) k_kalman_filter(const __grid_constant__ KFP<CD, CDY, RT> p, int64_t T,
                                                            const float *__restrict__ y, float *__restrict__ means,
                                                            float *__restrict__ covs, double *__restrict__ loglik) {
-  constexpr int M = D > DY ? D : DY;
-  __shared__ float mu[D], mup[D], P[D * D], Pp[D * D], T1[M * M], T2[M * M], S[DY * DY], Si[DY * DY],
-      W[DY * 2 * DY], K[D * DY], e[DY], col[DY];
+  constexpr int M = CD > CDY ? CD : CDY;
+  __shared__ float mu[CD], mup[CD], P[CD * CD], Pp[CD * CD], T1[M * M], T2[M * M], S[CDY * CDY], Si[CDY * CDY],
+      W[CDY * 2 * CDY], K[CD * CDY], e[CDY], col[CDY];
+  const int D = p.d(), DY = p.dy();
   __shared__ int piv;
   __shared__ double logdet;
   const int64_t b = blockIdx.x;
@@ -102,27 +111,27 @@ __global__ void __launch_bounds__(KF_TPB) k_kalman_filter(const __grid_constant_
       for (int i = threadIdx.x; i < D; i += KF_TPB) mup[i] = p.m0[i];
       for (int i = threadIdx.x; i < D * D; i += KF_TPB) Pp[i] = p.C0[i];
     } else {
-      mm<D, D, 1>(p.F, mu, nullptr, mup);
-      mm<D, D, D>(p.F, P, nullptr, T1);
+      mm(D, D, 1, p.F, mu, nullptr, mup);
+      mm(D, D, D, p.F, P, nullptr, T1);
       __syncthreads();
-      mm<D, D, D>(T1, p.F, p.Q, Pp, true);  // (F P) F' + Q
+      mm(D, D, D, T1, p.F, p.Q, Pp, true);  // (F P) F' + Q
     }
     __syncthreads();
     // S = H Pp H' + R, innovation e = y - H mup
-    mm<DY, D, D>(p.H, Pp, nullptr, T1);
+    mm(DY, D, D, p.H, Pp, nullptr, T1);
     for (int r = threadIdx.x; r < DY; r += KF_TPB) {
       float hm = __fmul_rn(p.H[r * D], mup[0]);
       for (int k = 1; k < D; ++k) hm = __fmaf_rn(p.H[r * D + k], mup[k], hm);
       e[r] = __fsub_rn(yb[t * DY + r], hm);
     }
     __syncthreads();
-    mm<DY, D, DY>(T1, p.H, p.R, S, true);
+    mm(DY, D, DY, T1, p.H, p.R, S, true);
     __syncthreads();
-    gj_inverse<DY>(S, W, Si, col, &piv, &logdet);
+    gj_inverse(DY, S, W, Si, col, &piv, &logdet);
     // K = Pp H' S^-1
-    mm<D, D, DY>(Pp, p.H, nullptr, T2, true);
+    mm(D, D, DY, Pp, p.H, nullptr, T2, true);
     __syncthreads();
-    mm<D, DY, DY>(T2, Si, nullptr, K);
+    mm(D, DY, DY, T2, Si, nullptr, K);
     __syncthreads();
     // mu = mup + K e; P = Pp - K (H Pp)
     for (int r = threadIdx.x; r < D; r += KF_TPB) {
@@ -130,7 +139,7 @@ __global__ void __launch_bounds__(KF_TPB) k_kalman_filter(const __grid_constant_
       for (int k = 1; k < DY; ++k) ke = __fmaf_rn(K[r * DY + k], e[k], ke);
       mu[r] = __fadd_rn(mup[r], ke);
     }
-    mm<D, DY, D>(K, T1, nullptr, T2);  // K (H Pp), T1 = H Pp still
+    mm(D, DY, D, K, T1, nullptr, T2);  // K (H Pp), T1 = H Pp still
     __syncthreads();
     for (int i = threadIdx.x; i < D * D; i += KF_TPB) P[i] = __fsub_rn(Pp[i], T2[i]);
     if (threadIdx.x == 0 && loglik) {
@@ -150,14 +159,15 @@ __global__ void __launch_bounds__(KF_TPB) k_kalman_filter(const __grid_constant_
   if (threadIdx.x == 0 && loglik) loglik[b] = ll;
 }
 
-template <int D, int DY>
-__global__ void __launch_bounds__(KF_TPB) k_kalman_smoother(const __grid_constant__ KFP<D, DY> p, int64_t T,
+template <int CD, int CDY, bool RT>
+__global__ void __launch_bounds__(KF_TPB) k_kalman_smoother(const __grid_constant__ KFP<CD, CDY, RT> p, int64_t T,
                                                              const float *__restrict__ fmeans,
                                                              const float *__restrict__ fcovs,
                                                              float *__restrict__ smeans, float *__restrict__ scovs,
                                                              float *__restrict__ lag) {
-  __shared__ float mus[D], Ps[D * D], Pf[D * D], A[D * D], Ai[D * D], W[D * 2 * D], G[D * D], T1[D * D],
-      T2[D * D], L[D * D], fm[D], fmn[D], dm[D], col[D];
+  __shared__ float mus[CD], Ps[CD * CD], Pf[CD * CD], A[CD * CD], Ai[CD * CD], W[CD * 2 * CD], G[CD * CD],
+      T1[CD * CD], T2[CD * CD], L[CD * CD], fm[CD], fmn[CD], dm[CD], col[CD];
+  const int D = p.d();
   __shared__ int piv;
   __shared__ double logdet;
   const int64_t b = blockIdx.x;
@@ -176,14 +186,14 @@ __global__ void __launch_bounds__(KF_TPB) k_kalman_smoother(const __grid_constan
     for (int i = threadIdx.x; i < D; i += KF_TPB) fm[i] = fmeans[mo + t * D + i];
     for (int i = threadIdx.x; i < D * D; i += KF_TPB) Pf[i] = fcovs[co + t * D * D + i];
     __syncthreads();
-    mm<D, D, D>(p.F, Pf, nullptr, T1);  // F Pf
+    mm(D, D, D, p.F, Pf, nullptr, T1);  // F Pf
     __syncthreads();
-    mm<D, D, D>(T1, p.F, p.Q, A, true);  // F Pf F' + Q
+    mm(D, D, D, T1, p.F, p.Q, A, true);  // F Pf F' + Q
     __syncthreads();
-    gj_inverse<D>(A, W, Ai, col, &piv, &logdet);
-    mm<D, D, D>(Pf, p.F, nullptr, T1, true);  // Pf F'
+    gj_inverse(D, A, W, Ai, col, &piv, &logdet);
+    mm(D, D, D, Pf, p.F, nullptr, T1, true);  // Pf F'
     __syncthreads();
-    mm<D, D, D>(T1, Ai, nullptr, G);  // G = Pf F' A^-1
+    mm(D, D, D, T1, Ai, nullptr, G);  // G = Pf F' A^-1
     // dm = mu_{t+1}^s - F mu_t
     for (int r = threadIdx.x; r < D; r += KF_TPB) {
       float fx = __fmul_rn(p.F[r * D], fm[0]);
@@ -210,9 +220,9 @@ __global__ void __launch_bounds__(KF_TPB) k_kalman_smoother(const __grid_constan
       for (int k = 1; k < D; ++k) g = __fmaf_rn(G[r * D + k], dm[k], g);
       mus[r] = __fadd_rn(fm[r], g);
     }
-    mm<D, D, D>(G, T2, nullptr, T1);  // G (P^s - A)
+    mm(D, D, D, G, T2, nullptr, T1);  // G (P^s - A)
     __syncthreads();
-    mm<D, D, D>(T1, G, Pf, Ps, true);  // ... G' + Pf
+    mm(D, D, D, T1, G, Pf, Ps, true);  // ... G' + Pf
     if (lag) {
       float *lo = lag + ((size_t)b * (T - 1) + t) * D * D;
       for (int i = threadIdx.x; i < D * D; i += KF_TPB) {
@@ -232,31 +242,36 @@ __global__ void __launch_bounds__(KF_TPB) k_kalman_smoother(const __grid_constan
   }
 }
 
-template <int D, int DY>
-static KFP<D, DY> pack_kf(const mgb_kalman_model *m) {
-  KFP<D, DY> p;
-  for (int i = 0; i < D * D; ++i) {
+// matrices packed with row strides d (run-time instance: the first d * d entries)
+template <int D, int DY, bool RT>
+static KFP<D, DY, RT> pack_kf(const mgb_kalman_model *m) {
+  KFP<D, DY, RT> p;
+  const int d = RT ? m->d : D, dy = RT ? m->dy : DY;
+  for (int i = 0; i < d * d; ++i) {
     p.F[i] = m->F[i];
     p.Q[i] = m->Q[i];
     p.C0[i] = m->C0[i];
   }
-  for (int i = 0; i < DY * D; ++i) p.H[i] = m->H[i];
-  for (int i = 0; i < DY * DY; ++i) p.R[i] = m->R[i];
-  for (int i = 0; i < D; ++i) p.m0[i] = m->m0[i];
+  for (int i = 0; i < dy * d; ++i) p.H[i] = m->H[i];
+  for (int i = 0; i < dy * dy; ++i) p.R[i] = m->R[i];
+  for (int i = 0; i < d; ++i) p.m0[i] = m->m0[i];
+  p.rd = d;
+  p.rdy = dy;
   return p;
 }
 
-template <int D, int DY>
+template <int D, int DY, bool RT = false>
 static int kf_run(const mgb_kalman_model *m, int64_t B, int64_t T, const float *y, float *means, float *covs,
                   double *loglik, cudaStream_t s) {
-  k_kalman_filter<D, DY><<<(unsigned)B, KF_TPB, 0, s>>>(pack_kf<D, DY>(m), T, y, means, covs, loglik);
+  k_kalman_filter<D, DY, RT><<<(unsigned)B, KF_TPB, 0, s>>>(pack_kf<D, DY, RT>(m), T, y, means, covs, loglik);
   return launch_status();
 }
 
-template <int D, int DY>
+template <int D, int DY, bool RT = false>
 static int ks_run(const mgb_kalman_model *m, int64_t B, int64_t T, const float *fm, const float *fc, float *sm,
                   float *sc, float *lag, cudaStream_t s) {
-  k_kalman_smoother<D, DY><<<(unsigned)B, KF_TPB, 0, s>>>(pack_kf<D, DY>(m), T, fm, fc, sm, sc, T > 1 ? lag : nullptr);
+  k_kalman_smoother<D, DY, RT><<<(unsigned)B, KF_TPB, 0, s>>>(pack_kf<D, DY, RT>(m), T, fm, fc, sm, sc,
+                                                               T > 1 ? lag : nullptr);
   return launch_status();
 }
 
@@ -272,7 +287,7 @@ static int ks_run(const mgb_kalman_model *m, int64_t B, int64_t T, const float *
         case 5: return FN<5, 1>(__VA_ARGS__);                  \
         case 8: return FN<8, 1>(__VA_ARGS__);                  \
         case 10: return FN<10, 1>(__VA_ARGS__);                \
-        default: return ERR_UNSUPPORTED;                       \
+        default: break;                                        \
       }                                                        \
     } else if (dy_ == d_) {                                    \
       switch (d_) {                                            \
@@ -282,9 +297,11 @@ static int ks_run(const mgb_kalman_model *m, int64_t B, int64_t T, const float *
         case 5: return FN<5, 5>(__VA_ARGS__);                  \
         case 8: return FN<8, 8>(__VA_ARGS__);                  \
         case 10: return FN<10, 10>(__VA_ARGS__);               \
-        default: return ERR_UNSUPPORTED;                       \
+        default: break;                                        \
       }                                                        \
     }                                                          \
+    /* no compiled pair: the run-time instance, d, dy <= KF_DMAX */  \
+    if (d_ <= KF_DMAX && dy_ <= KF_DMAX) return FN<KF_DMAX, KF_DMAX, true>(__VA_ARGS__); \
     return ERR_UNSUPPORTED;                                    \
   } while (0)
 

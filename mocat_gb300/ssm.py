@@ -129,8 +129,9 @@ class TimeHomogenousLinearGaussian(StateSpaceModel):
         return (self.dim, self.dim_obs) in LG_SUPPORTED
 
     def gpu_bootstrap_supported(self):
-        """the bootstrap filter runs on the GPU: compiled kernels, or the run-time-dimension
-        kernels (bit-identical, one launch per phase) for d, dy <= 32"""
+        """the bootstrap filter and the Kalman filter / smoothers run on the GPU: compiled
+        kernels, or the run-time-dimension kernels (the same operations; one launch per
+        phase for the particle filter) for d, dy <= 32"""
         return self.gpu_supported() or (self.dim <= LG_RUNTIME_MAX and self.dim_obs <= LG_RUNTIME_MAX)
 
     def simulate(self, t_all, random_key):
@@ -924,7 +925,8 @@ def _kalman_struct(ssm_scenario):
 def _check_kalman(ssm_scenario):
     if not isinstance(ssm_scenario, TimeHomogenousLinearGaussian):
         raise NotImplementedError(f"{ssm_scenario.__class__.__name__}: the Kalman filter takes a linear-Gaussian model")
-    if not ssm_scenario.gpu_supported():
+    # compiled pairs, or the run-time-dimension instance for d, dy <= 32
+    if not ssm_scenario.gpu_bootstrap_supported():
         raise NotImplementedError(f"(d, dy) = ({ssm_scenario.dim}, {ssm_scenario.dim_obs}) not compiled")
 
 

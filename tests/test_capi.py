@@ -83,11 +83,12 @@ def test_new_entry_points_reject_bad_arguments_on_host(L):
     import numpy as np
     null = None
     p = ctypes.c_void_p(256)
-    # Kalman: null model, then an unsupported (d, dy)
+    # Kalman: null model, then (d, dy) above the run-time-dimension limit (32)
     assert L.mgb_kalman_filter(null, 1, 4, p, p, p, null, null) == 1
-    e = np.eye(7, dtype=np.float32)
-    km = _lib.KalmanModel(7, 7, *([e.ctypes.data] * 5), np.zeros(7, np.float32).ctypes.data)
+    e = np.eye(33, dtype=np.float32)
+    km = _lib.KalmanModel(33, 33, *([e.ctypes.data] * 5), np.zeros(33, np.float32).ctypes.data)
     assert L.mgb_kalman_filter(ctypes.byref(km), 1, 4, p, p, p, null, null) == 2
+    assert L.mgb_kalman_smoother(ctypes.byref(km), 1, 4, p, p, p, p, null, null) == 2
     # rejection samplers: maximum_rejections must be >= 1
     F = np.eye(2, dtype=np.float32)
     tr = _lib.LGTransition(2, F.ctypes.data, F.ctypes.data, 0.0)

@@ -50,8 +50,11 @@ def _observations(ssm, T, seed):
     return y
 
 
-@pytest.mark.parametrize("d,dy", [(1, 1), (3, 1), (3, 3), (5, 5), (10, 1), (10, 10)])
+@pytest.mark.parametrize("d,dy", [(1, 1), (3, 1), (3, 3), (5, 5), (10, 1), (10, 10),
+                                  (6, 6), (7, 3), (2, 4), (12, 12), (32, 5)])
 def test_filter_and_smoother_match_oracle(cuda, d, dy):
+    """compiled pairs and, for (6, 6), (7, 3), (2, 4), (12, 12), (32, 5), the run-time-dimension
+    instance of the same kernels"""
     import mocat_gb300 as mg
     ssm, m = _model(d, dy, 10 * d + dy)
     T = 60
@@ -128,7 +131,9 @@ def test_reference_interval_check(cuda, dim, sds):
 
 
 def test_unsupported_model_raises(cuda):
+    """above the run-time-dimension limit (d or dy > 32) the Kalman filter is refused on the host"""
     import mocat_gb300 as mg
-    ssm = mg.ssm.TimeHomogenousLinearGaussian(np.zeros(6), np.eye(6), np.eye(6), np.eye(6), np.eye(6), np.eye(6))
+    e = np.eye(33)
+    ssm = mg.ssm.TimeHomogenousLinearGaussian(np.zeros(33), e, e, e, e, e)
     with pytest.raises(NotImplementedError):
-        mg.ssm.run_kalman_filter_for_marginals(ssm, np.zeros((4, 6), np.float32))
+        mg.ssm.run_kalman_filter_for_marginals(ssm, np.zeros((4, 33), np.float32))

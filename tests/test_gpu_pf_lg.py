@@ -77,7 +77,7 @@ def test_run_matches_oracle(cuda, scheme, d, odd, persistent):
 
 
 @pytest.mark.parametrize("d,dy,diag_r", [(6, 6, True), (7, 3, False), (4, 2, True), (12, 12, False), (9, 1, True),
-                                         (32, 5, False)])
+                                         (32, 5, False), (2, 4, False)])
 def test_runtime_dimensions_bit_exact(cuda, d, dy, diag_r):
     """(d, dy) pairs without a compiled kernel run on the run-time-dimension kernels: the
     online init / propagate and the whole filter (both resampling schemes, n even and odd)
@@ -122,8 +122,9 @@ def test_runtime_dimension_limits(cuda):
     with pytest.raises(NotImplementedError):
         mg.ssm.initiate_particles(ssm, mg.ssm.BootstrapFilter(), 100, O.PRNGKey(0), np.zeros(33, np.float32))
     _, ssm6 = _models(6, 6, seed=1)
-    with pytest.raises(NotImplementedError):
-        mg.ssm.run_kalman_filter_for_marginals(ssm6, np.zeros((4, 6), np.float32))
+    with pytest.raises(NotImplementedError):  # the optimal proposal needs a compiled pair
+        mg.ssm.initiate_particles(ssm6, mg.ssm.OptimalNonLinearGaussianParticleFilter(), 100, O.PRNGKey(0),
+                                  np.zeros(6, np.float32))
 
 
 @pytest.mark.parametrize("d", [3, 10])
