@@ -262,7 +262,9 @@ int mgb_pf_lg_score_batch(const mgb_lg_model *model_host, int64_t n, int64_t T, 
  * transition_potential(x0 -> x1) = 0.5 |(x1 - F x0) @ Pq|^2 + cq.
  * x_hist (T, d, N) dimension-major (the filter's history), lw_hist (T, N);
  * out (T, d, M) sampled trajectories, idx (T, M) the chosen particle indices.
- * d in {1,2,3,4,5,8,10}; M N < 2^32. */
+ * 1 <= d <= 32 (d in {1,2,3,4,5,8,10} compiled, any other d on the run-time-dimension
+ * kernels; the same operations); M N < 2^32.  The same range holds for every entry point
+ * that takes an mgb_lg_transition (stitching, potential pairs, the rejection variants). */
 typedef struct {
   int32_t d;
   const float *F;  /* d x d transition_matrix (host) */

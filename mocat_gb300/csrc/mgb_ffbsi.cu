@@ -14,8 +14,8 @@
 //   non-linear 1-D    mean = 0.5 x + 25 x / (1 + x^2) + 8 cos(1.2 t_prev),
 //                     potential(diff) = 0.5 (diff / transition_sd)^2 + log(2 pi) / 2
 //                     (nonlinear1d.py:41-61).
-// The kernels are templates over a transition policy (LGT<D>, NLT) that supplies
-// the two.  First maximum wins, NaN entries are skipped.
+// The kernels are templates over a transition policy (LGT<D>, NLT, SVT) that supplies
+// the two; LGT<32, true> reads its dimension (any d up to 32) from the parameter block.  First maximum wins, NaN entries are skipped.
 //
 // One CTA per sample: mean(x_t^i) is computed once per step by a separate kernel
 // (dimension-major, read through L2 by every CTA); the Gumbel bits of element
@@ -35,9 +35,10 @@ __global__ void __launch_bounds__(FB_TPB) k_ffbsi_step(const __grid_constant__ T
                                                         const float *__restrict__ fx, const float *__restrict__ lw,
                                                         const float *__restrict__ x_next_samples,
                                                         const uint32_t *tkey, int32_t *__restrict__ idx) {
-  constexpr int D = TP::DIM;
+  constexpr int DC = TP::DIM;
+  const int D = p.dim();
   __shared__ Best sm[FB_TPB / 32];
-  __shared__ float x1[D];
+  __shared__ float x1[DC];
   __shared__ uint32_t kj[2];
   const int64_t j = blockIdx.x;
   if (threadIdx.x < D) x1[threadIdx.x] = x_next_samples[threadIdx.x * M + j];
@@ -59,7 +60,7 @@ __global__ void __launch_bounds__(FB_TPB) k_ffbsi_step(const __grid_constant__ T
       const int64_t i = s ? q + h : q;
       if (i >= N) break;
       const float g = bits_to_gumbel(s ? r1 : r0);
-      float diff[D];
+      float diff[DC];
 #pragma unroll
       for (int r = 0; r < D; ++r) diff[r] = __fsub_rn(x1[r], fx[r * N + i]);
       best_take(b, __fadd_rn(g, __fsub_rn(lw[i], p.potential(diff))), (int32_t)i);
@@ -75,12 +76,13 @@ template <class TP>
 __global__ void __launch_bounds__(FB_TPB) k_pair_potential(const __grid_constant__ TP p, int64_t M,
                                                             const float *__restrict__ x0, const float *__restrict__ x1,
                                                             const float *__restrict__ lw, float *__restrict__ out) {
-  constexpr int D = TP::DIM;
+  constexpr int DC = TP::DIM;
+  const int D = p.dim();
   __shared__ float sd[1];
   const float drift = block_drift(p, sd);
   const int64_t i = blockIdx.x * (int64_t)FB_TPB + threadIdx.x;
   if (i >= M) return;
-  float xv[D], m[D], diff[D];
+  float xv[DC], m[DC], diff[DC];
 #pragma unroll
   for (int k = 0; k < D; ++k) xv[k] = x0[k * M + i];
   p.mean(xv, m, drift);
@@ -96,15 +98,16 @@ __global__ void __launch_bounds__(FB_TPB) k_stitch(const __grid_constant__ TP p,
                                                     const float *__restrict__ x0, const float *__restrict__ x1,
                                                     const float *__restrict__ lw1, const uint32_t *key,
                                                     int32_t *__restrict__ idx) {
-  constexpr int D = TP::DIM;
+  constexpr int DC = TP::DIM;
+  const int D = p.dim();
   __shared__ Best sm[FB_TPB / 32];
-  __shared__ float fx0[D];
+  __shared__ float fx0[DC];
   __shared__ uint32_t kj[2];
   __shared__ float sd[1];
   const float drift = block_drift(p, sd);
   const int64_t j = blockIdx.x;
   if (threadIdx.x == 0) {
-    float xv[D], m[D];
+    float xv[DC], m[DC];
 #pragma unroll
     for (int k = 0; k < D; ++k) xv[k] = x0[k * M0 + j];
     p.mean(xv, m, drift);
@@ -127,7 +130,7 @@ __global__ void __launch_bounds__(FB_TPB) k_stitch(const __grid_constant__ TP p,
       const int64_t i = s ? q + h : q;
       if (i >= M1) break;
       const float g = bits_to_gumbel(s ? r1 : r0);
-      float diff[D];
+      float diff[DC];
 #pragma unroll
       for (int r = 0; r < D; ++r) diff[r] = __fsub_rn(x1[r * M1 + i], fx0[r]);
       best_take(b, __fadd_rn(g, __fsub_rn(lw1[i], p.potential(diff))), (int32_t)i);
@@ -151,16 +154,16 @@ static int pairs_run(const TP &p, int64_t M, const float *x0, const float *x1, c
   return launch_status();
 }
 
-template <int D>
+template <int D, bool RT = false>
 static int stitch_lg(const mgb_lg_transition *tr, int64_t M0, int64_t M1, const float *x0, const float *x1,
                      const float *lw1, const uint32_t *key, int32_t *idx, cudaStream_t s) {
-  return stitch_run(pack_lgt<D>(tr), M0, M1, x0, x1, lw1, key, idx, s);
+  return stitch_run(pack_lgt<D, RT>(tr), M0, M1, x0, x1, lw1, key, idx, s);
 }
 
-template <int D>
+template <int D, bool RT = false>
 static int pair_potential(const mgb_lg_transition *tr, int64_t M, const float *x0, const float *x1, const float *lw,
                           float *out, cudaStream_t s) {
-  return pairs_run(pack_lgt<D>(tr), M, x0, x1, lw, out, s);
+  return pairs_run(pack_lgt<D, RT>(tr), M, x0, x1, lw, out, s);
 }
 
 // t_all (device, T times): step t's transition leaves x_t at t_all[t] (policies with a drift)
@@ -168,7 +171,8 @@ template <class TP>
 static int ffbsi_run(TP p, const float *t_all, int64_t T, int64_t N, int64_t M, const float *x_hist,
                      const float *lw_hist, const uint32_t *key, float *out, int32_t *idx, void *ws, size_t ws_bytes,
                      cudaStream_t s, const float *pqs_host = nullptr) {
-  constexpr int D = TP::DIM;
+  constexpr int TD = take_dim<TP>();
+  const int D = p.dim();
   Carver c(ws);
   float *fx = c.take<float>((size_t)D * N);
   uint32_t *tkeys = c.take<uint32_t>(2 * (size_t)T);
@@ -179,8 +183,8 @@ static int ffbsi_run(TP p, const float *t_all, int64_t T, int64_t N, int64_t M, 
   k_ffbsi_last<<<(unsigned)M, FB_TPB, 0, s>>>(N, M, lw_hist + (size_t)(T - 1) * N, tkeys + 2 * (T - 1),
                                               idx + (size_t)(T - 1) * M);
   if ((st = launch_status())) return st;
-  k_ffbsi_take<D><<<grid_for(M, 256), 256, 0, s>>>(N, M, x_hist + (size_t)(T - 1) * xs, idx + (size_t)(T - 1) * M,
-                                                   out + (size_t)(T - 1) * D * M);
+  k_ffbsi_take<TD><<<grid_for(M, 256), 256, 0, s>>>(N, M, x_hist + (size_t)(T - 1) * xs, idx + (size_t)(T - 1) * M,
+                                                    out + (size_t)(T - 1) * D * M, D);
   if ((st = launch_status())) return st;
   for (int64_t t = T - 2; t >= 0; --t) {
     if constexpr (TP::kDrift) p.tp = t_all + t;
@@ -191,18 +195,18 @@ static int ffbsi_run(TP p, const float *t_all, int64_t T, int64_t N, int64_t M, 
                                                     out + (size_t)(t + 1) * D * M, tkeys + 2 * t,
                                                     idx + (size_t)t * M);
     if ((st = launch_status())) return st;
-    k_ffbsi_take<D><<<grid_for(M, 256), 256, 0, s>>>(N, M, x_hist + (size_t)t * xs, idx + (size_t)t * M,
-                                                     out + (size_t)t * D * M);
+    k_ffbsi_take<TD><<<grid_for(M, 256), 256, 0, s>>>(N, M, x_hist + (size_t)t * xs, idx + (size_t)t * M,
+                                                      out + (size_t)t * D * M, D);
     if ((st = launch_status())) return st;
   }
   return OK;
 }
 
-template <int D>
+template <int D, bool RT = false>
 static int ffbsi_lg(const mgb_lg_transition *tr, int64_t T, int64_t N, int64_t M, const float *x_hist,
                     const float *lw_hist, const uint32_t *key, float *out, int32_t *idx, void *ws, size_t ws_bytes,
                     cudaStream_t s) {
-  return ffbsi_run(pack_lgt<D>(tr), nullptr, T, N, M, x_hist, lw_hist, key, out, idx, ws, ws_bytes, s);
+  return ffbsi_run(pack_lgt<D, RT>(tr), nullptr, T, N, M, x_hist, lw_hist, key, out, idx, ws, ws_bytes, s);
 }
 
 static bool ffbsi_sizes_ok(int64_t T, int64_t N, int64_t M) {
@@ -213,6 +217,21 @@ static bool ffbsi_sizes_ok(int64_t T, int64_t N, int64_t M) {
 }  // namespace mgb
 
 using namespace mgb;
+
+// compiled dimensions take their own instances; any other d up to 32 the run-time one
+#define MGB_FB_DISPATCH(FN, ...)                                                    \
+  switch (tr->d) {                                                                  \
+    case 1: return FN<1>(__VA_ARGS__);                                              \
+    case 2: return FN<2>(__VA_ARGS__);                                              \
+    case 3: return FN<3>(__VA_ARGS__);                                              \
+    case 4: return FN<4>(__VA_ARGS__);                                              \
+    case 5: return FN<5>(__VA_ARGS__);                                              \
+    case 8: return FN<8>(__VA_ARGS__);                                              \
+    case 10: return FN<10>(__VA_ARGS__);                                            \
+    default:                                                                        \
+      if (tr->d >= 1 && tr->d <= LGT_DMAX) return FN<LGT_DMAX, true>(__VA_ARGS__);  \
+      return ERR_UNSUPPORTED;                                                       \
+  }
 
 extern "C" {
 
@@ -229,30 +248,8 @@ int mgb_ffbsi_lg(const mgb_lg_transition *tr, int64_t T, int64_t N, int64_t M, c
                  void *stream) {
   if (!tr || !tr->F || !tr->Pq || !ffbsi_sizes_ok(T, N, M) || !x_hist || !lw_hist || !key || !out || !idx || !ws)
     return ERR_BAD_ARG;
-  cudaStream_t s = (cudaStream_t)stream;
-  switch (tr->d) {
-    case 1: return ffbsi_lg<1>(tr, T, N, M, x_hist, lw_hist, key, out, idx, ws, ws_bytes, s);
-    case 2: return ffbsi_lg<2>(tr, T, N, M, x_hist, lw_hist, key, out, idx, ws, ws_bytes, s);
-    case 3: return ffbsi_lg<3>(tr, T, N, M, x_hist, lw_hist, key, out, idx, ws, ws_bytes, s);
-    case 4: return ffbsi_lg<4>(tr, T, N, M, x_hist, lw_hist, key, out, idx, ws, ws_bytes, s);
-    case 5: return ffbsi_lg<5>(tr, T, N, M, x_hist, lw_hist, key, out, idx, ws, ws_bytes, s);
-    case 8: return ffbsi_lg<8>(tr, T, N, M, x_hist, lw_hist, key, out, idx, ws, ws_bytes, s);
-    case 10: return ffbsi_lg<10>(tr, T, N, M, x_hist, lw_hist, key, out, idx, ws, ws_bytes, s);
-    default: return ERR_UNSUPPORTED;
-  }
+  MGB_FB_DISPATCH(ffbsi_lg, tr, T, N, M, x_hist, lw_hist, key, out, idx, ws, ws_bytes, (cudaStream_t)stream);
 }
-
-#define MGB_FB_DISPATCH(FN, ...)                 \
-  switch (tr->d) {                               \
-    case 1: return FN<1>(__VA_ARGS__);           \
-    case 2: return FN<2>(__VA_ARGS__);           \
-    case 3: return FN<3>(__VA_ARGS__);           \
-    case 4: return FN<4>(__VA_ARGS__);           \
-    case 5: return FN<5>(__VA_ARGS__);           \
-    case 8: return FN<8>(__VA_ARGS__);           \
-    case 10: return FN<10>(__VA_ARGS__);         \
-    default: return ERR_UNSUPPORTED;             \
-  }
 
 int mgb_stitch_lg(const mgb_lg_transition *tr, int64_t M0, int64_t M1, const float *x0, const float *x1,
                   const float *lw1, const uint32_t *key, int32_t *idx, void *stream) {

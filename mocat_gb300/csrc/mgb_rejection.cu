@@ -73,8 +73,9 @@ __device__ __forceinline__ void rej_state(const RejSlot &s, float infl, int64_t 
 template <class TP, bool BACK>
 __device__ __forceinline__ float rej_potential(const TP &p, const float *u, const float *__restrict__ pool, int64_t Np,
                                                int64_t j) {
-  constexpr int D = TP::DIM;
-  float diff[D];
+  constexpr int DC = TP::DIM;
+  const int D = p.dim();
+  float diff[DC];
 #pragma unroll
   for (int r = 0; r < D; ++r) diff[r] = BACK ? __fsub_rn(u[r], pool[r * Np + j]) : __fsub_rn(pool[r * Np + j], u[r]);
   return p.potential(diff);
@@ -110,7 +111,8 @@ __global__ void __launch_bounds__(FB_TPB) k_rej_prerun(const __grid_constant__ T
                                                         const float *__restrict__ lw, const uint32_t *key,
                                                         int32_t *__restrict__ idx, float *__restrict__ dens,
                                                         RejCtl *ctl) {
-  constexpr int D = TP::DIM;
+  constexpr int DC = TP::DIM;
+  const int D = p.dim();
   __shared__ Best sm[FB_TPB / 32];
   __shared__ uint32_t kc[2];
   const int64_t i = blockIdx.x;
@@ -125,7 +127,7 @@ __global__ void __launch_bounds__(FB_TPB) k_rej_prerun(const __grid_constant__ T
   }
   const int32_t bi = block_argmax<FB_TPB>(b, sm);
   if (threadIdx.x == 0) {
-    float u[D];
+    float u[DC];
 #pragma unroll
     for (int r = 0; r < D; ++r) u[r] = itm[r * n + i];
     const float dv = expf_(-rej_potential<TP, BACK>(p, u, pool, Np, bi));
@@ -171,12 +173,13 @@ __global__ void __launch_bounds__(FB_TPB) k_rej_iter(const __grid_constant__ TP 
                                                       const float *__restrict__ lw, RejCfg cfg,
                                                       int32_t *__restrict__ idx, uint32_t *__restrict__ keys,
                                                       uint8_t *__restrict__ nya, RejSlot *ring, RejCtl *ctl) {
-  constexpr int D = TP::DIM;
+  constexpr int DC = TP::DIM;
+  const int D = p.dim();
   __shared__ Best sm[FB_TPB / 32];
   __shared__ uint32_t ks[6];
   __shared__ float sb;
   __shared__ int go;
-  __shared__ float su[D];
+  __shared__ float su[DC];
   const int64_t i = blockIdx.x;
   if (threadIdx.x == 0) {
     int g = 0;
@@ -234,11 +237,12 @@ __global__ void __launch_bounds__(FB_TPB) k_rej_final(const __grid_constant__ TP
                                                        int32_t *__restrict__ idx, const uint32_t *__restrict__ keys,
                                                        const uint8_t *__restrict__ nya, const RejSlot *ring,
                                                        const RejCtl *ctl, long long *evals) {
-  constexpr int D = TP::DIM;
+  constexpr int DC = TP::DIM;
+  const int D = p.dim();
   __shared__ Best sm[FB_TPB / 32];
   __shared__ uint32_t ks[2];
   __shared__ int go;
-  __shared__ float su[D];
+  __shared__ float su[DC];
   const int64_t i = blockIdx.x;
   if (threadIdx.x == 0) {
     bool reset;
@@ -312,7 +316,8 @@ static int ffbsi_rej_run(TP p, const RejCfg &cfg, const float *t_all, int64_t T,
                          const float *x_hist, const float *lw_hist, const uint32_t *key, float *out, int32_t *idx,
                          long long *evals, void *ws, size_t ws_bytes, cudaStream_t s,
                          const float *pqs_host = nullptr) {
-  constexpr int D = TP::DIM;
+  constexpr int TD = take_dim<TP>();
+  const int D = p.dim();
   Carver c(ws);
   float *fx = c.take<float>((size_t)D * N);
   uint32_t *tkeys = c.take<uint32_t>(2 * (size_t)T);
@@ -325,8 +330,8 @@ static int ffbsi_rej_run(TP p, const RejCfg &cfg, const float *t_all, int64_t T,
   k_ffbsi_last<<<(unsigned)M, FB_TPB, 0, s>>>(N, M, lw_hist + (size_t)(T - 1) * N, tkeys + 2 * (T - 1),
                                               idx + (size_t)(T - 1) * M);
   if ((st = launch_status())) return st;
-  k_ffbsi_take<D><<<grid_for(M, 256), 256, 0, s>>>(N, M, x_hist + (size_t)(T - 1) * xs, idx + (size_t)(T - 1) * M,
-                                                   out + (size_t)(T - 1) * D * M);
+  k_ffbsi_take<TD><<<grid_for(M, 256), 256, 0, s>>>(N, M, x_hist + (size_t)(T - 1) * xs, idx + (size_t)(T - 1) * M,
+                                                    out + (size_t)(T - 1) * D * M, D);
   if ((st = launch_status())) return st;
   for (int64_t t = T - 2; t >= 0; --t) {
     if constexpr (TP::kDrift) p.tp = t_all + t;
@@ -336,8 +341,8 @@ static int ffbsi_rej_run(TP p, const RejCfg &cfg, const float *t_all, int64_t T,
     st = rej_run<TP, true>(p, cfg, M, N, out + (size_t)(t + 1) * D * M, fx, lw_hist + (size_t)t * N, tkeys + 2 * t,
                            idx + (size_t)t * M, evals + t + 1, w, s);
     if (st) return st;
-    k_ffbsi_take<D><<<grid_for(M, 256), 256, 0, s>>>(N, M, x_hist + (size_t)t * xs, idx + (size_t)t * M,
-                                                     out + (size_t)t * D * M);
+    k_ffbsi_take<TD><<<grid_for(M, 256), 256, 0, s>>>(N, M, x_hist + (size_t)t * xs, idx + (size_t)t * M,
+                                                      out + (size_t)t * D * M, D);
     if ((st = launch_status())) return st;
   }
   return OK;
@@ -348,7 +353,7 @@ template <class TP>
 static int stitch_rej_run(const TP &p, const RejCfg &cfg, int64_t M, const float *x0, const float *x1,
                           const float *lw1, const uint32_t *key, int32_t *idx, long long *evals, void *ws,
                           size_t ws_bytes, cudaStream_t s) {
-  constexpr int D = TP::DIM;
+  const int D = p.dim();
   Carver c(ws);
   float *fx0 = c.take<float>((size_t)D * M);
   const RejWs w = carve_rej(c, M);
@@ -387,35 +392,38 @@ static bool rej_sizes_ok(int64_t T, int64_t N, int64_t M) {
          (uint64_t)M * (uint64_t)N < (1ull << 32);
 }
 
-template <int D>
+template <int D, bool RT = false>
 static int ffbsi_rej_lg(const mgb_lg_transition *tr, const RejCfg &cfg, int64_t T, int64_t N, int64_t M,
                         const float *x_hist, const float *lw_hist, const uint32_t *key, float *out, int32_t *idx,
                         long long *evals, void *ws, size_t ws_bytes, cudaStream_t s) {
-  return ffbsi_rej_run(pack_lgt<D>(tr), cfg, nullptr, T, N, M, x_hist, lw_hist, key, out, idx, evals, ws, ws_bytes,
+  return ffbsi_rej_run(pack_lgt<D, RT>(tr), cfg, nullptr, T, N, M, x_hist, lw_hist, key, out, idx, evals, ws, ws_bytes,
                        s);
 }
 
-template <int D>
+template <int D, bool RT = false>
 static int stitch_rej_lg(const mgb_lg_transition *tr, const RejCfg &cfg, int64_t M, const float *x0, const float *x1,
                          const float *lw1, const uint32_t *key, int32_t *idx, long long *evals, void *ws,
                          size_t ws_bytes, cudaStream_t s) {
-  return stitch_rej_run(pack_lgt<D>(tr), cfg, M, x0, x1, lw1, key, idx, evals, ws, ws_bytes, s);
+  return stitch_rej_run(pack_lgt<D, RT>(tr), cfg, M, x0, x1, lw1, key, idx, evals, ws, ws_bytes, s);
 }
 
 }  // namespace mgb
 
 using namespace mgb;
 
-#define MGB_RJ_DISPATCH(FN, ...)                 \
-  switch (tr->d) {                               \
-    case 1: return FN<1>(__VA_ARGS__);           \
-    case 2: return FN<2>(__VA_ARGS__);           \
-    case 3: return FN<3>(__VA_ARGS__);           \
-    case 4: return FN<4>(__VA_ARGS__);           \
-    case 5: return FN<5>(__VA_ARGS__);           \
-    case 8: return FN<8>(__VA_ARGS__);           \
-    case 10: return FN<10>(__VA_ARGS__);         \
-    default: return ERR_UNSUPPORTED;             \
+// compiled dimensions take their own instances; any other d up to 32 the run-time one
+#define MGB_RJ_DISPATCH(FN, ...)                                                    \
+  switch (tr->d) {                                                                  \
+    case 1: return FN<1>(__VA_ARGS__);                                              \
+    case 2: return FN<2>(__VA_ARGS__);                                              \
+    case 3: return FN<3>(__VA_ARGS__);                                              \
+    case 4: return FN<4>(__VA_ARGS__);                                              \
+    case 5: return FN<5>(__VA_ARGS__);                                              \
+    case 8: return FN<8>(__VA_ARGS__);                                              \
+    case 10: return FN<10>(__VA_ARGS__);                                            \
+    default:                                                                        \
+      if (tr->d >= 1 && tr->d <= LGT_DMAX) return FN<LGT_DMAX, true>(__VA_ARGS__);  \
+      return ERR_UNSUPPORTED;                                                       \
   }
 
 extern "C" {

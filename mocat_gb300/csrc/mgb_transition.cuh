@@ -17,44 +17,55 @@ namespace mgb {
 
 constexpr int FB_TPB = 256;
 
-// linear-Gaussian transition
-template <int D>
+// linear-Gaussian transition; RT: D is the capacity (32) and the dimension d_ is read from the
+// parameter block, F and Pq packed d_ x d_ row-major at the front of their arrays
+template <int D, bool RT = false>
 struct LGT {
   static constexpr int DIM = D;
   static constexpr bool kDrift = false;
+  static constexpr bool kRT = RT;
   float F[D * D], Pq[D * D];
   float cq;
   uint32_t one;
+  int d_;
+  __host__ __device__ __forceinline__ int dim() const { return RT ? d_ : D; }
   __device__ __forceinline__ void mean(const float (&x)[D], float (&m)[D], float) const {
+    const int d = dim();
 #pragma unroll
-    for (int r = 0; r < D; ++r) {
-      float v = __fmul_rn(F[r * D], x[0]);
+    for (int r = 0; r < d; ++r) {
+      float v = __fmul_rn(F[r * d], x[0]);
 #pragma unroll
-      for (int k = 1; k < D; ++k) v = __fmaf_rn(F[r * D + k], x[k], v);
+      for (int k = 1; k < d; ++k) v = __fmaf_rn(F[r * d + k], x[k], v);
       m[r] = v;
     }
   }
   __device__ __forceinline__ float potential(const float (&diff)[D]) const {
+    const int d = dim();
     float quad = 0.0f;
 #pragma unroll
-    for (int k = 0; k < D; ++k) {
+    for (int k = 0; k < d; ++k) {
       float v = __fmul_rn(diff[0], Pq[k]);
 #pragma unroll
-      for (int r = 1; r < D; ++r) v = __fmaf_rn(diff[r], Pq[r * D + k], v);
+      for (int r = 1; r < d; ++r) v = __fmaf_rn(diff[r], Pq[r * d + k], v);
       quad = k == 0 ? __fmul_rn(v, v) : __fmaf_rn(v, v, quad);
     }
     return __fadd_rn(__fmul_rn(0.5f, quad), cq);
   }
 };
 
+// the run-time-dimension capacity of the linear-Gaussian transition
+constexpr int LGT_DMAX = 32;
+
 // non-linear 1-D benchmark transition; t_previous from *tp (device) or tv
 struct NLT {
   static constexpr int DIM = 1;
   static constexpr bool kDrift = true;
+  static constexpr bool kRT = false;
   float tsd, c;
   const float *tp;
   float tv;
   uint32_t one;
+  __host__ __device__ __forceinline__ int dim() const { return 1; }
   __device__ __forceinline__ void mean(const float (&x)[1], float (&m)[1], float drift) const {
     m[0] = nl_mean(x[0], drift);
   }
@@ -69,8 +80,10 @@ struct NLT {
 struct SVT {
   static constexpr int DIM = 1;
   static constexpr bool kDrift = false;
+  static constexpr bool kRT = false;
   float phi, pqs;
   uint32_t one;
+  __host__ __device__ __forceinline__ int dim() const { return 1; }
   __device__ __forceinline__ void mean(const float (&x)[1], float (&m)[1], float) const {
     m[0] = __fmul_rn(x[0], phi);
   }
@@ -105,12 +118,13 @@ __device__ __forceinline__ float block_drift(const TP &p, float *sm) {
 template <class TP>
 __global__ void __launch_bounds__(FB_TPB) k_ffbsi_fx(const __grid_constant__ TP p, int64_t N,
                                                       const float *__restrict__ x, float *__restrict__ fx) {
-  constexpr int D = TP::DIM;
+  constexpr int DC = TP::DIM;
+  const int D = p.dim();
   __shared__ float sm[1];
   const float drift = block_drift(p, sm);
   const int64_t i = blockIdx.x * (int64_t)FB_TPB + threadIdx.x;
   if (i >= N) return;
-  float xv[D], m[D];
+  float xv[DC], m[DC];
 #pragma unroll
   for (int k = 0; k < D; ++k) xv[k] = x[k * N + i];
   p.mean(xv, m, drift);
@@ -173,10 +187,11 @@ static __global__ void __launch_bounds__(FB_TPB) k_ffbsi_last(int64_t N, int64_t
   if (threadIdx.x == 0) idx[j] = bi;
 }
 
-// xs_t[:, j] = x_t[:, idx_j]
-template <int D>
+// xs_t[:, j] = x_t[:, idx_j]; DC = 0: the dimension d is a run-time argument
+template <int DC>
 __global__ void k_ffbsi_take(int64_t N, int64_t M, const float *__restrict__ x, const int32_t *__restrict__ idx,
-                             float *__restrict__ out) {
+                             float *__restrict__ out, int d) {
+  const int D = DC ? DC : d;
   for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < M; j += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = idx[j];
 #pragma unroll
@@ -184,16 +199,24 @@ __global__ void k_ffbsi_take(int64_t N, int64_t M, const float *__restrict__ x, 
   }
 }
 
-template <int D>
-LGT<D> pack_lgt(const mgb_lg_transition *tr) {
-  LGT<D> p;
-  for (int i = 0; i < D * D; ++i) {
+template <int D, bool RT = false>
+LGT<D, RT> pack_lgt(const mgb_lg_transition *tr) {
+  LGT<D, RT> p{};
+  const int d = RT ? tr->d : D;
+  for (int i = 0; i < d * d; ++i) {
     p.F[i] = tr->F[i];
     p.Pq[i] = tr->Pq[i];
   }
   p.cq = tr->cq;
   p.one = 1u;
+  p.d_ = d;
   return p;
+}
+
+// the take kernel's compile-time dimension for policy TP (0: run-time)
+template <class TP>
+constexpr int take_dim() {
+  return TP::kRT ? 0 : TP::DIM;
 }
 
 inline NLT pack_nlt(const mgb_nl1d_model *m, const float *tp, float tv) {

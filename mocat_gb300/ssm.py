@@ -125,11 +125,12 @@ class TimeHomogenousLinearGaussian(StateSpaceModel):
         return x_previous @ torch.as_tensor(np.asarray(self.transition_matrix, np.float32), device=x_previous.device).T
 
     def gpu_supported(self):
-        """(d, dy) has compiled kernels for every path (filters, Kalman, smoothers, gradients)"""
+        """(d, dy) has compiled kernels for every path, the optimal proposal and the gradients included"""
         return (self.dim, self.dim_obs) in LG_SUPPORTED
 
     def gpu_bootstrap_supported(self):
-        """the bootstrap filter and the Kalman filter / smoothers run on the GPU: compiled
+        """the bootstrap filter, the Kalman filter / smoothers and the particle smoothers
+        (backward simulation, stitching, rejection sampling) run on the GPU: compiled
         kernels, or the run-time-dimension kernels (the same operations; one launch per
         phase for the particle filter) for d, dy <= 32"""
         return self.gpu_supported() or (self.dim <= LG_RUNTIME_MAX and self.dim_obs <= LG_RUNTIME_MAX)
@@ -1028,8 +1029,8 @@ def backward_simulation(ssm_scenario, marginal_particles, random_key, n_samps=No
         raise NotImplementedError(f"{ssm_scenario.__class__.__name__}: no backward-simulation kernel for this model")
     if sv and ssm_scenario.dim != 1:
         raise NotImplementedError("StochasticVolatility: the GPU kernels take dim = 1")
-    if not sv and not ssm_scenario.gpu_supported():
-        raise NotImplementedError(f"d = {ssm_scenario.dim} not compiled")
+    if not nl and not sv and not ssm_scenario.gpu_bootstrap_supported():
+        raise NotImplementedError(f"d = {ssm_scenario.dim} above the run-time-dimension limit ({LG_RUNTIME_MAX})")
     value = marginal_particles.value
     T, n, d = value.shape
     M = n if n_samps is None else int(n_samps)
@@ -1199,8 +1200,9 @@ def _check_smoother(ssm_scenario, particle_filter):
     _check_lg(ssm_scenario, particle_filter)
     if isinstance(ssm_scenario, StochasticVolatility) and ssm_scenario.dim != 1:
         raise NotImplementedError("StochasticVolatility: the smoothing kernels take dim = 1")
-    if isinstance(ssm_scenario, TimeHomogenousLinearGaussian) and not ssm_scenario.gpu_supported():
-        raise NotImplementedError(f"(d, dy) = ({ssm_scenario.dim}, {ssm_scenario.dim_obs}) not compiled")
+    if isinstance(ssm_scenario, TimeHomogenousLinearGaussian) and not ssm_scenario.gpu_bootstrap_supported():
+        raise NotImplementedError(f"(d, dy) = ({ssm_scenario.dim}, {ssm_scenario.dim_obs}) above the "
+                                  f"run-time-dimension limit ({LG_RUNTIME_MAX})")
     if not isinstance(particle_filter, BootstrapFilter):
         raise NotImplementedError("the online smoother runs the bootstrap filter")
 

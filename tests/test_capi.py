@@ -75,6 +75,16 @@ def test_unsupported_dimension_rejected_on_host(L):
     assert L.mgb_pf_lg_propagate(ctypes.byref(m), 1000, p, p, p, None, None, p, p, None) == 2
     m1 = _lib.LGModel(5, 33, *[a.ctypes.data for a in arrs], 1.0)  # dy above the limit
     assert L.mgb_pf_lg_init(ctypes.byref(m1), 1000, p, p, p, p, None) == 2
+    # the particle smoothers: the same limit on the transition's d
+    tr = _lib.LGTransition(d, arrs[0].ctypes.data, arrs[1].ctypes.data, 0.0)
+    assert L.mgb_ffbsi_lg(ctypes.byref(tr), 4, 64, 16, p, p, p, p, p, p, 1 << 30, None) == 2
+    assert L.mgb_stitch_lg(ctypes.byref(tr), 16, 64, p, p, p, p, p, None) == 2
+    assert L.mgb_transition_potential_pairs(ctypes.byref(tr), 16, p, p, None, p, None) == 2
+    cfg = _lib.RejectionConfig(5, 0.0, 1.01)
+    assert L.mgb_ffbsi_rejection_lg(ctypes.byref(tr), ctypes.byref(cfg), 4, 64, 16, p, p, p, p, p, p, p, 1 << 30,
+                                    None) == 2
+    assert L.mgb_stitch_rejection_lg(ctypes.byref(tr), ctypes.byref(cfg), 16, p, p, p, p, p, p, p, 1 << 30,
+                                     None) == 2
 
 
 def test_new_entry_points_reject_bad_arguments_on_host(L):

@@ -23,7 +23,8 @@ def _lg(d, seed=0):
     return p, ssm, F, Q
 
 
-@pytest.mark.parametrize("d,n,M,T", [(1, 300, 200, 12), (3, 257, 64, 10), (10, 512, 33, 6)])
+@pytest.mark.parametrize("d,n,M,T", [(1, 300, 200, 12), (3, 257, 64, 10), (10, 512, 33, 6),
+                                     (7, 300, 40, 6), (16, 200, 17, 4)])  # 7, 16: run-time dimension
 def test_backward_simulation_matches_oracle(cuda, d, n, M, T):
     import mocat_gb300 as mg
     p, ssm, F, Q = _lg(d, seed=d)

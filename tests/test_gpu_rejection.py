@@ -26,7 +26,8 @@ def _lg(d, seed=0):
     return p, ssm
 
 
-@pytest.mark.parametrize("d,n,M,T", [(1, 300, 200, 8), (3, 257, 64, 6), (10, 512, 33, 5)])
+@pytest.mark.parametrize("d,n,M,T", [(1, 300, 200, 8), (3, 257, 64, 6), (10, 512, 33, 5),
+                                     (6, 257, 40, 5)])  # 6: run-time dimension
 @pytest.mark.parametrize("max_rej,ibp,infl", [(2, 0.0, 1.01), (10, 0.0, 1.01), (25, 0.02, 1.3)])
 def test_backward_simulation_rejection_matches_oracle(cuda, d, n, M, T, max_rej, ibp, infl):
     import mocat_gb300 as mg
@@ -45,7 +46,7 @@ def test_backward_simulation_rejection_matches_oracle(cuda, d, n, M, T, max_rej,
     assert rev[0] == 0 and (rev[1:] >= M).all()
 
 
-@pytest.mark.parametrize("d,M", [(1, 1000), (2, 777), (5, 256)])
+@pytest.mark.parametrize("d,M", [(1, 1000), (2, 777), (5, 256), (7, 300)])  # 7: run-time dimension
 @pytest.mark.parametrize("max_rej", [1, 3, 40])
 def test_stitch_rejection_matches_oracle(cuda, d, M, max_rej):
     import mocat_gb300 as mg

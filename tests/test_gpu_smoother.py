@@ -25,7 +25,8 @@ def _lg(d, seed=0):
     return p, ssm
 
 
-@pytest.mark.parametrize("d,M0,M1", [(1, 100, 300), (3, 65, 257), (10, 40, 128)])
+@pytest.mark.parametrize("d,M0,M1", [(1, 100, 300), (3, 65, 257), (10, 40, 128),
+                                     (12, 50, 129), (32, 20, 70)])  # 12, 32: run-time dimension
 def test_stitch_and_pair_potential_bit_exact(cuda, d, M0, M1):
     import mocat_gb300 as mg
     _, ssm = _lg(d, d)
@@ -66,7 +67,7 @@ def _oracle_smoother_pf(p, keep, x0, lw0, y, keys, lag):
     return np.stack(value)
 
 
-@pytest.mark.parametrize("d,n", [(1, 400), (3, 256)])
+@pytest.mark.parametrize("d,n", [(1, 400), (3, 256), (6, 256)])  # 6: run-time dimension
 def test_smoother_pf_variant_matches_oracle(cuda, d, n):
     import mocat_gb300 as mg
     p, ssm = _lg(d, 10 + d)
