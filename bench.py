@@ -833,6 +833,12 @@ def profile_other(args):
         t = min(ts)
         out.update(precision=args.profile_precision, n_data=n_data, d=d, ms=t * 1e3,
                    tflops_alg=4.0 * n_data * d * n / t / 1e12)
+        if args.profile_precision == "bf16":
+            # accuracy against the fp32 CUDA-core kernel on the first 4096 rows
+            l16, g16 = (v.double() for v in sc.likelihood_potential_and_grad(beta[:4096], precision="bf16"))
+            l32, g32 = (v.double() for v in sc.likelihood_potential_and_grad(beta[:4096], precision="fp32"))
+            out["potential_max_rel_err"] = float(((l16 - l32).abs() / l32.abs()).max())
+            out["grad_median_rel_err"] = float(((g16 - g32).norm(dim=1) / g32.norm(dim=1)).median())
     else:
         ns, y, Tb, keys = mg.batched.synthetic_sv_batch(n, seed=0, t_range=(50, T))
         sc = mg.ssm.StochasticVolatility(dim=1, initial_covariance=0.3 ** 2 / (1 - 0.95 ** 2),

@@ -12,9 +12,13 @@ constexpr int PP_MAX_TILES = 1024;  // n <= 2^21 on this path
 constexpr int BAR_SPIN_LIMIT = 1 << 22;  // polls of an L2 word (>= ~0.5 us each under load): seconds
 constexpr int PP_MAX_CHUNKS = 4096;  // 256-pair chunks per step (n <= 2^21)
 
+// arrival counter and generation on separate 128-byte lines: the waiters' polling loads
+// of gen do not queue behind the arrivals' atomics on count
 struct GridBar {
   unsigned int count;
+  unsigned int pad0[31];
   unsigned int gen;
+  unsigned int pad1[31];
 };
 
 struct PersistArgs {

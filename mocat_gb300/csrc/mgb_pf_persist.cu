@@ -70,7 +70,8 @@ __device__ __forceinline__ bool grid_sync(GridBar *bar, unsigned nblocks, int *e
         unsigned int cur;
         asm volatile("ld.acquire.gpu.u32 %0, [%1];" : "=r"(cur) : "l"(&bar->gen) : "memory");
         if (cur != g) break;
-        if (*(volatile int *)err & EB_TIMEOUT) {
+        // another block's timeout (checked every 64 polls: one load per poll on the barrier's line)
+        if ((polls & 63) == 63 && (*(volatile int *)err & EB_TIMEOUT)) {
           out = 1;
           break;
         }
@@ -584,7 +585,7 @@ int run_sv_persistent(const mgb_sv_model *m, const PersistArgs &a, cudaStream_t 
 
 using namespace mgb;
 
-extern "C" size_t mgb_wait_selftest_workspace(void) { return 256; }
+extern "C" size_t mgb_wait_selftest_workspace(void) { return 512; }
 
 extern "C" int mgb_wait_selftest(int which, int32_t polls, void *ws, size_t ws_bytes, void *stream) {
   if ((which != MGB_WAIT_GRID_BARRIER && which != MGB_WAIT_LOOKBACK) || polls < 1 || polls > BAR_SPIN_LIMIT || !ws ||
@@ -592,10 +593,11 @@ extern "C" int mgb_wait_selftest(int which, int32_t polls, void *ws, size_t ws_b
     return ERR_BAD_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   char *base = (char *)ws;
-  int *err = (int *)base;                       // [0, 4)
-  GridBar *bar = (GridBar *)(base + 16);        // [16, 24)
-  uint64_t *status = (uint64_t *)(base + 32);   // [32, 48): tiles 0 and 1
-  if (cudaMemsetAsync(ws, 0, 64, s) != cudaSuccess) return ERR_CUDA;
+  int *err = (int *)base;                        // [0, 4)
+  GridBar *bar = (GridBar *)(base + 128);        // [128, 384)
+  uint64_t *status = (uint64_t *)(base + 384);   // [384, 400): tiles 0 and 1
+  static_assert(128 + sizeof(GridBar) <= 384, "selftest layout");
+  if (cudaMemsetAsync(ws, 0, 512, s) != cudaSuccess) return ERR_CUDA;
   if (which == MGB_WAIT_GRID_BARRIER)
     k_wait_selftest_barrier<<<4, 32, 0, s>>>(bar, err, polls);
   else
