@@ -299,7 +299,8 @@ int mgb_ffbsi_lg(const mgb_lg_transition *transition_host, int64_t T, int64_t N,
  *   W (dy x dy) weight_precision_sqrt; cw = (dy log 2 pi - log weight_precision_det) / 2;
  *   K0 (d x dy) initial_kalman_gain; C0c (d x d) initial_conditioned_covariance_sqrt;
  *   m0 (d) initial_mean.
- * Supported (d, dy) as for mgb_lg_model; n d < 2^32.
+ * Supported (d, dy): the compiled pairs of mgb_lg_model, and any other pair with d, dy <= 32
+ * on the run-time-dimension instance (the same operations in the same order); n d < 2^32.
  */
 typedef struct {
   int32_t d, dy;

@@ -25,16 +25,26 @@
 
 namespace mgb {
 
-template <int D, int DY>
+// CD, CDY: the arrays' capacities.  A compiled pair has RT = false and the dimensions are the
+// template constants; RT = true reads them from rd, rdy (the run-time-dimension instance, d and
+// dy up to 32), with every matrix packed at its run-time strides at the front of its array.
+template <int CD, int CDY, bool RT = false>
 struct OPTP {
-  float F[D * D], H[DY * D], K[D * DY], S[D * D], W[DY * DY], K0[D * DY], C0c[D * D], m0[D];
+  float F[CD * CD], H[CDY * CD], K[CD * CDY], S[CD * CD], W[CDY * CDY], K0[CD * CDY], C0c[CD * CD], m0[CD];
   float cw;
   uint32_t one;  // == 1, multiplier of the cipher's multiply-adds
+  int rd, rdy;
+  __host__ __device__ __forceinline__ int d() const { return RT ? rd : CD; }
+  __host__ __device__ __forceinline__ int dy() const { return RT ? rdy : CDY; }
 };
 
-template <int D, int DY>
-OPTP<D, DY> pack_opt(const mgb_opt_model *m) {
-  OPTP<D, DY> p;
+// the run-time-dimension capacity
+constexpr int OPT_DMAX = 32;
+
+template <int CD, int CDY, bool RT>
+OPTP<CD, CDY, RT> pack_opt(const mgb_opt_model *m) {
+  OPTP<CD, CDY, RT> p{};
+  const int D = RT ? m->d : CD, DY = RT ? m->dy : CDY;
   for (int i = 0; i < D * D; ++i) {
     p.F[i] = m->F[i];
     p.S[i] = m->S[i];
@@ -49,13 +59,15 @@ OPTP<D, DY> pack_opt(const mgb_opt_model *m) {
   for (int i = 0; i < D; ++i) p.m0[i] = m->m0[i];
   p.cw = m->cw;
   p.one = 1u;
+  p.rd = D;
+  p.rdy = DY;
   return p;
 }
 
 // eps of particles i and i + n/2 (n even): one cipher call per component
-template <int D>
-__device__ __forceinline__ void pair_noise(uint32_t k0, uint32_t k1, int64_t i, int64_t h, uint32_t one,
-                                           float (&ea)[D], float (&eb)[D]) {
+template <int CD>
+__device__ __forceinline__ void pair_noise(uint32_t k0, uint32_t k1, int64_t i, int64_t h, uint32_t one, int D,
+                                           float (&ea)[CD], float (&eb)[CD]) {
   const uint64_t hN = (uint64_t)h * D;
 #pragma unroll
   for (int j = 0; j < D; ++j) {
@@ -68,8 +80,8 @@ __device__ __forceinline__ void pair_noise(uint32_t k0, uint32_t k1, int64_t i, 
 }
 
 // eps of particle i for any n: element-wise counter layout
-template <int D>
-__device__ __forceinline__ void single_noise(uint32_t k0, uint32_t k1, int64_t n, int64_t i, float (&e)[D]) {
+template <int CD>
+__device__ __forceinline__ void single_noise(uint32_t k0, uint32_t k1, int64_t n, int64_t i, int D, float (&e)[CD]) {
 #pragma unroll
   for (int j = 0; j < D; ++j) e[j] = bits_to_normal(bits_at(k0, k1, (uint64_t)n * D, (uint64_t)i * D + j));
 }
@@ -86,9 +98,10 @@ __device__ __forceinline__ void block_noise_key(const uint32_t *key, int64_t n, 
 }
 
 // x_0 = mean0 + eps C0c (column sums in ascending order), mean0 = m0 + K0 (y0 - H m0)
-template <int D, int DY>
-__device__ __forceinline__ void opt_init_particle(const OPTP<D, DY> &p, const float *mean0, const float (&e)[D],
-                                                  int64_t n, int64_t i, float *x) {
+template <int CD, int CDY, bool RT>
+__device__ __forceinline__ void opt_init_particle(const OPTP<CD, CDY, RT> &p, const float *mean0,
+                                                  const float (&e)[CD], int64_t n, int64_t i, float *x) {
+  const int D = p.d();
 #pragma unroll
   for (int r = 0; r < D; ++r) {
     float v = __fmul_rn(e[0], p.C0c[r]);
@@ -99,10 +112,11 @@ __device__ __forceinline__ void opt_init_particle(const OPTP<D, DY> &p, const fl
 }
 
 // mean0 into shared memory (thread 0; the caller synchronises)
-template <int D, int DY>
-__device__ __forceinline__ void opt_mean0(const OPTP<D, DY> &p, const float *y0, float *mean0) {
+template <int CD, int CDY, bool RT>
+__device__ __forceinline__ void opt_mean0(const OPTP<CD, CDY, RT> &p, const float *y0, float *mean0) {
+  const int D = p.d(), DY = p.dy();
   if (threadIdx.x == 0) {
-    float innov[DY];
+    float innov[CDY];
 #pragma unroll
     for (int j = 0; j < DY; ++j) {
       float hm = __fmul_rn(p.H[j * D], p.m0[0]);
@@ -120,13 +134,14 @@ __device__ __forceinline__ void opt_mean0(const OPTP<D, DY> &p, const float *y0,
   }
 }
 
-template <int D, int DY, bool FUSED>
-__global__ void __launch_bounds__(PF_TPB) k_opt_init(const __grid_constant__ OPTP<D, DY> p, int64_t n,
+template <int CD, int CDY, bool RT, bool FUSED>
+__global__ void __launch_bounds__(PF_TPB) k_opt_init(const __grid_constant__ OPTP<CD, CDY, RT> p, int64_t n,
                                                       const uint32_t *key, const float *y0, float *__restrict__ x,
                                                       float *__restrict__ lw, PFCtl ctl) {
+  const int D = p.d();
   __shared__ uint32_t ks[2];
-  __shared__ float mean0[D];
-  opt_mean0<D, DY>(p, y0, mean0);
+  __shared__ float mean0[CD];
+  opt_mean0(p, y0, mean0);
   block_noise_key(key, n, ks);
   const uint32_t k0 = ks[0], k1 = ks[1];
   float m = -INFINITY, a1 = 0.0f, a2 = 0.0f;
@@ -135,10 +150,10 @@ __global__ void __launch_bounds__(PF_TPB) k_opt_init(const __grid_constant__ OPT
     const int64_t h = n >> 1;
     const int64_t i = blockIdx.x * (int64_t)PF_TPB + threadIdx.x;
     if (i < h) {
-      float ea[D], eb[D];
-      pair_noise<D>(k0, k1, i, h, p.one, ea, eb);
-      opt_init_particle<D, DY>(p, mean0, ea, n, i, x);
-      opt_init_particle<D, DY>(p, mean0, eb, n, i + h, x);
+      float ea[CD], eb[CD];
+      pair_noise<CD>(k0, k1, i, h, p.one, D, ea, eb);
+      opt_init_particle(p, mean0, ea, n, i, x);
+      opt_init_particle(p, mean0, eb, n, i + h, x);
       lw[i] = 0.0f;
       lw[i + h] = 0.0f;
       online_acc(0.0f, m, a1, a2, nanf);
@@ -147,9 +162,9 @@ __global__ void __launch_bounds__(PF_TPB) k_opt_init(const __grid_constant__ OPT
   } else {
     const int64_t i = blockIdx.x * (int64_t)PF_TPB + threadIdx.x;
     if (i < n) {
-      float e[D];
-      single_noise<D>(k0, k1, n, i, e);
-      opt_init_particle<D, DY>(p, mean0, e, n, i, x);
+      float e[CD];
+      single_noise<CD>(k0, k1, n, i, D, e);
+      opt_init_particle(p, mean0, e, n, i, x);
       lw[i] = 0.0f;
       online_acc(0.0f, m, a1, a2, nanf);
     }
@@ -158,13 +173,14 @@ __global__ void __launch_bounds__(PF_TPB) k_opt_init(const __grid_constant__ OPT
 }
 
 // one particle of the fused step (nonlinear_gaussian.py:264-281), oracle op order
-template <int D, int DY>
-__device__ __forceinline__ float opt_particle(const OPTP<D, DY> &p, int64_t n, int64_t i, const float (&e)[D],
+template <int CD, int CDY, bool RT>
+__device__ __forceinline__ float opt_particle(const OPTP<CD, CDY, RT> &p, int64_t n, int64_t i, const float (&e)[CD],
                                               bool res, const float *__restrict__ x_prev, const int32_t *anc,
                                               const float *lws, const float *y, float *__restrict__ x_new,
                                               float *__restrict__ lw_new) {
+  const int D = p.d(), DY = p.dy();
   const int64_t src = res ? (int64_t)anc[i] : i;
-  float xs[D], mx[D], innov[DY];
+  float xs[CD], mx[CD], innov[CDY];
 #pragma unroll
   for (int j = 0; j < D; ++j) xs[j] = __ldg(&x_prev[j * n + src]);
 #pragma unroll
@@ -206,15 +222,16 @@ __device__ __forceinline__ float opt_particle(const OPTP<D, DY> &p, int64_t n, i
 }
 
 // one step; res_flag (nullable) decides resampled vs identity at run time
-template <int D, int DY, bool FUSED>
-__global__ void __launch_bounds__(PF_TPB) k_opt_step(const __grid_constant__ OPTP<D, DY> p, int64_t n,
+template <int CD, int CDY, bool RT, bool FUSED>
+__global__ void __launch_bounds__(PF_TPB) k_opt_step(const __grid_constant__ OPTP<CD, CDY, RT> p, int64_t n,
                                                       const uint32_t *key, const float *y_t,
                                                       const float *__restrict__ x_prev, const int32_t *anc,
                                                       const float *lw_prev, const int32_t *res_flag,
                                                       float *__restrict__ x_new, float *__restrict__ lw_new,
                                                       PFCtl ctl, int64_t t) {
+  const int D = p.d(), DY = p.dy();
   __shared__ uint32_t ks[2];
-  __shared__ float y[DY];
+  __shared__ float y[CDY];
   if (threadIdx.x < DY) y[threadIdx.x] = y_t[threadIdx.x];
   block_noise_key(key, n, ks);
   const uint32_t k0 = ks[0], k1 = ks[1];
@@ -227,15 +244,15 @@ __global__ void __launch_bounds__(PF_TPB) k_opt_step(const __grid_constant__ OPT
   if (n % 2 == 0) {
     const int64_t h = n >> 1;
     if (i < h) {
-      float ea[D], eb[D];
-      pair_noise<D>(k0, k1, i, h, p.one, ea, eb);
-      online_acc(opt_particle<D, DY>(p, n, i, ea, res, x_prev, anc, lws, y, x_new, lw_new), m, a1, a2, nanf);
-      online_acc(opt_particle<D, DY>(p, n, i + h, eb, res, x_prev, anc, lws, y, x_new, lw_new), m, a1, a2, nanf);
+      float ea[CD], eb[CD];
+      pair_noise<CD>(k0, k1, i, h, p.one, D, ea, eb);
+      online_acc(opt_particle(p, n, i, ea, res, x_prev, anc, lws, y, x_new, lw_new), m, a1, a2, nanf);
+      online_acc(opt_particle(p, n, i + h, eb, res, x_prev, anc, lws, y, x_new, lw_new), m, a1, a2, nanf);
     }
   } else if (i < n) {
-    float e[D];
-    single_noise<D>(k0, k1, n, i, e);
-    online_acc(opt_particle<D, DY>(p, n, i, e, res, x_prev, anc, lws, y, x_new, lw_new), m, a1, a2, nanf);
+    float e[CD];
+    single_noise<CD>(k0, k1, n, i, D, e);
+    online_acc(opt_particle(p, n, i, e, res, x_prev, anc, lws, y, x_new, lw_new), m, a1, a2, nanf);
   }
   if (FUSED) pf_reduce_online<PF_TPB>(m, a1, a2, nanf, ctl, t);
 }
@@ -245,10 +262,11 @@ inline unsigned opt_grid(int64_t n) {
   return (unsigned)((work + PF_TPB - 1) / PF_TPB);
 }
 
-template <int D, int DY>
+template <int CD, int CDY, bool RT = false>
 static int run_opt(const mgb_opt_model *m, int64_t n, int64_t T, const uint32_t *key, const float *y, float thr,
                    int scheme, void *ws, size_t ws_bytes, const mgb_pf_outputs *out, cudaStream_t s) {
-  const OPTP<D, DY> p = pack_opt<D, DY>(m);
+  const OPTP<CD, CDY, RT> p = pack_opt<CD, CDY, RT>(m);
+  const int D = p.d(), DY = p.dy();
   const bool hx = out && out->x_hist, hl = out && out->lw_hist;
   Carver c(ws);
   RunWs w = carve_run(c, n, T, D, scheme, !hx, !hl, !(out && out->ess));
@@ -277,14 +295,15 @@ static int run_opt(const mgb_opt_model *m, int64_t n, int64_t T, const uint32_t 
   auto xbuf = [&](int64_t t) -> float * { return hx ? out->x_hist + (size_t)t * D * n : (t & 1 ? w.xb : w.xa); };
   auto lbuf = [&](int64_t t) -> float * { return hl ? out->lw_hist + (size_t)t * n : (t & 1 ? w.lb : w.la); };
   const unsigned grid = opt_grid(n);
-  k_opt_init<D, DY, true><<<grid, PF_TPB, 0, s>>>(p, n, w.keys, y, xbuf(0), lbuf(0), ctl);
+  k_opt_init<CD, CDY, RT, true><<<grid, PF_TPB, 0, s>>>(p, n, w.keys, y, xbuf(0), lbuf(0), ctl);
   if ((st = launch_status())) return st;
   for (int64_t t = 1; t < T; ++t) {
     st = launch_resample(lbuf(t - 1), n, scheme, &w.st->M, w.keys + 2 * t, 0, 0u, w.res_hist + t, w.rws, w.anc,
                          err, s);
     if (st) return st;
-    k_opt_step<D, DY, true><<<grid, PF_TPB, 0, s>>>(p, n, w.keys + 2 * t, y + (size_t)t * DY, xbuf(t - 1), w.anc,
-                                                     lbuf(t - 1), w.res_hist + t, xbuf(t), lbuf(t), ctl, t);
+    k_opt_step<CD, CDY, RT, true><<<grid, PF_TPB, 0, s>>>(p, n, w.keys + 2 * t, y + (size_t)t * DY, xbuf(t - 1),
+                                                           w.anc, lbuf(t - 1), w.res_hist + t, xbuf(t), lbuf(t), ctl,
+                                                           t);
     if ((st = launch_status())) return st;
   }
   if ((st = launch_finish(w.st, w.res_hist, T, out ? out->log_z : nullptr, out ? out->resampled : nullptr, s)))
@@ -298,21 +317,22 @@ static int run_opt(const mgb_opt_model *m, int64_t n, int64_t T, const uint32_t 
   return launch_status();
 }
 
-template <int D, int DY>
+template <int CD, int CDY, bool RT = false>
 static int init_opt(const mgb_opt_model *m, int64_t n, const uint32_t *key, const float *y0, float *x, float *lw,
                     cudaStream_t s) {
-  const OPTP<D, DY> p = pack_opt<D, DY>(m);
+  const OPTP<CD, CDY, RT> p = pack_opt<CD, CDY, RT>(m);
   PFCtl ctl{};
-  k_opt_init<D, DY, false><<<opt_grid(n), PF_TPB, 0, s>>>(p, n, key, y0, x, lw, ctl);
+  k_opt_init<CD, CDY, RT, false><<<opt_grid(n), PF_TPB, 0, s>>>(p, n, key, y0, x, lw, ctl);
   return launch_status();
 }
 
-template <int D, int DY>
+template <int CD, int CDY, bool RT = false>
 static int step_opt(const mgb_opt_model *m, int64_t n, const uint32_t *key, const float *y, const float *xp,
                     const int32_t *anc, const float *lwp, float *xn, float *lwn, cudaStream_t s) {
-  const OPTP<D, DY> p = pack_opt<D, DY>(m);
+  const OPTP<CD, CDY, RT> p = pack_opt<CD, CDY, RT>(m);
   PFCtl ctl{};
-  k_opt_step<D, DY, false><<<opt_grid(n), PF_TPB, 0, s>>>(p, n, key, y, xp, anc, lwp, nullptr, xn, lwn, ctl, 0);
+  k_opt_step<CD, CDY, RT, false><<<opt_grid(n), PF_TPB, 0, s>>>(p, n, key, y, xp, anc, lwp, nullptr, xn, lwn, ctl,
+                                                                0);
   return launch_status();
 }
 
@@ -325,32 +345,34 @@ static bool opt_size_ok(const mgb_opt_model *m, int64_t n) {
   return n >= 1 && n <= 0x7FFFFFFFll && (uint64_t)n * (uint64_t)m->d < (1ull << 32);
 }
 
-#define MGB_OPT_DISPATCH(FN, ...)                   \
-  do {                                              \
-    const int d_ = m->d, dy_ = m->dy;               \
-    if (dy_ == 1) {                                 \
-      switch (d_) {                                 \
-        case 1: return FN<1, 1>(__VA_ARGS__);       \
-        case 2: return FN<2, 1>(__VA_ARGS__);       \
-        case 3: return FN<3, 1>(__VA_ARGS__);       \
-        case 4: return FN<4, 1>(__VA_ARGS__);       \
-        case 5: return FN<5, 1>(__VA_ARGS__);       \
-        case 8: return FN<8, 1>(__VA_ARGS__);       \
-        case 10: return FN<10, 1>(__VA_ARGS__);     \
-        default: return ERR_UNSUPPORTED;            \
-      }                                             \
-    } else if (dy_ == d_) {                         \
-      switch (d_) {                                 \
-        case 2: return FN<2, 2>(__VA_ARGS__);       \
-        case 3: return FN<3, 3>(__VA_ARGS__);       \
-        case 4: return FN<4, 4>(__VA_ARGS__);       \
-        case 5: return FN<5, 5>(__VA_ARGS__);       \
-        case 8: return FN<8, 8>(__VA_ARGS__);       \
-        case 10: return FN<10, 10>(__VA_ARGS__);    \
-        default: return ERR_UNSUPPORTED;            \
-      }                                             \
-    }                                               \
-    return ERR_UNSUPPORTED;                         \
+// compiled pairs take their own instances; any other (d, dy) up to 32 the run-time one
+#define MGB_OPT_DISPATCH(FN, ...)                                                      \
+  do {                                                                                 \
+    const int d_ = m->d, dy_ = m->dy;                                                  \
+    if (dy_ == 1) {                                                                    \
+      switch (d_) {                                                                    \
+        case 1: return FN<1, 1>(__VA_ARGS__);                                          \
+        case 2: return FN<2, 1>(__VA_ARGS__);                                          \
+        case 3: return FN<3, 1>(__VA_ARGS__);                                          \
+        case 4: return FN<4, 1>(__VA_ARGS__);                                          \
+        case 5: return FN<5, 1>(__VA_ARGS__);                                          \
+        case 8: return FN<8, 1>(__VA_ARGS__);                                          \
+        case 10: return FN<10, 1>(__VA_ARGS__);                                        \
+        default: break;                                                                \
+      }                                                                                \
+    } else if (dy_ == d_) {                                                            \
+      switch (d_) {                                                                    \
+        case 2: return FN<2, 2>(__VA_ARGS__);                                          \
+        case 3: return FN<3, 3>(__VA_ARGS__);                                          \
+        case 4: return FN<4, 4>(__VA_ARGS__);                                          \
+        case 5: return FN<5, 5>(__VA_ARGS__);                                          \
+        case 8: return FN<8, 8>(__VA_ARGS__);                                          \
+        case 10: return FN<10, 10>(__VA_ARGS__);                                       \
+        default: break;                                                                \
+      }                                                                                \
+    }                                                                                  \
+    if (d_ <= OPT_DMAX && dy_ <= OPT_DMAX) return FN<OPT_DMAX, OPT_DMAX, true>(__VA_ARGS__); \
+    return ERR_UNSUPPORTED;                                                            \
   } while (0)
 
 }  // namespace mgb

@@ -125,14 +125,15 @@ class TimeHomogenousLinearGaussian(StateSpaceModel):
         return x_previous @ torch.as_tensor(np.asarray(self.transition_matrix, np.float32), device=x_previous.device).T
 
     def gpu_supported(self):
-        """(d, dy) has compiled kernels for every path, the optimal proposal and the gradients included"""
+        """(d, dy) has compiled kernels for every path, the gradients included"""
         return (self.dim, self.dim_obs) in LG_SUPPORTED
 
-    def gpu_bootstrap_supported(self):
-        """the bootstrap filter, the Kalman filter / smoothers and the particle smoothers
-        (backward simulation, stitching, rejection sampling) run on the GPU: compiled
-        kernels, or the run-time-dimension kernels (the same operations; one launch per
-        phase for the particle filter) for d, dy <= 32"""
+    def gpu_runtime_supported(self):
+        """the bootstrap and optimal-proposal filters, the Kalman filter / smoothers and the
+        particle smoothers (backward simulation, stitching, rejection sampling) run on the
+        GPU: compiled kernels, or the run-time-dimension kernels (the same operations; one
+        launch per phase for the bootstrap filter) for d, dy <= 32.  The gradients need a
+        compiled pair (gpu_supported)."""
         return self.gpu_supported() or (self.dim <= LG_RUNTIME_MAX and self.dim_obs <= LG_RUNTIME_MAX)
 
     def simulate(self, t_all, random_key):
@@ -577,9 +578,9 @@ def _check_lg(ssm_scenario, particle_filter):
         raise NotImplementedError(f"{ssm_scenario.__class__.__name__}: no fused GPU kernel for this model")
     if not isinstance(particle_filter, (BootstrapFilter, OptimalNonLinearGaussianParticleFilter)):
         raise NotImplementedError(f"{particle_filter.__class__.__name__}: no fused GPU kernel for this filter")
-    boot = not isinstance(particle_filter, OptimalNonLinearGaussianParticleFilter)
-    if not (ssm_scenario.gpu_bootstrap_supported() if boot else ssm_scenario.gpu_supported()):
-        raise NotImplementedError(f"(d, dy) = ({ssm_scenario.dim}, {ssm_scenario.dim_obs}) not compiled")
+    if not ssm_scenario.gpu_runtime_supported():
+        raise NotImplementedError(f"(d, dy) = ({ssm_scenario.dim}, {ssm_scenario.dim_obs}) above the "
+                                  f"run-time-dimension limit ({LG_RUNTIME_MAX})")
 
 
 def _kernels(ssm_scenario, particle_filter):
@@ -927,7 +928,7 @@ def _check_kalman(ssm_scenario):
     if not isinstance(ssm_scenario, TimeHomogenousLinearGaussian):
         raise NotImplementedError(f"{ssm_scenario.__class__.__name__}: the Kalman filter takes a linear-Gaussian model")
     # compiled pairs, or the run-time-dimension instance for d, dy <= 32
-    if not ssm_scenario.gpu_bootstrap_supported():
+    if not ssm_scenario.gpu_runtime_supported():
         raise NotImplementedError(f"(d, dy) = ({ssm_scenario.dim}, {ssm_scenario.dim_obs}) not compiled")
 
 
@@ -1029,7 +1030,7 @@ def backward_simulation(ssm_scenario, marginal_particles, random_key, n_samps=No
         raise NotImplementedError(f"{ssm_scenario.__class__.__name__}: no backward-simulation kernel for this model")
     if sv and ssm_scenario.dim != 1:
         raise NotImplementedError("StochasticVolatility: the GPU kernels take dim = 1")
-    if not nl and not sv and not ssm_scenario.gpu_bootstrap_supported():
+    if not nl and not sv and not ssm_scenario.gpu_runtime_supported():
         raise NotImplementedError(f"d = {ssm_scenario.dim} above the run-time-dimension limit ({LG_RUNTIME_MAX})")
     value = marginal_particles.value
     T, n, d = value.shape
@@ -1200,7 +1201,7 @@ def _check_smoother(ssm_scenario, particle_filter):
     _check_lg(ssm_scenario, particle_filter)
     if isinstance(ssm_scenario, StochasticVolatility) and ssm_scenario.dim != 1:
         raise NotImplementedError("StochasticVolatility: the smoothing kernels take dim = 1")
-    if isinstance(ssm_scenario, TimeHomogenousLinearGaussian) and not ssm_scenario.gpu_bootstrap_supported():
+    if isinstance(ssm_scenario, TimeHomogenousLinearGaussian) and not ssm_scenario.gpu_runtime_supported():
         raise NotImplementedError(f"(d, dy) = ({ssm_scenario.dim}, {ssm_scenario.dim_obs}) above the "
                                   f"run-time-dimension limit ({LG_RUNTIME_MAX})")
     if not isinstance(particle_filter, BootstrapFilter):

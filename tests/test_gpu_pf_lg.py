@@ -85,7 +85,7 @@ def test_runtime_dimensions_bit_exact(cuda, d, dy, diag_r):
     import mocat_gb300 as mg
     from mocat_gb300.ssm import _step
     p, ssm = _models(d, dy, seed=40 + d, diag_r=diag_r)
-    assert not ssm.gpu_supported() and ssm.gpu_bootstrap_supported()
+    assert not ssm.gpu_supported() and ssm.gpu_runtime_supported()
     T = 15
     _, y = models.simulate_lg(p, T, O.PRNGKey(0))
     for n in (3000, 3001):
@@ -115,16 +115,15 @@ def test_runtime_dimensions_bit_exact(cuda, d, dy, diag_r):
 
 
 def test_runtime_dimension_limits(cuda):
-    """above 32 the bootstrap filter is refused on the host; the other paths need a compiled pair"""
+    """above 32 the bootstrap and optimal-proposal filters are refused on the host"""
     import mocat_gb300 as mg
     p, ssm = _models(33, 33, seed=1)
-    assert not ssm.gpu_bootstrap_supported()
+    assert not ssm.gpu_runtime_supported()
     with pytest.raises(NotImplementedError):
         mg.ssm.initiate_particles(ssm, mg.ssm.BootstrapFilter(), 100, O.PRNGKey(0), np.zeros(33, np.float32))
-    _, ssm6 = _models(6, 6, seed=1)
-    with pytest.raises(NotImplementedError):  # the optimal proposal needs a compiled pair
-        mg.ssm.initiate_particles(ssm6, mg.ssm.OptimalNonLinearGaussianParticleFilter(), 100, O.PRNGKey(0),
-                                  np.zeros(6, np.float32))
+    pf = mg.ssm.OptimalNonLinearGaussianParticleFilter()
+    with pytest.raises(NotImplementedError):
+        mg.ssm.initiate_particles(ssm, pf, 100, O.PRNGKey(0), np.zeros(33, np.float32))
 
 
 @pytest.mark.parametrize("d", [3, 10])

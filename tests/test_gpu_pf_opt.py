@@ -32,7 +32,8 @@ def _models(d, dy=None, seed=0):
 
 
 @pytest.mark.parametrize("n", [3000, 3001])
-@pytest.mark.parametrize("d,dy", [(1, 1), (2, 1), (3, 3), (10, 10), (10, 1)])
+@pytest.mark.parametrize("d,dy", [(1, 1), (2, 1), (3, 3), (10, 10), (10, 1),
+                                  (6, 6), (7, 3), (2, 4), (32, 5)])  # the last four: run-time dimensions
 def test_init_and_step_bit_exact(cuda, d, dy, n):
     import mocat_gb300 as mg
     from mocat_gb300.ssm import _step
@@ -58,7 +59,7 @@ def test_init_and_step_bit_exact(cuda, d, dy, n):
 
 
 @pytest.mark.parametrize("scheme", ["systematic", "multinomial", "categorical"])
-@pytest.mark.parametrize("d,dy", [(1, 1), (3, 3), (10, 10)])
+@pytest.mark.parametrize("d,dy", [(1, 1), (3, 3), (10, 10), (6, 6), (7, 3)])  # 6, 7: run-time dimensions
 @pytest.mark.parametrize("odd", [False, True])
 def test_run_matches_oracle(cuda, scheme, d, dy, odd):
     import mocat_gb300 as mg
