@@ -129,11 +129,13 @@ __device__ __forceinline__ uint32_t asu(float f) { return __float_as_uint(f); }
 
 // natural log of a positive normal float
 __device__ __forceinline__ float logf_(float x) {
-  uint32_t ix = asu(x);
-  int e = (int)((ix >> 23) & 0xffu) - 127;
-  uint32_t mb = (ix & 0x007fffffu) | 0x3f800000u;
-  if (mb > 0x3fb504f3u) { mb -= 0x00800000u; e += 1; }
-  const float m = asf(mb);
+  // x = 2^e m with m in [sqrt(1/2), sqrt(2)) split off in integer arithmetic: subtracting the
+  // bits of the lower bound 0x3f3504f4 leaves e in the high bits and the mantissa offset in
+  // the low 23 (the same (e, m) as taking m = 1.mantissa and halving it when above sqrt(2),
+  // for every positive normal float)
+  const uint32_t t = asu(x) - 0x3f3504f4u;
+  const int e = (int)t >> 23;
+  const float m = asf((t & 0x007fffffu) + 0x3f3504f4u);
   // log(1 + f) = f - f^2/2 + f^3 q(f), f = m - 1 (exact) in [sqrt(1/2) - 1, sqrt(2) - 1];
   // q: degree-7 weighted least-squares fit (no division on the path)
   const float f = __fsub_rn(m, 1.0f);
