@@ -720,6 +720,11 @@ def _profile_model(name):
     import mocat_gb300 as mg
     if name == "nl1d":
         return mg.ssm.NonLinear1DBenchmark(), 1, "mgb_pf_nl1d"
+    if name == "lg1":  # the 1-D model of the config-1 leg
+        return mg.ssm.TimeHomogenousLinearGaussian(initial_mean=np.zeros(1), initial_covariance=np.eye(1),
+                                                   transition_matrix=[[0.9]], transition_covariance=np.eye(1),
+                                                   likelihood_matrix=np.eye(1), likelihood_covariance=[[0.25]]), \
+            1, "mgb_pf_lg"
     return mg.ssm.TimeHomogenousLinearGaussian(**model_arrays()), D, "mgb_pf_lg"
 
 
@@ -930,7 +935,7 @@ def main():
     ap.add_argument("--profile-run", action="store_true")
     ap.add_argument("--phase-trace", action="store_true")
     ap.add_argument("--profile-model", default="lg",
-                    choices=["lg", "nl1d", "adjoint", "lgstep", "score", "logreg", "svbatch"])
+                    choices=["lg", "lg1", "nl1d", "adjoint", "lgstep", "score", "logreg", "svbatch"])
     ap.add_argument("--profile-precision", default="bf16", choices=["bf16", "fp32"])
     ap.add_argument("--launch-per-step", action="store_true")
     ap.add_argument("--smc-B", type=int, default=256)

@@ -627,7 +627,21 @@ __device__ __forceinline__ float gk_unkey(uint32_t k) {
   return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
 }
 
-// one CTA per parameter row: n_raw draws, sort, thinned order statistics, distance
+// compare-exchange of bitonic stage (kk, j) for element e holding v, partner value o:
+// the lower index of an ascending (e & kk == 0) pair keeps the minimum
+__device__ __forceinline__ uint32_t gk_cx(uint32_t v, uint32_t o, int e, int kk, int j) {
+  const bool keep_min = ((e & j) == 0) == ((e & kk) == 0);
+  return keep_min ? min(v, o) : max(v, o);
+}
+
+constexpr int GK_EPT = GK_MAX_RAW / GK_TPB;  // sort elements per thread at the largest length
+
+// one CTA per parameter row: n_raw draws, sort, thinned order statistics, distance.
+// Draws: element q and q + ceil(n_raw/2) of random_bits(key, (n_raw,)) are the two halves of one
+// cipher call.  Sort: a bitonic network over p2 keys in shared memory; the stages with partner
+// distance j < 32 run on warp shuffles (thread t holds elements t + 256 m, so e and e ^ j share
+// a warp), the others through shared memory.  Distance: the order statistics and their squared
+// differences are gathered in parallel, then summed in index order by one thread.
 __global__ void __launch_bounds__(GK_TPB) k_gk_sim(const GKP p, int64_t P, const float *__restrict__ x,
                                                     const uint32_t *__restrict__ keys, const int32_t *mask,
                                                     float *__restrict__ dist, float *__restrict__ summary) {
@@ -644,12 +658,21 @@ __global__ void __launch_bounds__(GK_TPB) k_gk_sim(const GKP p, int64_t P, const
   __syncthreads();
   const float qv[4] = {q[0], q[1], q[2], q[3]};
   const uint32_t k0 = keys[2 * r], k1 = keys[2 * r + 1];
-  for (int i = threadIdx.x; i < p.p2; i += GK_TPB)
-    sk[i] = i < p.n_raw ? gk_key(gk_value(p, qv, bits_at(k0, k1, (uint64_t)p.n_raw, (uint64_t)i))) : 0xFFFFFFFFu;
+  const int n_raw = p.n_raw, P2 = p.p2, t = threadIdx.x;
+  const int h = (n_raw + 1) >> 1;
+  for (int i = t; i < h; i += GK_TPB) {
+    uint32_t r0, r1;
+    threefry2x32_m(k0, k1, (uint32_t)i, i + h < n_raw ? (uint32_t)(i + h) : 0u, p.one, r0, r1);
+    sk[i] = gk_key(gk_value(p, qv, r0));
+    if (i + h < n_raw) sk[i + h] = gk_key(gk_value(p, qv, r1));
+  }
+  for (int i = n_raw + t; i < P2; i += GK_TPB) sk[i] = 0xFFFFFFFFu;
   __syncthreads();
-  for (int kk = 2; kk <= p.p2; kk <<= 1) {
-    for (int j = kk >> 1; j > 0; j >>= 1) {
-      for (int i = threadIdx.x; i < p.p2; i += GK_TPB) {
+  const bool warp_live = (t & ~31) < P2;  // the warp holds elements (all lanes join the shuffles)
+  for (int kk = 2; kk <= P2; kk <<= 1) {
+    int j = kk >> 1;
+    for (; j >= 32; j >>= 1) {
+      for (int i = t; i < P2; i += GK_TPB) {
         const int ixj = i ^ j;
         if (ixj > i) {
           const uint32_t a = sk[i], b = sk[ixj];
@@ -661,17 +684,67 @@ __global__ void __launch_bounds__(GK_TPB) k_gk_sim(const GKP p, int64_t P, const
       }
       __syncthreads();
     }
-  }
-  if (summary)
-    for (int j = threadIdx.x; j < p.n_sum; j += GK_TPB)
-      summary[r * p.n_sum + j] = gk_unkey(sk[(int)(((int64_t)j * p.n_raw) / p.n_sum)]);
-  if (dist && threadIdx.x == 0) {
-    float acc = 0.0f;
-    for (int j = 0; j < p.n_sum; ++j) {
-      const float dv = __fsub_rn(gk_unkey(sk[(int)(((int64_t)j * p.n_raw) / p.n_sum)]), p.data[j]);
-      acc = j == 0 ? __fmul_rn(dv, dv) : __fadd_rn(acc, __fmul_rn(dv, dv));
+    // the stages j < 32 of this kk in registers
+    if (warp_live) {
+      uint32_t v[GK_EPT];
+#pragma unroll
+      for (int m = 0; m < GK_EPT; ++m) {
+        const int e = t + GK_TPB * m;
+        v[m] = e < P2 ? sk[e] : 0xFFFFFFFFu;
+      }
+      for (int jj = j; jj > 0; jj >>= 1) {
+#pragma unroll
+        for (int m = 0; m < GK_EPT; ++m) {
+          if (GK_TPB * m < P2) {  // uniform across the CTA
+            const uint32_t o = __shfl_xor_sync(0xffffffffu, v[m], jj);
+            v[m] = gk_cx(v[m], o, t + GK_TPB * m, kk, jj);
+          }
+        }
+      }
+#pragma unroll
+      for (int m = 0; m < GK_EPT; ++m) {
+        const int e = t + GK_TPB * m;
+        if (e < P2) sk[e] = v[m];
+      }
     }
-    dist[r] = __fsqrt_rn(acc);
+    __syncthreads();
+  }
+  // thinned order statistics j < n_sum (ranks floor(j n_raw / n_sum), below 2^22) and, for the
+  // distance, their squared differences to the data, gathered in parallel
+  float sv[GK_EPT], dv2[GK_EPT];
+#pragma unroll
+  for (int m = 0; m < GK_EPT; ++m) {
+    const int j = t + GK_TPB * m;
+    if (j < p.n_sum) {
+      sv[m] = gk_unkey(sk[(int)(((uint32_t)j * (uint32_t)n_raw) / (uint32_t)p.n_sum)]);
+      if (dist) {
+        const float dv = __fsub_rn(sv[m], p.data[j]);
+        dv2[m] = __fmul_rn(dv, dv);
+      }
+    }
+  }
+  if (summary) {
+#pragma unroll
+    for (int m = 0; m < GK_EPT; ++m) {
+      const int j = t + GK_TPB * m;
+      if (j < p.n_sum) summary[r * p.n_sum + j] = sv[m];
+    }
+  }
+  if (dist) {
+    __syncthreads();  // every rank read before sk is reused for the squared differences
+    float *sd = reinterpret_cast<float *>(sk);
+#pragma unroll
+    for (int m = 0; m < GK_EPT; ++m) {
+      const int j = t + GK_TPB * m;
+      if (j < p.n_sum) sd[j] = dv2[m];
+    }
+    __syncthreads();
+    if (t == 0) {
+      float acc = sd[0];
+#pragma unroll 8
+      for (int j = 1; j < p.n_sum; ++j) acc = __fadd_rn(acc, sd[j]);
+      dist[r] = __fsqrt_rn(acc);
+    }
   }
 }
 
