@@ -231,6 +231,45 @@ __global__ void __launch_bounds__(256) k_categorical(const float *__restrict__ l
   }
 }
 
+// the same draw for an even number of outputs: element (k, i) and (k + nout/2, i) of the
+// (nout, n) Gumbel array are the two halves of one cipher call (counter k n + i and
+// k n + i + n nout / 2), so one warp takes the row pair and spends one call per column
+__global__ void __launch_bounds__(256) k_categorical_pairs(const float *__restrict__ lw, int64_t n, int64_t nout,
+                                                            const uint32_t *key, const int32_t *flag,
+                                                            uint32_t one, int32_t *__restrict__ anc) {
+  if (flag && *flag == 0) return;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * 256LL + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * 256) >> 5;
+  const uint32_t k0 = key[0], k1 = key[1];
+  const int64_t half = nout >> 1;
+  const uint64_t h = (uint64_t)n * (uint64_t)half;
+  for (int64_t k = warp; k < half; k += nwarps) {
+    float best0 = -INFINITY, best1 = -INFINITY;
+    int64_t bi0 = n, bi1 = n;
+    for (int64_t i = lane; i < n; i += 32) {
+      const uint64_t c = (uint64_t)k * (uint64_t)n + (uint64_t)i;
+      uint32_t r0, r1;
+      threefry2x32_m(k0, k1, (uint32_t)c, (uint32_t)(c + h), one, r0, r1);
+      const float l = lw[i];
+      const float v0 = __fadd_rn(bits_to_gumbel(r0), l), v1 = __fadd_rn(bits_to_gumbel(r1), l);
+      if (v0 > best0) { best0 = v0; bi0 = i; }
+      if (v1 > best1) { best1 = v1; bi1 = i; }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float ob0 = __shfl_xor_sync(0xffffffffu, best0, o), ob1 = __shfl_xor_sync(0xffffffffu, best1, o);
+      const int64_t oi0 = __shfl_xor_sync(0xffffffffu, bi0, o), oi1 = __shfl_xor_sync(0xffffffffu, bi1, o);
+      if (ob0 > best0 || (ob0 == best0 && oi0 < bi0)) { best0 = ob0; bi0 = oi0; }
+      if (ob1 > best1 || (ob1 == best1 && oi1 < bi1)) { best1 = ob1; bi1 = oi1; }
+    }
+    if (lane == 0) {
+      anc[k] = (int32_t)(bi0 < n ? bi0 : 0);
+      anc[k + half] = (int32_t)(bi1 < n ? bi1 : 0);
+    }
+  }
+}
+
 // out[k, :] = x[anc[k], :]
 __global__ void k_gather_rows_v4(const float4 *__restrict__ x, int64_t w4, const int32_t *__restrict__ anc,
                                  int64_t n_out, float4 *__restrict__ out) {
@@ -291,7 +330,10 @@ int launch_resample(const float *lw, int64_t n, int scheme, const float *Mptr, c
     const unsigned g = (unsigned)((2 * n + MP_L - 1) / MP_L);
     k_merge_path<<<g, MP_TPB, 0, s>>>(w.C, w.S, n, Mptr, flag, &w.ctl->degenerate, anc, err);
   } else if (scheme == MGB_RESAMPLE_CATEGORICAL) {
-    k_categorical<<<grid_for(n * 32, 256, 8LL * kNumSMs), 256, 0, s>>>(lw, n, n, key, flag, anc);
+    if (n % 2 == 0)
+      k_categorical_pairs<<<grid_for(n * 16, 256, 8LL * kNumSMs), 256, 0, s>>>(lw, n, n, key, flag, 1u, anc);
+    else
+      k_categorical<<<grid_for(n * 32, 256, 8LL * kNumSMs), 256, 0, s>>>(lw, n, n, key, flag, anc);
   } else {
     return ERR_BAD_ARG;
   }

@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(ADAPT_TPB) k_smc_resample(SMCView v) {
 
 // the reference's categorical resampling per posterior (random.categorical(key, lw, (N,)),
 // smc.py:61-71): a_k = argmax_i gumbel(bits(key, N N)[k N + i]) + lw_i, first maximum, NaN
-// ignored (as k_categorical); one warp per output, grid (., B)
+// ignored (as k_categorical); one warp per output (per output pair for even N), grid (., B)
 __global__ void __launch_bounds__(256) k_smc_categorical(SMCView v) {
   const int b = blockIdx.y, N = v.N, lane = threadIdx.x & 31;
   int32_t *anc = v.anc + (int64_t)b * N;
@@ -290,6 +290,49 @@ __global__ void __launch_bounds__(256) k_smc_categorical(SMCView v) {
   const float *lw = v.lw + (int64_t)b * N;
   const uint32_t k0 = v.rkey[2 * b], k1 = v.rkey[2 * b + 1];
   const uint64_t tot = (uint64_t)N * (uint64_t)N;
+  if (N % 2 == 0) {
+    // elements (k, i) and (k + N/2, i) are the two halves of one cipher call (counters k N + i
+    // and k N + i + N^2/2): one warp takes the row pair, one call per column
+    const int64_t half = N >> 1;
+    const uint64_t h = tot >> 1;
+    for (int64_t k = warp; k < half; k += nwarps) {
+      float best0 = -INFINITY, best1 = -INFINITY;
+      int64_t bi0 = N, bi1 = N;
+      for (int64_t i = lane; i < N; i += 32) {
+        const uint64_t c = (uint64_t)k * (uint64_t)N + (uint64_t)i;
+        uint32_t r0, r1;
+        threefry2x32(k0, k1, (uint32_t)c, (uint32_t)(c + h), r0, r1);
+        const float l = lw[i];
+        const float v0 = __fadd_rn(bits_to_gumbel(r0), l), v1 = __fadd_rn(bits_to_gumbel(r1), l);
+        if (v0 > best0) {
+          best0 = v0;
+          bi0 = i;
+        }
+        if (v1 > best1) {
+          best1 = v1;
+          bi1 = i;
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float ob0 = __shfl_xor_sync(0xffffffffu, best0, o), ob1 = __shfl_xor_sync(0xffffffffu, best1, o);
+        const int64_t oi0 = __shfl_xor_sync(0xffffffffu, bi0, o), oi1 = __shfl_xor_sync(0xffffffffu, bi1, o);
+        if (ob0 > best0 || (ob0 == best0 && oi0 < bi0)) {
+          best0 = ob0;
+          bi0 = oi0;
+        }
+        if (ob1 > best1 || (ob1 == best1 && oi1 < bi1)) {
+          best1 = ob1;
+          bi1 = oi1;
+        }
+      }
+      if (lane == 0) {
+        anc[k] = (int32_t)(bi0 < N ? bi0 : 0);
+        anc[k + half] = (int32_t)(bi1 < N ? bi1 : 0);
+      }
+    }
+    return;
+  }
   for (int64_t k = warp; k < N; k += nwarps) {
     float best = -INFINITY;
     int64_t bi = N;

@@ -63,7 +63,7 @@ def test_multinomial_bit_exact(cuda, n):
     assert ok and np.array_equal(got, ref), (n, np.flatnonzero(got != ref)[:10])
 
 
-@pytest.mark.parametrize("n", [1, 5, 64, 1000, 4096])
+@pytest.mark.parametrize("n", [1, 2, 5, 64, 1000, 4096, 4097])  # even n: the row-pair kernel
 def test_categorical_bit_exact(cuda, n):
     from mocat_gb300.resampling import resample
     lw = _lw(n, n + 4)
