@@ -145,8 +145,7 @@ __global__ void __launch_bounds__(ABC_MOVE_TPB) k_abc_init(const __grid_constant
   if (g >= B * N) return;
   const int64_t b = g / N, i = g - b * N;
   uint32_t e0, e1, s0, s1;
-  split_at(keys[2 * b], keys[2 * b + 1], 2, 0, e0, e1);  // extra.random_key
-  split_at(keys[2 * b], keys[2 * b + 1], 2, 1, s0, s1);  // sub_key of the prior draws
+  split2(keys[2 * b], keys[2 * b + 1], e0, e1, s0, s1);  // extra.random_key, sub_key of the prior draws
   uint32_t a0, a1;
   split_at(s0, s1, (uint64_t)N, (uint64_t)i, a0, a1);
   uint32_t bits[D];
@@ -437,10 +436,11 @@ __global__ void __launch_bounds__(ABC_MOVE_TPB) k_abc_move(const __grid_constant
   for (int s = 0; s < ctl.mcmc_steps; ++s) {
     uint32_t t0, t1;
     split_at(k0, k1, 2, 0, t0, t1);  // always(): key <- split(key)[0]
-    uint32_t n0, n1, a0, a1, c0, c1;
-    split_at(t0, t1, 4, 0, n0, n1);  // new extra key
-    split_at(t0, t1, 4, 1, a0, a1);  // proposal normals
-    split_at(t0, t1, 4, 3, c0, c1);  // simulation
+    uint32_t sk4[8];
+    split4(t0, t1, sk4);
+    const uint32_t n0 = sk4[0], n1 = sk4[1];  // new extra key
+    const uint32_t a0 = sk4[2], a1 = sk4[3];  // proposal normals
+    const uint32_t c0 = sk4[6], c1 = sk4[7];  // simulation
     uint32_t bits[D];
     bits_vec<D>(a0, a1, bits, p.one);
     float xp[D];
@@ -452,8 +452,7 @@ __global__ void __launch_bounds__(ABC_MOVE_TPB) k_abc_move(const __grid_constant
     float a = __fmul_rn(expf_(__fsub_rn(pp, ppn)), dn < thr ? 1.0f : 0.0f);
     a = a != a ? 0.0f : fminf(1.0f, a);
     uint32_t u0, u1, v0, v1;
-    split_at(n0, n1, 2, 0, u0, u1);
-    split_at(n0, n1, 2, 1, v0, v1);
+    split2(n0, n1, u0, u1, v0, v1);
     const float u = bits_to_unit(bits_at(v0, v1, 1, 0));
     if (u < a) {
 #pragma unroll
@@ -836,9 +835,14 @@ __global__ void __launch_bounds__(ABC_MOVE_TPB) k_gk_prop(ABCCtl ctl, int64_t B,
   }
   uint32_t t0, t1, n0, n1, a0, a1, c0, c1;
   split_at(k0, k1, 2, 0, t0, t1);
-  split_at(t0, t1, 4, 0, n0, n1);
-  split_at(t0, t1, 4, 1, a0, a1);
-  split_at(t0, t1, 4, 3, c0, c1);
+  uint32_t sk4[8];  // split(t, 4): 0 new extra key, 1 proposal normals, 3 simulation
+  split4(t0, t1, sk4);
+  n0 = sk4[0];
+  n1 = sk4[1];
+  a0 = sk4[2];
+  a1 = sk4[3];
+  c0 = sk4[6];
+  c1 = sk4[7];
   uint32_t bits[D];
   bits_vec<D>(a0, a1, bits, one);
   float xp[D];
@@ -868,8 +872,7 @@ __global__ void __launch_bounds__(ABC_MOVE_TPB) k_gk_accept(ABCCtl ctl, int64_t 
   a = a != a ? 0.0f : fminf(1.0f, a);
   const uint32_t n0 = g.mkey[2 * i0], n1 = g.mkey[2 * i0 + 1];
   uint32_t u0, u1, v0, v1;
-  split_at(n0, n1, 2, 0, u0, u1);
-  split_at(n0, n1, 2, 1, v0, v1);
+  split2(n0, n1, u0, u1, v0, v1);
   const float u = bits_to_unit(bits_at(v0, v1, 1, 0));
   if (u < a) {
 #pragma unroll
@@ -1148,9 +1151,14 @@ __global__ void __launch_bounds__(128) k_abc_mcmc_lg(const __grid_constant__ ABC
   for (int64_t i = 1; i < n; ++i) {
     split_at(K0, K1, 2, 0, t0, t1);  // always
     uint32_t n0, n1, c0, c1;
-    split_at(t0, t1, 4, 0, n0, n1);
-    split_at(t0, t1, 4, 1, a0, a1);
-    split_at(t0, t1, 4, 3, c0, c1);
+    uint32_t sk4[8];  // split(t, 4): 0 new extra key, 1 proposal normals, 3 simulation
+    split4(t0, t1, sk4);
+    n0 = sk4[0];
+    n1 = sk4[1];
+    a0 = sk4[2];
+    a1 = sk4[3];
+    c0 = sk4[6];
+    c1 = sk4[7];
     bits_vec<D>(a0, a1, bits, p.one);
     float xp[D];
 #pragma unroll
@@ -1160,8 +1168,7 @@ __global__ void __launch_bounds__(128) k_abc_mcmc_lg(const __grid_constant__ ABC
     float a = __fmul_rn(expf_(__fsub_rn(pp, ppn)), dn < thr ? 1.0f : 0.0f);
     a = a != a ? 0.0f : fminf(1.0f, a);
     uint32_t u0, u1, v0, v1;
-    split_at(n0, n1, 2, 0, u0, u1);
-    split_at(n0, n1, 2, 1, v0, v1);
+    split2(n0, n1, u0, u1, v0, v1);
     const float u = bits_to_unit(bits_at(v0, v1, 1, 0));
     if (u < a) {
 #pragma unroll

@@ -110,6 +110,24 @@ MGB_HD void split_at(uint32_t k0, uint32_t k1, uint64_t num, uint64_t i, uint32_
   o1 = bits_at(k0, k1, 2 * num, 2 * i + 1);
 }
 
+// both sub-keys of split(key, 2) from the two cipher calls of random_bits(key, (4,)): call
+// (0, 2) gives words 0 and 2, call (1, 3) words 1 and 3; sub-key j is words 2j, 2j + 1
+MGB_HD void split2(uint32_t k0, uint32_t k1, uint32_t &a0, uint32_t &a1, uint32_t &b0, uint32_t &b1) {
+  uint32_t x0, x1, y0, y1;
+  threefry2x32(k0, k1, 0u, 2u, x0, x1);
+  threefry2x32(k0, k1, 1u, 3u, y0, y1);
+  a0 = x0;
+  a1 = y0;
+  b0 = x1;
+  b1 = y1;
+}
+
+// the four sub-keys of split(key, 4) from the four cipher calls of random_bits(key, (8,)):
+// call (q, q + 4) gives words q and q + 4; o[2j], o[2j + 1] = sub-key j
+MGB_HD void split4(uint32_t k0, uint32_t k1, uint32_t (&o)[8]) {
+  for (int q = 0; q < 4; ++q) threefry2x32(k0, k1, (uint32_t)q, (uint32_t)(q + 4), o[q], o[q + 4]);
+}
+
 // random_bits(key, (D,)) for a compile-time D: ceil(D/2) cipher calls
 template <int D>
 __device__ __forceinline__ void bits_vec(uint32_t k0, uint32_t k1, uint32_t (&b)[D], uint32_t one = 1u) {
