@@ -137,6 +137,52 @@ __global__ void __launch_bounds__(FB_TPB) k_rej_prerun(const __grid_constant__ T
   }
 }
 
+// the prerun draw for an even number of items: element (i, j) and (i + n/2, j) of the (n, Np)
+// Gumbel array are the two halves of one cipher call (counters i Np + j and i Np + j + n Np / 2),
+// so CTA i takes items i and i + n/2 and spends one call per pool element
+template <class TP, bool BACK>
+__global__ void __launch_bounds__(FB_TPB) k_rej_prerun_pairs(const __grid_constant__ TP p, int64_t n, int64_t Np,
+                                                              const float *__restrict__ itm,
+                                                              const float *__restrict__ pool,
+                                                              const float *__restrict__ lw, const uint32_t *key,
+                                                              int32_t *__restrict__ idx, float *__restrict__ dens,
+                                                              RejCtl *ctl) {
+  constexpr int DC = TP::DIM;
+  const int D = p.dim();
+  __shared__ Best sm0[FB_TPB / 32], sm1[FB_TPB / 32];
+  __shared__ uint32_t kc[2];
+  const int64_t i = blockIdx.x, half = n >> 1;
+  if (threadIdx.x == 0) split_at(key[0], key[1], 3, 0, kc[0], kc[1]);
+  __syncthreads();
+  const uint32_t k0 = kc[0], k1 = kc[1];
+  const uint64_t h = (uint64_t)half * (uint64_t)Np;
+  Best b0{-INFINITY, 0, 0}, b1{-INFINITY, 0, 0};
+  for (int64_t j = threadIdx.x; j < Np; j += FB_TPB) {
+    const uint64_t c = (uint64_t)i * Np + j;
+    uint32_t r0, r1;
+    threefry2x32_m(k0, k1, (uint32_t)c, (uint32_t)(c + h), p.one, r0, r1);
+    const float l = lw[j];
+    best_take(b0, __fadd_rn(bits_to_gumbel(r0), l), (int32_t)j);
+    best_take(b1, __fadd_rn(bits_to_gumbel(r1), l), (int32_t)j);
+  }
+  const int32_t bi0 = block_argmax<FB_TPB>(b0, sm0);
+  const int32_t bi1 = block_argmax<FB_TPB>(b1, sm1);
+  if (threadIdx.x == 0) {
+#pragma unroll 1
+    for (int s = 0; s < 2; ++s) {
+      const int64_t it = s ? i + half : i;
+      const int32_t bi = s ? bi1 : bi0;
+      float u[DC];
+#pragma unroll
+      for (int r = 0; r < D; ++r) u[r] = itm[r * n + it];
+      const float dv = expf_(-rej_potential<TP, BACK>(p, u, pool, Np, bi));
+      idx[it] = bi;
+      dens[it] = dv;
+      atomicMax(&ctl->pre_max, asu(dv));
+    }
+  }
+}
+
 // prerun acceptance: the initial bound, nya_i, the items' keys, slot 0
 __global__ void k_rej_accept(int64_t n, RejCfg cfg, const uint32_t *key, const float *__restrict__ dens,
                              uint8_t *__restrict__ nya, uint32_t *__restrict__ keys, RejSlot *ring, RejCtl *ctl) {
@@ -289,7 +335,11 @@ static int rej_run(const TP &p, const RejCfg &cfg, int64_t n, int64_t Np, const 
   if (e == cudaSuccess) e = cudaMemsetAsync(w.ctl, 0, sizeof(RejCtl), s);
   if (e != cudaSuccess) return ERR_CUDA;
   int st;
-  k_rej_prerun<TP, BACK><<<(unsigned)n, FB_TPB, 0, s>>>(p, n, Np, itm, pool, lw, key, idx, w.dens, w.ctl);
+  if (n % 2 == 0)
+    k_rej_prerun_pairs<TP, BACK><<<(unsigned)(n / 2), FB_TPB, 0, s>>>(p, n, Np, itm, pool, lw, key, idx, w.dens,
+                                                                       w.ctl);
+  else
+    k_rej_prerun<TP, BACK><<<(unsigned)n, FB_TPB, 0, s>>>(p, n, Np, itm, pool, lw, key, idx, w.dens, w.ctl);
   if ((st = launch_status())) return st;
   k_rej_accept<<<grid_for(n, 256), 256, 0, s>>>(n, cfg, key, w.dens, w.nya, w.keys, w.ring, w.ctl);
   if ((st = launch_status())) return st;
