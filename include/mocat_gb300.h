@@ -763,6 +763,20 @@ int mgb_abc_gk_simulate(const mgb_abc_gk_model *model_host, int64_t P, const flo
 int mgb_abc_mcmc_lg(const mgb_abc_lg_model *model_host, int64_t B, int64_t n, const uint32_t *keys_dev, float stepsize,
                     float threshold, float *x_dev, float *distance_dev, float *prior_potential_dev, float *alpha_dev,
                     void *stream);
+/* RandomWalkABC() with the RMMetropolisDiagStepsize correction (mocat/src/abc/mcmc.py:105-140,
+ * mocat/src/mcmc/metropolis.py:73-160) at the sampler's defaults: the chain starts at threshold
+ * 50 and stepsize 1 per dimension, post_mean x_0, diag_post_cov = stepsize d / 2.38^2; after
+ * every step, with rm = scale * iter^-neg_exp:
+ *   threshold <- exp(log threshold - rm (alpha - target))
+ *   r = min(rm, 1 - 1e-3); diag_post_cov <- (1 - r) diag_post_cov + r (x - post_mean)^2;
+ *   post_mean <- (1 - r) post_mean + r x; stepsize <- diag_post_cov / d * 2.38^2.
+ * B independent chains (keys_dev (B, 2)) of n states; x (B, n, d), alpha (B, n), threshold
+ * (B, n) and stepsize (B, n, d) device outputs, each state's values after its adaptation.
+ * target: the tuning target of alpha (0.1 in the reference); scale > 0: rm_stepsize_scale;
+ * neg_exp >= 0: rm_stepsize_neg_exponent (2/3). */
+int mgb_abc_mcmc_rm_lg(const mgb_abc_lg_model *model_host, int64_t B, int64_t n, const uint32_t *keys_dev,
+                       float target, float scale, float neg_exp, float *x_dev, float *alpha_dev, float *threshold_dev,
+                       float *stepsize_dev, void *stream);
 size_t mgb_abc_vanilla_workspace(int64_t n);
 int mgb_abc_vanilla_lg(const mgb_abc_lg_model *model_host, int64_t n, const uint32_t *key_dev, float threshold,
                        float acceptance_rate, void *ws_dev, size_t ws_bytes, float *x_dev, float *prior_potential_dev,

@@ -165,6 +165,24 @@ class RandomWalkABC:
     def __init__(self, threshold=None, stepsize=None):
         self.threshold = threshold
         self.stepsize = stepsize
+        # the Robbins-Monro target of RMMetropolisDiagStepsize (abc/mcmc.py:44-48)
+        self.tuning = cdict(parameter="threshold", target=0.1, metric="alpha", monotonicity="increasing")
+
+
+class RMMetropolisDiagStepsize:
+    """The adaptive correction of RandomWalkABC chains (abc/mcmc.py:105-140 over RMMetropolis,
+    mcmc/metropolis.py:73-160): after every Metropolis step, a log Robbins-Monro update of the
+    threshold towards sampler.tuning.target acceptance, and the per-dimension stepsize set to
+    2.38^2 / d times a running estimate of the posterior variances; rm step = scale iter^-neg_exp."""
+
+    def __init__(self, super_correction=None, adapt_cut_off=math.inf, rm_stepsize_scale=1.0,
+                 rm_stepsize_neg_exponent=2.0 / 3.0, log_update=True):
+        if super_correction not in (None, "Metropolis"):
+            raise NotImplementedError("the GPU chain uses the Metropolis correction underneath")
+        if adapt_cut_off != math.inf or not log_update:
+            raise NotImplementedError("the GPU chain adapts at every step with the log update")
+        self.rm_stepsize_scale = float(rm_stepsize_scale)
+        self.rm_stepsize_neg_exponent = float(rm_stepsize_neg_exponent)
 
 
 class VanillaABC:
@@ -346,14 +364,33 @@ def run_batched(scenario, sampler, n, random_keys, chain=False):
     return BatchedABCSMC(scenario, sampler, n, random_keys).run(chain)
 
 
-def run_chains(scenario, sampler, n, random_keys):
-    """RandomWalkABC(stepsize, threshold) run as an MCMC sampler (abc/mcmc.py:16-100, mocat.run) for
-    B independent chains, one per key: value (B, n, d), distance, prior_potential, alpha (B, n).
-    Fixed stepsize and threshold (the Metropolis correction)."""
+def run_chains(scenario, sampler, n, random_keys, correction=None):
+    """RandomWalkABC run as an MCMC sampler (abc/mcmc.py:16-100, mocat.run) for B independent
+    chains, one per key.  With the Metropolis correction (correction=None): fixed stepsize and
+    threshold; value (B, n, d), distance, prior_potential, alpha (B, n).  With
+    correction=RMMetropolisDiagStepsize(): the adaptive chain from the sampler's defaults
+    (threshold and stepsize unset); value (B, n, d), alpha, threshold (B, n), stepsize (B, n, d)."""
     if not isinstance(scenario, LinearGaussian):
         raise NotImplementedError(f"{scenario.__class__.__name__}: no GPU ABC-MCMC kernel for this scenario")
     if (scenario.dim, scenario.dim_obs) not in SUPPORTED:
         raise NotImplementedError(f"(d, dy) = ({scenario.dim}, {scenario.dim_obs}) not compiled")
+    if isinstance(correction, RMMetropolisDiagStepsize):
+        if sampler.stepsize is not None or sampler.threshold is not None:
+            raise NotImplementedError("the adaptive GPU chain starts from the sampler's defaults "
+                                      "(threshold and stepsize unset)")
+        keys = _dev.as_key(random_keys).reshape(-1, 2).contiguous()
+        B, d, dev = keys.shape[0], scenario.dim, keys.device
+        x = torch.empty((B, n, d), dtype=torch.float32, device=dev)
+        st = torch.empty((B, n, d), dtype=torch.float32, device=dev)
+        al, th = (torch.empty((B, n), dtype=torch.float32, device=dev) for _ in range(2))
+        _keep, model = scenario.derived()
+        call("mgb_abc_mcmc_rm_lg", ctypes.byref(model), B, n, _dev.ptr(keys), float(sampler.tuning.target),
+             correction.rm_stepsize_scale, correction.rm_stepsize_neg_exponent, _dev.ptr(x), _dev.ptr(al),
+             _dev.ptr(th), _dev.ptr(st), _dev.stream_ptr())
+        return cdict(value=x, alpha=al, threshold=th, stepsize=st)
+    name = getattr(correction, "__name__", type(correction).__name__)
+    if correction is not None and correction != "Metropolis" and name != "Metropolis":
+        raise NotImplementedError(f"{name}: no GPU chain for this correction")
     if sampler.stepsize is None or sampler.threshold is None:
         raise NotImplementedError("RandomWalkABC chains need a fixed stepsize and threshold")
     keys = _dev.as_key(random_keys).reshape(-1, 2).contiguous()
@@ -366,7 +403,7 @@ def run_chains(scenario, sampler, n, random_keys):
     return cdict(value=x, distance=dist, prior_potential=pp, alpha=al)
 
 
-def run(scenario, sampler, n, random_key):
+def run(scenario, sampler, n, random_key, correction=None):
     """mocat.run (sample.py:110-148) for MetropolisedABCSMCSampler, VanillaABC or RandomWalkABC (an MCMC
     chain) on an ABC scenario.
     ABC-SMC returns the reference's stacked layout: value (L, n, d), log_weight and distance
@@ -374,7 +411,7 @@ def run(scenario, sampler, n, random_key):
     if isinstance(sampler, VanillaABC):
         return _run_vanilla(scenario, sampler, n, random_key)
     if isinstance(sampler, RandomWalkABC):
-        out = run_chains(scenario, sampler, n, _dev.as_key(random_key).reshape(1, 2))
+        out = run_chains(scenario, sampler, n, _dev.as_key(random_key).reshape(1, 2), correction)
         return cdict(**{k: v[0] for k, v in out.__dict__.items()})
     out = run_batched(scenario, sampler, n, _dev.as_key(random_key).reshape(1, 2), chain=True)
     L = int(out.iterations[0]) + 1

@@ -1186,6 +1186,105 @@ __global__ void __launch_bounds__(128) k_abc_mcmc_lg(const __grid_constant__ ABC
   }
 }
 
+// RandomWalkABC with the RMMetropolisDiagStepsize correction (abc/mcmc.py:105-140,
+// mcmc/metropolis.py:73-160) at the sampler's defaults (threshold and stepsize unset: 50 and 1 per
+// dimension, post_mean x_0, diag_post_cov = stepsize d / 2.38^2), one thread per chain.  Each step
+// is the fixed-parameter chain's step with the current threshold and per-dimension stepsize,
+// followed by, with rm = scale iter^-neg_exp (iter = the step index; the library's exp and log):
+//   threshold <- exp(log threshold - rm (alpha - target))       (log Robbins-Monro, increasing)
+//   r = min(rm, 1 - 1e-3); diag <- (1 - r) diag + r (x - post_mean)^2; post_mean <- (1 - r) post_mean + r x;
+//   stepsize <- diag / d * 2.38^2
+template <int D, int DY>
+__global__ void __launch_bounds__(128) k_abc_mcmc_rm_lg(const __grid_constant__ ABCP<D, DY> p, int64_t B, int64_t n,
+                                                         const uint32_t *keys, float target, float scale,
+                                                         float neg_exp, float *__restrict__ x_out,
+                                                         float *__restrict__ alpha_out, float *__restrict__ thr_out,
+                                                         float *__restrict__ st_out) {
+  const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  uint32_t K0 = keys[2 * b], K1 = keys[2 * b + 1], a0, a1, t0, t1;
+  split_at(K0, K1, 2, 1, a0, a1);
+  split_at(K0, K1, 2, 0, t0, t1);
+  split_at(t0, t1, 2, 0, K0, K1);  // prior potential
+  uint32_t bits[D];
+  bits_vec<D>(a0, a1, bits, p.one);
+  float e[D], x[D];
+#pragma unroll
+  for (int j = 0; j < D; ++j) e[j] = bits_to_normal(bits[j]);
+#pragma unroll
+  for (int r = 0; r < D; ++r) {
+    float v = __fmul_rn(p.C0[r * D], e[0]);
+#pragma unroll
+    for (int k = 1; k < D; ++k) v = __fmaf_rn(p.C0[r * D + k], e[k], v);
+    x[r] = __fadd_rn(p.m0[r], v);
+  }
+  float pp = abc_prior_potential<D, DY>(p, x);
+  split_at(K0, K1, 2, 0, t0, t1);  // the initial simulation takes split(K)[1]; its distance is unused
+  K0 = t0;
+  K1 = t1;
+  float thr = 50.0f, st[D], pm[D], dg[D];
+#pragma unroll
+  for (int j = 0; j < D; ++j) {
+    st[j] = 1.0f;
+    pm[j] = x[j];
+    dg[j] = __fdiv_rn(__fmul_rn(st[j], (float)D), 5.6644f);
+  }
+  const int64_t base = b * n;
+#pragma unroll
+  for (int j = 0; j < D; ++j) {
+    x_out[base * D + j] = x[j];
+    st_out[base * D + j] = st[j];
+  }
+  alpha_out[base] = 1.0f;
+  thr_out[base] = thr;
+#pragma unroll 1
+  for (int64_t i = 1; i < n; ++i) {
+    split_at(K0, K1, 2, 0, t0, t1);  // always
+    uint32_t sk4[8];                 // split(t, 4): 0 new extra key, 1 proposal normals, 3 simulation
+    split4(t0, t1, sk4);
+    bits_vec<D>(sk4[2], sk4[3], bits, p.one);
+    float xp[D];
+#pragma unroll
+    for (int j = 0; j < D; ++j) xp[j] = __fadd_rn(x[j], __fmul_rn(__fsqrt_rn(st[j]), bits_to_normal(bits[j])));
+    const float ppn = abc_prior_potential<D, DY>(p, xp);
+    const float dn = abc_sim_distance<D, DY>(p, xp, sk4[6], sk4[7]);
+    float a = __fmul_rn(expf_(__fsub_rn(pp, ppn)), dn < thr ? 1.0f : 0.0f);
+    a = a != a ? 0.0f : fminf(1.0f, a);
+    uint32_t u0, u1, v0, v1;
+    split2(sk4[0], sk4[1], u0, u1, v0, v1);
+    const float u = bits_to_unit(bits_at(v0, v1, 1, 0));
+    if (u < a) {
+#pragma unroll
+      for (int j = 0; j < D; ++j) x[j] = xp[j];
+      pp = ppn;
+    }
+    K0 = u0;
+    K1 = u1;
+    const float rm = __fmul_rn(scale, expf_(__fmul_rn(-neg_exp, logf_((float)i))));
+    thr = expf_(__fsub_rn(logf_(thr), __fmul_rn(rm, __fsub_rn(a, target))));
+    const float r2 = fminf(rm, 0.999f), q2 = __fsub_rn(1.0f, r2);
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      const float dv = __fsub_rn(x[j], pm[j]);
+      dg[j] = __fadd_rn(__fmul_rn(q2, dg[j]), __fmul_rn(r2, __fmul_rn(dv, dv)));
+      pm[j] = __fadd_rn(__fmul_rn(q2, pm[j]), __fmul_rn(r2, x[j]));
+      st[j] = __fmul_rn(__fdiv_rn(dg[j], (float)D), 5.6644f);
+      x_out[(base + i) * D + j] = x[j];
+      st_out[(base + i) * D + j] = st[j];
+    }
+    alpha_out[base + i] = a;
+    thr_out[base + i] = thr;
+  }
+}
+
+template <int D, int DY>
+static int abc_mcmc_rm_lg(const mgb_abc_lg_model *m, int64_t B, int64_t n, const uint32_t *keys, float target,
+                          float scale, float neg_exp, float *x, float *alpha, float *thr, float *st, cudaStream_t s) {
+  k_abc_mcmc_rm_lg<D, DY><<<(unsigned)((B + 127) / 128), 128, 0, s>>>(pack_abc<D, DY>(m), B, n, keys, target, scale,
+                                                                      neg_exp, x, alpha, thr, st);
+  return launch_status();
+}
+
 template <int D, int DY>
 static int abc_mcmc_lg(const mgb_abc_lg_model *m, int64_t B, int64_t n, const uint32_t *keys, float stepsize,
                        float thr, float *x, float *dist, float *pp, float *alpha, cudaStream_t s) {
@@ -1328,6 +1427,17 @@ int mgb_abc_mcmc_lg(const mgb_abc_lg_model *m, int64_t B, int64_t n, const uint3
       !keys || !x || !dist || !pp || !alpha || !(stepsize >= 0.0f))
     return ERR_BAD_ARG;
   MGB_ABC_DISPATCH(abc_mcmc_lg, m, B, n, keys, stepsize, threshold, x, dist, pp, alpha, (cudaStream_t)stream);
+}
+
+int mgb_abc_mcmc_rm_lg(const mgb_abc_lg_model *m, int64_t B, int64_t n, const uint32_t *keys, float target,
+                       float scale, float neg_exp, float *x, float *alpha, float *threshold, float *stepsize,
+                       void *stream) {
+  if (!m || !m->m0 || !m->C0 || !m->P0 || !m->H || !m->L || !m->data || B < 1 || B > 0x7FFFFFFFll || n < 1 ||
+      !keys || !x || !alpha || !threshold || !stepsize || !(target == target) || !(scale > 0.0f) ||
+      !(neg_exp >= 0.0f) || scale > 3.0e38f || neg_exp > 3.0e38f)
+    return ERR_BAD_ARG;
+  MGB_ABC_DISPATCH(abc_mcmc_rm_lg, m, B, n, keys, target, scale, neg_exp, x, alpha, threshold, stepsize,
+                   (cudaStream_t)stream);
 }
 
 int mgb_abc_gk_simulate(const mgb_abc_gk_model *m, int64_t P, const float *x, const uint32_t *keys, float *summary,

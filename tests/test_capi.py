@@ -129,6 +129,9 @@ def test_new_entry_points_reject_bad_arguments_on_host(L):
     assert need > 0
     assert L.mgb_abc_vanilla_lg(ctypes.byref(am), 1000, p, 1.0, -1.0, p, need - 1, p, p, p, p, p, null) == 4
     assert L.mgb_abc_mcmc_lg(ctypes.byref(am), 1, 100, p, -0.1, 1.0, p, p, p, p, null) == 1
+    # the adaptive chain: a non-positive Robbins-Monro scale, a negative exponent
+    assert L.mgb_abc_mcmc_rm_lg(ctypes.byref(am), 1, 100, p, 0.1, 0.0, 2.0 / 3.0, p, p, p, p, null) == 1
+    assert L.mgb_abc_mcmc_rm_lg(ctypes.byref(am), 1, 100, p, 0.1, 1.0, -1.0, p, p, p, p, null) == 1
 
 
 def test_score_entry_points_reject_bad_arguments_on_host(L):
