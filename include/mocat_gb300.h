@@ -777,6 +777,12 @@ int mgb_abc_mcmc_lg(const mgb_abc_lg_model *model_host, int64_t B, int64_t n, co
 int mgb_abc_mcmc_rm_lg(const mgb_abc_lg_model *model_host, int64_t B, int64_t n, const uint32_t *keys_dev,
                        float target, float scale, float neg_exp, float *x_dev, float *alpha_dev, float *threshold_dev,
                        float *stepsize_dev, void *stream);
+/* the same adaptive chain on a g-and-k scenario (model_host->data_dev required), one CTA per
+ * chain: x_0 = normal(split(key)[1], (d,)), prior potential 0.5 |x|^2, one g-and-k simulation
+ * per step; outputs as mgb_abc_mcmc_rm_lg (the reference's TestMCMCGK / TestMCMCGKOnlyA). */
+int mgb_abc_mcmc_rm_gk(const mgb_abc_gk_model *model_host, int64_t B, int64_t n, const uint32_t *keys_dev,
+                       float target, float scale, float neg_exp, float *x_dev, float *alpha_dev, float *threshold_dev,
+                       float *stepsize_dev, void *stream);
 size_t mgb_abc_vanilla_workspace(int64_t n);
 int mgb_abc_vanilla_lg(const mgb_abc_lg_model *model_host, int64_t n, const uint32_t *key_dev, float threshold,
                        float acceptance_rate, void *ws_dev, size_t ws_bytes, float *x_dev, float *prior_potential_dev,

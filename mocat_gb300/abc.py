@@ -369,7 +369,24 @@ def run_chains(scenario, sampler, n, random_keys, correction=None):
     chains, one per key.  With the Metropolis correction (correction=None): fixed stepsize and
     threshold; value (B, n, d), distance, prior_potential, alpha (B, n).  With
     correction=RMMetropolisDiagStepsize(): the adaptive chain from the sampler's defaults
-    (threshold and stepsize unset); value (B, n, d), alpha, threshold (B, n), stepsize (B, n, d)."""
+    (threshold and stepsize unset), on the linear-Gaussian or a g-and-k scenario (one CTA per
+    chain there); value (B, n, d), alpha, threshold (B, n), stepsize (B, n, d)."""
+    if isinstance(scenario, GKTransformedUniformPrior) and isinstance(correction, RMMetropolisDiagStepsize):
+        if sampler.stepsize is not None or sampler.threshold is not None:
+            raise NotImplementedError("the adaptive GPU chain starts from the sampler's defaults "
+                                      "(threshold and stepsize unset)")
+        if scenario.data is None or np.size(scenario.data) != scenario.num_thin:
+            raise ValueError("the g-and-k scenario needs data: num_thin summary values")
+        keys = _dev.as_key(random_keys).reshape(-1, 2).contiguous()
+        B, d, dev = keys.shape[0], scenario.dim, keys.device
+        data = torch.as_tensor(np.asarray(scenario.data, np.float32), device=dev).contiguous()
+        x = torch.empty((B, n, d), dtype=torch.float32, device=dev)
+        st = torch.empty((B, n, d), dtype=torch.float32, device=dev)
+        al, th = (torch.empty((B, n), dtype=torch.float32, device=dev) for _ in range(2))
+        call("mgb_abc_mcmc_rm_gk", ctypes.byref(scenario.model(_dev.ptr(data))), B, n, _dev.ptr(keys),
+             float(sampler.tuning.target), correction.rm_stepsize_scale, correction.rm_stepsize_neg_exponent,
+             _dev.ptr(x), _dev.ptr(al), _dev.ptr(th), _dev.ptr(st), _dev.stream_ptr())
+        return cdict(value=x, alpha=al, threshold=th, stepsize=st)
     if not isinstance(scenario, LinearGaussian):
         raise NotImplementedError(f"{scenario.__class__.__name__}: no GPU ABC-MCMC kernel for this scenario")
     if (scenario.dim, scenario.dim_obs) not in SUPPORTED:

@@ -635,28 +635,16 @@ __device__ __forceinline__ uint32_t gk_cx(uint32_t v, uint32_t o, int e, int kk,
 
 constexpr int GK_EPT = GK_MAX_RAW / GK_TPB;  // sort elements per thread at the largest length
 
-// one CTA per parameter row: n_raw draws, sort, thinned order statistics, distance.
+// One g-and-k simulation by the whole CTA (every thread calls it): n_raw draws of parameters qv
+// with key (k0, k1), sort, thinned order statistics into summary_row (when given) and, when
+// want_dist, the distance to the data, returned in thread 0.
 // Draws: element q and q + ceil(n_raw/2) of random_bits(key, (n_raw,)) are the two halves of one
 // cipher call.  Sort: a bitonic network over p2 keys in shared memory; the stages with partner
 // distance j < 32 run on warp shuffles (thread t holds elements t + 256 m, so e and e ^ j share
 // a warp), the others through shared memory.  Distance: the order statistics and their squared
 // differences are gathered in parallel, then summed in index order by one thread.
-__global__ void __launch_bounds__(GK_TPB) k_gk_sim(const GKP p, int64_t P, const float *__restrict__ x,
-                                                    const uint32_t *__restrict__ keys, const int32_t *mask,
-                                                    float *__restrict__ dist, float *__restrict__ summary) {
-  __shared__ uint32_t sk[GK_MAX_RAW];
-  __shared__ float q[4];
-  const int64_t r = blockIdx.x;
-  if (r >= P || (mask && !mask[r])) return;
-  if (threadIdx.x == 0) {
-    float qq[4];
-    gk_params(p, x + r * p.d, qq);
-#pragma unroll
-    for (int j = 0; j < 4; ++j) q[j] = qq[j];
-  }
-  __syncthreads();
-  const float qv[4] = {q[0], q[1], q[2], q[3]};
-  const uint32_t k0 = keys[2 * r], k1 = keys[2 * r + 1];
+__device__ float gk_sim_cta(const GKP &p, const float (&qv)[4], uint32_t k0, uint32_t k1, uint32_t *sk, bool want_dist,
+                            float *summary_row) {
   const int n_raw = p.n_raw, P2 = p.p2, t = threadIdx.x;
   const int h = (n_raw + 1) >> 1;
   for (int i = t; i < h; i += GK_TPB) {
@@ -716,20 +704,21 @@ __global__ void __launch_bounds__(GK_TPB) k_gk_sim(const GKP p, int64_t P, const
     const int j = t + GK_TPB * m;
     if (j < p.n_sum) {
       sv[m] = gk_unkey(sk[(int)(((uint32_t)j * (uint32_t)n_raw) / (uint32_t)p.n_sum)]);
-      if (dist) {
+      if (want_dist) {
         const float dv = __fsub_rn(sv[m], p.data[j]);
         dv2[m] = __fmul_rn(dv, dv);
       }
     }
   }
-  if (summary) {
+  if (summary_row) {
 #pragma unroll
     for (int m = 0; m < GK_EPT; ++m) {
       const int j = t + GK_TPB * m;
-      if (j < p.n_sum) summary[r * p.n_sum + j] = sv[m];
+      if (j < p.n_sum) summary_row[j] = sv[m];
     }
   }
-  if (dist) {
+  float dist = 0.0f;
+  if (want_dist) {
     __syncthreads();  // every rank read before sk is reused for the squared differences
     float *sd = reinterpret_cast<float *>(sk);
 #pragma unroll
@@ -742,9 +731,31 @@ __global__ void __launch_bounds__(GK_TPB) k_gk_sim(const GKP p, int64_t P, const
       float acc = sd[0];
 #pragma unroll 8
       for (int j = 1; j < p.n_sum; ++j) acc = __fadd_rn(acc, sd[j]);
-      dist[r] = __fsqrt_rn(acc);
+      dist = __fsqrt_rn(acc);
     }
   }
+  return dist;
+}
+
+// one CTA per parameter row
+__global__ void __launch_bounds__(GK_TPB) k_gk_sim(const GKP p, int64_t P, const float *__restrict__ x,
+                                                    const uint32_t *__restrict__ keys, const int32_t *mask,
+                                                    float *__restrict__ dist, float *__restrict__ summary) {
+  __shared__ uint32_t sk[GK_MAX_RAW];
+  __shared__ float q[4];
+  const int64_t r = blockIdx.x;
+  if (r >= P || (mask && !mask[r])) return;
+  if (threadIdx.x == 0) {
+    float qq[4];
+    gk_params(p, x + r * p.d, qq);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) q[j] = qq[j];
+  }
+  __syncthreads();
+  const float qv[4] = {q[0], q[1], q[2], q[3]};
+  const float dv = gk_sim_cta(p, qv, keys[2 * r], keys[2 * r + 1], sk, dist != nullptr,
+                              summary ? summary + r * p.n_sum : nullptr);
+  if (dist && threadIdx.x == 0) dist[r] = dv;
 }
 
 template <int D>
@@ -753,6 +764,106 @@ __device__ __forceinline__ float gk_prior_pot(const float (&x)[D]) {
 #pragma unroll
   for (int j = 1; j < D; ++j) s = __fadd_rn(s, __fmul_rn(x[j], x[j]));
   return __fmul_rn(0.5f, s);
+}
+
+// RandomWalkABC() with the RMMetropolisDiagStepsize correction on a g-and-k scenario, one CTA per
+// chain (the reference's TestMCMCGK / TestMCMCGKOnlyA): thread 0 holds the chain (keys, proposal,
+// Metropolis step and the Robbins-Monro updates of k_abc_mcmc_rm_lg); every step's simulation
+// runs on the whole CTA.  The prior is the transformed-uniform one: x_0 = normal(split(key)[1],
+// (d,)), potential 0.5 |x|^2.
+template <int D>
+__global__ void __launch_bounds__(GK_TPB) k_abc_mcmc_rm_gk(const GKP p, int64_t B, int64_t n, const uint32_t *keys,
+                                                            float target, float scale, float neg_exp,
+                                                            float *__restrict__ x_out, float *__restrict__ alpha_out,
+                                                            float *__restrict__ thr_out, float *__restrict__ st_out) {
+  __shared__ uint32_t sk[GK_MAX_RAW];
+  __shared__ float q_s[4];
+  __shared__ uint32_t ck[2];
+  const int64_t b = blockIdx.x;
+  if (b >= B) return;
+  const bool lead = threadIdx.x == 0;
+  float x[D], xp[D], st[D], pm[D], dg[D], pp = 0.0f, ppn = 0.0f, thr = 50.0f;
+  uint32_t K0 = 0, K1 = 0, n0 = 0, n1 = 0;
+  const int64_t base = b * n;
+  if (lead) {
+    uint32_t a0, a1, t0, t1;
+    K0 = keys[2 * b];
+    K1 = keys[2 * b + 1];
+    split_at(K0, K1, 2, 1, a0, a1);
+    split_at(K0, K1, 2, 0, t0, t1);
+    split_at(t0, t1, 2, 0, K0, K1);  // prior potential
+    uint32_t bits[D];
+    bits_vec<D>(a0, a1, bits, p.one);
+#pragma unroll
+    for (int j = 0; j < D; ++j) x[j] = bits_to_normal(bits[j]);
+    pp = gk_prior_pot<D>(x);
+    split_at(K0, K1, 2, 0, t0, t1);  // the initial simulation takes split(K)[1]; its distance is unused
+    K0 = t0;
+    K1 = t1;
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      st[j] = 1.0f;
+      pm[j] = x[j];
+      dg[j] = __fdiv_rn(__fmul_rn(st[j], (float)D), 5.6644f);
+      x_out[base * D + j] = x[j];
+      st_out[base * D + j] = st[j];
+    }
+    alpha_out[base] = 1.0f;
+    thr_out[base] = thr;
+  }
+#pragma unroll 1
+  for (int64_t i = 1; i < n; ++i) {
+    if (lead) {
+      uint32_t t0, t1;
+      split_at(K0, K1, 2, 0, t0, t1);  // always
+      uint32_t sk4[8];                 // split(t, 4): 0 new extra key, 1 proposal normals, 3 simulation
+      split4(t0, t1, sk4);
+      uint32_t bits[D];
+      bits_vec<D>(sk4[2], sk4[3], bits, p.one);
+#pragma unroll
+      for (int j = 0; j < D; ++j) xp[j] = __fadd_rn(x[j], __fmul_rn(__fsqrt_rn(st[j]), bits_to_normal(bits[j])));
+      ppn = gk_prior_pot<D>(xp);
+      float qq[4];
+      gk_params(p, xp, qq);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) q_s[j] = qq[j];
+      ck[0] = sk4[6];
+      ck[1] = sk4[7];
+      n0 = sk4[0];
+      n1 = sk4[1];
+    }
+    __syncthreads();
+    const float qv[4] = {q_s[0], q_s[1], q_s[2], q_s[3]};
+    const float dn = gk_sim_cta(p, qv, ck[0], ck[1], sk, true, nullptr);
+    if (lead) {
+      float a = __fmul_rn(expf_(__fsub_rn(pp, ppn)), dn < thr ? 1.0f : 0.0f);
+      a = a != a ? 0.0f : fminf(1.0f, a);
+      uint32_t u0, u1, v0, v1;
+      split2(n0, n1, u0, u1, v0, v1);
+      const float u = bits_to_unit(bits_at(v0, v1, 1, 0));
+      if (u < a) {
+#pragma unroll
+        for (int j = 0; j < D; ++j) x[j] = xp[j];
+        pp = ppn;
+      }
+      K0 = u0;
+      K1 = u1;
+      const float rm = __fmul_rn(scale, expf_(__fmul_rn(-neg_exp, logf_((float)i))));
+      thr = expf_(__fsub_rn(logf_(thr), __fmul_rn(rm, __fsub_rn(a, target))));
+      const float r2 = fminf(rm, 0.999f), q2 = __fsub_rn(1.0f, r2);
+#pragma unroll
+      for (int j = 0; j < D; ++j) {
+        const float dv = __fsub_rn(x[j], pm[j]);
+        dg[j] = __fadd_rn(__fmul_rn(q2, dg[j]), __fmul_rn(r2, __fmul_rn(dv, dv)));
+        pm[j] = __fadd_rn(__fmul_rn(q2, pm[j]), __fmul_rn(r2, x[j]));
+        st[j] = __fmul_rn(__fdiv_rn(dg[j], (float)D), 5.6644f);
+        x_out[(base + i) * D + j] = x[j];
+        st_out[(base + i) * D + j] = st[j];
+      }
+      alpha_out[base + i] = a;
+      thr_out[base + i] = thr;
+    }
+  }
 }
 
 // per-particle state of the split moves (the simulation is a CTA per particle)
@@ -1438,6 +1549,23 @@ int mgb_abc_mcmc_rm_lg(const mgb_abc_lg_model *m, int64_t B, int64_t n, const ui
     return ERR_BAD_ARG;
   MGB_ABC_DISPATCH(abc_mcmc_rm_lg, m, B, n, keys, target, scale, neg_exp, x, alpha, threshold, stepsize,
                    (cudaStream_t)stream);
+}
+
+int mgb_abc_mcmc_rm_gk(const mgb_abc_gk_model *m, int64_t B, int64_t n, const uint32_t *keys, float target,
+                       float scale, float neg_exp, float *x, float *alpha, float *threshold, float *stepsize,
+                       void *stream) {
+  if (!gk_ok(m) || !m->data_dev || B < 1 || B > 0x7FFFFFFFll || n < 1 || !keys || !x || !alpha || !threshold ||
+      !stepsize || !(target == target) || !(scale > 0.0f) || !(neg_exp >= 0.0f) || scale > 3.0e38f ||
+      neg_exp > 3.0e38f)
+    return ERR_BAD_ARG;
+  const GKP p = pack_gk(m);
+  if (m->d == 4)
+    k_abc_mcmc_rm_gk<4><<<(unsigned)B, GK_TPB, 0, (cudaStream_t)stream>>>(p, B, n, keys, target, scale, neg_exp, x,
+                                                                          alpha, threshold, stepsize);
+  else
+    k_abc_mcmc_rm_gk<1><<<(unsigned)B, GK_TPB, 0, (cudaStream_t)stream>>>(p, B, n, keys, target, scale, neg_exp, x,
+                                                                          alpha, threshold, stepsize);
+  return launch_status();
 }
 
 int mgb_abc_gk_simulate(const mgb_abc_gk_model *m, int64_t P, const float *x, const uint32_t *keys, float *summary,

@@ -168,6 +168,8 @@ def lib():
         L.o_gk_simulate.argtypes = [ctypes.POINTER(_GKModel), i64, f32p, u32p, vp, vp]
         L.o_abc_mcmc_rm_lg.argtypes = [ctypes.POINTER(_ABCModel), ctypes.c_int, u32p, ctypes.c_float, ctypes.c_float,
                                        ctypes.c_float, f32p, f32p, f32p, f32p]
+        L.o_abc_mcmc_rm_gk.argtypes = [ctypes.POINTER(_GKModel), ctypes.c_int, u32p, ctypes.c_float, ctypes.c_float,
+                                       ctypes.c_float, f32p, f32p, f32p, f32p]
         L.o_abc_mcmc_lg.argtypes = [ctypes.POINTER(_ABCModel), ctypes.c_int, u32p, ctypes.c_float, ctypes.c_float,
                                     f32p, f32p, f32p, f32p]
         for nm, mt in (("o_abc_vanilla_lg", _ABCModel), ("o_abc_vanilla_gk", _GKModel)):
@@ -730,6 +732,18 @@ def abc_mcmc_rm_lg(params, n, key, target=0.1, scale=1.0, neg_exp=2.0 / 3.0):
     x, st = np.empty((n, d), np.float32), np.empty((n, d), np.float32)
     al, th = np.empty(n, np.float32), np.empty(n, np.float32)
     lib().o_abc_mcmc_rm_lg(ctypes.byref(md), n, _u32(key), float(target), float(scale), float(np.float32(neg_exp)),
+                           x.reshape(-1), al, th, st.reshape(-1))
+    return dict(value=x, alpha=al, threshold=th, stepsize=st)
+
+
+def abc_mcmc_rm_gk(d, data, n, key, target=0.1, scale=1.0, neg_exp=2.0 / 3.0, n_raw=1000, n_sum=100):
+    """RandomWalkABC() with RMMetropolisDiagStepsize(rm_stepsize_scale=scale) on a g-and-k scenario
+    (d = 4 or 1, data: the n_sum summary values), one chain: dict(value (n, d), alpha, threshold (n),
+    stepsize (n, d))."""
+    s, keep = _gk_struct(d, n_raw, n_sum, data)
+    x, st = np.empty((n, d), np.float32), np.empty((n, d), np.float32)
+    al, th = np.empty(n, np.float32), np.empty(n, np.float32)
+    lib().o_abc_mcmc_rm_gk(ctypes.byref(s), n, _u32(key), float(target), float(scale), float(np.float32(neg_exp)),
                            x.reshape(-1), al, th, st.reshape(-1))
     return dict(value=x, alpha=al, threshold=th, stepsize=st)
 

@@ -1974,24 +1974,30 @@ void o_abc_mcmc_lg(const o_abc_model *md, int n, const uint32_t *key, float step
  *   r = min(rm, 1 - 1e-3); diag <- (1 - r) diag + r (x - post_mean)^2; post_mean <- (1 - r) post_mean + r x;
  *   stepsize <- diag / d * 2.38^2
  * Outputs per state: x (n, d), alpha (n), threshold (n), stepsize (n, d). */
-void o_abc_mcmc_rm_lg(const o_abc_model *md, int n, const uint32_t *key, float target, float scale, float neg_exp,
-                      float *x, float *alpha, float *thr_out, float *step_out)
+static void o_abc_mcmc_rm(const o_abc_model *md, const o_gk_model *gk, int n, const uint32_t *key, float target,
+                          float scale, float neg_exp, float *x, float *alpha, float *thr_out, float *step_out)
 {
-    const int d = md->d;
+    const int d = gk ? gk->d : md->d;
     uint32_t K0, K1, a0, a1, t0, t1;
     o_split_at(key[0], key[1], 2, 1, &a0, &a1);
     o_split_at(key[0], key[1], 2, 0, &t0, &t1);
     o_split_at(t0, t1, 2, 0, &K0, &K1);
     float e[16], xc[16] = {0.0f}, xp[16] = {0.0f}, st[16], pm[16], dg[16];
     o_normal_vec(a0, a1, d, e);
-    for (int r = 0; r < d; ++r) {
-        float v = md->C0[r * d] * e[0];
-        for (int k = 1; k < d; ++k) v = fmaf(md->C0[r * d + k], e[k], v);
-        xc[r] = md->m0[r] + v;
+    float p;
+    if (gk) {
+        /* the transformed-uniform prior: x_0 = the normal draw itself, potential 0.5 |x|^2 */
+        for (int r = 0; r < d; ++r) xc[r] = e[r];
+        p = o_gk_prior_pot(d, xc);
+    } else {
+        for (int r = 0; r < d; ++r) {
+            float v = md->C0[r * d] * e[0];
+            for (int k = 1; k < d; ++k) v = fmaf(md->C0[r * d + k], e[k], v);
+            xc[r] = md->m0[r] + v;
+        }
+        p = o_abc_prior_pot(md, xc);
     }
-    float p = o_abc_prior_pot(md, xc);
-    o_split_at(K0, K1, 2, 1, &a0, &a1);
-    float ds = o_abc_sim_dist(md, xc, a0, a1);
+    /* the initial simulation takes split(K)[1]; the adaptive chain does not use its distance */
     o_split_at(K0, K1, 2, 0, &t0, &t1);
     K0 = t0; K1 = t1;
     float thr = 50.0f;
@@ -2003,7 +2009,6 @@ void o_abc_mcmc_rm_lg(const o_abc_model *md, int n, const uint32_t *key, float t
     memcpy(x, xc, sizeof(float) * d);
     memcpy(step_out, st, sizeof(float) * d);
     alpha[0] = 1.0f; thr_out[0] = thr;
-    (void)ds;
     for (int i = 1; i < n; ++i) {
         uint32_t n0, n1, c0, c1, u0, u1, v0, v1;
         o_split_at(K0, K1, 2, 0, &t0, &t1);
@@ -2012,8 +2017,8 @@ void o_abc_mcmc_rm_lg(const o_abc_model *md, int n, const uint32_t *key, float t
         o_split_at(t0, t1, 4, 3, &c0, &c1);
         o_normal_vec(a0, a1, d, e);
         for (int j = 0; j < d; ++j) xp[j] = xc[j] + sqrtf(st[j]) * e[j];
-        const float ppn = o_abc_prior_pot(md, xp);
-        const float dn = o_abc_sim_dist(md, xp, c0, c1);
+        const float ppn = gk ? o_gk_prior_pot(d, xp) : o_abc_prior_pot(md, xp);
+        const float dn = gk ? o_gk_sim(gk, xp, c0, c1, NULL) : o_abc_sim_dist(md, xp, c0, c1);
         float a = o_expf(p - ppn) * (dn < thr ? 1.0f : 0.0f);
         a = a != a ? 0.0f : fminf(1.0f, a);
         o_split_at(n0, n1, 2, 0, &u0, &u1);
@@ -2022,7 +2027,6 @@ void o_abc_mcmc_rm_lg(const o_abc_model *md, int n, const uint32_t *key, float t
         if (u < a) {
             memcpy(xc, xp, sizeof(float) * d);
             p = ppn;
-            ds = dn;
         }
         K0 = u0; K1 = u1;
         const float rm = scale * o_expf(-neg_exp * o_logf((float)i));
@@ -2038,6 +2042,21 @@ void o_abc_mcmc_rm_lg(const o_abc_model *md, int n, const uint32_t *key, float t
         memcpy(step_out + (size_t)i * d, st, sizeof(float) * d);
         alpha[i] = a; thr_out[i] = thr;
     }
+}
+
+void o_abc_mcmc_rm_lg(const o_abc_model *md, int n, const uint32_t *key, float target, float scale, float neg_exp,
+                      float *x, float *alpha, float *thr_out, float *step_out)
+{
+    o_abc_mcmc_rm(md, NULL, n, key, target, scale, neg_exp, x, alpha, thr_out, step_out);
+}
+
+/* the same adaptive chain on a g-and-k scenario (the reference's TestMCMCGK / TestMCMCGKOnlyA):
+ * prior draws x_0 = normal(split(key)[1], (d,)), prior potential 0.5 |x|^2, one g-and-k
+ * simulation per step */
+void o_abc_mcmc_rm_gk(const o_gk_model *gk, int n, const uint32_t *key, float target, float scale, float neg_exp,
+                      float *x, float *alpha, float *thr_out, float *step_out)
+{
+    o_abc_mcmc_rm(NULL, gk, n, key, target, scale, neg_exp, x, alpha, thr_out, step_out);
 }
 
 /* the same sampler on a g-and-k scenario */

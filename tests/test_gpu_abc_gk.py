@@ -2,7 +2,8 @@
 mgb_abc_gk_*) vs the oracle: summaries of the simulator bit for bit, and the whole
 MetropolisedABCSMCSampler run (particles, distances, log-weights, stepsizes, every
 iteration's threshold, ESS, acceptance and resampling flag) bit for bit for B posteriors;
-and the reference's own check (tests/test_abc_gk.py TestMetSMCGK / TestMetSMCGKOnlyA)."""
+the adaptive RandomWalkABC chain bit for bit; and the reference's own checks
+(tests/test_abc_gk.py TestMetSMCGK / TestMetSMCGKOnlyA, TestMCMCGK / TestMCMCGKOnlyA)."""
 import numpy as np
 import pytest
 import torch
@@ -75,3 +76,41 @@ def test_reference_check(cuda, onlyA, mode):
         smp = mg.abc.MetropolisedABCSMCSampler(ess_threshold_retain=0.8, termination_alpha=0.1)
     out = mg.abc.run(sc, smp, 1000, mg.random.PRNGKey(0))
     assert np.abs(true_u - out.value[-1].double().cpu().numpy().mean(0)).sum() < 3.0
+
+
+@pytest.mark.parametrize("onlyA", [False, True])
+def test_rm_chain_matches_oracle(cuda, onlyA):
+    """RandomWalkABC() with RMMetropolisDiagStepsize on g-and-k (mgb_abc_mcmc_rm_gk, one CTA per
+    chain): states, acceptance probabilities, thresholds and stepsizes of two chains equal the
+    oracle's bit for bit"""
+    import mocat_gb300 as mg
+    d = 1 if onlyA else 4
+    true_u = _unconstrain(TRUE1 if onlyA else TRUE4).astype(np.float32)
+    data, _ = O.gk_simulate(true_u[None], O.PRNGKey(0)[None], d)
+    sc = _scenario(onlyA, data=data[0])
+    keys = np.stack([O.PRNGKey(31), O.PRNGKey(32)])
+    smp = mg.abc.RandomWalkABC()
+    scale = 0.1 if onlyA else 0.01
+    out = mg.abc.run_chains(sc, smp, 300, keys, correction=mg.abc.RMMetropolisDiagStepsize(rm_stepsize_scale=scale))
+    for b in range(2):
+        ref = O.abc_mcmc_rm_gk(d, data[0], 300, keys[b], 0.1, scale)
+        for k in ("value", "alpha", "threshold", "stepsize"):
+            assert np.array_equal(getattr(out, k)[b].cpu().numpy(), ref[k]), k
+
+
+@pytest.mark.parametrize("onlyA", [False, True])
+def test_reference_mcmc_adaptive_diag_stepsize(cuda, onlyA):
+    """TestMCMCGK / TestMCMCGKOnlyA.test_adaptive_diag_stepsize: n = 1e5 steps of RandomWalkABC() with
+    RMMetropolisDiagStepsize(rm_stepsize_scale=0.01 (0.1 for A only)), target 0.1: |true - mean|_1 < 3
+    and the mean acceptance 0.1 to one decimal"""
+    import mocat_gb300 as mg
+    true_u = _unconstrain(TRUE1 if onlyA else TRUE4).astype(np.float32)
+    sc = _scenario(onlyA)
+    sc.data = sc.likelihood_sample(true_u, mg.random.PRNGKey(0)).cpu().numpy()
+    smp = mg.abc.RandomWalkABC()
+    smp.tuning.target = 0.1
+    corr = mg.abc.RMMetropolisDiagStepsize(rm_stepsize_scale=0.1 if onlyA else 0.01)
+    out = mg.abc.run(sc, smp, 100000, mg.random.PRNGKey(0), correction=corr)
+    assert out.value.shape == (100000, 1 if onlyA else 4)
+    assert np.abs(true_u - out.value.double().cpu().numpy().mean(0)).sum() < 3.0
+    np.testing.assert_almost_equal(float(out.alpha.double().mean()), 0.1, decimal=1)

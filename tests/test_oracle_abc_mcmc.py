@@ -139,3 +139,14 @@ def test_rm_reference_check():
     np.testing.assert_almost_equal(out["alpha"].mean(), 0.1, decimal=1)
     np.testing.assert_array_almost_equal(out["stepsize"][-1], np.diag(np.cov(x, rowvar=False)) / 3 * 2.38 ** 2,
                                          decimal=1)
+
+
+def test_rm_gk_oracle_adapts():
+    """the g-and-k adaptive chain (o_abc_mcmc_rm_gk) on a short run: finite states, the threshold
+    moves off its start of 50 and every stepsize stays positive"""
+    from test_oracle_abc_gk import TRUE4, _unconstrain
+    true_u = _unconstrain(TRUE4).astype(np.float32)
+    data, _ = O.gk_simulate(true_u[None], O.PRNGKey(0)[None], 4)
+    out = O.abc_mcmc_rm_gk(4, data[0], 200, O.PRNGKey(3), 0.1, 0.01)
+    assert np.isfinite(out["value"]).all() and (out["stepsize"] > 0).all()
+    assert out["threshold"][0] == 50.0 and out["threshold"][-1] != 50.0
