@@ -777,6 +777,12 @@ int mgb_abc_mcmc_lg(const mgb_abc_lg_model *model_host, int64_t B, int64_t n, co
 int mgb_abc_mcmc_rm_lg(const mgb_abc_lg_model *model_host, int64_t B, int64_t n, const uint32_t *keys_dev,
                        float target, float scale, float neg_exp, float *x_dev, float *alpha_dev, float *threshold_dev,
                        float *stepsize_dev, void *stream);
+/* RandomWalkABC(stepsize, threshold) chains on a g-and-k scenario (model_host->data_dev required),
+ * one CTA per chain: x_0 = normal(split(key)[1], (d,)), prior potential 0.5 |x|^2, the key chain and
+ * Metropolis step of mgb_abc_mcmc_lg; x (B, n, d), distance, prior_potential, alpha (B, n). */
+int mgb_abc_mcmc_gk(const mgb_abc_gk_model *model_host, int64_t B, int64_t n, const uint32_t *keys_dev, float stepsize,
+                    float threshold, float *x_dev, float *distance_dev, float *prior_potential_dev, float *alpha_dev,
+                    void *stream);
 /* the same adaptive chain on a g-and-k scenario (model_host->data_dev required), one CTA per
  * chain: x_0 = normal(split(key)[1], (d,)), prior potential 0.5 |x|^2, one g-and-k simulation
  * per step; outputs as mgb_abc_mcmc_rm_lg (the reference's TestMCMCGK / TestMCMCGKOnlyA). */

@@ -208,6 +208,7 @@ _SIGNATURES = {
     "mgb_abc_mcmc_lg": ([ctypes.POINTER(ABCModel), _I64, _I64, _P, _F, _F, _P, _P, _P, _P, _P], _I32),
     "mgb_abc_mcmc_rm_lg": ([ctypes.POINTER(ABCModel), _I64, _I64, _P, _F, _F, _F, _P, _P, _P, _P, _P], _I32),
     "mgb_abc_mcmc_rm_gk": ([ctypes.POINTER(GKModel), _I64, _I64, _P, _F, _F, _F, _P, _P, _P, _P, _P], _I32),
+    "mgb_abc_mcmc_gk": ([ctypes.POINTER(GKModel), _I64, _I64, _P, _F, _F, _P, _P, _P, _P, _P], _I32),
     "mgb_abc_vanilla_workspace": ([_I64], _SZ),
     "mgb_abc_vanilla_lg": ([ctypes.POINTER(ABCModel), _I64, _P, _F, _F, _P, _SZ, _P, _P, _P, _P, _P, _P], _I32),
     "mgb_abc_vanilla_gk": ([ctypes.POINTER(GKModel), _I64, _P, _F, _F, _P, _SZ, _P, _P, _P, _P, _P, _P], _I32),

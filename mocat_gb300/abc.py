@@ -364,29 +364,46 @@ def run_batched(scenario, sampler, n, random_keys, chain=False):
     return BatchedABCSMC(scenario, sampler, n, random_keys).run(chain)
 
 
+def _gk_chains(scenario, sampler, n, random_keys, correction):
+    """RandomWalkABC chains on a g-and-k scenario, one CTA per chain (run_chains)"""
+    rm = isinstance(correction, RMMetropolisDiagStepsize)
+    name = getattr(correction, "__name__", type(correction).__name__)
+    if not rm and correction is not None and correction != "Metropolis" and name != "Metropolis":
+        raise NotImplementedError(f"{name}: no GPU chain for this correction")
+    if scenario.data is None or np.size(scenario.data) != scenario.num_thin:
+        raise ValueError("the g-and-k scenario needs data: num_thin summary values")
+    keys = _dev.as_key(random_keys).reshape(-1, 2).contiguous()
+    B, d, dev = keys.shape[0], scenario.dim, keys.device
+    data = torch.as_tensor(np.asarray(scenario.data, np.float32), device=dev).contiguous()
+    model = scenario.model(_dev.ptr(data))
+    x = torch.empty((B, n, d), dtype=torch.float32, device=dev)
+    if rm:
+        if sampler.stepsize is not None or sampler.threshold is not None:
+            raise NotImplementedError("the adaptive GPU chain starts from the sampler's defaults "
+                                      "(threshold and stepsize unset)")
+        st = torch.empty((B, n, d), dtype=torch.float32, device=dev)
+        al, th = (torch.empty((B, n), dtype=torch.float32, device=dev) for _ in range(2))
+        call("mgb_abc_mcmc_rm_gk", ctypes.byref(model), B, n, _dev.ptr(keys), float(sampler.tuning.target),
+             correction.rm_stepsize_scale, correction.rm_stepsize_neg_exponent, _dev.ptr(x), _dev.ptr(al),
+             _dev.ptr(th), _dev.ptr(st), _dev.stream_ptr())
+        return cdict(value=x, alpha=al, threshold=th, stepsize=st)
+    if sampler.stepsize is None or sampler.threshold is None:
+        raise NotImplementedError("RandomWalkABC chains need a fixed stepsize and threshold")
+    dist, pp, al = (torch.empty((B, n), dtype=torch.float32, device=dev) for _ in range(3))
+    call("mgb_abc_mcmc_gk", ctypes.byref(model), B, n, _dev.ptr(keys), float(sampler.stepsize),
+         float(sampler.threshold), _dev.ptr(x), _dev.ptr(dist), _dev.ptr(pp), _dev.ptr(al), _dev.stream_ptr())
+    return cdict(value=x, distance=dist, prior_potential=pp, alpha=al)
+
+
 def run_chains(scenario, sampler, n, random_keys, correction=None):
     """RandomWalkABC run as an MCMC sampler (abc/mcmc.py:16-100, mocat.run) for B independent
     chains, one per key.  With the Metropolis correction (correction=None): fixed stepsize and
     threshold; value (B, n, d), distance, prior_potential, alpha (B, n).  With
     correction=RMMetropolisDiagStepsize(): the adaptive chain from the sampler's defaults
-    (threshold and stepsize unset), on the linear-Gaussian or a g-and-k scenario (one CTA per
-    chain there); value (B, n, d), alpha, threshold (B, n), stepsize (B, n, d)."""
-    if isinstance(scenario, GKTransformedUniformPrior) and isinstance(correction, RMMetropolisDiagStepsize):
-        if sampler.stepsize is not None or sampler.threshold is not None:
-            raise NotImplementedError("the adaptive GPU chain starts from the sampler's defaults "
-                                      "(threshold and stepsize unset)")
-        if scenario.data is None or np.size(scenario.data) != scenario.num_thin:
-            raise ValueError("the g-and-k scenario needs data: num_thin summary values")
-        keys = _dev.as_key(random_keys).reshape(-1, 2).contiguous()
-        B, d, dev = keys.shape[0], scenario.dim, keys.device
-        data = torch.as_tensor(np.asarray(scenario.data, np.float32), device=dev).contiguous()
-        x = torch.empty((B, n, d), dtype=torch.float32, device=dev)
-        st = torch.empty((B, n, d), dtype=torch.float32, device=dev)
-        al, th = (torch.empty((B, n), dtype=torch.float32, device=dev) for _ in range(2))
-        call("mgb_abc_mcmc_rm_gk", ctypes.byref(scenario.model(_dev.ptr(data))), B, n, _dev.ptr(keys),
-             float(sampler.tuning.target), correction.rm_stepsize_scale, correction.rm_stepsize_neg_exponent,
-             _dev.ptr(x), _dev.ptr(al), _dev.ptr(th), _dev.ptr(st), _dev.stream_ptr())
-        return cdict(value=x, alpha=al, threshold=th, stepsize=st)
+    (threshold and stepsize unset); value (B, n, d), alpha, threshold (B, n), stepsize (B, n, d).
+    Linear-Gaussian and g-and-k scenarios (one CTA per chain on g-and-k)."""
+    if isinstance(scenario, GKTransformedUniformPrior):
+        return _gk_chains(scenario, sampler, n, random_keys, correction)
     if not isinstance(scenario, LinearGaussian):
         raise NotImplementedError(f"{scenario.__class__.__name__}: no GPU ABC-MCMC kernel for this scenario")
     if (scenario.dim, scenario.dim_obs) not in SUPPORTED:

@@ -866,6 +866,106 @@ __global__ void __launch_bounds__(GK_TPB) k_abc_mcmc_rm_gk(const GKP p, int64_t 
   }
 }
 
+// RandomWalkABC(stepsize, threshold) on a g-and-k scenario (the Metropolis correction), one CTA
+// per chain: the key chain and Metropolis step of k_abc_mcmc_lg with the transformed-uniform
+// prior, every simulation (the initial one included) on the whole CTA
+template <int D>
+__global__ void __launch_bounds__(GK_TPB) k_abc_mcmc_gk(const GKP p, int64_t B, int64_t n, const uint32_t *keys,
+                                                         float stepsize, float thr, float *__restrict__ x_out,
+                                                         float *__restrict__ dist_out, float *__restrict__ pp_out,
+                                                         float *__restrict__ alpha_out) {
+  __shared__ uint32_t sk[GK_MAX_RAW];
+  __shared__ float q_s[4];
+  __shared__ uint32_t ck[2];
+  const int64_t b = blockIdx.x;
+  if (b >= B) return;
+  const bool lead = threadIdx.x == 0;
+  const float sq = __fsqrt_rn(stepsize);
+  float x[D], xp[D], pp = 0.0f, ppn = 0.0f, dist = 0.0f;
+  uint32_t K0 = 0, K1 = 0, n0 = 0, n1 = 0;
+  const int64_t base = b * n;
+  if (lead) {
+    uint32_t a0, a1, t0, t1;
+    K0 = keys[2 * b];
+    K1 = keys[2 * b + 1];
+    split_at(K0, K1, 2, 1, a0, a1);
+    split_at(K0, K1, 2, 0, t0, t1);
+    split_at(t0, t1, 2, 0, K0, K1);  // prior potential
+    uint32_t bits[D];
+    bits_vec<D>(a0, a1, bits, p.one);
+#pragma unroll
+    for (int j = 0; j < D; ++j) x[j] = bits_to_normal(bits[j]);
+    pp = gk_prior_pot<D>(x);
+    float qq[4];
+    gk_params(p, x, qq);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) q_s[j] = qq[j];
+    split2(K0, K1, t0, t1, a0, a1);  // split(K): [0] the chain key, [1] the initial simulation
+    ck[0] = a0;
+    ck[1] = a1;
+    K0 = t0;
+    K1 = t1;
+  }
+  __syncthreads();
+  {
+    const float qv[4] = {q_s[0], q_s[1], q_s[2], q_s[3]};
+    const float d0 = gk_sim_cta(p, qv, ck[0], ck[1], sk, true, nullptr);
+    if (lead) {
+      dist = d0;
+#pragma unroll
+      for (int j = 0; j < D; ++j) x_out[base * D + j] = x[j];
+      dist_out[base] = dist;
+      pp_out[base] = pp;
+      alpha_out[base] = 1.0f;
+    }
+  }
+#pragma unroll 1
+  for (int64_t i = 1; i < n; ++i) {
+    if (lead) {
+      uint32_t t0, t1;
+      split_at(K0, K1, 2, 0, t0, t1);  // always
+      uint32_t sk4[8];                 // split(t, 4): 0 new extra key, 1 proposal normals, 3 simulation
+      split4(t0, t1, sk4);
+      uint32_t bits[D];
+      bits_vec<D>(sk4[2], sk4[3], bits, p.one);
+#pragma unroll
+      for (int j = 0; j < D; ++j) xp[j] = __fadd_rn(x[j], __fmul_rn(sq, bits_to_normal(bits[j])));
+      ppn = gk_prior_pot<D>(xp);
+      float qq[4];
+      gk_params(p, xp, qq);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) q_s[j] = qq[j];
+      ck[0] = sk4[6];
+      ck[1] = sk4[7];
+      n0 = sk4[0];
+      n1 = sk4[1];
+    }
+    __syncthreads();
+    const float qv[4] = {q_s[0], q_s[1], q_s[2], q_s[3]};
+    const float dn = gk_sim_cta(p, qv, ck[0], ck[1], sk, true, nullptr);
+    if (lead) {
+      float a = __fmul_rn(expf_(__fsub_rn(pp, ppn)), dn < thr ? 1.0f : 0.0f);
+      a = a != a ? 0.0f : fminf(1.0f, a);
+      uint32_t u0, u1, v0, v1;
+      split2(n0, n1, u0, u1, v0, v1);
+      const float u = bits_to_unit(bits_at(v0, v1, 1, 0));
+      if (u < a) {
+#pragma unroll
+        for (int j = 0; j < D; ++j) x[j] = xp[j];
+        pp = ppn;
+        dist = dn;
+      }
+      K0 = u0;
+      K1 = u1;
+#pragma unroll
+      for (int j = 0; j < D; ++j) x_out[(base + i) * D + j] = x[j];
+      dist_out[base + i] = dist;
+      pp_out[base + i] = pp;
+      alpha_out[base + i] = a;
+    }
+  }
+}
+
 // per-particle state of the split moves (the simulation is a CTA per particle)
 struct GKWs {
   float *xp;        // (B N, d) proposals
@@ -1549,6 +1649,21 @@ int mgb_abc_mcmc_rm_lg(const mgb_abc_lg_model *m, int64_t B, int64_t n, const ui
     return ERR_BAD_ARG;
   MGB_ABC_DISPATCH(abc_mcmc_rm_lg, m, B, n, keys, target, scale, neg_exp, x, alpha, threshold, stepsize,
                    (cudaStream_t)stream);
+}
+
+int mgb_abc_mcmc_gk(const mgb_abc_gk_model *m, int64_t B, int64_t n, const uint32_t *keys, float stepsize,
+                    float threshold, float *x, float *dist, float *pp, float *alpha, void *stream) {
+  if (!gk_ok(m) || !m->data_dev || B < 1 || B > 0x7FFFFFFFll || n < 1 || !keys || !x || !dist || !pp || !alpha ||
+      !(stepsize >= 0.0f))
+    return ERR_BAD_ARG;
+  const GKP p = pack_gk(m);
+  if (m->d == 4)
+    k_abc_mcmc_gk<4><<<(unsigned)B, GK_TPB, 0, (cudaStream_t)stream>>>(p, B, n, keys, stepsize, threshold, x, dist,
+                                                                       pp, alpha);
+  else
+    k_abc_mcmc_gk<1><<<(unsigned)B, GK_TPB, 0, (cudaStream_t)stream>>>(p, B, n, keys, stepsize, threshold, x, dist,
+                                                                       pp, alpha);
+  return launch_status();
 }
 
 int mgb_abc_mcmc_rm_gk(const mgb_abc_gk_model *m, int64_t B, int64_t n, const uint32_t *keys, float target,

@@ -172,6 +172,8 @@ def lib():
                                        ctypes.c_float, f32p, f32p, f32p, f32p]
         L.o_abc_mcmc_lg.argtypes = [ctypes.POINTER(_ABCModel), ctypes.c_int, u32p, ctypes.c_float, ctypes.c_float,
                                     f32p, f32p, f32p, f32p]
+        L.o_abc_mcmc_gk.argtypes = [ctypes.POINTER(_GKModel), ctypes.c_int, u32p, ctypes.c_float, ctypes.c_float,
+                                    f32p, f32p, f32p, f32p]
         for nm, mt in (("o_abc_vanilla_lg", _ABCModel), ("o_abc_vanilla_gk", _GKModel)):
             getattr(L, nm).argtypes = [ctypes.POINTER(mt), ctypes.c_int, u32p, ctypes.c_float, ctypes.c_float, f32p,
                                        f32p, f32p, f32p]
@@ -734,6 +736,16 @@ def abc_mcmc_rm_lg(params, n, key, target=0.1, scale=1.0, neg_exp=2.0 / 3.0):
     lib().o_abc_mcmc_rm_lg(ctypes.byref(md), n, _u32(key), float(target), float(scale), float(np.float32(neg_exp)),
                            x.reshape(-1), al, th, st.reshape(-1))
     return dict(value=x, alpha=al, threshold=th, stepsize=st)
+
+
+def abc_mcmc_gk(d, data, n, key, stepsize, threshold, n_raw=1000, n_sum=100):
+    """RandomWalkABC(stepsize, threshold) on a g-and-k scenario, one chain: dict(value (n, d),
+    distance, prior_potential, alpha (n))."""
+    s, keep = _gk_struct(d, n_raw, n_sum, data)
+    x = np.empty((n, d), np.float32)
+    dist, pp, al = (np.empty(n, np.float32) for _ in range(3))
+    lib().o_abc_mcmc_gk(ctypes.byref(s), n, _u32(key), float(stepsize), float(threshold), x.reshape(-1), dist, pp, al)
+    return dict(value=x, distance=dist, prior_potential=pp, alpha=al)
 
 
 def abc_mcmc_rm_gk(d, data, n, key, target=0.1, scale=1.0, neg_exp=2.0 / 3.0, n_raw=1000, n_sum=100):

@@ -1916,24 +1916,30 @@ float o_abc_vanilla_gk(const o_gk_model *gk, int n, const uint32_t *key, float t
  * per step (K, _) = split(K); (K, k1, k2, k3) = split(K, 4); x' = x + sqrt(stepsize) normal(k1);
  * alpha = min(1, exp(pp - pp') [dist' < threshold]) (NaN -> 0); (K, ku) = split(K); accept if
  * uniform(ku) < alpha.  x (n, d), dist, pp, alpha (n). */
-void o_abc_mcmc_lg(const o_abc_model *md, int n, const uint32_t *key, float stepsize, float thr, float *x, float *dist,
-                   float *pp, float *alpha)
+static void o_abc_mcmc(const o_abc_model *md, const o_gk_model *gk, int n, const uint32_t *key, float stepsize,
+                       float thr, float *x, float *dist, float *pp, float *alpha)
 {
-    const int d = md->d;
+    const int d = gk ? gk->d : md->d;
     uint32_t K0, K1, a0, a1, t0, t1;
     o_split_at(key[0], key[1], 2, 1, &a0, &a1);
     o_split_at(key[0], key[1], 2, 0, &t0, &t1);
     o_split_at(t0, t1, 2, 0, &K0, &K1);
-    float e[16], xc[16], xp[16] = {0.0f};
+    float e[16], xc[16] = {0.0f}, xp[16] = {0.0f};
     o_normal_vec(a0, a1, d, e);
-    for (int r = 0; r < d; ++r) {
-        float v = md->C0[r * d] * e[0];
-        for (int k = 1; k < d; ++k) v = fmaf(md->C0[r * d + k], e[k], v);
-        xc[r] = md->m0[r] + v;
+    float p;
+    if (gk) {
+        for (int r = 0; r < d; ++r) xc[r] = e[r];
+        p = o_gk_prior_pot(d, xc);
+    } else {
+        for (int r = 0; r < d; ++r) {
+            float v = md->C0[r * d] * e[0];
+            for (int k = 1; k < d; ++k) v = fmaf(md->C0[r * d + k], e[k], v);
+            xc[r] = md->m0[r] + v;
+        }
+        p = o_abc_prior_pot(md, xc);
     }
-    float p = o_abc_prior_pot(md, xc);
     o_split_at(K0, K1, 2, 1, &a0, &a1);
-    float ds = o_abc_sim_dist(md, xc, a0, a1);
+    float ds = gk ? o_gk_sim(gk, xc, a0, a1, NULL) : o_abc_sim_dist(md, xc, a0, a1);
     o_split_at(K0, K1, 2, 0, &t0, &t1);
     K0 = t0; K1 = t1;
     const float sq = sqrtf(stepsize);
@@ -1947,8 +1953,8 @@ void o_abc_mcmc_lg(const o_abc_model *md, int n, const uint32_t *key, float step
         o_split_at(t0, t1, 4, 3, &c0, &c1);
         o_normal_vec(a0, a1, d, e);
         for (int j = 0; j < d; ++j) xp[j] = xc[j] + sq * e[j];
-        const float ppn = o_abc_prior_pot(md, xp);
-        const float dn = o_abc_sim_dist(md, xp, c0, c1);
+        const float ppn = gk ? o_gk_prior_pot(d, xp) : o_abc_prior_pot(md, xp);
+        const float dn = gk ? o_gk_sim(gk, xp, c0, c1, NULL) : o_abc_sim_dist(md, xp, c0, c1);
         float a = o_expf(p - ppn) * (dn < thr ? 1.0f : 0.0f);
         a = a != a ? 0.0f : fminf(1.0f, a);
         o_split_at(n0, n1, 2, 0, &u0, &u1);
@@ -1963,6 +1969,19 @@ void o_abc_mcmc_lg(const o_abc_model *md, int n, const uint32_t *key, float step
         memcpy(x + (size_t)i * d, xc, sizeof(float) * d);
         dist[i] = ds; pp[i] = p; alpha[i] = a;
     }
+}
+
+void o_abc_mcmc_lg(const o_abc_model *md, int n, const uint32_t *key, float stepsize, float thr, float *x, float *dist,
+                   float *pp, float *alpha)
+{
+    o_abc_mcmc(md, NULL, n, key, stepsize, thr, x, dist, pp, alpha);
+}
+
+/* the same fixed chain on a g-and-k scenario: x_0 = normal(split(key)[1], (d,)), potential 0.5 |x|^2 */
+void o_abc_mcmc_gk(const o_gk_model *gk, int n, const uint32_t *key, float stepsize, float thr, float *x, float *dist,
+                   float *pp, float *alpha)
+{
+    o_abc_mcmc(NULL, gk, n, key, stepsize, thr, x, dist, pp, alpha);
 }
 
 /* RandomWalkABC with the RMMetropolisDiagStepsize correction (abc/mcmc.py:105-140,

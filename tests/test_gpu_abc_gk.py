@@ -114,3 +114,24 @@ def test_reference_mcmc_adaptive_diag_stepsize(cuda, onlyA):
     assert out.value.shape == (100000, 1 if onlyA else 4)
     assert np.abs(true_u - out.value.double().cpu().numpy().mean(0)).sum() < 3.0
     np.testing.assert_almost_equal(float(out.alpha.double().mean()), 0.1, decimal=1)
+
+
+@pytest.mark.parametrize("onlyA", [False, True])
+def test_fixed_chain_matches_oracle(cuda, onlyA):
+    """RandomWalkABC(stepsize, threshold) on g-and-k (mgb_abc_mcmc_gk, one CTA per chain): states,
+    distances, prior potentials and acceptance probabilities of two chains equal the oracle's"""
+    import mocat_gb300 as mg
+    d = 1 if onlyA else 4
+    true_u = _unconstrain(TRUE1 if onlyA else TRUE4).astype(np.float32)
+    data, _ = O.gk_simulate(true_u[None], O.PRNGKey(0)[None], d)
+    sc = _scenario(onlyA, data=data[0])
+    keys = np.stack([O.PRNGKey(41), O.PRNGKey(42)])
+    thr = 50.0
+    out = mg.abc.run_chains(sc, mg.abc.RandomWalkABC(stepsize=0.05, threshold=thr), 300, keys)
+    accepted = 0
+    for b in range(2):
+        ref = O.abc_mcmc_gk(d, data[0], 300, keys[b], 0.05, thr)
+        accepted += int((ref["alpha"][1:] > 0).sum())
+        for k in ("value", "distance", "prior_potential", "alpha"):
+            assert np.array_equal(getattr(out, k)[b].cpu().numpy(), ref[k]), k
+    assert accepted > 100  # the chains move
