@@ -626,13 +626,6 @@ __device__ __forceinline__ float gk_unkey(uint32_t k) {
   return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
 }
 
-// compare-exchange of bitonic stage (kk, j) for element e holding v, partner value o:
-// the lower index of an ascending (e & kk == 0) pair keeps the minimum
-__device__ __forceinline__ uint32_t gk_cx(uint32_t v, uint32_t o, int e, int kk, int j) {
-  const bool keep_min = ((e & j) == 0) == ((e & kk) == 0);
-  return keep_min ? min(v, o) : max(v, o);
-}
-
 constexpr int GK_EPT = GK_MAX_RAW / GK_TPB;  // sort elements per thread at the largest length
 
 // One g-and-k simulation by the whole CTA (every thread calls it): n_raw draws of parameters qv
@@ -659,32 +652,36 @@ __device__ float gk_sim_cta(const GKP &p, const float (&qv)[4], uint32_t k0, uin
   for (int kk = 2; kk <= P2; kk <<= 1) {
     int j = kk >> 1;
     for (; j >= 32; j >>= 1) {
-      for (int i = t; i < P2; i += GK_TPB) {
-        const int ixj = i ^ j;
-        if (ixj > i) {
-          const uint32_t a = sk[i], b = sk[ixj];
-          if ((a > b) == ((i & kk) == 0)) {
-            sk[i] = b;
-            sk[ixj] = a;
-          }
-        }
+      // pair q joins elements i (bit j clear) and i + j; the lower index of an ascending pair
+      // (i & kk == 0) keeps the minimum
+      for (int q = t; q < (P2 >> 1); q += GK_TPB) {
+        const int i = ((q & ~(j - 1)) << 1) | (q & (j - 1));
+        const uint32_t a = sk[i], b = sk[i + j];
+        const bool asc = (i & kk) == 0;
+        sk[i] = asc ? min(a, b) : max(a, b);
+        sk[i + j] = asc ? max(a, b) : min(a, b);
       }
       __syncthreads();
     }
-    // the stages j < 32 of this kk in registers
+    // the stages j < 32 of this kk in registers.  For element e = t + 256 m the pair direction
+    // (e & kk) == 0 is fixed per m over the phase, and for jj < 32 the lower-index test
+    // (e & jj) == 0 is (t & jj) == 0 for every m
     if (warp_live) {
       uint32_t v[GK_EPT];
+      bool asc[GK_EPT];
 #pragma unroll
       for (int m = 0; m < GK_EPT; ++m) {
         const int e = t + GK_TPB * m;
         v[m] = e < P2 ? sk[e] : 0xFFFFFFFFu;
+        asc[m] = (e & kk) == 0;
       }
       for (int jj = j; jj > 0; jj >>= 1) {
+        const bool lower = (t & jj) == 0;
 #pragma unroll
         for (int m = 0; m < GK_EPT; ++m) {
           if (GK_TPB * m < P2) {  // uniform across the CTA
             const uint32_t o = __shfl_xor_sync(0xffffffffu, v[m], jj);
-            v[m] = gk_cx(v[m], o, t + GK_TPB * m, kk, jj);
+            v[m] = lower == asc[m] ? min(v[m], o) : max(v[m], o);
           }
         }
       }
