@@ -628,6 +628,55 @@ __device__ __forceinline__ float gk_unkey(uint32_t k) {
 
 constexpr int GK_EPT = GK_MAX_RAW / GK_TPB;  // sort elements per thread at the largest length
 
+// bitonic sort of the P2 keys in sk (P2 a power of two, at most EPT * 256) by the whole CTA;
+// thread t holds elements t + 256 m, m < EPT, in the register phases
+template <int EPT>
+__device__ __forceinline__ void gk_sort(uint32_t *sk, int P2, int t) {
+  const bool warp_live = (t & ~31) < P2;  // the warp holds elements (all lanes join the shuffles)
+  for (int kk = 2; kk <= P2; kk <<= 1) {
+    int j = kk >> 1;
+    for (; j >= 32; j >>= 1) {
+      // pair q joins elements i (bit j clear) and i + j; the lower index of an ascending pair
+      // (i & kk == 0) keeps the minimum
+      for (int q = t; q < (P2 >> 1); q += GK_TPB) {
+        const int i = ((q & ~(j - 1)) << 1) | (q & (j - 1));
+        const uint32_t a = sk[i], b = sk[i + j];
+        const bool asc = (i & kk) == 0;
+        sk[i] = asc ? min(a, b) : max(a, b);
+        sk[i + j] = asc ? max(a, b) : min(a, b);
+      }
+      __syncthreads();
+    }
+    // the stages j < 32 of this kk in registers.  For element e = t + 256 m the pair direction
+    // (e & kk) == 0 is fixed per m over the phase, and for jj < 32 the lower-index test
+    // (e & jj) == 0 is (t & jj) == 0 for every m
+    if (warp_live) {
+      uint32_t v[EPT];
+      bool asc[EPT];
+#pragma unroll
+      for (int m = 0; m < EPT; ++m) {
+        const int e = t + GK_TPB * m;
+        v[m] = e < P2 ? sk[e] : 0xFFFFFFFFu;
+        asc[m] = (e & kk) == 0;
+      }
+      for (int jj = j; jj > 0; jj >>= 1) {
+        const bool lower = (t & jj) == 0;
+#pragma unroll
+        for (int m = 0; m < EPT; ++m) {
+          const uint32_t o = __shfl_xor_sync(0xffffffffu, v[m], jj);
+          v[m] = lower == asc[m] ? min(v[m], o) : max(v[m], o);
+        }
+      }
+#pragma unroll
+      for (int m = 0; m < EPT; ++m) {
+        const int e = t + GK_TPB * m;
+        if (e < P2) sk[e] = v[m];
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // One g-and-k simulation by the whole CTA (every thread calls it): n_raw draws of parameters qv
 // with key (k0, k1), sort, thinned order statistics into summary_row (when given) and, when
 // want_dist, the distance to the data, returned in thread 0.
@@ -648,51 +697,14 @@ __device__ float gk_sim_cta(const GKP &p, const float (&qv)[4], uint32_t k0, uin
   }
   for (int i = n_raw + t; i < P2; i += GK_TPB) sk[i] = 0xFFFFFFFFu;
   __syncthreads();
-  const bool warp_live = (t & ~31) < P2;  // the warp holds elements (all lanes join the shuffles)
-  for (int kk = 2; kk <= P2; kk <<= 1) {
-    int j = kk >> 1;
-    for (; j >= 32; j >>= 1) {
-      // pair q joins elements i (bit j clear) and i + j; the lower index of an ascending pair
-      // (i & kk == 0) keeps the minimum
-      for (int q = t; q < (P2 >> 1); q += GK_TPB) {
-        const int i = ((q & ~(j - 1)) << 1) | (q & (j - 1));
-        const uint32_t a = sk[i], b = sk[i + j];
-        const bool asc = (i & kk) == 0;
-        sk[i] = asc ? min(a, b) : max(a, b);
-        sk[i + j] = asc ? max(a, b) : min(a, b);
-      }
-      __syncthreads();
-    }
-    // the stages j < 32 of this kk in registers.  For element e = t + 256 m the pair direction
-    // (e & kk) == 0 is fixed per m over the phase, and for jj < 32 the lower-index test
-    // (e & jj) == 0 is (t & jj) == 0 for every m
-    if (warp_live) {
-      uint32_t v[GK_EPT];
-      bool asc[GK_EPT];
-#pragma unroll
-      for (int m = 0; m < GK_EPT; ++m) {
-        const int e = t + GK_TPB * m;
-        v[m] = e < P2 ? sk[e] : 0xFFFFFFFFu;
-        asc[m] = (e & kk) == 0;
-      }
-      for (int jj = j; jj > 0; jj >>= 1) {
-        const bool lower = (t & jj) == 0;
-#pragma unroll
-        for (int m = 0; m < GK_EPT; ++m) {
-          if (GK_TPB * m < P2) {  // uniform across the CTA
-            const uint32_t o = __shfl_xor_sync(0xffffffffu, v[m], jj);
-            v[m] = lower == asc[m] ? min(v[m], o) : max(v[m], o);
-          }
-        }
-      }
-#pragma unroll
-      for (int m = 0; m < GK_EPT; ++m) {
-        const int e = t + GK_TPB * m;
-        if (e < P2) sk[e] = v[m];
-      }
-    }
-    __syncthreads();
-  }
+  if (P2 <= GK_TPB)
+    gk_sort<1>(sk, P2, t);
+  else if (P2 <= 2 * GK_TPB)
+    gk_sort<2>(sk, P2, t);
+  else if (P2 <= 4 * GK_TPB)
+    gk_sort<4>(sk, P2, t);
+  else
+    gk_sort<8>(sk, P2, t);
   // thinned order statistics j < n_sum (ranks floor(j n_raw / n_sum), below 2^22) and, for the
   // distance, their squared differences to the data, gathered in parallel
   float sv[GK_EPT], dv2[GK_EPT];
