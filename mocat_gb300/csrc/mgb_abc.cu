@@ -212,33 +212,65 @@ __device__ __forceinline__ int abc_block_count(int v, int *sm) {
 }
 
 // the rank-th smallest (0-based) of the non-negative floats v[0..n) (bit order
-// = value order; NaN sorts last, as jnp.sort places it): 4 passes of 8-bit digits
+// = value order; NaN sorts last, as jnp.sort places it): 4 passes of 8-bit digits.  Lanes of
+// a warp with the same digit add to the histogram once (__match_any_sync: the values of one
+// posterior mostly share their high byte), and warp 0 finds the digit of the rank, 8 bins
+// per lane
 __device__ __forceinline__ float abc_block_select(const float *v, int64_t n, int64_t rank, unsigned *hist,
                                                   unsigned *res) {
   unsigned prefix = 0u, mask = 0u;
-  int64_t r = rank;
+  unsigned r = (unsigned)rank;  // rank < n < 2^31
+  const int lane = threadIdx.x & 31;
 #pragma unroll 1
   for (int pass = 0; pass < 4; ++pass) {
     const int shift = 24 - 8 * pass;
     for (int k = threadIdx.x; k < 256; k += ABC_TPB) hist[k] = 0u;
     __syncthreads();
-    for (int64_t i = threadIdx.x; i < n; i += ABC_TPB) {
-      const unsigned u = __float_as_uint(v[i]);
-      if ((u & mask) == prefix) atomicAdd(&hist[(u >> shift) & 255u], 1u);
+    for (int64_t base = threadIdx.x - lane; base < n; base += ABC_TPB) {
+      const int64_t i = base + lane;
+      const unsigned u = i < n ? __float_as_uint(v[i]) : 0u;
+      const bool want = i < n && (u & mask) == prefix;
+      const unsigned wm = __ballot_sync(0xffffffffu, want);
+      if (want) {
+        const unsigned bin = (u >> shift) & 255u;
+        const unsigned peers = __match_any_sync(wm, bin);
+        if (lane == __ffs(peers) - 1) atomicAdd(&hist[bin], (unsigned)__popc(peers));
+      }
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-      int64_t cum = 0;
-      unsigned bin = 255u;
-      for (unsigned k = 0; k < 256u; ++k) {
-        if (r < cum + (int64_t)hist[k]) {
-          bin = k;
-          break;
-        }
-        cum += hist[k];
+    if (threadIdx.x < 32) {
+      unsigned c[8], tot = 0u;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        c[k] = hist[8 * lane + k];
+        tot += c[k];
       }
-      res[0] = bin;
-      res[1] = (unsigned)(r - cum);
+      unsigned incl = tot;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+      }
+      const unsigned excl = incl - tot;
+      const bool mine = excl <= r && r < incl;
+      if (mine) {
+        unsigned cum = excl, bin = 8u * lane + 7u;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          if (r < cum + c[k]) {
+            bin = 8u * lane + k;
+            break;
+          }
+          cum += c[k];
+        }
+        res[0] = bin;
+        res[1] = r - cum;
+      }
+      const unsigned all = __shfl_sync(0xffffffffu, incl, 31);
+      if (__ballot_sync(0xffffffffu, mine) == 0u && lane == 0) {
+        res[0] = 255u;  // no bin holds the rank (not reached: rank < n)
+        res[1] = r - all;
+      }
     }
     __syncthreads();
     prefix |= res[0] << shift;
@@ -249,6 +281,29 @@ __device__ __forceinline__ float abc_block_select(const float *v, int64_t n, int
   return __uint_as_float(prefix);
 }
 
+// the (rank + 1)-th smallest given vlo, the rank-th: vlo again when more than rank + 1 values
+// are <= vlo, else the smallest value above it (one pass instead of a second select)
+__device__ __forceinline__ float abc_block_next(const float *v, int64_t n, int64_t rank, float vlo, int *smi,
+                                                unsigned *res) {
+  const unsigned ub = __float_as_uint(vlo);
+  int cnt = 0;
+  unsigned mn = 0xFFFFFFFFu;
+  for (int64_t i = threadIdx.x; i < n; i += ABC_TPB) {
+    const unsigned u = __float_as_uint(v[i]);
+    if (u <= ub)
+      ++cnt;
+    else
+      mn = min(mn, u);
+  }
+  mn = __reduce_min_sync(0xffffffffu, mn);
+  if ((threadIdx.x & 31) == 0) res[2 + (threadIdx.x >> 5)] = mn;
+  cnt = abc_block_count(cnt, smi);  // its barriers order the per-warp minima
+  unsigned m = 0xFFFFFFFFu;
+  for (int k = 0; k < ABC_TPB / 32; ++k) m = min(m, res[2 + k]);
+  __syncthreads();
+  return (int64_t)cnt > rank + 1 ? vlo : __uint_as_float(m);
+}
+
 // --------------------------------------------------------------- adapt
 // MetropolisedABCSMCSampler.adapt (abc/smc.py:226-245) after startup (startup = 1)
 // or after an iteration's moves
@@ -256,7 +311,7 @@ template <int D>
 __global__ void __launch_bounds__(ABC_TPB) k_abc_adapt(ABCCtl ctl, ABCWs w, int startup) {
   __shared__ double smd[33];
   __shared__ int smi[33];
-  __shared__ unsigned hist[256], res[2];
+  __shared__ unsigned hist[256], res[2 + ABC_TPB / 32];
   const int64_t b = blockIdx.x, N = ctl.N;
   if (!startup && !w.active[b]) return;
   const int64_t off = b * N;
@@ -286,7 +341,7 @@ __global__ void __launch_bounds__(ABC_TPB) k_abc_adapt(ABCCtl ctl, ABCWs w, int 
     int64_t ilo = (int64_t)fminf(fmaxf(lo, 0.0f), (float)(N - 1));
     int64_t ihi = (int64_t)fminf(fmaxf(hi, 0.0f), (float)(N - 1));
     const float vlo = abc_block_select(w.dist + off, N, ilo, hist, res);
-    const float vhi = ihi == ilo ? vlo : abc_block_select(w.dist + off, N, ihi, hist, res);
+    const float vhi = ihi == ilo ? vlo : abc_block_next(w.dist + off, N, ilo, vlo, smi, res);
     thr = __fadd_rn(__fmul_rn(vlo, lwt), __fmul_rn(vhi, hw));
   }
   // log-weights and ESS
@@ -1262,7 +1317,8 @@ __global__ void __launch_bounds__(ABC_MOVE_TPB) k_vabc_gk_prior(int64_t n, const
 // the threshold (given, or the acceptance-rate quantile of the distances) and the weights; one block
 __global__ void __launch_bounds__(ABC_TPB) k_vabc_weights(int64_t n, float thr_in, float rate, const float *dist,
                                                           float *lw, float *thr_out) {
-  __shared__ unsigned hist[256], res[2];
+  __shared__ unsigned hist[256], res[2 + ABC_TPB / 32];
+  __shared__ int smi[33];
   float thr = thr_in;
   if (rate >= 0.0f) {
     const float pos = __fmul_rn(rate, (float)(n - 1));
@@ -1271,7 +1327,7 @@ __global__ void __launch_bounds__(ABC_TPB) k_vabc_weights(int64_t n, float thr_i
     const int64_t ilo = (int64_t)fminf(fmaxf(lo, 0.0f), (float)(n - 1));
     const int64_t ihi = (int64_t)fminf(fmaxf(hi, 0.0f), (float)(n - 1));
     const float vlo = abc_block_select(dist, n, ilo, hist, res);
-    const float vhi = ihi == ilo ? vlo : abc_block_select(dist, n, ihi, hist, res);
+    const float vhi = ihi == ilo ? vlo : abc_block_next(dist, n, ilo, vlo, smi, res);
     thr = __fadd_rn(__fmul_rn(vlo, lwt), __fmul_rn(vhi, hw));
   }
   for (int64_t i = threadIdx.x; i < n; i += ABC_TPB) lw[i] = dist[i] < thr ? 0.0f : -INFINITY;
