@@ -178,8 +178,8 @@ __global__ void __launch_bounds__(ABC_MOVE_TPB) k_abc_init(const __grid_constant
 }
 
 // ------------------------------------------------------- block primitives
-// fixed-order float64 block sum: per-thread partials, a shuffle-down tree per
-// warp, warp results added in warp order by thread 0 (the oracle mirrors it)
+// fixed-order float64 block sum of per-thread partials (each a float sum in index order): a
+// shuffle-down tree per warp, warp results added in warp order by thread 0 (the oracle mirrors it)
 __device__ __forceinline__ double abc_block_sum(double v, double *sm) {
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
@@ -316,15 +316,17 @@ __global__ void __launch_bounds__(ABC_TPB) k_abc_adapt(ABCCtl ctl, ABCWs w, int 
   if (!startup && !w.active[b]) return;
   const int64_t off = b * N;
   const int iter = startup ? 0 : w.iter[b] + 1;
-  // mean acceptance over the particles alive before the moves
-  double as = 0.0;
+  // mean acceptance over the particles alive before the moves.  Each thread sums its values
+  // in float in index order; the block adds the 1024 partials in float64 in a fixed tree (the
+  // FP64 pipe is slow on this GPU, so only the combination runs on it)
+  float asf_ = 0.0f;
   int ac = 0;
   for (int64_t i = threadIdx.x; i < N; i += ABC_TPB)
     if (w.lw[off + i] > -INFINITY) {
-      as += (double)w.alpha[off + i];
+      asf_ = __fadd_rn(asf_, w.alpha[off + i]);
       ++ac;
     }
-  as = abc_block_sum(as, smd);
+  const double as = abc_block_sum((double)asf_, smd);
   ac = abc_block_count(ac, smi);
   const float alpha_mean = (float)(as / (double)ac);
   // next threshold: the schedule (index clamped, as jax indexing is) or the quantile
@@ -357,15 +359,16 @@ __global__ void __launch_bounds__(ABC_TPB) k_abc_adapt(ABCCtl ctl, ABCWs w, int 
   if (ctl.adapt_stepsize) {
 #pragma unroll 1
     for (int j = 0; j < D; ++j) {
-      double s1 = 0.0;
-      for (int64_t i = threadIdx.x; i < N; i += ABC_TPB) s1 += (double)w.value[(off + i) * D + j];
-      const double mean = abc_block_sum(s1, smd) / (double)N;
-      double s2 = 0.0;
+      float s1 = 0.0f;
+      for (int64_t i = threadIdx.x; i < N; i += ABC_TPB) s1 = __fadd_rn(s1, w.value[(off + i) * D + j]);
+      const double mean = abc_block_sum((double)s1, smd) / (double)N;
+      const float mf = (float)mean;
+      float s2 = 0.0f;
       for (int64_t i = threadIdx.x; i < N; i += ABC_TPB) {
-        const double dv = (double)w.value[(off + i) * D + j] - mean;
-        s2 += dv * dv;
+        const float dv = __fsub_rn(w.value[(off + i) * D + j], mf);
+        s2 = __fadd_rn(s2, __fmul_rn(dv, dv));
       }
-      const double var = abc_block_sum(s2, smd) / (double)(N - 1);
+      const double var = abc_block_sum((double)s2, smd) / (double)(N - 1);
       if (threadIdx.x == 0) w.stepsize[b * D + j] = __fmul_rn(__fdiv_rn((float)var, (float)D), 5.6644f);
     }
   } else if (threadIdx.x < D) {

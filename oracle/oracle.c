@@ -1508,7 +1508,8 @@ static float o_abc_sim_dist(const o_abc_model *md, const float *x, uint32_t k0, 
     return sqrtf(s);
 }
 
-/* the GPU's fixed-order float64 block sum over 1024 thread partials: a
+/* the GPU's fixed-order float64 block sum over 1024 thread partials (each thread's float sum
+ * of its values in index order): a
  * shuffle-down tree (16, 8, 4, 2, 1) inside each warp, then the 32 warp results
  * in warp order */
 #define O_ABC_TPB 1024
@@ -1554,11 +1555,13 @@ static int o_abc_adapt(int d, const o_abc_config *cf, int iter, float ess_prev, 
     const int N = cf->N;
     double part[O_ABC_TPB];
     int cnt = 0;
+    /* each GPU thread sums its values in float in index order; the 1024 partials are added
+     * in float64 in the fixed tree */
     for (int t = 0; t < O_ABC_TPB; ++t) {
-        double s = 0.0;
+        float s = 0.0f;
         for (int i = t; i < N; i += O_ABC_TPB)
-            if (lw[i] > -INFINITY) { s += (double)alpha[i]; ++cnt; }
-        part[t] = s;
+            if (lw[i] > -INFINITY) { s = s + alpha[i]; ++cnt; }
+        part[t] = (double)s;
     }
     const float alpha_mean = (float)(o_abc_block_sum(part) / (double)cnt);
     float thr;
@@ -1585,18 +1588,19 @@ static int o_abc_adapt(int d, const o_abc_config *cf, int iter, float ess_prev, 
     for (int j = 0; j < d; ++j) {
         if (!cf->adapt_stepsize) { stepsize[j] = cf->stepsize; continue; }
         for (int t = 0; t < O_ABC_TPB; ++t) {
-            double s = 0.0;
-            for (int i = t; i < N; i += O_ABC_TPB) s += (double)x[(size_t)i * d + j];
-            part[t] = s;
+            float s = 0.0f;
+            for (int i = t; i < N; i += O_ABC_TPB) s = s + x[(size_t)i * d + j];
+            part[t] = (double)s;
         }
         const double mean = o_abc_block_sum(part) / (double)N;
+        const float mf = (float)mean;
         for (int t = 0; t < O_ABC_TPB; ++t) {
-            double s = 0.0;
+            float s = 0.0f;
             for (int i = t; i < N; i += O_ABC_TPB) {
-                const double dv = (double)x[(size_t)i * d + j] - mean;
-                s += dv * dv;
+                const float dv = x[(size_t)i * d + j] - mf;
+                s = s + dv * dv;
             }
-            part[t] = s;
+            part[t] = (double)s;
         }
         const double var = o_abc_block_sum(part) / (double)(N - 1);
         stepsize[j] = ((float)var / (float)d) * 5.6644f;

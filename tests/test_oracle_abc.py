@@ -52,11 +52,12 @@ def _block_sum(part):
 
 
 def _strided_sum(vals, mask=None):
-    part = [0.0] * 1024
+    """thread t's float32 sum of its values t, t + 1024, ... in index order, then the float64 tree"""
+    part = [np.float32(0.0)] * 1024
     for i, v in enumerate(vals):
         if mask is None or mask[i]:
-            part[i % 1024] += float(v)
-    return _block_sum(part)
+            part[i % 1024] = np.float32(part[i % 1024] + np.float32(v))
+    return _block_sum([float(q) for q in part])
 
 
 def _round_f32(q):
@@ -124,7 +125,8 @@ def _adapt(p, N, iter_, ess_prev, x, dist, lw, alpha, retain, schedule, term_alp
     step = np.empty(d, np.float32)
     for j in range(d):
         mean = _strided_sum(x[:, j]) / N
-        var = _strided_sum([(float(v) - mean) ** 2 for v in x[:, j]]) / (N - 1)
+        mf = np.float32(mean)
+        var = _strided_sum([np.float32(np.float32(v - mf) * np.float32(v - mf)) for v in x[:, j]]) / (N - 1)
         step[j] = F(F(F(var) / F(d)) * F(5.6644))
     active = not (alive == 0 or am <= F(term_alpha) or iter_ >= max_iter)
     return thr, F(ess), am, lw, step, active
