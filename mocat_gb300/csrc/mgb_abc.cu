@@ -178,9 +178,11 @@ __global__ void __launch_bounds__(ABC_MOVE_TPB) k_abc_init(const __grid_constant
 }
 
 // ------------------------------------------------------- block primitives
-// fixed-order float64 block sum of per-thread partials (each a float sum in index order): a
-// shuffle-down tree per warp, warp results added in warp order by thread 0 (the oracle mirrors it)
-__device__ __forceinline__ double abc_block_sum(double v, double *sm) {
+// (float)(sum / denom) of the block's per-thread partials (each a float sum in index order),
+// summed in float64 in a fixed order: a shuffle-down tree per warp, warp results added in warp
+// order by thread 0 (the oracle mirrors it).  Thread 0 divides once and every thread reads the
+// float (the FP64 pipe is slow: a division in every thread costs more than the whole sum)
+__device__ __forceinline__ float abc_block_ratio(double v, double denom, double *sm) {
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
   if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
@@ -188,10 +190,10 @@ __device__ __forceinline__ double abc_block_sum(double v, double *sm) {
   if (threadIdx.x == 0) {
     double s = sm[0];
     for (int k = 1; k < ABC_TPB / 32; ++k) s += sm[k];
-    sm[32] = s;
+    sm[32] = (double)(float)(s / denom);
   }
   __syncthreads();
-  const double r = sm[32];
+  const float r = (float)sm[32];
   __syncthreads();
   return r;
 }
@@ -326,9 +328,8 @@ __global__ void __launch_bounds__(ABC_TPB) k_abc_adapt(ABCCtl ctl, ABCWs w, int 
       asf_ = __fadd_rn(asf_, w.alpha[off + i]);
       ++ac;
     }
-  const double as = abc_block_sum((double)asf_, smd);
   ac = abc_block_count(ac, smi);
-  const float alpha_mean = (float)(as / (double)ac);
+  const float alpha_mean = abc_block_ratio((double)asf_, (double)ac, smd);
   // next threshold: the schedule (index clamped, as jax indexing is) or the quantile
   // of the distances at retain * ess / N (jnp.quantile, linear interpolation)
   float thr;
@@ -357,19 +358,28 @@ __global__ void __launch_bounds__(ABC_TPB) k_abc_adapt(ABCCtl ctl, ABCWs w, int 
   const float ess = alive > 0 ? expf_(logf_((float)alive)) : __int_as_float(0x7fc00000);
   // stepsize: per-dimension variance (ddof 1) of all particles / d * 2.38^2
   if (ctl.adapt_stepsize) {
+    // one pass per moment over the particles' rows, a float accumulator per dimension (the
+    // same per-dimension sums, in the same order, as a pass per dimension)
+    float s1[D], mf[D], s2[D];
+#pragma unroll
+    for (int j = 0; j < D; ++j) s1[j] = s2[j] = 0.0f;
+    for (int64_t i = threadIdx.x; i < N; i += ABC_TPB) {
+#pragma unroll
+      for (int j = 0; j < D; ++j) s1[j] = __fadd_rn(s1[j], w.value[(off + i) * D + j]);
+    }
+#pragma unroll 1
+    for (int j = 0; j < D; ++j) mf[j] = abc_block_ratio((double)s1[j], (double)N, smd);
+    for (int64_t i = threadIdx.x; i < N; i += ABC_TPB) {
+#pragma unroll
+      for (int j = 0; j < D; ++j) {
+        const float dv = __fsub_rn(w.value[(off + i) * D + j], mf[j]);
+        s2[j] = __fadd_rn(s2[j], __fmul_rn(dv, dv));
+      }
+    }
 #pragma unroll 1
     for (int j = 0; j < D; ++j) {
-      float s1 = 0.0f;
-      for (int64_t i = threadIdx.x; i < N; i += ABC_TPB) s1 = __fadd_rn(s1, w.value[(off + i) * D + j]);
-      const double mean = abc_block_sum((double)s1, smd) / (double)N;
-      const float mf = (float)mean;
-      float s2 = 0.0f;
-      for (int64_t i = threadIdx.x; i < N; i += ABC_TPB) {
-        const float dv = __fsub_rn(w.value[(off + i) * D + j], mf);
-        s2 = __fadd_rn(s2, __fmul_rn(dv, dv));
-      }
-      const double var = abc_block_sum((double)s2, smd) / (double)(N - 1);
-      if (threadIdx.x == 0) w.stepsize[b * D + j] = __fmul_rn(__fdiv_rn((float)var, (float)D), 5.6644f);
+      const float var = abc_block_ratio((double)s2[j], (double)(N - 1), smd);
+      if (threadIdx.x == 0) w.stepsize[b * D + j] = __fmul_rn(__fdiv_rn(var, (float)D), 5.6644f);
     }
   } else if (threadIdx.x < D) {
     w.stepsize[b * D + threadIdx.x] = ctl.fixed_stepsize;
