@@ -5,7 +5,7 @@
 //
 // For 128 parameter rows beta (one CTA) and the data streamed in 128-row tiles:
 //   MMA1  Z = beta X_t^T          M = 128 rows, N = 128 data rows, K = 64 features
-//   epi   pot += sum softplus(z) - y z;   R = sigmoid(Z) - y  (bf16, into smem)
+//   epi   pot += sum softplus(z) - y z;   R = sigmoid(Z) - y  (bf16, into tensor memory)
 //   MMA2  G += R X_t              M = 128 rows, N = 64 features, K = 128 data rows
 // Reference computation: the vmapped likelihood_potential_and_grad that
 // mocat's MALA moves call (mocat/src/mcmc/standard_mcmc.py:121-131,
@@ -22,7 +22,8 @@
 // Operand layouts (K-major / MN-major, SWIZZLE_128B, 1024-byte aligned tiles):
 //   beta tile  128 x 64 bf16 K-major    (written by the CTA from fp32 rows)
 //   X tile     128 x 64 bf16 row-major: K-major B of MMA1, MN-major B of MMA2
-//   R tile     128 x 128 bf16 K-major   (two 64-column sub-tiles)
+//   R tile     128 x 128 bf16 in tensor memory (lane = parameter row, two data rows per
+//              32-bit column), the A operand of MMA2 read from tensor memory
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
@@ -38,9 +39,11 @@ constexpr int TC_STAGES = 4;
 constexpr int TC_EPI_WARPS = 16;  // 4 column groups x 4 tensor-memory lane quarters
 constexpr int TC_THREADS = 64 + 32 * TC_EPI_WARPS;
 constexpr uint32_t TC_TMEM_COLS = 512;
+// tensor-memory columns: Z buffers 0 and 128, G 256 .. 319, R buffers (bf16 pairs) 320 and 384
+constexpr uint32_t TC_R_COL = 320;
 constexpr uint32_t TILE_BYTES = TC_DT * TC_K * 2;  // 16 KB
-// alignment slack + beta tile + X ring + R double buffer + one tile of guard space
-constexpr size_t TC_SMEM = 1024 + TILE_BYTES + TC_STAGES * TILE_BYTES + 2 * 2 * TILE_BYTES + TILE_BYTES;
+// alignment slack + beta tile + X ring + one tile of guard space (R lives in tensor memory)
+constexpr size_t TC_SMEM = 1024 + TILE_BYTES + TC_STAGES * TILE_BYTES + TILE_BYTES;
 constexpr uint32_t TC_WAIT_LIMIT = 1u << 24;
 
 // ---------------------------------------------------------------- PTX helpers
@@ -107,6 +110,16 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b
       "l"(a), "l"(b), "r"(idesc), "r"(acc)
       : "memory");
 }
+// the same MMA with A read from tensor memory (row i of A in lane i, two 16-bit K elements per
+// 32-bit column): a_tmem is the address of the K-step's first column
+__device__ __forceinline__ void mma_bf16_ta(uint32_t d_tmem, uint32_t a_tmem, uint64_t b, uint32_t idesc,
+                                            uint32_t acc) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}\n" ::"r"(
+          d_tmem),
+      "r"(a_tmem), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
 __device__ __forceinline__ void mma_commit(uint64_t *bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
                : "memory");
@@ -121,6 +134,14 @@ __device__ __forceinline__ void mma_commit(uint64_t *bar) {
         "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])   \
       : "r"(taddr))
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+// 16 consecutive 32-bit columns of this thread's lane
+#define MGB_TMEM_ST16(taddr, v)                                                                                  \
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, " \
+               "%13, %14, %15, %16};" ::"r"(taddr),                                                             \
+               "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]), \
+               "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15])                \
+               : "memory")
+__device__ __forceinline__ void tmem_st_wait() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 // byte offset of element (row, col) of a 64-column bf16 K-major SWIZZLE_128B tile
 __device__ __forceinline__ uint32_t sw128_off(int row, int col) {
@@ -201,7 +222,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_logreg_tc(const __grid_consta
   unsigned char *base = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   unsigned char *sA = base;                        // beta tile
   unsigned char *sX = sA + TILE_BYTES;             // X ring
-  unsigned char *sR = sX + TC_STAGES * TILE_BYTES;  // R double buffer, 2 sub-tiles each
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < TC_STAGES; ++s) {
@@ -286,12 +306,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_logreg_tc(const __grid_consta
           ok = mbar_wait(&bar_rfull[rb], (u >> 1) & 1, &abort_flag);
           if (!ok) break;
           tc_fence_after();
-          const uint32_t aR = smem_u32(sR + rb * 2 * TILE_BYTES);
+          const uint32_t tR = tmem + TC_R_COL + (uint32_t)rb * (TC_DT / 2);
           const uint32_t aX = smem_u32(sX + s * TILE_BYTES);
 #pragma unroll
           for (int k = 0; k < TC_DT / 16; ++k)
-            mma_bf16(tg, sw128_desc(aR + (k >> 2) * TILE_BYTES + (k & 3) * 32), sw128_desc(aX + k * 2048), id2,
-                     (u > 0 || k > 0) ? 1u : 0u);
+            mma_bf16_ta(tg, tR + (uint32_t)k * 8u, sw128_desc(aX + k * 2048), id2, (u > 0 || k > 0) ? 1u : 0u);
           mma_commit(&bar_xempty[s]);
           mma_commit(&bar_rempty[rb]);
         }
@@ -356,14 +375,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_logreg_tc(const __grid_consta
       }
       const float s_l2 = log2f_approx(prod0 * prod1);
       const float tsum = fmaf(0.69314718055994531f, s_l2, 0.5f * s_abs);
-      unsigned char *sub = sR + rb * 2 * TILE_BYTES + (cg >> 1) * TILE_BYTES;
-#pragma unroll
-      for (int m = 0; m < 4; ++m) {
-        const int col = (cg & 1) * 32 + m * 8;
-        *(uint4 *)(sub + sw128_off(row, col)) =
-            make_uint4(packed[4 * m], packed[4 * m + 1], packed[4 * m + 2], packed[4 * m + 3]);
-      }
-      fence_async_smem();
+      // R of this lane's row, data columns cg*32 .. +32 as bf16 pairs: tensor-memory columns
+      // cg*16 .. +16 of R buffer rb (the A operand of MMA2)
+      MGB_TMEM_ST16(tmem + TC_R_COL + (uint32_t)rb * (TC_DT / 2) + lane_off + (uint32_t)(cg * 16), packed);
+      tmem_st_wait();
+      tc_fence_before();
       mbar_arrive(&bar_rfull[rb]);
       pot_f += tsum;
       if ((t & 15) == 15) {
